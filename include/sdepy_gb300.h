@@ -1,0 +1,214 @@
+/*
+ * sdepy_gb300 C-ABI: Monte Carlo path integration of the sdepy preset SDEs
+ * on one GB300 GPU (sm_103a).
+ *
+ * Plain C types only: the Python host binds it with ctypes, and any other
+ * host (C, C++, Fortran, another FFI) can bind it the same way.
+ *
+ * Every entry point returns an int status (SDE_OK == 0, negative on error);
+ * sde_last_error() returns the message of the last failure on the calling
+ * thread.
+ *
+ * Vocabulary follows sdepy:
+ *   paths   - independent realisations (last axis of every array);
+ *   wshape  - working shape of the integrated state of one path, flattened
+ *             here to groups * group_size state variables;
+ *   group   - the state variables that share one correlated Wiener
+ *             increment (sdepy correlates along the last wshape axis);
+ *   steps   - points of the integration grid (sdepy's steps_tt);
+ *   rows    - points of the output timeline (sdepy's tt / xx[i]).
+ *
+ * Array layouts (C order, paths innermost):
+ *   xx  [n_rows][n_out_vars][paths]   precision of the run (f64 or f32)
+ *   dw  [n_steps][groups*group_size][paths]  f64, injected increments
+ */
+#ifndef SDEPY_GB300_H
+#define SDEPY_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define SDE_API __attribute__((visibility("default")))
+#else
+#define SDE_API
+#endif
+
+#define SDE_ABI_VERSION 1
+
+#define SDE_MAX_GROUP   16   /* largest correlated group (state vars) */
+#define SDE_MAX_PARAMS  6    /* coefficient arrays per state variable */
+#define SDE_MAX_STRIKES 8    /* payoff strikes of one fused reduction  */
+#define SDE_MAX_JUMPS_PER_STEP 4096
+
+/* status codes */
+#define SDE_OK                 0
+#define SDE_ERR_INVALID       -1   /* bad argument (shape, pointer, value) */
+#define SDE_ERR_UNSUPPORTED   -2   /* valid request outside the GPU path  */
+#define SDE_ERR_CUDA          -3   /* CUDA runtime failure                */
+#define SDE_ERR_DEVICE        -4   /* kernel reported an error flag       */
+#define SDE_ERR_NO_DEVICE     -5   /* no CUDA device visible              */
+
+/* model: the coefficient form integrated by the Euler step */
+#define SDE_MODEL_LINEAR  0  /* dx = c_dt*dt + c_dw*dw [+ dj]: wiener, lognorm, jumpdiff */
+#define SDE_MODEL_OU      1  /* dx = k*(theta - x)*dt + sigma*dw: OU, Hull-White factors */
+#define SDE_MODEL_HESTON  2  /* (log x, y) with full truncation y+ = max(y, 0)           */
+
+/* params[p][w] meaning, per model (w = state variable index):
+ *   LINEAR : p0 = c_dt, p1 = c_dw, p2 = lam, p3 = a, p4 = b, p5 = pa
+ *   OU     : p0 = k, p1 = theta, p2 = sigma
+ *   HESTON : w in the first half of a group (log-price):  p0 = mu, p1 = sigma
+ *            w in the second half of a group (variance):  p0 = k, p1 = theta, p2 = xi
+ */
+
+/* jump-size law of the compound Poisson source (LINEAR model only) */
+#define SDE_JUMP_NONE        0
+#define SDE_JUMP_NORM        1   /* y = a + b*z                    */
+#define SDE_JUMP_DOUBLE_EXP  2   /* y = a*e w.p. pa, else -b*e     */
+#define SDE_JUMP_UNIFORM     3   /* y = a + (b - a)*u              */
+#define SDE_JUMP_EXP         4   /* y = a*e                        */
+
+/* arithmetic of the path states */
+#define SDE_FP64  0
+#define SDE_FP32  1
+
+/* how a group's state is stored into an output row */
+#define SDE_OUT_STATE      0  /* all group_size states, as integrated          */
+#define SDE_OUT_EXP        1  /* exp() of all states (sdepy log=True models)   */
+#define SDE_OUT_SUM        2  /* one value: sum of the states (Hull-White)     */
+#define SDE_OUT_HESTON_X   3  /* exp() of the first half (heston_process)      */
+#define SDE_OUT_HESTON_XY  4  /* exp() of first half, second half as is        */
+
+typedef struct SdeSpec {
+    int32_t abi_version;   /* SDE_ABI_VERSION */
+    int32_t model;         /* SDE_MODEL_* */
+    int32_t precision;     /* SDE_FP64 | SDE_FP32 */
+    int32_t jump_law;      /* SDE_JUMP_* */
+    int64_t paths;
+    int32_t groups;        /* independent groups per path */
+    int32_t group_size;    /* M: states per group, 1..SDE_MAX_GROUP */
+    int32_t out_mode;      /* SDE_OUT_* */
+    int32_t reserved0;
+    const double *x0;      /* [groups*M] initial state (already log()-ed for log models) */
+    const double *params;  /* [SDE_MAX_PARAMS][groups*M] */
+    const double *corr;    /* [M*M] correlation matrix shared by all groups, or NULL */
+    uint64_t seed;         /* Philox-4x32-10 key */
+    uint32_t stream;       /* Philox counter word 3 (call / instance id) */
+    uint32_t reserved1;
+} SdeSpec;
+
+typedef struct SdeGrid {
+    const double *tt;       /* [n_pts] integration points, in integration order      */
+    const int32_t *out_row; /* [n_pts] output row stored at each point, or -1         */
+    int32_t n_pts;          /* >= 1; n_steps = n_pts - 1                               */
+    uint32_t step_offset;   /* added to the step index in the Philox counter          */
+} SdeGrid;
+
+typedef struct SdeNoise {   /* host arrays of injected increments (f64) */
+    const double *dw;       /* [n_steps][groups*M][paths], required        */
+    const double *dj;       /* [n_steps][groups*M][paths] or NULL           */
+    const int64_t *dn;      /* [n_steps][groups*M][paths] or NULL (info)    */
+} SdeNoise;
+
+typedef struct SdeOut {
+    void *xx;               /* [n_rows][n_out_vars][paths] or NULL (write nothing)  */
+    int32_t n_rows;
+    int32_t on_device;      /* 1: every pointer below and xx is device memory      */
+    int32_t *neg_count;     /* HESTON: [groups*M/2][paths] steps with y < 0, or NULL */
+    int32_t *jump_count;    /* jumps:  [groups*M][paths] Poisson events, or NULL     */
+    int64_t *row_jumps;     /* jumps:  [n_rows] events per output interval, or NULL  */
+} SdeOut;
+
+typedef struct SdeStatsReq {
+    int32_t row;            /* output row whose values are summarised              */
+    int32_t bins;           /* histogram bins, 0 for none                          */
+    int32_t has_range;      /* 1: use [range_lo, range_hi], else data min..max     */
+    int32_t n_strikes;      /* payoff sums E[max(x - K, 0)], 0..SDE_MAX_STRIKES    */
+    double range_lo, range_hi;
+    double strikes[SDE_MAX_STRIKES];
+} SdeStatsReq;
+
+/* per output variable o (host arrays):
+ *   moments[o*8 + 0..7] = n, mean, M2, M3, M4 (central sums), min, max, 0
+ *   payoff [o*n_strikes + s] = mean of max(x - K_s, 0)
+ *   counts [o*bins + b], edges [o*(bins+1) + e] as numpy.histogram returns them
+ */
+typedef struct SdeStatsOut {
+    double *moments;
+    double *payoff;
+    int64_t *counts;
+    double *edges;
+} SdeStatsOut;
+
+/* ---- version / device / errors --------------------------------------- */
+
+SDE_API int32_t sde_abi_version(void);
+
+/* message of the last failed call on this thread (NUL-terminated, truncated) */
+SDE_API int32_t sde_last_error(char *buf, int32_t len);
+
+/* number of visible CUDA devices (0 if none); never fails */
+SDE_API int32_t sde_device_count(void);
+
+/* free the device scratch cached by the library on the current device */
+SDE_API int32_t sde_release(void);
+
+/* run later calls on the current device on this cudaStream_t (NULL: the
+ * library's own stream, which is ordered with the legacy default stream) */
+SDE_API int32_t sde_set_stream(void *stream);
+
+/* ---- host utilities (no GPU) ------------------------------------------ */
+
+/* Lower-triangular L with L*L^T = corr (M x M, row-major); tolerant of
+ * semi-definite input (zero pivots give zero columns).
+ * Replaces the factorisation done inside numpy multivariate_normal
+ * (sdepy/infrastructure.py:1532-1534). */
+SDE_API int32_t sde_cholesky(const double *corr, int32_t M, double *L);
+
+/* ---- path integration -------------------------------------------------- */
+
+/* Euler-Maruyama integration of all paths along grid; stores the states at
+ * the points flagged in grid->out_row into out->xx.
+ * noise == NULL draws Philox normals / uniforms on the device; otherwise the
+ * given increments are used (FP64 parity mode).
+ * Replaces paths_generator.__call__ / _generate_paths with
+ * integrator.euler_next (sdepy/integration.py:476-584, 392-474, 707-723),
+ * SDE.A / SDEs.A (integration.py:1216-1225, 1711-1730) for the presets of
+ * integration.py:2056-2747, and the sources wiener_source,
+ * poisson_source, cpoisson_source (sdepy/infrastructure.py:1503-1560,
+ * 1617-1633, 2017-2040). */
+SDE_API int32_t sde_run(const SdeSpec *spec, const SdeGrid *grid,
+                const SdeNoise *noise, SdeOut *out);
+
+/* sde_run plus a fused montecarlo summary of one output row: moments,
+ * payoff means and histogram, written to stats (host arrays).
+ * out->xx may be NULL: the states are then reduced in-kernel and no path
+ * array is written.
+ * Replaces montecarlo(x[row], bins=..., range=...)
+ * (sdepy/infrastructure.py:2826-2922, 2924-3021). */
+SDE_API int32_t sde_run_stats(const SdeSpec *spec, const SdeGrid *grid,
+                      const SdeNoise *noise, SdeOut *out,
+                      const SdeStatsReq *req, SdeStatsOut *stats);
+
+/* montecarlo summary of an existing sample [n_vars][paths] (f64 if
+ * is_fp32 == 0, else f32; host or device per on_device).
+ * Replaces montecarlo._update_moments / _update_histogram
+ * (sdepy/infrastructure.py:2924-3021) for one update call. */
+SDE_API int32_t sde_sample_stats(const void *sample, int32_t is_fp32, int32_t on_device,
+                         int64_t n_vars, int64_t paths,
+                         const SdeStatsReq *req, SdeStatsOut *stats);
+
+/* Histogram of sample [n_vars][paths] against given edges [n_vars][bins+1]
+ * with numpy.histogram's bin rule (used by montecarlo.update after the
+ * first sample fixed the bins). */
+SDE_API int32_t sde_sample_histogram(const void *sample, int32_t is_fp32, int32_t on_device,
+                             int64_t n_vars, int64_t paths, int32_t bins,
+                             const double *edges, int64_t *counts);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SDEPY_GB300_H */

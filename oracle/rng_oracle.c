@@ -1,0 +1,268 @@
+/*
+ * ORACLE -- test infrastructure only; the product never links this file.
+ *
+ * Plain-C restatement of the device-RNG integration of include/sdepy_gb300.h,
+ * in FP64, path by path:
+ *   - Philox-4x32-10 (Salmon et al., SC'11: multipliers 0xD2511F53,
+ *     0xCD9E8D57; Weyl increments 0x9E3779B9, 0xBB67AE85; 10 rounds);
+ *   - uniforms u = (x + 0.5) 2^-32, Box-Muller normals
+ *     r = sqrt(-2 log u(a)), v = (b >> 9) 2^-22 - 1, (r cos pi v, r sin pi v);
+ *   - Poisson counts by CDF inversion of one uniform word;
+ *   - jump sizes of the norm / double_exp / uniform / exp laws;
+ *   - the Euler step in sdepy's operation order
+ *     (sdepy/integration.py:707-718 with the preset coefficients of
+ *     sdepy/integration.py:2066-2747) and sdepy's output transforms.
+ * The counter layout is (path, step + offset, group << 8 | call, stream) for
+ * normals and Poisson uniforms and (path, step + offset,
+ * 0x80000000 | var << 12 | jump, stream) for jump sizes.
+ *
+ * Compiled with -ffp-contract=off so that every product and sum rounds as
+ * written.  Pinned by the published Philox-4x32-10 known-answer vectors and by
+ * scipy.stats.poisson.ppf (tests/test_oracle.py).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../include/sdepy_gb300.h"
+
+void oracle_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int i = 0; i < 10; ++i) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        c0 = hi1 ^ c1 ^ k0;
+        c1 = lo1;
+        c2 = hi0 ^ c3 ^ k1;
+        c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+static double u01(uint32_t x) { return ((double)x + 0.5) * 0x1p-32; }
+static double vpm1(uint32_t b) { return (double)(b >> 9) * 0x1p-22 - 1.0; }
+
+void oracle_normal2(uint32_t a, uint32_t b, double *z0, double *z1) {
+    const double r = sqrt(-2.0 * log(u01(a)));
+    const double v = vpm1(b);
+    const double th = M_PI * v;
+    *z0 = r * cos(th);
+    *z1 = r * sin(th);
+}
+
+/* smallest k with u(word) <= F(k), F the Poisson(lam) CDF, p0 = exp(-lam) */
+int oracle_poisson(uint32_t word, double p0, double lam) {
+    const double u = u01(word);
+    int k = 0;
+    double pk = p0, F = p0;
+    while (u > F) {
+        ++k;
+        pk = (pk * lam) / (double)k;
+        F = F + pk;
+        if (k >= SDE_MAX_JUMPS_PER_STEP) return -1;
+    }
+    return k;
+}
+
+/* Cholesky-Banachiewicz, zero column on a vanishing pivot */
+int oracle_cholesky(const double *C, int M, double *L) {
+    for (int i = 0; i < M * M; ++i) L[i] = 0.0;
+    for (int i = 0; i < M; ++i)
+        for (int j = 0; j <= i; ++j) {
+            double s = C[i * M + j];
+            for (int k = 0; k < j; ++k) s -= L[i * M + k] * L[j * M + k];
+            if (i == j) {
+                if (s < -1e-10 * fabs(C[i * M + i]) - 1e-300) return -1;
+                L[i * M + i] = s > 1e-14 * fabs(C[i * M + i]) ? sqrt(s) : 0.0;
+            } else {
+                L[i * M + j] = L[j * M + j] > 0.0 ? s / L[j * M + j] : 0.0;
+            }
+        }
+    return 0;
+}
+
+static double jump_size(int law, const uint32_t r[4], double a, double b, double pa) {
+    double z0, z1;
+    switch (law) {
+    case SDE_JUMP_NORM:
+        oracle_normal2(r[0], r[1], &z0, &z1);
+        return a + b * z0;
+    case SDE_JUMP_DOUBLE_EXP: {
+        const double e = -log(u01(r[0]));
+        const double us = u01(r[2]);
+        return (us <= pa) ? a * e : -(b * e);
+    }
+    case SDE_JUMP_UNIFORM:
+        return a + (b - a) * u01(r[2]);
+    case SDE_JUMP_EXP:
+        return a * (-log(u01(r[0])));
+    }
+    return 0.0;
+}
+
+/*
+ * Integrate every path of spec along grid (device-RNG mode) in FP64.
+ * xx: [n_rows][n_out_vars][paths] doubles (rows not on the grid untouched);
+ * neg / jcnt / rowj as in SdeOut (may be NULL).  Returns 0, or -1 on a bad
+ * argument / jump cap.
+ */
+int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
+               int32_t *neg, int32_t *jcnt, int64_t *rowj) {
+    const int M = s->group_size, G = s->groups, W = G * M;
+    const int64_t paths = s->paths;
+    const int n_steps = g->n_pts - 1;
+    const int jumps = s->jump_law != SDE_JUMP_NONE;
+    int opg;
+    switch (s->out_mode) {
+    case SDE_OUT_SUM: opg = 1; break;
+    case SDE_OUT_HESTON_X: opg = M / 2; break;
+    default: opg = M;
+    }
+    const int64_t n_out = (int64_t)G * opg;
+    double L[SDE_MAX_GROUP * SDE_MAX_GROUP];
+    if (s->corr && oracle_cholesky(s->corr, M, L)) return -1;
+    const uint32_t key[2] = {(uint32_t)s->seed, (uint32_t)(s->seed >> 32)};
+    double sgn = 1.0;
+    if (n_steps > 0 && g->tt[1] < g->tt[0]) sgn = -1.0;
+    double *dtv = malloc(sizeof(double) * (n_steps + 1));
+    double *sqv = malloc(sizeof(double) * (n_steps + 1));
+    for (int k = 0; k < n_steps; ++k) {
+        dtv[k] = g->tt[k + 1] - g->tt[k];
+        sqv[k] = sqrt(fabs(dtv[k]));
+    }
+    if (rowj) memset(rowj, 0, sizeof(int64_t) * n_rows);
+    const double *prm = s->params;
+    int rc = 0;
+    for (int64_t p = 0; p < paths && !rc; ++p) {
+        for (int gi = 0; gi < G && !rc; ++gi) {
+            double st[SDE_MAX_GROUP], z[SDE_MAX_GROUP + 1], dW[SDE_MAX_GROUP], dJ[SDE_MAX_GROUP];
+            int negc[SDE_MAX_GROUP] = {0}, jc[SDE_MAX_GROUP] = {0};
+            int64_t row_jc = 0;
+            for (int m = 0; m < M; ++m) st[m] = s->x0[gi * M + m];
+            for (int k = -1; k < n_steps; ++k) {
+                if (k >= 0) {
+                    const double dt = dtv[k], sq = sqv[k];
+                    const uint32_t c1 = (uint32_t)k + g->step_offset;
+                    const int P = (M + 1) / 2;
+                    const int U = 2 * P + (jumps ? M : 0);
+                    const int NC = (U + 3) / 4;
+                    uint32_t u[4 * ((2 * SDE_MAX_GROUP + 2 + 3) / 4) + 4];
+                    for (int c = 0; c < NC; ++c) {
+                        const uint32_t ctr[4] = {(uint32_t)p, c1, ((uint32_t)gi << 8) | (uint32_t)c, s->stream};
+                        oracle_philox(ctr, key, &u[4 * c]);
+                    }
+                    for (int q = 0; q < P; ++q) oracle_normal2(u[2 * q], u[2 * q + 1], &z[2 * q], &z[2 * q + 1]);
+                    for (int m = 0; m < M; ++m) {
+                        if (s->corr) {
+                            double acc = L[m * M + 0] * z[0];
+                            for (int j = 1; j <= m; ++j) acc = acc + L[m * M + j] * z[j];
+                            dW[m] = acc * sq;
+                        } else {
+                            dW[m] = z[m] * sq;
+                        }
+                        dJ[m] = 0.0;
+                    }
+                    if (jumps) {
+                        for (int m = 0; m < M; ++m) {
+                            const int w = gi * M + m;
+                            const double lam = fabs(dt) * prm[2 * W + w];
+                            const double p0 = exp(-lam);
+                            const uint32_t word = u[2 * P + m];
+                            if (u01(word) > p0) {
+                                const int cnt = oracle_poisson(word, p0, lam);
+                                if (cnt < 0) { rc = -1; break; }
+                                double S = 0.0;
+                                for (int j = 0; j < cnt; ++j) {
+                                    const uint32_t ctr[4] = {(uint32_t)p, c1,
+                                                             0x80000000u | ((uint32_t)w << 12) | (uint32_t)j, s->stream};
+                                    uint32_t r[4];
+                                    oracle_philox(ctr, key, r);
+                                    const double y = jump_size(s->jump_law, r, prm[3 * W + w], prm[4 * W + w], prm[5 * W + w]);
+                                    S = (j == 0) ? y : S + y;
+                                }
+                                dJ[m] = sgn * S;
+                                jc[m] += sgn < 0 ? -cnt : cnt;
+                                row_jc += cnt;
+                            }
+                        }
+                    }
+                    if (s->model == SDE_MODEL_LINEAR) {
+                        for (int m = 0; m < M; ++m) {
+                            const int w = gi * M + m;
+                            double inc = prm[0 * W + w] * dt + prm[1 * W + w] * dW[m];
+                            if (jumps) inc = inc + dJ[m];
+                            st[m] = st[m] + inc;
+                        }
+                    } else if (s->model == SDE_MODEL_OU) {
+                        for (int m = 0; m < M; ++m) {
+                            const int w = gi * M + m;
+                            const double drift = prm[0 * W + w] * (prm[1 * W + w] - st[m]);
+                            st[m] = st[m] + (drift * dt + prm[2 * W + w] * dW[m]);
+                        }
+                    } else {
+                        const int h = M / 2;
+                        double nx[SDE_MAX_GROUP];
+                        for (int i = 0; i < h; ++i) {
+                            const int wx = gi * M + i, wy = gi * M + h + i;
+                            const double y = st[h + i];
+                            if (y < 0.0) negc[i] += 1;
+                            const double yp = y > 0.0 ? y : 0.0;
+                            const double sqy = sqrt(yp);
+                            const double mu = prm[0 * W + wx], sg = prm[1 * W + wx];
+                            const double adt = mu - ((sg * sg) * yp) * 0.5;
+                            const double adw = sg * sqy;
+                            nx[i] = st[i] + (adt * dt + adw * dW[i]);
+                            const double kk = prm[0 * W + wy], th = prm[1 * W + wy], xi = prm[2 * W + wy];
+                            const double bdt = kk * (th - yp);
+                            const double bdw = xi * sqy;
+                            nx[h + i] = y + (bdt * dt + bdw * dW[h + i]);
+                        }
+                        for (int m = 0; m < M; ++m) st[m] = nx[m];
+                    }
+                }
+                const int row = g->out_row[k + 1];
+                if (row < 0) continue;
+                double ov[SDE_MAX_GROUP];
+                int no = M;
+                switch (s->out_mode) {
+                case SDE_OUT_EXP:
+                    for (int m = 0; m < M; ++m) ov[m] = exp(st[m]);
+                    break;
+                case SDE_OUT_SUM: {
+                    double a = st[0];
+                    for (int m = 1; m < M; ++m) a = a + st[m];
+                    ov[0] = a;
+                    no = 1;
+                    break;
+                }
+                case SDE_OUT_HESTON_X:
+                    for (int m = 0; m < M / 2; ++m) ov[m] = exp(st[m]);
+                    no = M / 2;
+                    break;
+                case SDE_OUT_HESTON_XY:
+                    for (int m = 0; m < M; ++m) ov[m] = m < M / 2 ? exp(st[m]) : st[m];
+                    break;
+                default:
+                    for (int m = 0; m < M; ++m) ov[m] = st[m];
+                }
+                for (int m = 0; m < no; ++m)
+                    xx[((int64_t)row * n_out + (int64_t)gi * opg + m) * paths + p] = ov[m];
+                if (rowj) rowj[row] += row_jc;
+                row_jc = 0;
+            }
+            if (neg && s->model == SDE_MODEL_HESTON)
+                for (int i = 0; i < M / 2; ++i) neg[((int64_t)gi * (M / 2) + i) * paths + p] = negc[i];
+            if (jcnt && jumps)
+                for (int m = 0; m < M; ++m) jcnt[((int64_t)gi * M + m) * paths + p] = jc[m];
+        }
+    }
+    free(dtv);
+    free(sqv);
+    return rc;
+}

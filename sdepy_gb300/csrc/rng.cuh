@@ -1,0 +1,115 @@
+// Counter-based random numbers drawn in registers.
+//
+// Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+// easy as 1, 2, 3", SC'11): 10 rounds of two 32x32->64 multiplies with the
+// published multipliers and Weyl key increments.  Every draw is a pure
+// function of (counter, key), so any thread can regenerate any increment of
+// any path -- the adjoint kernel recomputes forward states this way.
+//
+// Counter words used by the integrator:
+//   c0 = path index, c1 = step index + leg offset,
+//   c2 = (group << 8) | call      (normals, then Poisson uniforms)
+//      = 0x80000000 | (var << 12) | jump   (jump sizes)
+//   c3 = stream (call / instance id);  key = 64-bit seed.
+//
+// Uniforms: u = (x + 0.5) * 2^-32 in (0, 1) for a 32-bit word x.
+// Normals (Box-Muller) from a word pair (a, b):
+//   r = sqrt(-2 log u(a)),  v = (b >> 9) * 2^-22 - 1  in [-1, 1),
+//   z0 = r cos(pi v),  z1 = r sin(pi v).
+// FP64 evaluates this exactly as written; FP32 evaluates the same formula
+// with the SFU approximations, so both precisions consume identical draws.
+#pragma once
+#include <cstdint>
+
+namespace sdegpu {
+
+struct PhiloxKey {
+    uint32_t k0, k1;
+};
+
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, PhiloxKey key) {
+    uint32_t k0 = key.k0, k1 = key.k1;
+#pragma unroll
+    for (int i = 0; i < 10; ++i) {
+        const uint32_t lo0 = 0xD2511F53u * c.x;
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+__device__ __forceinline__ double u01_f64(uint32_t x) {
+    return ((double)x + 0.5) * 0x1p-32;
+}
+
+// v = (b >> 9) * 2^-22 - 1, exact in both precisions
+__device__ __forceinline__ float vpm1_f32(uint32_t b) {
+    return __uint_as_float(0x40000000u | (b >> 9)) - 3.0f;
+}
+__device__ __forceinline__ double vpm1_f64(uint32_t b) {
+    return (double)(b >> 9) * 0x1p-22 - 1.0;
+}
+
+__device__ __forceinline__ float approx_lg2(float x) {
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float approx_sqrt(float x) {
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float approx_sin(float x) {
+    float y;
+    asm("sin.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float approx_cos(float x) {
+    float y;
+    asm("cos.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+template <typename R> struct Rng;
+
+template <> struct Rng<double> {
+    static __device__ __forceinline__ void normal2(uint32_t a, uint32_t b,
+                                                   double &z0, double &z1) {
+        const double r = sqrt(-2.0 * log(u01_f64(a)));
+        double s, c;
+        sincospi(vpm1_f64(b), &s, &c);
+        z0 = r * c;
+        z1 = r * s;
+    }
+    // -log(u), the unit exponential
+    static __device__ __forceinline__ double expo(uint32_t a) {
+        return -log(u01_f64(a));
+    }
+    static __device__ __forceinline__ double unif(uint32_t a) { return u01_f64(a); }
+};
+
+template <> struct Rng<float> {
+    static __device__ __forceinline__ void normal2(uint32_t a, uint32_t b,
+                                                   float &z0, float &z1) {
+        const float u = fmaf((float)a, 0x1p-32f, 0x1p-33f);
+        // -2 ln u = -2 ln2 * log2 u
+        const float r = approx_sqrt(-1.38629436f * approx_lg2(u));
+        const float th = 3.14159265f * vpm1_f32(b);
+        z0 = r * approx_cos(th);
+        z1 = r * approx_sin(th);
+    }
+    static __device__ __forceinline__ float expo(uint32_t a) {
+        const float u = fmaf((float)a, 0x1p-32f, 0x1p-33f);
+        return -0.69314718f * approx_lg2(u);
+    }
+    static __device__ __forceinline__ float unif(uint32_t a) {
+        return fmaf((float)a, 0x1p-32f, 0x1p-33f);
+    }
+};
+
+}  // namespace sdegpu

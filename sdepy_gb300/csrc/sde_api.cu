@@ -1,0 +1,688 @@
+// C-ABI runtime of sdepy_gb300: argument validation, host-side tables,
+// device scratch cache, kernel dispatch and copies (include/sdepy_gb300.h).
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "sde_kernels.cuh"
+#include "sde_stats.cuh"
+
+using namespace sdegpu;
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+static thread_local std::string g_err;
+
+static int fail(int code, const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CU(call)                                                                         \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess)                                                           \
+            return fail(SDE_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));   \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// per-device state: one blocking stream (ordered with the legacy default
+// stream that torch uses by default) and a grow-only scratch cache
+// ---------------------------------------------------------------------------
+enum Slot {
+    S_TABLES, S_NOISE_DW, S_NOISE_DJ, S_NOISE_DN, S_XX, S_NEG, S_JCNT, S_ROWJ,
+    S_PART, S_RES, S_EDGES, S_EDGES64, S_COUNTS, S_VALS, S_ERR, S_SAMPLE, N_SLOTS
+};
+
+struct Device {
+    bool init = false;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t user_stream = nullptr;
+    bool has_user_stream = false;
+    void *ptr[N_SLOTS] = {};
+    size_t cap[N_SLOTS] = {};
+    std::vector<char> host_tables;
+};
+
+static std::mutex g_mu;
+static Device g_dev[64];
+
+static int current_device(Device **out) {
+    int d = 0;
+    cudaError_t e = cudaGetDevice(&d);
+    if (e != cudaSuccess) return fail(SDE_ERR_NO_DEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+    if (d < 0 || d >= 64) return fail(SDE_ERR_NO_DEVICE, "device id %d out of range", d);
+    Device &D = g_dev[d];
+    if (!D.init) {
+        int n = 0;
+        CU(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, d));
+        D.sms = n;
+        CU(cudaStreamCreate(&D.stream));
+        D.init = true;
+    }
+    *out = &D;
+    return SDE_OK;
+}
+
+static cudaStream_t dev_stream(Device *D) { return D->has_user_stream ? D->user_stream : D->stream; }
+
+static int scratch(Device *D, Slot s, size_t bytes, void **p) {
+    if (bytes == 0) bytes = 16;
+    if (D->cap[s] < bytes) {
+        if (D->ptr[s]) {
+            CU(cudaStreamSynchronize(dev_stream(D)));
+            CU(cudaFree(D->ptr[s]));
+            D->ptr[s] = nullptr;
+            D->cap[s] = 0;
+        }
+        size_t want = bytes + bytes / 8;
+        CU(cudaMalloc(&D->ptr[s], want));
+        D->cap[s] = want;
+    }
+    *p = D->ptr[s];
+    return SDE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// exported utilities
+// ---------------------------------------------------------------------------
+extern "C" int32_t sde_abi_version(void) { return SDE_ABI_VERSION; }
+
+extern "C" int32_t sde_last_error(char *buf, int32_t len) {
+    if (!buf || len <= 0) return SDE_ERR_INVALID;
+    snprintf(buf, (size_t)len, "%s", g_err.c_str());
+    return SDE_OK;
+}
+
+extern "C" int32_t sde_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+extern "C" int32_t sde_release(void) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    int d = 0;
+    if (cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= 64) return SDE_OK;
+    Device &D = g_dev[d];
+    if (!D.init) return SDE_OK;
+    cudaStreamSynchronize(dev_stream(&D));
+    for (int s = 0; s < N_SLOTS; ++s) {
+        if (D.ptr[s]) cudaFree(D.ptr[s]);
+        D.ptr[s] = nullptr;
+        D.cap[s] = 0;
+    }
+    return SDE_OK;
+}
+
+extern "C" int32_t sde_set_stream(void *stream) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    Device *D;
+    int rc = current_device(&D);
+    if (rc) return rc;
+    D->user_stream = (cudaStream_t)stream;
+    D->has_user_stream = stream != nullptr;
+    return SDE_OK;
+}
+
+// Cholesky-Banachiewicz, row by row: L[i][j] = (C[i][j] - sum_{k<j} L[i][k] L[j][k]) / L[j][j],
+// L[i][i] = sqrt(C[i][i] - sum_{k<i} L[i][k]^2).  A pivot <= 1e-14 * C[i][i]
+// (semi-definite input, e.g. |rho| = 1) gives a zero column.
+extern "C" int32_t sde_cholesky(const double *C, int32_t M, double *L) {
+    if (!C || !L || M < 1 || M > 1024) return fail(SDE_ERR_INVALID, "sde_cholesky: bad arguments");
+    for (int i = 0; i < M * M; ++i) L[i] = 0.0;
+    for (int i = 0; i < M; ++i) {
+        for (int j = 0; j <= i; ++j) {
+            double s = C[i * M + j];
+            for (int k = 0; k < j; ++k) s -= L[i * M + k] * L[j * M + k];
+            if (i == j) {
+                const double tol = 1e-14 * fabs(C[i * M + i]);
+                if (s < -1e-10 * fabs(C[i * M + i]) - 1e-300)
+                    return fail(SDE_ERR_INVALID, "correlation matrix is not positive semi-definite");
+                L[i * M + i] = s > tol ? sqrt(s) : 0.0;
+            } else {
+                L[i * M + j] = L[j * M + j] > 0.0 ? s / L[j * M + j] : 0.0;
+            }
+        }
+    }
+    return SDE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// validation
+// ---------------------------------------------------------------------------
+static int check_spec(const SdeSpec *s, int *opg) {
+    if (!s) return fail(SDE_ERR_INVALID, "spec is NULL");
+    if (s->abi_version != SDE_ABI_VERSION)
+        return fail(SDE_ERR_INVALID, "spec abi_version %d != %d", s->abi_version, SDE_ABI_VERSION);
+    if (s->model < SDE_MODEL_LINEAR || s->model > SDE_MODEL_HESTON)
+        return fail(SDE_ERR_UNSUPPORTED, "unknown model %d", s->model);
+    if (s->precision != SDE_FP64 && s->precision != SDE_FP32)
+        return fail(SDE_ERR_UNSUPPORTED, "unknown precision %d", s->precision);
+    if (s->paths < 1 || s->paths > 0x7fffffffLL)
+        return fail(SDE_ERR_INVALID, "paths must be in [1, 2^31-1], not %lld", (long long)s->paths);
+    if (s->groups < 1) return fail(SDE_ERR_INVALID, "groups must be >= 1");
+    if (s->groups > 65535) return fail(SDE_ERR_UNSUPPORTED, "more than 65535 groups per path");
+    if (s->group_size < 1 || s->group_size > SDE_MAX_GROUP)
+        return fail(SDE_ERR_UNSUPPORTED, "group size %d outside 1..%d", s->group_size, SDE_MAX_GROUP);
+    if ((int64_t)s->groups * s->group_size >= (1 << 19))
+        return fail(SDE_ERR_UNSUPPORTED, "too many state variables per path");
+    if (s->jump_law < SDE_JUMP_NONE || s->jump_law > SDE_JUMP_EXP)
+        return fail(SDE_ERR_UNSUPPORTED, "unknown jump law %d", s->jump_law);
+    if (s->jump_law != SDE_JUMP_NONE && s->model != SDE_MODEL_LINEAR)
+        return fail(SDE_ERR_UNSUPPORTED, "jumps are supported for the LINEAR model only");
+    if (s->model == SDE_MODEL_HESTON) {
+        const int M = s->group_size;
+        if (M != 2 && M != 4 && M != 8 && M != 16)
+            return fail(SDE_ERR_UNSUPPORTED, "Heston group size must be 2, 4, 8 or 16, not %d", M);
+    }
+    if (!s->x0 || !s->params) return fail(SDE_ERR_INVALID, "x0 and params are required");
+    const int M = s->group_size;
+    switch (s->out_mode) {
+    case SDE_OUT_STATE:
+    case SDE_OUT_EXP: *opg = M; break;
+    case SDE_OUT_SUM: *opg = 1; break;
+    case SDE_OUT_HESTON_X:
+        if (s->model != SDE_MODEL_HESTON) return fail(SDE_ERR_INVALID, "HESTON_X output needs the HESTON model");
+        *opg = M / 2;
+        break;
+    case SDE_OUT_HESTON_XY:
+        if (s->model != SDE_MODEL_HESTON) return fail(SDE_ERR_INVALID, "HESTON_XY output needs the HESTON model");
+        *opg = M;
+        break;
+    default: return fail(SDE_ERR_INVALID, "unknown out_mode %d", s->out_mode);
+    }
+    return SDE_OK;
+}
+
+static int check_grid(const SdeGrid *g, int n_rows) {
+    if (!g || !g->tt || !g->out_row) return fail(SDE_ERR_INVALID, "grid arrays are required");
+    if (g->n_pts < 1) return fail(SDE_ERR_INVALID, "grid needs at least one point");
+    for (int k = 0; k < g->n_pts; ++k) {
+        if (!std::isfinite(g->tt[k])) return fail(SDE_ERR_INVALID, "grid point %d is not finite", k);
+        if (g->out_row[k] < -1 || g->out_row[k] >= n_rows)
+            return fail(SDE_ERR_INVALID, "grid out_row[%d] = %d outside [-1, %d)", k, g->out_row[k], n_rows);
+    }
+    return SDE_OK;
+}
+
+static int maxm_of(int M) {
+    if (M <= 1) return 1;
+    if (M <= 2) return 2;
+    if (M <= 4) return 4;
+    if (M <= 8) return 8;
+    return 16;
+}
+
+template <typename R> struct Finder;
+template <> struct Finder<double> {
+    static FwdLauncher<double> find(int model, int maxm, bool inj, bool jmp, int *bps) {
+        FwdLauncher<double> f = find_fwd_f64_linear(model, maxm, inj, jmp, bps);
+        return f ? f : find_fwd_f64_ou_heston(model, maxm, inj, jmp, bps);
+    }
+};
+template <> struct Finder<float> {
+    static FwdLauncher<float> find(int model, int maxm, bool inj, bool jmp, int *bps) {
+        FwdLauncher<float> f = find_fwd_f32_linear(model, maxm, inj, jmp, bps);
+        return f ? f : find_fwd_f32_ou_heston(model, maxm, inj, jmp, bps);
+    }
+};
+
+// number of blocks along paths: enough for every SM, capped by the paths
+static int path_blocks(Device *D, int64_t paths, int groups, int bps) {
+    if (bps < 1) bps = 1;
+    int64_t want = (paths + BLOCK - 1) / BLOCK;
+    int64_t resident = (int64_t)D->sms * bps;
+    int64_t per_group = (resident + groups - 1) / groups;
+    if (per_group < 1) per_group = 1;
+    int64_t nb = want < per_group ? want : per_group;
+    if (nb < 1) nb = 1;
+    return (int)nb;
+}
+
+// ---------------------------------------------------------------------------
+// the run
+// ---------------------------------------------------------------------------
+template <typename R>
+static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, SdeOut *out,
+                    const SdeStatsReq *req, SdeStatsOut *so) {
+    int opg = 0, rc;
+    if ((rc = check_spec(s, &opg))) return rc;
+    if (!out) return fail(SDE_ERR_INVALID, "out is NULL");
+    if (out->n_rows < 1) return fail(SDE_ERR_INVALID, "out->n_rows must be >= 1");
+    if ((rc = check_grid(gr, out->n_rows))) return rc;
+    const bool jumps = s->jump_law != SDE_JUMP_NONE;
+    const bool inject = noise != nullptr;
+    if (inject) {
+        if (!noise->dw) return fail(SDE_ERR_INVALID, "injected noise needs dw");
+        if (jumps && !noise->dj) return fail(SDE_ERR_INVALID, "injected noise of a jump model needs dj");
+    }
+    const bool stats = req != nullptr;
+    if (stats) {
+        if (!so || !so->moments) return fail(SDE_ERR_INVALID, "stats output arrays are required");
+        if (req->row < 0 || req->row >= out->n_rows) return fail(SDE_ERR_INVALID, "stats row %d out of range", req->row);
+        if (req->bins < 0) return fail(SDE_ERR_INVALID, "bins must be >= 0");
+        if (req->bins > 0 && (!so->counts || !so->edges)) return fail(SDE_ERR_INVALID, "histogram arrays are required");
+        if (req->n_strikes < 0 || req->n_strikes > SDE_MAX_STRIKES)
+            return fail(SDE_ERR_INVALID, "n_strikes must be in 0..%d", SDE_MAX_STRIKES);
+        if (req->n_strikes > 0 && !so->payoff) return fail(SDE_ERR_INVALID, "payoff array is required");
+        if (req->has_range && !(std::isfinite(req->range_lo) && std::isfinite(req->range_hi) && req->range_lo <= req->range_hi))
+            return fail(SDE_ERR_INVALID, "histogram range must be finite with min <= max");
+    }
+    const int M = s->group_size, W = s->groups * M;
+    const int64_t paths = s->paths;
+    const int n_steps = gr->n_pts - 1;
+    const int64_t n_out = (int64_t)s->groups * opg;
+
+    std::lock_guard<std::mutex> lk(g_mu);
+    Device *D;
+    if ((rc = current_device(&D))) return rc;
+    cudaStream_t st = dev_stream(D);
+
+    // ---- host tables, packed in one staging buffer ---------------------------
+    // layout: dt[R n_steps] sqdt[R n_steps] out_row[int n_pts] x0[R W] prm[R 6W]
+    //         lamdt[f64 n_steps*W] p0[f64 n_steps*W] thr[i64 n_steps*W]
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t o_dt = 0;
+    const size_t o_sq = o_dt + al(sizeof(R) * (n_steps + 1));
+    const size_t o_row = o_sq + al(sizeof(R) * (n_steps + 1));
+    const size_t o_x0 = o_row + al(sizeof(int32_t) * gr->n_pts);
+    const size_t o_prm = o_x0 + al(sizeof(R) * W);
+    const size_t o_lam = o_prm + al(sizeof(R) * SDE_MAX_PARAMS * W);
+    const size_t njt = jumps ? (size_t)n_steps * W + 1 : 1;
+    const size_t o_p0 = o_lam + al(sizeof(double) * njt);
+    const size_t o_thr = o_p0 + al(sizeof(double) * njt);
+    const size_t o_end = o_thr + al(sizeof(long long) * njt);
+    D->host_tables.resize(o_end);
+    char *H = D->host_tables.data();
+    R *h_dt = (R *)(H + o_dt), *h_sq = (R *)(H + o_sq), *h_x0 = (R *)(H + o_x0), *h_prm = (R *)(H + o_prm);
+    int32_t *h_row = (int32_t *)(H + o_row);
+    double *h_lam = (double *)(H + o_lam), *h_p0 = (double *)(H + o_p0);
+    long long *h_thr = (long long *)(H + o_thr);
+    double sgn = 1.0;
+    for (int k = 0; k < n_steps; ++k) {
+        const double dt = gr->tt[k + 1] - gr->tt[k];
+        if (k == 0) sgn = dt < 0 ? -1.0 : 1.0;
+        if ((dt < 0 ? -1.0 : 1.0) != sgn || dt == 0.0)
+            return fail(SDE_ERR_INVALID, "grid points must be strictly monotonic (step %d)", k);
+        h_dt[k] = (R)dt;
+        h_sq[k] = (R)sqrt(fabs(dt));
+    }
+    memcpy(h_row, gr->out_row, sizeof(int32_t) * gr->n_pts);
+    for (int w = 0; w < W; ++w) h_x0[w] = (R)s->x0[w];
+    for (int i = 0; i < SDE_MAX_PARAMS * W; ++i) h_prm[i] = (R)s->params[i];
+    if (jumps && !inject) {
+        for (int k = 0; k < n_steps; ++k) {
+            const double adt = fabs(gr->tt[k + 1] - gr->tt[k]);
+            for (int w = 0; w < W; ++w) {
+                const double lam = s->params[2 * W + w];
+                if (!(lam >= 0.0) || !std::isfinite(lam))
+                    return fail(SDE_ERR_INVALID, "Poisson intensity must be finite and >= 0");
+                const double L = adt * lam;
+                if (L > 700.0) return fail(SDE_ERR_UNSUPPORTED, "lam*dt = %g too large for inversion sampling", L);
+                const double p0 = exp(-L);
+                const size_t i = (size_t)k * W + w;
+                h_lam[i] = L;
+                h_p0[i] = p0;
+                h_thr[i] = (long long)floor(p0 * 4294967296.0 - 0.5);
+            }
+        }
+        if (s->jump_law == SDE_JUMP_DOUBLE_EXP)
+            for (int w = 0; w < W; ++w) {
+                const double a = s->params[3 * W + w], b = s->params[4 * W + w], pa = s->params[5 * W + w];
+                if (!(a > 0) || !(b > 0) || !(pa >= 0 && pa <= 1))
+                    return fail(SDE_ERR_INVALID, "domain error in arguments");
+            }
+    }
+
+    FwdArgs<R> a;
+    memset(&a, 0, sizeof a);
+    if (s->corr) {
+        std::vector<double> L(M * M);
+        if ((rc = sde_cholesky(s->corr, M, L.data()))) return rc;
+        for (int i = 0; i < M; ++i)
+            for (int j = 0; j <= i; ++j) a.chol[i * (i + 1) / 2 + j] = (R)L[i * M + j];
+        a.has_corr = 1;
+    }
+
+    void *d_tab;
+    if ((rc = scratch(D, S_TABLES, o_end, &d_tab))) return rc;
+    CU(cudaMemcpyAsync(d_tab, H, o_end, cudaMemcpyHostToDevice, st));
+    char *T = (char *)d_tab;
+
+    a.paths = paths;
+    a.groups = s->groups;
+    a.M = M;
+    a.W = W;
+    a.n_pts = gr->n_pts;
+    a.step_offset = gr->step_offset;
+    a.jump_law = s->jump_law;
+    a.out_mode = s->out_mode;
+    a.opg = opg;
+    a.seed = s->seed;
+    a.stream = s->stream;
+    a.sgn = (R)sgn;
+    a.dt = (const R *)(T + o_dt);
+    a.sqdt = (const R *)(T + o_sq);
+    a.out_row = (const int32_t *)(T + o_row);
+    a.lamdt = (const double *)(T + o_lam);
+    a.p0 = (const double *)(T + o_p0);
+    a.thr = (const long long *)(T + o_thr);
+    a.x0 = (const R *)(T + o_x0);
+    a.prm = (const R *)(T + o_prm);
+    a.n_out_vars = n_out;
+
+    // ---- injected noise ---------------------------------------------------------
+    const size_t nz = (size_t)n_steps * W * paths;
+    if (inject && n_steps > 0) {
+        void *p;
+        if ((rc = scratch(D, S_NOISE_DW, nz * sizeof(double), &p))) return rc;
+        CU(cudaMemcpyAsync(p, noise->dw, nz * sizeof(double), cudaMemcpyHostToDevice, st));
+        a.dw = (const double *)p;
+        if (jumps) {
+            if ((rc = scratch(D, S_NOISE_DJ, nz * sizeof(double), &p))) return rc;
+            CU(cudaMemcpyAsync(p, noise->dj, nz * sizeof(double), cudaMemcpyHostToDevice, st));
+            a.dj = (const double *)p;
+            if (noise->dn) {
+                if ((rc = scratch(D, S_NOISE_DN, nz * sizeof(int64_t), &p))) return rc;
+                CU(cudaMemcpyAsync(p, noise->dn, nz * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+                a.dn = (const long long *)p;
+            }
+        }
+    }
+
+    // ---- outputs -------------------------------------------------------------------
+    const bool dev = out->on_device != 0;
+    const size_t xx_bytes = (size_t)out->n_rows * n_out * paths * sizeof(R);
+    int rmin = out->n_rows, rmax = -1;
+    for (int k = 0; k < gr->n_pts; ++k)
+        if (gr->out_row[k] >= 0) {
+            rmin = gr->out_row[k] < rmin ? gr->out_row[k] : rmin;
+            rmax = gr->out_row[k] > rmax ? gr->out_row[k] : rmax;
+        }
+    if (out->xx) {
+        if (dev) {
+            a.xx = (R *)out->xx;
+        } else {
+            void *p;
+            if ((rc = scratch(D, S_XX, xx_bytes, &p))) return rc;
+            a.xx = (R *)p;
+        }
+    }
+    const int h = M / 2;
+    const size_t neg_n = (size_t)s->groups * h * paths, jc_n = (size_t)W * paths;
+    if (out->neg_count && s->model == SDE_MODEL_HESTON) {
+        if (dev) a.neg_count = out->neg_count;
+        else {
+            void *p;
+            if ((rc = scratch(D, S_NEG, neg_n * sizeof(int32_t), &p))) return rc;
+            a.neg_count = (int32_t *)p;
+        }
+    }
+    if (jumps && out->jump_count) {
+        if (dev) a.jump_count = out->jump_count;
+        else {
+            void *p;
+            if ((rc = scratch(D, S_JCNT, jc_n * sizeof(int32_t), &p))) return rc;
+            a.jump_count = (int32_t *)p;
+        }
+    }
+    if (jumps && out->row_jumps) {
+        if (dev) a.row_jumps = (unsigned long long *)out->row_jumps;
+        else {
+            void *p;
+            if ((rc = scratch(D, S_ROWJ, sizeof(int64_t) * out->n_rows, &p))) return rc;
+            a.row_jumps = (unsigned long long *)p;
+        }
+        CU(cudaMemsetAsync(a.row_jumps, 0, sizeof(int64_t) * out->n_rows, st));
+    }
+    void *d_err;
+    if ((rc = scratch(D, S_ERR, 16, &d_err))) return rc;
+    CU(cudaMemsetAsync(d_err, 0, 16, st));
+    a.err = (int32_t *)d_err;
+
+    // ---- launch ----------------------------------------------------------------------
+    int bps = 0;
+    FwdLauncher<R> L = Finder<R>::find(s->model, maxm_of(M), inject, jumps, &bps);
+    if (!L) return fail(SDE_ERR_UNSUPPORTED, "no kernel for model %d group size %d", s->model, M);
+    const int nbx = path_blocks(D, paths, s->groups, bps);
+    a.stats_row = -1;
+    const int bins = stats ? req->bins : 0;
+    if (stats) {
+        a.stats_row = req->row;
+        a.n_strikes = req->n_strikes;
+        for (int i = 0; i < req->n_strikes; ++i) a.strikes[i] = (R)req->strikes[i];
+        void *p;
+        if ((rc = scratch(D, S_PART, sizeof(double) * NPART * (size_t)s->groups * nbx * opg, &p))) return rc;
+        a.partials = (double *)p;
+        if (bins > 0 && !a.xx) {
+            if ((rc = scratch(D, S_VALS, sizeof(R) * n_out * paths, &p))) return rc;
+            a.stats_vals = (R *)p;
+        }
+    }
+    L(a, dim3(nbx, s->groups), st);
+    CU(cudaGetLastError());
+
+    // ---- fused statistics --------------------------------------------------------------
+    if (stats) {
+        void *res, *edges, *edges64, *counts;
+        if ((rc = scratch(D, S_RES, sizeof(double) * RES_STRIDE * n_out, &res))) return rc;
+        if ((rc = scratch(D, S_EDGES, sizeof(R) * (bins + 1) * n_out, &edges))) return rc;
+        if ((rc = scratch(D, S_EDGES64, sizeof(double) * (bins + 1) * n_out, &edges64))) return rc;
+        stats_finalize_kernel<R><<<(unsigned)n_out, BLOCK, 0, st>>>(
+            a.partials, nbx, opg, req->n_strikes, bins, req->has_range, req->range_lo, req->range_hi,
+            (double *)res, (R *)edges, (double *)edges64, a.err);
+        CU(cudaGetLastError());
+        if (bins > 0) {
+            if ((rc = scratch(D, S_COUNTS, sizeof(int64_t) * bins * n_out, &counts))) return rc;
+            CU(cudaMemsetAsync(counts, 0, sizeof(int64_t) * bins * n_out, st));
+            const R *vals;
+            int64_t vstride;
+            if (a.xx) {
+                vals = a.xx + (int64_t)req->row * n_out * paths;
+                vstride = paths;
+            } else {
+                vals = a.stats_vals;
+                vstride = paths;
+            }
+            int hb = (int)((paths + BLOCK * 16 - 1) / (BLOCK * 16));
+            if (hb > 4 * D->sms) hb = 4 * D->sms;
+            if (hb < 1) hb = 1;
+            const size_t smem = bins <= HIST_SMEM_BINS ? sizeof(unsigned) * bins : 0;
+            hist_kernel<R><<<dim3(hb, (unsigned)n_out), BLOCK, smem, st>>>(
+                vals, vstride, paths, bins, (const R *)edges, (const double *)res, req->has_range,
+                (unsigned long long *)counts);
+            CU(cudaGetLastError());
+        }
+        std::vector<double> hres(RES_STRIDE * n_out);
+        CU(cudaMemcpyAsync(hres.data(), res, sizeof(double) * RES_STRIDE * n_out, cudaMemcpyDeviceToHost, st));
+        if (bins > 0) {
+            CU(cudaMemcpyAsync(so->counts, counts, sizeof(int64_t) * bins * n_out, cudaMemcpyDeviceToHost, st));
+            CU(cudaMemcpyAsync(so->edges, edges64, sizeof(double) * (bins + 1) * n_out, cudaMemcpyDeviceToHost, st));
+        }
+        CU(cudaStreamSynchronize(st));
+        for (int64_t o = 0; o < n_out; ++o) {
+            for (int i = 0; i < 7; ++i) so->moments[o * 8 + i] = hres[o * RES_STRIDE + i];
+            so->moments[o * 8 + 7] = 0.0;
+            for (int k = 0; k < req->n_strikes; ++k)
+                so->payoff[o * req->n_strikes + k] = hres[o * RES_STRIDE + 9 + k];
+        }
+    }
+
+    // ---- copies back ----------------------------------------------------------------------
+    if (!dev) {
+        if (out->xx && rmax >= rmin) {
+            const size_t row_bytes = (size_t)n_out * paths * sizeof(R);
+            CU(cudaMemcpyAsync((char *)out->xx + rmin * row_bytes, (char *)a.xx + rmin * row_bytes,
+                               (size_t)(rmax - rmin + 1) * row_bytes, cudaMemcpyDeviceToHost, st));
+        }
+        if (a.neg_count) CU(cudaMemcpyAsync(out->neg_count, a.neg_count, neg_n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        if (a.jump_count) CU(cudaMemcpyAsync(out->jump_count, a.jump_count, jc_n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        if (a.row_jumps) CU(cudaMemcpyAsync(out->row_jumps, a.row_jumps, sizeof(int64_t) * out->n_rows, cudaMemcpyDeviceToHost, st));
+    }
+    int32_t herr = 0;
+    CU(cudaMemcpyAsync(&herr, d_err, sizeof herr, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    if (herr & ERRF_JUMP_CAP) return fail(SDE_ERR_DEVICE, "more than %d jumps in one step", SDE_MAX_JUMPS_PER_STEP);
+    if (herr & ERRF_RANGE) return fail(SDE_ERR_INVALID, "autodetected range of the histogram is not finite");
+    return SDE_OK;
+}
+
+extern "C" int32_t sde_run(const SdeSpec *spec, const SdeGrid *grid, const SdeNoise *noise, SdeOut *out) {
+    if (!spec) return fail(SDE_ERR_INVALID, "spec is NULL");
+    if (spec->precision == SDE_FP32) return run_impl<float>(spec, grid, noise, out, nullptr, nullptr);
+    return run_impl<double>(spec, grid, noise, out, nullptr, nullptr);
+}
+
+extern "C" int32_t sde_run_stats(const SdeSpec *spec, const SdeGrid *grid, const SdeNoise *noise, SdeOut *out,
+                                 const SdeStatsReq *req, SdeStatsOut *stats) {
+    if (!spec) return fail(SDE_ERR_INVALID, "spec is NULL");
+    if (!req) return fail(SDE_ERR_INVALID, "stats request is NULL");
+    if (spec->precision == SDE_FP32) return run_impl<float>(spec, grid, noise, out, req, stats);
+    return run_impl<double>(spec, grid, noise, out, req, stats);
+}
+
+// ---------------------------------------------------------------------------
+// summaries of an existing sample
+// ---------------------------------------------------------------------------
+template <typename R>
+static int sample_stats_impl(const void *sample, int on_device, int64_t n_vars, int64_t paths,
+                             const SdeStatsReq *req, SdeStatsOut *so) {
+    int rc;
+    if (!sample || !req || !so || !so->moments) return fail(SDE_ERR_INVALID, "NULL argument");
+    if (n_vars < 1 || paths < 1 || n_vars > 65535) return fail(SDE_ERR_INVALID, "bad sample shape");
+    const int bins = req->bins;
+    if (bins < 0) return fail(SDE_ERR_INVALID, "bins must be >= 0");
+    if (bins > 0 && (!so->counts || !so->edges)) return fail(SDE_ERR_INVALID, "histogram arrays are required");
+    std::lock_guard<std::mutex> lk(g_mu);
+    Device *D;
+    if ((rc = current_device(&D))) return rc;
+    cudaStream_t st = dev_stream(D);
+    const R *vals;
+    if (on_device) {
+        vals = (const R *)sample;
+    } else {
+        void *p;
+        if ((rc = scratch(D, S_SAMPLE, sizeof(R) * n_vars * paths, &p))) return rc;
+        CU(cudaMemcpyAsync(p, sample, sizeof(R) * n_vars * paths, cudaMemcpyHostToDevice, st));
+        vals = (const R *)p;
+    }
+    int bps = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, sample_partials_kernel<R>, BLOCK, 0);
+    const int nbx = path_blocks(D, paths, (int)n_vars, bps);
+    void *part, *res, *edges, *edges64, *counts, *d_err;
+    if ((rc = scratch(D, S_PART, sizeof(double) * NPART * n_vars * nbx, &part))) return rc;
+    if ((rc = scratch(D, S_RES, sizeof(double) * RES_STRIDE * n_vars, &res))) return rc;
+    if ((rc = scratch(D, S_EDGES, sizeof(R) * (bins + 1) * n_vars, &edges))) return rc;
+    if ((rc = scratch(D, S_EDGES64, sizeof(double) * (bins + 1) * n_vars, &edges64))) return rc;
+    if ((rc = scratch(D, S_ERR, 16, &d_err))) return rc;
+    CU(cudaMemsetAsync(d_err, 0, 16, st));
+    sample_partials_kernel<R><<<dim3(nbx, (unsigned)n_vars), BLOCK, 0, st>>>(vals, paths, (double *)part, nullptr);
+    CU(cudaGetLastError());
+    stats_finalize_kernel<R><<<(unsigned)n_vars, BLOCK, 0, st>>>(
+        (const double *)part, nbx, 1, 0, bins, req->has_range, req->range_lo, req->range_hi,
+        (double *)res, (R *)edges, (double *)edges64, (int32_t *)d_err);
+    CU(cudaGetLastError());
+    if (bins > 0) {
+        if ((rc = scratch(D, S_COUNTS, sizeof(int64_t) * bins * n_vars, &counts))) return rc;
+        CU(cudaMemsetAsync(counts, 0, sizeof(int64_t) * bins * n_vars, st));
+        int hb = (int)((paths + BLOCK * 16 - 1) / (BLOCK * 16));
+        if (hb > 4 * D->sms) hb = 4 * D->sms;
+        if (hb < 1) hb = 1;
+        const size_t smem = bins <= HIST_SMEM_BINS ? sizeof(unsigned) * bins : 0;
+        hist_kernel<R><<<dim3(hb, (unsigned)n_vars), BLOCK, smem, st>>>(
+            vals, paths, paths, bins, (const R *)edges, (const double *)res, req->has_range,
+            (unsigned long long *)counts);
+        CU(cudaGetLastError());
+        CU(cudaMemcpyAsync(so->counts, counts, sizeof(int64_t) * bins * n_vars, cudaMemcpyDeviceToHost, st));
+        CU(cudaMemcpyAsync(so->edges, edges64, sizeof(double) * (bins + 1) * n_vars, cudaMemcpyDeviceToHost, st));
+    }
+    std::vector<double> hres(RES_STRIDE * n_vars);
+    int32_t herr = 0;
+    CU(cudaMemcpyAsync(hres.data(), res, sizeof(double) * RES_STRIDE * n_vars, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(&herr, d_err, sizeof herr, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    if (herr & ERRF_RANGE) return fail(SDE_ERR_INVALID, "autodetected range of the histogram is not finite");
+    for (int64_t o = 0; o < n_vars; ++o) {
+        for (int i = 0; i < 7; ++i) so->moments[o * 8 + i] = hres[o * RES_STRIDE + i];
+        so->moments[o * 8 + 7] = 0.0;
+    }
+    return SDE_OK;
+}
+
+extern "C" int32_t sde_sample_stats(const void *sample, int32_t is_fp32, int32_t on_device, int64_t n_vars,
+                                    int64_t paths, const SdeStatsReq *req, SdeStatsOut *stats) {
+    if (is_fp32) return sample_stats_impl<float>(sample, on_device, n_vars, paths, req, stats);
+    return sample_stats_impl<double>(sample, on_device, n_vars, paths, req, stats);
+}
+
+template <typename R>
+static int sample_hist_impl(const void *sample, int on_device, int64_t n_vars, int64_t paths, int bins,
+                            const double *edges_in, int64_t *counts_out) {
+    int rc;
+    if (!sample || !edges_in || !counts_out || bins < 1 || n_vars < 1 || paths < 0 || n_vars > 65535)
+        return fail(SDE_ERR_INVALID, "bad histogram arguments");
+    for (int64_t o = 0; o < n_vars; ++o)
+        for (int i = 0; i < bins; ++i)
+            if (!(edges_in[o * (bins + 1) + i] <= edges_in[o * (bins + 1) + i + 1]))
+                return fail(SDE_ERR_INVALID, "`bins` must increase monotonically, when an array");
+    std::lock_guard<std::mutex> lk(g_mu);
+    Device *D;
+    if ((rc = current_device(&D))) return rc;
+    cudaStream_t st = dev_stream(D);
+    if (paths == 0) {
+        memset(counts_out, 0, sizeof(int64_t) * bins * n_vars);
+        return SDE_OK;
+    }
+    const R *vals;
+    if (on_device) {
+        vals = (const R *)sample;
+    } else {
+        void *p;
+        if ((rc = scratch(D, S_SAMPLE, sizeof(R) * n_vars * paths, &p))) return rc;
+        CU(cudaMemcpyAsync(p, sample, sizeof(R) * n_vars * paths, cudaMemcpyHostToDevice, st));
+        vals = (const R *)p;
+    }
+    // explicit edges: general (non-uniform) bins by binary search, numpy's
+    // searchsorted rule: right-closed last bin
+    std::vector<R> he((bins + 1) * n_vars);
+    std::vector<double> hres(RES_STRIDE * n_vars, 0.0);
+    for (size_t i = 0; i < he.size(); ++i) he[i] = (R)edges_in[i];
+    void *edges, *res, *counts;
+    if ((rc = scratch(D, S_EDGES, sizeof(R) * he.size(), &edges))) return rc;
+    if ((rc = scratch(D, S_RES, sizeof(double) * hres.size(), &res))) return rc;
+    if ((rc = scratch(D, S_COUNTS, sizeof(int64_t) * bins * n_vars, &counts))) return rc;
+    CU(cudaMemcpyAsync(edges, he.data(), sizeof(R) * he.size(), cudaMemcpyHostToDevice, st));
+    CU(cudaMemsetAsync(res, 0, sizeof(double) * hres.size(), st));
+    CU(cudaMemsetAsync(counts, 0, sizeof(int64_t) * bins * n_vars, st));
+    int hb = (int)((paths + BLOCK * 16 - 1) / (BLOCK * 16));
+    if (hb > 4 * D->sms) hb = 4 * D->sms;
+    if (hb < 1) hb = 1;
+    const size_t smem = bins <= HIST_SMEM_BINS ? sizeof(unsigned) * bins : 0;
+    hist_edges_kernel<R><<<dim3(hb, (unsigned)n_vars), BLOCK, smem, st>>>(
+        vals, paths, paths, bins, (const R *)edges, (unsigned long long *)counts);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(counts_out, counts, sizeof(int64_t) * bins * n_vars, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    return SDE_OK;
+}
+
+extern "C" int32_t sde_sample_histogram(const void *sample, int32_t is_fp32, int32_t on_device, int64_t n_vars,
+                                        int64_t paths, int32_t bins, const double *edges, int64_t *counts) {
+    if (is_fp32) return sample_hist_impl<float>(sample, on_device, n_vars, paths, bins, edges, counts);
+    return sample_hist_impl<double>(sample, on_device, n_vars, paths, bins, edges, counts);
+}

@@ -1,0 +1,564 @@
+// Euler-Maruyama path integration of the sdepy preset SDEs.
+//
+// One thread owns one path of one group (the state variables that share a
+// correlated Wiener increment) and walks the whole integration grid with the
+// state in registers.  Per step it draws the group's normals (and Poisson
+// uniforms / jump sizes) from Philox counters, or reads injected increments,
+// applies the Euler step and, at output points, stores the group's outputs
+// with paths innermost (a warp writes 32 consecutive paths: 128 B for f32,
+// 256 B for f64).  Nothing else touches HBM.
+//
+// FP64 follows the operation order of sdepy's integrator.euler_next
+// (sdepy/integration.py:707-718):  x + ((A_dt*dt + A_dw*dw) + A_dj*dj),
+// with the coefficients of SDE.sde for each preset, using _rn intrinsics so
+// that no multiply-add is contracted.  FP32 lets the compiler fuse.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/sdepy_gb300.h"
+#include "rng.cuh"
+
+namespace sdegpu {
+
+constexpr int BLOCK = 256;
+constexpr int NCHOL = SDE_MAX_GROUP * (SDE_MAX_GROUP + 1) / 2;
+constexpr int NPART = 8 + SDE_MAX_STRIKES;  // n, mean, M2, M3, M4, min, max, -, payoffs
+
+// error flags (bitwise) reported by kernels
+constexpr int ERRF_JUMP_CAP = 1;
+
+template <typename R>
+struct FwdArgs {
+    int64_t paths;
+    int32_t groups, M, W, n_pts;
+    uint32_t step_offset;
+    int32_t jump_law, out_mode, opg, has_corr;
+    uint64_t seed;
+    uint32_t stream;
+    R sgn;  // sign of dt on this leg (+1 forward, -1 backward)
+    // per-step tables
+    const R *dt, *sqdt;
+    const int32_t *out_row;
+    const double *lamdt, *p0;
+    const long long *thr;
+    // per-variable inputs
+    const R *x0, *prm;  // prm[p*W + w]
+    R chol[NCHOL];      // packed lower triangle, row m at m*(m+1)/2
+    // injected increments (FP64, device)
+    const double *dw, *dj;
+    const long long *dn;
+    // outputs
+    R *xx;
+    int64_t n_out_vars;
+    int32_t *neg_count, *jump_count;
+    unsigned long long *row_jumps;
+    // fused statistics
+    int32_t stats_row, n_strikes;
+    R strikes[SDE_MAX_STRIKES];
+    R *stats_vals;     // [n_out_vars][paths] copy of the stats row, or NULL
+    double *partials;  // [groups][gridDim.x][opg][NPART], or NULL
+    int32_t *err;
+};
+
+// exact-order arithmetic for FP64, fusable for FP32
+template <typename R> struct Ar;
+template <> struct Ar<double> {
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+    static __device__ __forceinline__ double sqrt_(double a) { return __dsqrt_rn(a); }
+    static __device__ __forceinline__ double exp_(double a) { return exp(a); }
+};
+template <> struct Ar<float> {
+    static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+    static __device__ __forceinline__ float add(float a, float b) { return a + b; }
+    static __device__ __forceinline__ float sub(float a, float b) { return a - b; }
+    static __device__ __forceinline__ float sqrt_(float a) { return approx_sqrt(a); }
+    static __device__ __forceinline__ float exp_(float a) { return __expf(a); }
+};
+
+// ---------------------------------------------------------------------------
+// block-level summary of one value per thread and output variable:
+// count, mean, central sums M2..M4 (two-pass inside the block), min, max,
+// payoff sums; merged into a running per-block partial in FP64 (Pebay's
+// pairwise update), so each block's partial is exact to FP64 merge order.
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ R warp_sum(R v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+template <typename R>
+__device__ __forceinline__ R warp_min(R v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+template <typename R>
+__device__ __forceinline__ R warp_max(R v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// block sum of one value (all threads must call; result valid in all threads)
+template <typename R>
+__device__ __forceinline__ R block_sum(R v, R *red) {
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    R s = (lane < BLOCK / 32) ? red[lane] : R(0);
+    s = warp_sum(s);
+    return s;
+}
+template <typename R>
+__device__ __forceinline__ R block_min(R v, R *red) {
+    v = warp_min(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    R s = (lane < BLOCK / 32) ? red[lane] : R(INFINITY);
+    return warp_min(s);
+}
+template <typename R>
+__device__ __forceinline__ R block_max(R v, R *red) {
+    v = warp_max(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    R s = (lane < BLOCK / 32) ? red[lane] : R(-INFINITY);
+    return warp_max(s);
+}
+
+// merge (nb, mb, M2b, M3b, M4b) into (na, ma, ...) -- Pebay 2008, eq. 2.1-2.3
+__device__ __forceinline__ void moments_merge(double *A, const double *B) {
+    const double na = A[0], nb = B[0];
+    if (nb == 0.0) return;
+    if (na == 0.0) {
+        for (int i = 0; i < 5; ++i) A[i] = B[i];
+        return;
+    }
+    const double n = na + nb;
+    const double d = B[1] - A[1];
+    const double dn = d / n;
+    const double dn2 = dn * dn;
+    const double t1 = d * dn * na * nb;
+    const double M2 = A[2] + B[2] + t1;
+    const double M3 = A[3] + B[3] + t1 * dn * (na - nb) +
+                      3.0 * dn * (na * B[2] - nb * A[2]);
+    const double M4 = A[4] + B[4] + t1 * dn2 * (na * na - na * nb + nb * nb) +
+                      6.0 * dn2 * (na * na * B[2] + nb * nb * A[2]) +
+                      4.0 * dn * (na * B[3] - nb * A[3]);
+    A[0] = n;
+    A[1] = A[1] + dn * nb;
+    A[2] = M2;
+    A[3] = M3;
+    A[4] = M4;
+}
+
+// One round: every thread of the block offers value v (valid if act) for
+// one output variable; the block's summary is merged into part (smem,
+// NPART doubles) by thread 0.  All threads must call.
+template <typename R>
+__device__ void block_round_stats(R v, bool act, const R *strikes, int n_strikes,
+                                  double *part, R *red) {
+    const R one = act ? R(1) : R(0);
+    const R n = block_sum<R>(one, red);
+    if (n == R(0)) return;  // uniform across the block
+    const R s1 = block_sum<R>(act ? v : R(0), red);
+    const R mean = s1 / n;
+    const R d = act ? (v - mean) : R(0);
+    const R d2 = d * d;
+    const R r1 = block_sum<R>(d, red);
+    const R m2 = block_sum<R>(d2, red);
+    const R m3 = block_sum<R>(d2 * d, red);
+    const R m4 = block_sum<R>(d2 * d2, red);
+    const R mn = block_min<R>(act ? v : R(INFINITY), red);
+    const R mx = block_max<R>(act ? v : R(-INFINITY), red);
+    R pay[SDE_MAX_STRIKES];
+#pragma unroll
+    for (int s = 0; s < SDE_MAX_STRIKES; ++s) {
+        if (s < n_strikes) {
+            const R x = act ? fmax(v - strikes[s], R(0)) : R(0);
+            pay[s] = block_sum<R>(x, red);
+        }
+    }
+    if (threadIdx.x == 0) {
+        // recentre on the refined mean (mean + sum(d)/n) in FP64:
+        // sum (d - e)^k with e = r/n, r = sum(d)
+        const double nn = (double)n, r = (double)r1;
+        const double a2 = (double)m2, a3 = (double)m3, a4 = (double)m4;
+        const double e = r / nn;
+        double B[5];
+        B[0] = nn;
+        B[1] = (double)mean + e;
+        B[2] = a2 - r * e;
+        B[3] = a3 - 3.0 * e * a2 + 2.0 * r * e * e;
+        B[4] = a4 - 4.0 * e * a3 + 6.0 * e * e * a2 - 3.0 * r * e * e * e;
+        moments_merge(part, B);
+        part[5] = fmin(part[5], (double)mn);
+        part[6] = fmax(part[6], (double)mx);
+#pragma unroll
+        for (int s = 0; s < SDE_MAX_STRIKES; ++s)
+            if (s < n_strikes) part[8 + s] += (double)pay[s];
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// output transform of one group's state
+// ---------------------------------------------------------------------------
+template <typename R, int MAXM>
+__device__ __forceinline__ int group_outputs(const R (&st)[MAXM], int M, int out_mode,
+                                             R (&ov)[MAXM]) {
+    switch (out_mode) {
+    case SDE_OUT_EXP:
+#pragma unroll
+        for (int m = 0; m < MAXM; ++m) ov[m] = Ar<R>::exp_(st[m]);
+        return M;
+    case SDE_OUT_SUM: {
+        R s = st[0];
+#pragma unroll
+        for (int m = 1; m < MAXM; ++m)
+            if (m < M) s = Ar<R>::add(s, st[m]);
+        ov[0] = s;
+        return 1;
+    }
+    case SDE_OUT_HESTON_X:
+#pragma unroll
+        for (int m = 0; m < MAXM; ++m) ov[m] = (m < M / 2) ? Ar<R>::exp_(st[m]) : st[m];
+        return M / 2;
+    case SDE_OUT_HESTON_XY:
+#pragma unroll
+        for (int m = 0; m < MAXM; ++m) ov[m] = (m < M / 2) ? Ar<R>::exp_(st[m]) : st[m];
+        return M;
+    default:
+#pragma unroll
+        for (int m = 0; m < MAXM; ++m) ov[m] = st[m];
+        return M;
+    }
+}
+
+// Poisson count by inversion of the CDF, in FP64 (bit-exact given the
+// uniform word): smallest k with u <= F(k).  Called only when u > p0.
+__device__ __forceinline__ int poisson_tail(uint32_t word, double p0, double lam, int32_t *err) {
+    const double u = u01_f64(word);
+    int k = 0;
+    double pk = p0, F = p0;
+    while (u > F) {
+        ++k;
+        pk = __ddiv_rn(__dmul_rn(pk, lam), (double)k);
+        F = __dadd_rn(F, pk);
+        if (k >= SDE_MAX_JUMPS_PER_STEP) {
+            atomicOr(err, ERRF_JUMP_CAP);
+            break;
+        }
+    }
+    return k;
+}
+
+// one jump size of law `law` from the 4 words of its Philox call
+template <typename R>
+__device__ __forceinline__ R jump_size(int law, uint4 r, R ja, R jb, R jpa) {
+    typedef Ar<R> A;
+    switch (law) {
+    case SDE_JUMP_NORM: {
+        R z0, z1;
+        Rng<R>::normal2(r.x, r.y, z0, z1);
+        return A::add(ja, A::mul(jb, z0));
+    }
+    case SDE_JUMP_DOUBLE_EXP: {
+        const R e = Rng<R>::expo(r.x);
+        const R us = Rng<R>::unif(r.z);
+        return (us <= jpa) ? A::mul(ja, e) : -A::mul(jb, e);
+    }
+    case SDE_JUMP_UNIFORM:
+        return A::add(ja, A::mul(A::sub(jb, ja), Rng<R>::unif(r.z)));
+    case SDE_JUMP_EXP:
+        return A::mul(ja, Rng<R>::expo(r.x));
+    default:
+        return R(0);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// the forward kernel
+// ---------------------------------------------------------------------------
+template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS>
+__global__ void __launch_bounds__(BLOCK)
+sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
+    typedef Ar<R> A;
+    constexpr int NCMAX = (2 * ((MAXM + 1) / 2) + (JUMPS ? MAXM : 0) + 3) / 4;
+    __shared__ R red[BLOCK / 32];
+    __shared__ double part[MAXM][NPART];
+
+    const int g = blockIdx.y;
+    const int M = a.M;
+    const int W = a.W;
+    const int P = (M + 1) >> 1;
+    const int NC = (2 * P + (JUMPS ? M : 0) + 3) >> 2;
+    const int n_steps = a.n_pts - 1;
+    const bool do_stats = a.partials != nullptr;
+    const PhiloxKey key = {(uint32_t)a.seed, (uint32_t)(a.seed >> 32)};
+
+    // this group's coefficients, in registers
+    R x0[MAXM], c0[MAXM], c1[MAXM], c2[MAXM], c3[MAXM], c4[MAXM], c5[MAXM];
+#pragma unroll
+    for (int m = 0; m < MAXM; ++m) {
+        const int w = g * M + (m < M ? m : 0);
+        x0[m] = a.x0[w];
+        c0[m] = a.prm[0 * W + w];
+        c1[m] = a.prm[1 * W + w];
+        c2[m] = a.prm[2 * W + w];
+        c3[m] = a.prm[3 * W + w];
+        c4[m] = a.prm[4 * W + w];
+        c5[m] = a.prm[5 * W + w];
+    }
+    if (do_stats && threadIdx.x < MAXM) {
+        for (int i = 0; i < NPART; ++i) part[threadIdx.x][i] = 0.0;
+        part[threadIdx.x][5] = INFINITY;
+        part[threadIdx.x][6] = -INFINITY;
+    }
+
+    const int64_t stride = (int64_t)gridDim.x * BLOCK;
+    const int64_t rounds = (a.paths + stride - 1) / stride;
+    for (int64_t rd = 0; rd < rounds; ++rd) {
+        const int64_t p = rd * stride + (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+        const bool act = p < a.paths;
+        R sv[MAXM];
+#pragma unroll
+        for (int m = 0; m < MAXM; ++m) sv[m] = R(0);
+        if (act) {
+            R st[MAXM];
+#pragma unroll
+            for (int m = 0; m < MAXM; ++m) st[m] = x0[m];
+            int negc[MAXM];
+            int jcnt[MAXM];
+#pragma unroll
+            for (int m = 0; m < MAXM; ++m) { negc[m] = 0; jcnt[m] = 0; }
+            unsigned int row_jc = 0;
+
+            // store helper (lambda keeps the loop body readable)
+            auto store = [&](int row) {
+                R ov[MAXM];
+                const int no = group_outputs<R, MAXM>(st, M, a.out_mode, ov);
+                if (a.xx) {
+#pragma unroll
+                    for (int m = 0; m < MAXM; ++m)
+                        if (m < no)
+                            a.xx[((int64_t)row * a.n_out_vars + (int64_t)g * a.opg + m) * a.paths + p] = ov[m];
+                }
+                if (row == a.stats_row) {
+#pragma unroll
+                    for (int m = 0; m < MAXM; ++m) sv[m] = ov[m];
+                    if (a.stats_vals) {
+#pragma unroll
+                        for (int m = 0; m < MAXM; ++m)
+                            if (m < no)
+                                a.stats_vals[((int64_t)g * a.opg + m) * a.paths + p] = ov[m];
+                    }
+                }
+                if (JUMPS && a.row_jumps) {
+                    if (row_jc) atomicAdd(&a.row_jumps[row], (unsigned long long)row_jc);
+                    row_jc = 0;
+                }
+            };
+
+            {
+                const int r0 = a.out_row[0];
+                if (r0 >= 0) store(r0);
+            }
+            for (int k = 0; k < n_steps; ++k) {
+                const R dt = a.dt[k];
+                const R sq = a.sqdt[k];
+                R dW[MAXM], dJ[MAXM];
+#pragma unroll
+                for (int m = 0; m < MAXM; ++m) dJ[m] = R(0);
+                if (INJECT) {
+#pragma unroll
+                    for (int m = 0; m < MAXM; ++m) {
+                        if (m < M) {
+                            const int64_t idx = ((int64_t)k * W + g * M + m) * a.paths + p;
+                            dW[m] = (R)a.dw[idx];
+                            if (JUMPS) {
+                                dJ[m] = (R)a.dj[idx];
+                                if (a.dn) {
+                                    const int c = (int)a.dn[idx];
+                                    jcnt[m] += c;
+                                    row_jc += (unsigned int)(c < 0 ? -c : c);
+                                }
+                            }
+                        } else {
+                            dW[m] = R(0);
+                        }
+                    }
+                } else {
+                    const uint32_t c1w = (uint32_t)k + a.step_offset;
+                    uint32_t u[4 * NCMAX];
+#pragma unroll
+                    for (int c = 0; c < NCMAX; ++c) {
+                        if (c < NC) {
+                            const uint4 r = philox4x32_10(
+                                make_uint4((uint32_t)p, c1w, ((uint32_t)g << 8) | (uint32_t)c, a.stream), key);
+                            u[4 * c + 0] = r.x;
+                            u[4 * c + 1] = r.y;
+                            u[4 * c + 2] = r.z;
+                            u[4 * c + 3] = r.w;
+                        } else {
+                            u[4 * c + 0] = u[4 * c + 1] = u[4 * c + 2] = u[4 * c + 3] = 0u;
+                        }
+                    }
+                    R z[MAXM];
+#pragma unroll
+                    for (int q = 0; q < (MAXM + 1) / 2; ++q) {
+                        R z0, z1;
+                        Rng<R>::normal2(u[2 * q], u[2 * q + 1], z0, z1);
+                        z[2 * q] = z0;
+                        if (2 * q + 1 < MAXM) z[2 * q + 1] = z1;
+                    }
+                    if (a.has_corr) {
+#pragma unroll
+                        for (int m = 0; m < MAXM; ++m) {
+                            const int base = m * (m + 1) / 2;
+                            R acc = A::mul(a.chol[base], z[0]);
+#pragma unroll
+                            for (int j = 1; j <= m; ++j) acc = A::add(acc, A::mul(a.chol[base + j], z[j]));
+                            dW[m] = A::mul(acc, sq);
+                        }
+                    } else {
+#pragma unroll
+                        for (int m = 0; m < MAXM; ++m) dW[m] = A::mul(z[m], sq);
+                    }
+                    if (JUMPS) {
+#pragma unroll
+                        for (int m = 0; m < MAXM; ++m) {
+                            if (m < M) {
+                                int idx = 2 * P + m;
+                                uint32_t word = u[0];
+#pragma unroll
+                                for (int i = 0; i < 4 * NCMAX; ++i)
+                                    if (i == idx) word = u[i];
+                                const int w = g * M + m;
+                                const int64_t tix = (int64_t)k * W + w;
+                                if ((long long)word > a.thr[tix]) {
+                                    const int cnt = poisson_tail(word, a.p0[tix], a.lamdt[tix], a.err);
+                                    R S = R(0);
+                                    for (int j = 0; j < cnt; ++j) {
+                                        const uint4 r = philox4x32_10(
+                                            make_uint4((uint32_t)p, c1w,
+                                                       0x80000000u | ((uint32_t)w << 12) | (uint32_t)j,
+                                                       a.stream), key);
+                                        const R y = jump_size<R>(a.jump_law, r, c3[m], c4[m], c5[m]);
+                                        S = (j == 0) ? y : A::add(S, y);
+                                    }
+                                    dJ[m] = A::mul(a.sgn, S);
+                                    const int sc = a.sgn < R(0) ? -cnt : cnt;
+                                    jcnt[m] += sc;
+                                    row_jc += (unsigned int)cnt;
+                                }
+                            }
+                        }
+                    }
+                }
+
+                // ---- Euler step -------------------------------------------------
+                if (MODEL == SDE_MODEL_LINEAR) {
+#pragma unroll
+                    for (int m = 0; m < MAXM; ++m) {
+                        R inc = A::add(A::mul(c0[m], dt), A::mul(c1[m], dW[m]));
+                        if (JUMPS) inc = A::add(inc, dJ[m]);
+                        st[m] = A::add(st[m], inc);
+                    }
+                } else if (MODEL == SDE_MODEL_OU) {
+#pragma unroll
+                    for (int m = 0; m < MAXM; ++m) {
+                        const R drift = A::mul(c0[m], A::sub(c1[m], st[m]));
+                        st[m] = A::add(st[m], A::add(A::mul(drift, dt), A::mul(c2[m], dW[m])));
+                    }
+                } else {  // HESTON: first half log-price, second half variance
+                    // Heston kernels run with group_size == MAXM exactly
+                    constexpr int h = MAXM / 2;
+                    R nx[MAXM];
+#pragma unroll
+                    for (int i = 0; i < h; ++i) {
+                        {
+                            const R y = st[h + i];
+                            if (y < R(0)) negc[i] += 1;
+                            const R yp = fmax(y, R(0));
+                            const R sqy = A::sqrt_(yp);
+                            // x part: mu - sigma*sigma*y+/2, sigma*sqrt(y+)
+                            const R mu = c0[i], sg = c1[i];
+                            const R adt = A::sub(mu, A::mul(A::mul(A::mul(sg, sg), yp), R(0.5)));
+                            const R adw = A::mul(sg, sqy);
+                            nx[i] = A::add(st[i], A::add(A::mul(adt, dt), A::mul(adw, dW[i])));
+                            // y part: k*(theta - y+), xi*sqrt(y+)
+                            const R kk = c0[h + i], th = c1[h + i], xi = c2[h + i];
+                            const R bdt = A::mul(kk, A::sub(th, yp));
+                            const R bdw = A::mul(xi, sqy);
+                            nx[h + i] = A::add(y, A::add(A::mul(bdt, dt), A::mul(bdw, dW[h + i])));
+                        }
+                    }
+#pragma unroll
+                    for (int m = 0; m < MAXM; ++m) st[m] = nx[m];
+                }
+                const int r = a.out_row[k + 1];
+                if (r >= 0) store(r);
+            }
+            if (MODEL == SDE_MODEL_HESTON && a.neg_count) {
+                constexpr int h = MAXM / 2;
+#pragma unroll
+                for (int i = 0; i < h; ++i) a.neg_count[((int64_t)g * h + i) * a.paths + p] = negc[i];
+            }
+            if (JUMPS && a.jump_count) {
+#pragma unroll
+                for (int m = 0; m < MAXM; ++m)
+                    if (m < M) a.jump_count[((int64_t)g * M + m) * a.paths + p] = jcnt[m];
+            }
+        }
+        if (do_stats) {
+#pragma unroll
+            for (int m = 0; m < MAXM; ++m) {
+                if (m < a.opg) block_round_stats<R>(sv[m], act, a.strikes, a.n_strikes, part[m], red);
+            }
+        }
+    }
+    if (do_stats) {
+        __syncthreads();
+        if (threadIdx.x < a.opg && threadIdx.x < MAXM) {
+            double *dst = a.partials +
+                          (((int64_t)g * gridDim.x + blockIdx.x) * a.opg + threadIdx.x) * NPART;
+            for (int i = 0; i < NPART; ++i) dst[i] = part[threadIdx.x][i];
+        }
+    }
+}
+
+// launcher signature shared by the instantiation units
+template <typename R>
+using FwdLauncher = void (*)(const FwdArgs<R> &, dim3, cudaStream_t);
+
+template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS>
+void launch_fwd(const FwdArgs<R> &a, dim3 grid, cudaStream_t s) {
+    sde_fwd_kernel<R, MODEL, MAXM, INJECT, JUMPS><<<grid, BLOCK, 0, s>>>(a);
+}
+
+template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS>
+int fwd_max_blocks_per_sm() {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sde_fwd_kernel<R, MODEL, MAXM, INJECT, JUMPS>,
+                                                  BLOCK, 0);
+    return n;
+}
+
+// dispatch lookup implemented in the instantiation units (fwd_*.cu)
+FwdLauncher<double> find_fwd_f64_linear(int model, int maxm, bool inject, bool jumps, int *bps);
+FwdLauncher<double> find_fwd_f64_ou_heston(int model, int maxm, bool inject, bool jumps, int *bps);
+FwdLauncher<float> find_fwd_f32_linear(int model, int maxm, bool inject, bool jumps, int *bps);
+FwdLauncher<float> find_fwd_f32_ou_heston(int model, int maxm, bool inject, bool jumps, int *bps);
+
+}  // namespace sdegpu

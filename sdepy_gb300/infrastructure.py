@@ -1,0 +1,433 @@
+"""Host-side infrastructure mirroring sdepy's: the ``process`` result type,
+random-number keys for the device Philox streams, and the numpy
+stochasticity sources and jump-size laws.
+
+The numpy sources are not the hot path: the GPU integrator draws its own
+Philox normals and Poisson events on the device.  They exist so that a
+process built with an explicit source (``dw=...``, ``dj=...``, ``dn=...``,
+as sdepy allows) gets exactly sdepy's noise: the host realises every
+increment in sdepy's order and the device integrates them (injection mode).
+
+References (sdepy 1.2.1):
+  process constructor          sdepy/infrastructure.py:423-456
+  wiener_source                sdepy/infrastructure.py:1388-1560
+  poisson_source               sdepy/infrastructure.py:1566-1633
+  cpoisson_source              sdepy/infrastructure.py:1881-2040
+  norm/uniform/exp/double_exp  sdepy/infrastructure.py:1653-1791
+  corr / rho preprocessing     sdepy/infrastructure.py:128-206
+"""
+import numbers
+
+import numpy as np
+
+# default generator for keys and host sources (sdepy/infrastructure.py:26-41)
+default_rng = np.random.default_rng()
+
+
+def _shape_setup(shape):
+    return (shape,) if isinstance(shape, int) else tuple(shape)
+
+
+# ---------------------------------------------------------------------------
+# the process result type
+# ---------------------------------------------------------------------------
+class process(np.ndarray):
+    """Array of process values shaped ``(timeline,) + vshape + (paths,)``
+    with the timeline in the ``t`` attribute (the constructor contract of
+    sdepy.process, sdepy/infrastructure.py:423-456)."""
+
+    def __new__(cls, t=0., *, x=None, v=None, c=None, dtype=None):
+        t = np.asarray(t)
+        if t.ndim > 1 or t.size == 0:
+            raise ValueError('the shape of a process timeline should be '
+                             '() or (n,), not {}'.format(t.shape))
+        if t.ndim == 0:
+            t = t.reshape(1)
+        if sum(z is not None for z in (x, v, c)) != 1:
+            raise ValueError('when creating a process instance, one and '
+                             'only one of x or v or c should be provided')
+        if x is not None:
+            x = np.asarray(x, dtype=dtype)
+        elif v is not None:
+            x = np.asarray(v, dtype=dtype)[..., np.newaxis]
+        else:
+            c = np.asarray(c, dtype=dtype)
+            x = np.empty(t.shape + c.shape + (1,), dtype=c.dtype)
+            x[...] = c[np.newaxis, ..., np.newaxis]
+        if t.shape != x.shape[:1]:
+            raise ValueError('process could not be created from timeline t '
+                             'shaped {} and body shaped {}'
+                             .format(t.shape, x.shape))
+        obj = x.view(cls)
+        obj.t = t
+        return obj
+
+    def __array_finalize__(self, obj):
+        if obj is not None:
+            self.t = getattr(obj, 't', None)
+
+    @property
+    def paths(self):
+        return self.shape[-1]
+
+    @property
+    def vshape(self):
+        return self.shape[1:-1]
+
+    @property
+    def tx(self):
+        """Timeline broadcast to the process shape."""
+        return self.t.reshape((-1,) + (1,)*(self.ndim - 1))
+
+    def pmean(self, dtype=None):
+        return process(t=self.t, x=np.asarray(self).mean(axis=-1, keepdims=True, dtype=dtype))
+
+    def pvar(self, dtype=None, ddof=0):
+        return process(t=self.t, x=np.asarray(self).var(axis=-1, keepdims=True, dtype=dtype, ddof=ddof))
+
+    def pstd(self, dtype=None, ddof=0):
+        return process(t=self.t, x=np.asarray(self).std(axis=-1, keepdims=True, dtype=dtype, ddof=ddof))
+
+
+# ---------------------------------------------------------------------------
+# Philox keys
+# ---------------------------------------------------------------------------
+class philox_rng:
+    """Explicit key of the device Philox-4x32-10 streams.
+
+    ``philox_rng(seed)`` passed as ``rng=`` makes a process integrate the
+    counter-based stream with key ``seed``; each call of the process uses the
+    next ``stream`` value, so successive calls give independent paths while
+    a fresh ``philox_rng(seed)`` reproduces them."""
+
+    def __init__(self, seed=0, stream=0):
+        self.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+        self.stream = int(stream) & 0xFFFFFFFF
+
+    def next_key(self):
+        key = (self.seed, self.stream)
+        self.stream = (self.stream + 1) & 0xFFFFFFFF
+        return key
+
+
+def draw_key(rng):
+    """(seed, stream) for one integration: drawn from a numpy generator (so
+    that identically seeded generators give identical paths), or taken from
+    a philox_rng."""
+    if isinstance(rng, philox_rng):
+        return rng.next_key()
+    if isinstance(rng, np.random.Generator):
+        return int(rng.integers(0, 2**64, dtype=np.uint64)), 0
+    if isinstance(rng, np.random.RandomState):
+        a, b = rng.randint(0, 2**32, size=2, dtype=np.int64)
+        return (int(a) << 32) | int(b), 0
+    raise TypeError('`rng` must be a numpy.random.Generator, a '
+                    'numpy.random.RandomState or a sdepy_gb300.philox_rng, '
+                    'not {}'.format(type(rng)))
+
+
+def check_rng(rng):
+    if isinstance(rng, (numbers.Integral, list, np.ndarray)):
+        raise TypeError(
+            f'`rng` must be an instance of a random number generator, '
+            f'not {type(rng)}.')
+
+
+# ---------------------------------------------------------------------------
+# correlations (sdepy/infrastructure.py:128-206, constant values only)
+# ---------------------------------------------------------------------------
+def const_rho_to_corr(rho):
+    rho = np.asarray(rho)
+    n = rho.size
+    if rho.shape not in {(), (n,), (n, 1)}:
+        raise ValueError(
+            "correlation ``rho`` should be a vector, "
+            "possibly with a trailing 1-dimensional axis matching "
+            "the paths axis, not an array with shape {}".format(rho.shape))
+    if n == 1:
+        r = float(rho.reshape(()))
+        return np.array(((1, r), (r, 1)), dtype=float)
+    rho = rho.reshape(n)
+    I, R = np.eye(n), np.diag(rho)
+    return np.concatenate((np.concatenate((I, R)),
+                           np.concatenate((R, I))), axis=1)
+
+
+def get_corr_matrix(corr, rho):
+    """Constant correlation matrix from ``corr`` or ``rho`` (None if both
+    are None).  Time-dependent correlations are not on the GPU path."""
+    if corr is None and rho is None:
+        return None
+    z = corr if corr is not None else rho
+    if callable(z) or isinstance(z, process):
+        raise NotImplementedError(
+            'time-dependent correlations are not supported by the GPU '
+            'integrator')
+    if corr is not None:
+        c = np.asarray(corr, dtype=float)
+        if c.ndim not in (2, 3) or c.shape[0] != c.shape[1] or \
+           (c.ndim == 3 and c.shape[2] != 1):
+            raise ValueError(
+                "the correlation matrix ``corr`` should be square, "
+                "possibly with a trailing 1-dimensional axis matching "
+                "the paths axis, not an array with shape {}".format(c.shape))
+        return c[..., 0] if c.ndim == 3 else c
+    rho = np.asarray(rho, dtype=float)
+    if rho.ndim > 2 or (rho.ndim == 2 and rho.shape[1] != 1):
+        raise ValueError(
+            "correlation ``rho`` should be a vector, "
+            "possibly with a trailing 1-dimensional axis matching "
+            "the paths axis, not an array with shape {}".format(rho.shape))
+    return const_rho_to_corr(rho)
+
+
+# ---------------------------------------------------------------------------
+# jump-size laws (scipy.stats semantics of sdepy's _norm_rv etc.)
+# ---------------------------------------------------------------------------
+class _law:
+    """A constant-parameter jump-size law, recognised by the GPU kernels and
+    sampled with numpy on the host for injection mode."""
+    kind = None
+
+    def __init__(self, **params):
+        for k, v in params.items():
+            if callable(v):
+                raise NotImplementedError(
+                    'time-dependent jump-size parameters are not supported '
+                    'by the GPU integrator')
+            setattr(self, k, np.asarray(v, dtype=float))
+
+
+class norm_rv(_law):
+    """Normal jump sizes, mean ``a`` and standard deviation ``b``."""
+    kind = 'norm'
+
+    def __init__(self, a=0, b=1):
+        super().__init__(a=a, b=b)
+
+    def rvs(self, size, random_state=None):
+        rs = default_rng if random_state is None else random_state
+        return self.a + self.b*rs.standard_normal(size=size)
+
+    def mean(self):
+        return self.a + 0
+
+    def exp_mean(self):
+        return np.exp(self.a + self.b*self.b/2) + 0
+
+
+class uniform_rv(_law):
+    """Uniform jump sizes between ``a`` and ``b``."""
+    kind = 'uniform'
+
+    def __init__(self, a=0, b=1):
+        super().__init__(a=a, b=b)
+
+    def rvs(self, size, random_state=None):
+        rs = default_rng if random_state is None else random_state
+        return self.a + (self.b - self.a)*rs.uniform(size=size)
+
+    def mean(self):
+        return (self.a + self.b)/2
+
+    def exp_mean(self):
+        return (np.exp(self.b) - np.exp(self.a))/(self.b - self.a) + 0
+
+
+class exp_rv(_law):
+    """Exponential jump sizes with scale ``a`` (negative ``a``: negative
+    jumps)."""
+    kind = 'exp'
+
+    def __init__(self, a=1):
+        super().__init__(a=a)
+        if (self.a == 0).any():
+            raise ValueError('domain error in arguments')
+
+    def rvs(self, size, random_state=None):
+        rs = default_rng if random_state is None else random_state
+        return self.a*rs.standard_exponential(size=size)
+
+    def mean(self):
+        return self.a + 0
+
+    def exp_mean(self):
+        return np.where(self.a < 1, 1/(1 - self.a), np.inf) + 0
+
+
+class double_exp_rv(_law):
+    """Double exponential jump sizes: scale ``a`` with probability ``pa``,
+    ``-b`` with probability ``1 - pa``."""
+    kind = 'double_exp'
+
+    def __init__(self, a=1, b=1, pa=0.5):
+        super().__init__(a=a, b=b, pa=pa)
+        if (self.a <= 0).any() or (self.b <= 0).any() or \
+           (self.pa > 1).any() or (self.pa < 0).any():
+            raise ValueError('domain error in arguments')
+
+    def rvs(self, size, random_state=None):
+        rs = default_rng if random_state is None else random_state
+        plus = self.a*rs.standard_exponential(size=size)
+        minus = self.b*rs.standard_exponential(size=size)
+        u = rs.uniform(size=size)
+        return np.where(u <= self.pa, plus, -minus) + 0
+
+    def mean(self):
+        return self.pa*self.a - (1 - self.pa)*self.b + 0
+
+    def exp_mean(self):
+        a, b, pa = self.a, self.b, self.pa
+        return (pa/(1 - a) if a < 1 else np.inf) + (1 - pa)/(1 + b) + 0
+
+
+def law_of(y):
+    """(kind, params) of a jump-size law, recognising this module's laws
+    and scipy.stats frozen norm / uniform / expon distributions (the objects
+    sdepy's norm_rv and uniform_rv return)."""
+    if isinstance(y, _law):
+        return y.kind, y
+    dist = getattr(getattr(y, 'dist', None), 'name', None)
+    if dist in ('norm', 'uniform', 'expon'):
+        args, kwds = getattr(y, 'args', ()), getattr(y, 'kwds', {})
+        loc = kwds.get('loc', args[0] if len(args) > 0 else 0.)
+        scale = kwds.get('scale', args[1] if len(args) > 1 else 1.)
+        if dist == 'norm':
+            return 'norm', norm_rv(loc, scale)
+        if dist == 'uniform':
+            return 'uniform', uniform_rv(loc, np.asarray(loc) + np.asarray(scale))
+        if np.any(np.asarray(loc) != 0):
+            return None, None
+        return 'exp', exp_rv(scale)
+    cls = type(y).__name__
+    if cls == '_double_exp_rv':
+        return 'double_exp', double_exp_rv(y._a, y._b, y._pa)
+    if cls == '_exp_rv':
+        return 'exp', exp_rv(y._a)
+    return None, None
+
+
+# ---------------------------------------------------------------------------
+# numpy sources (host realisation for injection mode)
+# ---------------------------------------------------------------------------
+class source:
+    """Base of the host sources (sdepy/infrastructure.py:1291-1380)."""
+
+    def __init__(self, *, paths=1, vshape=(), dtype=None, rng=None):
+        self.paths, self.dtype = paths, dtype
+        self.vshape = _shape_setup(vshape)
+        check_rng(rng)
+        self._rng = default_rng if rng is None else rng
+
+    @property
+    def rng(self):
+        return self._rng
+
+
+class wiener_source(source):
+    """dw: standard Wiener increments, optionally correlated along the last
+    vshape axis (sdepy/infrastructure.py:1388-1560, constant corr)."""
+
+    def __init__(self, *, paths=1, vshape=(), dtype=None, rng=None,
+                 corr=None, rho=None):
+        super().__init__(paths=paths, vshape=vshape, dtype=dtype, rng=rng)
+        self.corr = corr = get_corr_matrix(corr, rho)
+        if corr is not None:
+            if self.vshape == ():
+                raise ValueError(
+                    'if vshape is (), no correlations apply, but '
+                    'corr={}, rho={} were given'.format(corr, rho))
+            if corr.shape[:2] != 2*self.vshape[-1:]:
+                raise ValueError(
+                    'cannot instantiate a Wiener source with '
+                    'values shape {} and correlation matrix shape {}'
+                    .format(self.vshape, corr.shape))
+
+    def __call__(self, t, dt):
+        paths, vshape, dtype = self.paths, self.vshape, self.dtype
+        t, dt = np.broadcast_arrays(t, dt)
+        tshape = dt.shape
+        if self.corr is None:
+            dz = self.rng.normal(0., 1., size=tshape + vshape + (paths,)
+                                 ).astype(dtype, copy=False)
+        else:
+            M = vshape[-1]
+            dz = self.rng.multivariate_normal(
+                mean=np.zeros(M), cov=self.corr,
+                size=tshape + vshape[:-1] + (paths,)).astype(dtype, copy=False)
+            dz = dz.swapaxes(-1, -2)
+        dt = dt.reshape(tshape + (1,)*len(vshape) + (1,))
+        dz *= np.sqrt(np.abs(dt))
+        return dz
+
+
+class poisson_source(source):
+    """dn: Poisson increments with constant intensity ``lam``
+    (sdepy/infrastructure.py:1566-1633)."""
+
+    def __init__(self, *, paths=1, vshape=(), dtype=int, rng=None, lam=1.):
+        super().__init__(paths=paths, vshape=vshape, dtype=dtype, rng=rng)
+        if callable(lam):
+            raise NotImplementedError(
+                'time-dependent intensities are not supported by the GPU '
+                'integrator')
+        self.lam = np.asarray(lam)
+        try:
+            np.broadcast_to(np.empty(self.lam.shape), self.vshape + (paths,))
+        except ValueError:
+            raise ValueError(
+                'cannot broadcast lambda parameter shaped {} to'
+                'requested poisson source shape = vshape + (paths,) = {}'
+                .format(self.lam.shape, self.vshape + (paths,)))
+
+    def __call__(self, t, dt):
+        t, dt = np.broadcast_arrays(t, dt)
+        abs_dt, sign_dt = np.abs(dt), np.sign(dt).astype(int)
+        tshape = dt.shape
+        dn = np.empty(tshape + self.vshape + (self.paths,), dtype=self.dtype)
+        for i in np.ndindex(tshape):
+            dn[i] = sign_dt[i]*self.rng.poisson(abs_dt[i]*self.lam,
+                                                self.vshape + (self.paths,))
+        return dn
+
+
+class cpoisson_source(source):
+    """dj: compound Poisson increments, the sum of ``dn`` draws of ``y``
+    (sdepy/infrastructure.py:1881-2040)."""
+
+    def __init__(self, *, paths=1, vshape=(), dtype=None, rng=None,
+                 dn=None, ptype=int, lam=1., y=None):
+        super().__init__(paths=paths, vshape=vshape, dtype=dtype, rng=rng)
+        if dn is None:
+            self.dn = poisson_source(paths=paths, vshape=vshape, dtype=ptype,
+                                     rng=rng, lam=lam)
+        elif isinstance(dn, type):
+            self.dn = dn(paths=paths, vshape=vshape, dtype=ptype, rng=rng,
+                         lam=lam)
+        else:
+            self.dn = dn
+        self.ptype = getattr(self.dn, 'dtype', ptype)
+        self.lam = getattr(self.dn, 'lam', lam)
+        self.y = uniform_rv(a=0, b=1) if y is None else y
+
+    def __call__(self, t, dt):
+        t, dt = np.broadcast_arrays(t, dt)
+        sign_dt = np.sign(dt).astype(int)
+        shape = self.vshape + (self.paths,)
+        dn = self.dn(t, dt)
+        dz = np.zeros(dt.shape + shape, dtype=self.dtype)
+        y_value = []
+        for i in np.ndindex(dt.shape):
+            dn_positive_i = sign_dt[i]*dn[i]
+            nmax = dn_positive_i.max()
+            rv = self.y(t[i] + dt[i]/2) if callable(self.y) else self.y
+            for j in range(1, nmax + 1):
+                index = (dn_positive_i == j)
+                if index.any():
+                    y_sample = rv.rvs(size=(index.sum(), j),
+                                      random_state=self.rng)
+                    dz[i][index] = sign_dt[i]*y_sample.sum(axis=-1)
+                    y_value.append(y_sample)
+        self.dn_value = dn
+        self.y_value = y_value
+        return dz

@@ -1,0 +1,235 @@
+"""Generate the golden fixtures of tests/golden/ by running the sdepy reference.
+
+Run in a container where the reference is importable:
+
+    python tests/golden/make_golden.py [REFERENCE_DIR]
+
+REFERENCE_DIR defaults to /root/reference (the read-only sdepy checkout).
+Nothing under tests/ imports this script; the tests only read the .npz files
+it writes, so the fixtures travel to machines without the reference.
+
+Each path-integration case wraps sdepy's own stochasticity sources in a
+recorder that satisfies the source protocol (sdepy/infrastructure.py:209-232:
+callable with ``paths`` and ``vshape``), so the reference integrates with its
+stock wiener_source / cpoisson_source draws while every increment it consumes
+(dw per step, dj and the Poisson counts dn_value per step) is saved next to
+its output ``xx`` and ``info``.  Replaying those increments through the GPU
+integrator must reproduce ``xx`` per path.
+
+The montecarlo cases save samples together with the reference's summary
+statistics and histograms (sdepy/infrastructure.py:2718-3115).
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+class Recorder:
+    """Source-protocol wrapper that records every realization."""
+
+    def __init__(self, src):
+        self.src = src
+        self.paths = src.paths
+        self.vshape = src.vshape
+        self.calls = []
+
+    def __call__(self, t, dt):
+        v = self.src(t, dt)
+        dn = getattr(self.src, 'dn_value', None)
+        self.calls.append((float(t), float(dt), np.array(v),
+                           None if dn is None else np.array(dn)))
+        return v
+
+    @property
+    def dn_value(self):
+        return self.src.dn_value
+
+
+def corr8(seed=7):
+    """8x8 correlation matrix: normalised A A^T + 0.1 I, A seeded Gaussian."""
+    A = np.random.default_rng(seed).normal(size=(8, 8))
+    C = A @ A.T + 0.1*np.eye(8)
+    d = np.sqrt(np.diag(C))
+    return C/np.outer(d, d)
+
+
+def run_case(sdepy, name, cls_name, kw, timeline, wshape, *, paths,
+             steps=None, i0=0, corr=None, rho=None, jumps=None, seed=0,
+             dw_src=None):
+    inf = sdepy.infrastructure
+    cls = getattr(sdepy, cls_name)
+    rng = np.random.default_rng(seed)
+    if dw_src is None:
+        dw_src = inf.wiener_source(paths=paths, vshape=wshape, rng=rng,
+                                   corr=corr, rho=rho)
+    dw = Recorder(dw_src)
+    args = dict(kw)
+    args.update(paths=paths, steps=steps, i0=i0, dw=dw)
+    dj = None
+    if jumps is not None:
+        dj = Recorder(inf.cpoisson_source(paths=paths, vshape=wshape,
+                                          rng=rng, lam=jumps['lam'],
+                                          y=jumps['y']))
+        args['dj'] = dj
+    P = cls(**args)
+    out = P(timeline)
+    outs = out if isinstance(out, tuple) else (out,)
+    rec = {
+        'name': name, 'cls': cls_name, 'paths': paths,
+        'timeline': np.asarray(timeline),
+        'steps': json.dumps(steps if (steps is None or np.isscalar(steps))
+                            else list(steps)),
+        'i0': i0,
+        'kw': json.dumps({k: np.asarray(v).tolist() for k, v in kw.items()}),
+        'corr': np.asarray(np.nan if corr is None else corr, dtype=float),
+        'rec_t': np.array([c[0] for c in dw.calls]),
+        'rec_dt': np.array([c[1] for c in dw.calls]),
+        'rec_dw': np.stack([np.broadcast_to(c[2], wshape + (paths,))
+                            for c in dw.calls]),
+        'n_out': len(outs),
+        'computed_steps': P.info['computed_steps'],
+        'stored_steps': P.info['stored_steps'],
+    }
+    for k, o in enumerate(outs):
+        rec['xx%d' % k] = np.asarray(o)
+        rec['t%d' % k] = np.asarray(o.t)
+    if dj is not None:
+        rec['rec_dj'] = np.stack([np.broadcast_to(c[2], wshape + (paths,))
+                                  for c in dj.calls])
+        rec['rec_dn'] = np.stack([np.broadcast_to(c[3], wshape + (paths,))
+                                  for c in dj.calls]).astype(np.int64)
+        rec['jump_count'] = P.info['jump_count']
+        rec['jump_rate'] = P.info['jump_rate']
+    if 'negative_y_count' in P.info:
+        rec['negative_y_count'] = P.info['negative_y_count']
+    np.savez_compressed(os.path.join(HERE, 'path_%s.npz' % name), **rec)
+    print('wrote path_%s.npz' % name, rec['rec_dw'].shape)
+
+
+def path_cases(sdepy):
+    inf = sdepy.infrastructure
+    lin = np.linspace
+    run_case(sdepy, 'lognorm_small', 'lognorm_process',
+             dict(x0=1., mu=.05, sigma=.2), lin(0, 1, 11), (), paths=64,
+             steps=40, seed=1)
+    # configs[0] grid: 253-point timeline merged with 252 linspace points
+    run_case(sdepy, 'lognorm_cfg0grid', 'lognorm_process',
+             dict(x0=1., mu=.05, sigma=.2), lin(0, 1, 253), (), paths=16,
+             steps=252, seed=2)
+    run_case(sdepy, 'wiener_vec', 'wiener_process',
+             dict(x0=[[0.], [1.]], mu=[[.1], [-.2]], sigma=[[1.], [.5]],
+                  vshape=2), lin(0, 2, 6), (2,), paths=32, steps=17, seed=3)
+    g = np.random.default_rng(11)
+    k = g.uniform(.5, 3, size=(8, 1))
+    theta = g.uniform(-1, 1, size=(8, 1))
+    sigma = g.uniform(.1, .5, size=(8, 1))
+    C = corr8()
+    run_case(sdepy, 'ou_corr8', 'ornstein_uhlenbeck_process',
+             dict(x0=0., k=k, theta=theta, sigma=sigma, vshape=8, corr=C),
+             lin(0, 5, 11), (8,), paths=48, steps=60, corr=C, seed=4)
+    run_case(sdepy, 'hull_white', 'hull_white_process',
+             dict(x0=[[.01], [.02]], k=[[.5], [2.]], theta=.03,
+                  sigma=[[.01], [.02]], vshape=3, factors=2, rho=.5),
+             lin(0, 1, 5), (3, 2), paths=24, steps=25, rho=.5, seed=5)
+    run_case(sdepy, 'heston', 'heston_process',
+             dict(x0=100., mu=.02, y0=.04, k=1.5, theta=.04, xi=.5,
+                  rho=-.7), np.array([0., .5, 1., 2.]), (2,), paths=64,
+             steps=100, rho=-.7, seed=6)
+    run_case(sdepy, 'full_heston_vec', 'full_heston_process',
+             dict(x0=[[100.], [50.]], mu=[[.02], [.01]], y0=[[.04], [.09]],
+                  k=[[1.5], [3.]], theta=[[.04], [.06]], xi=[[.5], [.9]],
+                  vshape=2, rho=[-.7, -.3]),
+             lin(0, 1, 6), (4,), paths=40, steps=60, rho=[-.7, -.3], seed=7)
+    run_case(sdepy, 'merton', 'merton_jumpdiff_process',
+             dict(x0=1., mu=.03, sigma=.15, lam=5., a=-.1, b=.15),
+             lin(0, 1, 5), (), paths=64, steps=100, seed=8,
+             jumps=dict(lam=5., y=inf.norm_rv(-.1, .15)))
+    run_case(sdepy, 'kou', 'kou_jumpdiff_process',
+             dict(x0=1., mu=.03, sigma=.15, lam=6., a=.1, b=.2, pa=.4),
+             lin(0, 1, 5), (), paths=64, steps=100, seed=9,
+             jumps=dict(lam=6., y=inf.double_exp_rv(.1, .2, .4)))
+    run_case(sdepy, 'jumpdiff_uniform', 'jumpdiff_process',
+             dict(x0=2., mu=-.1, sigma=.3, lam=3.), lin(0, 2, 3), (),
+             paths=50, steps=80, seed=10,
+             jumps=dict(lam=3., y=inf.uniform_rv(0, 1)))
+    # backward + forward integration from tt[i0]
+    run_case(sdepy, 'lognorm_i0', 'lognorm_process',
+             dict(x0=1.5, mu=.1, sigma=.4), lin(0, 1, 6), (), paths=20,
+             steps=20, i0=3, seed=12)
+    run_case(sdepy, 'ou_steps_iter', 'ornstein_uhlenbeck_process',
+             dict(x0=.5, k=2., theta=-.3, sigma=.6),
+             np.array([0., .5, 1.]), (), paths=30,
+             steps=(0.1, 0.25, 0.33, 0.9, 2.5), seed=13)
+    run_case(sdepy, 'ou_int_timeline', 'ornstein_uhlenbeck_process',
+             dict(x0=[[1.], [2.], [3.]], k=1., theta=0., sigma=1.,
+                  vshape=3), np.array([0, 1, 2, 3]), (3,), paths=12,
+             steps=10, seed=14)
+    # known answer of test_processes_misc (sdepy/tests/test_processes.py:
+    # 681-708): with a true_wiener_source the lognormal Euler scheme in
+    # log space equals the exact solution
+    paths = 31
+    dwt = inf.true_wiener_source(paths=paths,
+                                 rng=np.random.default_rng(15))
+    run_case(sdepy, 'lognorm_true_wiener', 'lognorm_process',
+             dict(x0=10., mu=.2, sigma=.7), lin(1, 4, 100), (),
+             paths=paths, dw_src=dwt)
+    np.savez_compressed(os.path.join(HERE, 'path_lognorm_true_wiener_exact.npz'),
+                        exact=10.*np.exp((.2 - .7*.7/2)*3 + .7*dwt(1, 3)))
+
+
+def mc_cases(sdepy):
+    inf = sdepy.infrastructure
+    g = np.random.default_rng(21)
+    out = {}
+    # one-shot summaries, float64 and float32
+    s64 = 1 + g.normal(size=(3, 1000))*np.array([[1.], [.1], [3.]])
+    s32 = (g.lognormal(size=(2, 777))).astype(np.float32)
+    for name, sample, kw in (('basic64', s64, dict(bins=50)),
+                             ('basic32', s32, dict(bins=40)),
+                             ('range64', s64, dict(bins=20, range=(0., 2.)))):
+        a = inf.montecarlo(sample, **kw)
+        out[name + '_sample'] = sample
+        out[name + '_mean'] = a.mean()
+        out[name + '_var'] = a.var()
+        out[name + '_std'] = a.std()
+        out[name + '_skew'] = a.skew()
+        out[name + '_kurtosis'] = a.kurtosis()
+        out[name + '_stderr'] = a.stderr()
+        out[name + '_outside'] = a._paths_outside
+        for i in range(sample.shape[0]):
+            c, b = a[i].histogram()
+            out['%s_counts%d' % (name, i)] = c
+            out['%s_bins%d' % (name, i)] = b
+    # cumulated updates: bins fixed by the first sample
+    s1 = g.normal(size=(2, 500))
+    s2 = 2*g.normal(size=(2, 700)) + .5
+    a = inf.montecarlo(s1, bins=30)
+    a.update(s2)
+    out['cum_s1'], out['cum_s2'] = s1, s2
+    out['cum_mean'], out['cum_var'] = a.mean(), a.var()
+    out['cum_skew'], out['cum_kurtosis'] = a.skew(), a.kurtosis()
+    out['cum_stderr'] = a.stderr()
+    out['cum_outside'] = a._paths_outside
+    for i in range(2):
+        c, b = a[i].histogram()
+        out['cum_counts%d' % i] = c
+        out['cum_bins%d' % i] = b
+    np.savez_compressed(os.path.join(HERE, 'montecarlo.npz'), **out)
+    print('wrote montecarlo.npz')
+
+
+def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+    sys.path.insert(0, ref)
+    import sdepy
+    print('sdepy', sdepy.__version__, 'numpy', np.__version__)
+    path_cases(sdepy)
+    mc_cases(sdepy)
+
+
+if __name__ == '__main__':
+    main()

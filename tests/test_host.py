@@ -1,0 +1,159 @@
+"""Host logic without a GPU: step grid, argument handling and the
+device spec of each preset, the C-ABI library's exports."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import sdepy_gb300 as sg
+from sdepy_gb300 import _lib
+from sdepy_gb300.grid import Grid
+from conftest import ROOT, golden_cases
+from oracle import euler
+
+
+@pytest.mark.parametrize('path', golden_cases(), ids=os.path.basename)
+def test_grid_matches_reference_steps(path):
+    """The grid's points are the (t, dt) pairs the reference called its
+    sources with, leg by leg (backward leg first)."""
+    z = np.load(path)
+    import json
+    steps = json.loads(str(z['steps']))
+    g = Grid(z['timeline'], steps, int(z['i0']))
+    t = np.concatenate([leg.tt[:-1] for leg in g.legs])
+    dt = np.concatenate([np.diff(leg.tt) for leg in g.legs])
+    np.testing.assert_array_equal(t, z['rec_t'])
+    np.testing.assert_array_equal(dt, z['rec_dt'])
+    assert g.computed_steps == int(z['computed_steps'])
+    # and the oracle's own restatement agrees
+    _, _, steps_tt, legs = euler.step_grid(z['timeline'], steps, int(z['i0']))
+    np.testing.assert_array_equal(steps_tt, g.steps_tt)
+    for (st, tt, rows, rev), leg in zip(legs, g.legs):
+        np.testing.assert_array_equal(st, leg.tt)
+        np.testing.assert_array_equal(rows, leg.out_row[leg.out_row >= 0])
+        assert rev == leg.reverse
+
+
+def test_grid_configs():
+    # configs[0] grid: 253 timeline points with 252 linspace points
+    g = Grid(np.linspace(0, 1, 253), 252)
+    assert g.computed_steps == 502
+    assert np.diff(g.steps_tt).min() > 1.5e-5
+    g = Grid(np.linspace(0, 5, 11), 1000)
+    assert g.computed_steps == 1008
+    g = Grid((0., 2.), 500)
+    assert g.computed_steps == 499
+    g = Grid((0., 1.), 365)
+    assert g.computed_steps == 364
+
+
+def test_grid_errors():
+    with pytest.raises(ValueError):
+        Grid(np.arange(6.).reshape(2, 3))
+    with pytest.raises(ValueError):
+        Grid((0., 2., 1.))
+    with pytest.raises(IndexError):
+        Grid((0., 1.), i0=5)
+
+
+def test_argument_errors():
+    with pytest.raises(TypeError):
+        sg.lognorm_process(foo=1.)
+    with pytest.raises(ValueError):
+        sg.lognorm_process(method='milstein')
+    with pytest.raises(NotImplementedError):
+        sg.lognorm_process(mu=lambda t: t)
+    with pytest.raises(NotImplementedError):
+        sg.lognorm_process(dtype=np.float16)
+    with pytest.raises(ValueError):
+        sg.ornstein_uhlenbeck_process(corr=np.eye(2))   # vshape () with corr
+    with pytest.raises(ValueError):
+        sg.ornstein_uhlenbeck_process(vshape=3, corr=np.eye(2))
+    with pytest.raises(TypeError):
+        sg.lognorm_process(rng=1234)
+    with pytest.raises(NotImplementedError):
+        sg.heston_process(vshape=3)
+    with pytest.raises(ValueError):
+        sg.kou_jumpdiff_process(a=-1.)
+
+
+def test_spec_lognorm():
+    p = sg.lognorm_process(x0=2., mu=.05, sigma=.2, paths=10)
+    assert (p._G, p._M) == (1, 1)
+    np.testing.assert_array_equal(p._x0, [np.log(2.)])
+    assert p._prm[0, 0] == .05 - .2*.2/2
+    assert p._prm[1, 0] == .2
+    assert p._out == _lib.OUT_EXP
+
+
+def test_spec_ou_corr():
+    k = np.arange(1, 9.).reshape(8, 1)
+    A = np.random.default_rng(0).normal(size=(8, 8))
+    Cm = A @ A.T + np.eye(8)
+    d = np.sqrt(np.diag(Cm))
+    Cm = Cm/np.outer(d, d)
+    p = sg.ornstein_uhlenbeck_process(vshape=8, k=k, theta=.5, sigma=.3,
+                                      corr=Cm, paths=4)
+    assert (p._G, p._M) == (1, 8)
+    np.testing.assert_array_equal(p._prm[0], k.ravel())
+    np.testing.assert_array_equal(p._prm[1], .5)
+    q = sg.ornstein_uhlenbeck_process(vshape=8, paths=4)
+    assert (q._G, q._M) == (2, 4)
+
+
+def test_spec_heston_layout():
+    p = sg.full_heston_process(vshape=2, x0=[[100.], [50.]], y0=[[.04], [.09]],
+                               mu=[[.1], [.2]], sigma=1., k=[[1.], [2.]],
+                               theta=[[.3], [.4]], xi=[[.5], [.6]], paths=3)
+    assert p.wshape == (4,) and (p._G, p._M) == (1, 4)
+    np.testing.assert_allclose(p._x0, [np.log(100.), np.log(50.), .04, .09])
+    np.testing.assert_array_equal(p._prm[0], [.1, .2, 1., 2.])
+    np.testing.assert_array_equal(p._prm[1], [1., 1., .3, .4])
+    np.testing.assert_array_equal(p._prm[2], [0., 0., .5, .6])
+    h = sg.heston_process(x0=100., paths=3)
+    assert h.wshape == (2,) and h.xshape == ()
+
+
+def test_spec_hull_white_and_jumps():
+    p = sg.hull_white_process(vshape=3, factors=2, rho=.5, paths=5)
+    assert p.wshape == (3, 2) and (p._G, p._M) == (3, 2)
+    assert p._out == _lib.OUT_SUM
+    m = sg.merton_jumpdiff_process(lam=2., a=-.1, b=.15, paths=5)
+    assert m._jump_law_id == _lib.JUMP_NORM
+    np.testing.assert_array_equal(m._prm[2:5, 0], [2., -.1, .15])
+    k = sg.kou_jumpdiff_process(lam=2., a=.1, b=.2, pa=.4, paths=5)
+    assert k._jump_law_id == _lib.JUMP_DOUBLE_EXP
+    np.testing.assert_array_equal(k._prm[2:6, 0], [2., .1, .2, .4])
+    j = sg.jumpdiff_process(paths=5)
+    assert j._jump_law_id == _lib.JUMP_UNIFORM
+
+
+def _header_symbols():
+    with open(os.path.join(ROOT, 'include', 'sdepy_gb300.h')) as f:
+        return re.findall(r'SDE_API\s+\w+\s+(sde_\w+)\s*\(', f.read())
+
+
+def test_library_exports_header_symbols():
+    import sdepy_gb300._build as b
+    path = b.build()
+    lib = C.CDLL(path)
+    syms = _header_symbols()
+    assert len(syms) >= 10
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert lib.sde_abi_version() == _lib.ABI_VERSION
+    # every header symbol has a ctypes signature in the binding
+    assert set(syms) <= set(_lib.SIGNATURES)
+
+
+def test_library_host_cholesky_without_gpu():
+    lib = _lib.load()
+    Cm = np.array([[1., .3], [.3, 1.]])
+    L = np.zeros((2, 2))
+    assert lib.sde_cholesky(_lib.dptr(Cm), 2, _lib.dptr(L)) == 0
+    np.testing.assert_allclose(L, np.linalg.cholesky(Cm), rtol=1e-15)
+    bad = np.array([[1., 2.], [2., 1.]])
+    assert lib.sde_cholesky(_lib.dptr(bad), 2, _lib.dptr(L)) == _lib.ERR_INVALID
+    assert 'semi-definite' in _lib.last_error()

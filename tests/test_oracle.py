@@ -1,0 +1,108 @@
+"""The oracle pinned against the reference: the numpy restatement against
+the fixtures recorded from sdepy itself, the C restatement against the
+published Philox known answers and scipy's Poisson quantiles."""
+import ctypes as C
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_cases
+from oracle import euler
+
+
+@pytest.mark.parametrize('path', golden_cases(), ids=os.path.basename)
+def test_numpy_oracle_reproduces_reference(path):
+    args, z = euler.load_case(path)
+    res, info = euler.integrate(**args)
+    outs = res if isinstance(res, tuple) else (res,)
+    assert len(outs) == int(z['n_out'])
+    for k, o in enumerate(outs):
+        np.testing.assert_array_equal(o, z['xx%d' % k])
+    assert info['computed_steps'] == int(z['computed_steps'])
+    assert info['stored_steps'] == int(z['stored_steps'])
+    if 'jump_count' in z:
+        np.testing.assert_array_equal(info['jump_count'], z['jump_count'])
+        np.testing.assert_array_equal(info['jump_rate'], z['jump_rate'])
+    if 'negative_y_count' in z:
+        np.testing.assert_array_equal(info['negative_y_count'], z['negative_y_count'])
+
+
+def test_numpy_oracle_known_answer():
+    # sdepy/tests/test_processes.py:681-708: with a true Wiener source the
+    # log-space Euler scheme is exact
+    args, z = euler.load_case(os.path.join(GOLDEN, 'path_lognorm_true_wiener.npz'))
+    res, _ = euler.integrate(**args)
+    exact = np.load(os.path.join(GOLDEN, 'path_lognorm_true_wiener_exact.npz'))['exact']
+    np.testing.assert_allclose(res[-1], exact, rtol=16*np.finfo(float).resolution)
+
+
+def _philox(clib, ctr, key):
+    c = (C.c_uint32*4)(*ctr)
+    k = (C.c_uint32*2)(*key)
+    o = (C.c_uint32*4)()
+    clib.oracle_philox(c, k, o)
+    return list(o)
+
+
+def test_c_oracle_philox_known_answers(clib):
+    with open(os.path.join(GOLDEN, 'philox_kat.json')) as f:
+        kat = json.load(f)
+    assert len(kat) >= 3
+    for case in kat:
+        assert _philox(clib, case['ctr'], case['key']) == case['out']
+
+
+def test_c_oracle_poisson_inversion_matches_scipy(clib):
+    stats = pytest.importorskip('scipy.stats')
+    rng = np.random.default_rng(5)
+    words = rng.integers(0, 2**32, size=4000, dtype=np.uint64)
+    for lam in (1e-3, 0.05, 0.7, 3.0, 25.0):
+        p0 = np.exp(-lam)
+        u = (words.astype(float) + 0.5)*2.0**-32
+        ref = stats.poisson.ppf(u, lam).astype(int)
+        cdf = stats.poisson.cdf(ref, lam)
+        got = np.array([clib.oracle_poisson(int(w), p0, lam) for w in words])
+        # away from CDF jumps (where rounding decides) the counts agree
+        safe = np.abs(cdf - u) > 1e-12
+        assert np.array_equal(got[safe], ref[safe])
+        assert (got >= 0).all()
+
+
+def test_c_oracle_normals(clib):
+    rng = np.random.default_rng(6)
+    a = rng.integers(0, 2**32, size=20000, dtype=np.uint64)
+    b = rng.integers(0, 2**32, size=20000, dtype=np.uint64)
+    z0, z1 = C.c_double(), C.c_double()
+    zs = []
+    for x, y in zip(a, b):
+        clib.oracle_normal2(int(x), int(y), C.byref(z0), C.byref(z1))
+        zs += [z0.value, z1.value]
+    zs = np.array(zs)
+    # the stated formula
+    u = (a.astype(float) + 0.5)*2.0**-32
+    v = (b >> np.uint64(9)).astype(float)*2.0**-22 - 1
+    r = np.sqrt(-2*np.log(u))
+    np.testing.assert_allclose(zs[0::2], r*np.cos(np.pi*v), rtol=0, atol=1e-14)
+    np.testing.assert_allclose(zs[1::2], r*np.sin(np.pi*v), rtol=0, atol=1e-14)
+    n = zs.size
+    assert abs(zs.mean()) < 4/np.sqrt(n)
+    assert abs(zs.var() - 1) < 4*np.sqrt(2/n)
+
+
+def test_c_oracle_cholesky(clib):
+    A = np.random.default_rng(7).normal(size=(8, 8))
+    Cm = A @ A.T + .1*np.eye(8)
+    d = np.sqrt(np.diag(Cm))
+    Cm = Cm/np.outer(d, d)
+    L = np.zeros((8, 8))
+    assert clib.oracle_cholesky(Cm.ctypes.data_as(C.POINTER(C.c_double)), 8,
+                                L.ctypes.data_as(C.POINTER(C.c_double))) == 0
+    np.testing.assert_allclose(L, np.linalg.cholesky(Cm), rtol=1e-13, atol=1e-15)
+    # semi-definite: rho = 1
+    S = np.ones((2, 2))
+    L2 = np.zeros((2, 2))
+    assert clib.oracle_cholesky(S.ctypes.data_as(C.POINTER(C.c_double)), 2,
+                                L2.ctypes.data_as(C.POINTER(C.c_double))) == 0
+    np.testing.assert_allclose(L2 @ L2.T, S, atol=1e-15)
