@@ -160,6 +160,19 @@ SDE_API int32_t sde_release(void);
  * library's own stream, which is ordered with the legacy default stream) */
 SDE_API int32_t sde_set_stream(void *stream);
 
+/* Kernel timing of later calls on the current device (enable = 1 / 0,
+ * or -1 to leave it unchanged).  last_ms (4 doubles, may be NULL) receives,
+ * for the last sde_run / sde_run_stats: [0] forward kernel ms, [1]
+ * statistics kernels ms, [2] blocks of the forward grid, [3] kernels
+ * launched -- measured with CUDA events on the launching stream. */
+SDE_API int32_t sde_timing(int32_t enable, double *last_ms);
+
+/* Peak-rate probe used as roofline denominator for the non-tensor,
+ * non-HBM-bound kernels: which = 0 SFU (lg2/sqrt/sin/cos approx) ops/s,
+ * 1 FP32 FMA ops/s, 2 32-bit integer multiply-high ops/s; result in ops/s
+ * for the whole device, measured with CUDA events. */
+SDE_API int32_t sde_peak_probe(int32_t which, double *ops_per_s);
+
 /* ---- host utilities (no GPU) ------------------------------------------ */
 
 /* Lower-triangular L with L*L^T = corr (M x M, row-major); tolerant of
@@ -192,6 +205,29 @@ SDE_API int32_t sde_run(const SdeSpec *spec, const SdeGrid *grid,
 SDE_API int32_t sde_run_stats(const SdeSpec *spec, const SdeGrid *grid,
                       const SdeNoise *noise, SdeOut *out,
                       const SdeStatsReq *req, SdeStatsOut *stats);
+
+/* Pathwise gradients of  L = sum_o mean_paths f(X_o(T)),
+ *   f(X) = mean_weight * X + sum_s weights[s] * max(X - strikes[s], 0),
+ * X_o(T) the outputs at the last grid point, for the device-RNG paths of
+ * (spec, grid) -- the same paths sde_run integrates.  grad is
+ * [groups*M][8]: per state variable d L / d of x0 (integration variable),
+ * params p0..p5, and in slot 7 of a group's first variable d L / d rho
+ * (2-variable Heston group with corr = [[1, rho], [rho, 1]]).  value = L.
+ * The adjoint of the Euler recursion is propagated backwards through
+ * checkpointed segments recomputed from Philox counters (constant for the
+ * LINEAR model); no path is stored.  No counterpart in the reference
+ * (sdepy has no derivatives); it differentiates the recursion of
+ * sdepy/integration.py:707-718. */
+typedef struct SdeAdjReq {
+    int32_t n_strikes;
+    int32_t checkpoint;      /* steps per segment, 0: ceil(sqrt(steps)) */
+    double strikes[SDE_MAX_STRIKES];
+    double weights[SDE_MAX_STRIKES];
+    double mean_weight;
+} SdeAdjReq;
+
+SDE_API int32_t sde_adjoint(const SdeSpec *spec, const SdeGrid *grid,
+                            const SdeAdjReq *req, double *grad, double *value);
 
 /* montecarlo summary of an existing sample [n_vars][paths] (f64 if
  * is_fp32 == 0, else f32; host or device per on_device).

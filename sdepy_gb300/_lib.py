@@ -70,8 +70,7 @@ class SdeStatsOut(C.Structure):
 
 
 class SdeAdjReq(C.Structure):
-    _fields_ = [('row', C.c_int32), ('n_strikes', C.c_int32),
-                ('checkpoint', C.c_int32), ('reserved', C.c_int32),
+    _fields_ = [('n_strikes', C.c_int32), ('checkpoint', C.c_int32),
                 ('strikes', C.c_double*MAX_STRIKES),
                 ('weights', C.c_double*MAX_STRIKES),
                 ('mean_weight', C.c_double)]
@@ -84,6 +83,8 @@ SIGNATURES = {
     'sde_device_count': (C.c_int32, []),
     'sde_release': (C.c_int32, []),
     'sde_set_stream': (C.c_int32, [C.c_void_p]),
+    'sde_timing': (C.c_int32, [C.c_int32, _dp]),
+    'sde_peak_probe': (C.c_int32, [C.c_int32, _dp]),
     'sde_cholesky': (C.c_int32, [_dp, C.c_int32, _dp]),
     'sde_run': (C.c_int32, [C.POINTER(SdeSpec), C.POINTER(SdeGrid),
                             C.POINTER(SdeNoise), C.POINTER(SdeOut)]),
@@ -91,6 +92,8 @@ SIGNATURES = {
                                   C.POINTER(SdeNoise), C.POINTER(SdeOut),
                                   C.POINTER(SdeStatsReq),
                                   C.POINTER(SdeStatsOut)]),
+    'sde_adjoint': (C.c_int32, [C.POINTER(SdeSpec), C.POINTER(SdeGrid),
+                                C.POINTER(SdeAdjReq), _dp, _dp]),
     'sde_sample_stats': (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32,
                                      C.c_int64, C.c_int64,
                                      C.POINTER(SdeStatsReq),

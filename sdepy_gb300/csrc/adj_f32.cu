@@ -1,0 +1,70 @@
+// Instantiations of sde_adj_kernel (float)
+#include "sde_adjoint.cuh"
+
+namespace sdegpu {
+
+AdjLauncher<float> find_adj_f32(int model, int maxm, bool jumps, int *bps) {
+    if (model == SDE_MODEL_LINEAR && maxm == 1 && jumps == false) {
+        if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_LINEAR, 1, false>();
+        return &launch_adj<float, SDE_MODEL_LINEAR, 1, false>;
+    }
+    if (model == SDE_MODEL_LINEAR && maxm == 1 && jumps == true) {
+        if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_LINEAR, 1, true>();
+        return &launch_adj<float, SDE_MODEL_LINEAR, 1, true>;
+    }
+    if (model == SDE_MODEL_LINEAR && maxm == 2 && jumps == false) {
+        if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_LINEAR, 2, false>();
+        return &launch_adj<float, SDE_MODEL_LINEAR, 2, false>;
+    }
+    if (model == SDE_MODEL_LINEAR && maxm == 2 && jumps == true) {
+        if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_LINEAR, 2, true>();
+        return &launch_adj<float, SDE_MODEL_LINEAR, 2, true>;
+    }
+    if (model == SDE_MODEL_LINEAR && maxm == 4 && jumps == false) {
+        if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_LINEAR, 4, false>();
+        return &launch_adj<float, SDE_MODEL_LINEAR, 4, false>;
+    }
+    if (model == SDE_MODEL_LINEAR && maxm == 4 && jumps == true) {
+        if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_LINEAR, 4, true>();
+        return &launch_adj<float, SDE_MODEL_LINEAR, 4, true>;
+    }
+    if (model == SDE_MODEL_LINEAR && maxm == 8 && jumps == false) {
+        if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_LINEAR, 8, false>();
+        return &launch_adj<float, SDE_MODEL_LINEAR, 8, false>;
+    }
+    if (model == SDE_MODEL_LINEAR && maxm == 8 && jumps == true) {
+        if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_LINEAR, 8, true>();
+        return &launch_adj<float, SDE_MODEL_LINEAR, 8, true>;
+    }
+    if (model == SDE_MODEL_OU && maxm == 1 && jumps == false) {
+        if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_OU, 1, false>();
+        return &launch_adj<float, SDE_MODEL_OU, 1, false>;
+    }
+    if (model == SDE_MODEL_OU && maxm == 2 && jumps == false) {
+        if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_OU, 2, false>();
+        return &launch_adj<float, SDE_MODEL_OU, 2, false>;
+    }
+    if (model == SDE_MODEL_OU && maxm == 4 && jumps == false) {
+        if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_OU, 4, false>();
+        return &launch_adj<float, SDE_MODEL_OU, 4, false>;
+    }
+    if (model == SDE_MODEL_OU && maxm == 8 && jumps == false) {
+        if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_OU, 8, false>();
+        return &launch_adj<float, SDE_MODEL_OU, 8, false>;
+    }
+    if (model == SDE_MODEL_HESTON && maxm == 2 && jumps == false) {
+        if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_HESTON, 2, false>();
+        return &launch_adj<float, SDE_MODEL_HESTON, 2, false>;
+    }
+    if (model == SDE_MODEL_HESTON && maxm == 4 && jumps == false) {
+        if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_HESTON, 4, false>();
+        return &launch_adj<float, SDE_MODEL_HESTON, 4, false>;
+    }
+    if (model == SDE_MODEL_HESTON && maxm == 8 && jumps == false) {
+        if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_HESTON, 8, false>();
+        return &launch_adj<float, SDE_MODEL_HESTON, 8, false>;
+    }
+    return nullptr;
+}
+
+}  // namespace sdegpu

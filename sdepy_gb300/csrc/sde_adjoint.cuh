@@ -1,0 +1,377 @@
+// Adjoint (reverse-mode) kernel of the Euler recursion: pathwise gradients
+// of L = sum_o mean_paths f(X_o(T)),  f(X) = w0*X + sum_s w_s max(X - K_s, 0),
+// with respect to the initial state and the SDE coefficients of every state
+// variable (and rho for a 2-variable Heston group).
+//
+// * LINEAR models (wiener, lognorm, jump-diffusions): dx'/dx = 1, so the
+//   adjoint is constant along the path and one forward sweep accumulating
+//   sum dt, sum dW and the jump-size derivatives gives the exact gradient.
+// * OU and Heston: the path is swept forward once storing the state every
+//   `seg` steps (checkpoints, seg ~ sqrt(N)); then, segment by segment from
+//   the last, the segment's states and increments are recomputed from their
+//   Philox counters and the adjoint is propagated backwards through it.
+//   Nothing per step is ever written to global memory.
+//
+// Integer Poisson counts are not differentiated (their intensity gets no
+// gradient); the Heston full-truncation kink contributes its one-sided
+// derivative (zero where y <= 0).
+#pragma once
+#include "sde_kernels.cuh"
+
+namespace sdegpu {
+
+constexpr int NGV = 8;          // gradient slots per state variable
+constexpr int ADJ_MAXSEG = 64;  // checkpoints and steps per segment
+
+template <typename R>
+struct AdjArgs {
+    int64_t paths;
+    int32_t groups, M, W, n_steps, seg, nseg;
+    uint32_t step_offset;
+    int32_t out_mode, jump_law, has_corr, rho_grad;
+    uint64_t seed;
+    uint32_t stream;
+    const R *dt, *sqdt;
+    const double *lamdt, *p0;
+    const long long *thr;
+    const R *x0, *prm;
+    R chol[NCHOL];
+    R rho_k;  // -rho / sqrt(1 - rho^2) for the rho gradient (2-variable Heston)
+    int32_t n_strikes;
+    R strikes[SDE_MAX_STRIKES], weights[SDE_MAX_STRIKES];
+    R wmean;
+    double *partials;  // [groups][gridDim.x][MAXM*NGV + 2]
+    int32_t *err;
+};
+
+template <typename R>
+__device__ __forceinline__ R f_value(const AdjArgs<R> &a, R X) {
+    R v = a.wmean * X;
+    for (int s = 0; s < a.n_strikes; ++s) v += a.weights[s] * fmax(X - a.strikes[s], R(0));
+    return v;
+}
+template <typename R>
+__device__ __forceinline__ R f_prime(const AdjArgs<R> &a, R X) {
+    R d = a.wmean;
+    for (int s = 0; s < a.n_strikes; ++s)
+        if (X > a.strikes[s]) d += a.weights[s];
+    return d;
+}
+
+template <typename R>
+__device__ __forceinline__ void kahan_add(R &s, R &c, R v) {
+    const R y = v - c;
+    const R t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+// terminal adjoint of the states from the functional of the outputs;
+// returns the functional's value for this path
+template <typename R, int MAXM>
+__device__ __forceinline__ R terminal_adjoint(const AdjArgs<R> &a, const R (&st)[MAXM], R (&xb)[MAXM]) {
+    const int M = a.M;
+    R val = R(0);
+#pragma unroll
+    for (int m = 0; m < MAXM; ++m) xb[m] = R(0);
+    switch (a.out_mode) {
+    case SDE_OUT_EXP:
+#pragma unroll
+        for (int m = 0; m < MAXM; ++m)
+            if (m < M) {
+                const R X = Ar<R>::exp_(st[m]);
+                val += f_value(a, X);
+                xb[m] = f_prime(a, X) * X;
+            }
+        break;
+    case SDE_OUT_SUM: {
+        R X = st[0];
+#pragma unroll
+        for (int m = 1; m < MAXM; ++m)
+            if (m < M) X = X + st[m];
+        val = f_value(a, X);
+        const R d = f_prime(a, X);
+#pragma unroll
+        for (int m = 0; m < MAXM; ++m)
+            if (m < M) xb[m] = d;
+        break;
+    }
+    case SDE_OUT_HESTON_X:
+    case SDE_OUT_HESTON_XY:
+#pragma unroll
+        for (int m = 0; m < MAXM / 2; ++m) {
+            const R X = Ar<R>::exp_(st[m]);
+            val += f_value(a, X);
+            xb[m] = f_prime(a, X) * X;
+        }
+        if (a.out_mode == SDE_OUT_HESTON_XY) {
+#pragma unroll
+            for (int m = MAXM / 2; m < MAXM; ++m) {
+                val += f_value(a, st[m]);
+                xb[m] = f_prime(a, st[m]);
+            }
+        }
+        break;
+    default:
+#pragma unroll
+        for (int m = 0; m < MAXM; ++m)
+            if (m < M) {
+                val += f_value(a, st[m]);
+                xb[m] = f_prime(a, st[m]);
+            }
+    }
+    return val;
+}
+
+// one forward Euler step of the OU / Heston models (same arithmetic as the
+// forward kernel); z: uncorrelated normals, dW: correlated increments
+template <typename R, int MODEL, int MAXM>
+__device__ __forceinline__ void fwd_step(const R (&c0)[MAXM], const R (&c1)[MAXM], const R (&c2)[MAXM],
+                                         R dt, const R (&dW)[MAXM], R (&st)[MAXM]) {
+    typedef Ar<R> A;
+    if (MODEL == SDE_MODEL_OU) {
+#pragma unroll
+        for (int m = 0; m < MAXM; ++m) {
+            const R drift = A::mul(c0[m], A::sub(c1[m], st[m]));
+            st[m] = A::add(st[m], A::add(A::mul(drift, dt), A::mul(c2[m], dW[m])));
+        }
+    } else {
+        constexpr int h = MAXM / 2;
+        R nx[MAXM];
+#pragma unroll
+        for (int i = 0; i < h; ++i) {
+            const R y = st[h + i];
+            const R yp = fmax(y, R(0));
+            const R sqy = A::sqrt_(yp);
+            const R adt = A::sub(c0[i], A::mul(A::mul(A::mul(c1[i], c1[i]), yp), R(0.5)));
+            nx[i] = A::add(st[i], A::add(A::mul(adt, dt), A::mul(A::mul(c1[i], sqy), dW[i])));
+            const R bdt = A::mul(c0[h + i], A::sub(c1[h + i], yp));
+            nx[h + i] = A::add(y, A::add(A::mul(bdt, dt), A::mul(A::mul(c2[h + i], sqy), dW[h + i])));
+        }
+#pragma unroll
+        for (int m = 0; m < MAXM; ++m) st[m] = nx[m];
+    }
+}
+
+template <typename R, int MODEL, int MAXM, bool JUMPS>
+__global__ void __launch_bounds__(BLOCK)
+sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
+    typedef Ar<R> A;
+    constexpr int NCMAX = NoiseShape<MAXM, JUMPS>::NCMAX;
+    constexpr int NPA = MAXM * NGV + 2;
+    __shared__ R red[BLOCK / 32];
+
+    const int g = blockIdx.y;
+    const int M = a.M;
+    const int W = a.W;
+    const int P = (M + 1) >> 1;
+    const int NC = (2 * P + (JUMPS ? M : 0) + 3) >> 2;
+    const PhiloxKey key = {(uint32_t)a.seed, (uint32_t)(a.seed >> 32)};
+
+    R x0[MAXM], c0[MAXM], c1[MAXM], c2[MAXM], c3[MAXM], c4[MAXM], c5[MAXM];
+#pragma unroll
+    for (int m = 0; m < MAXM; ++m) {
+        const int w = g * M + (m < M ? m : 0);
+        x0[m] = a.x0[w];
+        c0[m] = a.prm[0 * W + w];
+        c1[m] = a.prm[1 * W + w];
+        c2[m] = a.prm[2 * W + w];
+        c3[m] = a.prm[3 * W + w];
+        c4[m] = a.prm[4 * W + w];
+        c5[m] = a.prm[5 * W + w];
+    }
+    // per-thread Kahan accumulators of the gradient slots and the value
+    R acc[NPA], cmp[NPA];
+#pragma unroll
+    for (int i = 0; i < NPA; ++i) acc[i] = cmp[i] = R(0);
+
+    const int64_t stride = (int64_t)gridDim.x * BLOCK;
+    for (int64_t p = (int64_t)blockIdx.x * BLOCK + threadIdx.x; p < a.paths; p += stride) {
+        R gr[MAXM][NGV];
+#pragma unroll
+        for (int m = 0; m < MAXM; ++m)
+#pragma unroll
+            for (int j = 0; j < NGV; ++j) gr[m][j] = R(0);
+        R val;
+        if (MODEL == SDE_MODEL_LINEAR) {
+            // ---- constant adjoint: one forward sweep ------------------------------
+            R st[MAXM], sdw[MAXM], sja[MAXM], sjb[MAXM];
+            R sdt = R(0);
+#pragma unroll
+            for (int m = 0; m < MAXM; ++m) { st[m] = x0[m]; sdw[m] = sja[m] = sjb[m] = R(0); }
+            for (int k = 0; k < a.n_steps; ++k) {
+                const R dt = a.dt[k], sq = a.sqdt[k];
+                const uint32_t c1w = (uint32_t)k + a.step_offset;
+                uint32_t u[4 * NCMAX];
+                step_words<MAXM, JUMPS>(key, (uint32_t)p, c1w, (uint32_t)g, a.stream, NC, u);
+                R z[MAXM], dW[MAXM];
+                words_to_normals<R, MAXM>(u, z);
+                correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
+                sdt = sdt + dt;
+#pragma unroll
+                for (int m = 0; m < MAXM; ++m) {
+                    R inc = A::add(A::mul(c0[m], dt), A::mul(c1[m], dW[m]));
+                    sdw[m] = sdw[m] + dW[m];
+                    if (JUMPS && m < M) {
+                        const uint32_t word = pick_word(u, 2 * P + m);
+                        const int w = g * M + m;
+                        const int64_t tix = (int64_t)k * W + w;
+                        if ((long long)word > a.thr[tix]) {
+                            const int cnt = poisson_tail(word, a.p0[tix], a.lamdt[tix], a.err);
+                            R S = R(0);
+                            for (int j = 0; j < cnt; ++j) {
+                                const uint4 r = philox4x32_10(
+                                    make_uint4((uint32_t)p, c1w, 0x80000000u | ((uint32_t)w << 12) | (uint32_t)j,
+                                               a.stream), key);
+                                const R y = jump_size<R>(a.jump_law, r, c3[m], c4[m], c5[m]);
+                                R da, db;
+                                jump_size_grad<R>(a.jump_law, r, c3[m], c4[m], c5[m], da, db);
+                                sja[m] = sja[m] + da;
+                                sjb[m] = sjb[m] + db;
+                                S = (j == 0) ? y : A::add(S, y);
+                            }
+                            inc = A::add(inc, S);
+                        }
+                    }
+                    st[m] = A::add(st[m], inc);
+                }
+            }
+            R xb[MAXM];
+            val = terminal_adjoint<R, MAXM>(a, st, xb);
+#pragma unroll
+            for (int m = 0; m < MAXM; ++m) {
+                gr[m][0] = xb[m];
+                gr[m][1] = xb[m] * sdt;
+                gr[m][2] = xb[m] * sdw[m];
+                gr[m][4] = xb[m] * sja[m];
+                gr[m][5] = xb[m] * sjb[m];
+            }
+        } else {
+            // ---- checkpointed reverse sweep (OU, Heston) ----------------------------
+            R ck[ADJ_MAXSEG][MAXM];
+            R st[MAXM];
+#pragma unroll
+            for (int m = 0; m < MAXM; ++m) st[m] = x0[m];
+            for (int k = 0; k < a.n_steps; ++k) {
+                if (k % a.seg == 0) {
+#pragma unroll
+                    for (int m = 0; m < MAXM; ++m) ck[k / a.seg][m] = st[m];
+                }
+                const R sq = a.sqdt[k];
+                uint32_t u[4 * NCMAX];
+                step_words<MAXM, JUMPS>(key, (uint32_t)p, (uint32_t)k + a.step_offset, (uint32_t)g,
+                                        a.stream, NC, u);
+                R z[MAXM], dW[MAXM];
+                words_to_normals<R, MAXM>(u, z);
+                correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
+                fwd_step<R, MODEL, MAXM>(c0, c1, c2, a.dt[k], dW, st);
+            }
+            R xb[MAXM];
+            val = terminal_adjoint<R, MAXM>(a, st, xb);
+            R bx[ADJ_MAXSEG][MAXM], bw[ADJ_MAXSEG][MAXM], bz[ADJ_MAXSEG][2];
+            for (int sidx = a.nseg - 1; sidx >= 0; --sidx) {
+                const int k0 = sidx * a.seg;
+                const int k1 = min(k0 + a.seg, a.n_steps);
+#pragma unroll
+                for (int m = 0; m < MAXM; ++m) st[m] = ck[sidx][m];
+                for (int k = k0; k < k1; ++k) {
+                    const R sq = a.sqdt[k];
+                    uint32_t u[4 * NCMAX];
+                    step_words<MAXM, JUMPS>(key, (uint32_t)p, (uint32_t)k + a.step_offset, (uint32_t)g,
+                                            a.stream, NC, u);
+                    R z[MAXM], dW[MAXM];
+                    words_to_normals<R, MAXM>(u, z);
+                    correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
+#pragma unroll
+                    for (int m = 0; m < MAXM; ++m) {
+                        bx[k - k0][m] = st[m];
+                        bw[k - k0][m] = dW[m];
+                    }
+                    bz[k - k0][0] = z[0];
+                    bz[k - k0][1] = MAXM > 1 ? z[MAXM > 1 ? 1 : 0] : R(0);
+                    fwd_step<R, MODEL, MAXM>(c0, c1, c2, a.dt[k], dW, st);
+                }
+                for (int k = k1 - 1; k >= k0; --k) {
+                    const R dt = a.dt[k], sq = a.sqdt[k];
+                    if (MODEL == SDE_MODEL_OU) {
+#pragma unroll
+                        for (int m = 0; m < MAXM; ++m) {
+                            const R x = bx[k - k0][m];
+                            const R xbn = xb[m];
+                            gr[m][1] += xbn * (c1[m] - x) * dt;   // k
+                            gr[m][2] += xbn * c0[m] * dt;         // theta
+                            gr[m][3] += xbn * bw[k - k0][m];      // sigma
+                            xb[m] = xbn * (R(1) - c0[m] * dt);
+                        }
+                    } else {
+                        constexpr int h = MAXM / 2;
+#pragma unroll
+                        for (int i = 0; i < h; ++i) {
+                            const R y = bx[k - k0][h + i];
+                            const R yp = fmax(y, R(0));
+                            const R s = A::sqrt_(yp);
+                            const R ab = xb[i], ybn = xb[h + i];
+                            const R mu = c0[i], sg = c1[i];
+                            const R kk = c0[h + i], th = c1[h + i], xi = c2[h + i];
+                            const R dWx = bw[k - k0][i], dWy = bw[k - k0][h + i];
+                            gr[i][1] += ab * dt;                              // mu
+                            gr[i][2] += ab * (s * dWx - sg * yp * dt);         // sigma
+                            gr[h + i][1] += ybn * (th - yp) * dt;              // k
+                            gr[h + i][2] += ybn * kk * dt;                     // theta
+                            gr[h + i][3] += ybn * s * dWy;                     // xi
+                            if (MAXM == 2 && a.rho_grad) {
+                                // dW_y = (rho z0 + sqrt(1 - rho^2) z1) sq
+                                const R ddw = (bz[k - k0][0] + a.rho_k * bz[k - k0][1]) * sq;
+                                gr[0][7] += ybn * xi * s * ddw;
+                            }
+                            R ny = ybn;
+                            if (y > R(0) && s > R(0)) {
+                                const R inv = R(0.5) / s;
+                                const R dadyp = -sg * sg * dt * R(0.5) + sg * dWx * inv;
+                                const R dydyp = -kk * dt + xi * dWy * inv;
+                                ny = ybn + ab * dadyp + ybn * dydyp;
+                            }
+                            xb[h + i] = ny;
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int m = 0; m < MAXM; ++m) gr[m][0] = xb[m];
+        }
+        // accumulate this path
+#pragma unroll
+        for (int m = 0; m < MAXM; ++m)
+#pragma unroll
+            for (int j = 0; j < NGV; ++j) kahan_add(acc[m * NGV + j], cmp[m * NGV + j], gr[m][j]);
+        kahan_add(acc[MAXM * NGV], cmp[MAXM * NGV], val);
+    }
+    // block reduction, FP64 partial per block
+#pragma unroll
+    for (int i = 0; i < NPA - 1; ++i) {
+        const R s = block_sum<R>(acc[i] - cmp[i], red);
+        if (threadIdx.x == 0)
+            a.partials[(((int64_t)g * gridDim.x + blockIdx.x) * NPA) + i] = (double)s;
+    }
+    if (threadIdx.x == 0) a.partials[(((int64_t)g * gridDim.x + blockIdx.x) * NPA) + NPA - 1] = 0.0;
+}
+
+template <typename R>
+using AdjLauncher = void (*)(const AdjArgs<R> &, dim3, cudaStream_t);
+
+template <typename R, int MODEL, int MAXM, bool JUMPS>
+void launch_adj(const AdjArgs<R> &a, dim3 grid, cudaStream_t s) {
+    sde_adj_kernel<R, MODEL, MAXM, JUMPS><<<grid, BLOCK, 0, s>>>(a);
+}
+
+template <typename R, int MODEL, int MAXM, bool JUMPS>
+int adj_max_blocks_per_sm() {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sde_adj_kernel<R, MODEL, MAXM, JUMPS>, BLOCK, 0);
+    return n;
+}
+
+AdjLauncher<float> find_adj_f32(int model, int maxm, bool jumps, int *bps);
+AdjLauncher<double> find_adj_f64(int model, int maxm, bool jumps, int *bps);
+
+}  // namespace sdegpu

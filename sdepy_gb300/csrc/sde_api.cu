@@ -10,6 +10,7 @@
 
 #include "sde_kernels.cuh"
 #include "sde_stats.cuh"
+#include "sde_adjoint.cuh"
 
 using namespace sdegpu;
 
@@ -53,6 +54,11 @@ struct Device {
     void *ptr[N_SLOTS] = {};
     size_t cap[N_SLOTS] = {};
     std::vector<char> host_tables;
+    // optional kernel timing: events around the forward kernel and the
+    // statistics kernels of the last call, on the launching stream
+    bool timing = false;
+    cudaEvent_t ev[4] = {};
+    double last_ms[4] = {};
 };
 
 static std::mutex g_mu;
@@ -69,6 +75,7 @@ static int current_device(Device **out) {
         CU(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, d));
         D.sms = n;
         CU(cudaStreamCreate(&D.stream));
+        for (int i = 0; i < 4; ++i) CU(cudaEventCreate(&D.ev[i]));
         D.init = true;
     }
     *out = &D;
@@ -126,6 +133,17 @@ extern "C" int32_t sde_release(void) {
         D.ptr[s] = nullptr;
         D.cap[s] = 0;
     }
+    return SDE_OK;
+}
+
+extern "C" int32_t sde_timing(int32_t enable, double *last_ms) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    Device *D;
+    int rc = current_device(&D);
+    if (rc) return rc;
+    if (last_ms)
+        for (int i = 0; i < 4; ++i) last_ms[i] = D->last_ms[i];
+    if (enable >= 0) D->timing = enable != 0;
     return SDE_OK;
 }
 
@@ -474,8 +492,10 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
             a.stats_vals = (R *)p;
         }
     }
+    if (D->timing) CU(cudaEventRecord(D->ev[0], st));
     L(a, dim3(nbx, s->groups), st);
     CU(cudaGetLastError());
+    if (D->timing) CU(cudaEventRecord(D->ev[1], st));
 
     // ---- fused statistics --------------------------------------------------------------
     if (stats) {
@@ -508,6 +528,7 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
                 (unsigned long long *)counts);
             CU(cudaGetLastError());
         }
+        if (D->timing) CU(cudaEventRecord(D->ev[2], st));
         std::vector<double> hres(RES_STRIDE * n_out);
         CU(cudaMemcpyAsync(hres.data(), res, sizeof(double) * RES_STRIDE * n_out, cudaMemcpyDeviceToHost, st));
         if (bins > 0) {
@@ -537,6 +558,18 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     int32_t herr = 0;
     CU(cudaMemcpyAsync(&herr, d_err, sizeof herr, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
+    if (D->timing) {
+        float ms = 0.f;
+        CU(cudaEventElapsedTime(&ms, D->ev[0], D->ev[1]));
+        D->last_ms[0] = ms;
+        D->last_ms[1] = 0.0;
+        if (stats) {
+            CU(cudaEventElapsedTime(&ms, D->ev[1], D->ev[2]));
+            D->last_ms[1] = ms;
+        }
+        D->last_ms[2] = (double)nbx;
+        D->last_ms[3] = (double)(stats ? (bins > 0 ? 3 : 2) : 1);
+    }
     if (herr & ERRF_JUMP_CAP) return fail(SDE_ERR_DEVICE, "more than %d jumps in one step", SDE_MAX_JUMPS_PER_STEP);
     if (herr & ERRF_RANGE) return fail(SDE_ERR_INVALID, "autodetected range of the histogram is not finite");
     return SDE_OK;
@@ -685,4 +718,185 @@ extern "C" int32_t sde_sample_histogram(const void *sample, int32_t is_fp32, int
                                         int64_t paths, int32_t bins, const double *edges, int64_t *counts) {
     if (is_fp32) return sample_hist_impl<float>(sample, on_device, n_vars, paths, bins, edges, counts);
     return sample_hist_impl<double>(sample, on_device, n_vars, paths, bins, edges, counts);
+}
+
+// ---------------------------------------------------------------------------
+// adjoint
+// ---------------------------------------------------------------------------
+// fixed-order FP64 tree over blocks: out[i] = sum_b part[b*stride + i]
+__global__ void __launch_bounds__(BLOCK) reduce_partials_kernel(const double *part, int nb, int stride,
+                                                                 double *out) {
+    __shared__ double sh[BLOCK];
+    const int i = blockIdx.x;
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nb; b += BLOCK) v += part[(int64_t)b * stride + i];
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = BLOCK / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[i] = sh[0];
+}
+
+template <typename R> struct AdjFinder;
+template <> struct AdjFinder<float> {
+    static AdjLauncher<float> find(int model, int maxm, bool jumps, int *bps) { return find_adj_f32(model, maxm, jumps, bps); }
+};
+template <> struct AdjFinder<double> {
+    static AdjLauncher<double> find(int model, int maxm, bool jumps, int *bps) { return find_adj_f64(model, maxm, jumps, bps); }
+};
+
+template <typename R>
+static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *req, double *grad, double *value) {
+    int opg = 0, rc;
+    if ((rc = check_spec(s, &opg))) return rc;
+    if (!req || !grad) return fail(SDE_ERR_INVALID, "adjoint request and grad are required");
+    if (!gr || !gr->tt || gr->n_pts < 2) return fail(SDE_ERR_INVALID, "the adjoint needs a grid of >= 2 points");
+    const int n_steps = gr->n_pts - 1;
+    for (int k = 0; k < n_steps; ++k)
+        if (!(gr->tt[k + 1] > gr->tt[k])) return fail(SDE_ERR_UNSUPPORTED, "the adjoint integrates forward grids only");
+    if (req->n_strikes < 0 || req->n_strikes > SDE_MAX_STRIKES) return fail(SDE_ERR_INVALID, "bad n_strikes");
+    const int M = s->group_size, W = s->groups * M;
+    const bool jumps = s->jump_law != SDE_JUMP_NONE;
+    int maxm = maxm_of(M);
+    if (maxm > 8) return fail(SDE_ERR_UNSUPPORTED, "the adjoint supports groups of up to 8 state variables");
+    int seg = req->checkpoint > 0 ? req->checkpoint : (int)ceil(sqrt((double)n_steps));
+    if (seg > ADJ_MAXSEG) seg = ADJ_MAXSEG;
+    const int nseg = (n_steps + seg - 1) / seg;
+    if (s->model != SDE_MODEL_LINEAR && nseg > ADJ_MAXSEG)
+        return fail(SDE_ERR_UNSUPPORTED, "the adjoint supports up to %d steps", ADJ_MAXSEG * ADJ_MAXSEG);
+
+    std::lock_guard<std::mutex> lk(g_mu);
+    Device *D;
+    if ((rc = current_device(&D))) return rc;
+    cudaStream_t st = dev_stream(D);
+
+    AdjArgs<R> a;
+    memset(&a, 0, sizeof a);
+    // host tables: dt, sqdt, x0, prm, jump tables
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t njt = jumps ? (size_t)n_steps * W : 1;
+    const size_t o_dt = 0, o_sq = o_dt + al(sizeof(R) * n_steps), o_x0 = o_sq + al(sizeof(R) * n_steps);
+    const size_t o_prm = o_x0 + al(sizeof(R) * W), o_lam = o_prm + al(sizeof(R) * SDE_MAX_PARAMS * W);
+    const size_t o_p0 = o_lam + al(sizeof(double) * njt), o_thr = o_p0 + al(sizeof(double) * njt);
+    const size_t o_end = o_thr + al(sizeof(long long) * njt);
+    D->host_tables.resize(o_end);
+    char *H = D->host_tables.data();
+    R *h_dt = (R *)(H + o_dt), *h_sq = (R *)(H + o_sq), *h_x0 = (R *)(H + o_x0), *h_prm = (R *)(H + o_prm);
+    double *h_lam = (double *)(H + o_lam), *h_p0 = (double *)(H + o_p0);
+    long long *h_thr = (long long *)(H + o_thr);
+    for (int k = 0; k < n_steps; ++k) {
+        const double dt = gr->tt[k + 1] - gr->tt[k];
+        h_dt[k] = (R)dt;
+        h_sq[k] = (R)sqrt(dt);
+    }
+    for (int w = 0; w < W; ++w) h_x0[w] = (R)s->x0[w];
+    for (int i = 0; i < SDE_MAX_PARAMS * W; ++i) h_prm[i] = (R)s->params[i];
+    if (jumps)
+        for (int k = 0; k < n_steps; ++k)
+            for (int w = 0; w < W; ++w) {
+                const double L = (gr->tt[k + 1] - gr->tt[k]) * s->params[2 * W + w];
+                if (!(L >= 0.0) || L > 700.0) return fail(SDE_ERR_INVALID, "bad Poisson intensity");
+                const double p0 = exp(-L);
+                h_lam[(size_t)k * W + w] = L;
+                h_p0[(size_t)k * W + w] = p0;
+                h_thr[(size_t)k * W + w] = (long long)floor(p0 * 4294967296.0 - 0.5);
+            }
+    if (s->corr) {
+        std::vector<double> L(M * M);
+        if ((rc = sde_cholesky(s->corr, M, L.data()))) return rc;
+        for (int i = 0; i < M; ++i)
+            for (int j = 0; j <= i; ++j) a.chol[i * (i + 1) / 2 + j] = (R)L[i * M + j];
+        a.has_corr = 1;
+        if (M == 2 && s->model == SDE_MODEL_HESTON) {
+            const double rho = s->corr[2];
+            if (fabs(rho) < 1.0) {
+                a.rho_grad = 1;
+                a.rho_k = (R)(-rho / sqrt(1.0 - rho * rho));
+            }
+        }
+    }
+    void *d_tab;
+    if ((rc = scratch(D, S_TABLES, o_end, &d_tab))) return rc;
+    CU(cudaMemcpyAsync(d_tab, H, o_end, cudaMemcpyHostToDevice, st));
+    char *T = (char *)d_tab;
+    a.paths = s->paths;
+    a.groups = s->groups;
+    a.M = M;
+    a.W = W;
+    a.n_steps = n_steps;
+    a.seg = seg;
+    a.nseg = nseg;
+    a.step_offset = gr->step_offset;
+    a.out_mode = s->out_mode;
+    a.jump_law = s->jump_law;
+    a.seed = s->seed;
+    a.stream = s->stream;
+    a.dt = (const R *)(T + o_dt);
+    a.sqdt = (const R *)(T + o_sq);
+    a.x0 = (const R *)(T + o_x0);
+    a.prm = (const R *)(T + o_prm);
+    a.lamdt = (const double *)(T + o_lam);
+    a.p0 = (const double *)(T + o_p0);
+    a.thr = (const long long *)(T + o_thr);
+    a.n_strikes = req->n_strikes;
+    for (int i = 0; i < req->n_strikes; ++i) {
+        a.strikes[i] = (R)req->strikes[i];
+        a.weights[i] = (R)req->weights[i];
+    }
+    a.wmean = (R)req->mean_weight;
+    void *d_err;
+    if ((rc = scratch(D, S_ERR, 16, &d_err))) return rc;
+    CU(cudaMemsetAsync(d_err, 0, 16, st));
+    a.err = (int32_t *)d_err;
+
+    int bps = 0;
+    AdjLauncher<R> L = AdjFinder<R>::find(s->model, maxm, jumps, &bps);
+    if (!L) return fail(SDE_ERR_UNSUPPORTED, "no adjoint kernel for model %d group size %d", s->model, M);
+    const int nbx = path_blocks(D, s->paths, s->groups, bps);
+    const int npa = maxm * NGV + 2;
+    void *part, *res;
+    if ((rc = scratch(D, S_PART, sizeof(double) * (size_t)s->groups * nbx * npa, &part))) return rc;
+    if ((rc = scratch(D, S_RES, sizeof(double) * (size_t)s->groups * npa, &res))) return rc;
+    a.partials = (double *)part;
+    if (D->timing) CU(cudaEventRecord(D->ev[0], st));
+    L(a, dim3(nbx, s->groups), st);
+    CU(cudaGetLastError());
+    if (D->timing) CU(cudaEventRecord(D->ev[1], st));
+    for (int g = 0; g < s->groups; ++g) {
+        reduce_partials_kernel<<<npa, BLOCK, 0, st>>>((const double *)part + (size_t)g * nbx * npa, nbx, npa,
+                                                     (double *)res + (size_t)g * npa);
+    }
+    CU(cudaGetLastError());
+    std::vector<double> h((size_t)s->groups * npa);
+    int32_t herr = 0;
+    CU(cudaMemcpyAsync(h.data(), res, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(&herr, d_err, sizeof herr, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    if (D->timing) {
+        float ms = 0.f;
+        CU(cudaEventElapsedTime(&ms, D->ev[0], D->ev[1]));
+        D->last_ms[0] = ms;
+        D->last_ms[1] = 0.0;
+        D->last_ms[2] = nbx;
+        D->last_ms[3] = 1 + s->groups;
+    }
+    if (herr & ERRF_JUMP_CAP) return fail(SDE_ERR_DEVICE, "more than %d jumps in one step", SDE_MAX_JUMPS_PER_STEP);
+    const double inv = 1.0 / (double)s->paths;
+    double v = 0.0;
+    for (int g = 0; g < s->groups; ++g) {
+        for (int m = 0; m < M; ++m)
+            for (int j = 0; j < NGV; ++j) grad[((size_t)g * M + m) * NGV + j] = h[(size_t)g * npa + m * NGV + j] * inv;
+        v += h[(size_t)g * npa + maxm * NGV];
+    }
+    if (value) *value = v * inv;
+    return SDE_OK;
+}
+
+extern "C" int32_t sde_adjoint(const SdeSpec *spec, const SdeGrid *grid, const SdeAdjReq *req, double *grad,
+                               double *value) {
+    if (!spec) return fail(SDE_ERR_INVALID, "spec is NULL");
+    if (spec->precision == SDE_FP32) return adjoint_impl<float>(spec, grid, req, grad, value);
+    return adjoint_impl<double>(spec, grid, req, grad, value);
 }

@@ -288,13 +288,116 @@ __device__ __forceinline__ R jump_size(int law, uint4 r, R ja, R jb, R jpa) {
 }
 
 // ---------------------------------------------------------------------------
+// per-step noise of one group, shared by the forward and adjoint kernels so
+// that both see identical increments
+// ---------------------------------------------------------------------------
+template <int MAXM, bool JUMPS>
+struct NoiseShape {
+    static constexpr int NCMAX = (2 * ((MAXM + 1) / 2) + (JUMPS ? MAXM : 0) + 3) / 4;
+};
+
+// Philox words of step k: u[0 .. 2P) feed the Box-Muller pairs, u[2P + m]
+// is the Poisson uniform of state m (jump models)
+template <int MAXM, bool JUMPS>
+__device__ __forceinline__ void step_words(PhiloxKey key, uint32_t p, uint32_t c1w, uint32_t g,
+                                           uint32_t stream, int NC,
+                                           uint32_t (&u)[4 * NoiseShape<MAXM, JUMPS>::NCMAX]) {
+    constexpr int NCMAX = NoiseShape<MAXM, JUMPS>::NCMAX;
+#pragma unroll
+    for (int c = 0; c < NCMAX; ++c) {
+        if (c < NC) {
+            const uint4 r = philox4x32_10(make_uint4(p, c1w, (g << 8) | (uint32_t)c, stream), key);
+            u[4 * c + 0] = r.x;
+            u[4 * c + 1] = r.y;
+            u[4 * c + 2] = r.z;
+            u[4 * c + 3] = r.w;
+        } else {
+            u[4 * c + 0] = u[4 * c + 1] = u[4 * c + 2] = u[4 * c + 3] = 0u;
+        }
+    }
+}
+
+template <typename R, int MAXM, int NW>
+__device__ __forceinline__ void words_to_normals(const uint32_t (&u)[NW], R (&z)[MAXM]) {
+#pragma unroll
+    for (int q = 0; q < (MAXM + 1) / 2; ++q) {
+        R z0, z1;
+        Rng<R>::normal2(u[2 * q], u[2 * q + 1], z0, z1);
+        z[2 * q] = z0;
+        if (2 * q + 1 < MAXM) z[2 * q + 1] = z1;
+    }
+}
+
+// dW = (L z) * sqrt|dt| (or z * sqrt|dt| without correlation)
+template <typename R, int MAXM>
+__device__ __forceinline__ void correlate(const R *chol, bool has_corr, const R (&z)[MAXM], R sq,
+                                          R (&dW)[MAXM]) {
+    typedef Ar<R> A;
+    if (has_corr) {
+#pragma unroll
+        for (int m = 0; m < MAXM; ++m) {
+            const int base = m * (m + 1) / 2;
+            R acc = A::mul(chol[base], z[0]);
+#pragma unroll
+            for (int j = 1; j <= m; ++j) acc = A::add(acc, A::mul(chol[base + j], z[j]));
+            dW[m] = A::mul(acc, sq);
+        }
+    } else {
+#pragma unroll
+        for (int m = 0; m < MAXM; ++m) dW[m] = A::mul(z[m], sq);
+    }
+}
+
+template <int NW>
+__device__ __forceinline__ uint32_t pick_word(const uint32_t (&u)[NW], int idx) {
+    uint32_t word = u[0];
+#pragma unroll
+    for (int i = 0; i < NW; ++i)
+        if (i == idx) word = u[i];
+    return word;
+}
+
+// derivatives of one jump size with respect to the law's a and b
+template <typename R>
+__device__ __forceinline__ void jump_size_grad(int law, uint4 r, R ja, R jb, R jpa, R &da, R &db) {
+    switch (law) {
+    case SDE_JUMP_NORM: {
+        R z0, z1;
+        Rng<R>::normal2(r.x, r.y, z0, z1);
+        da = R(1);
+        db = z0;
+        return;
+    }
+    case SDE_JUMP_DOUBLE_EXP: {
+        const R e = Rng<R>::expo(r.x);
+        const R us = Rng<R>::unif(r.z);
+        if (us <= jpa) { da = e; db = R(0); }
+        else { da = R(0); db = -e; }
+        return;
+    }
+    case SDE_JUMP_UNIFORM: {
+        const R u = Rng<R>::unif(r.z);
+        da = R(1) - u;
+        db = u;
+        return;
+    }
+    case SDE_JUMP_EXP:
+        da = Rng<R>::expo(r.x);
+        db = R(0);
+        return;
+    default:
+        da = db = R(0);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // the forward kernel
 // ---------------------------------------------------------------------------
 template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS>
 __global__ void __launch_bounds__(BLOCK)
 sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     typedef Ar<R> A;
-    constexpr int NCMAX = (2 * ((MAXM + 1) / 2) + (JUMPS ? MAXM : 0) + 3) / 4;
+    constexpr int NCMAX = NoiseShape<MAXM, JUMPS>::NCMAX;
     __shared__ R red[BLOCK / 32];
     __shared__ double part[MAXM][NPART];
 
@@ -401,49 +504,15 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                 } else {
                     const uint32_t c1w = (uint32_t)k + a.step_offset;
                     uint32_t u[4 * NCMAX];
-#pragma unroll
-                    for (int c = 0; c < NCMAX; ++c) {
-                        if (c < NC) {
-                            const uint4 r = philox4x32_10(
-                                make_uint4((uint32_t)p, c1w, ((uint32_t)g << 8) | (uint32_t)c, a.stream), key);
-                            u[4 * c + 0] = r.x;
-                            u[4 * c + 1] = r.y;
-                            u[4 * c + 2] = r.z;
-                            u[4 * c + 3] = r.w;
-                        } else {
-                            u[4 * c + 0] = u[4 * c + 1] = u[4 * c + 2] = u[4 * c + 3] = 0u;
-                        }
-                    }
+                    step_words<MAXM, JUMPS>(key, (uint32_t)p, c1w, (uint32_t)g, a.stream, NC, u);
                     R z[MAXM];
-#pragma unroll
-                    for (int q = 0; q < (MAXM + 1) / 2; ++q) {
-                        R z0, z1;
-                        Rng<R>::normal2(u[2 * q], u[2 * q + 1], z0, z1);
-                        z[2 * q] = z0;
-                        if (2 * q + 1 < MAXM) z[2 * q + 1] = z1;
-                    }
-                    if (a.has_corr) {
-#pragma unroll
-                        for (int m = 0; m < MAXM; ++m) {
-                            const int base = m * (m + 1) / 2;
-                            R acc = A::mul(a.chol[base], z[0]);
-#pragma unroll
-                            for (int j = 1; j <= m; ++j) acc = A::add(acc, A::mul(a.chol[base + j], z[j]));
-                            dW[m] = A::mul(acc, sq);
-                        }
-                    } else {
-#pragma unroll
-                        for (int m = 0; m < MAXM; ++m) dW[m] = A::mul(z[m], sq);
-                    }
+                    words_to_normals<R, MAXM>(u, z);
+                    correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
                     if (JUMPS) {
 #pragma unroll
                         for (int m = 0; m < MAXM; ++m) {
                             if (m < M) {
-                                int idx = 2 * P + m;
-                                uint32_t word = u[0];
-#pragma unroll
-                                for (int i = 0; i < 4 * NCMAX; ++i)
-                                    if (i == idx) word = u[i];
+                                const uint32_t word = pick_word(u, 2 * P + m);
                                 const int w = g * M + m;
                                 const int64_t tix = (int64_t)k * W + w;
                                 if ((long long)word > a.thr[tix]) {

@@ -272,13 +272,61 @@ class _gpu_process:
 
     def __call__(self, timeline):
         grid = Grid(timeline, self.steps, self.i0)
-        return self._integrate(grid)
+        xx, _ = self._integrate(grid)
+        return self.exit(grid.tt_asis, xx)
 
-    def _integrate(self, grid, stats=None):
+    def montecarlo(self, timeline, bins=100, range=None, at=-1, strikes=None,
+                   paths_out=False):
+        """Integrate along ``timeline`` and summarise the values at timeline
+        point ``at`` with a fused device reduction.
+
+        Returns a ``montecarlo`` equal to ``montecarlo(x[at], bins=bins,
+        range=range)`` for ``x = self(timeline)`` (one per output process
+        for full_heston_process); with ``strikes``, its ``payoff``
+        attribute holds mean(max(x - K, 0)) for each strike K.  Unless
+        ``paths_out`` is true no path array is written (the states are
+        reduced in registers); with ``paths_out`` the process is returned
+        too, as ``(x, montecarlo)``."""
+        from .montecarlo import montecarlo as mc
+        grid = Grid(timeline, self.steps, self.i0)
+        row = int(np.arange(grid.n_rows)[at])
+        strikes = [] if strikes is None else [float(k) for k in np.atleast_1d(strikes)]
+        if len(strikes) > _lib.MAX_STRIKES:
+            raise ValueError('at most {} strikes'.format(_lib.MAX_STRIKES))
+        nb = 0 if bins is None else int(bins)
+        xx, st = self._integrate(grid, write=paths_out,
+                                 stats=dict(row=row, bins=nb, range=range,
+                                            strikes=strikes))
+        mom, pay, counts, edges = st
+        sdtype = np.float32 if self._precision == _lib.FP32 else np.float64
+        nout = mom.shape[0]
+
+        def build(sl, vshape):
+            a = mc.from_summary(mom[sl, :7].reshape(tuple(vshape) + (7,)), tuple(vshape),
+                                sdtype,
+                                None if counts is None else counts[sl].reshape(tuple(vshape) + (-1,)),
+                                None if edges is None else edges[sl].reshape(tuple(vshape) + (-1,)),
+                                bins=bins, range=range)
+            a.payoff = pay[sl].reshape(tuple(vshape) + (len(strikes),))
+            return a
+
+        if self._out == _lib.OUT_HESTON_XY:
+            h = nout//2
+            res = (build(slice(0, h), self.vshape), build(slice(h, nout), self.vshape))
+        else:
+            res = build(slice(0, nout), self.xshape)
+        if paths_out:
+            return self.exit(grid.tt_asis, xx), res
+        return res
+
+    def _integrate(self, grid, write=True, stats=None):
         lib = _lib.load()
         rows = grid.n_rows
         out_dtype = np.float32 if self._precision == _lib.FP32 else np.float64
-        xx = np.full((rows,) + self.xshape + (self.paths,), np.nan, dtype=out_dtype)
+        xx = None
+        if write:
+            # every row is stored by one of the legs (sdepy fills NaN first)
+            xx = np.empty((rows,) + self.xshape + (self.paths,), dtype=out_dtype)
         jumps = 'dj' in self._sources
         heston = self._model == _lib.MODEL_HESTON
         if self.getinfo:
@@ -287,9 +335,13 @@ class _gpu_process:
                              computed_steps=0, stored_steps=0)
         if not self._inject:
             seed, stream = draw_key(self._rng)
+        legs = grid.legs
+        if stats is not None and not write:
+            # only the leg that reaches the summarised row is needed
+            legs = [leg for leg in legs if stats['row'] in leg.out_row][-1:]
         neg = jc = rj = None
         stats_res = None
-        for leg in grid.legs:
+        for leg in legs:
             spec = self._make_spec(0, 0) if self._inject else \
                 self._make_spec(seed, stream)
             g = _lib.SdeGrid()
@@ -298,7 +350,7 @@ class _gpu_process:
             g.n_pts = leg.tt.size
             g.step_offset = leg.step_offset
             out = _lib.SdeOut()
-            out.xx = xx.ctypes.data
+            out.xx = None if xx is None else xx.ctypes.data
             out.n_rows = rows
             out.on_device = 0
             if self.getinfo and heston:
@@ -319,11 +371,11 @@ class _gpu_process:
                 if dj is not None:
                     noise.dj = _lib.dptr(np.ascontiguousarray(dj))
                     noise.dn = _lib.lptr(dn)
-            if stats is not None and leg is grid.legs[-1]:
-                req, so, keep_s = stats
+            if stats is not None and stats['row'] in leg.out_row:
+                req, so, arrs = self._stats_request(stats)
                 st = lib.sde_run_stats(spec, g, noise, out, req, so)
                 _lib.check(st, 'sde_run_stats')
-                stats_res = keep_s
+                stats_res = arrs
             else:
                 st = lib.sde_run(spec, g, noise, out)
                 _lib.check(st, 'sde_run')
@@ -332,8 +384,38 @@ class _gpu_process:
                 self.info['computed_steps'] += leg.n_steps
                 self.info['stored_steps'] += int((leg.out_row[1:] >= 0).sum())
                 self._leg_info(grid, leg, neg, jc, rj)
-        self._last_stats = stats_res
-        return self.exit(grid.tt_asis, xx)
+        return xx, stats_res
+
+    def _stats_request(self, stats):
+        nout = self._n_out
+        req = _lib.SdeStatsReq()
+        req.row = stats['row']
+        req.bins = stats['bins']
+        rg = stats['range']
+        if rg is not None:
+            lo, hi = rg
+            if lo > hi:
+                raise ValueError('max must be larger than min in range parameter.')
+            if not (np.isfinite(lo) and np.isfinite(hi)):
+                raise ValueError(
+                    f"supplied range of [{lo}, {hi}] is not finite")
+            req.has_range, req.range_lo, req.range_hi = 1, float(lo), float(hi)
+        ks = stats['strikes']
+        req.n_strikes = len(ks)
+        for i, k in enumerate(ks):
+            req.strikes[i] = k
+        mom = np.zeros((nout, 8))
+        pay = np.zeros((nout, max(len(ks), 1)))[:, :len(ks)].copy()
+        so = _lib.SdeStatsOut()
+        so.moments = _lib.dptr(mom)
+        so.payoff = _lib.dptr(pay) if len(ks) else None
+        counts = edges = None
+        if stats['bins'] > 0:
+            counts = np.zeros((nout, stats['bins']), dtype=np.int64)
+            edges = np.zeros((nout, stats['bins'] + 1))
+            so.counts = _lib.lptr(counts)
+            so.edges = _lib.dptr(edges)
+        return req, so, (mom, pay, counts, edges)
 
     def _leg_info(self, grid, leg, neg, jc, rj):
         paths = self.paths
