@@ -1,0 +1,143 @@
+"""Differentiable Monte Carlo expectations (torch.autograd) on the GPU.
+
+``expectation(heston_process, (0., 2.), strikes=[90, 100], paths=..., steps=...,
+x0=torch.tensor(100., requires_grad=True), ...)`` returns the torch tensor
+``[E[X_T], E[max(X_T - K_1, 0)], ...]`` of the terminal values of a scalar
+preset process; its backward pass runs the adjoint kernel of the Euler
+recursion (sde_adjoint) on the same Philox paths, recomputing states from
+checkpoints instead of storing them.  Any parameter passed as a torch tensor
+with requires_grad receives d(output)/d(parameter).
+
+Differentiable parameters per preset:
+  wiener_process            x0, mu, sigma
+  lognorm_process           x0, mu, sigma
+  ornstein_uhlenbeck_process x0, k, theta, sigma
+  heston_process            x0, mu, sigma, y0, k, theta, xi, rho
+  merton_jumpdiff_process   x0, mu, sigma, a, b
+  kou_jumpdiff_process      x0, mu, sigma, a, b
+Poisson intensities and the Kou probability pa select integer / discrete
+outcomes and are not differentiated.
+"""
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from .grid import Grid
+from .infrastructure import philox_rng
+from . import integration as I
+
+# (state index, gradient slot) per differentiable parameter; slot j + 1 is
+# parameter array p_j, slot 0 the initial state, slot 7 rho
+_MAP = {
+    'wiener_process': {'x0': (0, 0), 'mu': (0, 1), 'sigma': (0, 2)},
+    'lognorm_process': {'x0': (0, 0), 'mu': (0, 1), 'sigma': (0, 2)},
+    'ornstein_uhlenbeck_process': {'x0': (0, 0), 'k': (0, 1), 'theta': (0, 2), 'sigma': (0, 3)},
+    'heston_process': {'x0': (0, 0), 'mu': (0, 1), 'sigma': (0, 2), 'y0': (1, 0),
+                       'k': (1, 1), 'theta': (1, 2), 'xi': (1, 3), 'rho': (0, 7)},
+    'merton_jumpdiff_process': {'x0': (0, 0), 'mu': (0, 1), 'sigma': (0, 2), 'a': (0, 4), 'b': (0, 5)},
+    'kou_jumpdiff_process': {'x0': (0, 0), 'mu': (0, 1), 'sigma': (0, 2), 'a': (0, 4), 'b': (0, 5)},
+}
+
+
+def _param_grads(name, g, vals):
+    """d/d(user parameter) from the per-state gradient slots g[w][8]."""
+    m = _MAP[name]
+    out = {}
+    for p, (w, j) in m.items():
+        out[p] = g[w, j]
+    log_models = name in ('lognorm_process', 'merton_jumpdiff_process',
+                          'kou_jumpdiff_process', 'heston_process')
+    if log_models:
+        out['x0'] = g[0, 0]/vals['x0']          # state a0 = log x0
+    if name in ('lognorm_process', 'merton_jumpdiff_process', 'kou_jumpdiff_process'):
+        # c_dt = mu - sigma^2/2, c_dw = sigma
+        out['sigma'] = -vals['sigma']*g[0, 1] + g[0, 2]
+    return out
+
+
+class _Expectation(torch.autograd.Function):
+
+    @staticmethod
+    def forward(ctx, spec_fn, names, *tensors):
+        proc, grid, strikes, seed, stream, value = spec_fn()
+        ctx.spec_fn = spec_fn
+        ctx.names = names
+        ctx.shapes = [t.shape for t in tensors]
+        ctx.dtypes = [t.dtype for t in tensors]
+        return torch.as_tensor(value, dtype=torch.float64)
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        proc, grid, strikes, seed, stream, _ = ctx.spec_fn(run=False)
+        lib = _lib.load()
+        w = grad_out.detach().to('cpu', torch.float64).numpy()
+        req = _lib.SdeAdjReq()
+        req.n_strikes = len(strikes)
+        req.checkpoint = 0
+        req.mean_weight = float(w[0])
+        for i, K in enumerate(strikes):
+            req.strikes[i] = K
+            req.weights[i] = float(w[1 + i])
+        leg = grid.legs[-1]
+        g = _lib.SdeGrid()
+        g.tt = _lib.dptr(leg.tt)
+        g.out_row = _lib.iptr(leg.out_row)
+        g.n_pts = leg.tt.size
+        g.step_offset = leg.step_offset
+        spec = proc._make_spec(seed, stream)
+        grad = np.zeros((proc._W, 8))
+        val = C.c_double()
+        st = lib.sde_adjoint(C.byref(spec), C.byref(g), C.byref(req),
+                             _lib.dptr(grad), C.byref(val))
+        _lib.check(st, 'sde_adjoint')
+        vals = {k: float(np.asarray(v)) for k, v in proc.args.items()
+                if k in _MAP[type(proc).__name__]}
+        pg = _param_grads(type(proc).__name__, grad, vals)
+        outs = []
+        for n, shp, dt in zip(ctx.names, ctx.shapes, ctx.dtypes):
+            outs.append(torch.full(shp, pg[n], dtype=dt))
+        return (None, None) + tuple(outs)
+
+
+def expectation(cls, timeline, strikes=(), *, paths, steps=None,
+                dtype=np.float32, seed=0, stream=0, **params):
+    """Differentiable Monte Carlo estimate of [E[X_T], E[max(X_T - K, 0)]
+    for K in strikes] for a scalar preset process ``cls`` integrated along
+    ``timeline``; torch-tensor parameters with requires_grad get gradients
+    from the adjoint kernel (same Philox paths as the forward)."""
+    name = cls.__name__
+    if name not in _MAP:
+        raise NotImplementedError('no adjoint for {}'.format(name))
+    strikes = [float(k) for k in strikes]
+    if len(strikes) > _lib.MAX_STRIKES:
+        raise ValueError('at most {} strikes'.format(_lib.MAX_STRIKES))
+    names, tensors = [], []
+    plain = {}
+    for k, v in params.items():
+        if isinstance(v, torch.Tensor):
+            if k not in _MAP[name]:
+                raise NotImplementedError('parameter {!r} is not differentiable'.format(k))
+            if v.numel() != 1:
+                raise NotImplementedError('differentiable parameters must be scalars')
+            names.append(k)
+            tensors.append(v)
+            plain[k] = float(v.detach().cpu())
+        else:
+            plain[k] = v
+    if 'rho' in plain and name != 'heston_process':
+        raise NotImplementedError('rho is differentiable for heston_process only')
+
+    def spec_fn(run=True):
+        P = cls(paths=paths, steps=steps, dtype=dtype,
+                rng=philox_rng(seed, stream), **plain)
+        grid = Grid(timeline, steps, 0)
+        value = None
+        if run:
+            mc = P.montecarlo(timeline, bins=None, strikes=strikes)
+            value = np.concatenate(([float(np.asarray(mc.mean()).reshape(-1)[0])],
+                                    np.asarray(mc.payoff).reshape(-1)))
+        return P, grid, strikes, seed, stream, value
+
+    return _Expectation.apply(spec_fn, tuple(names), *tensors)
