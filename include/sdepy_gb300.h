@@ -229,6 +229,26 @@ typedef struct SdeAdjReq {
 SDE_API int32_t sde_adjoint(const SdeSpec *spec, const SdeGrid *grid,
                             const SdeAdjReq *req, double *grad, double *value);
 
+/* sde_run_stats for callers that cannot allocate device memory: a serving
+ * or real-time loop where cudaMalloc's implicit synchronisation is not
+ * acceptable, a plugin inside a framework that owns all device memory, a
+ * process with a memory budget fixed at start-up.  Same inputs and same
+ * host outputs as sde_run_stats with out->xx == NULL (the fused summary of
+ * device-RNG paths, nothing else written), computed with one library-owned
+ * static device array of 16 MiB instead of allocated scratch; models with
+ * jumps are not supported.  Requests that need more than the 16 MiB (grid,
+ * tables, block partials, results and, when bins > 0, the summarised
+ * values: 4 or 8 bytes x paths x outputs) fail with SDE_ERR_INVALID.
+ * stream: a cudaStream_t, or NULL for the legacy default stream.  The first
+ * call on a device looks up the array's device address; make it before any
+ * stream capture.  Calls share the array and would race if they overlapped
+ * on the GPU; each call finishes (synchronises its stream) before
+ * returning.  Calls no cudaMalloc / cudaFree.  No counterpart in the
+ * reference: an allocation-free variant of the fused summary above. */
+SDE_API int32_t sde_run_stats_static(const SdeSpec *spec, const SdeGrid *grid,
+                                     const SdeStatsReq *req, SdeStatsOut *stats,
+                                     void *stream);
+
 /* montecarlo summary of an existing sample [n_vars][paths] (f64 if
  * is_fp32 == 0, else f32; host or device per on_device).
  * Replaces montecarlo._update_moments / _update_histogram

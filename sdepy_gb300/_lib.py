@@ -94,6 +94,9 @@ SIGNATURES = {
                                   C.POINTER(SdeStatsOut)]),
     'sde_adjoint': (C.c_int32, [C.POINTER(SdeSpec), C.POINTER(SdeGrid),
                                 C.POINTER(SdeAdjReq), _dp, _dp]),
+    'sde_run_stats_static': (C.c_int32, [C.POINTER(SdeSpec), C.POINTER(SdeGrid),
+                                         C.POINTER(SdeStatsReq),
+                                         C.POINTER(SdeStatsOut), C.c_void_p]),
     'sde_sample_stats': (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32,
                                      C.c_int64, C.c_int64,
                                      C.POINTER(SdeStatsReq),

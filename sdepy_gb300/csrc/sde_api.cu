@@ -29,6 +29,14 @@ static int fail(int code, const char *fmt, ...) {
     return code;
 }
 
+namespace sdegpu {
+// error text of entry points defined in other translation units
+int set_last_error(int code, const char *msg) {
+    g_err = msg;
+    return code;
+}
+}  // namespace sdegpu
+
 #define CU(call)                                                                         \
     do {                                                                                 \
         cudaError_t e_ = (call);                                                         \
