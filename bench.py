@@ -288,11 +288,115 @@ def run_gpu(args):
         'gpu_launches': launches,
         'clocks': clk.summary(),
     }
+    res['other_configs'] = extra_configs(lib)
     if rank == 0:
         res['cpu_baseline'] = cpu_baseline(args)
         print(json.dumps(res))
     if world > 1:
         dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# the other configurations, measured beside the headline workload
+# ---------------------------------------------------------------------------
+HESTON = dict(x0=100., mu=.02, y0=.04, k=1.5, theta=.04, xi=.5, rho=-.7)
+STRIKES = [80., 90., 100., 110., 120.]
+
+
+def _time_call(fn, lib, reps=3):
+    import ctypes as C
+    last = (C.c_double*4)()
+    ts = []
+    for _ in range(reps):
+        fn()
+        lib.sde_timing(-1, last)
+        ts.append(last[0] + last[1])
+    return float(np.median(ts))
+
+
+def extra_configs(lib):
+    """configs[2] Heston (FP32 forward with fused call payoffs vs the adjoint
+    gradient of the 6 parameters; FP64 forward), configs[3] Merton / Kou
+    (FP32), configs[0] lognormal (FP64, 1e5 paths, full paths written)."""
+    import ctypes as C
+    import sdepy_gb300 as sg
+    from sdepy_gb300 import _lib
+    from sdepy_gb300.grid import Grid
+    out = {}
+    lib.sde_timing(1, None)
+
+    def fused(P, timeline, strikes, seed):
+        leg = Grid(timeline, P.steps).legs[-1]
+        g = _lib.SdeGrid()
+        g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
+        g.n_pts, g.step_offset = leg.tt.size, 0
+        o = _lib.SdeOut()
+        o.xx, o.n_rows, o.on_device = None, len(timeline), 0
+        req, so, arrs = P._stats_request(dict(row=len(timeline) - 1, bins=0, range=None, strikes=strikes))
+        spec = P._make_spec(seed, 0)
+        _lib.check(lib.sde_run_stats(C.byref(spec), C.byref(g), None, C.byref(o), C.byref(req), C.byref(so)), 'fwd')
+        return arrs, leg
+
+    # ---- Heston, 2^22 paths, 499 steps on (0, 2)
+    tl = (0., 2.)
+    H = sg.heston_process(paths=2**22, steps=500, dtype=np.float32, **HESTON)
+    leg = Grid(tl, 500).legs[-1]
+    fwd_ms = _time_call(lambda: fused(H, tl, STRIKES, 3), lib)
+    arrs, _ = fused(H, tl, STRIKES, 3)
+
+    def adj():
+        g = _lib.SdeGrid()
+        g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
+        g.n_pts, g.step_offset = leg.tt.size, 0
+        req = _lib.SdeAdjReq()
+        req.n_strikes, req.checkpoint, req.mean_weight = 5, 0, 0.
+        for i, K in enumerate(STRIKES):
+            req.strikes[i], req.weights[i] = K, .2
+        grad = np.zeros((2, 8))
+        v = C.c_double()
+        spec = H._make_spec(3, 0)
+        _lib.check(lib.sde_adjoint(C.byref(spec), C.byref(g), C.byref(req), _lib.dptr(grad), C.byref(v)), 'adj')
+        return grad
+    adj_ms = _time_call(adj, lib)
+    grad = adj()
+    H64 = sg.heston_process(paths=2**18, steps=500, **HESTON)
+    fwd64_ms = _time_call(lambda: fused(H64, tl, STRIKES, 3), lib, reps=2)
+    n = leg.n_steps
+    out['heston_configs2'] = {
+        'paths': 2**22, 'computed_steps': n,
+        'fp32_forward_ms': fwd_ms, 'fp32_adjoint_ms': adj_ms,
+        'grad_over_forward': adj_ms/fwd_ms,
+        'fp32_path_steps_per_s': 2**22*n/(fwd_ms*1e-3),
+        'fp64_path_steps_per_s': 2**18*n/(fwd64_ms*1e-3),
+        'call_prices': [float(x) for x in arrs[1][0]],
+        'gradient': {'x0': float(grad[0, 0]/HESTON['x0']), 'y0': float(grad[1, 0]),
+                     'k': float(grad[1, 1]), 'theta': float(grad[1, 2]), 'xi': float(grad[1, 3]),
+                     'rho': float(grad[0, 7])},
+        'checkpoint_segment': int(np.ceil(np.sqrt(n))),
+    }
+    # ---- jump diffusions, 2^22 paths, 364 steps on (0, 1)
+    for name, cls, kw in (('merton', sg.merton_jumpdiff_process,
+                           dict(x0=1., mu=.03, sigma=.15, lam=1., a=-.1, b=.15)),
+                          ('kou', sg.kou_jumpdiff_process,
+                           dict(x0=1., mu=.03, sigma=.15, lam=2., pa=.4, a=.1, b=.2))):
+        J = cls(paths=2**22, steps=365, dtype=np.float32, **kw)
+        ms = _time_call(lambda: fused(J, (0., 1.), [1.], 4), lib)
+        out[name + '_configs3'] = {'fp32_path_steps_per_s': 2**22*364/(ms*1e-3), 'kernel_ms': ms}
+    # ---- lognormal configs[0]: FP64, 1e5 paths, 502 steps, all 253 rows written (host output)
+    import time
+    Ln = sg.lognorm_process(x0=1., mu=.05, sigma=.2, paths=100000, steps=252, rng=sg.philox_rng(0))
+    Ln(np.linspace(0, 1, 253))
+    t0 = time.perf_counter()
+    for _ in range(3):
+        x = Ln(np.linspace(0, 1, 253))
+    wall = (time.perf_counter() - t0)/3
+    last = (C.c_double*4)()
+    lib.sde_timing(-1, last)
+    out['lognorm_configs0'] = {'fp64_kernel_ms': last[0],
+                               'fp64_path_steps_per_s': 100000*502/(last[0]*1e-3),
+                               'e2e_path_steps_per_s': 100000*502/wall,
+                               'e2e_ms': wall*1e3, 'output_bytes': int(x.nbytes)}
+    return out
 
 
 # ---------------------------------------------------------------------------

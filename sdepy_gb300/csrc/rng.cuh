@@ -23,21 +23,39 @@
 
 namespace sdegpu {
 
+// The ten round keys (k + i*(0x9E3779B9, 0xBB67AE85)) are computed once on
+// the host and read from the kernel parameter block, so a round is two wide
+// multiplies and two three-input XORs.
 struct PhiloxKey {
-    uint32_t k0, k1;
+    uint32_t k0[10], k1[10];
 };
 
-__device__ __forceinline__ uint4 philox4x32_10(uint4 c, PhiloxKey key) {
-    uint32_t k0 = key.k0, k1 = key.k1;
+__host__ __device__ inline PhiloxKey philox_schedule(uint64_t seed) {
+    PhiloxKey k;
+    uint32_t a = (uint32_t)seed, b = (uint32_t)(seed >> 32);
+    for (int i = 0; i < 10; ++i) {
+        k.k0[i] = a;
+        k.k1[i] = b;
+        a += 0x9E3779B9u;
+        b += 0xBB67AE85u;
+    }
+    return k;
+}
+
+__device__ __forceinline__ void mulwide(uint32_t a, uint32_t b, uint32_t &hi, uint32_t &lo) {
+    unsigned long long p;
+    asm("mul.wide.u32 %0, %1, %2;" : "=l"(p) : "r"(a), "r"(b));
+    hi = (uint32_t)(p >> 32);
+    lo = (uint32_t)p;
+}
+
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, const PhiloxKey &key) {
 #pragma unroll
     for (int i = 0; i < 10; ++i) {
-        const uint32_t lo0 = 0xD2511F53u * c.x;
-        const uint32_t hi0 = __umulhi(0xD2511F53u, c.x);
-        const uint32_t lo1 = 0xCD9E8D57u * c.z;
-        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z);
-        c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
-        k0 += 0x9E3779B9u;
-        k1 += 0xBB67AE85u;
+        uint32_t hi0, lo0, hi1, lo1;
+        mulwide(0xD2511F53u, c.x, hi0, lo0);
+        mulwide(0xCD9E8D57u, c.z, hi1, lo1);
+        c = make_uint4(hi1 ^ c.y ^ key.k0[i], lo1, hi0 ^ c.w ^ key.k1[i], lo0);
     }
     return c;
 }

@@ -31,6 +31,7 @@ struct AdjArgs {
     int32_t out_mode, jump_law, has_corr, rho_grad;
     uint64_t seed;
     uint32_t stream;
+    PhiloxKey key;
     const R *dt, *sqdt;
     const double *lamdt, *p0;
     const long long *thr;
@@ -166,7 +167,7 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
     const int W = a.W;
     const int P = (M + 1) >> 1;
     const int NC = (2 * P + (JUMPS ? M : 0) + 3) >> 2;
-    const PhiloxKey key = {(uint32_t)a.seed, (uint32_t)(a.seed >> 32)};
+    const PhiloxKey key = a.key;  // by value: uniform registers, not indexed parameter loads
 
     R x0[MAXM], c0[MAXM], c1[MAXM], c2[MAXM], c3[MAXM], c4[MAXM], c5[MAXM];
 #pragma unroll

@@ -50,7 +50,7 @@ int set_last_error(int code, const char *msg) {
 // ---------------------------------------------------------------------------
 enum Slot {
     S_TABLES, S_NOISE_DW, S_NOISE_DJ, S_NOISE_DN, S_XX, S_NEG, S_JCNT, S_ROWJ,
-    S_PART, S_RES, S_EDGES, S_EDGES64, S_COUNTS, S_VALS, S_ERR, S_SAMPLE, N_SLOTS
+    S_PART, S_RES, S_EDGES, S_EDGES64, S_COUNTS, S_VALS, S_ERR, S_SAMPLE, S_COEF, N_SLOTS
 };
 
 struct Device {
@@ -332,7 +332,12 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     const size_t njt = jumps ? (size_t)n_steps * W + 1 : 1;
     const size_t o_p0 = o_lam + al(sizeof(double) * njt);
     const size_t o_thr = o_p0 + al(sizeof(double) * njt);
-    const size_t o_end = o_thr + al(sizeof(long long) * njt);
+    const bool tab = sizeof(R) == 4 && !inject && s->model != SDE_MODEL_HESTON;
+    const int tmaxm = maxm_of(M);
+    // raw FP64 grid and coefficients for the device-built coefficient table
+    const size_t o_rtt = o_thr + al(sizeof(long long) * njt);
+    const size_t o_rprm = o_rtt + al(sizeof(double) * gr->n_pts);
+    const size_t o_end = o_rprm + al(sizeof(double) * SDE_MAX_PARAMS * W);
     D->host_tables.resize(o_end);
     char *H = D->host_tables.data();
     R *h_dt = (R *)(H + o_dt), *h_sq = (R *)(H + o_sq), *h_x0 = (R *)(H + o_x0), *h_prm = (R *)(H + o_prm);
@@ -375,6 +380,9 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
             }
     }
 
+    memcpy(H + o_rtt, gr->tt, sizeof(double) * gr->n_pts);
+    memcpy(H + o_rprm, s->params, sizeof(double) * SDE_MAX_PARAMS * W);
+
     FwdArgs<R> a;
     memset(&a, 0, sizeof a);
     if (s->corr) {
@@ -410,6 +418,18 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     a.thr = (const long long *)(T + o_thr);
     a.x0 = (const R *)(T + o_x0);
     a.prm = (const R *)(T + o_prm);
+    a.coef = nullptr;
+    if (tab && n_steps > 0) {
+        const int64_t n = (int64_t)n_steps * s->groups * tmaxm;
+        void *p;
+        if ((rc = scratch(D, S_COEF, sizeof(float) * 3 * n, &p))) return rc;
+        coef_table_kernel<<<(unsigned)((n + BLOCK - 1) / BLOCK), BLOCK, 0, st>>>(
+            (const double *)(T + o_rtt), n_steps, (const double *)(T + o_rprm), s->groups, M, tmaxm, s->model,
+            (float *)p);
+        CU(cudaGetLastError());
+        a.coef = (const float *)p;
+    }
+    a.key = philox_schedule(s->seed);
     a.n_out_vars = n_out;
 
     // ---- injected noise ---------------------------------------------------------
@@ -580,6 +600,7 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     }
     if (herr & ERRF_JUMP_CAP) return fail(SDE_ERR_DEVICE, "more than %d jumps in one step", SDE_MAX_JUMPS_PER_STEP);
     if (herr & ERRF_RANGE) return fail(SDE_ERR_INVALID, "autodetected range of the histogram is not finite");
+    if (herr & ERRF_ARGS) return fail(SDE_ERR_DEVICE, "kernel launched without its coefficient table");
     return SDE_OK;
 }
 
@@ -841,6 +862,7 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     a.jump_law = s->jump_law;
     a.seed = s->seed;
     a.stream = s->stream;
+    a.key = philox_schedule(s->seed);
     a.dt = (const R *)(T + o_dt);
     a.sqdt = (const R *)(T + o_sq);
     a.x0 = (const R *)(T + o_x0);

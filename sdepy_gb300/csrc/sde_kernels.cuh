@@ -27,6 +27,7 @@ constexpr int NPART = 8 + SDE_MAX_STRIKES;  // n, mean, M2, M3, M4, min, max, -,
 
 // error flags (bitwise) reported by kernels
 constexpr int ERRF_JUMP_CAP = 1;
+constexpr int ERRF_ARGS = 4;  // a kernel was launched without a table it needs
 
 template <typename R>
 struct FwdArgs {
@@ -36,6 +37,7 @@ struct FwdArgs {
     int32_t jump_law, out_mode, opg, has_corr;
     uint64_t seed;
     uint32_t stream;
+    PhiloxKey key;  // round keys of seed
     R sgn;  // sign of dt on this leg (+1 forward, -1 backward)
     // per-step tables
     const R *dt, *sqdt;
@@ -44,6 +46,11 @@ struct FwdArgs {
     const long long *thr;
     // per-variable inputs
     const R *x0, *prm;  // prm[p*W + w]
+    // FP32 LINEAR / OU with device RNG: per-step coefficients
+    // [steps][groups][3][MAXM] = (d, b, c), rows padded to the kernel's MAXM with x' = a x + b + c (L z) (+ jumps):
+    // OU a = 1 - k dt, b = k theta dt, c = sigma sqrt|dt|; LINEAR a = 1,
+    // b = c_dt dt, c = c_dw sqrt|dt|  (evaluated in FP64 on the host)
+    const float *coef;
     R chol[NCHOL];      // packed lower triangle, row m at m*(m+1)/2
     // injected increments (FP64, device)
     const double *dw, *dj;
@@ -299,7 +306,7 @@ struct NoiseShape {
 // Philox words of step k: u[0 .. 2P) feed the Box-Muller pairs, u[2P + m]
 // is the Poisson uniform of state m (jump models)
 template <int MAXM, bool JUMPS>
-__device__ __forceinline__ void step_words(PhiloxKey key, uint32_t p, uint32_t c1w, uint32_t g,
+__device__ __forceinline__ void step_words(const PhiloxKey &key, uint32_t p, uint32_t c1w, uint32_t g,
                                            uint32_t stream, int NC,
                                            uint32_t (&u)[4 * NoiseShape<MAXM, JUMPS>::NCMAX]) {
     constexpr int NCMAX = NoiseShape<MAXM, JUMPS>::NCMAX;
@@ -348,6 +355,46 @@ __device__ __forceinline__ void correlate(const R *chol, bool has_corr, const R 
     }
 }
 
+// Same increments as step_words + words_to_normals + correlate, produced one
+// Philox call (4 normals) at a time so that only 4 normals are live; the
+// mat-vec accumulates in the same order (j ascending), so FP64 rounding is
+// identical.  Used by the kernels without jumps.
+template <typename R, int MAXM>
+__device__ __forceinline__ void step_increments(const PhiloxKey &key, uint32_t p, uint32_t c1w, uint32_t g,
+                                                uint32_t stream, int NC, const R *chol, bool has_corr,
+                                                R sq, R (&dW)[MAXM]) {
+    typedef Ar<R> A;
+    constexpr int NCN = (MAXM + 3) / 4;  // calls carrying normals
+#pragma unroll
+    for (int c = 0; c < NCN; ++c) {
+        if (c < NC) {
+            const uint4 r = philox4x32_10(make_uint4(p, c1w, (g << 8) | (uint32_t)c, stream), key);
+            R zc[4];
+            Rng<R>::normal2(r.x, r.y, zc[0], zc[1]);
+            Rng<R>::normal2(r.z, r.w, zc[2], zc[3]);
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                const int j = 4 * c + l;
+                if (j < MAXM) {
+                    if (has_corr) {
+#pragma unroll
+                        for (int m = 0; m < MAXM; ++m) {
+                            if (m >= j) {
+                                const R t = A::mul(chol[m * (m + 1) / 2 + j], zc[l]);
+                                dW[m] = (j == 0) ? t : A::add(dW[m], t);
+                            }
+                        }
+                    } else {
+                        dW[j] = zc[l];
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < MAXM; ++m) dW[m] = A::mul(dW[m], sq);
+}
+
 template <int NW>
 __device__ __forceinline__ uint32_t pick_word(const uint32_t (&u)[NW], int idx) {
     uint32_t word = u[0];
@@ -393,13 +440,22 @@ __device__ __forceinline__ void jump_size_grad(int law, uint4 r, R ja, R jb, R j
 // ---------------------------------------------------------------------------
 // the forward kernel
 // ---------------------------------------------------------------------------
+// FP32 device-RNG kernels without jumps, up to 8 states per thread, are
+// held to 80 registers: 3 resident blocks (24 warps) per SM
+template <typename R, int MAXM, bool INJECT, bool JUMPS>
+struct FwdOccupancy {
+    static constexpr int MIN_BLOCKS = (sizeof(R) == 4 && MAXM <= 8 && !INJECT && !JUMPS) ? 3 : 1;
+};
+
 template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS>
-__global__ void __launch_bounds__(BLOCK)
+__global__ void __launch_bounds__(BLOCK, (FwdOccupancy<R, MAXM, INJECT, JUMPS>::MIN_BLOCKS))
 sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     typedef Ar<R> A;
     constexpr int NCMAX = NoiseShape<MAXM, JUMPS>::NCMAX;
+    constexpr bool TAB = sizeof(R) == 4 && MODEL != SDE_MODEL_HESTON && !INJECT;
     __shared__ R red[BLOCK / 32];
     __shared__ double part[MAXM][NPART];
+    __shared__ R svs[MAXM][BLOCK];   // this round's value of each output at the stats row
 
     const int g = blockIdx.y;
     const int M = a.M;
@@ -408,7 +464,11 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     const int NC = (2 * P + (JUMPS ? M : 0) + 3) >> 2;
     const int n_steps = a.n_pts - 1;
     const bool do_stats = a.partials != nullptr;
-    const PhiloxKey key = {(uint32_t)a.seed, (uint32_t)(a.seed >> 32)};
+    const PhiloxKey key = a.key;  // by value: uniform registers, not indexed parameter loads
+    if (TAB && a.coef == nullptr) {  // uniform: the whole grid returns
+        if (threadIdx.x == 0 && blockIdx.x == 0 && blockIdx.y == 0) atomicOr(a.err, ERRF_ARGS);
+        return;
+    }
 
     // this group's coefficients, in registers
     R x0[MAXM], c0[MAXM], c1[MAXM], c2[MAXM], c3[MAXM], c4[MAXM], c5[MAXM];
@@ -434,9 +494,10 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     for (int64_t rd = 0; rd < rounds; ++rd) {
         const int64_t p = rd * stride + (int64_t)blockIdx.x * BLOCK + threadIdx.x;
         const bool act = p < a.paths;
-        R sv[MAXM];
+        if (do_stats) {
 #pragma unroll
-        for (int m = 0; m < MAXM; ++m) sv[m] = R(0);
+            for (int m = 0; m < MAXM; ++m) svs[m][threadIdx.x] = R(0);
+        }
         if (act) {
             R st[MAXM];
 #pragma unroll
@@ -459,7 +520,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                 }
                 if (row == a.stats_row) {
 #pragma unroll
-                    for (int m = 0; m < MAXM; ++m) sv[m] = ov[m];
+                    for (int m = 0; m < MAXM; ++m) svs[m][threadIdx.x] = ov[m];
                     if (a.stats_vals) {
 #pragma unroll
                         for (int m = 0; m < MAXM; ++m)
@@ -477,6 +538,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                 const int r0 = a.out_row[0];
                 if (r0 >= 0) store(r0);
             }
+#pragma unroll 1
             for (int k = 0; k < n_steps; ++k) {
                 const R dt = a.dt[k];
                 const R sq = a.sqdt[k];
@@ -504,10 +566,16 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                 } else {
                     const uint32_t c1w = (uint32_t)k + a.step_offset;
                     uint32_t u[4 * NCMAX];
-                    step_words<MAXM, JUMPS>(key, (uint32_t)p, c1w, (uint32_t)g, a.stream, NC, u);
-                    R z[MAXM];
-                    words_to_normals<R, MAXM>(u, z);
-                    correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
+                    if (JUMPS) {
+                        step_words<MAXM, JUMPS>(key, (uint32_t)p, c1w, (uint32_t)g, a.stream, NC, u);
+                        R z[MAXM];
+                        words_to_normals<R, MAXM>(u, z);
+                        correlate<R, MAXM>(a.chol, a.has_corr, z, TAB ? R(1) : sq, dW);
+                    } else {
+                        // with the coefficient table sqrt|dt| is folded into c
+                        step_increments<R, MAXM>(key, (uint32_t)p, c1w, (uint32_t)g, a.stream, NC, a.chol,
+                                                 a.has_corr, TAB ? R(1) : sq, dW);
+                    }
                     if (JUMPS) {
 #pragma unroll
                         for (int m = 0; m < MAXM; ++m) {
@@ -537,7 +605,37 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                 }
 
                 // ---- Euler step -------------------------------------------------
-                if (MODEL == SDE_MODEL_LINEAR) {
+                if constexpr (TAB) {
+                    float ca[MAXM], cb[MAXM], cc[MAXM];
+                    // rows padded to MAXM (d = b = c = 0 beyond M)
+                    const float *tb = a.coef + ((int64_t)k * a.groups + g) * 3 * MAXM;
+                    if constexpr (MAXM % 4 == 0) {
+#pragma unroll
+                        for (int q = 0; q < MAXM / 4; ++q) {
+                            const float4 va = __ldg(reinterpret_cast<const float4 *>(tb) + q);
+                            const float4 vb = __ldg(reinterpret_cast<const float4 *>(tb + MAXM) + q);
+                            const float4 vc = __ldg(reinterpret_cast<const float4 *>(tb + 2 * MAXM) + q);
+                            ca[4 * q] = va.x; ca[4 * q + 1] = va.y; ca[4 * q + 2] = va.z; ca[4 * q + 3] = va.w;
+                            cb[4 * q] = vb.x; cb[4 * q + 1] = vb.y; cb[4 * q + 2] = vb.z; cb[4 * q + 3] = vb.w;
+                            cc[4 * q] = vc.x; cc[4 * q + 1] = vc.y; cc[4 * q + 2] = vc.z; cc[4 * q + 3] = vc.w;
+                        }
+                    } else {
+#pragma unroll
+                        for (int m = 0; m < MAXM; ++m) {
+                            ca[m] = __ldg(tb + m);
+                            cb[m] = __ldg(tb + MAXM + m);
+                            cc[m] = __ldg(tb + 2 * MAXM + m);
+                        }
+                    }
+#pragma unroll
+                    for (int m = 0; m < MAXM; ++m) {
+                        const float xs = (float)st[m];
+                        float x = xs + fmaf(-ca[m], xs, cb[m]);
+                        x = fmaf(cc[m], (float)dW[m], x);
+                        if (JUMPS) x = x + (float)dJ[m];
+                        st[m] = (R)x;
+                    }
+                } else if (MODEL == SDE_MODEL_LINEAR) {
 #pragma unroll
                     for (int m = 0; m < MAXM; ++m) {
                         R inc = A::add(A::mul(c0[m], dt), A::mul(c1[m], dW[m]));
@@ -593,7 +691,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
         if (do_stats) {
 #pragma unroll
             for (int m = 0; m < MAXM; ++m) {
-                if (m < a.opg) block_round_stats<R>(sv[m], act, a.strikes, a.n_strikes, part[m], red);
+                if (m < a.opg) block_round_stats<R>(svs[m][threadIdx.x], act, a.strikes, a.n_strikes, part[m], red);
             }
         }
     }
@@ -604,6 +702,40 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                           (((int64_t)g * gridDim.x + blockIdx.x) * a.opg + threadIdx.x) * NPART;
             for (int i = 0; i < NPART; ++i) dst[i] = part[threadIdx.x][i];
         }
+    }
+}
+
+// per-step coefficients of the FP32 LINEAR / OU kernels, [steps][groups][3][MAXM]
+// (see FwdArgs::coef), from the FP64 grid and parameters with explicitly
+// rounded FP64 operations
+static __global__ void __launch_bounds__(BLOCK)
+coef_table_kernel(const double *tt, int n_steps, const double *prm, int groups, int M, int maxm,
+                  int model, float *coef) {
+    const int64_t i = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+    const int64_t n = (int64_t)n_steps * groups * maxm;
+    if (i >= n) return;
+    const int m = (int)(i % maxm);
+    const int64_t kg = i / maxm;
+    const int g = (int)(kg % groups);
+    const int k = (int)(kg / groups);
+    float *t = coef + kg * 3 * maxm;
+    if (m >= M) {
+        t[m] = 0.0f;
+        t[maxm + m] = 0.0f;
+        t[2 * maxm + m] = 0.0f;
+        return;
+    }
+    const int W = groups * M, w = g * M + m;
+    const double dt = __dsub_rn(tt[k + 1], tt[k]);
+    const double sq = __dsqrt_rn(fabs(dt));
+    if (model == SDE_MODEL_OU) {
+        t[m] = (float)__dmul_rn(prm[w], dt);
+        t[maxm + m] = (float)__dmul_rn(__dmul_rn(prm[w], prm[W + w]), dt);
+        t[2 * maxm + m] = (float)__dmul_rn(prm[2 * W + w], sq);
+    } else {
+        t[m] = 0.0f;
+        t[maxm + m] = (float)__dmul_rn(prm[w], dt);
+        t[2 * maxm + m] = (float)__dmul_rn(prm[W + w], sq);
     }
 }
 

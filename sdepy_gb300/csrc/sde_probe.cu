@@ -10,7 +10,7 @@ using namespace sdegpu;
 
 namespace {
 
-constexpr int PROBE_CHAINS = 8;
+constexpr int PROBE_CHAINS = 16;
 
 __global__ void __launch_bounds__(BLOCK) probe_sfu(float *sink, int iters) {
     float v[PROBE_CHAINS];
@@ -77,7 +77,9 @@ extern "C" int32_t sde_peak_probe(int32_t which, double *ops_per_s) {
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    const int blocks = sms * 8, iters = 4096;
+    // 8 resident blocks of 256 threads per SM, 16 independent chains per
+    // thread: enough operations in flight to cover the SFU latency
+    const int blocks = sms * 8, iters = 2048;
     auto launch = [&]() {
         if (which == 0) probe_sfu<<<blocks, BLOCK, 0, st>>>((float *)sink, iters);
         else if (which == 1) probe_fma<<<blocks, BLOCK, 0, st>>>((float *)sink, iters);

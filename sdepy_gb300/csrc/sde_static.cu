@@ -91,7 +91,7 @@ __global__ void static_pack_kernel(const double *res, int64_t n_out, int n_strik
 }
 
 struct Layout {
-    size_t tt, row, x0, prm, dt, sq, x0r, prmr, part, res, edges, edges64, counts, vals, mom, pay, err, end;
+    size_t tt, row, x0, prm, dt, sq, x0r, prmr, coef, part, res, edges, edges64, counts, vals, mom, pay, err, end;
 };
 
 size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -192,6 +192,8 @@ int run_static(const SdeSpec *s, const SdeGrid *gr, const SdeStatsReq *req, SdeS
     lo.sq = o; o = al256(o + sizeof(R) * (n_steps + 1));
     lo.x0r = o; o = al256(o + sizeof(R) * W);
     lo.prmr = o; o = al256(o + sizeof(R) * SDE_MAX_PARAMS * W);
+    const bool tab = sizeof(R) == 4 && s->model != SDE_MODEL_HESTON;
+    lo.coef = o; o = al256(o + (tab ? sizeof(float) * 3 * (size_t)n_steps * s->groups * maxm : 0));
     lo.part = o; o = al256(o + sizeof(double) * NPART * (size_t)s->groups * nbx * opg);
     lo.res = o; o = al256(o + sizeof(double) * RES_STRIDE * n_out);
     lo.edges = o; o = al256(o + sizeof(R) * (size_t)(bins + 1) * n_out);
@@ -247,6 +249,17 @@ int run_static(const SdeSpec *s, const SdeGrid *gr, const SdeStatsReq *req, SdeS
     a.out_row = (const int32_t *)(base + lo.row);
     a.x0 = (const R *)(base + lo.x0r);
     a.prm = (const R *)(base + lo.prmr);
+    a.key = philox_schedule(s->seed);
+    a.coef = nullptr;
+    if (tab && n_steps > 0) {
+        // the FP32 LINEAR / OU kernels read their per-step coefficients
+        const int64_t n = (int64_t)n_steps * s->groups * maxm;
+        coef_table_kernel<<<(unsigned)((n + BLOCK - 1) / BLOCK), BLOCK, 0, st>>>(
+            (const double *)(base + lo.tt), n_steps, (const double *)(base + lo.prm), s->groups, M, maxm,
+            s->model, (float *)(base + lo.coef));
+        CUS(cudaGetLastError());
+        a.coef = (const float *)(base + lo.coef);
+    }
     a.n_out_vars = n_out;
     a.stats_row = req->row;
     a.n_strikes = req->n_strikes;
