@@ -337,6 +337,7 @@ def extra_configs(lib):
         _lib.check(lib.sde_run_stats(C.byref(spec), C.byref(g), None, C.byref(o), C.byref(req), C.byref(so)), 'fwd')
         return arrs, leg
 
+    import time
     # ---- Heston, 2^22 paths, 499 steps on (0, 2)
     tl = (0., 2.)
     H = sg.heston_process(paths=2**22, steps=500, dtype=np.float32, **HESTON)
@@ -382,6 +383,36 @@ def extra_configs(lib):
         J = cls(paths=2**22, steps=365, dtype=np.float32, **kw)
         ms = _time_call(lambda: fused(J, (0., 1.), [1.], 4), lib)
         out[name + '_configs3'] = {'fp32_path_steps_per_s': 2**22*364/(ms*1e-3), 'kernel_ms': ms}
+    # ---- configs[4]: 4096 heterogeneous instances, one persistent launch
+    from sdepy_gb300.batch import batch, synthetic_instances, run_single
+    insts = synthetic_instances(4096, seed=1)
+    t0 = time.perf_counter()
+    B = batch(insts)                          # autotuned slab, CUDA graph
+    tune_s = time.perf_counter() - t0
+    B.run()
+    wall = []
+    dev = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        r = B.run()
+        wall.append(time.perf_counter() - t0)
+        dev.append(B.last_ms)
+    t0 = time.perf_counter()
+    for s_ in insts:
+        run_single(s_)
+    loop_s = time.perf_counter() - t0
+    ps = B.path_steps
+    out['batch_configs4'] = {
+        'instances': len(insts), 'path_steps': ps, 'work_items': B.items,
+        'slab': B.slab, 'autotune_ms': {str(k): v for k, v in (B.tuning or {}).items()},
+        'autotune_s': tune_s, 'batch_device_ms': float(np.median(dev)),
+        'batch_wall_ms': float(np.median(wall))*1e3,
+        'batch_path_steps_per_s': ps/np.median(wall),
+        'loop_wall_ms': loop_s*1e3, 'loop_path_steps_per_s': ps/loop_s,
+        'batch_over_loop': loop_s/np.median(wall),
+        'note': 'batch also computes 8 pathwise derivatives per instance; the loop '
+                'runs the forward summary only'}
+    B.close()
     # ---- lognormal configs[0]: FP64, 1e5 paths, 502 steps, all 253 rows written (host output)
     import time
     Ln = sg.lognorm_process(x0=1., mu=.05, sigma=.2, paths=100000, steps=252, rng=sg.philox_rng(0))

@@ -249,6 +249,50 @@ SDE_API int32_t sde_run_stats_static(const SdeSpec *spec, const SdeGrid *grid,
                                      const SdeStatsReq *req, SdeStatsOut *stats,
                                      void *stream);
 
+/* ---- batched instances ---------------------------------------------------- */
+
+/* One SDE instance of a batch: `paths` paths on `n_steps` equal Euler steps
+ * of [0, T] (device Philox noise with the counter layout of sde_run). */
+typedef struct SdeBatchInstance {
+    int32_t model;          /* SDE_MODEL_LINEAR | SDE_MODEL_OU | SDE_MODEL_HESTON      */
+    int32_t jump_law;       /* SDE_JUMP_NONE, or SDE_JUMP_NORM with the LINEAR model   */
+    int32_t nvars;          /* states: 1 (LINEAR), 1..4 (OU), 2 (HESTON)               */
+    int32_t n_steps;
+    int64_t paths;
+    double T;
+    double x0[4];           /* initial states, integration variable                    */
+    double params[6][4];    /* as SdeSpec.params, per state                            */
+    double rho;             /* HESTON: correlation of the two increments               */
+    uint64_t seed;          /* Philox key                                              */
+    uint32_t stream;        /* Philox counter word 3                                   */
+    int32_t out_exp;        /* 1: X = exp(state) (log models)                          */
+} SdeBatchInstance;
+
+/* Build a batch plan: the instances split into work items of `slab` paths
+ * (a multiple of 32), sorted longest first, and the device arrays of one
+ * persistent launch.  *handle identifies the plan.  Replaces looping the
+ * single-instance call over instances; no counterpart in the reference,
+ * which integrates one process per call (sdepy/integration.py:476). */
+SDE_API int32_t sde_batch_create(const SdeBatchInstance *inst, int32_t n,
+                                 int32_t slab, int32_t *handle);
+
+/* Run a plan: one persistent launch in which every warp takes work items
+ * from an atomic queue, then a fixed-order merge per instance; with
+ * use_graph the two launches are captured once into a CUDA graph and the
+ * graph is relaunched.  results (host, may be NULL) is [n][11]: paths, mean
+ * and std of X(T) of the first state, and 8 pathwise derivatives of the
+ * mean of X(T) (tangent mode): LINEAR d/d(x0, c_dt, c_dw, -, jump a,
+ * jump b), OU d/d(x0, k, theta, sigma), HESTON d/d(x0, mu, sigma, y0, k,
+ * theta, xi, rho), x0 in the integration variable.  ms: device time.
+ * Runs of the same plan must not overlap. */
+SDE_API int32_t sde_batch_run(int32_t handle, int32_t use_graph,
+                              double *results, double *ms);
+
+/* info[4] = instances, work items, slab, persistent blocks */
+SDE_API int32_t sde_batch_info(int32_t handle, int32_t *info);
+
+SDE_API int32_t sde_batch_destroy(int32_t handle);
+
 /* montecarlo summary of an existing sample [n_vars][paths] (f64 if
  * is_fp32 == 0, else f32; host or device per on_device).
  * Replaces montecarlo._update_moments / _update_histogram

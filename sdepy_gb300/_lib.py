@@ -76,6 +76,15 @@ class SdeAdjReq(C.Structure):
                 ('mean_weight', C.c_double)]
 
 
+class SdeBatchInstance(C.Structure):
+    _fields_ = [('model', C.c_int32), ('jump_law', C.c_int32),
+                ('nvars', C.c_int32), ('n_steps', C.c_int32),
+                ('paths', C.c_int64), ('T', C.c_double),
+                ('x0', C.c_double*4), ('params', (C.c_double*4)*6),
+                ('rho', C.c_double), ('seed', C.c_uint64),
+                ('stream', C.c_uint32), ('out_exp', C.c_int32)]
+
+
 # every symbol include/sdepy_gb300.h declares, with its ctypes signature
 SIGNATURES = {
     'sde_abi_version': (C.c_int32, []),
@@ -97,6 +106,11 @@ SIGNATURES = {
     'sde_run_stats_static': (C.c_int32, [C.POINTER(SdeSpec), C.POINTER(SdeGrid),
                                          C.POINTER(SdeStatsReq),
                                          C.POINTER(SdeStatsOut), C.c_void_p]),
+    'sde_batch_create': (C.c_int32, [C.POINTER(SdeBatchInstance), C.c_int32,
+                                     C.c_int32, _ip]),
+    'sde_batch_run': (C.c_int32, [C.c_int32, C.c_int32, _dp, _dp]),
+    'sde_batch_info': (C.c_int32, [C.c_int32, _ip]),
+    'sde_batch_destroy': (C.c_int32, [C.c_int32]),
     'sde_sample_stats': (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32,
                                      C.c_int64, C.c_int64,
                                      C.POINTER(SdeStatsReq),

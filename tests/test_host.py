@@ -157,3 +157,18 @@ def test_library_host_cholesky_without_gpu():
     bad = np.array([[1., 2.], [2., 1.]])
     assert lib.sde_cholesky(_lib.dptr(bad), 2, _lib.dptr(L)) == _lib.ERR_INVALID
     assert 'semi-definite' in _lib.last_error()
+
+
+def test_synthetic_batch_workload():
+    from sdepy_gb300.batch import synthetic_instances, LINEAR, OU, HESTON
+    insts = synthetic_instances(400, seed=2)
+    models = [s.model for s in insts]
+    assert {LINEAR, OU, HESTON} <= set(models)
+    steps = np.array([s.n_steps for s in insts])
+    paths = np.array([s.paths for s in insts])
+    assert steps.min() >= 50 and steps.max() <= 2000
+    assert paths.min() >= 1000 and paths.max() <= 256000
+    assert any(s.jump_law == _lib.JUMP_NORM for s in insts)
+    ou = [s for s in insts if s.model == OU]
+    assert {s.nvars for s in ou} == {1, 2, 3, 4}
+    assert all(s.nvars == 2 and -.9 <= s.rho <= -.5 for s in insts if s.model == HESTON)
