@@ -490,6 +490,49 @@ def run_reference(args):
     print(json.dumps(res))
 
 
+def run_case(args):
+    """Small single-kernel cases for profiling captures: 'heston_adjoint'
+    (configs[2] model, 2^18 paths, 499 steps: forward summary then adjoint),
+    'batch' (256 instances of the heterogeneous workload, paths <= 65536)."""
+    import ctypes as C
+    import sdepy_gb300 as sg
+    from sdepy_gb300 import _lib
+    from sdepy_gb300.grid import Grid
+    lib = _lib.load()
+    lib.sde_timing(1, None)
+    last = (C.c_double*4)()
+    if args.case == 'heston_adjoint':
+        H = sg.heston_process(paths=2**18, steps=500, dtype=np.float32, **HESTON)
+        leg = Grid((0., 2.), 500).legs[-1]
+        g = _lib.SdeGrid()
+        g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
+        g.n_pts, g.step_offset = leg.tt.size, 0
+        req = _lib.SdeAdjReq()
+        req.n_strikes, req.mean_weight = 5, 0.
+        for i, K in enumerate(STRIKES):
+            req.strikes[i], req.weights[i] = K, .2
+        grad = np.zeros((2, 8))
+        v = C.c_double()
+        ms = []
+        for i in range(args.warmup + args.steps):
+            spec = H._make_spec(3, i)
+            _lib.check(lib.sde_adjoint(C.byref(spec), C.byref(g), C.byref(req), _lib.dptr(grad), C.byref(v)), 'adj')
+            lib.sde_timing(-1, last)
+            ms.append(last[0])
+        print(json.dumps({'case': args.case, 'adjoint_ms': float(np.median(ms[args.warmup:])),
+                          'value': float(v.value)}))
+    elif args.case == 'batch':
+        from sdepy_gb300.batch import batch, synthetic_instances
+        insts = synthetic_instances(256, seed=1)
+        for s_ in insts:
+            s_.paths = min(s_.paths, 65536)
+        B = batch(insts, slab=1024, use_graph=False)
+        for i in range(args.warmup + args.steps):
+            B.run()
+        print(json.dumps({'case': args.case, 'batch_ms': B.last_ms, 'path_steps': B.path_steps}))
+        B.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -500,7 +543,12 @@ def main():
                     help='paths per step (profiling captures use fewer)')
     ap.add_argument('--quick', action='store_true',
                     help='timed steps only: no FP64 / e2e / CPU / probe extras')
+    ap.add_argument('--case', default=None, choices=['heston_adjoint', 'batch'],
+                    help='run one small single-kernel case (profiling)')
     args = ap.parse_args()
+    if args.case:
+        run_case(args)
+        return
     if args.impl == 'reference':
         run_reference(args)
     else:
