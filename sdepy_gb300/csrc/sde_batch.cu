@@ -81,12 +81,13 @@ __device__ __forceinline__ void kahan(float &s, float &c, float v) {
 }
 
 // integrate one path of instance I; returns X(T) and its derivatives
-__device__ __forceinline__ float path_lin(const DevInst &I, uint32_t p, float (&g)[NB_GRAD], int32_t *err) {
+__device__ __forceinline__ float path_lin(const DevInst &I, const PhiloxKey &key, uint32_t p, float (&g)[NB_GRAD],
+                                          int32_t *err) {
     float a = I.x0[0], sdw = 0.f, sja = 0.f, sjb = 0.f;
     const bool jumps = I.jump_law != SDE_JUMP_NONE;
 #pragma unroll 1
     for (int k = 0; k < I.n_steps; ++k) {
-        const uint4 r = philox4x32_10(make_uint4(p, (uint32_t)k, 0u, I.stream), I.key);
+        const uint4 r = philox4x32_10(make_uint4(p, (uint32_t)k, 0u, I.stream), key);
         float z0, z1;
         Rng<float>::normal2(r.x, r.y, z0, z1);
         a = a + I.b[0] + I.c[0] * z0;
@@ -94,7 +95,7 @@ __device__ __forceinline__ float path_lin(const DevInst &I, uint32_t p, float (&
         if (jumps && (long long)r.z > I.thr) {
             const int cnt = poisson_tail(r.z, I.p0d, I.lamdt, err);
             for (int j = 0; j < cnt; ++j) {
-                const uint4 q = philox4x32_10(make_uint4(p, (uint32_t)k, 0x80000000u | (uint32_t)j, I.stream), I.key);
+                const uint4 q = philox4x32_10(make_uint4(p, (uint32_t)k, 0x80000000u | (uint32_t)j, I.stream), key);
                 float y0, y1;
                 Rng<float>::normal2(q.x, q.y, y0, y1);
                 a += I.ja + I.jb * y0;
@@ -115,7 +116,7 @@ __device__ __forceinline__ float path_lin(const DevInst &I, uint32_t p, float (&
     return X;
 }
 
-__device__ __forceinline__ float path_ou(const DevInst &I, uint32_t p, float (&g)[NB_GRAD]) {
+__device__ __forceinline__ float path_ou(const DevInst &I, const PhiloxKey &key, uint32_t p, float (&g)[NB_GRAD]) {
     float x[4];
 #pragma unroll
     for (int m = 0; m < 4; ++m) x[m] = I.x0[m];
@@ -126,7 +127,7 @@ __device__ __forceinline__ float path_ou(const DevInst &I, uint32_t p, float (&g
     const int W = I.nvars;
 #pragma unroll 1
     for (int k = 0; k < I.n_steps; ++k) {
-        const uint4 r = philox4x32_10(make_uint4(p, (uint32_t)k, 0u, I.stream), I.key);
+        const uint4 r = philox4x32_10(make_uint4(p, (uint32_t)k, 0u, I.stream), key);
         float z[4];
         Rng<float>::normal2(r.x, r.y, z[0], z[1]);
         if (W > 2) Rng<float>::normal2(r.z, r.w, z[2], z[3]);
@@ -148,7 +149,8 @@ __device__ __forceinline__ float path_ou(const DevInst &I, uint32_t p, float (&g
     return x[0];
 }
 
-__device__ __forceinline__ float path_heston(const DevInst &I, uint32_t p, float (&g)[NB_GRAD]) {
+__device__ __forceinline__ float path_heston(const DevInst &I, const PhiloxKey &key, uint32_t p,
+                                             float (&g)[NB_GRAD]) {
     float a = I.x0[0], y = I.x0[1];
     // tangents (d a, d y) w.r.t. [x0, mu, sigma, y0, k, theta, xi, rho]
     float ta[NB_GRAD], ty[NB_GRAD];
@@ -160,7 +162,7 @@ __device__ __forceinline__ float path_heston(const DevInst &I, uint32_t p, float
     const float dt = I.dt, sq = I.sq;
 #pragma unroll 1
     for (int k = 0; k < I.n_steps; ++k) {
-        const uint4 r = philox4x32_10(make_uint4(p, (uint32_t)k, 0u, I.stream), I.key);
+        const uint4 r = philox4x32_10(make_uint4(p, (uint32_t)k, 0u, I.stream), key);
         float z0, z1;
         Rng<float>::normal2(r.x, r.y, z0, z1);
         const float dW1 = z0 * sq;
@@ -209,6 +211,7 @@ batch_kernel(const DevInst *insts, const Item *items, int n_items, unsigned int 
         if (it >= n_items) return;
         const Item item = items[it];
         const DevInst &I = insts[item.inst];
+        const PhiloxKey key = I.key;  // in registers for the whole item
         // per lane: Welford of X, Kahan sums of the derivatives
         float n = 0.f, mean = 0.f, m2 = 0.f;
         float gs[NB_GRAD], gc[NB_GRAD];
@@ -218,9 +221,9 @@ batch_kernel(const DevInst *insts, const Item *items, int n_items, unsigned int 
             const uint32_t p = (uint32_t)(item.base + q);
             float g[NB_GRAD];
             float X;
-            if (I.model == SDE_MODEL_LINEAR) X = path_lin(I, p, g, err);
-            else if (I.model == SDE_MODEL_OU) X = path_ou(I, p, g);
-            else X = path_heston(I, p, g);
+            if (I.model == SDE_MODEL_LINEAR) X = path_lin(I, key, p, g, err);
+            else if (I.model == SDE_MODEL_OU) X = path_ou(I, key, p, g);
+            else X = path_heston(I, key, p, g);
             n += 1.f;
             const float dd = X - mean;
             mean += dd / n;

@@ -516,7 +516,9 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
 #pragma unroll
                     for (int m = 0; m < MAXM; ++m)
                         if (m < no)
-                            a.xx[((int64_t)row * a.n_out_vars + (int64_t)g * a.opg + m) * a.paths + p] = ov[m];
+                            // streaming store: the path output must not evict
+                            // the per-step tables from L2
+                            __stcs(&a.xx[((int64_t)row * a.n_out_vars + (int64_t)g * a.opg + m) * a.paths + p], ov[m]);
                 }
                 if (row == a.stats_row) {
 #pragma unroll
@@ -525,7 +527,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
 #pragma unroll
                         for (int m = 0; m < MAXM; ++m)
                             if (m < no)
-                                a.stats_vals[((int64_t)g * a.opg + m) * a.paths + p] = ov[m];
+                                __stcs(&a.stats_vals[((int64_t)g * a.opg + m) * a.paths + p], ov[m]);
                     }
                 }
                 if (JUMPS && a.row_jumps) {
