@@ -465,7 +465,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     const int n_steps = a.n_pts - 1;
     const bool do_stats = a.partials != nullptr;
     const PhiloxKey key = a.key;  // by value: uniform registers, not indexed parameter loads
-    if (TAB && a.coef == nullptr) {  // uniform: the whole grid returns
+    if (TAB && a.coef == nullptr && n_steps > 0) {  // uniform: the whole grid returns
         if (threadIdx.x == 0 && blockIdx.x == 0 && blockIdx.y == 0) atomicOr(a.err, ERRF_ARGS);
         return;
     }
