@@ -334,10 +334,62 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     const size_t o_thr = o_p0 + al(sizeof(double) * njt);
     const bool tab = sizeof(R) == 4 && !inject && s->model != SDE_MODEL_HESTON;
     const int tmaxm = maxm_of(M);
-    // raw FP64 grid and coefficients for the device-built coefficient table
-    const size_t o_rtt = o_thr + al(sizeof(long long) * njt);
-    const size_t o_rprm = o_rtt + al(sizeof(double) * gr->n_pts);
-    const size_t o_end = o_rprm + al(sizeof(double) * SDE_MAX_PARAMS * W);
+    // FP32 LINEAR / OU: the grid as runs of steps with one coefficient row
+    // each, and the compact table of those rows (see FwdArgs::coef / runs)
+    std::vector<int4> runs;
+    std::vector<float> ctab;
+    if (tab && n_steps > 0) {
+        const size_t rowlen = (size_t)s->groups * 3 * tmaxm;
+        std::vector<float> cur(rowlen), nxt(rowlen);
+        const double *P0 = s->params, *P1 = s->params + W, *P2 = s->params + 2 * W;
+        auto coef_row = [&](int k, float *t) {
+            const double dt = gr->tt[k + 1] - gr->tt[k], sq = sqrt(fabs(dt));
+            for (int g = 0; g < s->groups; ++g) {
+                float *r = t + (size_t)g * 3 * tmaxm;
+                for (int m = 0; m < tmaxm; ++m) {
+                    if (m >= M) {
+                        r[m] = r[tmaxm + m] = r[2 * tmaxm + m] = 0.0f;
+                        continue;
+                    }
+                    const int w = g * M + m;
+                    if (s->model == SDE_MODEL_OU) {
+                        r[m] = (float)(P0[w] * dt);
+                        r[tmaxm + m] = (float)((P0[w] * P1[w]) * dt);
+                        r[2 * tmaxm + m] = (float)(P2[w] * sq);
+                    } else {
+                        r[m] = 0.0f;
+                        r[tmaxm + m] = (float)(P0[w] * dt);
+                        r[2 * tmaxm + m] = (float)(P1[w] * sq);
+                    }
+                }
+            }
+        };
+        int k = 0;
+        while (k < n_steps) {
+            coef_row(k, cur.data());
+            const size_t nrows = ctab.size() / rowlen;
+            int ci;
+            if (nrows > 0 && memcmp(ctab.data() + (nrows - 1) * rowlen, cur.data(), rowlen * sizeof(float)) == 0) {
+                ci = (int)nrows - 1;
+            } else {
+                ctab.insert(ctab.end(), cur.begin(), cur.end());
+                ci = (int)nrows;
+            }
+            const int k0 = k;
+            int row = -1;
+            for (;;) {
+                ++k;
+                if (gr->out_row[k] >= 0) { row = gr->out_row[k]; break; }
+                if (k == n_steps) break;
+                coef_row(k, nxt.data());
+                if (memcmp(nxt.data(), cur.data(), rowlen * sizeof(float)) != 0) break;
+            }
+            runs.push_back(make_int4(k0, k, row, ci));
+        }
+    }
+    const size_t o_runs = o_thr + al(sizeof(long long) * njt);
+    const size_t o_ctab = o_runs + al(sizeof(int4) * (runs.size() + 1));
+    const size_t o_end = o_ctab + al(sizeof(float) * (ctab.size() + 4));
     D->host_tables.resize(o_end);
     char *H = D->host_tables.data();
     R *h_dt = (R *)(H + o_dt), *h_sq = (R *)(H + o_sq), *h_x0 = (R *)(H + o_x0), *h_prm = (R *)(H + o_prm);
@@ -380,8 +432,8 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
             }
     }
 
-    memcpy(H + o_rtt, gr->tt, sizeof(double) * gr->n_pts);
-    memcpy(H + o_rprm, s->params, sizeof(double) * SDE_MAX_PARAMS * W);
+    if (!runs.empty()) memcpy(H + o_runs, runs.data(), sizeof(int4) * runs.size());
+    if (!ctab.empty()) memcpy(H + o_ctab, ctab.data(), sizeof(float) * ctab.size());
 
     FwdArgs<R> a;
     memset(&a, 0, sizeof a);
@@ -419,15 +471,11 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     a.x0 = (const R *)(T + o_x0);
     a.prm = (const R *)(T + o_prm);
     a.coef = nullptr;
+    a.runs = nullptr;
     if (tab && n_steps > 0) {
-        const int64_t n = (int64_t)n_steps * s->groups * tmaxm;
-        void *p;
-        if ((rc = scratch(D, S_COEF, sizeof(float) * 3 * n, &p))) return rc;
-        coef_table_kernel<<<(unsigned)((n + BLOCK - 1) / BLOCK), BLOCK, 0, st>>>(
-            (const double *)(T + o_rtt), n_steps, (const double *)(T + o_rprm), s->groups, M, tmaxm, s->model,
-            (float *)p);
-        CU(cudaGetLastError());
-        a.coef = (const float *)p;
+        a.coef = (const float *)(T + o_ctab);
+        a.runs = (const int4 *)(T + o_runs);
+        a.n_runs = (int32_t)runs.size();
     }
     a.key = philox_schedule(s->seed);
     a.n_out_vars = n_out;

@@ -46,11 +46,17 @@ struct FwdArgs {
     const long long *thr;
     // per-variable inputs
     const R *x0, *prm;  // prm[p*W + w]
-    // FP32 LINEAR / OU with device RNG: per-step coefficients
-    // [steps][groups][3][MAXM] = (d, b, c), rows padded to the kernel's MAXM with x' = a x + b + c (L z) (+ jumps):
-    // OU a = 1 - k dt, b = k theta dt, c = sigma sqrt|dt|; LINEAR a = 1,
-    // b = c_dt dt, c = c_dw sqrt|dt|  (evaluated in FP64 on the host)
+    // FP32 LINEAR / OU with device RNG: coefficient rows [row][groups][3][MAXM]
+    // = (d, b, c), padded to the kernel's MAXM, with the update
+    // x' = x + (b - d x) + c (L z) (+ jumps): OU d = k dt, b = k theta dt,
+    // c = sigma sqrt|dt|; LINEAR d = 0, b = c_dt dt, c = c_dw sqrt|dt|
+    // (FP64 products rounded to FP32).  d is kept small (not 1 - k dt) so
+    // that its rounding does not bias the decay over many steps.
     const float *coef;
+    // and the grid as runs of steps sharing one coefficient row:
+    // (first step, end step, output row stored after the run or -1, coef row)
+    const int4 *runs;
+    int32_t n_runs;
     R chol[NCHOL];      // packed lower triangle, row m at m*(m+1)/2
     // injected increments (FP64, device)
     const double *dw, *dj;
@@ -365,6 +371,21 @@ __device__ __forceinline__ void step_increments(const PhiloxKey &key, uint32_t p
                                                 R sq, R (&dW)[MAXM]) {
     typedef Ar<R> A;
     constexpr int NCN = (MAXM + 3) / 4;  // calls carrying normals
+    if (!has_corr) {  // tested once per step, not per normal
+#pragma unroll
+        for (int c = 0; c < NCN; ++c) {
+            if (c < NC) {
+                const uint4 r = philox4x32_10(make_uint4(p, c1w, (g << 8) | (uint32_t)c, stream), key);
+                R zc[4];
+                Rng<R>::normal2(r.x, r.y, zc[0], zc[1]);
+                Rng<R>::normal2(r.z, r.w, zc[2], zc[3]);
+#pragma unroll
+                for (int l = 0; l < 4; ++l)
+                    if (4 * c + l < MAXM) dW[4 * c + l] = A::mul(zc[l], sq);
+            }
+        }
+        return;
+    }
 #pragma unroll
     for (int c = 0; c < NCN; ++c) {
         if (c < NC) {
@@ -376,16 +397,12 @@ __device__ __forceinline__ void step_increments(const PhiloxKey &key, uint32_t p
             for (int l = 0; l < 4; ++l) {
                 const int j = 4 * c + l;
                 if (j < MAXM) {
-                    if (has_corr) {
 #pragma unroll
-                        for (int m = 0; m < MAXM; ++m) {
-                            if (m >= j) {
-                                const R t = A::mul(chol[m * (m + 1) / 2 + j], zc[l]);
-                                dW[m] = (j == 0) ? t : A::add(dW[m], t);
-                            }
+                    for (int m = 0; m < MAXM; ++m) {
+                        if (m >= j) {
+                            const R t = A::mul(chol[m * (m + 1) / 2 + j], zc[l]);
+                            dW[m] = (j == 0) ? t : A::add(dW[m], t);
                         }
-                    } else {
-                        dW[j] = zc[l];
                     }
                 }
             }
@@ -465,7 +482,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     const int n_steps = a.n_pts - 1;
     const bool do_stats = a.partials != nullptr;
     const PhiloxKey key = a.key;  // by value: uniform registers, not indexed parameter loads
-    if (TAB && a.coef == nullptr && n_steps > 0) {  // uniform: the whole grid returns
+    if (TAB && (a.coef == nullptr || a.runs == nullptr) && n_steps > 0) {  // uniform: the grid returns
         if (threadIdx.x == 0 && blockIdx.x == 0 && blockIdx.y == 0) atomicOr(a.err, ERRF_ARGS);
         return;
     }
@@ -540,11 +557,9 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                 const int r0 = a.out_row[0];
                 if (r0 >= 0) store(r0);
             }
-#pragma unroll 1
-            for (int k = 0; k < n_steps; ++k) {
-                const R dt = a.dt[k];
-                const R sq = a.sqdt[k];
-                R dW[MAXM], dJ[MAXM];
+            // increments of step k: injected, or drawn from Philox counters
+            // (normals, correlated; Poisson counts and jump sums)
+            auto draw = [&](int k, R sq, R (&dW)[MAXM], R (&dJ)[MAXM]) {
 #pragma unroll
                 for (int m = 0; m < MAXM; ++m) dJ[m] = R(0);
                 if (INJECT) {
@@ -565,98 +580,115 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                             dW[m] = R(0);
                         }
                     }
-                } else {
-                    const uint32_t c1w = (uint32_t)k + a.step_offset;
-                    uint32_t u[4 * NCMAX];
-                    if (JUMPS) {
-                        step_words<MAXM, JUMPS>(key, (uint32_t)p, c1w, (uint32_t)g, a.stream, NC, u);
-                        R z[MAXM];
-                        words_to_normals<R, MAXM>(u, z);
-                        correlate<R, MAXM>(a.chol, a.has_corr, z, TAB ? R(1) : sq, dW);
-                    } else {
-                        // with the coefficient table sqrt|dt| is folded into c
-                        step_increments<R, MAXM>(key, (uint32_t)p, c1w, (uint32_t)g, a.stream, NC, a.chol,
-                                                 a.has_corr, TAB ? R(1) : sq, dW);
-                    }
-                    if (JUMPS) {
+                    return;
+                }
+                const uint32_t c1w = (uint32_t)k + a.step_offset;
+                if (!JUMPS) {
+                    step_increments<R, MAXM>(key, (uint32_t)p, c1w, (uint32_t)g, a.stream, NC, a.chol,
+                                             a.has_corr, sq, dW);
+                    return;
+                }
+                uint32_t u[4 * NCMAX];
+                step_words<MAXM, JUMPS>(key, (uint32_t)p, c1w, (uint32_t)g, a.stream, NC, u);
+                R z[MAXM];
+                words_to_normals<R, MAXM>(u, z);
+                correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
 #pragma unroll
-                        for (int m = 0; m < MAXM; ++m) {
-                            if (m < M) {
-                                const uint32_t word = pick_word(u, 2 * P + m);
-                                const int w = g * M + m;
-                                const int64_t tix = (int64_t)k * W + w;
-                                if ((long long)word > a.thr[tix]) {
-                                    const int cnt = poisson_tail(word, a.p0[tix], a.lamdt[tix], a.err);
-                                    R S = R(0);
-                                    for (int j = 0; j < cnt; ++j) {
-                                        const uint4 r = philox4x32_10(
-                                            make_uint4((uint32_t)p, c1w,
-                                                       0x80000000u | ((uint32_t)w << 12) | (uint32_t)j,
-                                                       a.stream), key);
-                                        const R y = jump_size<R>(a.jump_law, r, c3[m], c4[m], c5[m]);
-                                        S = (j == 0) ? y : A::add(S, y);
-                                    }
-                                    dJ[m] = A::mul(a.sgn, S);
-                                    const int sc = a.sgn < R(0) ? -cnt : cnt;
-                                    jcnt[m] += sc;
-                                    row_jc += (unsigned int)cnt;
-                                }
+                for (int m = 0; m < MAXM; ++m) {
+                    if (m < M) {
+                        const uint32_t word = pick_word(u, 2 * P + m);
+                        const int w = g * M + m;
+                        const int64_t tix = (int64_t)k * W + w;
+                        if ((long long)word > a.thr[tix]) {
+                            const int cnt = poisson_tail(word, a.p0[tix], a.lamdt[tix], a.err);
+                            R S = R(0);
+                            for (int j = 0; j < cnt; ++j) {
+                                const uint4 r = philox4x32_10(
+                                    make_uint4((uint32_t)p, c1w, 0x80000000u | ((uint32_t)w << 12) | (uint32_t)j,
+                                               a.stream), key);
+                                const R y = jump_size<R>(a.jump_law, r, c3[m], c4[m], c5[m]);
+                                S = (j == 0) ? y : A::add(S, y);
                             }
+                            dJ[m] = A::mul(a.sgn, S);
+                            const int sc = a.sgn < R(0) ? -cnt : cnt;
+                            jcnt[m] += sc;
+                            row_jc += (unsigned int)cnt;
                         }
                     }
                 }
+            };
 
-                // ---- Euler step -------------------------------------------------
-                if constexpr (TAB) {
-                    float ca[MAXM], cb[MAXM], cc[MAXM];
-                    // rows padded to MAXM (d = b = c = 0 beyond M)
-                    const float *tb = a.coef + ((int64_t)k * a.groups + g) * 3 * MAXM;
-                    if constexpr (MAXM % 4 == 0) {
+            if constexpr (TAB) {
+                // runs of steps sharing one coefficient row: no per-step
+                // output-row test or table indexing
+#pragma unroll 1
+                for (int ri = 0; ri < a.n_runs; ++ri) {
+                    const int4 run = __ldg(a.runs + ri);
+                    // rows padded to MAXM (d = b = c = 0 beyond M); read every step
+                    // from L1 rather than held in registers across the run
+                    const float *tb = a.coef + ((int64_t)run.w * a.groups + g) * 3 * MAXM;
+#pragma unroll 1
+                    for (int k = run.x; k < run.y; ++k) {
+                        R dW[MAXM], dJ[MAXM];
+                        // sqrt|dt| is folded into c
+                        draw(k, R(1), dW, dJ);
+                        float ca[MAXM], cb[MAXM], cc[MAXM];
+                        if constexpr (MAXM % 4 == 0) {
 #pragma unroll
-                        for (int q = 0; q < MAXM / 4; ++q) {
-                            const float4 va = __ldg(reinterpret_cast<const float4 *>(tb) + q);
-                            const float4 vb = __ldg(reinterpret_cast<const float4 *>(tb + MAXM) + q);
-                            const float4 vc = __ldg(reinterpret_cast<const float4 *>(tb + 2 * MAXM) + q);
-                            ca[4 * q] = va.x; ca[4 * q + 1] = va.y; ca[4 * q + 2] = va.z; ca[4 * q + 3] = va.w;
-                            cb[4 * q] = vb.x; cb[4 * q + 1] = vb.y; cb[4 * q + 2] = vb.z; cb[4 * q + 3] = vb.w;
-                            cc[4 * q] = vc.x; cc[4 * q + 1] = vc.y; cc[4 * q + 2] = vc.z; cc[4 * q + 3] = vc.w;
+                            for (int q = 0; q < MAXM / 4; ++q) {
+                                const float4 va = __ldg(reinterpret_cast<const float4 *>(tb) + q);
+                                const float4 vb = __ldg(reinterpret_cast<const float4 *>(tb + MAXM) + q);
+                                const float4 vc = __ldg(reinterpret_cast<const float4 *>(tb + 2 * MAXM) + q);
+                                ca[4 * q] = va.x; ca[4 * q + 1] = va.y; ca[4 * q + 2] = va.z; ca[4 * q + 3] = va.w;
+                                cb[4 * q] = vb.x; cb[4 * q + 1] = vb.y; cb[4 * q + 2] = vb.z; cb[4 * q + 3] = vb.w;
+                                cc[4 * q] = vc.x; cc[4 * q + 1] = vc.y; cc[4 * q + 2] = vc.z; cc[4 * q + 3] = vc.w;
+                            }
+                        } else {
+#pragma unroll
+                            for (int m = 0; m < MAXM; ++m) {
+                                ca[m] = __ldg(tb + m);
+                                cb[m] = __ldg(tb + MAXM + m);
+                                cc[m] = __ldg(tb + 2 * MAXM + m);
+                            }
                         }
-                    } else {
 #pragma unroll
                         for (int m = 0; m < MAXM; ++m) {
-                            ca[m] = __ldg(tb + m);
-                            cb[m] = __ldg(tb + MAXM + m);
-                            cc[m] = __ldg(tb + 2 * MAXM + m);
+                            const float xs = (float)st[m];
+                            float x = xs + fmaf(-ca[m], xs, cb[m]);
+                            x = fmaf(cc[m], (float)dW[m], x);
+                            if (JUMPS) x = x + (float)dJ[m];
+                            st[m] = (R)x;
                         }
                     }
+                    if (run.z >= 0) store(run.z);
+                }
+            } else {
+#pragma unroll 1
+                for (int k = 0; k < n_steps; ++k) {
+                    const R dt = a.dt[k];
+                    const R sq = a.sqdt[k];
+                    R dW[MAXM], dJ[MAXM];
+                    draw(k, sq, dW, dJ);
+                    // ---- Euler step, sdepy's operation order ----------------------
+                    if (MODEL == SDE_MODEL_LINEAR) {
 #pragma unroll
-                    for (int m = 0; m < MAXM; ++m) {
-                        const float xs = (float)st[m];
-                        float x = xs + fmaf(-ca[m], xs, cb[m]);
-                        x = fmaf(cc[m], (float)dW[m], x);
-                        if (JUMPS) x = x + (float)dJ[m];
-                        st[m] = (R)x;
-                    }
-                } else if (MODEL == SDE_MODEL_LINEAR) {
+                        for (int m = 0; m < MAXM; ++m) {
+                            R inc = A::add(A::mul(c0[m], dt), A::mul(c1[m], dW[m]));
+                            if (JUMPS) inc = A::add(inc, dJ[m]);
+                            st[m] = A::add(st[m], inc);
+                        }
+                    } else if (MODEL == SDE_MODEL_OU) {
 #pragma unroll
-                    for (int m = 0; m < MAXM; ++m) {
-                        R inc = A::add(A::mul(c0[m], dt), A::mul(c1[m], dW[m]));
-                        if (JUMPS) inc = A::add(inc, dJ[m]);
-                        st[m] = A::add(st[m], inc);
-                    }
-                } else if (MODEL == SDE_MODEL_OU) {
+                        for (int m = 0; m < MAXM; ++m) {
+                            const R drift = A::mul(c0[m], A::sub(c1[m], st[m]));
+                            st[m] = A::add(st[m], A::add(A::mul(drift, dt), A::mul(c2[m], dW[m])));
+                        }
+                    } else {  // HESTON: first half log-price, second half variance
+                        // Heston kernels run with group_size == MAXM exactly
+                        constexpr int h = MAXM / 2;
+                        R nx[MAXM];
 #pragma unroll
-                    for (int m = 0; m < MAXM; ++m) {
-                        const R drift = A::mul(c0[m], A::sub(c1[m], st[m]));
-                        st[m] = A::add(st[m], A::add(A::mul(drift, dt), A::mul(c2[m], dW[m])));
-                    }
-                } else {  // HESTON: first half log-price, second half variance
-                    // Heston kernels run with group_size == MAXM exactly
-                    constexpr int h = MAXM / 2;
-                    R nx[MAXM];
-#pragma unroll
-                    for (int i = 0; i < h; ++i) {
-                        {
+                        for (int i = 0; i < h; ++i) {
                             const R y = st[h + i];
                             if (y < R(0)) negc[i] += 1;
                             const R yp = fmax(y, R(0));
@@ -672,12 +704,12 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                             const R bdw = A::mul(xi, sqy);
                             nx[h + i] = A::add(y, A::add(A::mul(bdt, dt), A::mul(bdw, dW[h + i])));
                         }
-                    }
 #pragma unroll
-                    for (int m = 0; m < MAXM; ++m) st[m] = nx[m];
+                        for (int m = 0; m < MAXM; ++m) st[m] = nx[m];
+                    }
+                    const int r = a.out_row[k + 1];
+                    if (r >= 0) store(r);
                 }
-                const int r = a.out_row[k + 1];
-                if (r >= 0) store(r);
             }
             if (MODEL == SDE_MODEL_HESTON && a.neg_count) {
                 constexpr int h = MAXM / 2;

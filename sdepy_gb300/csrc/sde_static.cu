@@ -81,6 +81,12 @@ __global__ void static_tables_kernel(const double *tt, int n_pts, const double *
     if (i < SDE_MAX_PARAMS * W) prmr[i] = (R)prm[i];
 }
 
+// one run per step: (k, k + 1, row stored after step k, coefficient row k)
+__global__ void static_runs_kernel(const int32_t *out_row, int n_steps, int4 *runs) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n_steps) runs[k] = make_int4(k, k + 1, out_row[k + 1], k);
+}
+
 // results [n_out][RES_STRIDE] -> moments [n_out][8] and payoff [n_out][n_strikes]
 __global__ void static_pack_kernel(const double *res, int64_t n_out, int n_strikes, double *mom, double *pay) {
     const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -91,7 +97,7 @@ __global__ void static_pack_kernel(const double *res, int64_t n_out, int n_strik
 }
 
 struct Layout {
-    size_t tt, row, x0, prm, dt, sq, x0r, prmr, coef, part, res, edges, edges64, counts, vals, mom, pay, err, end;
+    size_t tt, row, x0, prm, dt, sq, x0r, prmr, coef, runs, part, res, edges, edges64, counts, vals, mom, pay, err, end;
 };
 
 size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -194,6 +200,7 @@ int run_static(const SdeSpec *s, const SdeGrid *gr, const SdeStatsReq *req, SdeS
     lo.prmr = o; o = al256(o + sizeof(R) * SDE_MAX_PARAMS * W);
     const bool tab = sizeof(R) == 4 && s->model != SDE_MODEL_HESTON;
     lo.coef = o; o = al256(o + (tab ? sizeof(float) * 3 * (size_t)n_steps * s->groups * maxm : 0));
+    lo.runs = o; o = al256(o + (tab ? sizeof(int4) * (size_t)n_steps : 0));
     lo.part = o; o = al256(o + sizeof(double) * NPART * (size_t)s->groups * nbx * opg);
     lo.res = o; o = al256(o + sizeof(double) * RES_STRIDE * n_out);
     lo.edges = o; o = al256(o + sizeof(R) * (size_t)(bins + 1) * n_out);
@@ -259,6 +266,11 @@ int run_static(const SdeSpec *s, const SdeGrid *gr, const SdeStatsReq *req, SdeS
             s->model, (float *)(base + lo.coef));
         CUS(cudaGetLastError());
         a.coef = (const float *)(base + lo.coef);
+        static_runs_kernel<<<(n_steps + 255) / 256, 256, 0, st>>>((const int32_t *)(base + lo.row), n_steps,
+                                                                 (int4 *)(base + lo.runs));
+        CUS(cudaGetLastError());
+        a.runs = (const int4 *)(base + lo.runs);
+        a.n_runs = n_steps;
     }
     a.n_out_vars = n_out;
     a.stats_row = req->row;
