@@ -92,6 +92,8 @@ SIGNATURES = {
     'sde_device_count': (C.c_int32, []),
     'sde_release': (C.c_int32, []),
     'sde_set_stream': (C.c_int32, [C.c_void_p]),
+    'sde_host_alloc': (C.c_int32, [C.c_int64, C.POINTER(C.c_void_p)]),
+    'sde_host_free': (C.c_int32, [C.c_void_p]),
     'sde_timing': (C.c_int32, [C.c_int32, _dp]),
     'sde_peak_probe': (C.c_int32, [C.c_int32, _dp]),
     'sde_cholesky': (C.c_int32, [_dp, C.c_int32, _dp]),

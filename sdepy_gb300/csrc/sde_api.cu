@@ -155,6 +155,19 @@ extern "C" int32_t sde_timing(int32_t enable, double *last_ms) {
     return SDE_OK;
 }
 
+extern "C" int32_t sde_host_alloc(int64_t bytes, void **ptr) {
+    if (!ptr || bytes < 1) return fail(SDE_ERR_INVALID, "sde_host_alloc: bad arguments");
+    *ptr = nullptr;
+    CU(cudaHostAlloc(ptr, (size_t)bytes, cudaHostAllocPortable));
+    return SDE_OK;
+}
+
+extern "C" int32_t sde_host_free(void *ptr) {
+    if (!ptr) return SDE_OK;
+    CU(cudaFreeHost(ptr));
+    return SDE_OK;
+}
+
 extern "C" int32_t sde_set_stream(void *stream) {
     std::lock_guard<std::mutex> lk(g_mu);
     Device *D;
@@ -508,13 +521,24 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
             rmin = gr->out_row[k] < rmin ? gr->out_row[k] : rmin;
             rmax = gr->out_row[k] > rmax ? gr->out_row[k] : rmax;
         }
+    // host output in pinned (page-locked) memory: the kernel stores its rows
+    // straight into it, with no device buffer and no separate copy
+    bool xx_mapped = false;
     if (out->xx) {
         if (dev) {
             a.xx = (R *)out->xx;
         } else {
-            void *p;
-            if ((rc = scratch(D, S_XX, xx_bytes, &p))) return rc;
-            a.xx = (R *)p;
+            cudaPointerAttributes pa;
+            if (cudaPointerGetAttributes(&pa, out->xx) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
+                pa.devicePointer != nullptr) {
+                a.xx = (R *)pa.devicePointer;
+                xx_mapped = true;
+            } else {
+                cudaGetLastError();
+                void *p;
+                if ((rc = scratch(D, S_XX, xx_bytes, &p))) return rc;
+                a.xx = (R *)p;
+            }
         }
     }
     const int h = M / 2;
@@ -563,7 +587,9 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
         void *p;
         if ((rc = scratch(D, S_PART, sizeof(double) * NPART * (size_t)s->groups * nbx * opg, &p))) return rc;
         a.partials = (double *)p;
-        if (bins > 0 && !a.xx) {
+        // the histogram pass reads device memory: a private copy of the row
+        // when the paths go only to host memory
+        if (bins > 0 && (!a.xx || xx_mapped)) {
             if ((rc = scratch(D, S_VALS, sizeof(R) * n_out * paths, &p))) return rc;
             a.stats_vals = (R *)p;
         }
@@ -588,7 +614,7 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
             CU(cudaMemsetAsync(counts, 0, sizeof(int64_t) * bins * n_out, st));
             const R *vals;
             int64_t vstride;
-            if (a.xx) {
+            if (a.xx && !xx_mapped) {
                 vals = a.xx + (int64_t)req->row * n_out * paths;
                 vstride = paths;
             } else {
@@ -622,7 +648,7 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
 
     // ---- copies back ----------------------------------------------------------------------
     if (!dev) {
-        if (out->xx && rmax >= rmin) {
+        if (out->xx && !xx_mapped && rmax >= rmin) {
             const size_t row_bytes = (size_t)n_out * paths * sizeof(R);
             CU(cudaMemcpyAsync((char *)out->xx + rmin * row_bytes, (char *)a.xx + rmin * row_bytes,
                                (size_t)(rmax - rmin + 1) * row_bytes, cudaMemcpyDeviceToHost, st));

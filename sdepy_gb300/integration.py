@@ -17,7 +17,7 @@ than float64 / float32, and SDE classes this module does not define.
 """
 import numpy as np
 
-from . import _lib
+from . import _lib, _pinned
 from .grid import Grid
 from .infrastructure import (
     process, philox_rng, draw_key, check_rng, get_corr_matrix, law_of,
@@ -326,7 +326,8 @@ class _gpu_process:
         xx = None
         if write:
             # every row is stored by one of the legs (sdepy fills NaN first)
-            xx = np.empty((rows,) + self.xshape + (self.paths,), dtype=out_dtype)
+            # (page-locked: the kernel writes the rows straight to the host)
+            xx = _pinned.empty((rows,) + self.xshape + (self.paths,), out_dtype)
         jumps = 'dj' in self._sources
         heston = self._model == _lib.MODEL_HESTON
         if self.getinfo:
