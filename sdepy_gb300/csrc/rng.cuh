@@ -109,6 +109,12 @@ template <> struct Rng<double> {
         return -log(u01_f64(a));
     }
     static __device__ __forceinline__ double unif(uint32_t a) { return u01_f64(a); }
+    static __device__ __forceinline__ void normal2_s(uint32_t a, uint32_t b,
+                                                     double &z0, double &z1) {
+        normal2(a, b, z0, z1);
+        z0 *= 0.84932180028801907;  // 1 / sqrt(2 ln 2)
+        z1 *= 0.84932180028801907;
+    }
 };
 
 template <> struct Rng<float> {
@@ -117,7 +123,22 @@ template <> struct Rng<float> {
         const float u = fmaf((float)a, 0x1p-32f, 0x1p-33f);
         // -2 ln u = -2 ln2 * log2 u
         const float r = approx_sqrt(-1.38629436f * approx_lg2(u));
-        const float th = 3.14159265f * vpm1_f32(b);
+        const float th = angle(b);
+        z0 = r * approx_cos(th);
+        z1 = r * approx_sin(th);
+    }
+    // pi v = pi (s - 3) with s = 3 + v in [2, 4) built from the word's bits,
+    // as one fused multiply-add
+    static __device__ __forceinline__ float angle(uint32_t b) {
+        return fmaf(__uint_as_float(0x40000000u | (b >> 9)), 3.14159265f, -9.42477796f);
+    }
+    // the same pair divided by sqrt(2 ln 2): r = sqrt(-log2 u), one multiply
+    // less per pair for callers that fold the factor into their coefficients
+    static __device__ __forceinline__ void normal2_s(uint32_t a, uint32_t b,
+                                                     float &z0, float &z1) {
+        const float u = fmaf((float)a, 0x1p-32f, 0x1p-33f);
+        const float r = approx_sqrt(-approx_lg2(u));
+        const float th = angle(b);
         z0 = r * approx_cos(th);
         z1 = r * approx_sin(th);
     }

@@ -350,33 +350,37 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     // FP32 LINEAR / OU: the grid as runs of steps with one coefficient row
     // each, and the compact table of those rows (see FwdArgs::coef / runs)
     std::vector<int4> runs;
-    std::vector<float> ctab;
+    std::vector<float> ctab, tshift;
     if (tab && n_steps > 0) {
-        const size_t rowlen = (size_t)s->groups * 3 * tmaxm;
+        const size_t rowlen = (size_t)s->groups * 2 * tmaxm;
         std::vector<float> cur(rowlen), nxt(rowlen);
-        const double *P0 = s->params, *P1 = s->params + W, *P2 = s->params + 2 * W;
+        // the same FP64 operations as coef_table_kernel
+        const double *P0 = s->params, *PS = s->params + (s->model == SDE_MODEL_OU ? 2 : 1) * W;
         auto coef_row = [&](int k, float *t) {
             const double dt = gr->tt[k + 1] - gr->tt[k], sq = sqrt(fabs(dt));
             for (int g = 0; g < s->groups; ++g) {
-                float *r = t + (size_t)g * 3 * tmaxm;
+                float *r = t + (size_t)g * 2 * tmaxm;
                 for (int m = 0; m < tmaxm; ++m) {
                     if (m >= M) {
-                        r[m] = r[tmaxm + m] = r[2 * tmaxm + m] = 0.0f;
+                        r[m] = r[tmaxm + m] = 0.0f;
                         continue;
                     }
                     const int w = g * M + m;
-                    if (s->model == SDE_MODEL_OU) {
-                        r[m] = (float)(P0[w] * dt);
-                        r[tmaxm + m] = (float)((P0[w] * P1[w]) * dt);
-                        r[2 * tmaxm + m] = (float)(P2[w] * sq);
-                    } else {
-                        r[m] = 0.0f;
-                        r[tmaxm + m] = (float)(P0[w] * dt);
-                        r[2 * tmaxm + m] = (float)(P1[w] * sq);
-                    }
+                    const double cs = PS[w] * sq;
+                    r[m] = (float)(P0[w] * dt);
+                    r[tmaxm + m] = (float)(cs * SDE_SQRT_2LN2);
                 }
             }
         };
+        if (s->model == SDE_MODEL_OU) {
+            tshift.assign((size_t)s->groups * 2 * tmaxm, 0.0f);
+            for (int g = 0; g < s->groups; ++g)
+                for (int m = 0; m < M; ++m) {
+                    const int w = g * M + m;
+                    tshift[(size_t)g * 2 * tmaxm + m] = (float)s->params[W + w];
+                    tshift[(size_t)(g * 2 + 1) * tmaxm + m] = (float)(s->x0[w] - s->params[W + w]);
+                }
+        }
         int k = 0;
         while (k < n_steps) {
             coef_row(k, cur.data());
@@ -402,7 +406,8 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     }
     const size_t o_runs = o_thr + al(sizeof(long long) * njt);
     const size_t o_ctab = o_runs + al(sizeof(int4) * (runs.size() + 1));
-    const size_t o_end = o_ctab + al(sizeof(float) * (ctab.size() + 4));
+    const size_t o_tsh = o_ctab + al(sizeof(float) * (ctab.size() + 4));
+    const size_t o_end = o_tsh + al(sizeof(float) * (tshift.size() + 4));
     D->host_tables.resize(o_end);
     char *H = D->host_tables.data();
     R *h_dt = (R *)(H + o_dt), *h_sq = (R *)(H + o_sq), *h_x0 = (R *)(H + o_x0), *h_prm = (R *)(H + o_prm);
@@ -447,6 +452,7 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
 
     if (!runs.empty()) memcpy(H + o_runs, runs.data(), sizeof(int4) * runs.size());
     if (!ctab.empty()) memcpy(H + o_ctab, ctab.data(), sizeof(float) * ctab.size());
+    if (!tshift.empty()) memcpy(H + o_tsh, tshift.data(), sizeof(float) * tshift.size());
 
     FwdArgs<R> a;
     memset(&a, 0, sizeof a);
@@ -489,6 +495,7 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
         a.coef = (const float *)(T + o_ctab);
         a.runs = (const int4 *)(T + o_runs);
         a.n_runs = (int32_t)runs.size();
+        a.tshift = tshift.empty() ? nullptr : (const float *)(T + o_tsh);
     }
     a.key = philox_schedule(s->seed);
     a.n_out_vars = n_out;

@@ -46,13 +46,19 @@ struct FwdArgs {
     const long long *thr;
     // per-variable inputs
     const R *x0, *prm;  // prm[p*W + w]
-    // FP32 LINEAR / OU with device RNG: coefficient rows [row][groups][3][MAXM]
-    // = (d, b, c), padded to the kernel's MAXM, with the update
-    // x' = x + (b - d x) + c (L z) (+ jumps): OU d = k dt, b = k theta dt,
-    // c = sigma sqrt|dt|; LINEAR d = 0, b = c_dt dt, c = c_dw sqrt|dt|
-    // (FP64 products rounded to FP32).  d is kept small (not 1 - k dt) so
+    // FP32 LINEAR / OU with device RNG: coefficient rows [row][groups][2][MAXM],
+    // padded to the kernel's MAXM, with normals z' = z / sqrt(2 ln 2):
+    //   OU      (d, c): y' = (y - d y) + c (L z'),  y = x - theta,
+    //                   d = k dt, c = sigma sqrt|dt| sqrt(2 ln 2);
+    //   LINEAR  (b, c): x' = (x + b) + c (L z') (+ jumps),
+    //                   b = c_dt dt, c = c_dw sqrt|dt| sqrt(2 ln 2)
+    // (FP64 products rounded to FP32).  The OU state is held as the
+    // deviation from theta, so the update is two fused multiply-adds and
+    // rounds relative to the deviation; d is kept small (not 1 - k dt) so
     // that its rounding does not bias the decay over many steps.
     const float *coef;
+    // OU: [groups][2][MAXM] = (theta, x0 - theta) in FP32
+    const float *tshift;
     // and the grid as runs of steps sharing one coefficient row:
     // (first step, end step, output row stored after the run or -1, coef row)
     const int4 *runs;
@@ -330,12 +336,15 @@ __device__ __forceinline__ void step_words(const PhiloxKey &key, uint32_t p, uin
     }
 }
 
-template <typename R, int MAXM, int NW>
+// SC: normals divided by sqrt(2 ln 2) (Rng::normal2_s), for the FP32 table
+// kernels whose coefficients carry that factor
+template <typename R, int MAXM, int NW, bool SC = false>
 __device__ __forceinline__ void words_to_normals(const uint32_t (&u)[NW], R (&z)[MAXM]) {
 #pragma unroll
     for (int q = 0; q < (MAXM + 1) / 2; ++q) {
         R z0, z1;
-        Rng<R>::normal2(u[2 * q], u[2 * q + 1], z0, z1);
+        if (SC) Rng<R>::normal2_s(u[2 * q], u[2 * q + 1], z0, z1);
+        else Rng<R>::normal2(u[2 * q], u[2 * q + 1], z0, z1);
         z[2 * q] = z0;
         if (2 * q + 1 < MAXM) z[2 * q + 1] = z1;
     }
@@ -361,11 +370,22 @@ __device__ __forceinline__ void correlate(const R *chol, bool has_corr, const R 
     }
 }
 
+template <typename R, bool SC>
+__device__ __forceinline__ void normals4(uint4 r, R (&zc)[4]) {
+    if (SC) {
+        Rng<R>::normal2_s(r.x, r.y, zc[0], zc[1]);
+        Rng<R>::normal2_s(r.z, r.w, zc[2], zc[3]);
+    } else {
+        Rng<R>::normal2(r.x, r.y, zc[0], zc[1]);
+        Rng<R>::normal2(r.z, r.w, zc[2], zc[3]);
+    }
+}
+
 // Same increments as step_words + words_to_normals + correlate, produced one
 // Philox call (4 normals) at a time so that only 4 normals are live; the
 // mat-vec accumulates in the same order (j ascending), so FP64 rounding is
 // identical.  Used by the kernels without jumps.
-template <typename R, int MAXM>
+template <typename R, int MAXM, bool SC = false>
 __device__ __forceinline__ void step_increments(const PhiloxKey &key, uint32_t p, uint32_t c1w, uint32_t g,
                                                 uint32_t stream, int NC, const R *chol, bool has_corr,
                                                 R sq, R (&dW)[MAXM]) {
@@ -377,8 +397,7 @@ __device__ __forceinline__ void step_increments(const PhiloxKey &key, uint32_t p
             if (c < NC) {
                 const uint4 r = philox4x32_10(make_uint4(p, c1w, (g << 8) | (uint32_t)c, stream), key);
                 R zc[4];
-                Rng<R>::normal2(r.x, r.y, zc[0], zc[1]);
-                Rng<R>::normal2(r.z, r.w, zc[2], zc[3]);
+                normals4<R, SC>(r, zc);
 #pragma unroll
                 for (int l = 0; l < 4; ++l)
                     if (4 * c + l < MAXM) dW[4 * c + l] = A::mul(zc[l], sq);
@@ -391,8 +410,7 @@ __device__ __forceinline__ void step_increments(const PhiloxKey &key, uint32_t p
         if (c < NC) {
             const uint4 r = philox4x32_10(make_uint4(p, c1w, (g << 8) | (uint32_t)c, stream), key);
             R zc[4];
-            Rng<R>::normal2(r.x, r.y, zc[0], zc[1]);
-            Rng<R>::normal2(r.z, r.w, zc[2], zc[3]);
+            normals4<R, SC>(r, zc);
 #pragma unroll
             for (int l = 0; l < 4; ++l) {
                 const int j = 4 * c + l;
@@ -470,6 +488,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     typedef Ar<R> A;
     constexpr int NCMAX = NoiseShape<MAXM, JUMPS>::NCMAX;
     constexpr bool TAB = sizeof(R) == 4 && MODEL != SDE_MODEL_HESTON && !INJECT;
+    constexpr bool SHIFT = TAB && MODEL == SDE_MODEL_OU;  // state held as x - theta
     __shared__ R red[BLOCK / 32];
     __shared__ double part[MAXM][NPART];
     __shared__ R svs[MAXM][BLOCK];   // this round's value of each output at the stats row
@@ -482,7 +501,8 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     const int n_steps = a.n_pts - 1;
     const bool do_stats = a.partials != nullptr;
     const PhiloxKey key = a.key;  // by value: uniform registers, not indexed parameter loads
-    if (TAB && (a.coef == nullptr || a.runs == nullptr) && n_steps > 0) {  // uniform: the grid returns
+    if (TAB && (a.coef == nullptr || a.runs == nullptr || (SHIFT && a.tshift == nullptr)) &&
+        n_steps > 0) {  // uniform: the grid returns
         if (threadIdx.x == 0 && blockIdx.x == 0 && blockIdx.y == 0) atomicOr(a.err, ERRF_ARGS);
         return;
     }
@@ -525,10 +545,19 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
             for (int m = 0; m < MAXM; ++m) { negc[m] = 0; jcnt[m] = 0; }
             unsigned int row_jc = 0;
 
-            // store helper (lambda keeps the loop body readable)
-            auto store = [&](int row) {
+            // store helper (lambda keeps the loop body readable); sh: the
+            // state is the deviation from theta
+            auto store = [&](int row, bool sh) {
                 R ov[MAXM];
-                const int no = group_outputs<R, MAXM>(st, M, a.out_mode, ov);
+                int no;
+                if (SHIFT && sh) {
+                    R sx[MAXM];
+#pragma unroll
+                    for (int m = 0; m < MAXM; ++m) sx[m] = st[m] + (R)__ldg(a.tshift + g * 2 * MAXM + m);
+                    no = group_outputs<R, MAXM>(sx, M, a.out_mode, ov);
+                } else {
+                    no = group_outputs<R, MAXM>(st, M, a.out_mode, ov);
+                }
                 if (a.xx) {
 #pragma unroll
                     for (int m = 0; m < MAXM; ++m)
@@ -555,7 +584,11 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
 
             {
                 const int r0 = a.out_row[0];
-                if (r0 >= 0) store(r0);
+                if (r0 >= 0) store(r0, false);
+            }
+            if (SHIFT && n_steps > 0) {
+#pragma unroll
+                for (int m = 0; m < MAXM; ++m) st[m] = (R)__ldg(a.tshift + (g * 2 + 1) * MAXM + m);
             }
             // increments of step k: injected, or drawn from Philox counters
             // (normals, correlated; Poisson counts and jump sums)
@@ -584,14 +617,14 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                 }
                 const uint32_t c1w = (uint32_t)k + a.step_offset;
                 if (!JUMPS) {
-                    step_increments<R, MAXM>(key, (uint32_t)p, c1w, (uint32_t)g, a.stream, NC, a.chol,
-                                             a.has_corr, sq, dW);
+                    step_increments<R, MAXM, TAB>(key, (uint32_t)p, c1w, (uint32_t)g, a.stream, NC, a.chol,
+                                                  a.has_corr, sq, dW);
                     return;
                 }
                 uint32_t u[4 * NCMAX];
                 step_words<MAXM, JUMPS>(key, (uint32_t)p, c1w, (uint32_t)g, a.stream, NC, u);
                 R z[MAXM];
-                words_to_normals<R, MAXM>(u, z);
+                words_to_normals<R, MAXM, 4 * NCMAX, TAB>(u, z);
                 correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
 #pragma unroll
                 for (int m = 0; m < MAXM; ++m) {
@@ -626,41 +659,39 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                     const int4 run = __ldg(a.runs + ri);
                     // rows padded to MAXM (d = b = c = 0 beyond M); read every step
                     // from L1 rather than held in registers across the run
-                    const float *tb = a.coef + ((int64_t)run.w * a.groups + g) * 3 * MAXM;
+                    const float *tb = a.coef + ((int64_t)run.w * a.groups + g) * 2 * MAXM;
 #pragma unroll 1
                     for (int k = run.x; k < run.y; ++k) {
                         R dW[MAXM], dJ[MAXM];
-                        // sqrt|dt| is folded into c
+                        // sqrt|dt| sqrt(2 ln 2) is folded into c
                         draw(k, R(1), dW, dJ);
-                        float ca[MAXM], cb[MAXM], cc[MAXM];
+                        float ca[MAXM], cc[MAXM];
                         if constexpr (MAXM % 4 == 0) {
 #pragma unroll
                             for (int q = 0; q < MAXM / 4; ++q) {
                                 const float4 va = __ldg(reinterpret_cast<const float4 *>(tb) + q);
-                                const float4 vb = __ldg(reinterpret_cast<const float4 *>(tb + MAXM) + q);
-                                const float4 vc = __ldg(reinterpret_cast<const float4 *>(tb + 2 * MAXM) + q);
+                                const float4 vc = __ldg(reinterpret_cast<const float4 *>(tb + MAXM) + q);
                                 ca[4 * q] = va.x; ca[4 * q + 1] = va.y; ca[4 * q + 2] = va.z; ca[4 * q + 3] = va.w;
-                                cb[4 * q] = vb.x; cb[4 * q + 1] = vb.y; cb[4 * q + 2] = vb.z; cb[4 * q + 3] = vb.w;
                                 cc[4 * q] = vc.x; cc[4 * q + 1] = vc.y; cc[4 * q + 2] = vc.z; cc[4 * q + 3] = vc.w;
                             }
                         } else {
 #pragma unroll
                             for (int m = 0; m < MAXM; ++m) {
                                 ca[m] = __ldg(tb + m);
-                                cb[m] = __ldg(tb + MAXM + m);
-                                cc[m] = __ldg(tb + 2 * MAXM + m);
+                                cc[m] = __ldg(tb + MAXM + m);
                             }
                         }
 #pragma unroll
                         for (int m = 0; m < MAXM; ++m) {
-                            const float xs = (float)st[m];
-                            float x = xs + fmaf(-ca[m], xs, cb[m]);
+                            float x = (float)st[m];
+                            if (SHIFT) x = fmaf(-ca[m], x, x);   // y - d y
+                            else x = x + ca[m];                  // x + b
                             x = fmaf(cc[m], (float)dW[m], x);
                             if (JUMPS) x = x + (float)dJ[m];
                             st[m] = (R)x;
                         }
                     }
-                    if (run.z >= 0) store(run.z);
+                    if (run.z >= 0) store(run.z, true);
                 }
             } else {
 #pragma unroll 1
@@ -708,7 +739,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                         for (int m = 0; m < MAXM; ++m) st[m] = nx[m];
                     }
                     const int r = a.out_row[k + 1];
-                    if (r >= 0) store(r);
+                    if (r >= 0) store(r, false);
                 }
             }
             if (MODEL == SDE_MODEL_HESTON && a.neg_count) {
@@ -739,12 +770,16 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     }
 }
 
-// per-step coefficients of the FP32 LINEAR / OU kernels, [steps][groups][3][MAXM]
+// sqrt(2 ln 2), carried by the c coefficients of the FP32 table kernels
+#define SDE_SQRT_2LN2 1.1774100225154747
+
+// per-step coefficients of the FP32 LINEAR / OU kernels, [steps][groups][2][MAXM]
 // (see FwdArgs::coef), from the FP64 grid and parameters with explicitly
-// rounded FP64 operations
+// rounded FP64 operations (the host builds the same rows with the same
+// operations); OU also writes the shift table FwdArgs::tshift
 static __global__ void __launch_bounds__(BLOCK)
-coef_table_kernel(const double *tt, int n_steps, const double *prm, int groups, int M, int maxm,
-                  int model, float *coef) {
+coef_table_kernel(const double *tt, int n_steps, const double *x0, const double *prm, int groups, int M,
+                  int maxm, int model, float *coef, float *tshift) {
     const int64_t i = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
     const int64_t n = (int64_t)n_steps * groups * maxm;
     if (i >= n) return;
@@ -752,25 +787,22 @@ coef_table_kernel(const double *tt, int n_steps, const double *prm, int groups, 
     const int64_t kg = i / maxm;
     const int g = (int)(kg % groups);
     const int k = (int)(kg / groups);
-    float *t = coef + kg * 3 * maxm;
+    float *t = coef + kg * 2 * maxm;
+    const int W = groups * M, w = g * M + m;
+    if (k == 0 && model == SDE_MODEL_OU) {
+        tshift[g * 2 * maxm + m] = m < M ? (float)prm[W + w] : 0.0f;
+        tshift[(g * 2 + 1) * maxm + m] = m < M ? (float)__dsub_rn(x0[w], prm[W + w]) : 0.0f;
+    }
     if (m >= M) {
         t[m] = 0.0f;
         t[maxm + m] = 0.0f;
-        t[2 * maxm + m] = 0.0f;
         return;
     }
-    const int W = groups * M, w = g * M + m;
     const double dt = __dsub_rn(tt[k + 1], tt[k]);
     const double sq = __dsqrt_rn(fabs(dt));
-    if (model == SDE_MODEL_OU) {
-        t[m] = (float)__dmul_rn(prm[w], dt);
-        t[maxm + m] = (float)__dmul_rn(__dmul_rn(prm[w], prm[W + w]), dt);
-        t[2 * maxm + m] = (float)__dmul_rn(prm[2 * W + w], sq);
-    } else {
-        t[m] = 0.0f;
-        t[maxm + m] = (float)__dmul_rn(prm[w], dt);
-        t[2 * maxm + m] = (float)__dmul_rn(prm[W + w], sq);
-    }
+    const int ip = model == SDE_MODEL_OU ? 2 : 1;   // sigma
+    t[m] = (float)__dmul_rn(prm[w], dt);
+    t[maxm + m] = (float)__dmul_rn(__dmul_rn(prm[ip * W + w], sq), SDE_SQRT_2LN2);
 }
 
 // launcher signature shared by the instantiation units

@@ -97,7 +97,7 @@ __global__ void static_pack_kernel(const double *res, int64_t n_out, int n_strik
 }
 
 struct Layout {
-    size_t tt, row, x0, prm, dt, sq, x0r, prmr, coef, runs, part, res, edges, edges64, counts, vals, mom, pay, err, end;
+    size_t tt, row, x0, prm, dt, sq, x0r, prmr, coef, tshift, runs, part, res, edges, edges64, counts, vals, mom, pay, err, end;
 };
 
 size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -199,7 +199,8 @@ int run_static(const SdeSpec *s, const SdeGrid *gr, const SdeStatsReq *req, SdeS
     lo.x0r = o; o = al256(o + sizeof(R) * W);
     lo.prmr = o; o = al256(o + sizeof(R) * SDE_MAX_PARAMS * W);
     const bool tab = sizeof(R) == 4 && s->model != SDE_MODEL_HESTON;
-    lo.coef = o; o = al256(o + (tab ? sizeof(float) * 3 * (size_t)n_steps * s->groups * maxm : 0));
+    lo.coef = o; o = al256(o + (tab ? sizeof(float) * 2 * (size_t)n_steps * s->groups * maxm : 0));
+    lo.tshift = o; o = al256(o + (tab ? sizeof(float) * 2 * (size_t)s->groups * maxm : 0));
     lo.runs = o; o = al256(o + (tab ? sizeof(int4) * (size_t)n_steps : 0));
     lo.part = o; o = al256(o + sizeof(double) * NPART * (size_t)s->groups * nbx * opg);
     lo.res = o; o = al256(o + sizeof(double) * RES_STRIDE * n_out);
@@ -262,10 +263,11 @@ int run_static(const SdeSpec *s, const SdeGrid *gr, const SdeStatsReq *req, SdeS
         // the FP32 LINEAR / OU kernels read their per-step coefficients
         const int64_t n = (int64_t)n_steps * s->groups * maxm;
         coef_table_kernel<<<(unsigned)((n + BLOCK - 1) / BLOCK), BLOCK, 0, st>>>(
-            (const double *)(base + lo.tt), n_steps, (const double *)(base + lo.prm), s->groups, M, maxm,
-            s->model, (float *)(base + lo.coef));
+            (const double *)(base + lo.tt), n_steps, (const double *)(base + lo.x0), (const double *)(base + lo.prm),
+            s->groups, M, maxm, s->model, (float *)(base + lo.coef), (float *)(base + lo.tshift));
         CUS(cudaGetLastError());
         a.coef = (const float *)(base + lo.coef);
+        a.tshift = s->model == SDE_MODEL_OU ? (const float *)(base + lo.tshift) : nullptr;
         static_runs_kernel<<<(n_steps + 255) / 256, 256, 0, st>>>((const int32_t *)(base + lo.row), n_steps,
                                                                  (int4 *)(base + lo.runs));
         CUS(cudaGetLastError());

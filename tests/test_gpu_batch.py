@@ -43,8 +43,11 @@ def _mixed(n_each=4):
         out.append(instance(OU, paths=7003, n_steps=80, T=2., x0=np.full(W, .1),
                             params=[np.linspace(1, 2, W), np.linspace(-.5, .5, W), np.full(W, .3)],
                             seed=seed + 10 + i, stream=i))
+        # Feller condition 2 k theta > xi^2 holds: the variance stays off 0,
+        # where the pathwise derivative of sqrt(y+) is singular and two
+        # implementations' last-bit differences would dominate the comparison
         out.append(instance(HESTON, paths=9000, n_steps=50 + 5*i, T=1., x0=[np.log(100.), .04],
-                            params=[[.02, 1.5], [1., .04], [0., .5]], rho=-.7,
+                            params=[[.02, 1.5], [1., .04], [0., .3]], rho=-.7,
                             seed=seed + 20 + i, out_exp=True))
         out.append(instance(LINEAR, paths=6000, n_steps=70, T=1., x0=[0.],
                             params=[[.03 - .15**2/2], [.15], [2.], [-.1], [.15]],
