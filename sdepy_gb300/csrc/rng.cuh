@@ -60,6 +60,29 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, const PhiloxKey &key) {
     return c;
 }
 
+// The first round multiplies only c0 and c2; with c1 (the step) left out
+// it is invariant along a path, so a path loop computes it once:
+//   pre = philox_round0(c0, c2, c3, key),  out = philox_from_round0(pre, c1, key)
+// equals philox4x32_10((c0, c1, c2, c3), key) bit for bit.
+__device__ __forceinline__ uint4 philox_round0(uint32_t c0, uint32_t c2, uint32_t c3, const PhiloxKey &key) {
+    uint32_t hi0, lo0, hi1, lo1;
+    mulwide(0xD2511F53u, c0, hi0, lo0);
+    mulwide(0xCD9E8D57u, c2, hi1, lo1);
+    return make_uint4(hi1 ^ key.k0[0], lo1, hi0 ^ c3 ^ key.k1[0], lo0);
+}
+
+__device__ __forceinline__ uint4 philox_from_round0(uint4 c, uint32_t c1, const PhiloxKey &key) {
+    c.x ^= c1;
+#pragma unroll
+    for (int i = 1; i < 10; ++i) {
+        uint32_t hi0, lo0, hi1, lo1;
+        mulwide(0xD2511F53u, c.x, hi0, lo0);
+        mulwide(0xCD9E8D57u, c.z, hi1, lo1);
+        c = make_uint4(hi1 ^ c.y ^ key.k0[i], lo1, hi0 ^ c.w ^ key.k1[i], lo0);
+    }
+    return c;
+}
+
 __device__ __forceinline__ double u01_f64(uint32_t x) {
     return ((double)x + 0.5) * 0x1p-32;
 }

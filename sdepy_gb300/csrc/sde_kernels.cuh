@@ -385,17 +385,28 @@ __device__ __forceinline__ void normals4(uint4 r, R (&zc)[4]) {
 // Philox call (4 normals) at a time so that only 4 normals are live; the
 // mat-vec accumulates in the same order (j ascending), so FP64 rounding is
 // identical.  Used by the kernels without jumps.
+// first Philox rounds of a path's normal calls (see philox_round0)
+template <int MAXM>
+struct PathPre {
+    static constexpr int NCN = (MAXM + 3) / 4;  // calls carrying normals
+    uint4 r0[NCN];
+    __device__ __forceinline__ PathPre(const PhiloxKey &key, uint32_t p, uint32_t g, uint32_t stream) {
+#pragma unroll
+        for (int c = 0; c < NCN; ++c) r0[c] = philox_round0(p, (g << 8) | (uint32_t)c, stream, key);
+    }
+};
+
 template <typename R, int MAXM, bool SC = false>
-__device__ __forceinline__ void step_increments(const PhiloxKey &key, uint32_t p, uint32_t c1w, uint32_t g,
-                                                uint32_t stream, int NC, const R *chol, bool has_corr,
+__device__ __forceinline__ void step_increments(const PhiloxKey &key, const PathPre<MAXM> &pre, uint32_t c1w,
+                                                int NC, const R *chol, bool has_corr,
                                                 R sq, R (&dW)[MAXM]) {
     typedef Ar<R> A;
-    constexpr int NCN = (MAXM + 3) / 4;  // calls carrying normals
+    constexpr int NCN = PathPre<MAXM>::NCN;
     if (!has_corr) {  // tested once per step, not per normal
 #pragma unroll
         for (int c = 0; c < NCN; ++c) {
             if (c < NC) {
-                const uint4 r = philox4x32_10(make_uint4(p, c1w, (g << 8) | (uint32_t)c, stream), key);
+                const uint4 r = philox_from_round0(pre.r0[c], c1w, key);
                 R zc[4];
                 normals4<R, SC>(r, zc);
 #pragma unroll
@@ -408,7 +419,7 @@ __device__ __forceinline__ void step_increments(const PhiloxKey &key, uint32_t p
 #pragma unroll
     for (int c = 0; c < NCN; ++c) {
         if (c < NC) {
-            const uint4 r = philox4x32_10(make_uint4(p, c1w, (g << 8) | (uint32_t)c, stream), key);
+            const uint4 r = philox_from_round0(pre.r0[c], c1w, key);
             R zc[4];
             normals4<R, SC>(r, zc);
 #pragma unroll
@@ -590,6 +601,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
 #pragma unroll
                 for (int m = 0; m < MAXM; ++m) st[m] = (R)__ldg(a.tshift + (g * 2 + 1) * MAXM + m);
             }
+            const PathPre<MAXM> pre(key, (uint32_t)p, (uint32_t)g, a.stream);
             // increments of step k: injected, or drawn from Philox counters
             // (normals, correlated; Poisson counts and jump sums)
             auto draw = [&](int k, R sq, R (&dW)[MAXM], R (&dJ)[MAXM]) {
@@ -617,8 +629,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                 }
                 const uint32_t c1w = (uint32_t)k + a.step_offset;
                 if (!JUMPS) {
-                    step_increments<R, MAXM, TAB>(key, (uint32_t)p, c1w, (uint32_t)g, a.stream, NC, a.chol,
-                                                  a.has_corr, sq, dW);
+                    step_increments<R, MAXM, TAB>(key, pre, c1w, NC, a.chol, a.has_corr, sq, dW);
                     return;
                 }
                 uint32_t u[4 * NCMAX];
