@@ -315,6 +315,65 @@ def _time_call(fn, lib, reps=3):
     return float(np.median(ts))
 
 
+HESTON_GRAD = {'x0': (0, 0), 'y0': (1, 0), 'k': (1, 1), 'theta': (1, 2), 'xi': (1, 3), 'rho': (0, 7)}
+
+
+def heston_gradient_check(lib, batches=16, paths=2**18, steps=500):
+    """The configs[2] gradient with its standard error, from `batches`
+    independent Philox streams of `paths` paths each, against central finite
+    differences (h = 1e-3 relative) of the fused FP32 forward on the same
+    paths (common random numbers).  Per parameter: the adjoint mean and its
+    standard error, the finite-difference mean and its standard error, and
+    z = |mean(adj - fd)| / se(adj - fd) over the batches.  The payoff is the
+    mean of the five call prices."""
+    import ctypes as C
+    import sdepy_gb300 as sg
+    from sdepy_gb300 import _lib
+    from sdepy_gb300.grid import Grid
+    tl = (0., 2.)
+    leg = Grid(tl, steps).legs[-1]
+    g = _lib.SdeGrid()
+    g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
+    g.n_pts, g.step_offset = leg.tt.size, 0
+    req = _lib.SdeAdjReq()
+    req.n_strikes, req.checkpoint, req.mean_weight = 5, 0, 0.
+    for i, K in enumerate(STRIKES):
+        req.strikes[i], req.weights[i] = K, .2
+    seed = 11
+    A = {n: [] for n in HESTON_GRAD}
+    F = {n: [] for n in HESTON_GRAD}
+
+    def price(stream, **kw):
+        P = sg.heston_process(paths=paths, steps=steps, dtype=np.float32,
+                              rng=sg.philox_rng(seed, stream), **kw)
+        return float(np.mean(P.montecarlo(tl, bins=None, strikes=STRIKES).payoff))
+
+    for b in range(batches):
+        H = sg.heston_process(paths=paths, steps=steps, dtype=np.float32, **HESTON)
+        spec = H._make_spec(seed, b)
+        grad = np.zeros((2, 8))
+        v = C.c_double()
+        _lib.check(lib.sde_adjoint(C.byref(spec), C.byref(g), C.byref(req), _lib.dptr(grad), C.byref(v)), 'adj')
+        for n, (i, j) in HESTON_GRAD.items():
+            # the adjoint of x0 is with respect to log x0 (the integrated state)
+            A[n].append(grad[i, j]/(HESTON['x0'] if n == 'x0' else 1.))
+            h = 1e-3*abs(HESTON[n])
+            up, dn = dict(HESTON), dict(HESTON)
+            up[n] += h
+            dn[n] -= h
+            F[n].append((price(b, **up) - price(b, **dn))/(2*h))
+    out = {}
+    for n in HESTON_GRAD:
+        a, f = np.array(A[n]), np.array(F[n])
+        d = a - f
+        sd = float(d.std(ddof=1)/np.sqrt(batches))
+        out[n] = {'adjoint': float(a.mean()), 'se': float(a.std(ddof=1)/np.sqrt(batches)),
+                  'fd': float(f.mean()), 'fd_se': float(f.std(ddof=1)/np.sqrt(batches)),
+                  'z': float(abs(d.mean())/sd) if sd > 0 else None}
+    out['sample'] = '{} streams x {} paths, {} steps on (0, 2), FP32'.format(batches, paths, leg.n_steps)
+    return out
+
+
 def extra_configs(lib):
     """configs[2] Heston (FP32 forward with fused call payoffs vs the adjoint
     gradient of the 6 parameters; FP64 forward), configs[3] Merton / Kou
@@ -361,6 +420,7 @@ def extra_configs(lib):
         return grad
     adj_ms = _time_call(adj, lib)
     grad = adj()
+    check = heston_gradient_check(lib)
     H64 = sg.heston_process(paths=2**18, steps=500, **HESTON)
     fwd64_ms = _time_call(lambda: fused(H64, tl, STRIKES, 3), lib, reps=2)
     n = leg.n_steps
@@ -374,6 +434,7 @@ def extra_configs(lib):
         'gradient': {'x0': float(grad[0, 0]/HESTON['x0']), 'y0': float(grad[1, 0]),
                      'k': float(grad[1, 1]), 'theta': float(grad[1, 2]), 'xi': float(grad[1, 3]),
                      'rho': float(grad[0, 7])},
+        'gradient_check': check,
         'checkpoint_segment': int(np.ceil(np.sqrt(n))),
     }
     # ---- jump diffusions, 2^22 paths, 364 steps on (0, 1)
@@ -417,7 +478,8 @@ def extra_configs(lib):
     # ---- lognormal configs[0]: FP64, 1e5 paths, 502 steps, all 253 rows written (host output)
     import time
     Ln = sg.lognorm_process(x0=1., mu=.05, sigma=.2, paths=100000, steps=252, rng=sg.philox_rng(0))
-    Ln(np.linspace(0, 1, 253))
+    for _ in range(2):   # steady state: host buffers of two live results pooled
+        x = Ln(np.linspace(0, 1, 253))
     t0 = time.perf_counter()
     for _ in range(3):
         x = Ln(np.linspace(0, 1, 253))

@@ -193,6 +193,7 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
         for (int m = 0; m < MAXM; ++m)
 #pragma unroll
             for (int j = 0; j < NGV; ++j) gr[m][j] = R(0);
+        const PathPre<NCMAX> pre(key, (uint32_t)p, (uint32_t)g, a.stream);
         R val;
         if (MODEL == SDE_MODEL_LINEAR) {
             // ---- constant adjoint: one forward sweep ------------------------------
@@ -204,7 +205,7 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                 const R dt = a.dt[k], sq = a.sqdt[k];
                 const uint32_t c1w = (uint32_t)k + a.step_offset;
                 uint32_t u[4 * NCMAX];
-                step_words<MAXM, JUMPS>(key, (uint32_t)p, c1w, (uint32_t)g, a.stream, NC, u);
+                step_words<MAXM, JUMPS>(key, pre, c1w, NC, u);
                 R z[MAXM], dW[MAXM];
                 words_to_normals<R, MAXM>(u, z);
                 correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
@@ -260,8 +261,7 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                 }
                 const R sq = a.sqdt[k];
                 uint32_t u[4 * NCMAX];
-                step_words<MAXM, JUMPS>(key, (uint32_t)p, (uint32_t)k + a.step_offset, (uint32_t)g,
-                                        a.stream, NC, u);
+                step_words<MAXM, JUMPS>(key, pre, (uint32_t)k + a.step_offset, NC, u);
                 R z[MAXM], dW[MAXM];
                 words_to_normals<R, MAXM>(u, z);
                 correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
@@ -278,8 +278,7 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                 for (int k = k0; k < k1; ++k) {
                     const R sq = a.sqdt[k];
                     uint32_t u[4 * NCMAX];
-                    step_words<MAXM, JUMPS>(key, (uint32_t)p, (uint32_t)k + a.step_offset, (uint32_t)g,
-                                            a.stream, NC, u);
+                    step_words<MAXM, JUMPS>(key, pre, (uint32_t)k + a.step_offset, NC, u);
                     R z[MAXM], dW[MAXM];
                     words_to_normals<R, MAXM>(u, z);
                     correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);

@@ -85,9 +85,10 @@ __device__ __forceinline__ float path_lin(const DevInst &I, const PhiloxKey &key
                                           int32_t *err) {
     float a = I.x0[0], sdw = 0.f, sja = 0.f, sjb = 0.f;
     const bool jumps = I.jump_law != SDE_JUMP_NONE;
+    const uint4 pre = philox_round0(p, 0u, I.stream, key);
 #pragma unroll 1
     for (int k = 0; k < I.n_steps; ++k) {
-        const uint4 r = philox4x32_10(make_uint4(p, (uint32_t)k, 0u, I.stream), key);
+        const uint4 r = philox_from_round0(pre, (uint32_t)k, key);
         float z0, z1;
         Rng<float>::normal2(r.x, r.y, z0, z1);
         a = a + I.b[0] + I.c[0] * z0;
@@ -125,9 +126,10 @@ __device__ __forceinline__ float path_ou(const DevInst &I, const PhiloxKey &key,
     const float rho0 = 1.f - I.d[0];
     const float kdt = I.d[0];
     const int W = I.nvars;
+    const uint4 pre = philox_round0(p, 0u, I.stream, key);
 #pragma unroll 1
     for (int k = 0; k < I.n_steps; ++k) {
-        const uint4 r = philox4x32_10(make_uint4(p, (uint32_t)k, 0u, I.stream), key);
+        const uint4 r = philox_from_round0(pre, (uint32_t)k, key);
         float z[4];
         Rng<float>::normal2(r.x, r.y, z[0], z[1]);
         if (W > 2) Rng<float>::normal2(r.z, r.w, z[2], z[3]);
@@ -160,9 +162,10 @@ __device__ __forceinline__ float path_heston(const DevInst &I, const PhiloxKey &
     ty[3] = 1.f;
     const float mu = I.p0[0], sg = I.p1[0], kk = I.p0[1], th = I.p1[1], xi = I.p2[1];
     const float dt = I.dt, sq = I.sq;
+    const uint4 pre = philox_round0(p, 0u, I.stream, key);
 #pragma unroll 1
     for (int k = 0; k < I.n_steps; ++k) {
-        const uint4 r = philox4x32_10(make_uint4(p, (uint32_t)k, 0u, I.stream), key);
+        const uint4 r = philox_from_round0(pre, (uint32_t)k, key);
         float z0, z1;
         Rng<float>::normal2(r.x, r.y, z0, z1);
         const float dW1 = z0 * sq;

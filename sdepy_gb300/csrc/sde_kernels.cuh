@@ -315,17 +315,29 @@ struct NoiseShape {
     static constexpr int NCMAX = (2 * ((MAXM + 1) / 2) + (JUMPS ? MAXM : 0) + 3) / 4;
 };
 
-// Philox words of step k: u[0 .. 2P) feed the Box-Muller pairs, u[2P + m]
-// is the Poisson uniform of state m (jump models)
+// first Philox rounds of a path's per-step calls (counter (p, step,
+// (g << 8) | call, stream) for call < NCALLS), which do not depend on the
+// step (see philox_round0)
+template <int NCALLS>
+struct PathPre {
+    uint4 r0[NCALLS];
+    __device__ __forceinline__ PathPre(const PhiloxKey &key, uint32_t p, uint32_t g, uint32_t stream) {
+#pragma unroll
+        for (int c = 0; c < NCALLS; ++c) r0[c] = philox_round0(p, (g << 8) | (uint32_t)c, stream, key);
+    }
+};
+
+// Philox words of step k (c1w = step + leg offset): u[0 .. 2P) feed the
+// Box-Muller pairs, u[2P + m] is the Poisson uniform of state m (jump models)
 template <int MAXM, bool JUMPS>
-__device__ __forceinline__ void step_words(const PhiloxKey &key, uint32_t p, uint32_t c1w, uint32_t g,
-                                           uint32_t stream, int NC,
-                                           uint32_t (&u)[4 * NoiseShape<MAXM, JUMPS>::NCMAX]) {
+__device__ __forceinline__ void step_words(const PhiloxKey &key,
+                                           const PathPre<NoiseShape<MAXM, JUMPS>::NCMAX> &pre, uint32_t c1w,
+                                           int NC, uint32_t (&u)[4 * NoiseShape<MAXM, JUMPS>::NCMAX]) {
     constexpr int NCMAX = NoiseShape<MAXM, JUMPS>::NCMAX;
 #pragma unroll
     for (int c = 0; c < NCMAX; ++c) {
         if (c < NC) {
-            const uint4 r = philox4x32_10(make_uint4(p, c1w, (g << 8) | (uint32_t)c, stream), key);
+            const uint4 r = philox_from_round0(pre.r0[c], c1w, key);
             u[4 * c + 0] = r.x;
             u[4 * c + 1] = r.y;
             u[4 * c + 2] = r.z;
@@ -385,23 +397,12 @@ __device__ __forceinline__ void normals4(uint4 r, R (&zc)[4]) {
 // Philox call (4 normals) at a time so that only 4 normals are live; the
 // mat-vec accumulates in the same order (j ascending), so FP64 rounding is
 // identical.  Used by the kernels without jumps.
-// first Philox rounds of a path's normal calls (see philox_round0)
-template <int MAXM>
-struct PathPre {
-    static constexpr int NCN = (MAXM + 3) / 4;  // calls carrying normals
-    uint4 r0[NCN];
-    __device__ __forceinline__ PathPre(const PhiloxKey &key, uint32_t p, uint32_t g, uint32_t stream) {
-#pragma unroll
-        for (int c = 0; c < NCN; ++c) r0[c] = philox_round0(p, (g << 8) | (uint32_t)c, stream, key);
-    }
-};
-
 template <typename R, int MAXM, bool SC = false>
-__device__ __forceinline__ void step_increments(const PhiloxKey &key, const PathPre<MAXM> &pre, uint32_t c1w,
-                                                int NC, const R *chol, bool has_corr,
+__device__ __forceinline__ void step_increments(const PhiloxKey &key, const PathPre<(MAXM + 3) / 4> &pre,
+                                                uint32_t c1w, int NC, const R *chol, bool has_corr,
                                                 R sq, R (&dW)[MAXM]) {
     typedef Ar<R> A;
-    constexpr int NCN = PathPre<MAXM>::NCN;
+    constexpr int NCN = (MAXM + 3) / 4;  // calls carrying normals
     if (!has_corr) {  // tested once per step, not per normal
 #pragma unroll
         for (int c = 0; c < NCN; ++c) {
@@ -601,7 +602,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
 #pragma unroll
                 for (int m = 0; m < MAXM; ++m) st[m] = (R)__ldg(a.tshift + (g * 2 + 1) * MAXM + m);
             }
-            const PathPre<MAXM> pre(key, (uint32_t)p, (uint32_t)g, a.stream);
+            const PathPre<NCMAX> pre(key, (uint32_t)p, (uint32_t)g, a.stream);
             // increments of step k: injected, or drawn from Philox counters
             // (normals, correlated; Poisson counts and jump sums)
             auto draw = [&](int k, R sq, R (&dW)[MAXM], R (&dJ)[MAXM]) {
@@ -628,12 +629,12 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                     return;
                 }
                 const uint32_t c1w = (uint32_t)k + a.step_offset;
-                if (!JUMPS) {
+                if constexpr (!JUMPS) {
                     step_increments<R, MAXM, TAB>(key, pre, c1w, NC, a.chol, a.has_corr, sq, dW);
                     return;
                 }
                 uint32_t u[4 * NCMAX];
-                step_words<MAXM, JUMPS>(key, (uint32_t)p, c1w, (uint32_t)g, a.stream, NC, u);
+                step_words<MAXM, JUMPS>(key, pre, c1w, NC, u);
                 R z[MAXM];
                 words_to_normals<R, MAXM, 4 * NCMAX, TAB>(u, z);
                 correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
