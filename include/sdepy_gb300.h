@@ -173,9 +173,12 @@ SDE_API int32_t sde_timing(int32_t enable, double *last_ms);
  * for the whole device, measured with CUDA events. */
 SDE_API int32_t sde_peak_probe(int32_t which, double *ops_per_s);
 
-/* Page-locked host memory for results: an output array (SdeOut.xx with
+/* Page-locked host memory for results; stands where sdepy allocates the
+ * result array with numpy (sdepy/integration.py:550, np.full of NaN in
+ * paths_generator.__call__).  An output array (SdeOut.xx with
  * on_device == 0) that lives in such memory is written by the kernel
- * directly over the host link, with no device buffer and no separate copy. */
+ * directly over the host link, with no device buffer and no separate copy;
+ * other host memory goes through a device buffer and one copy. */
 SDE_API int32_t sde_host_alloc(int64_t bytes, void **ptr);
 SDE_API int32_t sde_host_free(void *ptr);
 
