@@ -22,6 +22,13 @@ def golden_cases():
                   if not f.endswith('_exact.npz'))
 
 
+def quant_cases():
+    """Fixtures of the reference's quantitative tests (make_quant.py)."""
+    import glob
+    return sorted(glob.glob(os.path.join(GOLDEN, 'quant2_*.npz')) +
+                  glob.glob(os.path.join(GOLDEN, 'params2_*.npz')))
+
+
 @pytest.fixture(scope='session')
 def lib():
     """The native library (built if missing); GPU tests only."""

@@ -35,3 +35,115 @@ def oracle_paths(clib, proc, timeline, seed, stream=0):
         assert rc == 0
         info = {'neg': neg, 'jump_count': jc, 'row_jumps': rj}
     return xx.reshape((rows,) + tuple(proc.xshape) + (proc.paths,)), info
+
+
+# ---------------------------------------------------------------------------
+# the reference's quantitative tests (sdepy/tests/test_quant.py, contexts
+# 'quant2' and 'params2'; fixtures from tests/golden/make_quant.py)
+# ---------------------------------------------------------------------------
+def noise_digest(calls, wshape, paths):
+    """SHA-256 of recorded source realisations ``{id: [(t, dt, value, dn)]}``
+    in source-id order (dj with its counts, then dw), each step broadcast to
+    wshape + (paths,)."""
+    import hashlib
+    h = hashlib.sha256()
+    for sid in sorted(calls):
+        for c in calls[sid]:
+            h.update(np.ascontiguousarray(np.broadcast_to(c[2], tuple(wshape) + (paths,)), dtype=float).tobytes())
+            if sid == 'dj':
+                h.update(np.ascontiguousarray(np.broadcast_to(c[3], tuple(wshape) + (paths,)),
+                                              dtype=np.int64).tobytes())
+    return h.hexdigest()
+
+
+class Recording:
+    """Source-protocol wrapper recording every realisation."""
+
+    def __init__(self, src):
+        self.src, self.paths, self.vshape = src, src.paths, src.vshape
+        self.calls = []
+
+    def __call__(self, t, dt):
+        v = self.src(t, dt)
+        dn = getattr(self.src, 'dn_value', None)
+        self.calls.append((t, dt, np.array(v), None if dn is None else np.array(dn)))
+        return v
+
+    @property
+    def dn_value(self):
+        return self.src.dn_value
+
+
+def quant_stats_errors(x, z):
+    """Relative (mean, max) errors of the fixture's statistics of ``x``
+    against its closed forms, as check_values computes them in mode 'rel'
+    (sdepy/tests/test_quant.py:66-75): quant2 -- pmean / pstd / pvar over
+    the timeline from its second point (:305-320); params2 -- pmean / pstd
+    at the last point across the parameter sweep (:555-565).  Heston
+    statistics are of log x."""
+    xs = np.asarray(x, dtype=float)
+    if str(z['context']) == 'params2':
+        xs = xs[-1]
+        xs = xs.reshape(xs.shape[0], -1)   # (K, paths); Heston's extra axis dropped
+    else:
+        xs = xs[1:]
+    if int(z['log']):
+        xs = np.log(xs)
+    real = {'mean': xs.mean(axis=-1), 'std': xs.std(axis=-1), 'var': xs.var(axis=-1)}
+    out = {}
+    for name in ('mean', 'std', 'var'):
+        if 'closed_' + name not in z:
+            continue
+        exp = z['closed_' + name]
+        delta = np.abs(exp - real[name].reshape(exp.shape))/exp
+        out[name] = (float(delta.mean()), float(delta.max()))
+    return out
+
+
+def quant_sources(cls, params, wshape, paths, rng):
+    """The stochasticity sources sdepy's preset ``cls`` builds by default,
+    restated by the oracle and drawing from ``rng``: a Wiener source
+    (correlated along the last axis by ``rho`` for Heston / Hull-White) and,
+    for jump models, the compound Poisson source of the preset's law."""
+    from oracle import euler
+    corr = None
+    rho = params.get('rho')
+    if rho is not None and cls in ('heston_process', 'full_heston_process', 'hull_white_process'):
+        r = float(np.asarray(rho).reshape(-1)[0])
+        corr = np.array([[1., r], [r, 1.]])
+    dw = euler.NumpyWiener(rng, paths, tuple(wshape), corr=corr, dtype=float)
+    dj = None
+    if 'jumpdiff' in cls:
+        p = {k: np.asarray(v, dtype=float) for k, v in params.items() if k not in ('vshape', 'factors')}
+        dj = euler.NumpyCPoisson(rng, paths, tuple(wshape), p['lam'], euler.law_rvs(cls, p), dtype=float)
+    return dw, dj
+
+
+def quant_params(z):
+    """The fixture's keyword arguments (vshape as a tuple, factors)."""
+    import json
+    kw = {k: (v if k == 'vshape' else np.asarray(v, dtype=float))
+          for k, v in json.loads(str(z['kw'])).items()}
+    kw.update(json.loads(str(z['extra'])))
+    if isinstance(kw.get('vshape'), list):
+        kw['vshape'] = tuple(kw['vshape'])
+    return kw
+
+
+def quant_kwargs(z, record=False):
+    """Keyword arguments of the drop-in class for a quant2 / params2 fixture,
+    with the reference's default sources restated and seeded as its test
+    seeds them (RandomState(1234)); with ``record`` the sources are wrapped
+    in Recording."""
+    kw = quant_params(z)
+    paths = int(z['paths'])
+    dw, dj = quant_sources(str(z['cls']), kw, tuple(z['wshape']), paths, np.random.RandomState(1234))
+    if record:
+        dw = Recording(dw)
+        dj = None if dj is None else Recording(dj)
+    kw['dw'] = dw
+    if dj is not None:
+        kw['dj'] = dj
+        for k in ('a', 'b', 'pa', 'lam'):   # the source carries the jump law
+            kw.pop(k, None)
+    return kw

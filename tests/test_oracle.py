@@ -8,7 +8,8 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, golden_cases
+from conftest import GOLDEN, golden_cases, quant_cases
+from helpers import Recording, noise_digest, quant_params, quant_sources, quant_stats_errors
 from oracle import euler
 
 
@@ -27,6 +28,33 @@ def test_numpy_oracle_reproduces_reference(path):
         np.testing.assert_array_equal(info['jump_rate'], z['jump_rate'])
     if 'negative_y_count' in z:
         np.testing.assert_array_equal(info['negative_y_count'], z['negative_y_count'])
+
+
+@pytest.mark.parametrize('path', quant_cases(), ids=os.path.basename)
+def test_numpy_oracle_reproduces_quant_errors(path):
+    # sdepy/tests/test_quant.py quant2 (:305-320) and params2 (:555-565):
+    # 100 paths from RandomState(1234).  The oracle's restated sources draw
+    # exactly the reference's increments (digest of the recorded ones), the
+    # oracle integrates them to the reference's paths, and the statistics
+    # give the errors the reference realises and records
+    # (sdepy/tests/cfr/quant2_err_expected.txt, params2_err_expected.txt)
+    z = np.load(path)
+    params = quant_params(z)
+    vshape = params.pop('vshape', ())
+    paths = int(z['paths'])
+    dw, dj = quant_sources(str(z['cls']), params, tuple(z['wshape']), paths, np.random.RandomState(1234))
+    dw = Recording(dw)
+    dj = None if dj is None else Recording(dj)
+    res, _ = euler.integrate(str(z['cls']), params, z['timeline'], paths=paths, vshape=vshape,
+                             steps=int(z['steps']), dw=dw, dj=dj)
+    calls = {'dw': dw.calls} if dj is None else {'dw': dw.calls, 'dj': dj.calls}
+    assert noise_digest(calls, tuple(z['wshape']), paths) == str(z['noise_sha256'])
+    x = res[0] if isinstance(res, tuple) else res
+    np.testing.assert_array_equal(x, z['xx'])
+    for name, (m, M) in quant_stats_errors(x, z).items():
+        np.testing.assert_allclose((m, M), z['ref_err_' + name], rtol=1e-12)
+        if int(z['file_matches']):
+            np.testing.assert_allclose((m, M), z['file_err_' + name], rtol=1e-4)
 
 
 def test_numpy_oracle_known_answer():
