@@ -13,6 +13,7 @@ from .integration import (
     heston_process, jumpdiff_process, merton_jumpdiff_process,
     kou_jumpdiff_process)
 from . import infrastructure
+from .montecarlo import montecarlo   # the class, as sdepy exports it
 
 __version__ = '0.1.0'
 
@@ -22,5 +23,5 @@ __all__ = [
     'wiener_process', 'lognorm_process', 'ornstein_uhlenbeck_process',
     'hull_white_process', 'hull_white_1factor_process',
     'full_heston_process', 'heston_process', 'jumpdiff_process',
-    'merton_jumpdiff_process', 'kou_jumpdiff_process',
+    'merton_jumpdiff_process', 'kou_jumpdiff_process', 'montecarlo',
 ]

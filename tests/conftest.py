@@ -26,6 +26,7 @@ def quant_cases():
     """Fixtures of the reference's quantitative tests (make_quant.py)."""
     import glob
     return sorted(glob.glob(os.path.join(GOLDEN, 'quant2_*.npz')) +
+                  glob.glob(os.path.join(GOLDEN, 'quant5_*.npz')) +
                   glob.glob(os.path.join(GOLDEN, 'params2_*.npz')))
 
 

@@ -74,29 +74,36 @@ class Recording:
         return self.src.dn_value
 
 
-def quant_stats_errors(x, z):
-    """Relative (mean, max) errors of the fixture's statistics of ``x``
-    against its closed forms, as check_values computes them in mode 'rel'
-    (sdepy/tests/test_quant.py:66-75): quant2 -- pmean / pstd / pvar over
-    the timeline from its second point (:305-320); params2 -- pmean / pstd
-    at the last point across the parameter sweep (:555-565).  Heston
+def quant_realized(x, z):
+    """The statistics the reference's test takes of ``x``: quant2 / quant5
+    -- pmean / pstd / pvar over paths at every timeline point from the
+    second (sdepy/tests/test_quant.py:305-320); params2 -- pmean / pstd at
+    the last point across the parameter sweep (:555-565).  Heston
     statistics are of log x."""
     xs = np.asarray(x, dtype=float)
-    if str(z['context']) == 'params2':
+    if str(z['context']).startswith('params'):
         xs = xs[-1]
         xs = xs.reshape(xs.shape[0], -1)   # (K, paths); Heston's extra axis dropped
     else:
         xs = xs[1:]
     if int(z['log']):
         xs = np.log(xs)
-    real = {'mean': xs.mean(axis=-1), 'std': xs.std(axis=-1), 'var': xs.var(axis=-1)}
+    return {'mean': xs.mean(axis=-1), 'std': xs.std(axis=-1), 'var': xs.var(axis=-1)}
+
+
+def quant_stats_errors(x, z):
+    """Relative (mean, max) errors of the fixture's statistics of ``x``
+    against its closed forms, as check_values computes them in mode 'rel'
+    (sdepy/tests/test_quant.py:66-75), with the realised statistics."""
+    real = quant_realized(x, z)
     out = {}
     for name in ('mean', 'std', 'var'):
         if 'closed_' + name not in z:
             continue
         exp = z['closed_' + name]
-        delta = np.abs(exp - real[name].reshape(exp.shape))/exp
-        out[name] = (float(delta.mean()), float(delta.max()))
+        r = real[name].reshape(exp.shape)
+        delta = np.abs(exp - r)/exp
+        out[name] = (float(delta.mean()), float(delta.max()), r)
     return out
 
 

@@ -1,19 +1,20 @@
 """The reference's quantitative tests on the GPU drop-ins
-(sdepy/tests/test_quant.py, contexts 'quant2' :305-320 and 'params2'
-:555-565).
+(sdepy/tests/test_quant.py: quant2 / quant5 :305-320, params2 :555-565,
+blackscholes :593-640).
 
-sdepy seeds RandomState(1234), integrates 100 paths of each preset (quant2:
-50 points in [1, 3]; params2: one parameter swept over 20 values along a
-vshape axis, points (1, 2, 3)) and records the relative errors of the
-sample mean / std / var against the closed forms in
-sdepy/tests/cfr/quant2_err_expected.txt and params2_err_expected.txt; its
-test fails when a realised error exceeds the recorded one by more than 1 %
+sdepy seeds RandomState(1234) and integrates each preset: quant2 / quant5
+with 100 / 100_000 paths on 50 points in [1, 3]; params2 with 100 paths and
+one parameter swept over 20 values along a vshape axis, points (1, 2, 3);
+blackscholes with 100_000 lognormal paths on (0, 2).  It records the
+relative errors of the sample mean / std / var against the closed forms in
+sdepy/tests/cfr/<context>_err_expected.txt, and its test fails when a
+realised error exceeds the recorded one by more than 1 %
 (sdepy/tests/shared.py:263-284).  Here the same RandomState draws, through
 the oracle's restatement of sdepy's sources, are injected into the FP64
-GPU kernels: the paths match the reference's to 1e-12 and the errors match
-those the reference realises to 1e-9, and the recorded ones to their
-printed precision (params2 heston1_k excepted: the reference itself no
-longer realises its recorded errors there, see tests/golden/make_quant.py).
+GPU kernels: paths (100-path cases) match the reference's to 1e-12, the
+statistics to 1e-11, the errors those the reference realises to 1e-9 and
+the recorded ones to their printed precision (params2 heston1_k excepted:
+the reference itself no longer realises its recorded errors there).
 """
 import os
 
@@ -21,8 +22,8 @@ import numpy as np
 import pytest
 
 import sdepy_gb300 as sg
-from conftest import quant_cases
-from helpers import quant_kwargs, quant_stats_errors
+from conftest import GOLDEN, quant_cases
+from helpers import quant_kwargs, quant_sources, quant_stats_errors
 
 pytestmark = pytest.mark.gpu
 
@@ -34,13 +35,34 @@ def test_quant_errors_reproduced(lib, path):
     P = cls(paths=int(z['paths']), steps=int(z['steps']), **quant_kwargs(z))
     out = P(z['timeline'])
     x = out[0] if isinstance(out, tuple) else out
-    ref = z['xx']
-    assert x.shape == ref.shape
-    assert np.max(np.abs(np.asarray(x) - ref)/np.maximum(np.abs(ref), 1.)) <= 1e-12
-    for name, (m, M) in quant_stats_errors(x, z).items():
+    if 'xx' in z:
+        ref = z['xx']
+        assert x.shape == ref.shape
+        assert np.max(np.abs(np.asarray(x) - ref)/np.maximum(np.abs(ref), 1.)) <= 1e-12
+    for name, (m, M, real) in quant_stats_errors(x, z).items():
+        np.testing.assert_allclose(real, z['ref_stat_' + name], rtol=1e-11)
         np.testing.assert_allclose((m, M), z['ref_err_' + name], rtol=1e-9)
         if int(z['file_matches']):
             fm, fM = z['file_err_' + name]
             np.testing.assert_allclose((m, M), (fm, fM), rtol=1e-4)
             # the reference test's own pass criterion
             assert m < fm*1.01 and M < fM*1.01
+
+
+def test_blackscholes_reproduced(lib):
+    z = np.load(os.path.join(GOLDEN, 'bs_blackscholes.npz'))
+    paths = int(z['paths'])
+    dw, _ = quant_sources('lognorm_process', {}, tuple(z['wshape']), paths, np.random.RandomState(1234))
+    kw = {k: float(v) for k, v in __import__('json').loads(str(z['kw'])).items()}
+    P = sg.lognorm_process(paths=paths, dw=dw, **kw)
+    X = P(z['timeline'])
+    assert P.info['computed_steps'] == int(z['computed_steps'])
+    np.testing.assert_allclose(np.asarray(X[-1]).sum(), float(z['x_last_sum']), rtol=1e-12)
+    r, T = float(z['r']), float(z['T'])
+    call = sg.montecarlo(np.maximum(X[-1] - float(z['Kc']), 0)*np.exp(-r*T))
+    put = sg.montecarlo(np.maximum(float(z['Kp']) - X[-1], 0)*np.exp(-r*T))
+    np.testing.assert_allclose([call.mean(), call.stderr()], [z['call_mean'], z['call_stderr']], rtol=1e-10)
+    np.testing.assert_allclose([put.mean(), put.stderr()], [z['put_mean'], z['put_stderr']], rtol=1e-10)
+    # the reference test's criterion
+    assert abs(float(z['bscall']) - call.mean())/call.stderr() < 3
+    assert abs(float(z['bsput']) - put.mean())/put.stderr() < 3

@@ -32,15 +32,16 @@ def test_numpy_oracle_reproduces_reference(path):
 
 @pytest.mark.parametrize('path', quant_cases(), ids=os.path.basename)
 def test_numpy_oracle_reproduces_quant_errors(path):
-    # sdepy/tests/test_quant.py quant2 (:305-320) and params2 (:555-565):
-    # 100 paths from RandomState(1234).  The oracle's restated sources draw
-    # exactly the reference's increments (digest of the recorded ones), the
-    # oracle integrates them to the reference's paths, and the statistics
-    # give the errors the reference realises and records
-    # (sdepy/tests/cfr/quant2_err_expected.txt, params2_err_expected.txt)
+    # sdepy/tests/test_quant.py quant2 / quant5 (:305-320) and params2
+    # (:555-565): 100 or 100_000 paths from RandomState(1234).  The oracle's
+    # restated sources draw exactly the reference's increments (digest of the
+    # recorded ones), the oracle integrates them to the reference's paths,
+    # and the statistics give the errors the reference realises and records
+    # (sdepy/tests/cfr/<context>_err_expected.txt)
     z = np.load(path)
     params = quant_params(z)
     vshape = params.pop('vshape', ())
+    vshape = (vshape,) if isinstance(vshape, int) else tuple(vshape)
     paths = int(z['paths'])
     dw, dj = quant_sources(str(z['cls']), params, tuple(z['wshape']), paths, np.random.RandomState(1234))
     dw = Recording(dw)
@@ -50,11 +51,26 @@ def test_numpy_oracle_reproduces_quant_errors(path):
     calls = {'dw': dw.calls} if dj is None else {'dw': dw.calls, 'dj': dj.calls}
     assert noise_digest(calls, tuple(z['wshape']), paths) == str(z['noise_sha256'])
     x = res[0] if isinstance(res, tuple) else res
-    np.testing.assert_array_equal(x, z['xx'])
-    for name, (m, M) in quant_stats_errors(x, z).items():
-        np.testing.assert_allclose((m, M), z['ref_err_' + name], rtol=1e-12)
+    if 'xx' in z:
+        np.testing.assert_array_equal(x, z['xx'])
+    for name, (m, M, real) in quant_stats_errors(x, z).items():
+        np.testing.assert_allclose(real, z['ref_stat_' + name], rtol=1e-13)
+        np.testing.assert_allclose((m, M), z['ref_err_' + name], rtol=1e-10)
         if int(z['file_matches']):
             np.testing.assert_allclose((m, M), z['file_err_' + name], rtol=1e-4)
+
+
+def test_numpy_oracle_reproduces_blackscholes():
+    # sdepy/tests/test_quant.py:593-640: call and put on 100_000 lognormal
+    # paths from RandomState(1234), within 3 standard errors of bscall/bsput
+    z = np.load(os.path.join(GOLDEN, 'bs_blackscholes.npz'))
+    paths = int(z['paths'])
+    dw, _ = quant_sources('lognorm_process', {}, tuple(z['wshape']), paths, np.random.RandomState(1234))
+    dw = Recording(dw)
+    x, info = euler.integrate('lognorm_process', json.loads(str(z['kw'])), z['timeline'], paths=paths, dw=dw)
+    assert noise_digest({'dw': dw.calls}, tuple(z['wshape']), paths) == str(z['noise_sha256'])
+    assert info['computed_steps'] == int(z['computed_steps'])
+    np.testing.assert_allclose(x[-1].sum(), float(z['x_last_sum']), rtol=1e-14)
 
 
 def test_numpy_oracle_known_answer():
