@@ -86,14 +86,19 @@ __device__ __forceinline__ float path_lin(const DevInst &I, const PhiloxKey &key
     float a = I.x0[0], sdw = 0.f, sja = 0.f, sjb = 0.f;
     const bool jumps = I.jump_law != SDE_JUMP_NONE;
     const uint4 pre = philox_round0(p, 0u, I.stream, key);
+    // the step loop's coefficients in registers (the loop's global writes
+    // would otherwise force a reload of every field each step)
+    const float b0 = I.b[0], c0 = I.c[0], sq = I.sq;
+    const long long thr = I.thr;
+    const int n_steps = I.n_steps;
 #pragma unroll 1
-    for (int k = 0; k < I.n_steps; ++k) {
+    for (int k = 0; k < n_steps; ++k) {
         const uint4 r = philox_from_round0(pre, (uint32_t)k, key);
         float z0, z1;
         Rng<float>::normal2(r.x, r.y, z0, z1);
-        a = a + I.b[0] + I.c[0] * z0;
-        sdw += I.sq * z0;
-        if (jumps && (long long)r.z > I.thr) {
+        a = a + b0 + c0 * z0;
+        sdw += sq * z0;
+        if (jumps && (long long)r.z > thr) {
             const int cnt = poisson_tail(r.z, I.p0d, I.lamdt, err);
             for (int j = 0; j < cnt; ++j) {
                 const uint4 q = philox4x32_10(make_uint4(p, (uint32_t)k, 0x80000000u | (uint32_t)j, I.stream), key);
@@ -127,21 +132,31 @@ __device__ __forceinline__ float path_ou(const DevInst &I, const PhiloxKey &key,
     const float kdt = I.d[0];
     const int W = I.nvars;
     const uint4 pre = philox_round0(p, 0u, I.stream, key);
+    // the step loop's coefficients in registers
+    float cd[4], cb[4], cc[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        cd[m] = I.d[m];
+        cb[m] = I.b[m];
+        cc[m] = I.c[m];
+    }
+    const float th0 = I.p1[0], dt = I.dt, sq = I.sq;
+    const int n_steps = I.n_steps;
 #pragma unroll 1
-    for (int k = 0; k < I.n_steps; ++k) {
+    for (int k = 0; k < n_steps; ++k) {
         const uint4 r = philox_from_round0(pre, (uint32_t)k, key);
         float z[4];
         Rng<float>::normal2(r.x, r.y, z[0], z[1]);
         if (W > 2) Rng<float>::normal2(r.z, r.w, z[2], z[3]);
         else z[2] = z[3] = 0.f;
-        const float dth = I.p1[0] - x[0];
-        tk = fmaf(rho0, tk, dth * I.dt);
+        const float dth = th0 - x[0];
+        tk = fmaf(rho0, tk, dth * dt);
         tth = fmaf(rho0, tth, kdt);
-        tsg = fmaf(rho0, tsg, I.sq * z[0]);
+        tsg = fmaf(rho0, tsg, sq * z[0]);
         tx = rho0 * tx;
 #pragma unroll
         for (int m = 0; m < 4; ++m)
-            if (m < W) x[m] = x[m] + fmaf(-I.d[m], x[m], I.b[m]) + I.c[m] * z[m];
+            if (m < W) x[m] = x[m] + fmaf(-cd[m], x[m], cb[m]) + cc[m] * z[m];
     }
     g[0] = tx;
     g[1] = tk;
@@ -162,14 +177,16 @@ __device__ __forceinline__ float path_heston(const DevInst &I, const PhiloxKey &
     ty[3] = 1.f;
     const float mu = I.p0[0], sg = I.p1[0], kk = I.p0[1], th = I.p1[1], xi = I.p2[1];
     const float dt = I.dt, sq = I.sq;
+    const float chol10 = I.chol10, chol11 = I.chol11, rho_k = I.rho_k;
+    const int n_steps = I.n_steps;
     const uint4 pre = philox_round0(p, 0u, I.stream, key);
 #pragma unroll 1
-    for (int k = 0; k < I.n_steps; ++k) {
+    for (int k = 0; k < n_steps; ++k) {
         const uint4 r = philox_from_round0(pre, (uint32_t)k, key);
         float z0, z1;
         Rng<float>::normal2(r.x, r.y, z0, z1);
         const float dW1 = z0 * sq;
-        const float dW2 = (I.chol10 * z0 + I.chol11 * z1) * sq;
+        const float dW2 = (chol10 * z0 + chol11 * z1) * sq;
         const float yp = fmaxf(y, 0.f);
         const float s = approx_sqrt(yp);
         float Ay = 0.f, By = 1.f;
@@ -186,7 +203,7 @@ __device__ __forceinline__ float path_heston(const DevInst &I, const PhiloxKey &
         ey[4] = (th - yp) * dt;
         ey[5] = kk * dt;
         ey[6] = s * dW2;
-        ey[7] = xi * s * (z0 + I.rho_k * z1) * sq;
+        ey[7] = xi * s * (z0 + rho_k * z1) * sq;
 #pragma unroll
         for (int j = 0; j < NB_GRAD; ++j) {
             const float nta = ta[j] + Ay * ty[j] + ea[j];
