@@ -14,7 +14,10 @@
  *     sdepy/integration.py:2066-2747) and sdepy's output transforms.
  * The counter layout is (path, step + offset, group << 8 | call, stream) for
  * normals and Poisson uniforms and (path, step + offset,
- * 0x80000000 | var << 12 | jump, stream) for jump sizes.
+ * 0x80000000 | var << 12 | jump, stream) for jump sizes.  Groups of one
+ * variable draw one call per two steps: the call of even step k gives its
+ * Box-Muller pair's z0 to step k and z1 to step k + 1, and its words z and
+ * w are the Poisson uniforms of steps k and k + 1.
  *
  * Compiled with -ffp-contract=off so that every product and sum rounds as
  * written.  Pinned by the published Philox-4x32-10 known-answer vectors and by
@@ -144,6 +147,8 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
             double st[SDE_MAX_GROUP], z[SDE_MAX_GROUP + 1], dW[SDE_MAX_GROUP], dJ[SDE_MAX_GROUP];
             int negc[SDE_MAX_GROUP] = {0}, jc[SDE_MAX_GROUP] = {0};
             int64_t row_jc = 0;
+            double pz0 = 0.0, pz1 = 0.0;   /* one-variable groups: the even step's pair */
+            uint32_t pw0 = 0, pw1 = 0;
             for (int m = 0; m < M; ++m) st[m] = s->x0[gi * M + m];
             for (int k = -1; k < n_steps; ++k) {
                 if (k >= 0) {
@@ -153,11 +158,25 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
                     const int U = 2 * P + (jumps ? M : 0);
                     const int NC = (U + 3) / 4;
                     uint32_t u[4 * ((2 * SDE_MAX_GROUP + 2 + 3) / 4) + 4];
-                    for (int c = 0; c < NC; ++c) {
-                        const uint32_t ctr[4] = {(uint32_t)p, c1, ((uint32_t)gi << 8) | (uint32_t)c, s->stream};
-                        oracle_philox(ctr, key, &u[4 * c]);
+                    if (M == 1) {
+                        if ((k & 1) == 0) {
+                            const uint32_t ctr[4] = {(uint32_t)p, c1, (uint32_t)gi << 8, s->stream};
+                            uint32_t r[4];
+                            oracle_philox(ctr, key, r);
+                            oracle_normal2(r[0], r[1], &pz0, &pz1);
+                            pw0 = r[2];
+                            pw1 = r[3];
+                        }
+                        z[0] = (k & 1) ? pz1 : pz0;
+                        u[2] = (k & 1) ? pw1 : pw0;   /* the Poisson word, index 2P + m */
+                    } else {
+                        for (int c = 0; c < NC; ++c) {
+                            const uint32_t ctr[4] = {(uint32_t)p, c1, ((uint32_t)gi << 8) | (uint32_t)c, s->stream};
+                            oracle_philox(ctr, key, &u[4 * c]);
+                        }
+                        for (int q = 0; q < P; ++q)
+                            oracle_normal2(u[2 * q], u[2 * q + 1], &z[2 * q], &z[2 * q + 1]);
                     }
-                    for (int q = 0; q < P; ++q) oracle_normal2(u[2 * q], u[2 * q + 1], &z[2 * q], &z[2 * q + 1]);
                     for (int m = 0; m < M; ++m) {
                         if (s->corr) {
                             double acc = L[m * M + 0] * z[0];

@@ -100,8 +100,9 @@ def single_spec(s, precision=_lib.FP32):
     if s.model == HESTON:
         G, M, out = 1, 2, _lib.OUT_HESTON_X
     elif s.model == OU:
-        M = 4 if W % 4 == 0 else (2 if W % 2 == 0 else 1)
-        G, out = W//M, _lib.OUT_STATE
+        # one group of W <= 4 states: the batch kernel's draws (one Philox
+        # call per step, or per two steps for one state)
+        G, M, out = 1, W, _lib.OUT_STATE
     else:
         G, M, out = 1, 1, (_lib.OUT_EXP if s.out_exp else _lib.OUT_STATE)
     x0 = np.array([s.x0[m] for m in range(W)])

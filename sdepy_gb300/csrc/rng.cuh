@@ -11,6 +11,8 @@
 //   c2 = (group << 8) | call      (normals, then Poisson uniforms)
 //      = 0x80000000 | (var << 12) | jump   (jump sizes)
 //   c3 = stream (call / instance id);  key = 64-bit seed.
+// Groups of one state variable use one call per two steps (the even
+// step's): see PairedSteps in sde_kernels.cuh.
 //
 // Uniforms: u = (x + 0.5) * 2^-32 in (0, 1) for a 32-bit word x.
 // Normals (Box-Muller) from a word pair (a, b):

@@ -194,6 +194,21 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
 #pragma unroll
             for (int j = 0; j < NGV; ++j) gr[m][j] = R(0);
         const PathPre<NCMAX> pre(key, (uint32_t)p, (uint32_t)g, a.stream);
+        PairedSteps<R> pair;   // groups of one variable (MAXM == 1)
+        // the words, normals and increments of step k, exactly as the
+        // forward kernel draws them
+        auto noise = [&](int k, R sq, uint32_t (&u)[4 * NCMAX], R (&z)[MAXM], R (&dW)[MAXM]) {
+            if constexpr (MAXM == 1) {
+                uint32_t pw;
+                pair.get(key, pre, k, a.step_offset, z[0], pw);
+                u[0] = u[1] = u[3] = 0u;
+                u[2] = pw;   // the Poisson word, index 2P + m with P = 1, m = 0
+            } else {
+                step_words<MAXM, JUMPS>(key, pre, (uint32_t)k + a.step_offset, NC, u);
+                words_to_normals<R, MAXM>(u, z);
+            }
+            correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
+        };
         R val;
         if (MODEL == SDE_MODEL_LINEAR) {
             // ---- constant adjoint: one forward sweep ------------------------------
@@ -205,10 +220,8 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                 const R dt = a.dt[k], sq = a.sqdt[k];
                 const uint32_t c1w = (uint32_t)k + a.step_offset;
                 uint32_t u[4 * NCMAX];
-                step_words<MAXM, JUMPS>(key, pre, c1w, NC, u);
                 R z[MAXM], dW[MAXM];
-                words_to_normals<R, MAXM>(u, z);
-                correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
+                noise(k, sq, u, z, dW);
                 sdt = sdt + dt;
 #pragma unroll
                 for (int m = 0; m < MAXM; ++m) {
@@ -261,10 +274,8 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                 }
                 const R sq = a.sqdt[k];
                 uint32_t u[4 * NCMAX];
-                step_words<MAXM, JUMPS>(key, pre, (uint32_t)k + a.step_offset, NC, u);
                 R z[MAXM], dW[MAXM];
-                words_to_normals<R, MAXM>(u, z);
-                correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
+                noise(k, sq, u, z, dW);
                 fwd_step<R, MODEL, MAXM>(c0, c1, c2, a.dt[k], dW, st);
             }
             R xb[MAXM];
@@ -278,10 +289,8 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                 for (int k = k0; k < k1; ++k) {
                     const R sq = a.sqdt[k];
                     uint32_t u[4 * NCMAX];
-                    step_words<MAXM, JUMPS>(key, pre, (uint32_t)k + a.step_offset, NC, u);
                     R z[MAXM], dW[MAXM];
-                    words_to_normals<R, MAXM>(u, z);
-                    correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
+                    noise(k, sq, u, z, dW);
 #pragma unroll
                     for (int m = 0; m < MAXM; ++m) {
                         bx[k - k0][m] = st[m];

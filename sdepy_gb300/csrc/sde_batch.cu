@@ -85,7 +85,9 @@ __device__ __forceinline__ float path_lin(const DevInst &I, const PhiloxKey &key
                                           int32_t *err) {
     float a = I.x0[0], sdw = 0.f, sja = 0.f, sjb = 0.f;
     const bool jumps = I.jump_law != SDE_JUMP_NONE;
-    const uint4 pre = philox_round0(p, 0u, I.stream, key);
+    // one variable: one Philox call per two steps, as the forward kernel
+    const PathPre<1> pre(key, p, 0u, I.stream);
+    PairedSteps<float> pair;
     // the step loop's coefficients in registers (the loop's global writes
     // would otherwise force a reload of every field each step)
     const float b0 = I.b[0], c0 = I.c[0], sq = I.sq;
@@ -93,13 +95,13 @@ __device__ __forceinline__ float path_lin(const DevInst &I, const PhiloxKey &key
     const int n_steps = I.n_steps;
 #pragma unroll 1
     for (int k = 0; k < n_steps; ++k) {
-        const uint4 r = philox_from_round0(pre, (uint32_t)k, key);
-        float z0, z1;
-        Rng<float>::normal2(r.x, r.y, z0, z1);
+        float z0;
+        uint32_t pw;
+        pair.get(key, pre, k, 0u, z0, pw);
         a = a + b0 + c0 * z0;
         sdw += sq * z0;
-        if (jumps && (long long)r.z > thr) {
-            const int cnt = poisson_tail(r.z, I.p0d, I.lamdt, err);
+        if (jumps && (long long)pw > thr) {
+            const int cnt = poisson_tail(pw, I.p0d, I.lamdt, err);
             for (int j = 0; j < cnt; ++j) {
                 const uint4 q = philox4x32_10(make_uint4(p, (uint32_t)k, 0x80000000u | (uint32_t)j, I.stream), key);
                 float y0, y1;
@@ -131,7 +133,8 @@ __device__ __forceinline__ float path_ou(const DevInst &I, const PhiloxKey &key,
     const float rho0 = 1.f - I.d[0];
     const float kdt = I.d[0];
     const int W = I.nvars;
-    const uint4 pre = philox_round0(p, 0u, I.stream, key);
+    const PathPre<1> pre(key, p, 0u, I.stream);
+    PairedSteps<float> pair;   // one variable: one Philox call per two steps
     // the step loop's coefficients in registers
     float cd[4], cb[4], cc[4];
 #pragma unroll
@@ -144,11 +147,17 @@ __device__ __forceinline__ float path_ou(const DevInst &I, const PhiloxKey &key,
     const int n_steps = I.n_steps;
 #pragma unroll 1
     for (int k = 0; k < n_steps; ++k) {
-        const uint4 r = philox_from_round0(pre, (uint32_t)k, key);
         float z[4];
-        Rng<float>::normal2(r.x, r.y, z[0], z[1]);
-        if (W > 2) Rng<float>::normal2(r.z, r.w, z[2], z[3]);
-        else z[2] = z[3] = 0.f;
+        if (W == 1) {
+            uint32_t pw;
+            pair.get(key, pre, k, 0u, z[0], pw);
+            z[1] = z[2] = z[3] = 0.f;
+        } else {
+            const uint4 r = philox_from_round0(pre.r0[0], (uint32_t)k, key);
+            Rng<float>::normal2(r.x, r.y, z[0], z[1]);
+            if (W > 2) Rng<float>::normal2(r.z, r.w, z[2], z[3]);
+            else z[2] = z[3] = 0.f;
+        }
         const float dth = th0 - x[0];
         tk = fmaf(rho0, tk, dth * dt);
         tth = fmaf(rho0, tth, kdt);

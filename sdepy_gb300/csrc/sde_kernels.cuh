@@ -327,6 +327,34 @@ struct PathPre {
     }
 };
 
+// Groups of one state variable draw one Philox call per two steps: the
+// call of even step k (counter (p, k + leg offset, g << 8, stream)) gives
+// its Box-Muller pair's z0 to step k and z1 to step k + 1, and its words z
+// and w are the Poisson uniforms of steps k and k + 1.  The cache holds the
+// last call's values; any step order works (the adjoint starts segments at
+// odd steps).  SC as for words_to_normals.
+template <typename R, bool SC = false>
+struct PairedSteps {
+    int k0 = -2;          // even step of the cached call
+    R z0, z1;
+    uint32_t w0, w1;
+    __device__ __forceinline__ void get(const PhiloxKey &key, const PathPre<1> &pre, int k, uint32_t offset,
+                                        R &z, uint32_t &pword) {
+        const int ke = k & ~1;
+        if (ke != k0) {
+            const uint4 r = philox_from_round0(pre.r0[0], (uint32_t)ke + offset, key);
+            if (SC) Rng<R>::normal2_s(r.x, r.y, z0, z1);
+            else Rng<R>::normal2(r.x, r.y, z0, z1);
+            w0 = r.z;
+            w1 = r.w;
+            k0 = ke;
+        }
+        const bool odd = (k & 1) != 0;
+        z = odd ? z1 : z0;
+        pword = odd ? w1 : w0;
+    }
+};
+
 // Philox words of step k (c1w = step + leg offset): u[0 .. 2P) feed the
 // Box-Muller pairs, u[2P + m] is the Poisson uniform of state m (jump models)
 template <int MAXM, bool JUMPS>
@@ -603,6 +631,28 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                 for (int m = 0; m < MAXM; ++m) st[m] = (R)__ldg(a.tshift + (g * 2 + 1) * MAXM + m);
             }
             const PathPre<NCMAX> pre(key, (uint32_t)p, (uint32_t)g, a.stream);
+            PairedSteps<R, TAB> pair;   // groups of one variable (MAXM == 1)
+            // Poisson count of state m at step k from uniform word `word`, and
+            // the sum of its jump sizes
+            auto add_jumps = [&](int m, uint32_t word, int k, uint32_t c1w, R (&dJ)[MAXM]) {
+                const int w = g * M + m;
+                const int64_t tix = (int64_t)k * W + w;
+                if ((long long)word > a.thr[tix]) {
+                    const int cnt = poisson_tail(word, a.p0[tix], a.lamdt[tix], a.err);
+                    R S = R(0);
+                    for (int j = 0; j < cnt; ++j) {
+                        const uint4 r = philox4x32_10(
+                            make_uint4((uint32_t)p, c1w, 0x80000000u | ((uint32_t)w << 12) | (uint32_t)j, a.stream),
+                            key);
+                        const R y = jump_size<R>(a.jump_law, r, c3[m], c4[m], c5[m]);
+                        S = (j == 0) ? y : A::add(S, y);
+                    }
+                    dJ[m] = A::mul(a.sgn, S);
+                    const int sc = a.sgn < R(0) ? -cnt : cnt;
+                    jcnt[m] += sc;
+                    row_jc += (unsigned int)cnt;
+                }
+            };
             // increments of step k: injected, or drawn from Philox counters
             // (normals, correlated; Poisson counts and jump sums)
             auto draw = [&](int k, R sq, R (&dW)[MAXM], R (&dJ)[MAXM]) {
@@ -629,6 +679,14 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                     return;
                 }
                 const uint32_t c1w = (uint32_t)k + a.step_offset;
+                if constexpr (MAXM == 1) {
+                    R z;
+                    uint32_t pword;
+                    pair.get(key, pre, k, a.step_offset, z, pword);
+                    dW[0] = A::mul(z, sq);   // a 1x1 correlation factor is 1
+                    if (JUMPS) add_jumps(0, pword, k, c1w, dJ);
+                    return;
+                }
                 if constexpr (!JUMPS) {
                     step_increments<R, MAXM, TAB>(key, pre, c1w, NC, a.chol, a.has_corr, sq, dW);
                     return;
@@ -639,28 +697,8 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                 words_to_normals<R, MAXM, 4 * NCMAX, TAB>(u, z);
                 correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
 #pragma unroll
-                for (int m = 0; m < MAXM; ++m) {
-                    if (m < M) {
-                        const uint32_t word = pick_word(u, 2 * P + m);
-                        const int w = g * M + m;
-                        const int64_t tix = (int64_t)k * W + w;
-                        if ((long long)word > a.thr[tix]) {
-                            const int cnt = poisson_tail(word, a.p0[tix], a.lamdt[tix], a.err);
-                            R S = R(0);
-                            for (int j = 0; j < cnt; ++j) {
-                                const uint4 r = philox4x32_10(
-                                    make_uint4((uint32_t)p, c1w, 0x80000000u | ((uint32_t)w << 12) | (uint32_t)j,
-                                               a.stream), key);
-                                const R y = jump_size<R>(a.jump_law, r, c3[m], c4[m], c5[m]);
-                                S = (j == 0) ? y : A::add(S, y);
-                            }
-                            dJ[m] = A::mul(a.sgn, S);
-                            const int sc = a.sgn < R(0) ? -cnt : cnt;
-                            jcnt[m] += sc;
-                            row_jc += (unsigned int)cnt;
-                        }
-                    }
-                }
+                for (int m = 0; m < MAXM; ++m)
+                    if (m < M) add_jumps(m, pick_word(u, 2 * P + m), k, c1w, dJ);
             };
 
             if constexpr (TAB) {
