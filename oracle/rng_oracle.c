@@ -17,7 +17,9 @@
  * 0x80000000 | var << 12 | jump, stream) for jump sizes.  Groups of one
  * variable draw one call per two steps: the call of even step k gives its
  * Box-Muller pair's z0 to step k and z1 to step k + 1, and its words z and
- * w are the Poisson uniforms of steps k and k + 1.
+ * w are the Poisson uniforms of steps k and k + 1.  Groups of two
+ * variables without jumps also draw one call per two steps: words (x, y)
+ * give the normals of step k, words (z, w) those of step k + 1.
  *
  * Compiled with -ffp-contract=off so that every product and sum rounds as
  * written.  Pinned by the published Philox-4x32-10 known-answer vectors and by
@@ -149,6 +151,7 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
             int64_t row_jc = 0;
             double pz0 = 0.0, pz1 = 0.0;   /* one-variable groups: the even step's pair */
             uint32_t pw0 = 0, pw1 = 0;
+            double pz[4] = {0.0, 0.0, 0.0, 0.0};   /* two-variable groups without jumps */
             for (int m = 0; m < M; ++m) st[m] = s->x0[gi * M + m];
             for (int k = -1; k < n_steps; ++k) {
                 if (k >= 0) {
@@ -169,6 +172,16 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
                         }
                         z[0] = (k & 1) ? pz1 : pz0;
                         u[2] = (k & 1) ? pw1 : pw0;   /* the Poisson word, index 2P + m */
+                    } else if (M == 2 && !jumps) {
+                        if ((k & 1) == 0) {
+                            const uint32_t ctr[4] = {(uint32_t)p, c1, (uint32_t)gi << 8, s->stream};
+                            uint32_t r[4];
+                            oracle_philox(ctr, key, r);
+                            oracle_normal2(r[0], r[1], &pz[0], &pz[1]);
+                            oracle_normal2(r[2], r[3], &pz[2], &pz[3]);
+                        }
+                        z[0] = (k & 1) ? pz[2] : pz[0];
+                        z[1] = (k & 1) ? pz[3] : pz[1];
                     } else {
                         for (int c = 0; c < NC; ++c) {
                             const uint32_t ctr[4] = {(uint32_t)p, c1, ((uint32_t)gi << 8) | (uint32_t)c, s->stream};

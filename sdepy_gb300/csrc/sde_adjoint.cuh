@@ -194,15 +194,19 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
 #pragma unroll
             for (int j = 0; j < NGV; ++j) gr[m][j] = R(0);
         const PathPre<NCMAX> pre(key, (uint32_t)p, (uint32_t)g, a.stream);
-        PairedSteps<R> pair;   // groups of one variable (MAXM == 1)
+        constexpr int NZ = Paired<MAXM, JUMPS>::NZ;
+        PairedSteps<R, NZ == 0 ? 1 : NZ> pair;   // groups of one or two variables
         // the words, normals and increments of step k, exactly as the
         // forward kernel draws them
         auto noise = [&](int k, R sq, uint32_t (&u)[4 * NCMAX], R (&z)[MAXM], R (&dW)[MAXM]) {
-            if constexpr (MAXM == 1) {
+            if constexpr (NZ == 1) {
                 uint32_t pw;
                 pair.get(key, pre, k, a.step_offset, z[0], pw);
                 u[0] = u[1] = u[3] = 0u;
                 u[2] = pw;   // the Poisson word, index 2P + m with P = 1, m = 0
+            } else if constexpr (NZ == 2) {
+                pair.get(key, pre, k, a.step_offset, z[0], z[1]);
+                for (int i = 0; i < 4 * NCMAX; ++i) u[i] = 0u;
             } else {
                 step_words<MAXM, JUMPS>(key, pre, (uint32_t)k + a.step_offset, NC, u);
                 words_to_normals<R, MAXM>(u, z);

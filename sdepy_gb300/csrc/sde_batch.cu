@@ -87,7 +87,7 @@ __device__ __forceinline__ float path_lin(const DevInst &I, const PhiloxKey &key
     const bool jumps = I.jump_law != SDE_JUMP_NONE;
     // one variable: one Philox call per two steps, as the forward kernel
     const PathPre<1> pre(key, p, 0u, I.stream);
-    PairedSteps<float> pair;
+    PairedSteps<float, 1> pair;
     // the step loop's coefficients in registers (the loop's global writes
     // would otherwise force a reload of every field each step)
     const float b0 = I.b[0], c0 = I.c[0], sq = I.sq;
@@ -134,7 +134,9 @@ __device__ __forceinline__ float path_ou(const DevInst &I, const PhiloxKey &key,
     const float kdt = I.d[0];
     const int W = I.nvars;
     const PathPre<1> pre(key, p, 0u, I.stream);
-    PairedSteps<float> pair;   // one variable: one Philox call per two steps
+    // one or two variables: one Philox call per two steps
+    PairedSteps<float, 1> pair1;
+    PairedSteps<float, 2> pair2;
     // the step loop's coefficients in registers
     float cd[4], cb[4], cc[4];
 #pragma unroll
@@ -150,8 +152,11 @@ __device__ __forceinline__ float path_ou(const DevInst &I, const PhiloxKey &key,
         float z[4];
         if (W == 1) {
             uint32_t pw;
-            pair.get(key, pre, k, 0u, z[0], pw);
+            pair1.get(key, pre, k, 0u, z[0], pw);
             z[1] = z[2] = z[3] = 0.f;
+        } else if (W == 2) {
+            pair2.get(key, pre, k, 0u, z[0], z[1]);
+            z[2] = z[3] = 0.f;
         } else {
             const uint4 r = philox_from_round0(pre.r0[0], (uint32_t)k, key);
             Rng<float>::normal2(r.x, r.y, z[0], z[1]);
@@ -188,12 +193,12 @@ __device__ __forceinline__ float path_heston(const DevInst &I, const PhiloxKey &
     const float dt = I.dt, sq = I.sq;
     const float chol10 = I.chol10, chol11 = I.chol11, rho_k = I.rho_k;
     const int n_steps = I.n_steps;
-    const uint4 pre = philox_round0(p, 0u, I.stream, key);
+    const PathPre<1> pre(key, p, 0u, I.stream);
+    PairedSteps<float, 2> pair;   // one Philox call per two steps
 #pragma unroll 1
     for (int k = 0; k < n_steps; ++k) {
-        const uint4 r = philox_from_round0(pre, (uint32_t)k, key);
         float z0, z1;
-        Rng<float>::normal2(r.x, r.y, z0, z1);
+        pair.get(key, pre, k, 0u, z0, z1);
         const float dW1 = z0 * sq;
         const float dW2 = (chol10 * z0 + chol11 * z1) * sq;
         const float yp = fmaxf(y, 0.f);

@@ -327,14 +327,23 @@ struct PathPre {
     }
 };
 
-// Groups of one state variable draw one Philox call per two steps: the
-// call of even step k (counter (p, k + leg offset, g << 8, stream)) gives
-// its Box-Muller pair's z0 to step k and z1 to step k + 1, and its words z
-// and w are the Poisson uniforms of steps k and k + 1.  The cache holds the
-// last call's values; any step order works (the adjoint starts segments at
-// odd steps).  SC as for words_to_normals.
-template <typename R, bool SC = false>
-struct PairedSteps {
+// Groups of one or two state variables draw one Philox call per two
+// steps, the call of even step k (counter (p, k + leg offset, g << 8,
+// stream)):
+//   one variable  -- its Box-Muller pair gives z0 to step k and z1 to step
+//                    k + 1; words z and w are the Poisson uniforms of steps
+//                    k and k + 1;
+//   two variables (no jumps) -- the pair of words (x, y) gives the normals
+//                    of step k, the pair of words (z, w) those of step k + 1.
+// (With jumps, two-variable groups draw one call per step: words z, w are
+// their Poisson uniforms.)  The cache holds the last call's values; any
+// step order works (the adjoint starts segments at odd steps).  SC as for
+// words_to_normals.
+template <typename R, int NZ, bool SC = false>
+struct PairedSteps;
+
+template <typename R, bool SC>
+struct PairedSteps<R, 1, SC> {
     int k0 = -2;          // even step of the cached call
     R z0, z1;
     uint32_t w0, w1;
@@ -353,6 +362,37 @@ struct PairedSteps {
         z = odd ? z1 : z0;
         pword = odd ? w1 : w0;
     }
+};
+
+template <typename R, bool SC>
+struct PairedSteps<R, 2, SC> {
+    int k0 = -2;
+    R z[4];
+    __device__ __forceinline__ void get(const PhiloxKey &key, const PathPre<1> &pre, int k, uint32_t offset,
+                                        R &za, R &zb) {
+        const int ke = k & ~1;
+        if (ke != k0) {
+            const uint4 r = philox_from_round0(pre.r0[0], (uint32_t)ke + offset, key);
+            if (SC) {
+                Rng<R>::normal2_s(r.x, r.y, z[0], z[1]);
+                Rng<R>::normal2_s(r.z, r.w, z[2], z[3]);
+            } else {
+                Rng<R>::normal2(r.x, r.y, z[0], z[1]);
+                Rng<R>::normal2(r.z, r.w, z[2], z[3]);
+            }
+            k0 = ke;
+        }
+        const bool odd = (k & 1) != 0;
+        za = odd ? z[2] : z[0];
+        zb = odd ? z[3] : z[1];
+    }
+};
+
+// the paired-step scheme applies to groups of width MAXM == 1, and to
+// MAXM == 2 without jumps
+template <int MAXM, bool JUMPS>
+struct Paired {
+    static constexpr int NZ = (MAXM == 1) ? 1 : ((MAXM == 2 && !JUMPS) ? 2 : 0);
 };
 
 // Philox words of step k (c1w = step + leg offset): u[0 .. 2P) feed the
@@ -631,7 +671,8 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                 for (int m = 0; m < MAXM; ++m) st[m] = (R)__ldg(a.tshift + (g * 2 + 1) * MAXM + m);
             }
             const PathPre<NCMAX> pre(key, (uint32_t)p, (uint32_t)g, a.stream);
-            PairedSteps<R, TAB> pair;   // groups of one variable (MAXM == 1)
+            constexpr int NZ = Paired<MAXM, JUMPS>::NZ;
+            PairedSteps<R, NZ == 0 ? 1 : NZ, TAB> pair;   // groups of one or two variables
             // Poisson count of state m at step k from uniform word `word`, and
             // the sum of its jump sizes
             auto add_jumps = [&](int m, uint32_t word, int k, uint32_t c1w, R (&dJ)[MAXM]) {
@@ -679,12 +720,17 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                     return;
                 }
                 const uint32_t c1w = (uint32_t)k + a.step_offset;
-                if constexpr (MAXM == 1) {
+                if constexpr (NZ == 1) {
                     R z;
                     uint32_t pword;
                     pair.get(key, pre, k, a.step_offset, z, pword);
                     dW[0] = A::mul(z, sq);   // a 1x1 correlation factor is 1
                     if (JUMPS) add_jumps(0, pword, k, c1w, dJ);
+                    return;
+                } else if constexpr (NZ == 2) {
+                    R z[MAXM];
+                    pair.get(key, pre, k, a.step_offset, z[0], z[1]);
+                    correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
                     return;
                 }
                 if constexpr (!JUMPS) {
