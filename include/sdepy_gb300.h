@@ -173,6 +173,13 @@ SDE_API int32_t sde_timing(int32_t enable, double *last_ms);
  * for the whole device, measured with CUDA events. */
 SDE_API int32_t sde_peak_probe(int32_t which, double *ops_per_s);
 
+/* The Box-Muller transform the kernels apply to a pair of Philox words
+ * (a, b) -> (z0, z1), for n pairs in host memory (words[2i], words[2i+1]),
+ * in FP64 or FP32 (returned as doubles).  No counterpart in sdepy: it lets
+ * tests check the device transform against other implementations on
+ * chosen words (extremes included). */
+SDE_API int32_t sde_normal_pairs(const uint32_t *words, int64_t n, int32_t precision, double *out);
+
 /* Page-locked host memory for results; stands where sdepy allocates the
  * result array with numpy (sdepy/integration.py:550, np.full of NaN in
  * paths_generator.__call__).  An output array (SdeOut.xx with

@@ -92,6 +92,7 @@ SIGNATURES = {
     'sde_device_count': (C.c_int32, []),
     'sde_release': (C.c_int32, []),
     'sde_set_stream': (C.c_int32, [C.c_void_p]),
+    'sde_normal_pairs': (C.c_int32, [C.POINTER(C.c_uint32), C.c_int64, C.c_int32, _dp]),
     'sde_host_alloc': (C.c_int32, [C.c_int64, C.POINTER(C.c_void_p)]),
     'sde_host_free': (C.c_int32, [C.c_void_p]),
     'sde_timing': (C.c_int32, [C.c_int32, _dp]),

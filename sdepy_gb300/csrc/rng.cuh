@@ -18,10 +18,13 @@
 // Normals (Box-Muller) from a word pair (a, b):
 //   r = sqrt(-2 log u(a)),  v = (b >> 9) * 2^-22 - 1  in [-1, 1),
 //   z0 = r cos(pi v),  z1 = r sin(pi v).
-// FP64 evaluates this exactly as written; FP32 evaluates the same formula
-// with the SFU approximations, so both precisions consume identical draws.
+// FP64 evaluates this formula to a few ulp with table-driven logarithm and
+// sine / cosine (ln_u01_f64, sincospi_f64 below); FP32 evaluates it with the
+// SFU approximations, so both precisions consume identical draws.
 #pragma once
 #include <cstdint>
+
+#include "fp64_tables.h"
 
 namespace sdegpu {
 
@@ -118,20 +121,75 @@ __device__ __forceinline__ float approx_cos(float x) {
     return y;
 }
 
+// ln u for u = (a + 0.5) 2^-32 = (2a + 1) 2^-33, within a few ulp.  Tang's
+// table-driven method (ACM TOMS 15(2), 1989): 2a + 1 = 2^e m with
+// m in [0.75, 1.5) built from the integer's bits, m = c_j (1 + r) with
+// c_j = 0.75 + j/128 the nearest table point, |r| <= 1/192, and
+// ln u = (e - 33) ln 2 + ln c_j + log1p(r), log1p by its Taylor series to
+// r^7 (the first omitted term is below 2^-56 of log1p(r)).  Near u = 1
+// the result is log1p(r) alone, so it keeps full relative accuracy there.
+__device__ __forceinline__ double ln_u01_f64(uint32_t a) {
+    const unsigned long long v = 2ull * a + 1ull;              // odd, in [1, 2^33)
+    const int lz = __clzll((long long)v);
+    const int e = 63 - lz;                                      // 2^e <= v < 2^(e+1)
+    const unsigned long long frac = ((v << lz) << 1) >> 12;     // the 52 bits below the leading one
+    const uint32_t fhi = (uint32_t)(frac >> 32);                // top 20 of them
+    const bool upper = fhi >= 0x80000u;                         // 1.f >= 1.5: use m = 1.f / 2
+    const int j = upper ? (int)((fhi + 0x2000u) >> 14) - 32 : (int)((fhi + 0x1000u) >> 13) + 32;
+    const int k = e - 33 + (upper ? 1 : 0);                     // in [-33, 0]
+    const double m = __longlong_as_double((long long)(((upper ? 1022ull : 1023ull) << 52) | frac));
+    const double d = m - __ldg(&F64_LOG_C[j]);                  // exact
+    const double r = d * __ldg(&F64_LOG_INVC[j]);
+    const double r2 = r * r;
+    double q = 1.0 / 7.0;
+    q = fma(q, r, -1.0 / 6.0);
+    q = fma(q, r, 1.0 / 5.0);
+    q = fma(q, r, -0.25);
+    q = fma(q, r, 1.0 / 3.0);
+    q = fma(q, r, -0.5);
+    const double p = fma(q, r2, r);                             // log1p(r)
+    return (__ldg(&F64_KLN2_HI[k + 35]) + __ldg(&F64_LOG_LNC[j])) + (__ldg(&F64_KLN2_LO[k + 35]) + p);
+}
+
+// sin(pi v), cos(pi v) for v = (b >> 9) 2^-22 - 1 in [-1, 1), within a few
+// ulp: v = n/64 + f with |f| <= 1/128 exact, x = pi f, Taylor series of
+// sin x to x^7 and cos x to x^6 (|x| <= pi/128: the first omitted terms
+// are below 2^-58), and the angle-addition formulas with the tabulated
+// sin(pi n/64), cos(pi n/64).  Where the result is near zero (n = 0, +-32,
+// +-64) the table's other factor is exactly zero, so no cancellation.
+__device__ __forceinline__ void sincospi_f64(uint32_t b, double &s, double &c) {
+    const int q = (int)(b >> 9);                     // v = q 2^-22 - 1
+    const int nn = (q + 0x8000) >> 16;               // n + 64, in [0, 128]
+    const int qd = q - (nn << 16);                   // f = qd 2^-22, |qd| <= 2^15
+    const double x = (double)qd * (0x1p-22 * F64_PI_HI);
+    const double x2 = x * x;
+    double ps = -1.0 / 5040.0;
+    ps = fma(ps, x2, 1.0 / 120.0);
+    ps = fma(ps, x2, -1.0 / 6.0);
+    const double sx = fma(x * x2, ps, x);            // sin x
+    double pc = -1.0 / 720.0;
+    pc = fma(pc, x2, 1.0 / 24.0);
+    pc = fma(pc, x2, -0.5);
+    const double cx = fma(x2, pc, 1.0);              // cos x
+    const double S = __ldg(&F64_SINPI_N[nn]), C = __ldg(&F64_COSPI_N[nn]);
+    s = fma(S, cx, C * sx);
+    c = fma(C, cx, -(S * sx));
+}
+
 template <typename R> struct Rng;
 
 template <> struct Rng<double> {
     static __device__ __forceinline__ void normal2(uint32_t a, uint32_t b,
                                                    double &z0, double &z1) {
-        const double r = sqrt(-2.0 * log(u01_f64(a)));
+        const double r = sqrt(-2.0 * ln_u01_f64(a));
         double s, c;
-        sincospi(vpm1_f64(b), &s, &c);
+        sincospi_f64(b, s, c);
         z0 = r * c;
         z1 = r * s;
     }
     // -log(u), the unit exponential
     static __device__ __forceinline__ double expo(uint32_t a) {
-        return -log(u01_f64(a));
+        return -ln_u01_f64(a);
     }
     static __device__ __forceinline__ double unif(uint32_t a) { return u01_f64(a); }
     static __device__ __forceinline__ void normal2_s(uint32_t a, uint32_t b,

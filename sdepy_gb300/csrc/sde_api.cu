@@ -155,6 +155,42 @@ extern "C" int32_t sde_timing(int32_t enable, double *last_ms) {
     return SDE_OK;
 }
 
+// ---------------------------------------------------------------------------
+// the Box-Muller transform of given word pairs, as the kernels apply it
+// ---------------------------------------------------------------------------
+template <typename R>
+static __global__ void normal_pairs_kernel(const uint32_t *words, int64_t n, double *out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    R z0, z1;
+    Rng<R>::normal2(words[2 * i], words[2 * i + 1], z0, z1);
+    out[2 * i] = (double)z0;
+    out[2 * i + 1] = (double)z1;
+}
+
+extern "C" int32_t sde_normal_pairs(const uint32_t *words, int64_t n, int32_t precision, double *out) {
+    if (!words || !out || n < 0 || n > (1ll << 30)) return fail(SDE_ERR_INVALID, "sde_normal_pairs: bad arguments");
+    if (precision != SDE_FP64 && precision != SDE_FP32)
+        return fail(SDE_ERR_UNSUPPORTED, "unknown precision %d", precision);
+    if (n == 0) return SDE_OK;
+    std::lock_guard<std::mutex> lock(g_mu);
+    Device *D;
+    int rc;
+    if ((rc = current_device(&D))) return rc;
+    cudaStream_t st = D->stream;
+    void *dw, *dz;
+    if ((rc = scratch(D, S_NOISE_DW, sizeof(uint32_t) * 2 * (size_t)n, &dw))) return rc;
+    if ((rc = scratch(D, S_NOISE_DJ, sizeof(double) * 2 * (size_t)n, &dz))) return rc;
+    CU(cudaMemcpyAsync(dw, words, sizeof(uint32_t) * 2 * (size_t)n, cudaMemcpyHostToDevice, st));
+    const unsigned nb = (unsigned)((n + BLOCK - 1) / BLOCK);
+    if (precision == SDE_FP64) normal_pairs_kernel<double><<<nb, BLOCK, 0, st>>>((const uint32_t *)dw, n, (double *)dz);
+    else normal_pairs_kernel<float><<<nb, BLOCK, 0, st>>>((const uint32_t *)dw, n, (double *)dz);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(out, dz, sizeof(double) * 2 * (size_t)n, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    return SDE_OK;
+}
+
 extern "C" int32_t sde_host_alloc(int64_t bytes, void **ptr) {
     if (!ptr || bytes < 1) return fail(SDE_ERR_INVALID, "sde_host_alloc: bad arguments");
     *ptr = nullptr;
