@@ -34,7 +34,7 @@ struct AdjArgs {
     PhiloxKey key;
     const R *dt, *sqdt;
     const double *lamdt, *p0;
-    const long long *thr;
+    const long long *thr, *thr1;
     const R *x0, *prm;
     R chol[NCHOL];
     R rho_k;  // -rho / sqrt(1 - rho^2) for the rho gradient (2-variable Heston)
@@ -236,7 +236,8 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                         const int w = g * M + m;
                         const int64_t tix = (int64_t)k * W + w;
                         if ((long long)word > a.thr[tix]) {
-                            const int cnt = poisson_tail(word, a.p0[tix], a.lamdt[tix], a.err);
+                            const int cnt = (long long)word <= a.thr1[tix]
+                                                ? 1 : poisson_tail(word, a.p0[tix], a.lamdt[tix], a.err);
                             R S = R(0);
                             for (int j = 0; j < cnt; ++j) {
                                 const uint4 r = philox4x32_10(

@@ -370,7 +370,7 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
 
     // ---- host tables, packed in one staging buffer ---------------------------
     // layout: dt[R n_steps] sqdt[R n_steps] out_row[int n_pts] x0[R W] prm[R 6W]
-    //         lamdt[f64 n_steps*W] p0[f64 n_steps*W] thr[i64 n_steps*W]
+    //         lamdt[f64 n_steps*W] p0[f64 n_steps*W] thr[i64 n_steps*W] thr1[i64 n_steps*W]
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     const size_t o_dt = 0;
     const size_t o_sq = o_dt + al(sizeof(R) * (n_steps + 1));
@@ -440,7 +440,8 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
             runs.push_back(make_int4(k0, k, row, ci));
         }
     }
-    const size_t o_runs = o_thr + al(sizeof(long long) * njt);
+    const size_t o_thr1 = o_thr + al(sizeof(long long) * njt);
+    const size_t o_runs = o_thr1 + al(sizeof(long long) * njt);
     const size_t o_ctab = o_runs + al(sizeof(int4) * (runs.size() + 1));
     const size_t o_tsh = o_ctab + al(sizeof(float) * (ctab.size() + 4));
     const size_t o_end = o_tsh + al(sizeof(float) * (tshift.size() + 4));
@@ -449,7 +450,7 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     R *h_dt = (R *)(H + o_dt), *h_sq = (R *)(H + o_sq), *h_x0 = (R *)(H + o_x0), *h_prm = (R *)(H + o_prm);
     int32_t *h_row = (int32_t *)(H + o_row);
     double *h_lam = (double *)(H + o_lam), *h_p0 = (double *)(H + o_p0);
-    long long *h_thr = (long long *)(H + o_thr);
+    long long *h_thr = (long long *)(H + o_thr), *h_thr1 = (long long *)(H + o_thr1);
     double sgn = 1.0;
     for (int k = 0; k < n_steps; ++k) {
         const double dt = gr->tt[k + 1] - gr->tt[k];
@@ -475,7 +476,7 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
                 const size_t i = (size_t)k * W + w;
                 h_lam[i] = L;
                 h_p0[i] = p0;
-                h_thr[i] = (long long)floor(p0 * 4294967296.0 - 0.5);
+                poisson_thresholds(p0, L, h_thr[i], h_thr1[i]);
             }
         }
         if (s->jump_law == SDE_JUMP_DOUBLE_EXP)
@@ -523,6 +524,7 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     a.lamdt = (const double *)(T + o_lam);
     a.p0 = (const double *)(T + o_p0);
     a.thr = (const long long *)(T + o_thr);
+    a.thr1 = (const long long *)(T + o_thr1);
     a.x0 = (const R *)(T + o_x0);
     a.prm = (const R *)(T + o_prm);
     a.coef = nullptr;
@@ -926,12 +928,13 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     const size_t o_dt = 0, o_sq = o_dt + al(sizeof(R) * n_steps), o_x0 = o_sq + al(sizeof(R) * n_steps);
     const size_t o_prm = o_x0 + al(sizeof(R) * W), o_lam = o_prm + al(sizeof(R) * SDE_MAX_PARAMS * W);
     const size_t o_p0 = o_lam + al(sizeof(double) * njt), o_thr = o_p0 + al(sizeof(double) * njt);
-    const size_t o_end = o_thr + al(sizeof(long long) * njt);
+    const size_t o_thr1 = o_thr + al(sizeof(long long) * njt);
+    const size_t o_end = o_thr1 + al(sizeof(long long) * njt);
     D->host_tables.resize(o_end);
     char *H = D->host_tables.data();
     R *h_dt = (R *)(H + o_dt), *h_sq = (R *)(H + o_sq), *h_x0 = (R *)(H + o_x0), *h_prm = (R *)(H + o_prm);
     double *h_lam = (double *)(H + o_lam), *h_p0 = (double *)(H + o_p0);
-    long long *h_thr = (long long *)(H + o_thr);
+    long long *h_thr = (long long *)(H + o_thr), *h_thr1 = (long long *)(H + o_thr1);
     for (int k = 0; k < n_steps; ++k) {
         const double dt = gr->tt[k + 1] - gr->tt[k];
         h_dt[k] = (R)dt;
@@ -947,7 +950,7 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
                 const double p0 = exp(-L);
                 h_lam[(size_t)k * W + w] = L;
                 h_p0[(size_t)k * W + w] = p0;
-                h_thr[(size_t)k * W + w] = (long long)floor(p0 * 4294967296.0 - 0.5);
+                poisson_thresholds(p0, L, h_thr[(size_t)k * W + w], h_thr1[(size_t)k * W + w]);
             }
     if (s->corr) {
         std::vector<double> L(M * M);
@@ -987,6 +990,7 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     a.lamdt = (const double *)(T + o_lam);
     a.p0 = (const double *)(T + o_p0);
     a.thr = (const long long *)(T + o_thr);
+    a.thr1 = (const long long *)(T + o_thr1);
     a.n_strikes = req->n_strikes;
     for (int i = 0; i < req->n_strikes; ++i) {
         a.strikes[i] = (R)req->strikes[i];

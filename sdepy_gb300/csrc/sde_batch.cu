@@ -58,7 +58,7 @@ struct DevInst {
     float d[4], b[4], c[4];       // x' = x + (b - d x) + c w  (LINEAR d = 0)
     float p0[4], p1[4], p2[4];    // raw coefficients (Heston, tangents)
     float ja, jb;                 // jump-size law (norm: a + b z)
-    long long thr;                // Poisson zero-event threshold of one step
+    long long thr, thr1;          // Poisson count >= 1 / >= 2 thresholds of one step
     double p0d, lamdt;            // exp(-lam dt), lam dt
     float rho, rho_k;             // Heston rho and -rho/sqrt(1-rho^2)
     float chol10, chol11;         // Heston 2x2 Cholesky factor
@@ -91,7 +91,7 @@ __device__ __forceinline__ float path_lin(const DevInst &I, const PhiloxKey &key
     // the step loop's coefficients in registers (the loop's global writes
     // would otherwise force a reload of every field each step)
     const float b0 = I.b[0], c0 = I.c[0], sq = I.sq;
-    const long long thr = I.thr;
+    const long long thr = I.thr, thr1 = I.thr1;
     const int n_steps = I.n_steps;
 #pragma unroll 1
     for (int k = 0; k < n_steps; ++k) {
@@ -101,7 +101,7 @@ __device__ __forceinline__ float path_lin(const DevInst &I, const PhiloxKey &key
         a = a + b0 + c0 * z0;
         sdw += sq * z0;
         if (jumps && (long long)pw > thr) {
-            const int cnt = poisson_tail(pw, I.p0d, I.lamdt, err);
+            const int cnt = (long long)pw <= thr1 ? 1 : poisson_tail(pw, I.p0d, I.lamdt, err);
             for (int j = 0; j < cnt; ++j) {
                 const uint4 q = philox4x32_10(make_uint4(p, (uint32_t)k, 0x80000000u | (uint32_t)j, I.stream), key);
                 float y0, y1;
@@ -414,7 +414,7 @@ extern "C" int32_t sde_batch_create(const SdeBatchInstance *inst, int32_t n, int
             if (!(L >= 0) || L > 700) return bfail(SDE_ERR_INVALID, "instance %d: bad intensity", i);
             d.p0d = exp(-L);
             d.lamdt = L;
-            d.thr = (long long)floor(d.p0d * 4294967296.0 - 0.5);
+            poisson_thresholds(d.p0d, d.lamdt, d.thr, d.thr1);
             d.ja = (float)s.params[3][0];
             d.jb = (float)s.params[4][0];
         }

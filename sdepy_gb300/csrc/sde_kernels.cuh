@@ -43,7 +43,7 @@ struct FwdArgs {
     const R *dt, *sqdt;
     const int32_t *out_row;
     const double *lamdt, *p0;
-    const long long *thr;
+    const long long *thr, *thr1;   // Poisson count >= 1 / >= 2 thresholds (poisson_thresholds)
     // per-variable inputs
     const R *x0, *prm;  // prm[p*W + w]
     // FP32 LINEAR / OU with device RNG: coefficient rows [row][groups][2][MAXM],
@@ -266,6 +266,20 @@ __device__ __forceinline__ int group_outputs(const R (&st)[MAXM], int M, int out
 
 // Poisson count by inversion of the CDF, in FP64 (bit-exact given the
 // uniform word): smallest k with u <= F(k).  Called only when u > p0.
+// Integer thresholds of the inversion for uniform word w, u = (w + 0.5) 2^-32:
+// count >= 1 <=> w > thr0 (u > p0), count >= 2 <=> w > thr1 (u > F(1)), with
+// F(1) = p0 + (p0 lam) / 1 formed by the same rounded FP64 operations as
+// poisson_tail (the temporaries keep the host compiler from fusing them).
+// F * 2^32 is exact and so is subtracting 0.5 (F < 1), so each comparison
+// is exactly the FP64 one; a step with one event needs no FP64 arithmetic.
+static inline void poisson_thresholds(double p0, double lam, long long &thr0, long long &thr1) {
+    thr0 = (long long)floor(p0 * 4294967296.0 - 0.5);
+    volatile double pk = p0 * lam;
+    volatile double pk1 = pk / 1.0;
+    volatile double F1 = p0 + pk1;
+    thr1 = (long long)floor(F1 * 4294967296.0 - 0.5);
+}
+
 __device__ __forceinline__ int poisson_tail(uint32_t word, double p0, double lam, int32_t *err) {
     const double u = u01_f64(word);
     int k = 0;
@@ -679,7 +693,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                 const int w = g * M + m;
                 const int64_t tix = (int64_t)k * W + w;
                 if ((long long)word > a.thr[tix]) {
-                    const int cnt = poisson_tail(word, a.p0[tix], a.lamdt[tix], a.err);
+                    const int cnt = (long long)word <= a.thr1[tix] ? 1 : poisson_tail(word, a.p0[tix], a.lamdt[tix], a.err);
                     R S = R(0);
                     for (int j = 0; j < cnt; ++j) {
                         const uint4 r = philox4x32_10(
