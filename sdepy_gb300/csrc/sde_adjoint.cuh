@@ -154,8 +154,10 @@ __device__ __forceinline__ void fwd_step(const R (&c0)[MAXM], const R (&c1)[MAXM
     }
 }
 
+// FP32 kernels of one or two states are held to 80 registers: 3 resident
+// blocks per SM (measured 2.4 % faster for Heston than 2 blocks at 90)
 template <typename R, int MODEL, int MAXM, bool JUMPS>
-__global__ void __launch_bounds__(BLOCK)
+__global__ void __launch_bounds__(BLOCK, (sizeof(R) == 4 && MAXM <= 2) ? 3 : 1)
 sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
     typedef Ar<R> A;
     constexpr int NCMAX = NoiseShape<MAXM, JUMPS>::NCMAX;
