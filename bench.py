@@ -561,8 +561,11 @@ def run_reference(args):
 def run_case(args):
     """Small single-kernel cases for profiling captures: 'heston_adjoint'
     (configs[2] model, 2^18 paths, 499 steps: forward summary then adjoint),
-    'batch' (256 instances of the heterogeneous workload, paths <= 65536)."""
+    'batch' (256 instances of the heterogeneous workload, paths <= 65536),
+    'lognorm_fp64' (configs[0]: FP64, 1e5 paths, 502 steps, 253 rows written
+    to device memory)."""
     import ctypes as C
+    import torch
     import sdepy_gb300 as sg
     from sdepy_gb300 import _lib
     from sdepy_gb300.grid import Grid
@@ -599,6 +602,24 @@ def run_case(args):
             B.run()
         print(json.dumps({'case': args.case, 'batch_ms': B.last_ms, 'path_steps': B.path_steps}))
         B.close()
+    elif args.case == 'lognorm_fp64':
+        P = sg.lognorm_process(x0=1., mu=.05, sigma=.2, paths=100000, steps=252)
+        grid = Grid(np.linspace(0, 1, 253), 252)
+        leg = grid.legs[0]
+        xx = torch.empty((grid.n_rows, 1, 100000), dtype=torch.float64, device='cuda')
+        ms = []
+        for i in range(args.warmup + args.steps):
+            spec = P._make_spec(1, i)
+            g = _lib.SdeGrid()
+            g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
+            g.n_pts, g.step_offset = leg.tt.size, 0
+            o = _lib.SdeOut()
+            o.xx, o.n_rows, o.on_device = xx.data_ptr(), grid.n_rows, 1
+            _lib.check(lib.sde_run(C.byref(spec), C.byref(g), None, C.byref(o)), 'run')
+            lib.sde_timing(-1, last)
+            ms.append(last[0])
+        print(json.dumps({'case': args.case, 'kernel_ms': float(np.median(ms[args.warmup:])),
+                          'path_steps': 100000*leg.n_steps}))
 
 
 def main():
@@ -611,7 +632,7 @@ def main():
                     help='paths per step (profiling captures use fewer)')
     ap.add_argument('--quick', action='store_true',
                     help='timed steps only: no FP64 / e2e / CPU / probe extras')
-    ap.add_argument('--case', default=None, choices=['heston_adjoint', 'batch'],
+    ap.add_argument('--case', default=None, choices=['heston_adjoint', 'batch', 'lognorm_fp64'],
                     help='run one small single-kernel case (profiling)')
     args = ap.parse_args()
     if args.case:
