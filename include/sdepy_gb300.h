@@ -37,7 +37,7 @@ extern "C" {
 #define SDE_API
 #endif
 
-#define SDE_ABI_VERSION 1
+#define SDE_ABI_VERSION 2
 
 #define SDE_MAX_GROUP   16   /* largest correlated group (state vars) */
 #define SDE_MAX_PARAMS  6    /* coefficient arrays per state variable */
@@ -105,6 +105,16 @@ typedef struct SdeGrid {
     const int32_t *out_row; /* [n_pts] output row stored at each point, or -1         */
     int32_t n_pts;          /* >= 1; n_steps = n_pts - 1                               */
     uint32_t step_offset;   /* added to the step index in the Philox counter          */
+    /* Time-dependent parameters, or NULL (SdeSpec.params apply at every
+     * step): [n_pts - 1][SDE_MAX_PARAMS][groups*M], row k the parameters of
+     * step k from tt[k] to tt[k+1].  Slots 0..2 are the SDE's coefficients
+     * evaluated at tt[k] (sdepy's SDE.A, sdepy/integration.py:1216-1225);
+     * for jump models slot 2 is the Poisson intensity evaluated at the
+     * step's midpoint tt[k] + dt/2 (sdepy/infrastructure.py:1629); slots
+     * 3..5 (jump-size laws) are read from SdeSpec.params.  sde_run and
+     * sde_run_stats accept it; sde_adjoint and sde_run_stats_static return
+     * SDE_ERR_UNSUPPORTED. */
+    const double *params_t;
 } SdeGrid;
 
 typedef struct SdeNoise {   /* host arrays of injected increments (f64) */

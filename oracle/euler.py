@@ -123,7 +123,10 @@ class NumpyCPoisson:
     def __call__(self, t, dt):
         shape = self.vshape + (self.paths,)
         sign = int(np.sign(dt))
-        dn = sign*self.rng.poisson(abs(dt)*self.lam, shape)
+        # a time-dependent intensity at the middle of the step
+        # (sdepy/infrastructure.py:1629)
+        lam = self.lam(t + dt/2) if callable(self.lam) else self.lam
+        dn = sign*self.rng.poisson(abs(dt)*lam, shape)
         dz = np.zeros(shape, dtype=self.dtype)
         dnp = sign*dn
         for j in range(1, dnp.max() + 1):
@@ -175,13 +178,16 @@ def integrate(preset, params=None, timeline=(0., 1.), *, paths=1, vshape=(),
     assert preset in PRESETS, preset
     p = dict(DEFAULTS[preset])
     p.update(params or {})
-    P = {k: (v if k == 'factors' else np.asarray(v)) for k, v in p.items()}
+    # callables (and processes) are time-dependent parameters, evaluated at
+    # the start of each step as sdepy's SDE.A does (integration.py:1216-1225)
+    P = {k: (v if k == 'factors' or callable(v) else np.asarray(v)) for k, v in p.items()}
     vshape = (vshape,) if isinstance(vshape, int) else tuple(vshape)
     xshape, wshape, addaxis = shapes(preset, vshape, p.get('factors', 1))
     dtype = float if dtype is None else dtype
     jumps = 'jumpdiff' in preset
     heston = 'heston' in preset
     log = preset in ('lognorm_process',) or jumps
+    P0 = P
     if dw is None:
         dw = NumpyWiener(rng, paths, wshape, corr=corr, dtype=dtype)
     if jumps and dj is None:
@@ -198,7 +204,8 @@ def integrate(preset, params=None, timeline=(0., 1.), *, paths=1, vshape=(),
         i = np.index_exp[..., np.newaxis, :] if addaxis else np.index_exp[...]
         return np.concatenate(tuple(np.broadcast_to(x, target)[i] for x in xs), axis=-2)
 
-    def sde(x):
+    def sde(s, x):
+        P = {k: (np.asarray(v(s)) if callable(v) else v) for k, v in P0.items()}
         if preset == 'wiener_process':
             return {'dt': P['mu'], 'dw': P['sigma']}
         if preset == 'lognorm_process':
@@ -222,6 +229,7 @@ def integrate(preset, params=None, timeline=(0., 1.), *, paths=1, vshape=(),
         return {i: pack(tuple(a.get(i, 0) for a in As)) for i in ids}
 
     def init(out_x):
+        P = P0
         if heston:
             ox, oy = unpack(out_x)
             ox[...] = np.log(P['x0'])
@@ -261,7 +269,7 @@ def integrate(preset, params=None, timeline=(0., 1.), *, paths=1, vshape=(),
         i = 1
         for k in range(steps_leg.size - 1):
             s, ds = steps_leg[k], steps_leg[k + 1] - steps_leg[k]
-            A = sde(x)
+            A = sde(s, x)
             dZ = {'dt': ds}
             for sid in order:
                 dZ[sid] = sources[sid](s, ds)

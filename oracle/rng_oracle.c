@@ -156,6 +156,9 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
             for (int k = -1; k < n_steps; ++k) {
                 if (k >= 0) {
                     const double dt = dtv[k], sq = sqv[k];
+                    /* coefficients of this step (slots 0..2; the Poisson
+                     * intensity of jump models is slot 2) */
+                    const double *pp = g->params_t ? g->params_t + (size_t)k * SDE_MAX_PARAMS * W : prm;
                     const uint32_t c1 = (uint32_t)k + g->step_offset;
                     const int P = (M + 1) / 2;
                     const int U = 2 * P + (jumps ? M : 0);
@@ -203,7 +206,7 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
                     if (jumps) {
                         for (int m = 0; m < M; ++m) {
                             const int w = gi * M + m;
-                            const double lam = fabs(dt) * prm[2 * W + w];
+                            const double lam = fabs(dt) * pp[2 * W + w];
                             const double p0 = exp(-lam);
                             const uint32_t word = u[2 * P + m];
                             if (u01(word) > p0) {
@@ -227,15 +230,15 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
                     if (s->model == SDE_MODEL_LINEAR) {
                         for (int m = 0; m < M; ++m) {
                             const int w = gi * M + m;
-                            double inc = prm[0 * W + w] * dt + prm[1 * W + w] * dW[m];
+                            double inc = pp[0 * W + w] * dt + pp[1 * W + w] * dW[m];
                             if (jumps) inc = inc + dJ[m];
                             st[m] = st[m] + inc;
                         }
                     } else if (s->model == SDE_MODEL_OU) {
                         for (int m = 0; m < M; ++m) {
                             const int w = gi * M + m;
-                            const double drift = prm[0 * W + w] * (prm[1 * W + w] - st[m]);
-                            st[m] = st[m] + (drift * dt + prm[2 * W + w] * dW[m]);
+                            const double drift = pp[0 * W + w] * (pp[1 * W + w] - st[m]);
+                            st[m] = st[m] + (drift * dt + pp[2 * W + w] * dW[m]);
                         }
                     } else {
                         const int h = M / 2;
@@ -246,11 +249,11 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
                             if (y < 0.0) negc[i] += 1;
                             const double yp = y > 0.0 ? y : 0.0;
                             const double sqy = sqrt(yp);
-                            const double mu = prm[0 * W + wx], sg = prm[1 * W + wx];
+                            const double mu = pp[0 * W + wx], sg = pp[1 * W + wx];
                             const double adt = mu - ((sg * sg) * yp) * 0.5;
                             const double adw = sg * sqy;
                             nx[i] = st[i] + (adt * dt + adw * dW[i]);
-                            const double kk = prm[0 * W + wy], th = prm[1 * W + wy], xi = prm[2 * W + wy];
+                            const double kk = pp[0 * W + wy], th = pp[1 * W + wy], xi = pp[2 * W + wy];
                             const double bdt = kk * (th - yp);
                             const double bdw = xi * sqy;
                             nx[h + i] = y + (bdt * dt + bdw * dW[h + i]);

@@ -79,4 +79,21 @@ FwdLauncher<float> find_fwd_f32_ou_heston(int model, int maxm, bool inject, bool
     return nullptr;
 }
 
+
+FwdLauncher<float> find_fwd_f32_ou_tdb(int maxm, int *bps) {
+    switch (maxm) {
+    case 1: if (bps) *bps = fwd_max_blocks_per_sm<float, SDE_MODEL_OU, 1, false, false, true>();
+            return &launch_fwd<float, SDE_MODEL_OU, 1, false, false, true>;
+    case 2: if (bps) *bps = fwd_max_blocks_per_sm<float, SDE_MODEL_OU, 2, false, false, true>();
+            return &launch_fwd<float, SDE_MODEL_OU, 2, false, false, true>;
+    case 4: if (bps) *bps = fwd_max_blocks_per_sm<float, SDE_MODEL_OU, 4, false, false, true>();
+            return &launch_fwd<float, SDE_MODEL_OU, 4, false, false, true>;
+    case 8: if (bps) *bps = fwd_max_blocks_per_sm<float, SDE_MODEL_OU, 8, false, false, true>();
+            return &launch_fwd<float, SDE_MODEL_OU, 8, false, false, true>;
+    case 16: if (bps) *bps = fwd_max_blocks_per_sm<float, SDE_MODEL_OU, 16, false, false, true>();
+             return &launch_fwd<float, SDE_MODEL_OU, 16, false, false, true>;
+    default: return nullptr;
+    }
+}
+
 }  // namespace sdegpu

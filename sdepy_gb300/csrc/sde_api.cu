@@ -309,12 +309,15 @@ template <> struct Finder<double> {
         FwdLauncher<double> f = find_fwd_f64_linear(model, maxm, inj, jmp, bps);
         return f ? f : find_fwd_f64_ou_heston(model, maxm, inj, jmp, bps);
     }
+    static FwdLauncher<double> find_tdb(int, int *) { return nullptr; }
 };
 template <> struct Finder<float> {
     static FwdLauncher<float> find(int model, int maxm, bool inj, bool jmp, int *bps) {
         FwdLauncher<float> f = find_fwd_f32_linear(model, maxm, inj, jmp, bps);
         return f ? f : find_fwd_f32_ou_heston(model, maxm, inj, jmp, bps);
     }
+    // OU run-table kernels with a time-dependent theta
+    static FwdLauncher<float> find_tdb(int maxm, int *bps) { return find_fwd_f32_ou_tdb(maxm, bps); }
 };
 
 // number of blocks along paths: enough for every SM, capped by the paths
@@ -383,28 +386,47 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     const size_t o_thr = o_p0 + al(sizeof(double) * njt);
     const bool tab = sizeof(R) == 4 && !inject && s->model != SDE_MODEL_HESTON;
     const int tmaxm = maxm_of(M);
+    // parameters of step k: the time-dependent table's row, or the constants
+    const double *ptab = gr->params_t;
+    auto params_of = [&](int k) -> const double * {
+        return ptab ? ptab + (size_t)k * SDE_MAX_PARAMS * W : s->params;
+    };
+    // OU with a time-dependent theta: the state is held as the deviation from
+    // the first step's theta0, and each row adds b = k dt (theta_k - theta0)
+    bool ou_b = false;
+    if (tab && ptab && s->model == SDE_MODEL_OU)
+        for (int k = 0; k < n_steps && !ou_b; ++k)
+            for (int w = 0; w < W && !ou_b; ++w) ou_b = params_of(k)[W + w] != params_of(0)[W + w];
+    const int nb = ou_b ? 3 : 2;   // coefficient vectors per row
     // FP32 LINEAR / OU: the grid as runs of steps with one coefficient row
     // each, and the compact table of those rows (see FwdArgs::coef / runs)
     std::vector<int4> runs;
     std::vector<float> ctab, tshift;
     if (tab && n_steps > 0) {
-        const size_t rowlen = (size_t)s->groups * 2 * tmaxm;
+        const size_t rowlen = (size_t)s->groups * nb * tmaxm;
         std::vector<float> cur(rowlen), nxt(rowlen);
+        const int ps = s->model == SDE_MODEL_OU ? 2 : 1;   // the sigma slot
+        const double *th0 = params_of(0) + W;
         // the same FP64 operations as coef_table_kernel
-        const double *P0 = s->params, *PS = s->params + (s->model == SDE_MODEL_OU ? 2 : 1) * W;
         auto coef_row = [&](int k, float *t) {
             const double dt = gr->tt[k + 1] - gr->tt[k], sq = sqrt(fabs(dt));
+            const double *P = params_of(k);
             for (int g = 0; g < s->groups; ++g) {
-                float *r = t + (size_t)g * 2 * tmaxm;
+                float *r = t + (size_t)g * nb * tmaxm;
                 for (int m = 0; m < tmaxm; ++m) {
                     if (m >= M) {
-                        r[m] = r[tmaxm + m] = 0.0f;
+                        for (int v = 0; v < nb; ++v) r[v * tmaxm + m] = 0.0f;
                         continue;
                     }
                     const int w = g * M + m;
-                    const double cs = PS[w] * sq;
-                    r[m] = (float)(P0[w] * dt);
+                    const double cs = P[ps * W + w] * sq;
+                    const double d = P[w] * dt;
+                    r[m] = (float)d;
                     r[tmaxm + m] = (float)(cs * SDE_SQRT_2LN2);
+                    if (ou_b) {
+                        const double dth = P[W + w] - th0[w];
+                        r[2 * tmaxm + m] = (float)(d * dth);
+                    }
                 }
             }
         };
@@ -413,8 +435,8 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
             for (int g = 0; g < s->groups; ++g)
                 for (int m = 0; m < M; ++m) {
                     const int w = g * M + m;
-                    tshift[(size_t)g * 2 * tmaxm + m] = (float)s->params[W + w];
-                    tshift[(size_t)(g * 2 + 1) * tmaxm + m] = (float)(s->x0[w] - s->params[W + w]);
+                    tshift[(size_t)g * 2 * tmaxm + m] = (float)th0[w];
+                    tshift[(size_t)(g * 2 + 1) * tmaxm + m] = (float)(s->x0[w] - th0[w]);
                 }
         }
         int k = 0;
@@ -444,7 +466,10 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     const size_t o_runs = o_thr1 + al(sizeof(long long) * njt);
     const size_t o_ctab = o_runs + al(sizeof(int4) * (runs.size() + 1));
     const size_t o_tsh = o_ctab + al(sizeof(float) * (ctab.size() + 4));
-    const size_t o_end = o_tsh + al(sizeof(float) * (tshift.size() + 4));
+    // the other kernels read time-dependent coefficients (slots 0..2) per step
+    const size_t nprmt = (ptab && !tab) ? (size_t)n_steps * 3 * W : 0;
+    const size_t o_prmt = o_tsh + al(sizeof(float) * (tshift.size() + 4));
+    const size_t o_end = o_prmt + al(sizeof(R) * (nprmt + 1));
     D->host_tables.resize(o_end);
     char *H = D->host_tables.data();
     R *h_dt = (R *)(H + o_dt), *h_sq = (R *)(H + o_sq), *h_x0 = (R *)(H + o_x0), *h_prm = (R *)(H + o_prm);
@@ -467,7 +492,7 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
         for (int k = 0; k < n_steps; ++k) {
             const double adt = fabs(gr->tt[k + 1] - gr->tt[k]);
             for (int w = 0; w < W; ++w) {
-                const double lam = s->params[2 * W + w];
+                const double lam = params_of(k)[2 * W + w];
                 if (!(lam >= 0.0) || !std::isfinite(lam))
                     return fail(SDE_ERR_INVALID, "Poisson intensity must be finite and >= 0");
                 const double L = adt * lam;
@@ -490,6 +515,12 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     if (!runs.empty()) memcpy(H + o_runs, runs.data(), sizeof(int4) * runs.size());
     if (!ctab.empty()) memcpy(H + o_ctab, ctab.data(), sizeof(float) * ctab.size());
     if (!tshift.empty()) memcpy(H + o_tsh, tshift.data(), sizeof(float) * tshift.size());
+    if (nprmt) {
+        R *h_prmt = (R *)(H + o_prmt);
+        for (int k = 0; k < n_steps; ++k)
+            for (int v = 0; v < 3; ++v)
+                for (int w = 0; w < W; ++w) h_prmt[((size_t)k * 3 + v) * W + w] = (R)params_of(k)[v * W + w];
+    }
 
     FwdArgs<R> a;
     memset(&a, 0, sizeof a);
@@ -535,6 +566,7 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
         a.n_runs = (int32_t)runs.size();
         a.tshift = tshift.empty() ? nullptr : (const float *)(T + o_tsh);
     }
+    a.prm_t = nprmt ? (const R *)(T + o_prmt) : nullptr;
     a.key = philox_schedule(s->seed);
     a.n_out_vars = n_out;
 
@@ -620,7 +652,8 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
 
     // ---- launch ----------------------------------------------------------------------
     int bps = 0;
-    FwdLauncher<R> L = Finder<R>::find(s->model, maxm_of(M), inject, jumps, &bps);
+    FwdLauncher<R> L = ou_b ? Finder<R>::find_tdb(maxm_of(M), &bps)
+                            : Finder<R>::find(s->model, maxm_of(M), inject, jumps, &bps);
     if (!L) return fail(SDE_ERR_UNSUPPORTED, "no kernel for model %d group size %d", s->model, M);
     const int nbx = path_blocks(D, paths, s->groups, bps);
     a.stats_row = -1;
@@ -1048,6 +1081,8 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
 extern "C" int32_t sde_adjoint(const SdeSpec *spec, const SdeGrid *grid, const SdeAdjReq *req, double *grad,
                                double *value) {
     if (!spec) return fail(SDE_ERR_INVALID, "spec is NULL");
+    if (grid && grid->params_t)
+        return fail(SDE_ERR_UNSUPPORTED, "the adjoint takes constant parameters (grid params_t must be NULL)");
     if (spec->precision == SDE_FP32) return adjoint_impl<float>(spec, grid, req, grad, value);
     return adjoint_impl<double>(spec, grid, req, grad, value);
 }

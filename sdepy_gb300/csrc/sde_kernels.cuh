@@ -56,9 +56,16 @@ struct FwdArgs {
     // deviation from theta, so the update is two fused multiply-adds and
     // rounds relative to the deviation; d is kept small (not 1 - k dt) so
     // that its rounding does not bias the decay over many steps.
+    // With a time-dependent theta an OU row carries a third vector
+    // b = k dt (theta_k - theta0) and the state is the deviation from the
+    // first step's theta0: y' = ((y - d y) + c (L z')) + b (kernels
+    // compiled with TDB, rows [row][groups][3][MAXM]).
     const float *coef;
-    // OU: [groups][2][MAXM] = (theta, x0 - theta) in FP32
+    // OU: [groups][2][MAXM] = (theta0, x0 - theta0) in FP32
     const float *tshift;
+    // the other kernels with time-dependent parameters: [steps][3][W] =
+    // parameter slots 0..2 of each step, or NULL (prm applies throughout)
+    const R *prm_t;
     // and the grid as runs of steps sharing one coefficient row:
     // (first step, end step, output row stored after the run or -1, coef row)
     const int4 *runs;
@@ -569,15 +576,19 @@ __device__ __forceinline__ void jump_size_grad(int law, uint4 r, R ja, R jb, R j
 // ---------------------------------------------------------------------------
 // the forward kernel
 // ---------------------------------------------------------------------------
-// FP32 device-RNG kernels without jumps, up to 8 states per thread, are
-// held to 80 registers: 3 resident blocks (24 warps) per SM
-template <typename R, int MAXM, bool INJECT, bool JUMPS>
+// FP32 device-RNG kernels without jumps, up to 8 states per thread (4 for
+// Heston, whose step keeps more values live), are held to 80 registers: 3
+// resident blocks (24 warps) per SM
+template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS>
 struct FwdOccupancy {
-    static constexpr int MIN_BLOCKS = (sizeof(R) == 4 && MAXM <= 8 && !INJECT && !JUMPS) ? 3 : 1;
+    static constexpr int MIN_BLOCKS =
+        (sizeof(R) == 4 && MAXM <= (MODEL == SDE_MODEL_HESTON ? 4 : 8) && !INJECT && !JUMPS) ? 3 : 1;
 };
 
-template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS>
-__global__ void __launch_bounds__(BLOCK, (FwdOccupancy<R, MAXM, INJECT, JUMPS>::MIN_BLOCKS))
+// TDB: FP32 OU run-table kernel with a time-dependent theta (a separate
+// instantiation, so that the common form carries no trace of the extra term)
+template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS, bool TDB = false>
+__global__ void __launch_bounds__(BLOCK, (FwdOccupancy<R, MODEL, MAXM, INJECT, JUMPS>::MIN_BLOCKS))
 sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     typedef Ar<R> A;
     constexpr int NCMAX = NoiseShape<MAXM, JUMPS>::NCMAX;
@@ -769,7 +780,8 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                     const int4 run = __ldg(a.runs + ri);
                     // rows padded to MAXM (d = b = c = 0 beyond M); read every step
                     // from L1 rather than held in registers across the run
-                    const float *tb = a.coef + ((int64_t)run.w * a.groups + g) * 2 * MAXM;
+                    constexpr int NB = TDB ? 3 : 2;   // coefficient vectors per row
+                    const float *tb = a.coef + ((int64_t)run.w * a.groups + g) * NB * MAXM;
 #pragma unroll 1
                     for (int k = run.x; k < run.y; ++k) {
                         R dW[MAXM], dJ[MAXM];
@@ -800,6 +812,10 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                             if (JUMPS) x = x + (float)dJ[m];
                             st[m] = (R)x;
                         }
+                        if constexpr (SHIFT && TDB) {   // a time-dependent theta
+#pragma unroll
+                            for (int m = 0; m < MAXM; ++m) st[m] = st[m] + __ldg(tb + 2 * MAXM + m);
+                        }
                     }
                     if (run.z >= 0) store(run.z, true);
                 }
@@ -808,6 +824,16 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                 for (int k = 0; k < n_steps; ++k) {
                     const R dt = a.dt[k];
                     const R sq = a.sqdt[k];
+                    if (a.prm_t) {   // uniform: time-dependent coefficients of step k
+                        const R *pk = a.prm_t + (int64_t)k * 3 * W;
+#pragma unroll
+                        for (int m = 0; m < MAXM; ++m) {
+                            const int w = g * M + (m < M ? m : 0);
+                            c0[m] = __ldg(pk + w);
+                            c1[m] = __ldg(pk + W + w);
+                            c2[m] = __ldg(pk + 2 * W + w);
+                        }
+                    }
                     R dW[MAXM], dJ[MAXM];
                     draw(k, sq, dW, dJ);
                     // ---- Euler step, sdepy's operation order ----------------------
@@ -919,15 +945,15 @@ coef_table_kernel(const double *tt, int n_steps, const double *x0, const double 
 template <typename R>
 using FwdLauncher = void (*)(const FwdArgs<R> &, dim3, cudaStream_t);
 
-template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS>
+template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS, bool TDB = false>
 void launch_fwd(const FwdArgs<R> &a, dim3 grid, cudaStream_t s) {
-    sde_fwd_kernel<R, MODEL, MAXM, INJECT, JUMPS><<<grid, BLOCK, 0, s>>>(a);
+    sde_fwd_kernel<R, MODEL, MAXM, INJECT, JUMPS, TDB><<<grid, BLOCK, 0, s>>>(a);
 }
 
-template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS>
+template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS, bool TDB = false>
 int fwd_max_blocks_per_sm() {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sde_fwd_kernel<R, MODEL, MAXM, INJECT, JUMPS>,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sde_fwd_kernel<R, MODEL, MAXM, INJECT, JUMPS, TDB>,
                                                   BLOCK, 0);
     return n;
 }
@@ -937,5 +963,7 @@ FwdLauncher<double> find_fwd_f64_linear(int model, int maxm, bool inject, bool j
 FwdLauncher<double> find_fwd_f64_ou_heston(int model, int maxm, bool inject, bool jumps, int *bps);
 FwdLauncher<float> find_fwd_f32_linear(int model, int maxm, bool inject, bool jumps, int *bps);
 FwdLauncher<float> find_fwd_f32_ou_heston(int model, int maxm, bool inject, bool jumps, int *bps);
+// FP32 OU run-table kernels with a time-dependent theta
+FwdLauncher<float> find_fwd_f32_ou_tdb(int maxm, int *bps);
 
 }  // namespace sdegpu

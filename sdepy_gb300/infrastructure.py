@@ -88,6 +88,40 @@ class process(np.ndarray):
     def pstd(self, dtype=None, ddof=0):
         return process(t=self.t, x=np.asarray(self).std(axis=-1, keepdims=True, dtype=dtype, ddof=ddof))
 
+    # interpolation in time (sdepy/infrastructure.py:545-633): a process is a
+    # valid time-dependent parameter of the presets
+    interp_kind = 'linear'
+
+    def interp(self, *, kind=None):
+        """``f`` with ``f(s)`` the process values interpolated at time(s)
+        ``s`` (scipy.interpolate.interp1d of the given kind, constant
+        outside the timeline; a one-point process is constant)."""
+        t, x = self.t, self.view(np.ndarray)
+        kind = self.interp_kind if kind is None else kind
+        if t.size == 1:
+            def f(s):
+                s = np.asarray(s)
+                return np.ones(s.shape + x.shape[1:], dtype=x.dtype) * \
+                    x.reshape(tuple(1 for i in s.shape) + x.shape[1:])
+            return f
+        import scipy.interpolate
+        g = scipy.interpolate.interp1d(t, x, axis=0, kind=kind, assume_sorted=True, copy=False,
+                                       bounds_error=False, fill_value=(x[0], x[-1]))
+
+        def f(s):
+            return g(s).astype(x.dtype, copy=False)
+        return f
+
+    def __call__(self, s, ds=None, *, kind=None):
+        """``p(s)``: values interpolated at ``s``; ``p(s, ds)``: their
+        increment from ``s`` to ``s + ds``."""
+        s = np.asarray(s)
+        f = self.interp(kind=kind)
+        if ds is None:
+            return f(s)
+        ds = np.asarray(ds)
+        return f(s + ds) - f(s)
+
 
 # ---------------------------------------------------------------------------
 # Philox keys
@@ -361,19 +395,29 @@ class wiener_source(source):
         return dz
 
 
+def _test_shape(f):
+    """Shape of f(1.), or None if the test call fails (sdepy's
+    _variable_param_setup, sdepy/infrastructure.py:64-125)."""
+    if isinstance(f, process):
+        return f.vshape + (f.paths,)
+    try:
+        return np.shape(f(1.))
+    except Exception:
+        return None
+
+
 class poisson_source(source):
-    """dn: Poisson increments with constant intensity ``lam``
+    """dn: Poisson increments with intensity ``lam``, a constant or a
+    callable evaluated at the middle of each step
     (sdepy/infrastructure.py:1566-1633)."""
 
     def __init__(self, *, paths=1, vshape=(), dtype=int, rng=None, lam=1.):
         super().__init__(paths=paths, vshape=vshape, dtype=dtype, rng=rng)
-        if callable(lam):
-            raise NotImplementedError(
-                'time-dependent intensities are not supported by the GPU '
-                'integrator')
-        self.lam = np.asarray(lam)
+        self.lam = lam if callable(lam) else np.asarray(lam)
+        shape = self.lam.shape if not callable(lam) else _test_shape(lam)
         try:
-            np.broadcast_to(np.empty(self.lam.shape), self.vshape + (paths,))
+            if shape is not None:
+                np.broadcast_to(np.empty(shape), self.vshape + (paths,))
         except ValueError:
             raise ValueError(
                 'cannot broadcast lambda parameter shaped {} to'
@@ -386,8 +430,8 @@ class poisson_source(source):
         tshape = dt.shape
         dn = np.empty(tshape + self.vshape + (self.paths,), dtype=self.dtype)
         for i in np.ndindex(tshape):
-            dn[i] = sign_dt[i]*self.rng.poisson(abs_dt[i]*self.lam,
-                                                self.vshape + (self.paths,))
+            L = self.lam(t[i] + dt[i]/2) if callable(self.lam) else self.lam
+            dn[i] = sign_dt[i]*self.rng.poisson(abs_dt[i]*L, self.vshape + (self.paths,))
         return dn
 
 

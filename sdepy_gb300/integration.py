@@ -11,9 +11,17 @@ Boundary (sdepy 1.2.1):
   integrator.euler_next             sdepy/integration.py:707-723
   presets                           sdepy/integration.py:2056-2747
 
-What stays an error (no CPU fallback): callable or process-valued
-parameters, per-path parameters, methods other than 'euler', dtypes other
-than float64 / float32, and SDE classes this module does not define.
+Time-dependent parameters: a callable or a ``process`` instance given for
+an SDE coefficient (e.g. ``theta=lambda t: ...``) is evaluated at the start
+of every step, as sdepy's SDE.A does (sdepy/integration.py:1216-1225), and a
+time-dependent Poisson intensity at the middle of every step, as sdepy's
+poisson_source does (sdepy/infrastructure.py:1629); the values go to the
+device as a per-step table (SdeGrid.params_t).
+
+What stays an error (no CPU fallback): time-dependent initial values,
+correlations and jump-size laws, per-path parameters, methods other than
+'euler', dtypes other than float64 / float32, and SDE classes this module
+does not define; gradients (the adjoint) take constant parameters.
 """
 import numpy as np
 
@@ -37,6 +45,14 @@ def _const(z, name):
             'time-dependent parameter {!r} is not supported by the GPU '
             'integrator'.format(name))
     return np.asarray(z, dtype=float)
+
+
+def _at(z, name, t):
+    """Value of parameter ``z`` at time ``t``: z(t) for a callable or a
+    process, else the constant."""
+    if z is not None and callable(z):
+        return np.asarray(z(t), dtype=float)
+    return _const(z, name)
 
 
 def _per_var(z, wshape, paths, name):
@@ -65,6 +81,7 @@ class _gpu_process:
     _model = _lib.MODEL_LINEAR
     _out = _lib.OUT_STATE
     _q = None              # number of equations (SDEs systems)
+    _tdep_names = ()       # parameters that may depend on time
 
     def __init__(self, *, paths=1, vshape=(), dtype=None, rng=None,
                  steps=None, i0=0, info=None, getinfo=True, method='euler',
@@ -210,13 +227,23 @@ class _gpu_process:
                 'supported by the GPU integrator'.format(_lib.MAX_GROUP))
         return W // M, M
 
-    def _coefficients(self):
-        """x0 (integration variable) and params[6][W] for the kernel."""
+    def _coefficients(self, t=1., tmid=1.):
+        """x0 (integration variable) and params[6][W] for the kernel, with
+        time-dependent SDE coefficients evaluated at ``t`` and a
+        time-dependent Poisson intensity at ``tmid``."""
         raise NotImplementedError
+
+    def _p(self, name, t):
+        return _at(self._args[name], name, t)
 
     def _setup_spec(self):
         self._W = int(np.prod(self.wshape, dtype=np.int64))
         self._G, self._M = self._groups()
+        self._tdep = any(self._args.get(n) is not None and callable(self._args[n])
+                         for n in self._tdep_names)
+        # constants, and time-dependent coefficients at t = 1 (sdepy's own
+        # test call, sdepy/infrastructure.py:64-109); the per-step values
+        # are tabulated for each integration leg
         self._x0, self._prm = self._coefficients()
         self._corr_c = None if self.corr is None else \
             np.ascontiguousarray(self.corr, dtype=float)
@@ -319,6 +346,17 @@ class _gpu_process:
             return self.exit(grid.tt_asis, xx), res
         return res
 
+    def _params_table(self, leg):
+        """[n_steps][6][W] parameters of each step of ``leg``: SDE
+        coefficients at the step's start, the Poisson intensity at its
+        middle."""
+        tt = leg.tt
+        tab = np.empty((leg.n_steps, _lib.MAX_PARAMS, self._W))
+        for k in range(leg.n_steps):
+            t0, t1 = float(tt[k]), float(tt[k + 1])
+            tab[k] = self._coefficients(t=t0, tmid=t0 + (t1 - t0)/2)[1]
+        return np.ascontiguousarray(tab)
+
     def _integrate(self, grid, write=True, stats=None):
         lib = _lib.load()
         rows = grid.n_rows
@@ -350,6 +388,8 @@ class _gpu_process:
             g.out_row = _lib.iptr(leg.out_row)
             g.n_pts = leg.tt.size
             g.step_offset = leg.step_offset
+            ptab = self._params_table(leg) if self._tdep else None
+            g.params_t = _lib.dptr(ptab)
             out = _lib.SdeOut()
             out.xx = None if xx is None else xx.ctypes.data
             out.n_rows = rows
@@ -472,15 +512,15 @@ class wiener_process(_gpu_process):
     """Wiener process with drift: dx = mu*dt + sigma*dw
     (sdepy/integration.py:2056-2116)."""
     _params = {'x0': 0., 'mu': 0., 'sigma': 1.}
+    _tdep_names = ('mu', 'sigma')
 
-    def _linear(self):
-        A = self._args
-        return _const(A['mu'], 'mu'), _const(A['sigma'], 'sigma')
+    def _linear(self, t):
+        return self._p('mu', t), self._p('sigma', t)
 
-    def _coefficients(self):
+    def _coefficients(self, t=1., tmid=1.):
         A = self._args
         ws, P = self.wshape, self.paths
-        cdt, cdw = self._linear()
+        cdt, cdw = self._linear(t)
         x0 = _per_var(_const(A['x0'], 'x0'), ws, P, 'x0')
         if self._log:
             x0 = np.log(x0)
@@ -488,7 +528,7 @@ class wiener_process(_gpu_process):
         prm[0] = _per_var(cdt, ws, P, 'mu')
         prm[1] = _per_var(cdw, ws, P, 'sigma')
         if 'dj' in self._sources and not self._inject:
-            prm[2] = _per_var(_const(A['lam'], 'lam'), ws, P, 'lam')
+            prm[2] = _per_var(self._p('lam', tmid), ws, P, 'lam')
             law = self._law
             if self._law_kind == 'norm':
                 prm[3] = _per_var(law.a, ws, P, 'a')
@@ -512,9 +552,8 @@ class lognorm_process(wiener_process):
     _log = True
     _out = _lib.OUT_EXP
 
-    def _linear(self):
-        A = self._args
-        mu, sigma = _const(A['mu'], 'mu'), _const(A['sigma'], 'sigma')
+    def _linear(self, t):
+        mu, sigma = self._p('mu', t), self._p('sigma', t)
         return mu - sigma*sigma/2, sigma
 
 
@@ -523,15 +562,16 @@ class ornstein_uhlenbeck_process(_gpu_process):
     (sdepy/integration.py:2185-2244)."""
     _params = {'x0': 0., 'theta': 0., 'k': 1., 'sigma': 1.}
     _model = _lib.MODEL_OU
+    _tdep_names = ('theta', 'k', 'sigma')
 
-    def _coefficients(self):
+    def _coefficients(self, t=1., tmid=1.):
         A = self._args
         ws, P = self.wshape, self.paths
         x0 = _per_var(_const(A['x0'], 'x0'), ws, P, 'x0')
         prm = np.zeros((_lib.MAX_PARAMS, self._W))
-        prm[0] = _per_var(_const(A['k'], 'k'), ws, P, 'k')
-        prm[1] = _per_var(_const(A['theta'], 'theta'), ws, P, 'theta')
-        prm[2] = _per_var(_const(A['sigma'], 'sigma'), ws, P, 'sigma')
+        prm[0] = _per_var(self._p('k', t), ws, P, 'k')
+        prm[1] = _per_var(self._p('theta', t), ws, P, 'theta')
+        prm[2] = _per_var(self._p('sigma', t), ws, P, 'sigma')
         return np.ascontiguousarray(x0), np.ascontiguousarray(prm)
 
 
@@ -564,6 +604,7 @@ class full_heston_process(_gpu_process):
     _params = {'x0': 1., 'mu': 0., 'sigma': 1., 'y0': 1., 'theta': 1.,
                'k': 1., 'xi': 1.}
     _model = _lib.MODEL_HESTON
+    _tdep_names = ('mu', 'sigma', 'theta', 'k', 'xi')
     _out = _lib.OUT_HESTON_XY
     _q = 2
 
@@ -583,14 +624,14 @@ class full_heston_process(_gpu_process):
                 '{}'.format(M//2))
         return self._W // M, M
 
-    def _coefficients(self):
+    def _coefficients(self, t=1., tmid=1.):
         A = self._args
         vs, P = self.vshape, self.paths
         h = self.wshape[-1]//2
         outer = int(np.prod(self.wshape[:-1], dtype=np.int64))
 
         def half(name, f=None):
-            v = _const(A[name], name)
+            v = _const(A[name], name) if name in ('x0', 'y0') else self._p(name, t)
             if f is not None:
                 v = f(v)
             return _per_var(v, vs, P, name).reshape(outer, h)
@@ -630,6 +671,7 @@ class jumpdiff_process(lognorm_process):
     (sdepy/integration.py:2576-2695)."""
     _params = {'x0': 1., 'mu': 0., 'sigma': 1.}
     _sources = ('dt', 'dw', 'dj')
+    _tdep_names = ('mu', 'sigma', 'lam')
 
 
 class merton_jumpdiff_process(jumpdiff_process):

@@ -22,6 +22,12 @@ def golden_cases():
                   if not f.endswith('_exact.npz'))
 
 
+def tdep_cases():
+    """Reference fixtures with time-dependent parameters (make_golden.py)."""
+    import glob
+    return sorted(glob.glob(os.path.join(GOLDEN, 'tdep_*.npz')))
+
+
 def quant_cases():
     """Fixtures of the reference's quantitative tests (make_quant.py)."""
     import glob

@@ -57,9 +57,26 @@ def corr8(seed=7):
     return C/np.outer(d, d)
 
 
+def encode_kw(sdepy, kw, arrays):
+    """JSON of the keyword arguments: a time-dependent parameter is
+    '@<function name>' (a function of tests/helpers.py) or '@process' with
+    the process stored as proc_<key>_t / proc_<key>_x arrays."""
+    out = {}
+    for k, v in kw.items():
+        if isinstance(v, sdepy.process):
+            arrays['proc_%s_t' % k] = np.asarray(v.t)
+            arrays['proc_%s_x' % k] = np.asarray(v)
+            out[k] = '@process'
+        elif callable(v):
+            out[k] = '@' + v.__name__
+        else:
+            out[k] = np.asarray(v).tolist()
+    return json.dumps(out)
+
+
 def run_case(sdepy, name, cls_name, kw, timeline, wshape, *, paths,
              steps=None, i0=0, corr=None, rho=None, jumps=None, seed=0,
-             dw_src=None):
+             dw_src=None, prefix='path'):
     inf = sdepy.infrastructure
     cls = getattr(sdepy, cls_name)
     rng = np.random.default_rng(seed)
@@ -78,13 +95,14 @@ def run_case(sdepy, name, cls_name, kw, timeline, wshape, *, paths,
     P = cls(**args)
     out = P(timeline)
     outs = out if isinstance(out, tuple) else (out,)
+    arrays = {}
     rec = {
         'name': name, 'cls': cls_name, 'paths': paths,
         'timeline': np.asarray(timeline),
         'steps': json.dumps(steps if (steps is None or np.isscalar(steps))
                             else list(steps)),
         'i0': i0,
-        'kw': json.dumps({k: np.asarray(v).tolist() for k, v in kw.items()}),
+        'kw': encode_kw(sdepy, kw, arrays),
         'corr': np.asarray(np.nan if corr is None else corr, dtype=float),
         'rec_t': np.array([c[0] for c in dw.calls]),
         'rec_dt': np.array([c[1] for c in dw.calls]),
@@ -106,8 +124,9 @@ def run_case(sdepy, name, cls_name, kw, timeline, wshape, *, paths,
         rec['jump_rate'] = P.info['jump_rate']
     if 'negative_y_count' in P.info:
         rec['negative_y_count'] = P.info['negative_y_count']
-    np.savez_compressed(os.path.join(HERE, 'path_%s.npz' % name), **rec)
-    print('wrote path_%s.npz' % name, rec['rec_dw'].shape)
+    rec.update(arrays)
+    np.savez_compressed(os.path.join(HERE, '%s_%s.npz' % (prefix, name)), **rec)
+    print('wrote %s_%s.npz' % (prefix, name), rec['rec_dw'].shape)
 
 
 def path_cases(sdepy):
@@ -222,6 +241,35 @@ def mc_cases(sdepy):
     print('wrote montecarlo.npz')
 
 
+def tdep_cases(sdepy):
+    """Time-dependent parameters: functions of t (tests/helpers.py) and a
+    process, evaluated by sdepy at each step's start (SDE.A) and, for a
+    Poisson intensity, at its middle (poisson_source)."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    import helpers as H
+    inf = sdepy.infrastructure
+    lin = np.linspace
+    run_case(sdepy, 'ou_theta_sigma', 'ornstein_uhlenbeck_process',
+             dict(x0=[[.3], [-.1]], k=H.tdep_k2, theta=H.tdep_theta2, sigma=H.tdep_sigma, vshape=2),
+             lin(0, 2, 5), (2,), paths=32, steps=40, i0=2, seed=31, prefix='tdep')
+    mu = sdepy.process(t=[0., .4, 1.], x=np.array([[.1], [-.05], [.2]]))
+    run_case(sdepy, 'lognorm_process_mu', 'lognorm_process',
+             dict(x0=1., mu=mu, sigma=H.tdep_sigma), lin(0, 1.5, 4), (), paths=40,
+             steps=30, seed=32, prefix='tdep')
+    run_case(sdepy, 'heston_theta_xi', 'heston_process',
+             dict(x0=100., mu=H.tdep_mu, y0=.04, k=1.5, theta=H.tdep_theta_h, xi=H.tdep_xi, rho=-.7),
+             np.array([0., .5, 1.]), (2,), paths=40, steps=50, rho=-.7, seed=33, prefix='tdep')
+    run_case(sdepy, 'merton_lam_mu', 'merton_jumpdiff_process',
+             dict(x0=1., mu=H.tdep_mu, sigma=.15, lam=H.tdep_lam, a=-.1, b=.15),
+             lin(0, 1, 3), (), paths=48, steps=60, seed=34, prefix='tdep',
+             jumps=dict(lam=H.tdep_lam, y=inf.norm_rv(-.1, .15)))
+    run_case(sdepy, 'hull_white_theta', 'hull_white_process',
+             dict(x0=[[.01], [.02]], k=[[.5], [2.]], theta=H.tdep_theta2, sigma=[[.01], [.02]],
+                  factors=2, rho=.3),
+             lin(0, 1, 3), (2,), paths=24, steps=20, rho=.3, seed=35, prefix='tdep')
+
+
 def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
     sys.path.insert(0, ref)
@@ -229,6 +277,7 @@ def main():
     print('sdepy', sdepy.__version__, 'numpy', np.__version__)
     path_cases(sdepy)
     mc_cases(sdepy)
+    tdep_cases(sdepy)
 
 
 if __name__ == '__main__':

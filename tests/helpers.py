@@ -24,6 +24,8 @@ def oracle_paths(clib, proc, timeline, seed, stream=0):
         g.out_row = _lib.iptr(leg.out_row)
         g.n_pts = leg.tt.size
         g.step_offset = leg.step_offset
+        ptab = proc._params_table(leg) if proc._tdep else None   # time-dependent parameters
+        g.params_t = _lib.dptr(ptab)
         neg = np.zeros((proc._G*proc._M//2, proc.paths), dtype=np.int32)
         jc = np.zeros((proc._W, proc.paths), dtype=np.int32)
         rj = np.zeros(rows, dtype=np.int64)
@@ -153,4 +155,57 @@ def quant_kwargs(z, record=False):
         kw['dj'] = dj
         for k in ('a', 'b', 'pa', 'lam'):   # the source carries the jump law
             kw.pop(k, None)
+    return kw
+
+
+# ---------------------------------------------------------------------------
+# time-dependent parameters of the tdep_* fixtures (tests/golden/make_golden.py
+# runs the reference with them; the tests run the drop-ins with them)
+# ---------------------------------------------------------------------------
+def tdep_theta2(t):
+    return np.array([[0.5 + 0.3*np.sin(2*t)], [-0.2*t]])
+
+
+def tdep_sigma(t):
+    return 0.2 + 0.1*t
+
+
+def tdep_mu(t):
+    return 0.05 - 0.03*t
+
+
+def tdep_theta_h(t):
+    return 0.04 + 0.02*t
+
+
+def tdep_xi(t):
+    return 0.5 + 0.2*np.cos(t)
+
+
+def tdep_lam(t):
+    return 2. + np.sin(3*t)
+
+
+def tdep_k2(t):
+    return np.array([[0.5 + 0.1*t], [2.]])
+
+
+TDEP = {name: f for name, f in dict(globals()).items() if name.startswith('tdep_')}
+
+
+def tdep_kwargs(z, process_cls):
+    """Keyword arguments of a tdep fixture: '@name' entries are the
+    functions above, '@process' entries the process stored in the fixture's
+    proc_<key>_t / proc_<key>_x arrays (built with ``process_cls``)."""
+    import json
+    kw = {}
+    for k, v in json.loads(str(z['kw'])).items():
+        if isinstance(v, str) and v == '@process':
+            kw[k] = process_cls(t=z['proc_%s_t' % k], x=z['proc_%s_x' % k])
+        elif isinstance(v, str) and v.startswith('@'):
+            kw[k] = TDEP[v[1:]]
+        elif k in ('vshape', 'factors'):
+            kw[k] = v
+        else:
+            kw[k] = np.asarray(v, dtype=float)
     return kw

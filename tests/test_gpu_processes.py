@@ -129,7 +129,7 @@ def test_unsupported_requests_raise(lib):
     with pytest.raises(NotImplementedError):
         sg.lognorm_process(sigma=np.linspace(.1, .2, 9), paths=9)   # per-path parameter
     with pytest.raises(NotImplementedError):
-        sg.merton_jumpdiff_process(lam=lambda t: t)
+        sg.merton_jumpdiff_process(x0=lambda t: 1. + t)   # time-dependent initial value
     with pytest.raises(NotImplementedError):
         sg.lognorm_process(x0=sg.process(t=(0., 1.), c=1.))
 

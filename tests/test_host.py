@@ -64,7 +64,7 @@ def test_argument_errors():
     with pytest.raises(ValueError):
         sg.lognorm_process(method='milstein')
     with pytest.raises(NotImplementedError):
-        sg.lognorm_process(mu=lambda t: t)
+        sg.lognorm_process(x0=lambda t: 1. + t)      # time-dependent initial value
     with pytest.raises(NotImplementedError):
         sg.lognorm_process(dtype=np.float16)
     with pytest.raises(ValueError):
@@ -77,6 +77,36 @@ def test_argument_errors():
         sg.heston_process(vshape=3)
     with pytest.raises(ValueError):
         sg.kou_jumpdiff_process(a=-1.)
+
+
+def test_time_dependent_parameter_tables():
+    # SDE coefficients at the start of each step (sdepy's SDE.A), a Poisson
+    # intensity at its middle (sdepy's poisson_source); a process parameter
+    # interpolated linearly, constant outside its timeline
+    from sdepy_gb300.grid import Grid
+    P = sg.ornstein_uhlenbeck_process(vshape=2, theta=lambda t: np.array([[t], [2*t]]), k=2., sigma=.3,
+                                      paths=5, steps=5)
+    assert P._tdep
+    leg = Grid((0., 1.), 5).legs[0]
+    tab = P._params_table(leg)
+    assert tab.shape == (leg.n_steps, 6, 2)
+    np.testing.assert_array_equal(tab[:, 1, 0], leg.tt[:-1])
+    np.testing.assert_array_equal(tab[:, 1, 1], 2*leg.tt[:-1])
+    assert np.all(tab[:, 0] == 2.) and np.all(tab[:, 2] == .3)
+    Q = sg.merton_jumpdiff_process(lam=lambda t: 1 + t, paths=3, steps=3)
+    leg = Grid((0., 1.), 3).legs[0]
+    mid = (leg.tt[:-1] + leg.tt[1:])/2
+    np.testing.assert_allclose(Q._params_table(leg)[:, 2, 0], 1 + mid, rtol=1e-15)
+    mu = sg.process(t=[0., 2.], x=np.array([[0.], [1.]]))
+    R = sg.lognorm_process(mu=mu, sigma=.2, paths=4, steps=5)
+    leg = Grid((0., 3.), 5).legs[0]
+    np.testing.assert_allclose(R._params_table(leg)[:, 0, 0],
+                               np.minimum(leg.tt[:-1]/2, 1.) - .2*.2/2, rtol=1e-15)
+    # a backward leg evaluates at its own step starts
+    S = sg.ornstein_uhlenbeck_process(theta=lambda t: t, paths=2, steps=4, i0=1)
+    legs = Grid((0., 1., 2.), 4, i0=1).legs
+    back = [lg for lg in legs if lg.tt[-1] < lg.tt[0]][0]
+    np.testing.assert_array_equal(S._params_table(back)[:, 1, 0], back.tt[:-1])
 
 
 def test_spec_lognorm():

@@ -1,0 +1,129 @@
+"""Time-dependent parameters (functions of t and processes): sdepy evaluates
+an SDE's coefficients at the start of every step (SDE.A,
+sdepy/integration.py:1216-1225) and a Poisson intensity at the middle of
+every step (sdepy/infrastructure.py:1629).
+
+* CPU: the numpy oracle replays the reference's recorded increments to its
+  paths exactly (tests/golden/tdep_*.npz, from make_golden.py);
+* GPU: the drop-ins replay them to 1e-12 per path (FP64, per-step parameter
+  tables on the device, forward and backward legs); with device noise the
+  FP64 kernels match the C oracle to 1e-12 and the FP32 kernels (with a
+  time-dependent OU theta: the run-table form with its theta offset) the FP64
+  oracle to FP32 accuracy; the adjoint refuses time-dependent parameters.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import sdepy_gb300 as sg
+from conftest import tdep_cases
+from helpers import TDEP, oracle_paths, tdep_kwargs
+from oracle import euler
+
+
+def _oracle_args(z):
+    kw = tdep_kwargs(z, sg.process)
+    vshape = kw.pop('vshape', ())
+    vshape = (vshape,) if isinstance(vshape, int) else tuple(vshape)
+    rho = kw.pop('rho', None)
+    corr = None
+    if rho is not None:
+        r = float(np.asarray(rho).reshape(-1)[0])
+        corr = np.array([[1., r], [r, 1.]])
+    cls = str(z['cls'])
+    _, wshape, _ = euler.shapes(cls, vshape, kw.get('factors', 1))
+    paths = int(z['paths'])
+    dw = euler.Replay(z['rec_dw'], paths=paths, vshape=wshape)
+    dj = euler.Replay(z['rec_dj'], dn=z['rec_dn'], paths=paths, vshape=wshape) if 'rec_dj' in z else None
+    return dict(preset=cls, params=kw, timeline=z['timeline'], paths=paths, vshape=vshape,
+                steps=json.loads(str(z['steps'])), i0=int(z['i0']), corr=corr, dw=dw, dj=dj)
+
+
+@pytest.mark.parametrize('path', tdep_cases(), ids=os.path.basename)
+def test_numpy_oracle_reproduces_reference_tdep(path):
+    z = np.load(path)
+    res, info = euler.integrate(**_oracle_args(z))
+    outs = res if isinstance(res, tuple) else (res,)
+    for k, o in enumerate(outs):
+        np.testing.assert_array_equal(o, z['xx%d' % k])
+    assert info['computed_steps'] == int(z['computed_steps'])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('path', tdep_cases(), ids=os.path.basename)
+def test_gpu_replay_matches_reference_tdep(lib, path):
+    z = np.load(path)
+    kw = tdep_kwargs(z, sg.process)
+    paths = int(z['paths'])
+    vshape = kw.get('vshape', ())
+    vshape = (vshape,) if isinstance(vshape, int) else tuple(vshape)
+    _, wshape, _ = euler.shapes(str(z['cls']), vshape, kw.get('factors', 1))
+    kw['dw'] = euler.Replay(z['rec_dw'], paths=paths, vshape=wshape)
+    if 'rec_dj' in z:
+        kw['dj'] = euler.Replay(z['rec_dj'], dn=z['rec_dn'], paths=paths, vshape=wshape)
+        for k in ('a', 'b', 'pa', 'lam'):
+            kw.pop(k, None)
+    P = getattr(sg, str(z['cls']))(paths=paths, steps=json.loads(str(z['steps'])), i0=int(z['i0']), **kw)
+    assert P._tdep
+    out = P(z['timeline'])
+    outs = out if isinstance(out, tuple) else (out,)
+    for k, o in enumerate(outs):
+        ref = z['xx%d' % k]
+        err = np.max(np.abs(np.asarray(o) - ref)/np.maximum(np.abs(ref), 1.))
+        assert err <= 1e-12, err
+    assert P.info['computed_steps'] == int(z['computed_steps'])
+
+
+DEVICE_CASES = [
+    ('ou', sg.ornstein_uhlenbeck_process,
+     dict(vshape=2, x0=[[.3], [-.1]], k=TDEP['tdep_k2'], theta=TDEP['tdep_theta2'], sigma=TDEP['tdep_sigma']),
+     np.linspace(0, 2, 5), 40, 2),
+    ('ou_corr', sg.ornstein_uhlenbeck_process,
+     dict(vshape=2, x0=0., k=1.5, theta=TDEP['tdep_theta2'], sigma=.3, corr=[[1., .4], [.4, 1.]]),
+     np.linspace(0, 1, 6), 50, 0),
+    ('lognorm', sg.lognorm_process, dict(x0=1., mu=TDEP['tdep_mu'], sigma=TDEP['tdep_sigma']),
+     np.linspace(0, 1, 5), 40, 0),
+    ('heston', sg.heston_process,
+     dict(x0=100., mu=TDEP['tdep_mu'], y0=.04, k=1.5, theta=TDEP['tdep_theta_h'], xi=TDEP['tdep_xi'], rho=-.7),
+     (0., .5, 1.), 60, 0),
+    ('merton', sg.merton_jumpdiff_process,
+     dict(x0=1., mu=TDEP['tdep_mu'], sigma=.15, lam=TDEP['tdep_lam'], a=-.1, b=.15),
+     np.linspace(0, 1, 3), 80, 0),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('case', DEVICE_CASES, ids=[c[0] for c in DEVICE_CASES])
+def test_device_rng_tdep_matches_c_oracle(lib, clib, case):
+    name, cls, kw, tl, steps, i0 = case
+    paths, seed = 777, 0x51ed
+    P = cls(paths=paths, steps=steps, i0=i0, rng=sg.philox_rng(seed, 3), **kw)
+    assert P._tdep
+    out = P(tl)
+    got = np.concatenate([np.asarray(o).reshape(len(o.t), -1, paths) for o in
+                          (out if isinstance(out, tuple) else (out,))], axis=1)
+    ref, info = oracle_paths(clib, P, tl, seed, 3)
+    ref = ref.reshape(got.shape)
+    err = np.max(np.abs(got - ref)/np.maximum(np.abs(ref), 1.))
+    assert err <= 1e-12, err
+    if 'jump_count' in P.info:
+        np.testing.assert_array_equal(P.info['jump_count'].reshape(-1, paths), info['jump_count'])
+        assert info['jump_count'].sum() > 0
+    # FP32: the same draws, FP32 arithmetic
+    P32 = cls(paths=paths, steps=steps, i0=i0, dtype=np.float32, rng=sg.philox_rng(seed, 3), **kw)
+    out32 = P32(tl)
+    g32 = np.concatenate([np.asarray(o, dtype=float).reshape(len(o.t), -1, paths) for o in
+                          (out32 if isinstance(out32, tuple) else (out32,))], axis=1)
+    assert np.max(np.abs(g32 - ref)/np.maximum(np.abs(ref), 1.)) < 2e-3
+    assert np.max(np.abs(g32.mean(-1) - ref.mean(-1))/np.maximum(np.abs(ref.mean(-1)), 1.)) < 2e-5
+
+
+@pytest.mark.gpu
+def test_adjoint_refuses_time_dependent_parameters(lib):
+    from sdepy_gb300.autograd import expectation
+    import torch
+    with pytest.raises(NotImplementedError):
+        expectation(sg.lognorm_process, (0., 1.), [], paths=100, steps=10,
+                    x0=torch.tensor(1., requires_grad=True), mu=TDEP['tdep_mu'], sigma=.2)
