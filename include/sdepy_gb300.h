@@ -82,6 +82,13 @@ extern "C" {
 #define SDE_OUT_HESTON_X   3  /* exp() of the first half (heston_process)      */
 #define SDE_OUT_HESTON_XY  4  /* exp() of first half, second half as is        */
 
+/* SdeSpec.flags: antithetic paths (device noise only): with paths = 2K,
+ * path K + q takes the draws of path q with opposite Wiener increments and
+ * the same Poisson counts and jump sizes, as sdepy's odd_wiener_source with
+ * even_cpoisson_source (sdepy/infrastructure.py:2047-2150); groups of up to
+ * 8 states, constant or time-dependent coefficients except an OU theta. */
+#define SDE_FLAG_ANTITHETIC 1
+
 typedef struct SdeSpec {
     int32_t abi_version;   /* SDE_ABI_VERSION */
     int32_t model;         /* SDE_MODEL_* */
@@ -91,7 +98,7 @@ typedef struct SdeSpec {
     int32_t groups;        /* independent groups per path */
     int32_t group_size;    /* M: states per group, 1..SDE_MAX_GROUP */
     int32_t out_mode;      /* SDE_OUT_* */
-    int32_t reserved0;
+    int32_t flags;         /* SDE_FLAG_* */
     const double *x0;      /* [groups*M] initial state (already log()-ed for log models) */
     const double *params;  /* [SDE_MAX_PARAMS][groups*M] */
     const double *corr;    /* [M*M] correlation matrix shared by all groups, or NULL */

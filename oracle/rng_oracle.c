@@ -19,7 +19,9 @@
  * Box-Muller pair's z0 to step k and z1 to step k + 1, and its words z and
  * w are the Poisson uniforms of steps k and k + 1.  Groups of two
  * variables without jumps also draw one call per two steps: words (x, y)
- * give the normals of step k, words (z, w) those of step k + 1.
+ * give the normals of step k, words (z, w) those of step k + 1.  With
+ * SDE_FLAG_ANTITHETIC (paths = 2K) path K + q takes the counters of path q,
+ * with opposite normals and the same jumps.
  *
  * Compiled with -ffp-contract=off so that every product and sum rounds as
  * written.  Pinned by the published Philox-4x32-10 known-answer vectors and by
@@ -144,7 +146,11 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
     if (rowj) memset(rowj, 0, sizeof(int64_t) * n_rows);
     const double *prm = s->params;
     int rc = 0;
+    const int anti = (s->flags & SDE_FLAG_ANTITHETIC) != 0;
     for (int64_t p = 0; p < paths && !rc; ++p) {
+        /* the counters' path word, and the sign of the normals */
+        const int64_t pc = (anti && p >= paths / 2) ? p - paths / 2 : p;
+        const double zsign = (anti && p >= paths / 2) ? -1.0 : 1.0;
         for (int gi = 0; gi < G && !rc; ++gi) {
             double st[SDE_MAX_GROUP], z[SDE_MAX_GROUP + 1], dW[SDE_MAX_GROUP], dJ[SDE_MAX_GROUP];
             int negc[SDE_MAX_GROUP] = {0}, jc[SDE_MAX_GROUP] = {0};
@@ -166,7 +172,7 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
                     uint32_t u[4 * ((2 * SDE_MAX_GROUP + 2 + 3) / 4) + 4];
                     if (M == 1) {
                         if ((k & 1) == 0) {
-                            const uint32_t ctr[4] = {(uint32_t)p, c1, (uint32_t)gi << 8, s->stream};
+                            const uint32_t ctr[4] = {(uint32_t)pc, c1, (uint32_t)gi << 8, s->stream};
                             uint32_t r[4];
                             oracle_philox(ctr, key, r);
                             oracle_normal2(r[0], r[1], &pz0, &pz1);
@@ -177,7 +183,7 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
                         u[2] = (k & 1) ? pw1 : pw0;   /* the Poisson word, index 2P + m */
                     } else if (M == 2 && !jumps) {
                         if ((k & 1) == 0) {
-                            const uint32_t ctr[4] = {(uint32_t)p, c1, (uint32_t)gi << 8, s->stream};
+                            const uint32_t ctr[4] = {(uint32_t)pc, c1, (uint32_t)gi << 8, s->stream};
                             uint32_t r[4];
                             oracle_philox(ctr, key, r);
                             oracle_normal2(r[0], r[1], &pz[0], &pz[1]);
@@ -187,12 +193,14 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
                         z[1] = (k & 1) ? pz[3] : pz[1];
                     } else {
                         for (int c = 0; c < NC; ++c) {
-                            const uint32_t ctr[4] = {(uint32_t)p, c1, ((uint32_t)gi << 8) | (uint32_t)c, s->stream};
+                            const uint32_t ctr[4] = {(uint32_t)pc, c1, ((uint32_t)gi << 8) | (uint32_t)c, s->stream};
                             oracle_philox(ctr, key, &u[4 * c]);
                         }
                         for (int q = 0; q < P; ++q)
                             oracle_normal2(u[2 * q], u[2 * q + 1], &z[2 * q], &z[2 * q + 1]);
                     }
+                    if (zsign < 0)   /* the antithetic path */
+                        for (int m = 0; m < M; ++m) z[m] = -z[m];
                     for (int m = 0; m < M; ++m) {
                         if (s->corr) {
                             double acc = L[m * M + 0] * z[0];
@@ -214,7 +222,7 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
                                 if (cnt < 0) { rc = -1; break; }
                                 double S = 0.0;
                                 for (int j = 0; j < cnt; ++j) {
-                                    const uint32_t ctr[4] = {(uint32_t)p, c1,
+                                    const uint32_t ctr[4] = {(uint32_t)pc, c1,
                                                              0x80000000u | ((uint32_t)w << 12) | (uint32_t)j, s->stream};
                                     uint32_t r[4];
                                     oracle_philox(ctr, key, r);

@@ -6,7 +6,8 @@ presets) integrate on the GPU through the C-ABI of include/sdepy_gb300.h;
 """
 from .infrastructure import (
     process, philox_rng, wiener_source, poisson_source, cpoisson_source,
-    norm_rv, uniform_rv, exp_rv, double_exp_rv)
+    norm_rv, uniform_rv, exp_rv, double_exp_rv, odd_wiener_source,
+    even_poisson_source, even_cpoisson_source)
 from .integration import (
     wiener_process, lognorm_process, ornstein_uhlenbeck_process,
     hull_white_process, hull_white_1factor_process, full_heston_process,
@@ -20,6 +21,7 @@ __version__ = '0.1.0'
 __all__ = [
     'process', 'philox_rng', 'wiener_source', 'poisson_source',
     'cpoisson_source', 'norm_rv', 'uniform_rv', 'exp_rv', 'double_exp_rv',
+    'odd_wiener_source', 'even_poisson_source', 'even_cpoisson_source',
     'wiener_process', 'lognorm_process', 'ornstein_uhlenbeck_process',
     'hull_white_process', 'hull_white_1factor_process',
     'full_heston_process', 'heston_process', 'jumpdiff_process',

@@ -25,6 +25,7 @@ MODEL_LINEAR, MODEL_OU, MODEL_HESTON = 0, 1, 2
 JUMP_NONE, JUMP_NORM, JUMP_DOUBLE_EXP, JUMP_UNIFORM, JUMP_EXP = 0, 1, 2, 3, 4
 FP64, FP32 = 0, 1
 OUT_STATE, OUT_EXP, OUT_SUM, OUT_HESTON_X, OUT_HESTON_XY = 0, 1, 2, 3, 4
+FLAG_ANTITHETIC = 1
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -36,7 +37,7 @@ class SdeSpec(C.Structure):
                 ('precision', C.c_int32), ('jump_law', C.c_int32),
                 ('paths', C.c_int64), ('groups', C.c_int32),
                 ('group_size', C.c_int32), ('out_mode', C.c_int32),
-                ('reserved0', C.c_int32),
+                ('flags', C.c_int32),
                 ('x0', _dp), ('params', _dp), ('corr', _dp),
                 ('seed', C.c_uint64), ('stream', C.c_uint32),
                 ('reserved1', C.c_uint32)]

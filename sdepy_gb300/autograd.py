@@ -128,6 +128,9 @@ def expectation(cls, timeline, strikes=(), *, paths, steps=None,
             plain[k] = v
     if 'rho' in plain and name != 'heston_process':
         raise NotImplementedError('rho is differentiable for heston_process only')
+    if any(k in plain for k in ('dw', 'dj', 'dn')):
+        raise NotImplementedError('gradients are taken on the default device sources '
+                                  '(no explicit, injected or antithetic sources)')
     if any(callable(v) for v in plain.values()):
         raise NotImplementedError('gradients need constant parameters (the adjoint '
                                   'kernel takes no time-dependent parameters)')

@@ -310,6 +310,9 @@ template <> struct Finder<double> {
         return f ? f : find_fwd_f64_ou_heston(model, maxm, inj, jmp, bps);
     }
     static FwdLauncher<double> find_tdb(int, int *) { return nullptr; }
+    static FwdLauncher<double> find_anti(int model, int maxm, bool jmp, int *bps) {
+        return find_fwd_f64_anti(model, maxm, jmp, bps);
+    }
 };
 template <> struct Finder<float> {
     static FwdLauncher<float> find(int model, int maxm, bool inj, bool jmp, int *bps) {
@@ -318,6 +321,9 @@ template <> struct Finder<float> {
     }
     // OU run-table kernels with a time-dependent theta
     static FwdLauncher<float> find_tdb(int maxm, int *bps) { return find_fwd_f32_ou_tdb(maxm, bps); }
+    static FwdLauncher<float> find_anti(int model, int maxm, bool jmp, int *bps) {
+        return find_fwd_f32_anti(model, maxm, jmp, bps);
+    }
 };
 
 // number of blocks along paths: enough for every SM, capped by the paths
@@ -345,6 +351,15 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     if ((rc = check_grid(gr, out->n_rows))) return rc;
     const bool jumps = s->jump_law != SDE_JUMP_NONE;
     const bool inject = noise != nullptr;
+    const bool anti = (s->flags & SDE_FLAG_ANTITHETIC) != 0;
+    if (s->flags & ~SDE_FLAG_ANTITHETIC) return fail(SDE_ERR_INVALID, "unknown spec flags %d", s->flags);
+    if (anti) {
+        if (inject) return fail(SDE_ERR_INVALID, "antithetic paths are drawn on the device, not injected");
+        if (s->paths % 2)
+            return fail(SDE_ERR_INVALID, "the number of paths for sources with antithetics should be even, not %lld",
+                        (long long)s->paths);
+        if (s->group_size > 8) return fail(SDE_ERR_UNSUPPORTED, "antithetic paths take groups of up to 8 states");
+    }
     if (inject) {
         if (!noise->dw) return fail(SDE_ERR_INVALID, "injected noise needs dw");
         if (jumps && !noise->dj) return fail(SDE_ERR_INVALID, "injected noise of a jump model needs dj");
@@ -652,10 +667,13 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
 
     // ---- launch ----------------------------------------------------------------------
     int bps = 0;
-    FwdLauncher<R> L = ou_b ? Finder<R>::find_tdb(maxm_of(M), &bps)
-                            : Finder<R>::find(s->model, maxm_of(M), inject, jumps, &bps);
+    if (anti && ou_b) return fail(SDE_ERR_UNSUPPORTED, "antithetic paths with a time-dependent OU theta");
+    FwdLauncher<R> L = anti   ? Finder<R>::find_anti(s->model, maxm_of(M), jumps, &bps)
+                       : ou_b ? Finder<R>::find_tdb(maxm_of(M), &bps)
+                              : Finder<R>::find(s->model, maxm_of(M), inject, jumps, &bps);
     if (!L) return fail(SDE_ERR_UNSUPPORTED, "no kernel for model %d group size %d", s->model, M);
-    const int nbx = path_blocks(D, paths, s->groups, bps);
+    // antithetic kernels integrate two paths per thread
+    const int nbx = path_blocks(D, anti ? paths / 2 : paths, s->groups, bps);
     a.stats_row = -1;
     const int bins = stats ? req->bins : 0;
     if (stats) {
@@ -1083,6 +1101,7 @@ extern "C" int32_t sde_adjoint(const SdeSpec *spec, const SdeGrid *grid, const S
     if (!spec) return fail(SDE_ERR_INVALID, "spec is NULL");
     if (grid && grid->params_t)
         return fail(SDE_ERR_UNSUPPORTED, "the adjoint takes constant parameters (grid params_t must be NULL)");
+    if (spec->flags) return fail(SDE_ERR_UNSUPPORTED, "the adjoint takes no spec flags (antithetic paths)");
     if (spec->precision == SDE_FP32) return adjoint_impl<float>(spec, grid, req, grad, value);
     return adjoint_impl<double>(spec, grid, req, grad, value);
 }

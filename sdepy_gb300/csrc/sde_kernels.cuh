@@ -577,26 +577,33 @@ __device__ __forceinline__ void jump_size_grad(int law, uint4 r, R ja, R jb, R j
 // the forward kernel
 // ---------------------------------------------------------------------------
 // FP32 device-RNG kernels without jumps, up to 8 states per thread (4 for
-// Heston, whose step keeps more values live), are held to 80 registers: 3
-// resident blocks (24 warps) per SM
-template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS>
+// Heston, whose step keeps more values live; half that for antithetic
+// kernels, which carry two paths), are held to 80 registers: 3 resident
+// blocks (24 warps) per SM
+template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS, bool ANTI = false>
 struct FwdOccupancy {
-    static constexpr int MIN_BLOCKS =
-        (sizeof(R) == 4 && MAXM <= (MODEL == SDE_MODEL_HESTON ? 4 : 8) && !INJECT && !JUMPS) ? 3 : 1;
+    static constexpr int CAP_M = (MODEL == SDE_MODEL_HESTON ? 4 : 8) / (ANTI ? 2 : 1);
+    static constexpr int MIN_BLOCKS = (sizeof(R) == 4 && MAXM <= CAP_M && !INJECT && !JUMPS) ? 3 : 1;
 };
 
 // TDB: FP32 OU run-table kernel with a time-dependent theta (a separate
-// instantiation, so that the common form carries no trace of the extra term)
-template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS, bool TDB = false>
-__global__ void __launch_bounds__(BLOCK, (FwdOccupancy<R, MODEL, MAXM, INJECT, JUMPS>::MIN_BLOCKS))
+// instantiation, so that the common form carries no trace of the extra term).
+// ANTI: antithetic paths (device noise): paths q and q + K (K = paths / 2)
+// share their draws, the second with the opposite Wiener increments and
+// the same jumps (sdepy's odd_wiener_source / even_cpoisson_source,
+// sdepy/infrastructure.py:2047-2150); one thread integrates both, drawing
+// once.
+template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS, bool TDB = false, bool ANTI = false>
+__global__ void __launch_bounds__(BLOCK, (FwdOccupancy<R, MODEL, MAXM, INJECT, JUMPS, ANTI>::MIN_BLOCKS))
 sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     typedef Ar<R> A;
     constexpr int NCMAX = NoiseShape<MAXM, JUMPS>::NCMAX;
     constexpr bool TAB = sizeof(R) == 4 && MODEL != SDE_MODEL_HESTON && !INJECT;
     constexpr bool SHIFT = TAB && MODEL == SDE_MODEL_OU;  // state held as x - theta
+    constexpr int NA = ANTI ? 2 : 1;   // paths per thread
     __shared__ R red[BLOCK / 32];
     __shared__ double part[MAXM][NPART];
-    __shared__ R svs[MAXM][BLOCK];   // this round's value of each output at the stats row
+    __shared__ R svs[NA][MAXM][BLOCK];   // this round's value of each output at the stats row
 
     const int g = blockIdx.y;
     const int M = a.M;
@@ -632,36 +639,49 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     }
 
     const int64_t stride = (int64_t)gridDim.x * BLOCK;
-    const int64_t rounds = (a.paths + stride - 1) / stride;
+    const int64_t npath = ANTI ? a.paths / 2 : a.paths;   // paths (pairs with ANTI) over threads
+    const int64_t rounds = (npath + stride - 1) / stride;
     for (int64_t rd = 0; rd < rounds; ++rd) {
         const int64_t p = rd * stride + (int64_t)blockIdx.x * BLOCK + threadIdx.x;
-        const bool act = p < a.paths;
+        const bool act = p < npath;
         if (do_stats) {
 #pragma unroll
-            for (int m = 0; m < MAXM; ++m) svs[m][threadIdx.x] = R(0);
+            for (int i = 0; i < NA; ++i)
+#pragma unroll
+                for (int m = 0; m < MAXM; ++m) svs[i][m][threadIdx.x] = R(0);
         }
         if (act) {
             R st[MAXM];
+            R st1[ANTI ? MAXM : 1];   // the antithetic path p + npath
 #pragma unroll
             for (int m = 0; m < MAXM; ++m) st[m] = x0[m];
-            int negc[MAXM];
+            if constexpr (ANTI) {
+#pragma unroll
+                for (int m = 0; m < MAXM; ++m) st1[m] = x0[m];
+            }
+            int negc[MAXM], negc1[ANTI ? MAXM : 1];
             int jcnt[MAXM];
 #pragma unroll
             for (int m = 0; m < MAXM; ++m) { negc[m] = 0; jcnt[m] = 0; }
+            if constexpr (ANTI) {
+#pragma unroll
+                for (int m = 0; m < MAXM; ++m) negc1[m] = 0;
+            }
             unsigned int row_jc = 0;
 
-            // store helper (lambda keeps the loop body readable); sh: the
-            // state is the deviation from theta
-            auto store = [&](int row, bool sh) {
+            // store helper (lambda keeps the loop body readable): state s of
+            // path pth, stats values in slot i; sh: the state is the
+            // deviation from theta
+            auto store1 = [&](int row, bool sh, const R (&s)[MAXM], int64_t pth, int i) {
                 R ov[MAXM];
                 int no;
                 if (SHIFT && sh) {
                     R sx[MAXM];
 #pragma unroll
-                    for (int m = 0; m < MAXM; ++m) sx[m] = st[m] + (R)__ldg(a.tshift + g * 2 * MAXM + m);
+                    for (int m = 0; m < MAXM; ++m) sx[m] = s[m] + (R)__ldg(a.tshift + g * 2 * MAXM + m);
                     no = group_outputs<R, MAXM>(sx, M, a.out_mode, ov);
                 } else {
-                    no = group_outputs<R, MAXM>(st, M, a.out_mode, ov);
+                    no = group_outputs<R, MAXM>(s, M, a.out_mode, ov);
                 }
                 if (a.xx) {
 #pragma unroll
@@ -669,18 +689,22 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                         if (m < no)
                             // streaming store: the path output must not evict
                             // the per-step tables from L2
-                            __stcs(&a.xx[((int64_t)row * a.n_out_vars + (int64_t)g * a.opg + m) * a.paths + p], ov[m]);
+                            __stcs(&a.xx[((int64_t)row * a.n_out_vars + (int64_t)g * a.opg + m) * a.paths + pth], ov[m]);
                 }
                 if (row == a.stats_row) {
 #pragma unroll
-                    for (int m = 0; m < MAXM; ++m) svs[m][threadIdx.x] = ov[m];
+                    for (int m = 0; m < MAXM; ++m) svs[i][m][threadIdx.x] = ov[m];
                     if (a.stats_vals) {
 #pragma unroll
                         for (int m = 0; m < MAXM; ++m)
                             if (m < no)
-                                __stcs(&a.stats_vals[((int64_t)g * a.opg + m) * a.paths + p], ov[m]);
+                                __stcs(&a.stats_vals[((int64_t)g * a.opg + m) * a.paths + pth], ov[m]);
                     }
                 }
+            };
+            auto store = [&](int row, bool sh) {
+                store1(row, sh, st, p, 0);
+                if constexpr (ANTI) store1(row, sh, st1, p + npath, 1);
                 if (JUMPS && a.row_jumps) {
                     if (row_jc) atomicAdd(&a.row_jumps[row], (unsigned long long)row_jc);
                     row_jc = 0;
@@ -694,6 +718,10 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
             if (SHIFT && n_steps > 0) {
 #pragma unroll
                 for (int m = 0; m < MAXM; ++m) st[m] = (R)__ldg(a.tshift + (g * 2 + 1) * MAXM + m);
+                if constexpr (ANTI) {
+#pragma unroll
+                    for (int m = 0; m < MAXM; ++m) st1[m] = st[m];
+                }
             }
             const PathPre<NCMAX> pre(key, (uint32_t)p, (uint32_t)g, a.stream);
             constexpr int NZ = Paired<MAXM, JUMPS>::NZ;
@@ -716,7 +744,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                     dJ[m] = A::mul(a.sgn, S);
                     const int sc = a.sgn < R(0) ? -cnt : cnt;
                     jcnt[m] += sc;
-                    row_jc += (unsigned int)cnt;
+                    row_jc += (unsigned int)(NA * cnt);   // the antithetic path jumps alike
                 }
             };
             // increments of step k: injected, or drawn from Philox counters
@@ -803,19 +831,24 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                                 cc[m] = __ldg(tb + MAXM + m);
                             }
                         }
+                        // one state array, increments dW times sgn
+                        auto tab_update = [&](R (&s)[MAXM], float sgn) {
 #pragma unroll
-                        for (int m = 0; m < MAXM; ++m) {
-                            float x = (float)st[m];
-                            if (SHIFT) x = fmaf(-ca[m], x, x);   // y - d y
-                            else x = x + ca[m];                  // x + b
-                            x = fmaf(cc[m], (float)dW[m], x);
-                            if (JUMPS) x = x + (float)dJ[m];
-                            st[m] = (R)x;
-                        }
-                        if constexpr (SHIFT && TDB) {   // a time-dependent theta
+                            for (int m = 0; m < MAXM; ++m) {
+                                float x = (float)s[m];
+                                if (SHIFT) x = fmaf(-ca[m], x, x);   // y - d y
+                                else x = x + ca[m];                  // x + b
+                                x = fmaf(sgn * cc[m], (float)dW[m], x);
+                                if (JUMPS) x = x + (float)dJ[m];
+                                s[m] = (R)x;
+                            }
+                            if constexpr (SHIFT && TDB) {   // a time-dependent theta
 #pragma unroll
-                            for (int m = 0; m < MAXM; ++m) st[m] = st[m] + __ldg(tb + 2 * MAXM + m);
-                        }
+                                for (int m = 0; m < MAXM; ++m) s[m] = s[m] + __ldg(tb + 2 * MAXM + m);
+                            }
+                        };
+                        tab_update(st, 1.0f);
+                        if constexpr (ANTI) tab_update(st1, -1.0f);
                     }
                     if (run.z >= 0) store(run.z, true);
                 }
@@ -837,6 +870,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                     R dW[MAXM], dJ[MAXM];
                     draw(k, sq, dW, dJ);
                     // ---- Euler step, sdepy's operation order ----------------------
+                    auto euler = [&](R (&st)[MAXM], const R (&dW)[MAXM], int (&negc)[MAXM]) {
                     if (MODEL == SDE_MODEL_LINEAR) {
 #pragma unroll
                         for (int m = 0; m < MAXM; ++m) {
@@ -874,6 +908,14 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
 #pragma unroll
                         for (int m = 0; m < MAXM; ++m) st[m] = nx[m];
                     }
+                    };
+                    euler(st, dW, negc);
+                    if constexpr (ANTI) {   // the antithetic path: exactly opposite increments
+                        R dWn[MAXM];
+#pragma unroll
+                        for (int m = 0; m < MAXM; ++m) dWn[m] = -dW[m];
+                        euler(st1, dWn, negc1);
+                    }
                     const int r = a.out_row[k + 1];
                     if (r >= 0) store(r, false);
                 }
@@ -881,19 +923,28 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
             if (MODEL == SDE_MODEL_HESTON && a.neg_count) {
                 constexpr int h = MAXM / 2;
 #pragma unroll
-                for (int i = 0; i < h; ++i) a.neg_count[((int64_t)g * h + i) * a.paths + p] = negc[i];
+                for (int i = 0; i < h; ++i) {
+                    a.neg_count[((int64_t)g * h + i) * a.paths + p] = negc[i];
+                    if constexpr (ANTI) a.neg_count[((int64_t)g * h + i) * a.paths + p + npath] = negc1[i];
+                }
             }
             if (JUMPS && a.jump_count) {
 #pragma unroll
                 for (int m = 0; m < MAXM; ++m)
-                    if (m < M) a.jump_count[((int64_t)g * M + m) * a.paths + p] = jcnt[m];
+                    if (m < M) {
+                        a.jump_count[((int64_t)g * M + m) * a.paths + p] = jcnt[m];
+                        if constexpr (ANTI) a.jump_count[((int64_t)g * M + m) * a.paths + p + npath] = jcnt[m];
+                    }
             }
         }
         if (do_stats) {
 #pragma unroll
-            for (int m = 0; m < MAXM; ++m) {
-                if (m < a.opg) block_round_stats<R>(svs[m][threadIdx.x], act, a.strikes, a.n_strikes, part[m], red);
-            }
+            for (int i = 0; i < NA; ++i)
+#pragma unroll
+                for (int m = 0; m < MAXM; ++m) {
+                    if (m < a.opg)
+                        block_round_stats<R>(svs[i][m][threadIdx.x], act, a.strikes, a.n_strikes, part[m], red);
+                }
         }
     }
     if (do_stats) {
@@ -945,15 +996,15 @@ coef_table_kernel(const double *tt, int n_steps, const double *x0, const double 
 template <typename R>
 using FwdLauncher = void (*)(const FwdArgs<R> &, dim3, cudaStream_t);
 
-template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS, bool TDB = false>
+template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS, bool TDB = false, bool ANTI = false>
 void launch_fwd(const FwdArgs<R> &a, dim3 grid, cudaStream_t s) {
-    sde_fwd_kernel<R, MODEL, MAXM, INJECT, JUMPS, TDB><<<grid, BLOCK, 0, s>>>(a);
+    sde_fwd_kernel<R, MODEL, MAXM, INJECT, JUMPS, TDB, ANTI><<<grid, BLOCK, 0, s>>>(a);
 }
 
-template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS, bool TDB = false>
+template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS, bool TDB = false, bool ANTI = false>
 int fwd_max_blocks_per_sm() {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sde_fwd_kernel<R, MODEL, MAXM, INJECT, JUMPS, TDB>,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sde_fwd_kernel<R, MODEL, MAXM, INJECT, JUMPS, TDB, ANTI>,
                                                   BLOCK, 0);
     return n;
 }
@@ -965,5 +1016,8 @@ FwdLauncher<float> find_fwd_f32_linear(int model, int maxm, bool inject, bool ju
 FwdLauncher<float> find_fwd_f32_ou_heston(int model, int maxm, bool inject, bool jumps, int *bps);
 // FP32 OU run-table kernels with a time-dependent theta
 FwdLauncher<float> find_fwd_f32_ou_tdb(int maxm, int *bps);
+// antithetic kernels (device noise, groups of up to 8 states)
+FwdLauncher<float> find_fwd_f32_anti(int model, int maxm, bool jumps, int *bps);
+FwdLauncher<double> find_fwd_f64_anti(int model, int maxm, bool jumps, int *bps);
 
 }  // namespace sdegpu

@@ -475,3 +475,58 @@ class cpoisson_source(source):
         self.dn_value = dn
         self.y_value = y_value
         return dz
+
+
+# ---------------------------------------------------------------------------
+# antithetic sources (sdepy/infrastructure.py:2047-2150): with paths = 2K the
+# trailing K paths are a transform of the leading K
+# ---------------------------------------------------------------------------
+def _antithetic(base, transform, name, doc):
+    class antithetic(source):
+        def __init__(self, *, paths=2, vshape=(), dtype=None, rng=None, **args):
+            if paths % 2:
+                raise ValueError('the number of paths for sources with antithetics '
+                                 'should be even, not {}'.format(paths))
+            self._dz = base(paths=paths//2, vshape=vshape, dtype=dtype, rng=rng, **args)
+
+        def __call__(self, t, dt=None):
+            dz = self._dz(t, dt)
+            return np.concatenate((dz, transform(dz)), axis=-1)
+
+        @property
+        def paths(self):
+            return 2*self._dz.paths
+
+        @property
+        def vshape(self):
+            return self._dz.vshape
+
+        @property
+        def dtype(self):
+            return self._dz.dtype
+
+        @property
+        def rng(self):
+            return self._dz.rng
+
+        @property
+        def dn_value(self):
+            dn = self._dz.dn_value
+            return np.concatenate((dn, dn), axis=-1)
+    antithetic.__name__ = antithetic.__qualname__ = name
+    antithetic.__doc__ = doc
+    return antithetic
+
+
+odd_wiener_source = _antithetic(
+    wiener_source, lambda z: -z, 'odd_wiener_source',
+    """dw with antithetic paths: the trailing K of 2K paths are the leading K
+    with opposite increments.  Given as ``dw=odd_wiener_source`` to a preset
+    (with ``dj=even_cpoisson_source`` for jump models), the paths are drawn on
+    the device, two per thread from one draw.""")
+even_poisson_source = _antithetic(
+    poisson_source, lambda z: z, 'even_poisson_source',
+    """dn with antithetic paths: the trailing K of 2K paths repeat the leading K.""")
+even_cpoisson_source = _antithetic(
+    cpoisson_source, lambda z: z, 'even_cpoisson_source',
+    """dj with antithetic paths: the trailing K of 2K paths repeat the leading K.""")

@@ -30,7 +30,7 @@ from .grid import Grid
 from .infrastructure import (
     process, philox_rng, draw_key, check_rng, get_corr_matrix, law_of,
     wiener_source, cpoisson_source, poisson_source, norm_rv, double_exp_rv,
-    uniform_rv, _shape_setup)
+    uniform_rv, _shape_setup, odd_wiener_source, even_cpoisson_source)
 from . import infrastructure as _inf
 
 _COMMON = ('paths', 'vshape', 'dtype', 'rng', 'steps', 'i0', 'info',
@@ -161,8 +161,17 @@ class _gpu_process:
                     'values shape {} and correlation matrix shape {}'
                     .format(self.wshape, self.corr.shape))
         jumps = 'dj' in self._sources
-        user = A['dw'] is not None or (jumps and (A['dj'] is not None or
-                                                  A['dn'] is not None))
+        # antithetic paths drawn on the device: dw=odd_wiener_source and, for
+        # jump models, dj=even_cpoisson_source (sdepy's antithetic sources,
+        # sdepy/infrastructure.py:2047-2150); other source combinations
+        # keep sdepy's semantics through host realisation
+        self._anti = A['dw'] is odd_wiener_source and (
+            not jumps or (A['dj'] is even_cpoisson_source and A['dn'] is None))
+        if self._anti and self.paths % 2:
+            raise ValueError('the number of paths for sources with antithetics '
+                             'should be even, not {}'.format(self.paths))
+        user = not self._anti and (A['dw'] is not None or (jumps and (A['dj'] is not None or
+                                                                      A['dn'] is not None)))
         self._inject = user
         self._law_kind, self._law = None, None
         if jumps:
@@ -264,6 +273,7 @@ class _gpu_process:
         s.groups = self._G
         s.group_size = self._M
         s.out_mode = self._out
+        s.flags = _lib.FLAG_ANTITHETIC if self._anti else 0
         s.x0 = _lib.dptr(self._x0)
         s.params = _lib.dptr(self._prm)
         s.corr = _lib.dptr(self._corr_c)
