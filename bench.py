@@ -37,7 +37,7 @@ TIMELINE = np.linspace(0, 5, 11)
 BINS = 200
 
 
-def cfg1_params(seed=11):
+def ou8_params(seed=11):
     g = np.random.default_rng(seed)
     k = g.uniform(.5, 3, size=(8, 1))
     theta = g.uniform(-1, 1, size=(8, 1))
@@ -136,7 +136,7 @@ def run_gpu(args):
     P = sg.ornstein_uhlenbeck_process(vshape=8, paths=PATHS, steps=STEPS,
                                       dtype=np.float32,
                                       rng=sg.philox_rng(0, 1000*rank),
-                                      **cfg1_params())
+                                      **ou8_params())
     grid = Grid(TIMELINE, STEPS)
     leg = grid.legs[0]
     n_steps = leg.n_steps
@@ -208,7 +208,7 @@ def run_gpu(args):
     t0 = time.perf_counter()
     fp64_paths = 2**16
     P64 = sg.ornstein_uhlenbeck_process(vshape=8, paths=fp64_paths, steps=STEPS,
-                                        rng=sg.philox_rng(0), **cfg1_params())
+                                        rng=sg.philox_rng(0), **ou8_params())
     P64._precision = _lib.FP64
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -220,7 +220,7 @@ def run_gpu(args):
     fp64_rate = fp64_paths*n_steps/(fp64_ms*1e-3)
     P32 = sg.ornstein_uhlenbeck_process(vshape=8, paths=fp64_paths, steps=STEPS,
                                         dtype=np.float32, rng=sg.philox_rng(0),
-                                        **cfg1_params())
+                                        **ou8_params())
     mc32 = P32.montecarlo(TIMELINE, bins=BINS)
     est_err = {
         'mean_abs_rel_max': float(np.max(np.abs(mc32.mean() - mc64.mean())/np.maximum(np.abs(mc64.mean()), 1e-3))),
@@ -232,7 +232,7 @@ def run_gpu(args):
     e2e_steps = max(1, min(3, args.steps))
     Pe = sg.ornstein_uhlenbeck_process(vshape=8, paths=PATHS, steps=STEPS,
                                        dtype=np.float32, rng=sg.philox_rng(5),
-                                       **cfg1_params())
+                                       **ou8_params())
     lib.sde_set_stream(None)
     for i in range(2):   # steady state: host buffers of two live results pooled
         x, mc = Pe.montecarlo(TIMELINE, bins=BINS, paths_out=True)
@@ -319,7 +319,7 @@ HESTON_GRAD = {'x0': (0, 0), 'y0': (1, 0), 'k': (1, 1), 'theta': (1, 2), 'xi': (
 
 
 def heston_gradient_check(lib, batches=16, paths=2**18, steps=500):
-    """The configs[2] gradient with its standard error, from `batches`
+    """The Heston (2^18 paths per stream, 499 steps) gradient with its standard error, from `batches`
     independent Philox streams of `paths` paths each, against central finite
     differences (h = 1e-3 relative) of the fused FP32 forward on the same
     paths (common random numbers).  Per parameter: the adjoint mean and its
@@ -380,9 +380,10 @@ def heston_gradient_check(lib, batches=16, paths=2**18, steps=500):
 
 
 def extra_configs(lib):
-    """configs[2] Heston (FP32 forward with fused call payoffs vs the adjoint
-    gradient of the 6 parameters; FP64 forward), configs[3] Merton / Kou
-    (FP32), configs[0] lognormal (FP64, 1e5 paths, full paths written)."""
+    """Heston 2^22 paths x 499 steps (FP32 forward with fused call payoffs
+    vs the adjoint gradient of the 6 parameters; FP64 forward), Merton / Kou
+    2^22 paths x 364 steps (FP32), the 4096-instance batch, antithetic
+    pairs, lognormal 1e5 paths x 502 steps (FP64, full paths written)."""
     import ctypes as C
     import sdepy_gb300 as sg
     from sdepy_gb300 import _lib
@@ -429,7 +430,7 @@ def extra_configs(lib):
     H64 = sg.heston_process(paths=2**18, steps=500, **HESTON)
     fwd64_ms = _time_call(lambda: fused(H64, tl, STRIKES, 3), lib, reps=2)
     n = leg.n_steps
-    out['heston_configs2'] = {
+    out['heston_2p22x499'] = {
         'paths': 2**22, 'computed_steps': n,
         'fp32_forward_ms': fwd_ms, 'fp32_adjoint_ms': adj_ms,
         'grad_over_forward': adj_ms/fwd_ms,
@@ -449,8 +450,8 @@ def extra_configs(lib):
                            dict(x0=1., mu=.03, sigma=.15, lam=2., pa=.4, a=.1, b=.2))):
         J = cls(paths=2**22, steps=365, dtype=np.float32, **kw)
         ms = _time_call(lambda: fused(J, (0., 1.), [1.], 4), lib)
-        out[name + '_configs3'] = {'fp32_path_steps_per_s': 2**22*364/(ms*1e-3), 'kernel_ms': ms}
-    # ---- configs[4]: 4096 heterogeneous instances, one persistent launch
+        out[name + '_2p22x364'] = {'fp32_path_steps_per_s': 2**22*364/(ms*1e-3), 'kernel_ms': ms}
+    # ---- 4096 heterogeneous instances, one persistent launch
     from sdepy_gb300.batch import batch, synthetic_instances, run_single
     insts = synthetic_instances(4096, seed=1)
     t0 = time.perf_counter()
@@ -469,7 +470,7 @@ def extra_configs(lib):
         run_single(s_)
     loop_s = time.perf_counter() - t0
     ps = B.path_steps
-    out['batch_configs4'] = {
+    out['batch_4096'] = {
         'instances': len(insts), 'path_steps': ps, 'work_items': B.items,
         'slab': B.slab, 'autotune_ms': {str(k): v for k, v in (B.tuning or {}).items()},
         'autotune_s': tune_s, 'batch_device_ms': float(np.median(dev)),
@@ -480,7 +481,26 @@ def extra_configs(lib):
         'note': 'batch also computes 8 pathwise derivatives per instance; the loop '
                 'runs the forward summary only'}
     B.close()
-    # ---- lognormal configs[0]: FP64, 1e5 paths, 502 steps, all 253 rows written (host output)
+    # ---- antithetic paths (dw=odd_wiener_source): the Heston and Merton
+    # forwards above with the same paths count, pairs drawn once
+    anti = {}
+    for name, cls, kw, tl, steps, strikes in (
+            ('heston_2p22x499', sg.heston_process, HESTON, (0., 2.), 500, STRIKES),
+            ('merton_2p22x364', sg.merton_jumpdiff_process,
+             dict(x0=1., mu=.03, sigma=.15, lam=1., a=-.1, b=.15), (0., 1.), 365, [1.])):
+        row = {}
+        for mode in ('plain', 'antithetic'):
+            src = {}
+            if mode == 'antithetic':
+                src['dw'] = sg.odd_wiener_source
+                if 'dj' in cls._sources:
+                    src['dj'] = sg.even_cpoisson_source
+            Pa = cls(paths=2**22, steps=steps, dtype=np.float32, **src, **kw)
+            row[mode + '_ms'] = _time_call(lambda: fused(Pa, tl, strikes, 6), lib)
+        row['speedup'] = row['plain_ms']/row['antithetic_ms']
+        anti[name] = row
+    out['antithetic_fp32'] = anti
+    # ---- lognormal: FP64, 1e5 paths, 502 steps, all 253 rows written (host output)
     import time
     Ln = sg.lognorm_process(x0=1., mu=.05, sigma=.2, paths=100000, steps=252, rng=sg.philox_rng(0))
     for _ in range(2):   # steady state: host buffers of two live results pooled
@@ -491,7 +511,7 @@ def extra_configs(lib):
     wall = (time.perf_counter() - t0)/3
     last = (C.c_double*4)()
     lib.sde_timing(-1, last)
-    out['lognorm_configs0'] = {'fp64_kernel_ms': last[0],
+    out['lognorm_1e5x502'] = {'fp64_kernel_ms': last[0],
                                'fp64_path_steps_per_s': 100000*502/(last[0]*1e-3),
                                'e2e_path_steps_per_s': 100000*502/wall,
                                'e2e_ms': wall*1e3, 'output_bytes': int(x.nbytes)}
@@ -504,7 +524,7 @@ def extra_configs(lib):
 def _cpu_worker(a):
     sample_paths, seed = a
     from oracle import euler
-    p = cfg1_params()
+    p = ou8_params()
     corr = p.pop('corr')
     rng = np.random.default_rng(seed)
     t0 = time.perf_counter()
@@ -560,9 +580,9 @@ def run_reference(args):
 
 def run_case(args):
     """Small single-kernel cases for profiling captures: 'heston_adjoint'
-    (configs[2] model, 2^18 paths, 499 steps: forward summary then adjoint),
+    (the Heston model, 2^18 paths, 499 steps: forward summary then adjoint),
     'batch' (256 instances of the heterogeneous workload, paths <= 65536),
-    'lognorm_fp64' (configs[0]: FP64, 1e5 paths, 502 steps, 253 rows written
+    'lognorm_fp64' (FP64, 1e5 paths, 502 steps, 253 rows written
     to device memory)."""
     import ctypes as C
     import torch

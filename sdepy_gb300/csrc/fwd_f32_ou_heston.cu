@@ -80,20 +80,25 @@ FwdLauncher<float> find_fwd_f32_ou_heston(int model, int maxm, bool inject, bool
 }
 
 
-FwdLauncher<float> find_fwd_f32_ou_tdb(int maxm, int *bps) {
-    switch (maxm) {
-    case 1: if (bps) *bps = fwd_max_blocks_per_sm<float, SDE_MODEL_OU, 1, false, false, true>();
-            return &launch_fwd<float, SDE_MODEL_OU, 1, false, false, true>;
-    case 2: if (bps) *bps = fwd_max_blocks_per_sm<float, SDE_MODEL_OU, 2, false, false, true>();
-            return &launch_fwd<float, SDE_MODEL_OU, 2, false, false, true>;
-    case 4: if (bps) *bps = fwd_max_blocks_per_sm<float, SDE_MODEL_OU, 4, false, false, true>();
-            return &launch_fwd<float, SDE_MODEL_OU, 4, false, false, true>;
-    case 8: if (bps) *bps = fwd_max_blocks_per_sm<float, SDE_MODEL_OU, 8, false, false, true>();
-            return &launch_fwd<float, SDE_MODEL_OU, 8, false, false, true>;
-    case 16: if (bps) *bps = fwd_max_blocks_per_sm<float, SDE_MODEL_OU, 16, false, false, true>();
-             return &launch_fwd<float, SDE_MODEL_OU, 16, false, false, true>;
-    default: return nullptr;
+// time-dependent coefficients: OU run tables with the theta term, Heston
+// with per-step coefficient reloads (device noise, no jumps)
+FwdLauncher<float> find_fwd_f32_tdep(int model, int maxm, int *bps) {
+#define SDE_TDEP(MODEL, M)                                                               \
+    if (model == MODEL && maxm == M) {                                                   \
+        if (bps) *bps = fwd_max_blocks_per_sm<float, MODEL, M, false, false, true>();    \
+        return &launch_fwd<float, MODEL, M, false, false, true>;                         \
     }
+    SDE_TDEP(SDE_MODEL_OU, 1)
+    SDE_TDEP(SDE_MODEL_OU, 2)
+    SDE_TDEP(SDE_MODEL_OU, 4)
+    SDE_TDEP(SDE_MODEL_OU, 8)
+    SDE_TDEP(SDE_MODEL_OU, 16)
+    SDE_TDEP(SDE_MODEL_HESTON, 2)
+    SDE_TDEP(SDE_MODEL_HESTON, 4)
+    SDE_TDEP(SDE_MODEL_HESTON, 8)
+    SDE_TDEP(SDE_MODEL_HESTON, 16)
+#undef SDE_TDEP
+    return nullptr;
 }
 
 }  // namespace sdegpu

@@ -309,7 +309,7 @@ template <> struct Finder<double> {
         FwdLauncher<double> f = find_fwd_f64_linear(model, maxm, inj, jmp, bps);
         return f ? f : find_fwd_f64_ou_heston(model, maxm, inj, jmp, bps);
     }
-    static FwdLauncher<double> find_tdb(int, int *) { return nullptr; }
+    static FwdLauncher<double> find_tdep(int, int, int *) { return nullptr; }
     static FwdLauncher<double> find_anti(int model, int maxm, bool jmp, int *bps) {
         return find_fwd_f64_anti(model, maxm, jmp, bps);
     }
@@ -319,8 +319,11 @@ template <> struct Finder<float> {
         FwdLauncher<float> f = find_fwd_f32_linear(model, maxm, inj, jmp, bps);
         return f ? f : find_fwd_f32_ou_heston(model, maxm, inj, jmp, bps);
     }
-    // OU run-table kernels with a time-dependent theta
-    static FwdLauncher<float> find_tdb(int maxm, int *bps) { return find_fwd_f32_ou_tdb(maxm, bps); }
+    // time-dependent coefficients: OU run tables with a time-dependent
+    // theta, Heston with per-step reloads
+    static FwdLauncher<float> find_tdep(int model, int maxm, int *bps) {
+        return find_fwd_f32_tdep(model, maxm, bps);
+    }
     static FwdLauncher<float> find_anti(int model, int maxm, bool jmp, int *bps) {
         return find_fwd_f32_anti(model, maxm, jmp, bps);
     }
@@ -668,9 +671,12 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     // ---- launch ----------------------------------------------------------------------
     int bps = 0;
     if (anti && ou_b) return fail(SDE_ERR_UNSUPPORTED, "antithetic paths with a time-dependent OU theta");
-    FwdLauncher<R> L = anti   ? Finder<R>::find_anti(s->model, maxm_of(M), jumps, &bps)
-                       : ou_b ? Finder<R>::find_tdb(maxm_of(M), &bps)
-                              : Finder<R>::find(s->model, maxm_of(M), inject, jumps, &bps);
+    // the FP32 Heston kernels of device noise read per-step coefficients
+    // only in their time-dependent instantiation
+    const bool tdep_k = ou_b || (sizeof(R) == 4 && nprmt && !inject && !anti && s->model == SDE_MODEL_HESTON);
+    FwdLauncher<R> L = anti     ? Finder<R>::find_anti(s->model, maxm_of(M), jumps, &bps)
+                       : tdep_k ? Finder<R>::find_tdep(s->model, maxm_of(M), &bps)
+                                : Finder<R>::find(s->model, maxm_of(M), inject, jumps, &bps);
     if (!L) return fail(SDE_ERR_UNSUPPORTED, "no kernel for model %d group size %d", s->model, M);
     // antithetic kernels integrate two paths per thread
     const int nbx = path_blocks(D, anti ? paths / 2 : paths, s->groups, bps);

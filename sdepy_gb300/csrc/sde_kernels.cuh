@@ -586,14 +586,16 @@ struct FwdOccupancy {
     static constexpr int MIN_BLOCKS = (sizeof(R) == 4 && MAXM <= CAP_M && !INJECT && !JUMPS) ? 3 : 1;
 };
 
-// TDB: FP32 OU run-table kernel with a time-dependent theta (a separate
-// instantiation, so that the common form carries no trace of the extra term).
+// TDEP: time-dependent-coefficient instantiations of the FP32 device-noise
+// kernels whose common form carries no trace of the extra code (even code
+// that never runs changes how the hot loop compiles): OU run tables with
+// the theta term, Heston with per-step coefficient reloads.
 // ANTI: antithetic paths (device noise): paths q and q + K (K = paths / 2)
 // share their draws, the second with the opposite Wiener increments and
 // the same jumps (sdepy's odd_wiener_source / even_cpoisson_source,
 // sdepy/infrastructure.py:2047-2150); one thread integrates both, drawing
 // once.
-template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS, bool TDB = false, bool ANTI = false>
+template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS, bool TDEP = false, bool ANTI = false>
 __global__ void __launch_bounds__(BLOCK, (FwdOccupancy<R, MODEL, MAXM, INJECT, JUMPS, ANTI>::MIN_BLOCKS))
 sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     typedef Ar<R> A;
@@ -601,6 +603,10 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     constexpr bool TAB = sizeof(R) == 4 && MODEL != SDE_MODEL_HESTON && !INJECT;
     constexpr bool SHIFT = TAB && MODEL == SDE_MODEL_OU;  // state held as x - theta
     constexpr int NA = ANTI ? 2 : 1;   // paths per thread
+    constexpr bool TDB = TDEP && SHIFT;   // OU rows with the time-dependent-theta term
+    // per-step coefficient reloads compiled in (the non-table kernels but
+    // the common FP32 Heston ones)
+    constexpr bool RELOAD = !TAB && (sizeof(R) == 8 || INJECT || ANTI || TDEP);
     __shared__ R red[BLOCK / 32];
     __shared__ double part[MAXM][NPART];
     __shared__ R svs[NA][MAXM][BLOCK];   // this round's value of each output at the stats row
@@ -613,7 +619,8 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     const int n_steps = a.n_pts - 1;
     const bool do_stats = a.partials != nullptr;
     const PhiloxKey key = a.key;  // by value: uniform registers, not indexed parameter loads
-    if (TAB && (a.coef == nullptr || a.runs == nullptr || (SHIFT && a.tshift == nullptr)) &&
+    if (((TAB && (a.coef == nullptr || a.runs == nullptr || (SHIFT && a.tshift == nullptr))) ||
+         (!TAB && !RELOAD && a.prm_t != nullptr)) &&
         n_steps > 0) {  // uniform: the grid returns
         if (threadIdx.x == 0 && blockIdx.x == 0 && blockIdx.y == 0) atomicOr(a.err, ERRF_ARGS);
         return;
@@ -857,7 +864,9 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                 for (int k = 0; k < n_steps; ++k) {
                     const R dt = a.dt[k];
                     const R sq = a.sqdt[k];
-                    if (a.prm_t) {   // uniform: time-dependent coefficients of step k
+                    // time-dependent coefficients of step k (uniform test; not
+                    // compiled into the FP32 Heston kernels' common form)
+                    if (RELOAD && a.prm_t) {
                         const R *pk = a.prm_t + (int64_t)k * 3 * W;
 #pragma unroll
                         for (int m = 0; m < MAXM; ++m) {
@@ -996,15 +1005,15 @@ coef_table_kernel(const double *tt, int n_steps, const double *x0, const double 
 template <typename R>
 using FwdLauncher = void (*)(const FwdArgs<R> &, dim3, cudaStream_t);
 
-template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS, bool TDB = false, bool ANTI = false>
+template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS, bool TDEP = false, bool ANTI = false>
 void launch_fwd(const FwdArgs<R> &a, dim3 grid, cudaStream_t s) {
-    sde_fwd_kernel<R, MODEL, MAXM, INJECT, JUMPS, TDB, ANTI><<<grid, BLOCK, 0, s>>>(a);
+    sde_fwd_kernel<R, MODEL, MAXM, INJECT, JUMPS, TDEP, ANTI><<<grid, BLOCK, 0, s>>>(a);
 }
 
-template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS, bool TDB = false, bool ANTI = false>
+template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS, bool TDEP = false, bool ANTI = false>
 int fwd_max_blocks_per_sm() {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sde_fwd_kernel<R, MODEL, MAXM, INJECT, JUMPS, TDB, ANTI>,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sde_fwd_kernel<R, MODEL, MAXM, INJECT, JUMPS, TDEP, ANTI>,
                                                   BLOCK, 0);
     return n;
 }
@@ -1014,8 +1023,9 @@ FwdLauncher<double> find_fwd_f64_linear(int model, int maxm, bool inject, bool j
 FwdLauncher<double> find_fwd_f64_ou_heston(int model, int maxm, bool inject, bool jumps, int *bps);
 FwdLauncher<float> find_fwd_f32_linear(int model, int maxm, bool inject, bool jumps, int *bps);
 FwdLauncher<float> find_fwd_f32_ou_heston(int model, int maxm, bool inject, bool jumps, int *bps);
-// FP32 OU run-table kernels with a time-dependent theta
-FwdLauncher<float> find_fwd_f32_ou_tdb(int maxm, int *bps);
+// FP32 device-noise kernels with time-dependent coefficients: OU with a
+// time-dependent theta, Heston
+FwdLauncher<float> find_fwd_f32_tdep(int model, int maxm, int *bps);
 // antithetic kernels (device noise, groups of up to 8 states)
 FwdLauncher<float> find_fwd_f32_anti(int model, int maxm, bool jumps, int *bps);
 FwdLauncher<double> find_fwd_f64_anti(int model, int maxm, bool jumps, int *bps);

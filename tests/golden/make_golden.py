@@ -135,8 +135,8 @@ def path_cases(sdepy):
     run_case(sdepy, 'lognorm_small', 'lognorm_process',
              dict(x0=1., mu=.05, sigma=.2), lin(0, 1, 11), (), paths=64,
              steps=40, seed=1)
-    # configs[0] grid: 253-point timeline merged with 252 linspace points
-    run_case(sdepy, 'lognorm_cfg0grid', 'lognorm_process',
+    # the lognormal workload's grid: 253-point timeline merged with 252 linspace points
+    run_case(sdepy, 'lognorm_252grid', 'lognorm_process',
              dict(x0=1., mu=.05, sigma=.2), lin(0, 1, 253), (), paths=16,
              steps=252, seed=2)
     run_case(sdepy, 'wiener_vec', 'wiener_process',

@@ -2,20 +2,20 @@
 checked by properties that hold exactly for the discrete Euler scheme (no
 time-step bias enters):
 
-* configs[1] -- correlated OU, vshape 8, 2^20 paths x 1008 steps, FP32:
+* correlated OU, vshape 8, 2^20 paths x 1008 steps, FP32:
   the mean and covariance of the Euler recursion
   (m' = (1 - k dt) m + k theta dt, C' = D C D + S R S dt, D = diag(1 - k dt),
   S = diag(sigma), R = corr) against the fused summary and the written
   paths; fused summary equal to the summary of the written paths;
-* configs[2] -- Heston, 2^22 paths x 499 steps, FP32: log-Euler makes
+* Heston, 2^22 paths x 499 steps, FP32: log-Euler makes
   E[X_T] = x0 exp(mu T) exact (each step's log increment is conditionally
   normal with variance sigma^2 y+ dt and mean (mu - sigma^2 y+ / 2) dt);
   call prices decreasing and convex in the strike and above the intrinsic
   value of the mean;
-* configs[3] -- Merton / Kou, 2^22 paths x 364 steps, FP32: with exact
+* Merton / Kou, 2^22 paths x 364 steps, FP32: with exact
   Poisson counts per step, E[X_T] = x0 exp((mu + lam (E[e^Y] - 1)) T)
   (sdepy/analytical.py mjd_mean, kou_mean);
-* configs[4] -- 4096 heterogeneous instances in one batched launch:
+* 4096 heterogeneous instances in one batched launch:
   spot instances against the single-instance kernels on the same paths.
 """
 import os
@@ -43,10 +43,10 @@ def _euler_ou_moments(steps_tt, x0, k, theta, sigma, corr):
     return m, C
 
 
-def test_configs1_ou8_full_size(lib):
+def test_ou8_2p20x1008_full_size(lib):
     import bench
     from sdepy_gb300.grid import Grid
-    p = bench.cfg1_params()
+    p = bench.ou8_params()
     n = 2**20
     P = sg.ornstein_uhlenbeck_process(vshape=8, paths=n, steps=1000, dtype=np.float32,
                                       rng=sg.philox_rng(5), **p)
@@ -75,7 +75,7 @@ def test_configs1_ou8_full_size(lib):
         np.testing.assert_array_equal(c, rc)
 
 
-def test_configs2_heston_full_size(lib):
+def test_heston_2p22x499_full_size(lib):
     n = 2**22
     x0, mu, T = 100., .02, 2.
     strikes = [80., 90., 100., 110., 120.]
@@ -92,7 +92,7 @@ def test_configs2_heston_full_size(lib):
 
 
 @pytest.mark.parametrize('name', ['merton', 'kou'])
-def test_configs3_jumps_full_size(lib, name):
+def test_jumps_2p22x364_full_size(lib, name):
     from oracle import analytical as an
     n = 2**22
     if name == 'merton':
@@ -108,7 +108,7 @@ def test_configs3_jumps_full_size(lib, name):
     assert abs(float(mc.mean()) - ref) < 4*float(mc.stderr())
 
 
-def test_configs4_batch_full_size(lib):
+def test_batch_4096_full_size(lib):
     from sdepy_gb300.batch import batch, synthetic_instances, run_single
     insts = synthetic_instances(4096, seed=0)
     b = batch(insts, slab=1024, use_graph=True)

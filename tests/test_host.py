@@ -37,7 +37,7 @@ def test_grid_matches_reference_steps(path):
 
 
 def test_grid_configs():
-    # configs[0] grid: 253 timeline points with 252 linspace points
+    # the lognormal workload's grid: 253 timeline points with 252 linspace points
     g = Grid(np.linspace(0, 1, 253), 252)
     assert g.computed_steps == 502
     assert np.diff(g.steps_tt).min() > 1.5e-5
