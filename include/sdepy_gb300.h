@@ -341,6 +341,54 @@ SDE_API int32_t sde_sample_histogram(const void *sample, int32_t is_fp32, int32_
                              int64_t n_vars, int64_t paths, int32_t bins,
                              const double *edges, int64_t *counts);
 
+/* ---- process post-processing: summaries of written process values -------
+ * x holds process values [n_rows][n_vars][paths] (f64, or f32 when
+ * is_fp32), in device memory when on_device, else in host memory:
+ * page-locked host memory (sde_host_alloc, cudaHostAlloc) is read in place
+ * by the kernels, other host memory is copied to the device first. */
+
+/* Summaries across paths of each of n_series = n_rows * n_vars series:
+ * out[n_series][SDE_PMOM_STRIDE] = (sum, mean, M2, min, max, NaN count),
+ * M2 = the sum of squared deviations from the mean (var = M2 / (paths -
+ * ddof)), accumulated in FP64 whatever the data precision; min and max are
+ * NaN when a value is.  Replaces process.pmin / pmax / psum / pmean / pvar /
+ * pstd (sdepy/infrastructure.py:833-889). */
+#define SDE_PMOM_STRIDE 6
+SDE_API int32_t sde_process_moments(const void *x, int32_t is_fp32, int32_t on_device,
+                                    int64_t n_series, int64_t paths, double *out);
+
+/* The n_t time points at which sde_process_cdf / sde_process_chf read the
+ * process: point i reads row lo[i] when hi[i] < 0, else the FP64 value
+ * wh[i] * x[hi[i]] + wl[i] * x[lo[i]] rounded to the data precision --
+ * scipy.interpolate.interp1d(kind='linear') with constant extrapolation,
+ * as process.interp / process.__call__ evaluate it
+ * (sdepy/infrastructure.py:544-633); the caller computes the rows and
+ * weights. */
+typedef struct {
+    const int64_t *lo;
+    const int64_t *hi;
+    const double *wl;
+    const double *wh;
+    int64_t n_t;
+} SdeTimes;
+
+/* out[n_t][n_x][n_vars] = (number of paths whose value is <= xv[j]) /
+ * paths, the comparison taken in FP64; NaN values count for no xv, a NaN
+ * xv gives 0.  Replaces process.cdf (sdepy/infrastructure.py:1169-1212). */
+SDE_API int32_t sde_process_cdf(const void *x, int32_t is_fp32, int32_t on_device,
+                                int64_t n_rows, int64_t n_vars, int64_t paths,
+                                const SdeTimes *at, const double *xv, int64_t n_x,
+                                double *out);
+
+/* out[n_t][n_u][n_vars][2] = the mean over paths of (cos(u_j v), sin(u_j
+ * v)) with u_j v rounded to FP64: the real and imaginary parts of
+ * exp(1j*u*v).mean(axis=-1).  Replaces process.chf
+ * (sdepy/infrastructure.py:1125-1167). */
+SDE_API int32_t sde_process_chf(const void *x, int32_t is_fp32, int32_t on_device,
+                                int64_t n_rows, int64_t n_vars, int64_t paths,
+                                const SdeTimes *at, const double *u, int64_t n_u,
+                                double *out);
+
 #ifdef __cplusplus
 }
 #endif

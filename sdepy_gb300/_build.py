@@ -32,7 +32,7 @@ def _sources():
 
 
 def _deps():
-    return _sources() + glob.glob(os.path.join(CSRC, '*.cuh')) + \
+    return _sources() + glob.glob(os.path.join(CSRC, '*.cuh')) + glob.glob(os.path.join(CSRC, '*.h')) + \
         [os.path.join(HERE, '..', 'include', 'sdepy_gb300.h')]
 
 

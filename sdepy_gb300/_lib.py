@@ -86,6 +86,13 @@ class SdeBatchInstance(C.Structure):
                 ('stream', C.c_uint32), ('out_exp', C.c_int32)]
 
 
+class SdeTimes(C.Structure):
+    _fields_ = [('lo', _lp), ('hi', _lp), ('wl', _dp), ('wh', _dp),
+                ('n_t', C.c_int64)]
+
+
+PMOM_STRIDE = 6   # sde_process_moments: (sum, mean, M2, min, max, NaN count)
+
 # every symbol include/sdepy_gb300.h declares, with its ctypes signature
 SIGNATURES = {
     'sde_abi_version': (C.c_int32, []),
@@ -122,6 +129,14 @@ SIGNATURES = {
     'sde_sample_histogram': (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32,
                                          C.c_int64, C.c_int64, C.c_int32,
                                          _dp, _lp]),
+    'sde_process_moments': (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32,
+                                        C.c_int64, C.c_int64, _dp]),
+    'sde_process_cdf': (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32,
+                                    C.c_int64, C.c_int64, C.c_int64,
+                                    C.POINTER(SdeTimes), _dp, C.c_int64, _dp]),
+    'sde_process_chf': (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32,
+                                    C.c_int64, C.c_int64, C.c_int64,
+                                    C.POINTER(SdeTimes), _dp, C.c_int64, _dp]),
 }
 
 _lock = threading.Lock()

@@ -11,6 +11,7 @@
 #include "sde_kernels.cuh"
 #include "sde_stats.cuh"
 #include "sde_adjoint.cuh"
+#include "sde_runtime.h"
 
 using namespace sdegpu;
 
@@ -50,7 +51,8 @@ int set_last_error(int code, const char *msg) {
 // ---------------------------------------------------------------------------
 enum Slot {
     S_TABLES, S_NOISE_DW, S_NOISE_DJ, S_NOISE_DN, S_XX, S_NEG, S_JCNT, S_ROWJ,
-    S_PART, S_RES, S_EDGES, S_EDGES64, S_COUNTS, S_VALS, S_ERR, S_SAMPLE, S_COEF, N_SLOTS
+    S_PART, S_RES, S_EDGES, S_EDGES64, S_COUNTS, S_VALS, S_ERR, S_SAMPLE, S_COEF,
+    S_AUX0, S_AUX1, S_AUX2, S_AUX3, N_SLOTS   // entry points of other translation units
 };
 
 struct Device {
@@ -108,6 +110,37 @@ static int scratch(Device *D, Slot s, size_t bytes, void **p) {
     *p = D->ptr[s];
     return SDE_OK;
 }
+
+// ---------------------------------------------------------------------------
+// runtime services for entry points defined in other translation units: the
+// caller holds rt_mutex() for the whole call
+// ---------------------------------------------------------------------------
+namespace sdegpu {
+std::mutex &rt_mutex() { return g_mu; }
+
+int rt_begin(RtCall *c) {
+    Device *D;
+    int rc = current_device(&D);
+    if (rc) return rc;
+    c->st = dev_stream(D);
+    c->sms = D->sms;
+    c->timing = D->timing;
+    c->ev0 = D->ev[0];
+    c->ev1 = D->ev[1];
+    c->last_ms = D->last_ms;
+    return SDE_OK;
+}
+
+int rt_scratch(int aux, size_t bytes, void **p) {
+    if (aux < 0 || aux > S_AUX3 - S_AUX0) return fail(SDE_ERR_INVALID, "scratch slot %d", aux);
+    Device *D;
+    int rc = current_device(&D);
+    if (rc) return rc;
+    return scratch(D, (Slot)(S_AUX0 + aux), bytes, p);
+}
+
+int rt_fail(int code, const char *msg) { return fail(code, "%s", msg); }
+}  // namespace sdegpu
 
 // ---------------------------------------------------------------------------
 // exported utilities

@@ -79,14 +79,135 @@ class process(np.ndarray):
         """Timeline broadcast to the process shape."""
         return self.t.reshape((-1,) + (1,)*(self.ndim - 1))
 
-    def pmean(self, dtype=None):
-        return process(t=self.t, x=np.asarray(self).mean(axis=-1, keepdims=True, dtype=dtype))
+    @property
+    def x(self):
+        """The values as a plain numpy.ndarray."""
+        return self.view(np.ndarray)
 
-    def pvar(self, dtype=None, ddof=0):
-        return process(t=self.t, x=np.asarray(self).var(axis=-1, keepdims=True, dtype=dtype, ddof=ddof))
+    # indexing by mode (sdepy/infrastructure.py:652-703): p['v', i...]
+    # selects value components, p['t', k] time points, p['p', k] paths (an
+    # integer k keeps its axis); any other key indexes the plain array
+    def __getitem__(self, key):
+        x = self.view(np.ndarray)
+        if isinstance(key, str):
+            key = (key,)
+        if not (isinstance(key, tuple) and key and isinstance(key[0], str)):
+            return x[key]
+        mode, rest = key[0], key[1:]
+        if len(rest) == 1 and isinstance(rest[0], tuple):
+            rest = rest[0]
+        if mode == 'v':
+            return type(self)(self.t, x=x[(slice(None),) + tuple(rest) + (slice(None),)])
+        if mode not in ('t', 'p'):
+            raise IndexError('process indexing error - unsupported indexing mode ' + repr(mode))
+        if len(rest) > 1:
+            raise IndexError('process indexing error - one index expected in mode ' + repr(mode))
+        k = rest[0] if rest else slice(None)
+        if isinstance(k, (int, np.integer)):
+            k = slice(k, None) if k == -1 else slice(k, k + 1)
+        if mode == 't':
+            return type(self)(self.t[k], x=x[k])
+        return type(self)(self.t, x=x[..., k])
 
-    def pstd(self, dtype=None, ddof=0):
-        return process(t=self.t, x=np.asarray(self).std(axis=-1, keepdims=True, dtype=dtype, ddof=ddof))
+    # ---- summaries across paths, on the device (sde_process_moments;
+    # sdepy/infrastructure.py:833-889): one process path per summary
+    def _summary(self, field, dtype, out, ddof=0):
+        from . import _post
+        x = self.view(np.ndarray)
+        dtype = self.dtype if dtype is None else np.dtype(dtype)
+        if x.shape[-1] == 0:          # no paths: numpy's results for an empty axis
+            with np.errstate(all='ignore'):
+                r = {'psum': np.sum, 'pmean': np.mean, 'pmin': np.min, 'pmax': np.max}.get(field)
+                v = r(x, axis=-1, keepdims=True) if r else np.var(x, axis=-1, keepdims=True, ddof=ddof)
+        else:
+            m = _post.moments(x)[..., np.newaxis, :]
+            n = x.shape[-1]
+            with np.errstate(divide='ignore', invalid='ignore'):
+                if field == 'psum':
+                    v = m[..., 0]
+                elif field == 'pmean':
+                    v = m[..., 1]
+                elif field == 'pmin':
+                    v = m[..., 3]
+                elif field == 'pmax':
+                    v = m[..., 4]
+                else:
+                    v = m[..., 2]/max(n - ddof, 0)
+                    if field == 'pstd':
+                        v = np.sqrt(v)
+        if out is not None:
+            out[...] = v
+            return process(t=self.t, x=out)
+        return process(t=self.t, x=np.asarray(v).astype(dtype, copy=False))
+
+    def pmin(self, out=None):
+        """One-path process of the minimum across paths at each time point."""
+        return self._summary('pmin', None, out)
+
+    def pmax(self, out=None):
+        """One-path process of the maximum across paths at each time point."""
+        return self._summary('pmax', None, out)
+
+    def psum(self, dtype=None, out=None):
+        """One-path process of the sum across paths (FP64 accumulation)."""
+        return self._summary('psum', dtype, out)
+
+    def pmean(self, dtype=None, out=None):
+        """One-path process of the mean across paths (FP64 accumulation)."""
+        return self._summary('pmean', dtype, out)
+
+    def pvar(self, dtype=None, out=None, ddof=0):
+        """One-path process of the variance across paths."""
+        return self._summary('pvar', dtype, out, ddof)
+
+    def pstd(self, dtype=None, out=None, ddof=0):
+        """One-path process of the standard deviation across paths."""
+        return self._summary('pstd', dtype, out, ddof)
+
+    # ---- distribution estimators, on the device (sdepy/infrastructure.py:
+    # 1125-1212): p.cdf(t, x) / p.chf(t, u) at interpolated times t, or
+    # p.cdf(x) / p.chf(u) at the timeline points
+    def _read_at(self, t):
+        """(values, time points, output time shape) of the read at t."""
+        from . import _post
+        x = self.view(np.ndarray)
+        if t is None:
+            return x, None, self.t.shape
+        t = np.asarray(t)
+        if (self.interp_kind if self.t.size > 1 else 'linear') != 'linear':
+            v = np.asarray(self(t)).reshape((t.size,) + x.shape[1:])
+            return v, None, t.shape
+        return x, _post.time_points(self.t, t), t.shape
+
+    def cdf(self, t=None, x=None):
+        """Empirical cdf of the values at time(s) ``t`` (the timeline when
+        omitted) and values ``x``: shape t.shape + x.shape + vshape."""
+        from . import _post
+        if t is None and x is None:
+            raise TypeError('x argument missing')
+        if x is None:
+            t, x = None, t
+        v, tp, tshape = self._read_at(t)
+        x = np.asarray(x)
+        if v.shape[-1] == 0:
+            return np.full(tshape + x.shape + v.shape[1:-1], np.nan)
+        r = _post.cdf(v, tp, x)
+        return r.reshape(tshape + x.shape + v.shape[1:-1])
+
+    def chf(self, t=None, u=None):
+        """Empirical characteristic function (the path mean of
+        exp(1j*u*p(t))): shape t.shape + u.shape + vshape."""
+        from . import _post
+        if t is None and u is None:
+            raise TypeError('u argument missing')
+        if u is None:
+            t, u = None, t
+        v, tp, tshape = self._read_at(t)
+        u = np.asarray(u)
+        if v.shape[-1] == 0:
+            return np.full(tshape + u.shape + v.shape[1:-1], np.nan + 1j*np.nan)
+        r = _post.chf(v, tp, u)
+        return r.reshape(tshape + u.shape + v.shape[1:-1])
 
     # interpolation in time (sdepy/infrastructure.py:545-633): a process is a
     # valid time-dependent parameter of the presets
@@ -98,11 +219,10 @@ class process(np.ndarray):
         outside the timeline; a one-point process is constant)."""
         t, x = self.t, self.view(np.ndarray)
         kind = self.interp_kind if kind is None else kind
-        if t.size == 1:
+        if t.size == 1:          # constant in time
             def f(s):
-                s = np.asarray(s)
-                return np.ones(s.shape + x.shape[1:], dtype=x.dtype) * \
-                    x.reshape(tuple(1 for i in s.shape) + x.shape[1:])
+                shape = np.shape(s) + x.shape[1:]
+                return np.array(np.broadcast_to(x[0], shape), dtype=x.dtype)
             return f
         import scipy.interpolate
         g = scipy.interpolate.interp1d(t, x, axis=0, kind=kind, assume_sorted=True, copy=False,

@@ -105,6 +105,50 @@ def _moments_about(center, n, mean, M2, M3, M4):
     return (d, c2 + d*d, c3 + 3*d*c2 + d**3, c4 + 4*d*c3 + 6*d*d*c2 + d**4)
 
 
+def density_estimate(ncounts, bins, x, *, method='gaussian_kde', bandwidth=1., kind='linear',
+                     cumulative=False):
+    """pdf (or cdf, when ``cumulative``) at ``x`` of the distribution whose
+    density histogram is ``(ncounts, bins)``, as montecarlo.pdf / cdf define
+    it (sdepy/infrastructure.py:3149-3278):
+
+    * 'gaussian_kde': one normal kernel per bin, centred on the bin's
+      midpoint with standard deviation ``bandwidth`` times the bin's width,
+      weighted by the bin's probability (density times width); the cdf is
+      the same mixture's distribution function (through erf);
+    * 'interp': interpolation of the given ``kind`` -- the pdf through the
+      density values at the midpoints and 0 at the outer edges (0 outside),
+      the cdf through the cumulated probabilities at the edges (0 below, 1
+      above).
+    """
+    import scipy.interpolate
+    import scipy.special
+    x = np.asarray(x)
+    width = np.diff(bins)
+    mid = (bins[:-1] + bins[1:])/2
+    if method == 'gaussian_kde':
+        z = (x[..., np.newaxis] - mid)/(width*bandwidth)
+        mass = ncounts*width
+        if cumulative:
+            k = (1 + scipy.special.erf(z/np.sqrt(2)))/2
+            return (k*mass).sum(axis=-1)
+        k = np.exp(-z*z/2)/np.sqrt(2*np.pi)
+        return (k*(mass/(width*bandwidth))).sum(axis=-1)
+    if method == 'interp':
+        if cumulative:
+            knots = bins
+            vals = np.concatenate(([0.], np.cumsum(width*ncounts)))
+            fill = (0., 1.)
+        else:
+            knots = np.concatenate((bins[:1], mid, bins[-1:]))
+            vals = np.concatenate(([0.], ncounts, [0.]))
+            fill = 0.
+        f = scipy.interpolate.interp1d(knots, vals, kind=kind, assume_sorted=True,
+                                       bounds_error=False, fill_value=fill)
+        return f(x)
+    raise ValueError('pdf or cdf method should be '
+                     "'gaussian_kde' or 'interp', not {}".format(method))
+
+
 class montecarlo:
     """Summary statistics of Monte Carlo simulations, cumulated across runs
     (interface of sdepy.montecarlo)."""
@@ -320,3 +364,43 @@ class montecarlo:
 
     def outerr(self):
         return self.outpaths/self.paths
+
+    # -- distribution estimates from the histogram (sdepy/infrastructure.py:
+    # 3149-3278): small host arrays, no path data involved
+    def pdf(self, x, method='gaussian_kde', bandwidth=1., kind='linear'):
+        """Probability density of the cumulated samples at ``x``
+        ('gaussian_kde' or 'interp' of the density histogram)."""
+        ncounts, bins = self.density_histogram()
+        return density_estimate(ncounts, bins, x, method=method, bandwidth=bandwidth, kind=kind)
+
+    def cdf(self, x, method='gaussian_kde', bandwidth=1., kind='linear'):
+        """Cumulative distribution of the cumulated samples at ``x``."""
+        ncounts, bins = self.density_histogram()
+        return density_estimate(ncounts, bins, x, method=method, bandwidth=bandwidth, kind=kind,
+                                cumulative=True)
+
+    # -- shortcuts (sdepy/infrastructure.py:3280-3320)
+    @property
+    def m(self):
+        return self.mean()
+
+    @property
+    def s(self):
+        return self.std()
+
+    @property
+    def e(self):
+        return self.stderr()
+
+    @property
+    def stats(self):
+        return dict(mean=self.mean(), stderr=self.stderr(), std=self.std(), skew=self.skew(),
+                    kurtosis=self.kurtosis())
+
+    @property
+    def h(self):
+        return self.histogram()
+
+    @property
+    def dh(self):
+        return self.density_histogram()
