@@ -315,6 +315,80 @@ def _time_call(fn, lib, reps=3):
     return float(np.median(ts))
 
 
+def process_post_bench(lib, paths=2**20, reps=3, api=True, dtypes=(np.float32, np.float64)):
+    """Process post-processing on the OU benchmark's output shape (11 points
+    x 8 values x paths; FP64 with half the paths, the same bytes):
+
+    * device-resident values through the C-ABI: sde_process_moments (pmean /
+      pstd / ...), sde_process_cdf at 41 values, sde_process_chf at 4 values
+      of u -- kernel time (library events), GB/s of values read against the
+      HBM peak;
+    * the public API on an integrator result in page-locked host memory
+      (x.pmean(), x.pstd(), x.cdf(xq), x.chf(u)) -- wall time, the values read
+      in place over the host link;
+    * numpy on the host cores for the same array (mean, var, one threshold)."""
+    import ctypes as C
+    import time
+    import torch
+    import sdepy_gb300 as sg
+    from sdepy_gb300 import _lib
+    pk, pk_kind = peaks()
+    last = (C.c_double*4)()
+    lib.sde_timing(1, None)
+    xq = np.linspace(-1.5, 2.5, 41)
+    u = np.array([-2., -.5, .5, 2.])
+    out = {'shape': '11 x 8 x paths', 'peak_gbs': pk['hbm_gbs'], 'peak_kind': pk_kind}
+    for dtype in dtypes:
+        fp32 = int(dtype == np.float32)
+        n = paths if fp32 else paths//2
+        gen = torch.Generator(device='cuda')
+        gen.manual_seed(1)
+        xd = torch.randn((11, 8, n), dtype=torch.float32 if fp32 else torch.float64, device='cuda',
+                         generator=gen)
+        nbytes = xd.numel()*xd.element_size()
+        ptr = C.c_void_p(xd.data_ptr())
+        mom = np.empty((88, _lib.PMOM_STRIDE))
+        cd = np.empty((11, 41, 8))
+        ch = np.empty((11, 4, 8, 2))
+        calls = {
+            'moments': lambda: lib.sde_process_moments(ptr, fp32, 1, 88, n, _lib.dptr(mom)),
+            'cdf41': lambda: lib.sde_process_cdf(ptr, fp32, 1, 11, 8, n, None, _lib.dptr(xq), 41,
+                                                 _lib.dptr(cd)),
+            'chf4': lambda: lib.sde_process_chf(ptr, fp32, 1, 11, 8, n, None, _lib.dptr(u), 4, _lib.dptr(ch)),
+        }
+        res = {'paths': n, 'bytes': nbytes}
+        for name, f in calls.items():
+            ts = []
+            for _ in range(reps + 1):     # values (369 MB) exceed L2: no flush needed
+                _lib.check(f(), name)
+                lib.sde_timing(-1, last)
+                ts.append(last[0])
+            ms = float(np.median(ts[1:]))
+            gbs = nbytes/(ms*1e-3)/1e9
+            res[name] = {'kernel_ms': ms, 'gbs': gbs, 'hbm_frac': gbs/pk['hbm_gbs']}
+        del xd
+        if api:
+            P = sg.ornstein_uhlenbeck_process(vshape=8, paths=n, steps=1000, dtype=dtype,
+                                              rng=sg.philox_rng(2), **ou8_params())
+            x = P(np.linspace(0, 5, 11))
+            for name, f in (('pmean', lambda: x.pmean()), ('pstd', lambda: x.pstd()),
+                            ('cdf41', lambda: x.cdf(xq)), ('chf4', lambda: x.chf(u))):
+                f()
+                t0 = time.perf_counter()
+                for _ in range(reps):
+                    f()
+                res['api_' + name + '_ms'] = (time.perf_counter() - t0)/reps*1e3
+            xa = np.asarray(x)
+            for name, f in (('mean', lambda: xa.mean(axis=-1)), ('var', lambda: xa.var(axis=-1)),
+                            ('cdf1', lambda: (xa <= .5).sum(axis=-1)/n)):
+                t0 = time.perf_counter()
+                f()
+                res['numpy_' + name + '_ms'] = (time.perf_counter() - t0)*1e3
+            del x, xa
+        out['f32' if fp32 else 'f64'] = res
+    return out
+
+
 HESTON_GRAD = {'x0': (0, 0), 'y0': (1, 0), 'k': (1, 1), 'theta': (1, 2), 'xi': (1, 3), 'rho': (0, 7)}
 
 
@@ -500,6 +574,7 @@ def extra_configs(lib):
         row['speedup'] = row['plain_ms']/row['antithetic_ms']
         anti[name] = row
     out['antithetic_fp32'] = anti
+    out['process_post'] = process_post_bench(lib)
     # ---- lognormal: FP64, 1e5 paths, 502 steps, all 253 rows written (host output)
     import time
     Ln = sg.lognorm_process(x0=1., mu=.05, sigma=.2, paths=100000, steps=252, rng=sg.philox_rng(0))
@@ -583,7 +658,8 @@ def run_case(args):
     (the Heston model, 2^18 paths, 499 steps: forward summary then adjoint),
     'batch' (256 instances of the heterogeneous workload, paths <= 65536),
     'lognorm_fp64' (FP64, 1e5 paths, 502 steps, 253 rows written
-    to device memory)."""
+    to device memory), 'process_post' (FP32 device-resident 11 x 8 x 2^20
+    values: moments, cdf at 41 values, chf at 4 values of u)."""
     import ctypes as C
     import torch
     import sdepy_gb300 as sg
@@ -640,6 +716,9 @@ def run_case(args):
             ms.append(last[0])
         print(json.dumps({'case': args.case, 'kernel_ms': float(np.median(ms[args.warmup:])),
                           'path_steps': 100000*leg.n_steps}))
+    elif args.case == 'process_post':
+        print(json.dumps({'case': args.case, 'result': process_post_bench(
+            lib, reps=args.steps, api=False, dtypes=(np.float32,))}))
 
 
 def main():
@@ -652,7 +731,7 @@ def main():
                     help='paths per step (profiling captures use fewer)')
     ap.add_argument('--quick', action='store_true',
                     help='timed steps only: no FP64 / e2e / CPU / probe extras')
-    ap.add_argument('--case', default=None, choices=['heston_adjoint', 'batch', 'lognorm_fp64'],
+    ap.add_argument('--case', default=None, choices=['heston_adjoint', 'batch', 'lognorm_fp64', 'process_post'],
                     help='run one small single-kernel case (profiling)')
     args = ap.parse_args()
     if args.case:

@@ -28,6 +28,7 @@
 #include <cstring>
 #include <mutex>
 #include <numeric>
+#include <type_traits>
 #include <vector>
 
 #include "sdepy_gb300.h"
@@ -42,6 +43,7 @@ constexpr int SHIFT_N = 64;       // leading values averaged into a series' shif
 constexpr int CHF_CHUNK = 4096;   // values staged per chf block iteration
 constexpr int CHF_UT = 8;         // u values per chf register tile
 constexpr int CDF_SMEM_MAX = 8192;  // thresholds held in shared memory
+constexpr int CDF_ILP = 4;          // values searched side by side per thread
 
 #define PCU(call)                                                                        \
     do {                                                                                 \
@@ -72,22 +74,46 @@ struct TimePoint {
     double wl, wh;
 };
 
-// value p of series (time point tp, component var); interpolated values are
-// formed in FP64 (wh * x_hi + wl * x_lo, no contraction) and rounded to R
-template <typename R>
-__device__ __forceinline__ R read_value(const R *__restrict__ x, const TimePoint &tp, int64_t n_vars,
-                                        int64_t var, int64_t paths, int64_t p) {
-    const R xl = __ldg(x + (tp.lo * n_vars + var) * paths + p);
-    if (tp.hi < 0) return xl;
-    const R xh = __ldg(x + (tp.hi * n_vars + var) * paths + p);
+// value p of series (time point tp, component var): row lo itself, or
+// (INTERP) the FP64 value wh * x_hi + wl * x_lo (no contraction) rounded to
+// R.  Callers branch on tp.hi once per series, so that the value loop of a
+// timeline read carries no interpolation arithmetic.
+template <bool INTERP, typename R>
+__device__ __forceinline__ R read_value(const R *__restrict__ xl_row, const R *__restrict__ xh_row,
+                                        const TimePoint &tp, int64_t p) {
+    const R xl = __ldg(xl_row + p);
+    if (!INTERP) return xl;
+    const R xh = __ldg(xh_row + p);
     return (R)__dadd_rn(__dmul_rn(tp.wh, (double)xh), __dmul_rn(tp.wl, (double)xl));
+}
+
+// order-preserving integer key of a double (the IEEE bit pattern with the
+// magnitude bits of negative numbers flipped; -0 maps to +0's key): key
+// comparisons agree with FP64 comparisons of non-NaN values and run on the
+// integer pipes (GB300 issues FP64 at 1/64 of the FP32 rate)
+__host__ __device__ __forceinline__ long long order_key(long long b) {
+    if ((b & 0x7fffffffffffffffLL) == 0) return 0;
+    return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ long long order_key(double v) { return order_key(__double_as_longlong(v)); }
+__device__ __forceinline__ double key_value(long long k) {
+    return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffLL));
+}
+
+// Knuth's TwoSum in FP32: s + e == a + b exactly (round-to-nearest, no
+// overflow)
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
 // ---------------------------------------------------------------------------
 // moments
 // ---------------------------------------------------------------------------
-// shift[s] = mean of the finite values among the first SHIFT_N of series s
-// (0 when none is finite); one warp per series, fixed reduction order
+// shift[s] = mean of the finite values among the first SHIFT_N of series s,
+// rounded to R (0 when none is finite); one warp per series, fixed
+// reduction order
 template <typename R>
 __global__ void __launch_bounds__(PB) pmom_shift_kernel(const R *__restrict__ x, int64_t n_series,
                                                         int64_t paths, double *__restrict__ shift) {
@@ -107,49 +133,115 @@ __global__ void __launch_bounds__(PB) pmom_shift_kernel(const R *__restrict__ x,
             sum += __shfl_xor_sync(0xffffffffu, sum, o);
             cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
         }
-        if (lane == 0) shift[s] = cnt ? sum / cnt : 0.0;
+        if (lane == 0) shift[s] = cnt ? (double)(R)(sum / cnt) : 0.0;
     }
 }
 
+// Per-thread accumulation of one series' values about the shift sh: sums of
+// d = w - sh and d^2 where w is the value, or sh itself for a non-finite
+// value (infinities and NaN are accounted for through min / max and the NaN
+// count); min, max (NaN ignored) and the NaN count.
+//
+// FP32 values: d is formed exactly as dh + dl (TwoSum), d^2 as p + q (the
+// FMA product error, dl^2 dropped: below 2^-48 d^2); the sums are carried
+// as FP32 pairs (compensated with TwoSum) over runs of 32 values and then
+// added to FP64 totals -- FP64-class accuracy from FP32 instructions
+// (differences of squares above FLT_MAX, |v - sh| > 1.8e19, overflow).
+// FP64 values: three FP64 operations per value; min / max on order keys.
+template <typename R> struct MomAcc;
+
+template <> struct MomAcc<float> {
+    double S1 = 0.0, S2 = 0.0;
+    float a1 = 0.f, c1 = 0.f, a2 = 0.f, c2 = 0.f;
+    float mn = INFINITY, mx = -INFINITY;
+    unsigned int nan = 0;
+    float sh;
+    __device__ explicit MomAcc(double shift) : sh((float)shift) {}
+    __device__ __forceinline__ void add(float v) {
+        nan += nan_bits(v);
+        mn = fminf(mn, v);
+        mx = fmaxf(mx, v);
+        const float w = finite_bits(v) ? v : sh;
+        float dh, dl, t, e;
+        two_sum(w, -sh, dh, dl);
+        two_sum(a1, dh, t, e);
+        a1 = t;
+        c1 = __fadd_rn(c1, __fadd_rn(e, dl));
+        const float pr = __fmul_rn(dh, dh);
+        const float q = __fmaf_rn(__fmul_rn(2.f, dh), dl, __fmaf_rn(dh, dh, -pr));
+        two_sum(a2, pr, t, e);
+        a2 = t;
+        c2 = __fadd_rn(c2, __fadd_rn(e, q));
+    }
+    __device__ __forceinline__ void flush() {
+        S1 += (double)a1 + (double)c1;
+        S2 += (double)a2 + (double)c2;
+        a1 = c1 = a2 = c2 = 0.f;
+    }
+    __device__ __forceinline__ double vmin() const { return (double)mn; }
+    __device__ __forceinline__ double vmax() const { return (double)mx; }
+};
+
+template <> struct MomAcc<double> {
+    double S1 = 0.0, S2 = 0.0;
+    long long kmn = 0x7fffffffffffffffLL, kmx = (long long)0x8000000000000000ULL;
+    unsigned int nan = 0;
+    double sh;
+    __device__ explicit MomAcc(double shift) : sh(shift) {}
+    __device__ __forceinline__ void add(double v) {
+        const long long b = __double_as_longlong(v);
+        const bool isnan = (b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+        nan += isnan;
+        const long long k = order_key(b);
+        if (!isnan) {
+            kmn = k < kmn ? k : kmn;
+            kmx = k > kmx ? k : kmx;
+        }
+        const double w = finite_bits(v) ? v : sh;
+        const double d = __dsub_rn(w, sh);
+        S1 = __dadd_rn(S1, d);
+        S2 = __fma_rn(d, d, S2);
+    }
+    __device__ __forceinline__ void flush() {}
+    __device__ __forceinline__ double vmin() const {
+        return kmn == 0x7fffffffffffffffLL ? (double)INFINITY : key_value(kmn);
+    }
+    __device__ __forceinline__ double vmax() const {
+        return kmx == (long long)0x8000000000000000ULL ? -(double)INFINITY : key_value(kmx);
+    }
+};
+
 // per-block partials [n_series][nch][6] = (n, S1, S2, min, max, NaN count)
-// of the chunk [bx * chunk, min(paths, (bx + 1) * chunk)) of each series,
-// S1 = sum(v - shift), S2 = sum((v - shift)^2) in FP64
+// of the chunk [bx * chunk, min(paths, (bx + 1) * chunk)) of each series
 template <typename R>
 __global__ void __launch_bounds__(PB) pmom_kernel(const R *__restrict__ x, int64_t n_series, int64_t paths,
                                                   int64_t chunk, int nch, const double *__restrict__ shift,
                                                   double *__restrict__ part) {
-    __shared__ double red[5][PB / 32];
+    __shared__ double red[4][PB / 32];
     __shared__ unsigned int redn[PB / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t c0 = (int64_t)blockIdx.x * chunk;
     const int64_t c1 = c0 + chunk < paths ? c0 + chunk : paths;
     for (int64_t s = blockIdx.y; s < n_series; s += gridDim.y) {
         const R *__restrict__ p = x + s * paths;
-        const double sh = shift[s];
-        double s1 = 0.0, s2 = 0.0;
-        R mn = (R)INFINITY, mx = (R)-INFINITY;
-        unsigned int nan = 0;
-        for (int64_t i = c0 + threadIdx.x; i < c1; i += 4 * PB) {
+        MomAcc<R> acc(shift[s]);
+        int run = 0;
+        int64_t i = c0 + threadIdx.x;
+        for (; i + 3 * PB < c1; i += 4 * PB) {   // whole groups of 4 values per thread
             R v[4];
-            bool ok[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int64_t j = i + (int64_t)u * PB;
-                ok[u] = j < c1;
-                v[u] = ok[u] ? __ldg(p + j) : (R)0;
-            }
+            for (int u = 0; u < 4; ++u) v[u] = __ldg(p + i + u * PB);
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                if (!ok[u]) continue;
-                const double d = (double)v[u] - sh;
-                s1 += d;
-                s2 = fma(d, d, s2);
-                mn = fmin(mn, v[u]);   // NaN-ignoring; NaN is counted apart
-                mx = fmax(mx, v[u]);
-                nan += nan_bits(v[u]);
+            for (int u = 0; u < 4; ++u) acc.add(v[u]);
+            if (++run == 8) {   // 32 values
+                acc.flush();
+                run = 0;
             }
         }
-        double m = (double)mn, M = (double)mx;
+        for (; i < c1; i += PB) acc.add(__ldg(p + i));   // at most 3 more
+        acc.flush();
+        double s1 = acc.S1, s2 = acc.S2, m = acc.vmin(), M = acc.vmax();
+        unsigned int nan = acc.nan;
         for (int o = 16; o > 0; o >>= 1) {
             s1 += __shfl_xor_sync(0xffffffffu, s1, o);
             s2 += __shfl_xor_sync(0xffffffffu, s2, o);
@@ -188,7 +280,9 @@ __global__ void __launch_bounds__(PB) pmom_kernel(const R *__restrict__ x, int64
 }
 
 // out[s][6] = (sum, mean, M2, min, max, NaN count) from the partials, in
-// fixed order
+// fixed order.  Non-finite values: any NaN makes every statistic NaN;
+// otherwise +inf (-inf) makes the sum and mean +inf (-inf), both NaN, and
+// M2 NaN -- numpy's results for such samples.
 __global__ void pmom_final_kernel(const double *__restrict__ part, int64_t n_series, int nch,
                                   const double *__restrict__ shift, double *__restrict__ out) {
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -205,59 +299,112 @@ __global__ void pmom_final_kernel(const double *__restrict__ part, int64_t n_ser
     }
     const double sh = shift[s];
     double *o = out + s * SDE_PMOM_STRIDE;
-    o[0] = sh * n + s1;
-    o[1] = sh + s1 / n;
-    const double m2 = s2 - s1 * (s1 / n);
-    o[2] = m2 < 0.0 ? 0.0 : m2;   // NaN stays NaN
-    o[3] = nan > 0.0 ? (double)NAN : lo;
-    o[4] = nan > 0.0 ? (double)NAN : hi;
+    const double qnan = (double)NAN;
+    const bool pinf = hi == (double)INFINITY, ninf = lo == -(double)INFINITY;
+    if (nan > 0.0) {
+        o[0] = o[1] = o[2] = o[3] = o[4] = qnan;
+    } else if (pinf || ninf) {
+        o[0] = o[1] = pinf && ninf ? qnan : pinf ? (double)INFINITY : -(double)INFINITY;
+        o[2] = qnan;
+        o[3] = lo;
+        o[4] = hi;
+    } else {
+        o[0] = sh * n + s1;
+        o[1] = sh + s1 / n;
+        const double m2 = s2 - s1 * (s1 / n);
+        o[2] = m2 < 0.0 ? 0.0 : m2;
+        o[3] = lo;
+        o[4] = hi;
+    }
     o[5] = nan;
 }
 
 // ---------------------------------------------------------------------------
 // cdf
 // ---------------------------------------------------------------------------
+// thresholds as the kernels compare them: FP32 data against floats (the
+// largest float not above each FP64 threshold: v <= x exactly when v <= that
+// float), FP64 data against order keys
+template <typename R> struct Thr;
+template <> struct Thr<float> {
+    using T = float;
+    __device__ static __forceinline__ float key(float v) { return v; }
+};
+template <> struct Thr<double> {
+    using T = long long;
+    __device__ static __forceinline__ long long key(double v) { return order_key(v); }
+};
+
 // counts[s][k] += number of values of series s whose first threshold not
-// below them is thr[k] (thr sorted ascending, NaN-free; values above every
-// threshold and NaN values are not counted)
+// below them is thr[k].  thr holds the n_thr sorted NaN-free thresholds
+// followed by sentinels (above every value) up to n_pad = 2^m - 1 entries,
+// so that the position is found by m halving steps without branches.
+// Values above every threshold and NaN values are not counted.  Each thread
+// runs the searches of CDF_ILP values side by side (independent chains of
+// shared-memory loads).  SMEM: thresholds and counters in shared memory,
+// shared atomics; else (n_thr above CDF_SMEM_MAX) thresholds in global
+// memory and global atomics.
 template <typename R, bool SMEM>
 __global__ void __launch_bounds__(PB) cdf_kernel(const R *__restrict__ x, int64_t n_vars, int64_t paths,
                                                  const TimePoint *__restrict__ tps, int64_t n_series,
-                                                 const R *__restrict__ thr_g, int n_thr, int64_t chunk,
+                                                 const typename Thr<R>::T *__restrict__ thr_g, int n_thr,
+                                                 int n_pad, int64_t chunk,
                                                  unsigned long long *__restrict__ counts) {
+    using T = typename Thr<R>::T;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned int *hist = reinterpret_cast<unsigned int *>(smem_raw);
-    R *thr_s = reinterpret_cast<R *>(smem_raw + (((size_t)n_thr * 4 + 15) & ~(size_t)15));
-    const R *thr = SMEM ? thr_s : thr_g;
+    T *thr_s = reinterpret_cast<T *>(smem_raw + (((size_t)n_thr * 4 + 15) & ~(size_t)15));
+    const T *thr = SMEM ? thr_s : thr_g;
     if (SMEM)
-        for (int k = threadIdx.x; k < n_thr; k += PB) thr_s[k] = thr_g[k];
+        for (int k = threadIdx.x; k < n_pad; k += PB) thr_s[k] = thr_g[k];
+    const int top = (n_pad + 1) >> 1;
     const int64_t c0 = (int64_t)blockIdx.x * chunk;
     const int64_t c1 = c0 + chunk < paths ? c0 + chunk : paths;
     for (int64_t s = blockIdx.y; s < n_series; s += gridDim.y) {
         const TimePoint tp = tps[s / n_vars];
         const int64_t var = s % n_vars;
+        const R *xl = x + (tp.lo * n_vars + var) * paths;
+        const R *xh = tp.hi < 0 ? xl : x + (tp.hi * n_vars + var) * paths;
         if (SMEM) {
             for (int k = threadIdx.x; k < n_thr; k += PB) hist[k] = 0;
             __syncthreads();
         }
-        for (int64_t i = c0 + threadIdx.x; i < c1; i += PB) {
-            const R v = read_value(x, tp, n_vars, var, paths, i);
-            if (nan_bits(v)) continue;
-            int b = 0, len = n_thr;   // lower bound: first thr[b] >= v
-            while (len > 0) {
-                const int half = len >> 1;
-                if (thr[b + half] < v) {
-                    b += half + 1;
-                    len -= half + 1;
-                } else {
-                    len = half;
-                }
-            }
-            if (b < n_thr) {
+        auto tally = [&](int b, bool ok) {
+            if (ok && b < n_thr) {
                 if (SMEM) atomicAdd(hist + b, 1u);
                 else atomicAdd(counts + s * n_thr + b, 1ull);
             }
-        }
+        };
+        auto count = [&](auto interp) {
+            constexpr bool IP = decltype(interp)::value;
+            int64_t i = c0 + threadIdx.x;
+            for (; i + (CDF_ILP - 1) * PB < c1; i += CDF_ILP * PB) {
+                T kv[CDF_ILP];
+                bool ok[CDF_ILP];
+                int b[CDF_ILP];
+#pragma unroll
+                for (int u = 0; u < CDF_ILP; ++u) {
+                    const R v = read_value<IP>(xl, xh, tp, i + u * PB);
+                    ok[u] = !nan_bits(v);
+                    kv[u] = Thr<R>::key(v);
+                    b[u] = 0;   // the number of thresholds below v
+                }
+                for (int step = top; step > 0; step >>= 1)
+#pragma unroll
+                    for (int u = 0; u < CDF_ILP; ++u) b[u] += thr[b[u] + step - 1] < kv[u] ? step : 0;
+#pragma unroll
+                for (int u = 0; u < CDF_ILP; ++u) tally(b[u], ok[u]);
+            }
+            for (; i < c1; i += PB) {
+                const R v = read_value<IP>(xl, xh, tp, i);
+                const T kv = Thr<R>::key(v);
+                int b = 0;
+                for (int step = top; step > 0; step >>= 1) b += thr[b + step - 1] < kv ? step : 0;
+                tally(b, !nan_bits(v));
+            }
+        };
+        if (tp.hi < 0) count(std::false_type{});
+        else count(std::true_type{});
         if (SMEM) {
             __syncthreads();
             for (int k = threadIdx.x; k < n_thr; k += PB)
@@ -299,11 +446,16 @@ __global__ void __launch_bounds__(PB) chf_kernel(const R *__restrict__ x, int64_
     for (int64_t s = blockIdx.y; s < n_series; s += gridDim.y) {
         const TimePoint tp = tps[s / n_vars];
         const int64_t var = s % n_vars;
+        const R *xl = x + (tp.lo * n_vars + var) * paths;
+        const R *xh = tp.hi < 0 ? xl : x + (tp.hi * n_vars + var) * paths;
         for (int k = threadIdx.x; k < 2 * n_u; k += PB) acc[k] = 0.0;
         for (int64_t c0 = (int64_t)blockIdx.x * CHF_CHUNK; c0 < paths; c0 += (int64_t)nch * CHF_CHUNK) {
             const int cn = (int)(paths - c0 < CHF_CHUNK ? paths - c0 : CHF_CHUNK);
             __syncthreads();
-            for (int k = threadIdx.x; k < cn; k += PB) vals[k] = (double)read_value(x, tp, n_vars, var, paths, c0 + k);
+            if (tp.hi < 0)
+                for (int k = threadIdx.x; k < cn; k += PB) vals[k] = (double)read_value<false>(xl, xh, tp, c0 + k);
+            else
+                for (int k = threadIdx.x; k < cn; k += PB) vals[k] = (double)read_value<true>(xl, xh, tp, c0 + k);
             __syncthreads();
             for (int j0 = 0; j0 < n_u; j0 += CHF_UT) {
                 double c[CHF_UT], sn[CHF_UT], uj[CHF_UT];
@@ -465,15 +617,24 @@ int moments_impl(const void *x, int on_device, int64_t n_series, int64_t paths, 
     return SDE_OK;
 }
 
-// thresholds as the kernels compare them: for f32 data, the largest float
-// not above each FP64 threshold (v <= x exactly when v <= that float)
-template <typename R> R thr_cast(double v);
-template <> double thr_cast<double>(double v) { return v; }
+// host form of the thresholds (Thr<R>::T): for f32 data the largest float
+// not above each FP64 threshold, for f64 data its order key
+template <typename R> typename Thr<R>::T thr_cast(double v);
+template <> long long thr_cast<double>(double v) {
+    long long b;
+    memcpy(&b, &v, sizeof b);
+    return order_key(b);
+}
 template <> float thr_cast<float>(double v) {
     float f = (float)v;
     if ((double)f > v) f = nextafterf(f, -INFINITY);
     return f;
 }
+// padding above every value's key: +inf (a value of +inf is not below it),
+// the largest key (above +inf's)
+template <typename R> typename Thr<R>::T thr_sentinel();
+template <> float thr_sentinel<float>() { return INFINITY; }
+template <> long long thr_sentinel<double>() { return 0x7fffffffffffffffLL; }
 
 template <typename R>
 int cdf_impl(const void *x, int on_device, int64_t n_rows, int64_t n_vars, int64_t paths, const SdeTimes *at,
@@ -492,7 +653,9 @@ int cdf_impl(const void *x, int on_device, int64_t n_rows, int64_t n_vars, int64
         if (!std::isnan(xv[j])) perm.push_back(j);
     std::stable_sort(perm.begin(), perm.end(), [&](int64_t a, int64_t b) { return xv[a] < xv[b]; });
     const int n_thr = (int)perm.size();
-    std::vector<R> thr(n_thr);
+    int n_pad = 1;   // 2^m - 1 >= n_thr
+    while (n_pad < n_thr) n_pad = 2 * n_pad + 1;
+    std::vector<typename Thr<R>::T> thr(n_pad, thr_sentinel<R>());
     for (int k = 0; k < n_thr; ++k) thr[k] = thr_cast<R>(xv[perm[k]]);
 
     std::lock_guard<std::mutex> lk(rt_mutex());
@@ -507,11 +670,11 @@ int cdf_impl(const void *x, int on_device, int64_t n_rows, int64_t n_vars, int64
         if ((rc = input_ptr(c, x, sizeof(R) * n_rows * n_vars * paths, on_device, &dx))) return rc;
         // tables: time points, thresholds, permutation
         const size_t o_thr = (sizeof(TimePoint) * n_t + 15) & ~(size_t)15;
-        const size_t o_perm = o_thr + ((sizeof(R) * n_thr + 15) & ~(size_t)15);
+        const size_t o_perm = o_thr + ((sizeof(typename Thr<R>::T) * n_pad + 15) & ~(size_t)15);
         const size_t tab_bytes = o_perm + sizeof(int64_t) * n_thr;
         std::vector<char> tab(tab_bytes);
         memcpy(tab.data(), tp.data(), sizeof(TimePoint) * n_t);
-        memcpy(tab.data() + o_thr, thr.data(), sizeof(R) * n_thr);
+        memcpy(tab.data() + o_thr, thr.data(), sizeof(typename Thr<R>::T) * n_pad);
         memcpy(tab.data() + o_perm, perm.data(), sizeof(int64_t) * n_thr);
         void *dtab, *cnt;
         if ((rc = rt_scratch(1, tab_bytes, &dtab))) return rc;
@@ -528,18 +691,18 @@ int cdf_impl(const void *x, int on_device, int64_t n_rows, int64_t n_vars, int64
         nch = (paths + chunk - 1) / chunk;
         const dim3 grid((unsigned)nch, grid_y(n_series));
         const TimePoint *dtp = (const TimePoint *)dtab;
-        const R *dthr = (const R *)((char *)dtab + o_thr);
+        const typename Thr<R>::T *dthr = (const typename Thr<R>::T *)((char *)dtab + o_thr);
         if (c.timing) PCU(cudaEventRecord(c.ev0, c.st));
         if (n_thr <= CDF_SMEM_MAX) {
-            const size_t smem = (((size_t)n_thr * 4 + 15) & ~(size_t)15) + sizeof(R) * n_thr;
+            const size_t smem = (((size_t)n_thr * 4 + 15) & ~(size_t)15) + sizeof(typename Thr<R>::T) * n_pad;
             if (smem > 48 * 1024)
                 PCU(cudaFuncSetAttribute(cdf_kernel<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem));
             cdf_kernel<R, true><<<grid, PB, smem, c.st>>>((const R *)dx, n_vars, paths, dtp, n_series, dthr, n_thr,
-                                                          chunk, (unsigned long long *)cnt);
+                                                          n_pad, chunk, (unsigned long long *)cnt);
         } else {
             cdf_kernel<R, false><<<grid, PB, 0, c.st>>>((const R *)dx, n_vars, paths, dtp, n_series, dthr, n_thr,
-                                                        chunk, (unsigned long long *)cnt);
+                                                        n_pad, chunk, (unsigned long long *)cnt);
         }
         cdf_final_kernel<<<(unsigned)((n_series + 255) / 256), 256, 0, c.st>>>(
             (const unsigned long long *)cnt, n_series, n_thr, (const int64_t *)((char *)dtab + o_perm), n_vars,

@@ -194,6 +194,12 @@ def test_full_size_ou8_results(lib, dtype):
     np.testing.assert_allclose(m[-1, :, 0], mc.mean(), **tol)
     np.testing.assert_allclose(x.pstd(dtype=np.float64)[-1, :, 0], mc.std(), **tol)
     assert x.pmean().dtype == dtype
+    # FP64-class accumulation whatever the data precision
+    xa = np.asarray(x)
+    np.testing.assert_allclose(m[..., 0], xa.mean(axis=-1, dtype=np.float64), rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(x.pvar(dtype=np.float64)[..., 0], xa.var(axis=-1, dtype=np.float64),
+                               rtol=1e-11)
+    np.testing.assert_array_equal(x.pmax()[..., 0], xa.max(axis=-1))
     xq = np.linspace(-1.5, 2.5, 41)
     F = x.cdf(xq)
     assert F.shape == (11, 41, 8)
