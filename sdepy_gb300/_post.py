@@ -103,21 +103,30 @@ def cdf(x, tp, xv):
 def chf(x, tp, u):
     """Empirical characteristic function of ``x`` at time points ``tp`` (or
     every row) and arguments ``u``: complex128 shaped (n_t,) + u.shape +
-    x.shape[1:-1]."""
+    x.shape[1:-1].
+
+    The device evaluates the distinct values of |u| only: its sine and
+    cosine are exactly odd and even (so is the reference's libm), and the
+    sums run in the same order for u and -u, so chf(-u) is exactly the
+    conjugate of chf(u)."""
     a, fp32 = _values(x)
     n_rows, n_vars, paths = _rows_vars(a)
-    u = np.ascontiguousarray(u, dtype=float)
+    u = np.asarray(u, dtype=float)
     uf = u.ravel()
+    ua, inv = np.unique(np.abs(uf), return_inverse=True)   # NaN sorts last
     T, keep = _times(tp) if tp is not None else (None, None)
     n_t = T.n_t if T is not None else n_rows
-    res = np.empty((n_t, uf.size, n_vars), dtype=complex)
+    res = np.empty((n_t, ua.size, n_vars), dtype=complex)
     lib = _lib.load()
-    for j0 in range(0, uf.size, CHF_MAX_U):
-        uj = np.ascontiguousarray(uf[j0:j0 + CHF_MAX_U])
+    for j0 in range(0, ua.size, CHF_MAX_U):
+        uj = np.ascontiguousarray(ua[j0:j0 + CHF_MAX_U])
         out = np.empty((n_t, uj.size, n_vars, 2))
         _lib.check(lib.sde_process_chf(a.ctypes.data, fp32, 0, n_rows, n_vars, paths,
                                        None if T is None else C.byref(T), _lib.dptr(uj), uj.size,
                                        _lib.dptr(out)), 'process chf')
         r = res[:, j0:j0 + uj.size]
         r.real, r.imag = out[..., 0], out[..., 1]
-    return res.reshape((n_t,) + u.shape + a.shape[1:-1])
+    full = res[:, inv.ravel()]
+    neg = np.signbit(uf)
+    full[:, neg] = np.conj(full[:, neg])
+    return full.reshape((n_t,) + u.shape + a.shape[1:-1])

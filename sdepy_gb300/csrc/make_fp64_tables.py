@@ -10,7 +10,10 @@ correctly), so each table entry is within half an ulp of the true value:
   c_j = 0.75 + j/128, j = 0..96, the exact c_j, 1/c_j and ln c_j; and the
   two-double split k ln 2 = hi + lo for k = -35..0;
 * sin(pi v), cos(pi v) by angle addition: sin(pi n/64), cos(pi n/64) for
-  n = -64..64; and pi split as hi + lo.
+  n = -64..64; and pi split as hi + lo;
+* sin x, cos x for the characteristic function (sde_process.cu): the same
+  table, 64/pi, and pi/64 split into three doubles for the Cody-Waite
+  reduction x = k pi/64 + r.
 
 Pi comes from Machin's formula pi = 16 atan(1/5) - 4 atan(1/239), the
 logarithm from the atanh series ln x = 2 atanh((x-1)/(x+1)), sine and cosine
@@ -121,6 +124,15 @@ def main():
     pi_lo = d(PI - Decimal(pi_hi))
     rows.append('// pi = hi + lo\nstatic constexpr double F64_PI_HI = %r;\nstatic constexpr double F64_PI_LO = %r;\n\n'
                 % (pi_hi, pi_lo))
+    q = PI/64
+    q1 = d(q)
+    q2 = d(q - Decimal(q1))
+    q3 = d(q - Decimal(q1) - Decimal(q2))
+    rows.append('// 64 / pi, and pi / 64 = c1 + c2 + c3\n'
+                'static constexpr double F64_INV_PIO64 = %r;\n'
+                'static constexpr double F64_PIO64_1 = %r;\n'
+                'static constexpr double F64_PIO64_2 = %r;\n'
+                'static constexpr double F64_PIO64_3 = %r;\n\n' % (d(64/PI), q1, q2, q3))
     rows.append('}  // namespace sdegpu\n')
     with open(os.path.join(HERE, 'fp64_tables.h'), 'w') as f:
         f.write(''.join(rows))

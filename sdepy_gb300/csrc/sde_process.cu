@@ -31,6 +31,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "fp64_tables.h"
 #include "sdepy_gb300.h"
 #include "sde_runtime.h"
 
@@ -41,7 +42,7 @@ namespace {
 constexpr int PB = 256;           // threads per block
 constexpr int SHIFT_N = 64;       // leading values averaged into a series' shift
 constexpr int CHF_CHUNK = 4096;   // values staged per chf block iteration
-constexpr int CHF_UT = 8;         // u values per chf register tile
+constexpr int CHF_UT = 8;         // u values per chf register tile (at most)
 constexpr int CDF_SMEM_MAX = 8192;  // thresholds held in shared memory
 constexpr int CDF_ILP = 4;          // values searched side by side per thread
 
@@ -431,9 +432,44 @@ __global__ void cdf_final_kernel(const unsigned long long *__restrict__ counts, 
 // ---------------------------------------------------------------------------
 // chf
 // ---------------------------------------------------------------------------
+// sin a and cos a in FP64 (|a| <= 2^20; larger or non-finite a go to CUDA's
+// sincos): Cody-Waite reduction a = k pi/64 + r with pi/64 split into two
+// doubles (a - k c1 is exact, the c2 term's rounding is below an ulp of r;
+// the third part of the split is below 2^-110 k), sin and cos of k pi/64
+// from the angle-addition table of the Box-Muller transform (entries
+// correctly rounded), the Taylor series of sin r to r^7 and of cos r - 1 to
+// r^6 (|r| <= pi/128: the next terms are below 2^-60 relative), and the
+// table values added last: s = S + (C sin r + S (cos r - 1)).  About 1 ulp,
+// 15 FP64 operations.
+__device__ __forceinline__ void sincos_tab(double a, double &s, double &c) {
+    if (!(fabs(a) <= 0x1p20)) {
+        sincos(a, &s, &c);
+        return;
+    }
+    const double big = 0x1.8p52;   // adding it rounds to an integer
+    const double t = __fma_rn(a, F64_INV_PIO64, big);
+    const double kd = __dsub_rn(t, big);
+    const int idx = (__double2loint(t) + 64) & 127;   // k mod 128 as n + 64, n in [-64, 64)
+    double r = __fma_rn(-kd, F64_PIO64_1, a);
+    r = __fma_rn(-kd, F64_PIO64_2, r);
+    const double r2 = __dmul_rn(r, r);
+    double ps = -1.0 / 5040.0;
+    ps = __fma_rn(ps, r2, 1.0 / 120.0);
+    ps = __fma_rn(ps, r2, -1.0 / 6.0);
+    const double sr = __fma_rn(__dmul_rn(r, r2), ps, r);
+    double pc = -1.0 / 720.0;
+    pc = __fma_rn(pc, r2, 1.0 / 24.0);
+    pc = __fma_rn(pc, r2, -0.5);
+    const double cm1 = __dmul_rn(r2, pc);
+    const double S = __ldg(&F64_SINPI_N[idx]), C = __ldg(&F64_COSPI_N[idx]);
+    s = __dadd_rn(S, __fma_rn(C, sr, __dmul_rn(S, cm1)));
+    c = __dadd_rn(C, __fma_rn(-S, sr, __dmul_rn(C, cm1)));
+}
+
 // part[s][bx][j][2] = sum over the values of series s handled by block bx
-// of (cos(u_j v), sin(u_j v)); block bx handles chunks bx, bx + nch, ...
-template <typename R>
+// of (cos(u_j v), sin(u_j v)); block bx handles chunks bx, bx + nch, ...;
+// UT values of u per register tile (1, 2, 4 or 8: no padding below 8 u)
+template <typename R, int UT>
 __global__ void __launch_bounds__(PB) chf_kernel(const R *__restrict__ x, int64_t n_vars, int64_t paths,
                                                  const TimePoint *__restrict__ tps, int64_t n_series,
                                                  const double *__restrict__ u, int n_u, int nch,
@@ -441,7 +477,7 @@ __global__ void __launch_bounds__(PB) chf_kernel(const R *__restrict__ x, int64_
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double *vals = reinterpret_cast<double *>(smem_raw);              // [CHF_CHUNK]
     double *acc = vals + CHF_CHUNK;                                     // [n_u][2]
-    __shared__ double red[PB / 32][2 * CHF_UT];
+    __shared__ double red[PB / 32][2 * UT];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int64_t s = blockIdx.y; s < n_series; s += gridDim.y) {
         const TimePoint tp = tps[s / n_vars];
@@ -457,10 +493,10 @@ __global__ void __launch_bounds__(PB) chf_kernel(const R *__restrict__ x, int64_
             else
                 for (int k = threadIdx.x; k < cn; k += PB) vals[k] = (double)read_value<true>(xl, xh, tp, c0 + k);
             __syncthreads();
-            for (int j0 = 0; j0 < n_u; j0 += CHF_UT) {
-                double c[CHF_UT], sn[CHF_UT], uj[CHF_UT];
+            for (int j0 = 0; j0 < n_u; j0 += UT) {
+                double c[UT], sn[UT], uj[UT];
 #pragma unroll
-                for (int q = 0; q < CHF_UT; ++q) {
+                for (int q = 0; q < UT; ++q) {
                     c[q] = 0.0;
                     sn[q] = 0.0;
                     uj[q] = j0 + q < n_u ? __ldg(u + j0 + q) : 0.0;
@@ -468,27 +504,27 @@ __global__ void __launch_bounds__(PB) chf_kernel(const R *__restrict__ x, int64_
                 for (int k = threadIdx.x; k < cn; k += PB) {
                     const double v = vals[k];
 #pragma unroll
-                    for (int q = 0; q < CHF_UT; ++q) {
+                    for (int q = 0; q < UT; ++q) {
                         double sv, cv;
-                        sincos(__dmul_rn(uj[q], v), &sv, &cv);
+                        sincos_tab(__dmul_rn(uj[q], v), sv, cv);
                         c[q] += cv;
                         sn[q] += sv;
                     }
                 }
 #pragma unroll
-                for (int q = 0; q < CHF_UT; ++q)
+                for (int q = 0; q < UT; ++q)
                     for (int o = 16; o > 0; o >>= 1) {
                         c[q] += __shfl_xor_sync(0xffffffffu, c[q], o);
                         sn[q] += __shfl_xor_sync(0xffffffffu, sn[q], o);
                     }
                 if (lane == 0)
 #pragma unroll
-                    for (int q = 0; q < CHF_UT; ++q) {
+                    for (int q = 0; q < UT; ++q) {
                         red[warp][2 * q] = c[q];
                         red[warp][2 * q + 1] = sn[q];
                     }
                 __syncthreads();
-                if (threadIdx.x < 2 * CHF_UT && j0 + threadIdx.x / 2 < n_u) {
+                if (threadIdx.x < 2 * UT && j0 + threadIdx.x / 2 < n_u) {
                     double a = 0.0;
                     for (int w = 0; w < PB / 32; ++w) a += red[w][threadIdx.x];
                     acc[2 * j0 + threadIdx.x] += a;
@@ -743,8 +779,8 @@ int chf_impl(const void *x, int on_device, int64_t n_rows, int64_t n_vars, int64
     void *dtab, *part, *res;
     if ((rc = rt_scratch(1, tab_bytes, &dtab))) return rc;
     PCU(cudaMemcpyAsync(dtab, tab.data(), tab_bytes, cudaMemcpyHostToDevice, c.st));
-    // blocks per series: 2 per SM in all, at most one per chunk
-    const int64_t target = (int64_t)c.sms * 2;
+    // blocks per series: 8 per SM in all, at most one per chunk
+    const int64_t target = (int64_t)c.sms * 8;
     int64_t nch = (target + n_series - 1) / n_series;
     const int64_t maxch = (paths + CHF_CHUNK - 1) / CHF_CHUNK;
     if (nch > maxch) nch = maxch;
@@ -753,11 +789,19 @@ int chf_impl(const void *x, int on_device, int64_t n_rows, int64_t n_vars, int64
     const size_t out_bytes = sizeof(double) * 2 * n_series * n_u;
     if ((rc = rt_scratch(3, out_bytes, &res))) return rc;
     const size_t smem = sizeof(double) * (CHF_CHUNK + 2 * n_u);
-    PCU(cudaFuncSetAttribute(chf_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    if (c.timing) PCU(cudaEventRecord(c.ev0, c.st));
-    chf_kernel<R><<<dim3((unsigned)nch, grid_y(n_series)), PB, smem, c.st>>>(
-        (const R *)dx, n_vars, paths, (const TimePoint *)dtab, n_series, (const double *)((char *)dtab + o_u),
-        (int)n_u, (int)nch, (double *)part);
+    auto launch = [&](auto kern) -> int {
+        PCU(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        if (c.timing) PCU(cudaEventRecord(c.ev0, c.st));
+        kern<<<dim3((unsigned)nch, grid_y(n_series)), PB, smem, c.st>>>(
+            (const R *)dx, n_vars, paths, (const TimePoint *)dtab, n_series,
+            (const double *)((char *)dtab + o_u), (int)n_u, (int)nch, (double *)part);
+        return SDE_OK;
+    };
+    rc = n_u >= CHF_UT ? launch(chf_kernel<R, CHF_UT>)
+         : n_u > 2    ? launch(chf_kernel<R, 4>)
+         : n_u > 1    ? launch(chf_kernel<R, 2>)
+                      : launch(chf_kernel<R, 1>);
+    if (rc) return rc;
     chf_final_kernel<<<(unsigned)((n_series * n_u + 255) / 256), 256, 0, c.st>>>(
         (const double *)part, n_series, (int)nch, (int)n_u, n_vars, paths, (double *)res);
     if (c.timing) PCU(cudaEventRecord(c.ev1, c.st));

@@ -215,3 +215,26 @@ def test_full_size_ou8_results(lib, dtype):
     Fi = x.cdf(2.25, xq)
     ref = pp.cdf(tl, np.asarray(x[:, 3:4]), 2.25, xq)
     np.testing.assert_array_equal(Fi[:, 3], ref[:, 0])
+
+
+@pytest.mark.gpu
+def test_device_sine_cosine_accuracy(lib):
+    """chf of a one-path process of value 1 is (cos u, sin u): the
+    table-driven FP64 sine and cosine of the chf kernel against libm
+    (numpy) -- reduction boundaries, multiples of pi/64, the largest
+    reduced arguments (2^20) and CUDA's sincos beyond them, non-finite u."""
+    rng = np.random.default_rng(8)
+    k = np.arange(-3000, 3000)
+    u = np.concatenate([np.linspace(-10, 10, 2001), rng.uniform(-1e3, 1e3, 3000),
+                        rng.uniform(-2.**20, 2.**20, 3000), k*np.pi/64, k*np.pi/64 + 1e-9,
+                        k*np.pi/64 + np.pi/128, np.pi/2*k[:100],
+                        [0., -0., 1e-300, -1e-20, 2.**20, -2.**20, 2.**20 + 1, 1e10, -3e15,
+                         np.inf, -np.inf, np.nan]])
+    p = sg.process(t=[0.], x=np.ones((1, 1)))
+    ch = p.chf(u)[0]
+    with np.errstate(invalid='ignore'):
+        c, s = np.cos(u), np.sin(u)
+    np.testing.assert_array_equal(np.isnan(ch.real), np.isnan(c))
+    m = ~np.isnan(c)
+    assert np.max(np.abs(ch.real[m] - c[m])) <= 4*2.**-53
+    assert np.max(np.abs(ch.imag[m] - s[m])) <= 4*2.**-53
