@@ -56,12 +56,14 @@ extern "C" {
 #define SDE_MODEL_LINEAR  0  /* dx = c_dt*dt + c_dw*dw [+ dj]: wiener, lognorm, jumpdiff */
 #define SDE_MODEL_OU      1  /* dx = k*(theta - x)*dt + sigma*dw: OU, Hull-White factors */
 #define SDE_MODEL_HESTON  2  /* (log x, y) with full truncation y+ = max(y, 0)           */
+#define SDE_MODEL_CIR     3  /* dx = k*(theta - x+)*dt + xi*sqrt(x+)*dw, x+ = max(x, 0)  */
 
 /* params[p][w] meaning, per model (w = state variable index):
  *   LINEAR : p0 = c_dt, p1 = c_dw, p2 = lam, p3 = a, p4 = b, p5 = pa
  *   OU     : p0 = k, p1 = theta, p2 = sigma
  *   HESTON : w in the first half of a group (log-price):  p0 = mu, p1 = sigma
  *            w in the second half of a group (variance):  p0 = k, p1 = theta, p2 = xi
+ *   CIR    : p0 = k, p1 = theta, p2 = xi
  */
 
 /* jump-size law of the compound Poisson source (LINEAR model only) */

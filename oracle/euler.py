@@ -27,7 +27,8 @@ import numpy as np
 PRESETS = ('wiener_process', 'lognorm_process', 'ornstein_uhlenbeck_process',
            'hull_white_1factor_process', 'hull_white_process',
            'full_heston_process', 'heston_process', 'jumpdiff_process',
-           'merton_jumpdiff_process', 'kou_jumpdiff_process')
+           'merton_jumpdiff_process', 'kou_jumpdiff_process',
+           'cox_ingersoll_ross_process')
 
 DEFAULTS = {
     'wiener_process': dict(x0=0., mu=0., sigma=1.),
@@ -40,6 +41,7 @@ DEFAULTS = {
     'jumpdiff_process': dict(x0=1., mu=0., sigma=1., lam=1.),
     'merton_jumpdiff_process': dict(x0=1., mu=0., sigma=1., lam=1., a=0., b=1.),
     'kou_jumpdiff_process': dict(x0=1., mu=0., sigma=1., lam=1., a=.5, b=.5, pa=.5),
+    'cox_ingersoll_ross_process': dict(x0=1., theta=1., k=1., xi=1.),
 }
 
 
@@ -217,6 +219,9 @@ def integrate(preset, params=None, timeline=(0., 1.), *, paths=1, vshape=(),
         if jumps:
             mu, sigma = P['mu'], P['sigma']
             return {'dt': (mu - sigma*sigma/2), 'dw': sigma, 'dj': 1}
+        if preset == 'cox_ingersoll_ross_process':   # integration.py:2350-2354
+            x_plus = np.maximum(x, 0.)
+            return {'dt': P['k']*(P['theta'] - x_plus), 'dw': P['xi']*np.sqrt(x_plus)}
         # heston (SDEs)
         xx_, y = unpack(x)
         mu, sigma, theta, k, xi = P['mu'], P['sigma'], P['theta'], P['k'], P['xi']

@@ -248,6 +248,14 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
                             const double drift = pp[0 * W + w] * (pp[1 * W + w] - st[m]);
                             st[m] = st[m] + (drift * dt + pp[2 * W + w] * dW[m]);
                         }
+                    } else if (s->model == SDE_MODEL_CIR) {   /* sdepy/integration.py:2350-2354 */
+                        for (int m = 0; m < M; ++m) {
+                            const int w = gi * M + m;
+                            const double xp = st[m] > 0.0 ? st[m] : 0.0;
+                            const double drift = pp[0 * W + w] * (pp[1 * W + w] - xp);
+                            const double vol = pp[2 * W + w] * sqrt(xp);
+                            st[m] = st[m] + (drift * dt + vol * dW[m]);
+                        }
                     } else {
                         const int h = M / 2;
                         double nx[SDE_MAX_GROUP];

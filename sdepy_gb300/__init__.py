@@ -12,7 +12,7 @@ from .integration import (
     wiener_process, lognorm_process, ornstein_uhlenbeck_process,
     hull_white_process, hull_white_1factor_process, full_heston_process,
     heston_process, jumpdiff_process, merton_jumpdiff_process,
-    kou_jumpdiff_process)
+    kou_jumpdiff_process, cox_ingersoll_ross_process)
 from . import infrastructure
 from .montecarlo import montecarlo   # the class, as sdepy exports it
 
@@ -25,5 +25,6 @@ __all__ = [
     'wiener_process', 'lognorm_process', 'ornstein_uhlenbeck_process',
     'hull_white_process', 'hull_white_1factor_process',
     'full_heston_process', 'heston_process', 'jumpdiff_process',
-    'merton_jumpdiff_process', 'kou_jumpdiff_process', 'montecarlo',
+    'merton_jumpdiff_process', 'kou_jumpdiff_process',
+    'cox_ingersoll_ross_process', 'montecarlo',
 ]

@@ -21,7 +21,7 @@ MAX_STRIKES = 8
 OK, ERR_INVALID, ERR_UNSUPPORTED, ERR_CUDA, ERR_DEVICE, ERR_NO_DEVICE = \
     0, -1, -2, -3, -4, -5
 
-MODEL_LINEAR, MODEL_OU, MODEL_HESTON = 0, 1, 2
+MODEL_LINEAR, MODEL_OU, MODEL_HESTON, MODEL_CIR = 0, 1, 2, 3
 JUMP_NONE, JUMP_NORM, JUMP_DOUBLE_EXP, JUMP_UNIFORM, JUMP_EXP = 0, 1, 2, 3, 4
 FP64, FP32 = 0, 1
 OUT_STATE, OUT_EXP, OUT_SUM, OUT_HESTON_X, OUT_HESTON_XY = 0, 1, 2, 3, 4

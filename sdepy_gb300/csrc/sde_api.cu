@@ -277,7 +277,7 @@ static int check_spec(const SdeSpec *s, int *opg) {
     if (!s) return fail(SDE_ERR_INVALID, "spec is NULL");
     if (s->abi_version != SDE_ABI_VERSION)
         return fail(SDE_ERR_INVALID, "spec abi_version %d != %d", s->abi_version, SDE_ABI_VERSION);
-    if (s->model < SDE_MODEL_LINEAR || s->model > SDE_MODEL_HESTON)
+    if (s->model < SDE_MODEL_LINEAR || s->model > SDE_MODEL_CIR)
         return fail(SDE_ERR_UNSUPPORTED, "unknown model %d", s->model);
     if (s->precision != SDE_FP64 && s->precision != SDE_FP32)
         return fail(SDE_ERR_UNSUPPORTED, "unknown precision %d", s->precision);
@@ -339,25 +339,30 @@ static int maxm_of(int M) {
 template <typename R> struct Finder;
 template <> struct Finder<double> {
     static FwdLauncher<double> find(int model, int maxm, bool inj, bool jmp, int *bps) {
+        if (model == SDE_MODEL_CIR) return jmp ? nullptr : find_fwd_f64_cir(maxm, inj, false, bps);
         FwdLauncher<double> f = find_fwd_f64_linear(model, maxm, inj, jmp, bps);
         return f ? f : find_fwd_f64_ou_heston(model, maxm, inj, jmp, bps);
     }
     static FwdLauncher<double> find_tdep(int, int, int *) { return nullptr; }
     static FwdLauncher<double> find_anti(int model, int maxm, bool jmp, int *bps) {
+        if (model == SDE_MODEL_CIR) return jmp ? nullptr : find_fwd_f64_cir(maxm, false, true, bps);
         return find_fwd_f64_anti(model, maxm, jmp, bps);
     }
 };
 template <> struct Finder<float> {
     static FwdLauncher<float> find(int model, int maxm, bool inj, bool jmp, int *bps) {
+        if (model == SDE_MODEL_CIR) return jmp ? nullptr : find_fwd_f32_cir(maxm, inj, false, false, bps);
         FwdLauncher<float> f = find_fwd_f32_linear(model, maxm, inj, jmp, bps);
         return f ? f : find_fwd_f32_ou_heston(model, maxm, inj, jmp, bps);
     }
     // time-dependent coefficients: OU run tables with a time-dependent
-    // theta, Heston with per-step reloads
+    // theta, Heston and CIR with per-step reloads
     static FwdLauncher<float> find_tdep(int model, int maxm, int *bps) {
+        if (model == SDE_MODEL_CIR) return find_fwd_f32_cir(maxm, false, true, false, bps);
         return find_fwd_f32_tdep(model, maxm, bps);
     }
     static FwdLauncher<float> find_anti(int model, int maxm, bool jmp, int *bps) {
+        if (model == SDE_MODEL_CIR) return jmp ? nullptr : find_fwd_f32_cir(maxm, false, false, true, bps);
         return find_fwd_f32_anti(model, maxm, jmp, bps);
     }
 };
@@ -435,7 +440,7 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     const size_t njt = jumps ? (size_t)n_steps * W + 1 : 1;
     const size_t o_p0 = o_lam + al(sizeof(double) * njt);
     const size_t o_thr = o_p0 + al(sizeof(double) * njt);
-    const bool tab = sizeof(R) == 4 && !inject && s->model != SDE_MODEL_HESTON;
+    const bool tab = sizeof(R) == 4 && !inject && (s->model == SDE_MODEL_LINEAR || s->model == SDE_MODEL_OU);
     const int tmaxm = maxm_of(M);
     // parameters of step k: the time-dependent table's row, or the constants
     const double *ptab = gr->params_t;
@@ -704,9 +709,10 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     // ---- launch ----------------------------------------------------------------------
     int bps = 0;
     if (anti && ou_b) return fail(SDE_ERR_UNSUPPORTED, "antithetic paths with a time-dependent OU theta");
-    // the FP32 Heston kernels of device noise read per-step coefficients
-    // only in their time-dependent instantiation
-    const bool tdep_k = ou_b || (sizeof(R) == 4 && nprmt && !inject && !anti && s->model == SDE_MODEL_HESTON);
+    // the FP32 Heston and CIR kernels of device noise read per-step
+    // coefficients only in their time-dependent instantiation
+    const bool tdep_k = ou_b || (sizeof(R) == 4 && nprmt && !inject && !anti &&
+                                 (s->model == SDE_MODEL_HESTON || s->model == SDE_MODEL_CIR));
     FwdLauncher<R> L = anti     ? Finder<R>::find_anti(s->model, maxm_of(M), jumps, &bps)
                        : tdep_k ? Finder<R>::find_tdep(s->model, maxm_of(M), &bps)
                                 : Finder<R>::find(s->model, maxm_of(M), inject, jumps, &bps);

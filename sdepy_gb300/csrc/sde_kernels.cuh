@@ -582,7 +582,7 @@ __device__ __forceinline__ void jump_size_grad(int law, uint4 r, R ja, R jb, R j
 // blocks (24 warps) per SM
 template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS, bool ANTI = false>
 struct FwdOccupancy {
-    static constexpr int CAP_M = (MODEL == SDE_MODEL_HESTON ? 4 : 8) / (ANTI ? 2 : 1);
+    static constexpr int CAP_M = (MODEL == SDE_MODEL_HESTON || MODEL == SDE_MODEL_CIR ? 4 : 8) / (ANTI ? 2 : 1);
     static constexpr int MIN_BLOCKS = (sizeof(R) == 4 && MAXM <= CAP_M && !INJECT && !JUMPS) ? 3 : 1;
 };
 
@@ -600,12 +600,12 @@ __global__ void __launch_bounds__(BLOCK, (FwdOccupancy<R, MODEL, MAXM, INJECT, J
 sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     typedef Ar<R> A;
     constexpr int NCMAX = NoiseShape<MAXM, JUMPS>::NCMAX;
-    constexpr bool TAB = sizeof(R) == 4 && MODEL != SDE_MODEL_HESTON && !INJECT;
+    constexpr bool TAB = sizeof(R) == 4 && (MODEL == SDE_MODEL_LINEAR || MODEL == SDE_MODEL_OU) && !INJECT;
     constexpr bool SHIFT = TAB && MODEL == SDE_MODEL_OU;  // state held as x - theta
     constexpr int NA = ANTI ? 2 : 1;   // paths per thread
     constexpr bool TDB = TDEP && SHIFT;   // OU rows with the time-dependent-theta term
     // per-step coefficient reloads compiled in (the non-table kernels but
-    // the common FP32 Heston ones)
+    // the common FP32 Heston and CIR ones)
     constexpr bool RELOAD = !TAB && (sizeof(R) == 8 || INJECT || ANTI || TDEP);
     __shared__ R red[BLOCK / 32];
     __shared__ double part[MAXM][NPART];
@@ -893,6 +893,14 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                             const R drift = A::mul(c0[m], A::sub(c1[m], st[m]));
                             st[m] = A::add(st[m], A::add(A::mul(drift, dt), A::mul(c2[m], dW[m])));
                         }
+                    } else if (MODEL == SDE_MODEL_CIR) {   // k*(theta - x+), xi*sqrt(x+)
+#pragma unroll
+                        for (int m = 0; m < MAXM; ++m) {
+                            const R xp = fmax(st[m], R(0));
+                            const R drift = A::mul(c0[m], A::sub(c1[m], xp));
+                            const R vol = A::mul(c2[m], A::sqrt_(xp));
+                            st[m] = A::add(st[m], A::add(A::mul(drift, dt), A::mul(vol, dW[m])));
+                        }
                     } else {  // HESTON: first half log-price, second half variance
                         // Heston kernels run with group_size == MAXM exactly
                         constexpr int h = MAXM / 2;
@@ -1026,6 +1034,9 @@ FwdLauncher<float> find_fwd_f32_ou_heston(int model, int maxm, bool inject, bool
 // FP32 device-noise kernels with time-dependent coefficients: OU with a
 // time-dependent theta, Heston
 FwdLauncher<float> find_fwd_f32_tdep(int model, int maxm, int *bps);
+// CIR kernels (fwd_cir.cu): plain, time-dependent (FP32), antithetic
+FwdLauncher<float> find_fwd_f32_cir(int maxm, bool inject, bool tdep, bool anti, int *bps);
+FwdLauncher<double> find_fwd_f64_cir(int maxm, bool inject, bool anti, int *bps);
 // antithetic kernels (device noise, groups of up to 8 states)
 FwdLauncher<float> find_fwd_f32_anti(int model, int maxm, bool jumps, int *bps);
 FwdLauncher<double> find_fwd_f64_anti(int model, int maxm, bool jumps, int *bps);

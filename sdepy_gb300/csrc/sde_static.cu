@@ -107,7 +107,7 @@ int run_static(const SdeSpec *s, const SdeGrid *gr, const SdeStatsReq *req, SdeS
     // ---- validation (no allocation anywhere below) ---------------------------------
     if (!s || !gr || !req || !so || !so->moments) return fail_static(SDE_ERR_INVALID, "NULL argument");
     if (s->abi_version != SDE_ABI_VERSION) return fail_static(SDE_ERR_INVALID, "spec abi_version mismatch");
-    if (s->model < SDE_MODEL_LINEAR || s->model > SDE_MODEL_HESTON)
+    if (s->model < SDE_MODEL_LINEAR || s->model > SDE_MODEL_CIR)
         return fail_static(SDE_ERR_UNSUPPORTED, "unknown model %d", s->model);
     if (s->jump_law != SDE_JUMP_NONE)
         return fail_static(SDE_ERR_UNSUPPORTED, "sde_run_stats_static does not integrate jump models");
@@ -173,10 +173,12 @@ int run_static(const SdeSpec *s, const SdeGrid *gr, const SdeStatsReq *req, SdeS
     FwdLauncher<R> L = nullptr;
     const int maxm = M <= 1 ? 1 : M <= 2 ? 2 : M <= 4 ? 4 : M <= 8 ? 8 : 16;
     if constexpr (sizeof(R) == 4) {
-        L = find_fwd_f32_linear(s->model, maxm, false, false, &bps);
+        L = s->model == SDE_MODEL_CIR ? find_fwd_f32_cir(maxm, false, false, false, &bps)
+                                      : find_fwd_f32_linear(s->model, maxm, false, false, &bps);
         if (!L) L = find_fwd_f32_ou_heston(s->model, maxm, false, false, &bps);
     } else {
-        L = find_fwd_f64_linear(s->model, maxm, false, false, &bps);
+        L = s->model == SDE_MODEL_CIR ? find_fwd_f64_cir(maxm, false, false, &bps)
+                                      : find_fwd_f64_linear(s->model, maxm, false, false, &bps);
         if (!L) L = find_fwd_f64_ou_heston(s->model, maxm, false, false, &bps);
     }
     if (!L) return fail_static(SDE_ERR_UNSUPPORTED, "no kernel for model %d group size %d", s->model, M);
@@ -198,7 +200,7 @@ int run_static(const SdeSpec *s, const SdeGrid *gr, const SdeStatsReq *req, SdeS
     lo.sq = o; o = al256(o + sizeof(R) * (n_steps + 1));
     lo.x0r = o; o = al256(o + sizeof(R) * W);
     lo.prmr = o; o = al256(o + sizeof(R) * SDE_MAX_PARAMS * W);
-    const bool tab = sizeof(R) == 4 && s->model != SDE_MODEL_HESTON;
+    const bool tab = sizeof(R) == 4 && (s->model == SDE_MODEL_LINEAR || s->model == SDE_MODEL_OU);
     lo.coef = o; o = al256(o + (tab ? sizeof(float) * 2 * (size_t)n_steps * s->groups * maxm : 0));
     lo.tshift = o; o = al256(o + (tab ? sizeof(float) * 2 * (size_t)s->groups * maxm : 0));
     lo.runs = o; o = al256(o + (tab ? sizeof(int4) * (size_t)n_steps : 0));

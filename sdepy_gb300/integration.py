@@ -607,6 +607,24 @@ class hull_white_process(ornstein_uhlenbeck_process):
         return self._W // F, F
 
 
+class cox_ingersoll_ross_process(_gpu_process):
+    """Cox-Ingersoll-Ross process: dx = k*(theta - x+)*dt + xi*sqrt(x+)*dw
+    with x+ = max(x, 0) (sdepy/integration.py:2342-2400)."""
+    _params = {'x0': 1., 'theta': 1., 'k': 1., 'xi': 1.}
+    _model = _lib.MODEL_CIR
+    _tdep_names = ('theta', 'k', 'xi')
+
+    def _coefficients(self, t=1., tmid=1.):
+        A = self._args
+        ws, P = self.wshape, self.paths
+        x0 = _per_var(_const(A['x0'], 'x0'), ws, P, 'x0')
+        prm = np.zeros((_lib.MAX_PARAMS, self._W))
+        prm[0] = _per_var(self._p('k', t), ws, P, 'k')
+        prm[1] = _per_var(self._p('theta', t), ws, P, 'theta')
+        prm[2] = _per_var(self._p('xi', t), ws, P, 'xi')
+        return np.ascontiguousarray(x0), np.ascontiguousarray(prm)
+
+
 class full_heston_process(_gpu_process):
     """Heston stochastic volatility process, returning (x, y)
     (sdepy/integration.py:2403-2514): log-price and variance with full

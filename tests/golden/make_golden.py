@@ -2,7 +2,9 @@
 
 Run in a container where the reference is importable:
 
-    python tests/golden/make_golden.py [REFERENCE_DIR]
+    python tests/golden/make_golden.py [REFERENCE_DIR [GROUP ...]]
+
+(groups path, mc, tdep, cir; all by default)
 
 REFERENCE_DIR defaults to /root/reference (the read-only sdepy checkout).
 Nothing under tests/ imports this script; the tests only read the .npz files
@@ -270,14 +272,32 @@ def tdep_cases(sdepy):
              lin(0, 1, 3), (2,), paths=24, steps=20, rho=.3, seed=35, prefix='tdep')
 
 
+def cir_cases(sdepy):
+    """Cox-Ingersoll-Ross: correlated components driven below zero (full
+    truncation), and time-dependent theta / xi."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    import helpers as H
+    lin = np.linspace
+    C = np.array([[1., .3], [.3, 1.]])
+    run_case(sdepy, 'cir_corr', 'cox_ingersoll_ross_process',
+             dict(x0=[[.05], [.3]], theta=[[.04], [.5]], k=[[1.], [3.]], xi=[[.6], [.5]], vshape=2,
+                  corr=C), lin(0, 2, 5), (2,), paths=48, steps=80, corr=C, seed=41)
+    run_case(sdepy, 'cir_theta_xi', 'cox_ingersoll_ross_process',
+             dict(x0=.04, theta=H.tdep_theta_h, k=1.5, xi=H.tdep_xi), np.array([0., .5, 1.]), (),
+             paths=40, steps=50, seed=42, prefix='tdep')
+
+
 def main():
+    # python make_golden.py [REFERENCE_DIR [GROUP ...]], groups path, mc, tdep, cir
     ref = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+    groups = sys.argv[2:] or ['path', 'mc', 'tdep', 'cir']
     sys.path.insert(0, ref)
     import sdepy
     print('sdepy', sdepy.__version__, 'numpy', np.__version__)
-    path_cases(sdepy)
-    mc_cases(sdepy)
-    tdep_cases(sdepy)
+    for name, f in (('path', path_cases), ('mc', mc_cases), ('tdep', tdep_cases), ('cir', cir_cases)):
+        if name in groups:
+            f(sdepy)
 
 
 if __name__ == '__main__':

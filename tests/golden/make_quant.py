@@ -12,7 +12,7 @@ reference's quantitative tests (sdepy/tests/test_quant.py):
 
 Run where the reference is importable:
 
-    python tests/golden/make_quant.py [REFERENCE_DIR]
+    python tests/golden/make_quant.py [REFERENCE_DIR [CASE_ID ...]]
 
 The reference's tests seed numpy's legacy generator (RandomState(1234),
 sdepy/tests/shared.py:169,199-219) before each case and fail when a realised
@@ -32,10 +32,8 @@ recorded draws bit for bit (the digest) and the reference's results
 exactly; the tests regenerate the increments the same way and inject them
 into the GPU integrator.
 
-CIR is skipped: the drop-in does not provide that preset.  The pdf / cdf /
-chf parts of the tests rely on process post-processing outside the
-integration path, and so do the params2 cases that check nothing else
-(mjd / kou sweeps).  params5 (the params sweep on 100_000 paths) is not
+The pdf / cdf / chf parts of the tests are not generated here, and neither
+are the params2 cases that check nothing else (mjd / kou sweeps).  params5 (the params sweep on 100_000 paths) is not
 generated: its Heston cases alone would inject ~6 GB of increments.
 """
 import json
@@ -78,6 +76,8 @@ QUANT_CASES = [
     ('kou', 'kou_jumpdiff_process',
      dict(sigma=0.3, mu=0.1, x0=6, lam=2., pa=.80, a=0.2, b=0.3, steps=200),
      ('kou_mean', None, None), False, {}),
+    ('cir', 'cox_ingersoll_ross_process', dict(x0=0.30, theta=0.5, k=3., xi=.50, steps=200),
+     ('cir_mean', 'cir_var', 'cir_std'), False, {}),
 ]
 
 
@@ -110,6 +110,8 @@ def params_cases():
          dict(vshape=(K, 1), k=KAPPA[..., np.newaxis], sigma=0.2, xi=2., **hest), hf, True, {}),
         ('heston1_xi', 'full_heston_process',
          dict(vshape=(K, 1), xi=XI[..., np.newaxis], sigma=0.2, k=3., **hest), hf, True, {}),
+        ('cir_k', 'cox_ingersoll_ross_process', dict(vshape=K, k=KAPPA, x0=0.30, theta=0.5, xi=.50, steps=200),
+         ('cir_mean', None, 'cir_std'), False, {}),
     ]
 
 
@@ -268,19 +270,24 @@ def run_bs(sdepy):
     np.savez_compressed(os.path.join(HERE, 'bs_blackscholes.npz'), **res)
 
 
-def main(ref_dir):
+def main(ref_dir, ids=()):
+    """All cases, or those whose id is in ``ids`` ('bs' for blackscholes)."""
     sys.path.insert(0, ref_dir)
     import sdepy
     tq = np.linspace(1, 3, 50)
     for context, paths in (('quant2', 100), ('quant5', 100_000)):
         err = expected_errors(ref_dir, context)
         for case in QUANT_CASES:
-            run_case(sdepy, context, paths, case, tq, err)
+            if not ids or case[0] in ids:
+                run_case(sdepy, context, paths, case, tq, err)
     err = expected_errors(ref_dir, 'params2')
     for case in params_cases():
-        run_case(sdepy, 'params2', 100, case, (1, 2., 3), err)
-    run_bs(sdepy)
+        if not ids or case[0] in ids:
+            run_case(sdepy, 'params2', 100, case, (1, 2., 3), err)
+    if not ids or 'bs' in ids:
+        run_bs(sdepy)
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+    # python make_quant.py [REFERENCE_DIR [CASE_ID ...]]
+    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference', tuple(sys.argv[2:]))

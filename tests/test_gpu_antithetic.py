@@ -36,6 +36,7 @@ CASES = [
     ('merton', sg.merton_jumpdiff_process, dict(x0=1., mu=.03, sigma=.15, lam=4., a=-.1, b=.15),
      np.linspace(0, 1, 3), 80, 0),
     ('lognorm_i0', sg.lognorm_process, dict(x0=1.5, mu=.1, sigma=.4), np.linspace(0, 1, 6), 20, 3),
+    ('cir', sg.cox_ingersoll_ross_process, dict(vshape=2, x0=.04, theta=.04, k=1.5, xi=.5), (0., 1.), 40, 0),
 ]
 
 

@@ -91,6 +91,9 @@ def _presets():
         ('jumpdiff_unif', sg.jumpdiff_process, dict(x0=2., mu=-.1, sigma=.3, lam=3.), (0., 1., 2.), 80),
         ('lognorm_i0', sg.lognorm_process, dict(x0=1.5, mu=.1, sigma=.4, i0=3), np.linspace(0, 1, 6), 20),
         ('merton_big_lam', sg.merton_jumpdiff_process, dict(x0=1., mu=0., sigma=.1, lam=40., a=0., b=.05), (0., 1.), 10),
+        # Feller condition violated (2 k theta < xi^2): paths hit zero (full truncation)
+        ('cir', sg.cox_ingersoll_ross_process, dict(x0=.04, theta=.04, k=1.5, xi=.5), (0., .5, 1., 2.), 100),
+        ('cir_corr4', sg.cox_ingersoll_ross_process, dict(vshape=4, x0=[[.02], [.1], [.3], [.5]], theta=.2, k=[[1.], [2.], [3.], [4.]], xi=.6, corr=C8[:4, :4]), np.linspace(0, 1, 5), 50),
     ]
 
 

@@ -24,6 +24,8 @@ CASES = [
     (sg.jumpdiff_process, dict(x0=1., mu=.05, sigma=.2, lam=2.)),
     (sg.merton_jumpdiff_process, dict(x0=1., mu=.05, sigma=.2, lam=2., a=-.1, b=.15)),
     (sg.kou_jumpdiff_process, dict(x0=1., mu=.05, sigma=.2, lam=2., a=.1, b=.2, pa=.4)),
+    (sg.cox_ingersoll_ross_process, dict(x0=.3, theta=.5, k=3., xi=.5)),
+    (sg.cox_ingersoll_ross_process, dict(vshape=3, x0=[[.1], [.2], [.3]], theta=.5, k=2., xi=.4)),
 ]
 
 

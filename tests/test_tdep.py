@@ -91,6 +91,9 @@ DEVICE_CASES = [
     ('merton', sg.merton_jumpdiff_process,
      dict(x0=1., mu=TDEP['tdep_mu'], sigma=.15, lam=TDEP['tdep_lam'], a=-.1, b=.15),
      np.linspace(0, 1, 3), 80, 0),
+    ('cir', sg.cox_ingersoll_ross_process,
+     dict(vshape=2, x0=.04, theta=TDEP['tdep_theta_h'], k=1.5, xi=TDEP['tdep_xi']),
+     (0., .5, 1.), 60, 0),
 ]
 
 
