@@ -37,7 +37,7 @@ extern "C" {
 #define SDE_API
 #endif
 
-#define SDE_ABI_VERSION 2
+#define SDE_ABI_VERSION 3
 
 #define SDE_MAX_GROUP   16   /* largest correlated group (state vars) */
 #define SDE_MAX_PARAMS  6    /* coefficient arrays per state variable */
@@ -124,6 +124,14 @@ typedef struct SdeGrid {
      * sde_run_stats accept it; sde_adjoint and sde_run_stats_static return
      * SDE_ERR_UNSUPPORTED. */
     const double *params_t;
+    /* Time-dependent correlation, or NULL (SdeSpec.corr applies at every
+     * step): [n_pts - 1][M][M], row k the correlation matrix of the Wiener
+     * increments of step k, evaluated at its midpoint tt[k] + dt/2 as
+     * sdepy's wiener_source evaluates a callable corr
+     * (sdepy/infrastructure.py:1540).  The library factors every step's
+     * matrix (sde_cholesky).  Ignored with injected increments; sde_adjoint
+     * and sde_run_stats_static return SDE_ERR_UNSUPPORTED. */
+    const double *corr_t;
 } SdeGrid;
 
 typedef struct SdeNoise {   /* host arrays of injected increments (f64) */

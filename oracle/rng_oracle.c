@@ -134,6 +134,18 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
     const int64_t n_out = (int64_t)G * opg;
     double L[SDE_MAX_GROUP * SDE_MAX_GROUP];
     if (s->corr && oracle_cholesky(s->corr, M, L)) return -1;
+    /* time-dependent correlation: each step's factor (the grid's corr_t,
+     * the step's matrix at its midpoint) */
+    double *Lt = NULL;
+    if (g->corr_t && n_steps > 0) {
+        Lt = malloc(sizeof(double) * (size_t)n_steps * M * M);
+        for (int k = 0; k < n_steps; ++k)
+            if (oracle_cholesky(g->corr_t + (size_t)k * M * M, M, Lt + (size_t)k * M * M)) {
+                free(Lt);
+                return -1;
+            }
+    }
+    const int has_corr = s->corr != NULL || Lt != NULL;
     const uint32_t key[2] = {(uint32_t)s->seed, (uint32_t)(s->seed >> 32)};
     double sgn = 1.0;
     if (n_steps > 0 && g->tt[1] < g->tt[0]) sgn = -1.0;
@@ -201,10 +213,11 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
                     }
                     if (zsign < 0)   /* the antithetic path */
                         for (int m = 0; m < M; ++m) z[m] = -z[m];
+                    const double *Lk = Lt ? Lt + (size_t)k * M * M : L;
                     for (int m = 0; m < M; ++m) {
-                        if (s->corr) {
-                            double acc = L[m * M + 0] * z[0];
-                            for (int j = 1; j <= m; ++j) acc = acc + L[m * M + j] * z[j];
+                        if (has_corr) {
+                            double acc = Lk[m * M + 0] * z[0];
+                            for (int j = 1; j <= m; ++j) acc = acc + Lk[m * M + j] * z[j];
                             dW[m] = acc * sq;
                         } else {
                             dW[m] = z[m] * sq;
@@ -315,5 +328,6 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
     }
     free(dtv);
     free(sqv);
+    free(Lt);
     return rc;
 }

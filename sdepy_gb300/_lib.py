@@ -13,7 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, '_native', 'libsdepy_gb300.so')
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 MAX_GROUP = 16
 MAX_PARAMS = 6
 MAX_STRIKES = 8
@@ -45,7 +45,7 @@ class SdeSpec(C.Structure):
 
 class SdeGrid(C.Structure):
     _fields_ = [('tt', _dp), ('out_row', _ip), ('n_pts', C.c_int32),
-                ('step_offset', C.c_uint32), ('params_t', _dp)]
+                ('step_offset', C.c_uint32), ('params_t', _dp), ('corr_t', _dp)]
 
 
 class SdeNoise(C.Structure):

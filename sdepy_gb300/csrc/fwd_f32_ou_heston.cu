@@ -80,14 +80,20 @@ FwdLauncher<float> find_fwd_f32_ou_heston(int model, int maxm, bool inject, bool
 }
 
 
-// time-dependent coefficients: OU run tables with the theta term, Heston
-// with per-step coefficient reloads (device noise, no jumps)
+// time-dependent coefficients and correlations (device noise, no jumps):
+// LINEAR run tables, OU run tables with the theta term, Heston with per-step
+// coefficient reloads; all with per-step correlation factors
 FwdLauncher<float> find_fwd_f32_tdep(int model, int maxm, int *bps) {
 #define SDE_TDEP(MODEL, M)                                                               \
     if (model == MODEL && maxm == M) {                                                   \
         if (bps) *bps = fwd_max_blocks_per_sm<float, MODEL, M, false, false, true>();    \
         return &launch_fwd<float, MODEL, M, false, false, true>;                         \
     }
+    SDE_TDEP(SDE_MODEL_LINEAR, 1)
+    SDE_TDEP(SDE_MODEL_LINEAR, 2)
+    SDE_TDEP(SDE_MODEL_LINEAR, 4)
+    SDE_TDEP(SDE_MODEL_LINEAR, 8)
+    SDE_TDEP(SDE_MODEL_LINEAR, 16)
     SDE_TDEP(SDE_MODEL_OU, 1)
     SDE_TDEP(SDE_MODEL_OU, 2)
     SDE_TDEP(SDE_MODEL_OU, 4)

@@ -453,6 +453,13 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     if (tab && ptab && s->model == SDE_MODEL_OU)
         for (int k = 0; k < n_steps && !ou_b; ++k)
             for (int w = 0; w < W && !ou_b; ++w) ou_b = params_of(k)[W + w] != params_of(0)[W + w];
+    // time-dependent correlation (device noise): per-step Cholesky factors,
+    // read by the kernels compiled with per-step reloads -- for FP32 the
+    // time-dependent instantiations, whose OU form carries the b column
+    const bool corr_steps = gr->corr_t != nullptr && !inject && M > 1;
+    if (corr_steps && sizeof(R) == 4 && jumps && !anti)
+        return fail(SDE_ERR_UNSUPPORTED, "time-dependent correlations of FP32 jump models");
+    if (corr_steps && tab && s->model == SDE_MODEL_OU && !anti) ou_b = true;
     const int nb = ou_b ? 3 : 2;   // coefficient vectors per row
     // FP32 LINEAR / OU: the grid as runs of steps with one coefficient row
     // each, and the compact table of those rows (see FwdArgs::coef / runs)
@@ -525,7 +532,9 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     // the other kernels read time-dependent coefficients (slots 0..2) per step
     const size_t nprmt = (ptab && !tab) ? (size_t)n_steps * 3 * W : 0;
     const size_t o_prmt = o_tsh + al(sizeof(float) * (tshift.size() + 4));
-    const size_t o_end = o_prmt + al(sizeof(R) * (nprmt + 1));
+    const size_t nchol = corr_steps ? (size_t)n_steps * NCHOL : 0;
+    const size_t o_cholt = o_prmt + al(sizeof(R) * (nprmt + 1));
+    const size_t o_end = o_cholt + al(sizeof(R) * (nchol + 1));
     D->host_tables.resize(o_end);
     char *H = D->host_tables.data();
     R *h_dt = (R *)(H + o_dt), *h_sq = (R *)(H + o_sq), *h_x0 = (R *)(H + o_x0), *h_prm = (R *)(H + o_prm);
@@ -577,6 +586,21 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
             for (int v = 0; v < 3; ++v)
                 for (int w = 0; w < W; ++w) h_prmt[((size_t)k * 3 + v) * W + w] = (R)params_of(k)[v * W + w];
     }
+    if (nchol) {
+        R *h_cholt = (R *)(H + o_cholt);
+        std::vector<double> L(M * M);
+        for (int k = 0; k < n_steps; ++k) {
+            if ((rc = sde_cholesky(gr->corr_t + (size_t)k * M * M, M, L.data()))) {
+                char m[256];
+                snprintf(m, sizeof m, "correlation of step %d: %s", k, g_err.c_str());
+                return fail(rc, "%s", m);
+            }
+            R *row = h_cholt + (size_t)k * NCHOL;
+            for (int i = 0; i < NCHOL; ++i) row[i] = R(0);
+            for (int i = 0; i < M; ++i)
+                for (int j = 0; j <= i; ++j) row[i * (i + 1) / 2 + j] = (R)L[i * M + j];
+        }
+    }
 
     FwdArgs<R> a;
     memset(&a, 0, sizeof a);
@@ -623,6 +647,8 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
         a.tshift = tshift.empty() ? nullptr : (const float *)(T + o_tsh);
     }
     a.prm_t = nprmt ? (const R *)(T + o_prmt) : nullptr;
+    a.chol_t = nchol ? (const R *)(T + o_cholt) : nullptr;
+    if (nchol) a.has_corr = 1;
     a.key = philox_schedule(s->seed);
     a.n_out_vars = n_out;
 
@@ -711,8 +737,9 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     if (anti && ou_b) return fail(SDE_ERR_UNSUPPORTED, "antithetic paths with a time-dependent OU theta");
     // the FP32 Heston and CIR kernels of device noise read per-step
     // coefficients only in their time-dependent instantiation
-    const bool tdep_k = ou_b || (sizeof(R) == 4 && nprmt && !inject && !anti &&
-                                 (s->model == SDE_MODEL_HESTON || s->model == SDE_MODEL_CIR));
+    const bool tdep_k = ou_b || (sizeof(R) == 4 && !inject && !anti &&
+                                 ((nprmt && (s->model == SDE_MODEL_HESTON || s->model == SDE_MODEL_CIR)) ||
+                                  corr_steps));
     FwdLauncher<R> L = anti     ? Finder<R>::find_anti(s->model, maxm_of(M), jumps, &bps)
                        : tdep_k ? Finder<R>::find_tdep(s->model, maxm_of(M), &bps)
                                 : Finder<R>::find(s->model, maxm_of(M), inject, jumps, &bps);
@@ -1146,6 +1173,8 @@ extern "C" int32_t sde_adjoint(const SdeSpec *spec, const SdeGrid *grid, const S
     if (!spec) return fail(SDE_ERR_INVALID, "spec is NULL");
     if (grid && grid->params_t)
         return fail(SDE_ERR_UNSUPPORTED, "the adjoint takes constant parameters (grid params_t must be NULL)");
+    if (grid && grid->corr_t)
+        return fail(SDE_ERR_UNSUPPORTED, "the adjoint takes a constant correlation (grid corr_t must be NULL)");
     if (spec->flags) return fail(SDE_ERR_UNSUPPORTED, "the adjoint takes no spec flags (antithetic paths)");
     if (spec->precision == SDE_FP32) return adjoint_impl<float>(spec, grid, req, grad, value);
     return adjoint_impl<double>(spec, grid, req, grad, value);

@@ -66,6 +66,10 @@ struct FwdArgs {
     // the other kernels with time-dependent parameters: [steps][3][W] =
     // parameter slots 0..2 of each step, or NULL (prm applies throughout)
     const R *prm_t;
+    // time-dependent correlation: [steps][NCHOL] packed Cholesky factors of
+    // each step's correlation matrix (rows as chol below), or NULL; read
+    // only by the kernels that reload per-step coefficients (STEPCORR)
+    const R *chol_t;
     // and the grid as runs of steps sharing one coefficient row:
     // (first step, end step, output row stored after the run or -1, coef row)
     const int4 *runs;
@@ -607,6 +611,9 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     // per-step coefficient reloads compiled in (the non-table kernels but
     // the common FP32 Heston and CIR ones)
     constexpr bool RELOAD = !TAB && (sizeof(R) == 8 || INJECT || ANTI || TDEP);
+    // per-step correlation factors compiled in (the same kernels, TAB ones
+    // included, with device noise)
+    constexpr bool STEPCORR = !INJECT && (sizeof(R) == 8 || ANTI || TDEP);
     __shared__ R red[BLOCK / 32];
     __shared__ double part[MAXM][NPART];
     __shared__ R svs[NA][MAXM][BLOCK];   // this round's value of each output at the stats row
@@ -759,6 +766,10 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
             auto draw = [&](int k, R sq, R (&dW)[MAXM], R (&dJ)[MAXM]) {
 #pragma unroll
                 for (int m = 0; m < MAXM; ++m) dJ[m] = R(0);
+                // the step's correlation factor (uniform choice)
+                const R *chol = a.chol;
+                if constexpr (STEPCORR)
+                    if (a.chol_t) chol = a.chol_t + (int64_t)k * NCHOL;
                 if (INJECT) {
 #pragma unroll
                     for (int m = 0; m < MAXM; ++m) {
@@ -790,18 +801,18 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                 } else if constexpr (NZ == 2) {
                     R z[MAXM];
                     pair.get(key, pre, k, a.step_offset, z[0], z[1]);
-                    correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
+                    correlate<R, MAXM>(chol, a.has_corr, z, sq, dW);
                     return;
                 }
                 if constexpr (!JUMPS) {
-                    step_increments<R, MAXM, TAB>(key, pre, c1w, NC, a.chol, a.has_corr, sq, dW);
+                    step_increments<R, MAXM, TAB>(key, pre, c1w, NC, chol, a.has_corr, sq, dW);
                     return;
                 }
                 uint32_t u[4 * NCMAX];
                 step_words<MAXM, JUMPS>(key, pre, c1w, NC, u);
                 R z[MAXM];
                 words_to_normals<R, MAXM, 4 * NCMAX, TAB>(u, z);
-                correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
+                correlate<R, MAXM>(chol, a.has_corr, z, sq, dW);
 #pragma unroll
                 for (int m = 0; m < MAXM; ++m)
                     if (m < M) add_jumps(m, pick_word(u, 2 * P + m), k, c1w, dJ);

@@ -326,8 +326,9 @@ extern "C" int32_t sde_run_stats_static(const SdeSpec *spec, const SdeGrid *grid
                                         SdeStatsOut *stats, void *stream) {
     std::lock_guard<std::mutex> lk(g_static_mu);
     if (!spec) return fail_static(SDE_ERR_INVALID, "spec is NULL");
-    if (grid && grid->params_t)
-        return fail_static(SDE_ERR_UNSUPPORTED, "constant parameters only (grid params_t must be NULL)");
+    if (grid && (grid->params_t || grid->corr_t))
+        return fail_static(SDE_ERR_UNSUPPORTED, "constant parameters and correlation only (grid params_t and "
+                                                "corr_t must be NULL)");
     if (spec->flags) return fail_static(SDE_ERR_UNSUPPORTED, "no spec flags (antithetic paths)");
     if (spec->precision == SDE_FP32) return run_static<float>(spec, grid, req, stats, (cudaStream_t)stream);
     if (spec->precision == SDE_FP64) return run_static<double>(spec, grid, req, stats, (cudaStream_t)stream);

@@ -307,32 +307,63 @@ def const_rho_to_corr(rho):
                            np.concatenate((R, I))), axis=1)
 
 
-def get_corr_matrix(corr, rho):
-    """Constant correlation matrix from ``corr`` or ``rho`` (None if both
-    are None).  Time-dependent correlations are not on the GPU path."""
-    if corr is None and rho is None:
-        return None
-    z = corr if corr is not None else rho
-    if callable(z) or isinstance(z, process):
-        raise NotImplementedError(
-            'time-dependent correlations are not supported by the GPU '
-            'integrator')
-    if corr is not None:
-        c = np.asarray(corr, dtype=float)
-        if c.ndim not in (2, 3) or c.shape[0] != c.shape[1] or \
-           (c.ndim == 3 and c.shape[2] != 1):
-            raise ValueError(
-                "the correlation matrix ``corr`` should be square, "
-                "possibly with a trailing 1-dimensional axis matching "
-                "the paths axis, not an array with shape {}".format(c.shape))
-        return c[..., 0] if c.ndim == 3 else c
+def _square_corr(c):
+    """A correlation matrix shaped (M, M) or (M, M, 1) (a trailing paths
+    axis of length 1), as (M, M)."""
+    c = np.asarray(c, dtype=float)
+    if c.ndim not in (2, 3) or c.shape[0] != c.shape[1] or \
+       (c.ndim == 3 and c.shape[2] != 1):
+        raise ValueError(
+            "the correlation matrix ``corr`` should be square, "
+            "possibly with a trailing 1-dimensional axis matching "
+            "the paths axis, not an array with shape {}".format(c.shape))
+    return c[..., 0] if c.ndim == 3 else c
+
+
+def _rho_vector(rho):
     rho = np.asarray(rho, dtype=float)
     if rho.ndim > 2 or (rho.ndim == 2 and rho.shape[1] != 1):
         raise ValueError(
             "correlation ``rho`` should be a vector, "
             "possibly with a trailing 1-dimensional axis matching "
             "the paths axis, not an array with shape {}".format(rho.shape))
-    return const_rho_to_corr(rho)
+    return rho
+
+
+class corr_of_t:
+    """A time-dependent correlation matrix: ``corr(t)`` from a callable or
+    process ``corr``, or the matrix [[I, diag(rho(t))], [diag(rho(t)), I]]
+    of a callable or process ``rho`` (sdepy/infrastructure.py:128-206).
+    ``shape`` is that of its value at t = 1, or None if that evaluation
+    fails.  The Wiener increments of a step from t to t + dt use
+    corr(t + dt/2) (sdepy/infrastructure.py:1540)."""
+
+    def __init__(self, f, from_rho=False):
+        self.f, self.from_rho = f, from_rho
+        try:
+            self.shape = self(1.).shape
+        except Exception:
+            self.shape = None
+
+    def __call__(self, t):
+        v = self.f(t)
+        if self.from_rho:
+            return const_rho_to_corr(_rho_vector(v))
+        return _square_corr(v)
+
+
+def get_corr_matrix(corr, rho):
+    """Correlation matrix from ``corr`` or ``rho`` (None if both are None):
+    an array, or a corr_of_t when either is a callable or a process."""
+    if corr is None and rho is None:
+        return None
+    if corr is not None:
+        if callable(corr) or isinstance(corr, process):
+            return corr_of_t(corr)
+        return _square_corr(corr)
+    if callable(rho) or isinstance(rho, process):
+        return corr_of_t(rho, from_rho=True)
+    return const_rho_to_corr(_rho_vector(rho))
 
 
 # ---------------------------------------------------------------------------
@@ -480,7 +511,8 @@ class source:
 
 class wiener_source(source):
     """dw: standard Wiener increments, optionally correlated along the last
-    vshape axis (sdepy/infrastructure.py:1388-1560, constant corr)."""
+    vshape axis, with a constant or time-dependent correlation
+    (sdepy/infrastructure.py:1388-1560)."""
 
     def __init__(self, *, paths=1, vshape=(), dtype=None, rng=None,
                  corr=None, rho=None):
@@ -504,11 +536,18 @@ class wiener_source(source):
         if self.corr is None:
             dz = self.rng.normal(0., 1., size=tshape + vshape + (paths,)
                                  ).astype(dtype, copy=False)
-        else:
+        elif not callable(self.corr):
             M = vshape[-1]
             dz = self.rng.multivariate_normal(
                 mean=np.zeros(M), cov=self.corr,
                 size=tshape + vshape[:-1] + (paths,)).astype(dtype, copy=False)
+            dz = dz.swapaxes(-1, -2)
+        else:   # corr(t + dt/2), one draw per time point
+            M = vshape[-1]
+            dz = np.empty(tshape + vshape[:-1] + (paths, M), dtype=dtype)
+            for i in np.ndindex(tshape):
+                dz[i] = self.rng.multivariate_normal(
+                    mean=np.zeros(M), cov=self.corr(t[i] + dt[i]/2), size=vshape[:-1] + (paths,))
             dz = dz.swapaxes(-1, -2)
         dt = dt.reshape(tshape + (1,)*len(vshape) + (1,))
         dz *= np.sqrt(np.abs(dt))

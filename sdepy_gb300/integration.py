@@ -16,10 +16,13 @@ an SDE coefficient (e.g. ``theta=lambda t: ...``) is evaluated at the start
 of every step, as sdepy's SDE.A does (sdepy/integration.py:1216-1225), and a
 time-dependent Poisson intensity at the middle of every step, as sdepy's
 poisson_source does (sdepy/infrastructure.py:1629); the values go to the
-device as a per-step table (SdeGrid.params_t).
+device as a per-step table (SdeGrid.params_t).  A callable or process
+``corr`` / ``rho`` is evaluated at the middle of every step, as sdepy's
+wiener_source does (sdepy/infrastructure.py:1540), into a per-step table of
+correlation matrices (SdeGrid.corr_t) that the library factors.
 
-What stays an error (no CPU fallback): time-dependent initial values,
-correlations and jump-size laws, per-path parameters, methods other than
+What stays an error (no CPU fallback): time-dependent initial values and
+jump-size laws, per-path parameters, methods other than
 'euler', dtypes other than float64 / float32, and SDE classes this module
 does not define; gradients (the adjoint) take constant parameters.
 """
@@ -28,7 +31,7 @@ import numpy as np
 from . import _lib, _pinned
 from .grid import Grid
 from .infrastructure import (
-    process, philox_rng, draw_key, check_rng, get_corr_matrix, law_of,
+    process, philox_rng, draw_key, check_rng, get_corr_matrix, corr_of_t, law_of,
     wiener_source, cpoisson_source, poisson_source, norm_rv, double_exp_rv,
     uniform_rv, _shape_setup, odd_wiener_source, even_cpoisson_source)
 from . import infrastructure as _inf
@@ -155,7 +158,7 @@ class _gpu_process:
                 raise ValueError(
                     'if vshape is (), no correlations apply, but '
                     'corr={}, rho={} were given'.format(A['corr'], A['rho']))
-            if self.corr.shape[:2] != 2*self.wshape[-1:]:
+            if self.corr.shape is not None and self.corr.shape[:2] != 2*self.wshape[-1:]:
                 raise ValueError(
                     'cannot instantiate a Wiener source with '
                     'values shape {} and correlation matrix shape {}'
@@ -254,7 +257,10 @@ class _gpu_process:
         # test call, sdepy/infrastructure.py:64-109); the per-step values
         # are tabulated for each integration leg
         self._x0, self._prm = self._coefficients()
-        self._corr_c = None if self.corr is None else \
+        # a time-dependent correlation goes to the device per leg and step
+        # (SdeGrid.corr_t), a constant one in the spec
+        self._corr_tdep = isinstance(self.corr, corr_of_t)
+        self._corr_c = None if (self.corr is None or self._corr_tdep) else \
             np.ascontiguousarray(self.corr, dtype=float)
         self._jump_law_id = _lib.JUMP_NONE
         if 'dj' in self._sources:
@@ -367,6 +373,16 @@ class _gpu_process:
             tab[k] = self._coefficients(t=t0, tmid=t0 + (t1 - t0)/2)[1]
         return np.ascontiguousarray(tab)
 
+    def _corr_table(self, leg):
+        """[n_steps][M][M] correlation matrices of the steps of ``leg``,
+        each at its midpoint t + dt/2 (sdepy/infrastructure.py:1540)."""
+        tt = leg.tt
+        tab = np.empty((leg.n_steps, self._M, self._M))
+        for k in range(leg.n_steps):
+            t0, t1 = float(tt[k]), float(tt[k + 1])
+            tab[k] = self.corr(t0 + (t1 - t0)/2)
+        return np.ascontiguousarray(tab)
+
     def _integrate(self, grid, write=True, stats=None):
         lib = _lib.load()
         rows = grid.n_rows
@@ -400,6 +416,8 @@ class _gpu_process:
             g.step_offset = leg.step_offset
             ptab = self._params_table(leg) if self._tdep else None
             g.params_t = _lib.dptr(ptab)
+            ctab = self._corr_table(leg) if (self._corr_tdep and not self._inject) else None
+            g.corr_t = _lib.dptr(ctab)
             out = _lib.SdeOut()
             out.xx = None if xx is None else xx.ctypes.data
             out.n_rows = rows

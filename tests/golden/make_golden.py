@@ -4,7 +4,7 @@ Run in a container where the reference is importable:
 
     python tests/golden/make_golden.py [REFERENCE_DIR [GROUP ...]]
 
-(groups path, mc, tdep, cir; all by default)
+(groups path, mc, tdep, cir, corr_t; all by default)
 
 REFERENCE_DIR defaults to /root/reference (the read-only sdepy checkout).
 Nothing under tests/ imports this script; the tests only read the .npz files
@@ -105,7 +105,7 @@ def run_case(sdepy, name, cls_name, kw, timeline, wshape, *, paths,
                             else list(steps)),
         'i0': i0,
         'kw': encode_kw(sdepy, kw, arrays),
-        'corr': np.asarray(np.nan if corr is None else corr, dtype=float),
+        'corr': np.asarray(np.nan if (corr is None or callable(corr)) else corr, dtype=float),
         'rec_t': np.array([c[0] for c in dw.calls]),
         'rec_dt': np.array([c[1] for c in dw.calls]),
         'rec_dw': np.stack([np.broadcast_to(c[2], wshape + (paths,))
@@ -272,6 +272,22 @@ def tdep_cases(sdepy):
              lin(0, 1, 3), (2,), paths=24, steps=20, rho=.3, seed=35, prefix='tdep')
 
 
+def tdep_corr_cases(sdepy):
+    """Time-dependent correlations: a callable corr and a callable rho,
+    evaluated by sdepy's wiener_source at each step's middle."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    import helpers as H
+    lin = np.linspace
+    run_case(sdepy, 'ou_corr_t', 'ornstein_uhlenbeck_process',
+             dict(x0=[[.2], [-.3]], k=[[1.], [2.5]], theta=[[.1], [.4]], sigma=[[.3], [.2]], vshape=2,
+                  corr=H.tdep_corr2),
+             lin(0, 2, 5), (2,), paths=32, steps=40, i0=2, corr=H.tdep_corr2, seed=51, prefix='tdep')
+    run_case(sdepy, 'heston_rho_t', 'heston_process',
+             dict(x0=100., mu=.02, y0=.04, k=1.5, theta=.04, xi=.5, rho=H.tdep_rho),
+             np.array([0., .5, 1.]), (2,), paths=40, steps=50, rho=H.tdep_rho, seed=52, prefix='tdep')
+
+
 def cir_cases(sdepy):
     """Cox-Ingersoll-Ross: correlated components driven below zero (full
     truncation), and time-dependent theta / xi."""
@@ -291,11 +307,12 @@ def cir_cases(sdepy):
 def main():
     # python make_golden.py [REFERENCE_DIR [GROUP ...]], groups path, mc, tdep, cir
     ref = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
-    groups = sys.argv[2:] or ['path', 'mc', 'tdep', 'cir']
+    groups = sys.argv[2:] or ['path', 'mc', 'tdep', 'cir', 'corr_t']
     sys.path.insert(0, ref)
     import sdepy
     print('sdepy', sdepy.__version__, 'numpy', np.__version__)
-    for name, f in (('path', path_cases), ('mc', mc_cases), ('tdep', tdep_cases), ('cir', cir_cases)):
+    for name, f in (('path', path_cases), ('mc', mc_cases), ('tdep', tdep_cases), ('cir', cir_cases),
+                    ('corr_t', tdep_corr_cases)):
         if name in groups:
             f(sdepy)
 

@@ -26,6 +26,8 @@ def oracle_paths(clib, proc, timeline, seed, stream=0):
         g.step_offset = leg.step_offset
         ptab = proc._params_table(leg) if proc._tdep else None   # time-dependent parameters
         g.params_t = _lib.dptr(ptab)
+        ctab = proc._corr_table(leg) if proc._corr_tdep else None   # time-dependent correlation
+        g.corr_t = _lib.dptr(ctab)
         neg = np.zeros((proc._G*proc._M//2, proc.paths), dtype=np.int32)
         jc = np.zeros((proc._W, proc.paths), dtype=np.int32)
         rj = np.zeros(rows, dtype=np.int64)
@@ -188,6 +190,25 @@ def tdep_lam(t):
 
 def tdep_k2(t):
     return np.array([[0.5 + 0.1*t], [2.]])
+
+
+def tdep_corr2(t):
+    r = 0.6*np.sin(2*t)
+    return np.array([[1., r], [r, 1.]])
+
+
+def tdep_rho(t):
+    return -0.7 + 0.3*t
+
+
+def tdep_corr4(t):
+    # positive definite: (A0 + t A1)(A0 + t A1)^T + I/5, scaled to unit diagonal
+    A0 = np.array([[1., .2, 0., .1], [.3, 1., .1, 0.], [0., .4, 1., .2], [.1, 0., .5, 1.]])
+    A1 = np.array([[0., .5, .1, 0.], [-.2, 0., .3, .1], [.1, -.1, 0., .4], [.2, .1, -.3, 0.]])
+    A = A0 + t*A1
+    C = A @ A.T + .2*np.eye(4)
+    d = np.sqrt(np.diag(C))
+    return C/np.outer(d, d)
 
 
 TDEP = {name: f for name, f in dict(globals()).items() if name.startswith('tdep_')}

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import sdepy_gb300 as sg
-from helpers import oracle_paths
+from helpers import TDEP, oracle_paths
 
 pytestmark = pytest.mark.gpu
 
@@ -37,6 +37,8 @@ CASES = [
      np.linspace(0, 1, 3), 80, 0),
     ('lognorm_i0', sg.lognorm_process, dict(x0=1.5, mu=.1, sigma=.4), np.linspace(0, 1, 6), 20, 3),
     ('cir', sg.cox_ingersoll_ross_process, dict(vshape=2, x0=.04, theta=.04, k=1.5, xi=.5), (0., 1.), 40, 0),
+    ('ou_corr_t', sg.ornstein_uhlenbeck_process,
+     dict(vshape=2, x0=.1, k=1.5, theta=.3, sigma=.3, corr=TDEP['tdep_corr2']), np.linspace(0, 1, 3), 30, 0),
 ]
 
 

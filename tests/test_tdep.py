@@ -27,11 +27,10 @@ def _oracle_args(z):
     kw = tdep_kwargs(z, sg.process)
     vshape = kw.pop('vshape', ())
     vshape = (vshape,) if isinstance(vshape, int) else tuple(vshape)
-    rho = kw.pop('rho', None)
+    # a replay takes the recorded increments: the correlation is in them
+    kw.pop('corr', None)
+    kw.pop('rho', None)
     corr = None
-    if rho is not None:
-        r = float(np.asarray(rho).reshape(-1)[0])
-        corr = np.array([[1., r], [r, 1.]])
     cls = str(z['cls'])
     _, wshape, _ = euler.shapes(cls, vshape, kw.get('factors', 1))
     paths = int(z['paths'])
@@ -66,7 +65,7 @@ def test_gpu_replay_matches_reference_tdep(lib, path):
         for k in ('a', 'b', 'pa', 'lam'):
             kw.pop(k, None)
     P = getattr(sg, str(z['cls']))(paths=paths, steps=json.loads(str(z['steps'])), i0=int(z['i0']), **kw)
-    assert P._tdep
+    assert P._tdep or P._corr_tdep
     out = P(z['timeline'])
     outs = out if isinstance(out, tuple) else (out,)
     for k, o in enumerate(outs):
@@ -94,6 +93,19 @@ DEVICE_CASES = [
     ('cir', sg.cox_ingersoll_ross_process,
      dict(vshape=2, x0=.04, theta=TDEP['tdep_theta_h'], k=1.5, xi=TDEP['tdep_xi']),
      (0., .5, 1.), 60, 0),
+    # time-dependent correlations (corr(t + dt/2) per step)
+    ('ou_corr_t', sg.ornstein_uhlenbeck_process,
+     dict(vshape=2, x0=[[.2], [-.3]], k=[[1.], [2.5]], theta=[[.1], [.4]], sigma=.3, corr=TDEP['tdep_corr2']),
+     np.linspace(0, 2, 5), 40, 2),
+    ('ou4_corr_t', sg.ornstein_uhlenbeck_process,
+     dict(vshape=4, x0=0., k=1.5, theta=.2, sigma=.3, corr=TDEP['tdep_corr4']),
+     np.linspace(0, 1, 3), 30, 0),
+    ('wiener4_corr_t', sg.wiener_process,
+     dict(vshape=4, x0=0., mu=.1, sigma=.5, corr=TDEP['tdep_corr4']), (0., 1.), 25, 0),
+    ('heston_rho_t', sg.heston_process,
+     dict(x0=100., mu=.02, y0=.04, k=1.5, theta=.04, xi=.5, rho=TDEP['tdep_rho']), (0., .5, 1.), 50, 0),
+    ('cir_corr_t', sg.cox_ingersoll_ross_process,
+     dict(vshape=2, x0=.1, theta=.2, k=2., xi=.4, corr=TDEP['tdep_corr2']), (0., 1.), 40, 0),
 ]
 
 
@@ -103,7 +115,7 @@ def test_device_rng_tdep_matches_c_oracle(lib, clib, case):
     name, cls, kw, tl, steps, i0 = case
     paths, seed = 777, 0x51ed
     P = cls(paths=paths, steps=steps, i0=i0, rng=sg.philox_rng(seed, 3), **kw)
-    assert P._tdep
+    assert P._tdep or P._corr_tdep
     out = P(tl)
     got = np.concatenate([np.asarray(o).reshape(len(o.t), -1, paths) for o in
                           (out if isinstance(out, tuple) else (out,))], axis=1)
@@ -121,6 +133,20 @@ def test_device_rng_tdep_matches_c_oracle(lib, clib, case):
                           (out32 if isinstance(out32, tuple) else (out32,))], axis=1)
     assert np.max(np.abs(g32 - ref)/np.maximum(np.abs(ref), 1.)) < 2e-3
     assert np.max(np.abs(g32.mean(-1) - ref.mean(-1))/np.maximum(np.abs(ref.mean(-1)), 1.)) < 2e-5
+
+
+@pytest.mark.parametrize('name', ['ou_corr_t', 'heston_rho_t'])
+def test_host_wiener_source_reproduces_reference_correlated_draws(name):
+    """The host wiener_source with a callable corr / rho (used for
+    injection) draws the reference's recorded increments from the same
+    generator: corr(t + dt/2) per call, multivariate_normal."""
+    z = np.load(os.path.join(os.path.dirname(__file__), 'golden', 'tdep_%s.npz' % name))
+    kw = tdep_kwargs(z, sg.process)
+    seed = {'ou_corr_t': 51, 'heston_rho_t': 52}[name]
+    src = sg.wiener_source(paths=int(z['paths']), vshape=z['rec_dw'].shape[1:-1],
+                           rng=np.random.default_rng(seed), corr=kw.get('corr'), rho=kw.get('rho'))
+    for t, dt, ref in zip(z['rec_t'], z['rec_dt'], z['rec_dw']):
+        np.testing.assert_array_equal(src(t, dt), ref)
 
 
 @pytest.mark.gpu
