@@ -57,6 +57,7 @@ extern "C" {
 #define SDE_MODEL_OU      1  /* dx = k*(theta - x)*dt + sigma*dw: OU, Hull-White factors */
 #define SDE_MODEL_HESTON  2  /* (log x, y) with full truncation y+ = max(y, 0)           */
 #define SDE_MODEL_CIR     3  /* dx = k*(theta - x+)*dt + xi*sqrt(x+)*dw, x+ = max(x, 0)  */
+#define SDE_MODEL_USER    4  /* dx = A_dt(t, x, p)*dt + A_dw(t, x, p)*dw, SdeUserProgram  */
 
 /* params[p][w] meaning, per model (w = state variable index):
  *   LINEAR : p0 = c_dt, p1 = c_dw, p2 = lam, p3 = a, p4 = b, p5 = pa
@@ -64,7 +65,37 @@ extern "C" {
  *   HESTON : w in the first half of a group (log-price):  p0 = mu, p1 = sigma
  *            w in the second half of a group (variance):  p0 = k, p1 = theta, p2 = xi
  *   CIR    : p0 = k, p1 = theta, p2 = xi
+ *   USER   : p0..p5 = the SDE function's parameters, in the program's order
  */
+
+/* A user SDE (sdepy's integrate decorator, sdepy/integration.py:1843-1955):
+ * the coefficients A_dt and A_dw of one equation, compiled from the SDE
+ * function into a straight-line program evaluated per state variable and
+ * step.  Registers: r0 = x (the state), r1 = t (the step's start), r2..r7 =
+ * parameters p0..p5, the rest temporaries; SDE_USER_MAX_REGS in all.  An
+ * instruction is code | dst << 8 | a << 16 | b << 24 (SDE_UOP_*: dst = f(ra,
+ * rb); SDE_UOP_CONST: dst = consts[a]).  The step is x + (A_1 dZ_1 + A_2 dZ_2)
+ * with the terms in the order of the SDE function's returned dict (sdepy's
+ * euler_next, sdepy/integration.py:707-718), dZ = dt or dw. */
+#define SDE_USER_MAX_OPS    64
+#define SDE_USER_MAX_CONSTS 16
+#define SDE_USER_MAX_REGS   48
+#define SDE_SRC_DT 0
+#define SDE_SRC_DW 1
+enum {
+    SDE_UOP_CONST = 0, SDE_UOP_ADD, SDE_UOP_SUB, SDE_UOP_MUL, SDE_UOP_DIV, SDE_UOP_NEG,
+    SDE_UOP_ABS, SDE_UOP_EXP, SDE_UOP_LOG, SDE_UOP_SQRT, SDE_UOP_MAX, SDE_UOP_MIN,
+    SDE_UOP_SIN, SDE_UOP_COS, SDE_UOP_TAN, SDE_UOP_TANH, SDE_UOP_POW, SDE_UOP_EXPM1,
+    SDE_UOP_LOG1P, SDE_UOP_ARCTAN, SDE_UOP_COPY, SDE_UOP_COUNT
+};
+typedef struct SdeUserProgram {
+    int32_t n_ops;
+    int32_t n_terms;                  /* terms of the Euler sum, 0..2            */
+    int32_t term_source[2];           /* SDE_SRC_DT | SDE_SRC_DW, in dict order   */
+    int32_t term_register[2];         /* register holding each term's coefficient */
+    uint32_t ops[SDE_USER_MAX_OPS];
+    double consts[SDE_USER_MAX_CONSTS];
+} SdeUserProgram;
 
 /* jump-size law of the compound Poisson source (LINEAR model only) */
 #define SDE_JUMP_NONE        0
@@ -107,6 +138,7 @@ typedef struct SdeSpec {
     uint64_t seed;         /* Philox-4x32-10 key */
     uint32_t stream;       /* Philox counter word 3 (call / instance id) */
     uint32_t reserved1;
+    const SdeUserProgram *program;   /* SDE_MODEL_USER: the coefficients, else NULL */
 } SdeSpec;
 
 typedef struct SdeGrid {

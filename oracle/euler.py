@@ -172,13 +172,22 @@ def shapes(preset, vshape, factors=1):
 
 def integrate(preset, params=None, timeline=(0., 1.), *, paths=1, vshape=(),
               steps=None, i0=0, dtype=None, corr=None, dw=None, dj=None,
-              rng=None, getinfo=True):
-    """Integrate one preset.  ``dw`` / ``dj`` are source-protocol objects
-    (e.g. Replay of recorded increments); when None they are realised with
-    numpy from ``rng`` as sdepy's default sources do.  Returns (result,
-    info) where result is an array or a tuple of arrays (full Heston)."""
-    assert preset in PRESETS, preset
-    p = dict(DEFAULTS[preset])
+              rng=None, getinfo=True, sde=None, log_flag=False):
+    """Integrate one preset, or (preset 'user') the SDE function ``sde(t,
+    x, **params)`` of sdepy's integrate decorator, in log space when
+    ``log_flag`` (sdepy/integration.py:1154-1197, 1843-1955).  ``dw`` /
+    ``dj`` are source-protocol objects (e.g. Replay of recorded
+    increments); when None they are realised with numpy from ``rng`` as
+    sdepy's default sources do.  Returns (result, info) where result is an
+    array or a tuple of arrays (full Heston)."""
+    user = preset == 'user'
+    assert user or preset in PRESETS, preset
+    if user:
+        import inspect
+        p = {'x0': 1.}
+        p.update({k: v.default for k, v in list(inspect.signature(sde).parameters.items())[2:]})
+    else:
+        p = dict(DEFAULTS[preset])
     p.update(params or {})
     # callables (and processes) are time-dependent parameters, evaluated at
     # the start of each step as sdepy's SDE.A does (integration.py:1216-1225)
@@ -188,7 +197,7 @@ def integrate(preset, params=None, timeline=(0., 1.), *, paths=1, vshape=(),
     dtype = float if dtype is None else dtype
     jumps = 'jumpdiff' in preset
     heston = 'heston' in preset
-    log = preset in ('lognorm_process',) or jumps
+    log = preset in ('lognorm_process',) or jumps or (user and log_flag)
     P0 = P
     if dw is None:
         dw = NumpyWiener(rng, paths, wshape, corr=corr, dtype=dtype)
@@ -206,8 +215,12 @@ def integrate(preset, params=None, timeline=(0., 1.), *, paths=1, vshape=(),
         i = np.index_exp[..., np.newaxis, :] if addaxis else np.index_exp[...]
         return np.concatenate(tuple(np.broadcast_to(x, target)[i] for x in xs), axis=-2)
 
+    user_sde = sde
+
     def sde(s, x):
         P = {k: (np.asarray(v(s)) if callable(v) else v) for k, v in P0.items()}
+        if user:   # the function's own coefficients, its dict order kept
+            return user_sde(s, x, **{k: v for k, v in P.items() if k != 'x0'})
         if preset == 'wiener_process':
             return {'dt': P['mu'], 'dw': P['sigma']}
         if preset == 'lognorm_process':

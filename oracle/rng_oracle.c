@@ -94,6 +94,53 @@ int oracle_cholesky(const double *C, int M, double *L) {
     return 0;
 }
 
+/* A user SDE's coefficients (SdeUserProgram): the program evaluated in FP64
+ * with C's operators and libm, numpy's maximum / minimum (NaN-propagating). */
+static double np_maxd(double a, double b) { return (a != a) ? a : (b != b) ? b : (a >= b ? a : b); }
+static double np_mind(double a, double b) { return (a != a) ? a : (b != b) ? b : (a <= b ? a : b); }
+
+static void user_coefs(const SdeUserProgram *u, double x, double t, const double *p, double out[2]) {
+    double r[SDE_USER_MAX_REGS] = {0};
+    r[0] = x;
+    r[1] = t;
+    for (int i = 0; i < 6; ++i) r[2 + i] = p[i];
+    for (int i = 0; i < u->n_ops; ++i) {
+        const uint32_t op = u->ops[i];
+        const int c = op & 0xff, d = (op >> 8) & 0xff, ia = (op >> 16) & 0xff, ib = op >> 24;
+        if (c == SDE_UOP_CONST) {
+            r[d] = u->consts[ia];
+            continue;
+        }
+        const double va = r[ia], vb = r[ib];
+        double v;
+        switch (c) {
+        case SDE_UOP_ADD: v = va + vb; break;
+        case SDE_UOP_SUB: v = va - vb; break;
+        case SDE_UOP_MUL: v = va * vb; break;
+        case SDE_UOP_DIV: v = va / vb; break;
+        case SDE_UOP_NEG: v = -va; break;
+        case SDE_UOP_ABS: v = fabs(va); break;
+        case SDE_UOP_EXP: v = exp(va); break;
+        case SDE_UOP_LOG: v = log(va); break;
+        case SDE_UOP_SQRT: v = sqrt(va); break;
+        case SDE_UOP_MAX: v = np_maxd(va, vb); break;
+        case SDE_UOP_MIN: v = np_mind(va, vb); break;
+        case SDE_UOP_SIN: v = sin(va); break;
+        case SDE_UOP_COS: v = cos(va); break;
+        case SDE_UOP_TAN: v = tan(va); break;
+        case SDE_UOP_TANH: v = tanh(va); break;
+        case SDE_UOP_POW: v = pow(va, vb); break;
+        case SDE_UOP_EXPM1: v = expm1(va); break;
+        case SDE_UOP_LOG1P: v = log1p(va); break;
+        case SDE_UOP_ARCTAN: v = atan(va); break;
+        default: v = va;
+        }
+        r[d] = v;
+    }
+    out[0] = u->n_terms > 0 ? r[u->term_register[0]] : 0.0;
+    out[1] = u->n_terms > 1 ? r[u->term_register[1]] : 0.0;
+}
+
 static double jump_size(int law, const uint32_t r[4], double a, double b, double pa) {
     double z0, z1;
     switch (law) {
@@ -260,6 +307,19 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
                             const int w = gi * M + m;
                             const double drift = pp[0 * W + w] * (pp[1 * W + w] - st[m]);
                             st[m] = st[m] + (drift * dt + pp[2 * W + w] * dW[m]);
+                        }
+                    } else if (s->model == SDE_MODEL_USER) {   /* sdepy/integration.py:707-718 */
+                        for (int m = 0; m < M; ++m) {
+                            const int w = gi * M + m;
+                            double pv[6], A[2];
+                            for (int i = 0; i < 6; ++i) pv[i] = pp[i * W + w];
+                            user_coefs(s->program, st[m], g->tt[k], pv, A);
+                            double sum = 0.0;
+                            for (int i = 0; i < s->program->n_terms; ++i) {
+                                const double term = A[i] * (s->program->term_source[i] == SDE_SRC_DT ? dt : dW[m]);
+                                sum = i == 0 ? term : sum + term;
+                            }
+                            st[m] = st[m] + sum;
                         }
                     } else if (s->model == SDE_MODEL_CIR) {   /* sdepy/integration.py:2350-2354 */
                         for (int m = 0; m < M; ++m) {

@@ -13,6 +13,7 @@ from .integration import (
     hull_white_process, hull_white_1factor_process, full_heston_process,
     heston_process, jumpdiff_process, merton_jumpdiff_process,
     kou_jumpdiff_process, cox_ingersoll_ross_process)
+from .usersde import integrate
 from . import infrastructure
 from .montecarlo import montecarlo   # the class, as sdepy exports it
 
@@ -26,5 +27,5 @@ __all__ = [
     'hull_white_process', 'hull_white_1factor_process',
     'full_heston_process', 'heston_process', 'jumpdiff_process',
     'merton_jumpdiff_process', 'kou_jumpdiff_process',
-    'cox_ingersoll_ross_process', 'montecarlo',
+    'cox_ingersoll_ross_process', 'integrate', 'montecarlo',
 ]

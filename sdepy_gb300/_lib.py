@@ -21,7 +21,13 @@ MAX_STRIKES = 8
 OK, ERR_INVALID, ERR_UNSUPPORTED, ERR_CUDA, ERR_DEVICE, ERR_NO_DEVICE = \
     0, -1, -2, -3, -4, -5
 
-MODEL_LINEAR, MODEL_OU, MODEL_HESTON, MODEL_CIR = 0, 1, 2, 3
+MODEL_LINEAR, MODEL_OU, MODEL_HESTON, MODEL_CIR, MODEL_USER = 0, 1, 2, 3, 4
+# user SDE programs (SdeUserProgram)
+USER_MAX_OPS, USER_MAX_CONSTS, USER_MAX_REGS = 64, 16, 48
+SRC_DT, SRC_DW = 0, 1
+(UOP_CONST, UOP_ADD, UOP_SUB, UOP_MUL, UOP_DIV, UOP_NEG, UOP_ABS, UOP_EXP, UOP_LOG, UOP_SQRT,
+ UOP_MAX, UOP_MIN, UOP_SIN, UOP_COS, UOP_TAN, UOP_TANH, UOP_POW, UOP_EXPM1, UOP_LOG1P,
+ UOP_ARCTAN, UOP_COPY) = range(21)
 JUMP_NONE, JUMP_NORM, JUMP_DOUBLE_EXP, JUMP_UNIFORM, JUMP_EXP = 0, 1, 2, 3, 4
 FP64, FP32 = 0, 1
 OUT_STATE, OUT_EXP, OUT_SUM, OUT_HESTON_X, OUT_HESTON_XY = 0, 1, 2, 3, 4
@@ -32,6 +38,12 @@ _ip = C.POINTER(C.c_int32)
 _lp = C.POINTER(C.c_int64)
 
 
+class SdeUserProgram(C.Structure):
+    _fields_ = [('n_ops', C.c_int32), ('n_terms', C.c_int32),
+                ('term_source', C.c_int32*2), ('term_register', C.c_int32*2),
+                ('ops', C.c_uint32*64), ('consts', C.c_double*16)]
+
+
 class SdeSpec(C.Structure):
     _fields_ = [('abi_version', C.c_int32), ('model', C.c_int32),
                 ('precision', C.c_int32), ('jump_law', C.c_int32),
@@ -40,7 +52,7 @@ class SdeSpec(C.Structure):
                 ('flags', C.c_int32),
                 ('x0', _dp), ('params', _dp), ('corr', _dp),
                 ('seed', C.c_uint64), ('stream', C.c_uint32),
-                ('reserved1', C.c_uint32)]
+                ('reserved1', C.c_uint32), ('program', C.POINTER(SdeUserProgram))]
 
 
 class SdeGrid(C.Structure):

@@ -277,8 +277,31 @@ static int check_spec(const SdeSpec *s, int *opg) {
     if (!s) return fail(SDE_ERR_INVALID, "spec is NULL");
     if (s->abi_version != SDE_ABI_VERSION)
         return fail(SDE_ERR_INVALID, "spec abi_version %d != %d", s->abi_version, SDE_ABI_VERSION);
-    if (s->model < SDE_MODEL_LINEAR || s->model > SDE_MODEL_CIR)
+    if (s->model < SDE_MODEL_LINEAR || s->model > SDE_MODEL_USER)
         return fail(SDE_ERR_UNSUPPORTED, "unknown model %d", s->model);
+    if (s->model == SDE_MODEL_USER) {
+        // every register and constant index in range before a launch
+        const SdeUserProgram *u = s->program;
+        if (!u) return fail(SDE_ERR_INVALID, "a user SDE needs its program");
+        if (u->n_ops < 0 || u->n_ops > SDE_USER_MAX_OPS) return fail(SDE_ERR_INVALID, "user program: n_ops");
+        if (u->n_terms < 0 || u->n_terms > 2) return fail(SDE_ERR_INVALID, "user program: n_terms");
+        for (int i = 0; i < u->n_terms; ++i)
+            if ((u->term_source[i] != SDE_SRC_DT && u->term_source[i] != SDE_SRC_DW) || u->term_register[i] < 0 ||
+                u->term_register[i] >= SDE_USER_MAX_REGS)
+                return fail(SDE_ERR_INVALID, "user program: term %d", i);
+        for (int i = 0; i < u->n_ops; ++i) {
+            const uint32_t op = u->ops[i];
+            const uint32_t code = op & 0xff, d = (op >> 8) & 0xff, ra = (op >> 16) & 0xff, rb = op >> 24;
+            if (code >= SDE_UOP_COUNT || d >= SDE_USER_MAX_REGS)
+                return fail(SDE_ERR_INVALID, "user program: instruction %d", i);
+            if (code == SDE_UOP_CONST ? ra >= SDE_USER_MAX_CONSTS : (ra >= SDE_USER_MAX_REGS || rb >= SDE_USER_MAX_REGS))
+                return fail(SDE_ERR_INVALID, "user program: operand of instruction %d", i);
+        }
+        if (s->jump_law != SDE_JUMP_NONE) return fail(SDE_ERR_UNSUPPORTED, "user SDEs with jumps");
+        if (s->out_mode != SDE_OUT_STATE && s->out_mode != SDE_OUT_EXP)
+            return fail(SDE_ERR_INVALID, "user SDEs store the state or its exp");
+        if (s->flags & SDE_FLAG_ANTITHETIC) return fail(SDE_ERR_UNSUPPORTED, "antithetic paths of user SDEs");
+    }
     if (s->precision != SDE_FP64 && s->precision != SDE_FP32)
         return fail(SDE_ERR_UNSUPPORTED, "unknown precision %d", s->precision);
     if (s->paths < 1 || s->paths > 0x7fffffffLL)
@@ -339,6 +362,7 @@ static int maxm_of(int M) {
 template <typename R> struct Finder;
 template <> struct Finder<double> {
     static FwdLauncher<double> find(int model, int maxm, bool inj, bool jmp, int *bps) {
+        if (model == SDE_MODEL_USER) return jmp ? nullptr : find_fwd_f64_user(maxm, inj, bps);
         if (model == SDE_MODEL_CIR) return jmp ? nullptr : find_fwd_f64_cir(maxm, inj, false, bps);
         FwdLauncher<double> f = find_fwd_f64_linear(model, maxm, inj, jmp, bps);
         return f ? f : find_fwd_f64_ou_heston(model, maxm, inj, jmp, bps);
@@ -351,6 +375,7 @@ template <> struct Finder<double> {
 };
 template <> struct Finder<float> {
     static FwdLauncher<float> find(int model, int maxm, bool inj, bool jmp, int *bps) {
+        if (model == SDE_MODEL_USER) return jmp ? nullptr : find_fwd_f32_user(maxm, inj, bps);
         if (model == SDE_MODEL_CIR) return jmp ? nullptr : find_fwd_f32_cir(maxm, inj, false, false, bps);
         FwdLauncher<float> f = find_fwd_f32_linear(model, maxm, inj, jmp, bps);
         return f ? f : find_fwd_f32_ou_heston(model, maxm, inj, jmp, bps);
@@ -530,11 +555,15 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     const size_t o_ctab = o_runs + al(sizeof(int4) * (runs.size() + 1));
     const size_t o_tsh = o_ctab + al(sizeof(float) * (ctab.size() + 4));
     // the other kernels read time-dependent coefficients (slots 0..2) per step
-    const size_t nprmt = (ptab && !tab) ? (size_t)n_steps * 3 * W : 0;
+    const bool user = s->model == SDE_MODEL_USER;
+    const int npt = user ? SDE_MAX_PARAMS : 3;   // parameter slots per table row
+    const size_t nprmt = (ptab && !tab) ? (size_t)n_steps * npt * W : 0;
     const size_t o_prmt = o_tsh + al(sizeof(float) * (tshift.size() + 4));
     const size_t nchol = corr_steps ? (size_t)n_steps * NCHOL : 0;
     const size_t o_cholt = o_prmt + al(sizeof(R) * (nprmt + 1));
-    const size_t o_end = o_cholt + al(sizeof(R) * (nchol + 1));
+    const size_t ntk = user ? (size_t)n_steps : 0;   // step starts, for user SDEs
+    const size_t o_tk = o_cholt + al(sizeof(R) * (nchol + 1));
+    const size_t o_end = o_tk + al(sizeof(R) * (ntk + 1));
     D->host_tables.resize(o_end);
     char *H = D->host_tables.data();
     R *h_dt = (R *)(H + o_dt), *h_sq = (R *)(H + o_sq), *h_x0 = (R *)(H + o_x0), *h_prm = (R *)(H + o_prm);
@@ -583,8 +612,12 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     if (nprmt) {
         R *h_prmt = (R *)(H + o_prmt);
         for (int k = 0; k < n_steps; ++k)
-            for (int v = 0; v < 3; ++v)
-                for (int w = 0; w < W; ++w) h_prmt[((size_t)k * 3 + v) * W + w] = (R)params_of(k)[v * W + w];
+            for (int v = 0; v < npt; ++v)
+                for (int w = 0; w < W; ++w) h_prmt[((size_t)k * npt + v) * W + w] = (R)params_of(k)[v * W + w];
+    }
+    if (ntk) {
+        R *h_tk = (R *)(H + o_tk);
+        for (int k = 0; k < n_steps; ++k) h_tk[k] = (R)gr->tt[k];
     }
     if (nchol) {
         R *h_cholt = (R *)(H + o_cholt);
@@ -649,6 +682,8 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     a.prm_t = nprmt ? (const R *)(T + o_prmt) : nullptr;
     a.chol_t = nchol ? (const R *)(T + o_cholt) : nullptr;
     if (nchol) a.has_corr = 1;
+    a.tk = ntk ? (const R *)(T + o_tk) : nullptr;
+    if (user) a.uprog = *s->program;
     a.key = philox_schedule(s->seed);
     a.n_out_vars = n_out;
 
@@ -740,7 +775,9 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     const bool tdep_k = ou_b || (sizeof(R) == 4 && !inject && !anti &&
                                  ((nprmt && (s->model == SDE_MODEL_HESTON || s->model == SDE_MODEL_CIR)) ||
                                   corr_steps));
-    FwdLauncher<R> L = anti     ? Finder<R>::find_anti(s->model, maxm_of(M), jumps, &bps)
+    // (user-SDE kernels reload per-step parameters and factors in every form)
+    FwdLauncher<R> L = user     ? Finder<R>::find(s->model, maxm_of(M), inject, jumps, &bps)
+                       : anti   ? Finder<R>::find_anti(s->model, maxm_of(M), jumps, &bps)
                        : tdep_k ? Finder<R>::find_tdep(s->model, maxm_of(M), &bps)
                                 : Finder<R>::find(s->model, maxm_of(M), inject, jumps, &bps);
     if (!L) return fail(SDE_ERR_UNSUPPORTED, "no kernel for model %d group size %d", s->model, M);

@@ -70,6 +70,9 @@ struct FwdArgs {
     // each step's correlation matrix (rows as chol below), or NULL; read
     // only by the kernels that reload per-step coefficients (STEPCORR)
     const R *chol_t;
+    // SDE_MODEL_USER: the coefficient program, and each step's start time
+    SdeUserProgram uprog;
+    const R *tk;
     // and the grid as runs of steps sharing one coefficient row:
     // (first step, end step, output row stored after the run or -1, coef row)
     const int4 *runs;
@@ -578,6 +581,93 @@ __device__ __forceinline__ void jump_size_grad(int law, uint4 r, R ja, R jb, R j
 }
 
 // ---------------------------------------------------------------------------
+// user SDEs: the coefficient program (SdeUserProgram), interpreted per state
+// variable and step.  Every thread runs the same instruction sequence (no
+// divergence); the register file lives in local memory (L1).  Register and
+// constant indices are checked on the host before launch.  FP64 arithmetic
+// is explicitly rounded (no contraction), so that the sequence of roundings
+// is numpy's; the elementary functions are CUDA's.
+// ---------------------------------------------------------------------------
+template <typename R> struct UFn;
+template <> struct UFn<double> {
+    __device__ static double exp_(double x) { return exp(x); }
+    __device__ static double log_(double x) { return log(x); }
+    __device__ static double sin_(double x) { return sin(x); }
+    __device__ static double cos_(double x) { return cos(x); }
+    __device__ static double tan_(double x) { return tan(x); }
+    __device__ static double tanh_(double x) { return tanh(x); }
+    __device__ static double pow_(double x, double y) { return pow(x, y); }
+    __device__ static double expm1_(double x) { return expm1(x); }
+    __device__ static double log1p_(double x) { return log1p(x); }
+    __device__ static double atan_(double x) { return atan(x); }
+};
+template <> struct UFn<float> {
+    __device__ static float exp_(float x) { return expf(x); }
+    __device__ static float log_(float x) { return logf(x); }
+    __device__ static float sin_(float x) { return sinf(x); }
+    __device__ static float cos_(float x) { return cosf(x); }
+    __device__ static float tan_(float x) { return tanf(x); }
+    __device__ static float tanh_(float x) { return tanhf(x); }
+    __device__ static float pow_(float x, float y) { return powf(x, y); }
+    __device__ static float expm1_(float x) { return expm1f(x); }
+    __device__ static float log1p_(float x) { return log1pf(x); }
+    __device__ static float atan_(float x) { return atanf(x); }
+};
+
+// numpy's maximum / minimum: NaN if either operand is NaN
+template <typename R>
+__device__ __forceinline__ R np_max(R a, R b) { return (a != a) ? a : (b != b) ? b : (a >= b ? a : b); }
+template <typename R>
+__device__ __forceinline__ R np_min(R a, R b) { return (a != a) ? a : (b != b) ? b : (a <= b ? a : b); }
+
+template <typename R>
+__device__ __noinline__ void user_coefs(const SdeUserProgram &u, R x, R t, const R (&p)[6], R (&out)[2]) {
+    typedef Ar<R> A;
+    typedef UFn<R> F;
+    R r[SDE_USER_MAX_REGS];
+    r[0] = x;
+    r[1] = t;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) r[2 + i] = p[i];
+    for (int i = 0; i < u.n_ops; ++i) {
+        const uint32_t op = u.ops[i];
+        const int d = (op >> 8) & 0xff, ia = (op >> 16) & 0xff, ib = op >> 24;
+        const int code = op & 0xff;
+        if (code == SDE_UOP_CONST) {
+            r[d] = (R)u.consts[ia];
+            continue;
+        }
+        const R va = r[ia], vb = r[ib];
+        R v;
+        switch (code) {
+        case SDE_UOP_ADD: v = A::add(va, vb); break;
+        case SDE_UOP_SUB: v = A::sub(va, vb); break;
+        case SDE_UOP_MUL: v = A::mul(va, vb); break;
+        case SDE_UOP_DIV: v = va / vb; break;   // IEEE division, correctly rounded
+        case SDE_UOP_NEG: v = -va; break;
+        case SDE_UOP_ABS: v = fabs(va); break;
+        case SDE_UOP_EXP: v = F::exp_(va); break;
+        case SDE_UOP_LOG: v = F::log_(va); break;
+        case SDE_UOP_SQRT: v = A::sqrt_(va); break;
+        case SDE_UOP_MAX: v = np_max(va, vb); break;
+        case SDE_UOP_MIN: v = np_min(va, vb); break;
+        case SDE_UOP_SIN: v = F::sin_(va); break;
+        case SDE_UOP_COS: v = F::cos_(va); break;
+        case SDE_UOP_TAN: v = F::tan_(va); break;
+        case SDE_UOP_TANH: v = F::tanh_(va); break;
+        case SDE_UOP_POW: v = F::pow_(va, vb); break;
+        case SDE_UOP_EXPM1: v = F::expm1_(va); break;
+        case SDE_UOP_LOG1P: v = F::log1p_(va); break;
+        case SDE_UOP_ARCTAN: v = F::atan_(va); break;
+        default: v = va; break;   // SDE_UOP_COPY
+        }
+        r[d] = v;
+    }
+    out[0] = u.n_terms > 0 ? r[u.term_register[0]] : R(0);
+    out[1] = u.n_terms > 1 ? r[u.term_register[1]] : R(0);
+}
+
+// ---------------------------------------------------------------------------
 // the forward kernel
 // ---------------------------------------------------------------------------
 // FP32 device-RNG kernels without jumps, up to 8 states per thread (4 for
@@ -587,7 +677,8 @@ __device__ __forceinline__ void jump_size_grad(int law, uint4 r, R ja, R jb, R j
 template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS, bool ANTI = false>
 struct FwdOccupancy {
     static constexpr int CAP_M = (MODEL == SDE_MODEL_HESTON || MODEL == SDE_MODEL_CIR ? 4 : 8) / (ANTI ? 2 : 1);
-    static constexpr int MIN_BLOCKS = (sizeof(R) == 4 && MAXM <= CAP_M && !INJECT && !JUMPS) ? 3 : 1;
+    static constexpr int MIN_BLOCKS =
+        (sizeof(R) == 4 && MAXM <= CAP_M && !INJECT && !JUMPS && MODEL != SDE_MODEL_USER) ? 3 : 1;
 };
 
 // TDEP: time-dependent-coefficient instantiations of the FP32 device-noise
@@ -610,10 +701,13 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     constexpr bool TDB = TDEP && SHIFT;   // OU rows with the time-dependent-theta term
     // per-step coefficient reloads compiled in (the non-table kernels but
     // the common FP32 Heston and CIR ones)
-    constexpr bool RELOAD = !TAB && (sizeof(R) == 8 || INJECT || ANTI || TDEP);
+    constexpr bool USER = MODEL == SDE_MODEL_USER;
+    constexpr bool RELOAD = !TAB && (sizeof(R) == 8 || INJECT || ANTI || TDEP || USER);
     // per-step correlation factors compiled in (the same kernels, TAB ones
     // included, with device noise)
-    constexpr bool STEPCORR = !INJECT && (sizeof(R) == 8 || ANTI || TDEP);
+    constexpr bool STEPCORR = !INJECT && (sizeof(R) == 8 || ANTI || TDEP || USER);
+    // parameter slots of a time-dependent table row (all six for USER)
+    constexpr int NPT = USER ? 6 : 3;
     __shared__ R red[BLOCK / 32];
     __shared__ double part[MAXM][NPART];
     __shared__ R svs[NA][MAXM][BLOCK];   // this round's value of each output at the stats row
@@ -878,15 +972,21 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                     // time-dependent coefficients of step k (uniform test; not
                     // compiled into the FP32 Heston kernels' common form)
                     if (RELOAD && a.prm_t) {
-                        const R *pk = a.prm_t + (int64_t)k * 3 * W;
+                        const R *pk = a.prm_t + (int64_t)k * NPT * W;
 #pragma unroll
                         for (int m = 0; m < MAXM; ++m) {
                             const int w = g * M + (m < M ? m : 0);
                             c0[m] = __ldg(pk + w);
                             c1[m] = __ldg(pk + W + w);
                             c2[m] = __ldg(pk + 2 * W + w);
+                            if constexpr (USER) {
+                                c3[m] = __ldg(pk + 3 * W + w);
+                                c4[m] = __ldg(pk + 4 * W + w);
+                                c5[m] = __ldg(pk + 5 * W + w);
+                            }
                         }
                     }
+                    const R tk = USER ? a.tk[k] : R(0);   // the step's start (user SDEs)
                     R dW[MAXM], dJ[MAXM];
                     draw(k, sq, dW, dJ);
                     // ---- Euler step, sdepy's operation order ----------------------
@@ -903,6 +1003,22 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                         for (int m = 0; m < MAXM; ++m) {
                             const R drift = A::mul(c0[m], A::sub(c1[m], st[m]));
                             st[m] = A::add(st[m], A::add(A::mul(drift, dt), A::mul(c2[m], dW[m])));
+                        }
+                    } else if (MODEL == SDE_MODEL_USER) {
+                        // x + (A_1 dZ_1 + A_2 dZ_2), the terms in the order of the
+                        // SDE function's dict (sdepy sums from 0: 0 + v == v)
+#pragma unroll
+                        for (int m = 0; m < MAXM; ++m) {
+                            const R pv[6] = {c0[m], c1[m], c2[m], c3[m], c4[m], c5[m]};
+                            R A2[2];
+                            user_coefs<R>(a.uprog, st[m], tk, pv, A2);
+                            R s = R(0);
+                            for (int i = 0; i < a.uprog.n_terms; ++i) {
+                                const R dz = a.uprog.term_source[i] == SDE_SRC_DT ? dt : dW[m];
+                                const R term = A::mul(A2[i], dz);
+                                s = i == 0 ? term : A::add(s, term);
+                            }
+                            st[m] = A::add(st[m], s);
                         }
                     } else if (MODEL == SDE_MODEL_CIR) {   // k*(theta - x+), xi*sqrt(x+)
 #pragma unroll
@@ -1048,6 +1164,9 @@ FwdLauncher<float> find_fwd_f32_tdep(int model, int maxm, int *bps);
 // CIR kernels (fwd_cir.cu): plain, time-dependent (FP32), antithetic
 FwdLauncher<float> find_fwd_f32_cir(int maxm, bool inject, bool tdep, bool anti, int *bps);
 FwdLauncher<double> find_fwd_f64_cir(int maxm, bool inject, bool anti, int *bps);
+// user-SDE kernels (fwd_user.cu): device or injected noise
+FwdLauncher<float> find_fwd_f32_user(int maxm, bool inject, int *bps);
+FwdLauncher<double> find_fwd_f64_user(int maxm, bool inject, int *bps);
 // antithetic kernels (device noise, groups of up to 8 states)
 FwdLauncher<float> find_fwd_f32_anti(int model, int maxm, bool jumps, int *bps);
 FwdLauncher<double> find_fwd_f64_anti(int model, int maxm, bool jumps, int *bps);

@@ -1,0 +1,309 @@
+"""User SDEs on the GPU: sdepy's ``integrate`` decorator
+(sdepy/integration.py:1843-1955).
+
+``@integrate`` turns a function ``sde(t, x, **params)`` returning the
+coefficients ``{'dt': A_dt, 'dw': A_dw}`` of one Ito SDE into a process
+class, as sdepy does.  Here the function is traced once, at decoration, with
+symbolic values for t, x and the parameters: every arithmetic operation and
+numpy ufunc it applies is recorded, in Python's evaluation order, into a
+straight-line program (``SdeUserProgram`` of include/sdepy_gb300.h) that the
+device evaluates per state variable and step.  The Euler step then adds the
+terms in the order of the returned dict, as sdepy's ``euler_next`` does
+(sdepy/integration.py:707-718), so the FP64 result follows numpy's sequence
+of roundings.
+
+Supported (no CPU fallback -- anything else raises NotImplementedError at
+decoration): one equation driven by 'dt' and / or 'dw'; up to 6 parameters,
+constant or functions / processes of t, per state variable; +, -, *, /,
+unary -, abs, ** (numpy's fast forms for the exponents 2, 0.5, -1, 1, 0),
+and numpy's exp, log, sqrt, maximum, minimum, sin, cos, tan, tanh, power,
+expm1, log1p, arctan, square, absolute, negative; correlated Wiener
+increments through ``corr`` / ``rho``; the ``log`` flag.  Control flow on the
+state (``if x > 0``, Python's ``max``), systems of SDEs (q > 0) and other
+sources (jumps) are refused.
+"""
+import ctypes as C
+import inspect
+import numbers
+
+import numpy as np
+
+from . import _lib
+from .integration import _const, _gpu_process, _per_var
+
+_MAX_PARAMS = 6
+
+
+class _Program:
+    """The straight-line program being recorded: r0 = x, r1 = t, r2..r7 =
+    parameters, then one register per recorded operation."""
+
+    def __init__(self):
+        self.ops = []
+        self.consts = []
+        self.nreg = 8
+
+    def _new(self):
+        if self.nreg >= _lib.USER_MAX_REGS:
+            raise NotImplementedError('the SDE function needs more than {} intermediate values'
+                                      .format(_lib.USER_MAX_REGS - 8))
+        d = self.nreg
+        self.nreg += 1
+        return d
+
+    def emit(self, code, a, b=0):
+        if len(self.ops) >= _lib.USER_MAX_OPS:
+            raise NotImplementedError('the SDE function needs more than {} operations'
+                                      .format(_lib.USER_MAX_OPS))
+        d = self._new()
+        self.ops.append(code | d << 8 | a << 16 | b << 24)
+        return _Sym(self, d)
+
+    def const(self, v):
+        v = float(v)
+        key = np.float64(v).tobytes()
+        for i, c in enumerate(self.consts):
+            if np.float64(c).tobytes() == key:
+                return self.emit(_lib.UOP_CONST, i)
+        if len(self.consts) >= _lib.USER_MAX_CONSTS:
+            raise NotImplementedError('the SDE function uses more than {} constants'
+                                      .format(_lib.USER_MAX_CONSTS))
+        self.consts.append(v)
+        return self.emit(_lib.UOP_CONST, len(self.consts) - 1)
+
+
+def _is_number(v):
+    return isinstance(v, numbers.Real) or (isinstance(v, np.ndarray) and v.ndim == 0 and
+                                           v.dtype.kind in 'fiub')
+
+
+_UFUNCS = {
+    np.exp: 'EXP', np.log: 'LOG', np.sqrt: 'SQRT', np.sin: 'SIN', np.cos: 'COS', np.tan: 'TAN',
+    np.tanh: 'TANH', np.expm1: 'EXPM1', np.log1p: 'LOG1P', np.arctan: 'ARCTAN',
+    np.absolute: 'ABS', np.fabs: 'ABS', np.negative: 'NEG',
+    np.add: 'ADD', np.subtract: 'SUB', np.multiply: 'MUL', np.true_divide: 'DIV',
+    np.maximum: 'MAX', np.minimum: 'MIN', np.power: 'POW',
+}
+
+
+class _Sym:
+    """A value of the traced SDE function: a register of the program."""
+    __array_priority__ = 1000
+
+    def __init__(self, prog, reg):
+        self.prog, self.reg = prog, reg
+
+    def _reg(self, v):
+        if isinstance(v, _Sym):
+            return v.reg
+        if _is_number(v):
+            return self.prog.const(v).reg
+        raise NotImplementedError(
+            'the GPU compiler of SDE functions takes numbers and traced values, not {!r}'.format(v))
+
+    def _bin(self, code, a, b):
+        return self.prog.emit(getattr(_lib, 'UOP_' + code), self._reg(a), self._reg(b))
+
+    def __add__(self, o):
+        return self._bin('ADD', self, o)
+
+    def __radd__(self, o):
+        return self._bin('ADD', o, self)
+
+    def __sub__(self, o):
+        return self._bin('SUB', self, o)
+
+    def __rsub__(self, o):
+        return self._bin('SUB', o, self)
+
+    def __mul__(self, o):
+        return self._bin('MUL', self, o)
+
+    def __rmul__(self, o):
+        return self._bin('MUL', o, self)
+
+    def __truediv__(self, o):
+        return self._bin('DIV', self, o)
+
+    def __rtruediv__(self, o):
+        return self._bin('DIV', o, self)
+
+    def __neg__(self):
+        return self.prog.emit(_lib.UOP_NEG, self.reg)
+
+    def __pos__(self):
+        return self
+
+    def __abs__(self):
+        return self.prog.emit(_lib.UOP_ABS, self.reg)
+
+    def __pow__(self, o):
+        # numpy's ** on arrays: exact forms for these scalar exponents
+        if _is_number(o):
+            e = float(o)
+            if e == 2:
+                return self._bin('MUL', self, self)
+            if e == 0.5:
+                return self.prog.emit(_lib.UOP_SQRT, self.reg)
+            if e == -1:
+                return self._bin('DIV', 1., self)
+            if e == 1:
+                return self.prog.emit(_lib.UOP_COPY, self.reg)
+            if e == 0:
+                return self.prog.const(1.)
+        return self._bin('POW', self, o)
+
+    def __rpow__(self, o):
+        return self._bin('POW', o, self)
+
+    def __array_ufunc__(self, ufunc, method, *inputs, **kwargs):
+        if method != '__call__' or kwargs:
+            return NotImplemented
+        if ufunc is np.square:
+            return self._bin('MUL', inputs[0], inputs[0])
+        if ufunc is np.positive:
+            return inputs[0] if isinstance(inputs[0], _Sym) else self.prog.const(inputs[0])
+        name = _UFUNCS.get(ufunc)
+        if name is None:
+            raise NotImplementedError('numpy.{} is not supported by the GPU compiler of SDE '
+                                      'functions'.format(ufunc.__name__))
+        if ufunc.nin == 1:
+            return self.prog.emit(getattr(_lib, 'UOP_' + name), self._reg(inputs[0]))
+        return self._bin(name, inputs[0], inputs[1])
+
+    def _refuse(self, *args):
+        raise NotImplementedError(
+            'the SDE function branches on a traced value (comparison, bool, int or float of '
+            'x, t or a parameter): not supported by the GPU compiler of SDE functions')
+
+    __bool__ = __float__ = __int__ = __index__ = _refuse
+    __lt__ = __le__ = __gt__ = __ge__ = __eq__ = __ne__ = _refuse
+    __hash__ = object.__hash__
+
+
+def compile_sde(f, pnames):
+    """SdeUserProgram of ``f(t, x, **params)`` with parameters ``pnames``
+    (registers r2...), and the recorded program for inspection."""
+    prog = _Program()
+    x, t = _Sym(prog, 0), _Sym(prog, 1)
+    params = {n: _Sym(prog, 2 + i) for i, n in enumerate(pnames)}
+    try:
+        A = f(t, x, **params)
+    except NotImplementedError:
+        raise
+    except Exception as e:
+        raise NotImplementedError('the SDE function {!r} cannot be traced for the GPU: {}: {}'
+                                  .format(getattr(f, '__name__', f), type(e).__name__, e))
+    if not isinstance(A, dict):
+        raise NotImplementedError('the SDE function must return a dict of coefficients')
+    srcs = {'dt': _lib.SRC_DT, 'dw': _lib.SRC_DW}
+    terms = []
+    for k, v in A.items():
+        if k not in srcs:
+            raise NotImplementedError('source {!r} is not supported by the GPU integrator of user '
+                                      'SDEs (dt and dw are)'.format(k))
+        reg = v.reg if isinstance(v, _Sym) else prog.const(v).reg
+        terms.append((srcs[k], reg))
+    u = _lib.SdeUserProgram()
+    u.n_ops = len(prog.ops)
+    u.n_terms = len(terms)
+    for i, (s, r) in enumerate(terms):
+        u.term_source[i] = s
+        u.term_register[i] = r
+    for i, op in enumerate(prog.ops):
+        u.ops[i] = op
+    for i, c in enumerate(prog.consts):
+        u.consts[i] = c
+    return u, prog
+
+
+def _sde_parameters(f):
+    """Parameters of ``f`` after (t, x), with their defaults (sdepy's
+    _inspect_args_defaults, sdepy/integration.py:986-1055)."""
+    ps = list(inspect.signature(f).parameters.values())
+    if len(ps) < 2:
+        raise TypeError('the SDE function takes (t, x, **params)')
+    out = {}
+    for p in ps[2:]:
+        if p.kind not in (p.POSITIONAL_OR_KEYWORD, p.KEYWORD_ONLY):
+            raise NotImplementedError('variable arguments of the SDE function')
+        out[p.name] = None if p.default is p.empty else p.default
+    return out
+
+
+class _user_process(_gpu_process):
+    """A process class made by ``integrate`` from an SDE function."""
+    _model = _lib.MODEL_USER
+    _pnames = ()
+    _program = None
+
+    def _coefficients(self, t=1., tmid=1.):
+        A = self._args
+        ws, P = self.wshape, self.paths
+        x0 = _per_var(_const(A['x0'], 'x0'), ws, P, 'x0')
+        if self._log:
+            x0 = np.log(x0)
+        prm = np.zeros((_lib.MAX_PARAMS, self._W))
+        for i, n in enumerate(self._pnames):
+            prm[i] = _per_var(self._p(n, t), ws, P, n)
+        return np.ascontiguousarray(x0), np.ascontiguousarray(prm)
+
+    def _make_spec(self, seed=0, stream=0):
+        s = super()._make_spec(seed, stream)
+        s.program = C.pointer(self._program)
+        return s
+
+
+def integrate(sde=None, *, q=None, sources=None, log=False, addaxis=False):
+    """Decorator making a GPU process class of an SDE function
+    ``sde(t, x, **params)`` (sdepy's ``integrate``,
+    sdepy/integration.py:1890-1955): ``@integrate def my_process(t, x,
+    theta=1., k=1., sigma=1.): return {'dt': k*(theta - x), 'dw': sigma}``,
+    then ``my_process(x0=1, sigma=.5, paths=..., steps=...)(timeline)``."""
+    if sde is None:
+        def decorator(f):
+            return integrate(f, q=q, sources=sources, log=log, addaxis=addaxis)
+        return decorator
+    # the reference's test evaluation (sdepy/integration.py:1843-1886)
+    if q is not None and sources is not None:
+        neq, ids = q, set(sources)
+    else:
+        try:
+            try:
+                test_val = sde()
+            except Exception:
+                test_val = sde(np.array(1.), np.array(1.))
+        except Exception:
+            raise TypeError('test evaluation of {} failed'.format(sde))
+        if isinstance(test_val, (tuple, list)):
+            neq = len(test_val)
+            if neq == 0:
+                raise ValueError('non empty list or tuple expected')
+        else:
+            neq = 0
+            test_val = (test_val,)
+        ids = set()
+        for z in test_val:
+            ids.update(z.keys())
+        if (q is not None and neq != q) or (sources is not None and set(sources) != ids):
+            raise TypeError("test evaluation of {} inconsistent with given 'q' or 'sources'"
+                            .format(sde))
+    if neq != 0:
+        raise NotImplementedError('systems of SDEs (q = {}) are not supported by the GPU '
+                                  'integrator'.format(neq))
+    if not ids <= {'dt', 'dw'}:
+        raise NotImplementedError('sources {} are not supported by the GPU integrator of user '
+                                  'SDEs (dt and dw are)'.format(sorted(ids - {'dt', 'dw'})))
+    defaults = _sde_parameters(sde)
+    if len(defaults) > _MAX_PARAMS:
+        raise NotImplementedError('user SDEs take at most {} parameters on the GPU, not {}'
+                                  .format(_MAX_PARAMS, len(defaults)))
+    pnames = tuple(defaults)
+    program, _ = compile_sde(sde, pnames)
+    params = {'x0': 1.}
+    params.update(defaults)
+    attrs = dict(_params=params, _pnames=pnames, _tdep_names=pnames, _program=program,
+                 _log=bool(log), _out=_lib.OUT_EXP if log else _lib.OUT_STATE,
+                 sde=staticmethod(sde), q=0, sources_ids=frozenset(ids), addaxis=bool(addaxis),
+                 __doc__=sde.__doc__)
+    return type(getattr(sde, '__name__', 'sde_integrator'), (_user_process,), attrs)

@@ -4,7 +4,7 @@ Run in a container where the reference is importable:
 
     python tests/golden/make_golden.py [REFERENCE_DIR [GROUP ...]]
 
-(groups path, mc, tdep, cir, corr_t; all by default)
+(groups path, mc, tdep, cir, corr_t, user; all by default)
 
 REFERENCE_DIR defaults to /root/reference (the read-only sdepy checkout).
 Nothing under tests/ imports this script; the tests only read the .npz files
@@ -78,9 +78,9 @@ def encode_kw(sdepy, kw, arrays):
 
 def run_case(sdepy, name, cls_name, kw, timeline, wshape, *, paths,
              steps=None, i0=0, corr=None, rho=None, jumps=None, seed=0,
-             dw_src=None, prefix='path'):
+             dw_src=None, prefix='path', cls=None):
     inf = sdepy.infrastructure
-    cls = getattr(sdepy, cls_name)
+    cls = getattr(sdepy, cls_name) if cls is None else cls
     rng = np.random.default_rng(seed)
     if dw_src is None:
         dw_src = inf.wiener_source(paths=paths, vshape=wshape, rng=rng,
@@ -304,15 +304,42 @@ def cir_cases(sdepy):
              paths=40, steps=50, seed=42, prefix='tdep')
 
 
+def user_cases(sdepy):
+    """User SDEs through sdepy's integrate decorator: the functions of
+    tests/helpers.py (class recorded as 'integrate:<name>' or
+    'integrate_log:<name>')."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    import helpers as H
+    lin = np.linspace
+
+    def case(name, spec, kw, timeline, wshape, **more):
+        run_case(sdepy, name, spec, kw, timeline, wshape, prefix='user', cls=H.user_class(sdepy, spec), **more)
+    case('ou', 'integrate:user_ou', dict(x0=1., theta=.5, k=2., sigma=.3), lin(0, 1, 5), (), paths=40, steps=30,
+         seed=61)
+    C = np.array([[1., .4], [.4, 1.]])
+    case('ou_vec_corr', 'integrate:user_ou', dict(x0=[[.2], [-.1]], theta=[[.5], [0.]], k=[[1.], [3.]], sigma=.2,
+                                                   vshape=2, corr=C),
+         lin(0, 2, 5), (2,), paths=32, steps=40, i0=2, corr=C, seed=62)
+    case('cev', 'integrate:user_cev', dict(x0=1., mu=.05, sigma=.6, gamma=.7), lin(0, 1, 3), (), paths=48,
+         steps=60, seed=63)
+    case('gbm_log', 'integrate_log:user_gbm', dict(x0=2., mu=.1, sigma=.3), lin(0, 1, 6), (), paths=40, steps=20,
+         seed=64)
+    case('mixed', 'integrate:user_mixed', dict(x0=.5, a=1.5, b=.7, s=.25), lin(0, 2, 3), (), paths=40, steps=50,
+         seed=65)
+    case('cir_tdep', 'integrate:user_cir', dict(x0=.04, k=1.5, theta=H.tdep_theta_h, xi=H.tdep_xi), (0., .5, 1.),
+         (), paths=40, steps=50, seed=66)
+
+
 def main():
-    # python make_golden.py [REFERENCE_DIR [GROUP ...]], groups path, mc, tdep, cir
+    # python make_golden.py [REFERENCE_DIR [GROUP ...]], groups path, mc, tdep, cir, corr_t, user
     ref = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
-    groups = sys.argv[2:] or ['path', 'mc', 'tdep', 'cir', 'corr_t']
+    groups = sys.argv[2:] or ['path', 'mc', 'tdep', 'cir', 'corr_t', 'user']
     sys.path.insert(0, ref)
     import sdepy
     print('sdepy', sdepy.__version__, 'numpy', np.__version__)
     for name, f in (('path', path_cases), ('mc', mc_cases), ('tdep', tdep_cases), ('cir', cir_cases),
-                    ('corr_t', tdep_corr_cases)):
+                    ('corr_t', tdep_corr_cases), ('user', user_cases)):
         if name in groups:
             f(sdepy)
 

@@ -214,6 +214,41 @@ def tdep_corr4(t):
 TDEP = {name: f for name, f in dict(globals()).items() if name.startswith('tdep_')}
 
 
+# ---------------------------------------------------------------------------
+# user SDE functions (sdepy's integrate decorator) of the user_* fixtures
+# ---------------------------------------------------------------------------
+def user_ou(t, x, theta=1., k=1., sigma=1.):
+    return {'dt': k*(theta - x), 'dw': sigma}
+
+
+def user_cev(t, x, mu=.05, sigma=.3, gamma=.8):
+    return {'dt': mu*x, 'dw': sigma*np.maximum(x, 0.)**gamma}
+
+
+def user_gbm(t, x, mu=.05, sigma=.2):
+    # integrated in log space (integrate(log=True)); dw listed first
+    return {'dw': sigma, 'dt': mu - sigma**2/2}
+
+
+def user_mixed(t, x, a=1., b=.5, s=.3):
+    return {'dt': a*np.sin(t) - b*x + np.exp(-t), 'dw': s*np.sqrt(1. + x*x)*(1 + np.tanh(x))}
+
+
+def user_cir(t, x, k=1., theta=1., xi=1.):
+    xp = np.maximum(x, 0.)
+    return {'dt': k*(theta - xp), 'dw': xi*np.sqrt(xp)}
+
+
+USER = {name: f for name, f in dict(globals()).items() if name.startswith('user_')}
+
+
+def user_class(module, spec):
+    """The process class of a fixture's ``cls`` entry 'integrate:<function>'
+    or 'integrate_log:<function>', made by ``module.integrate``."""
+    kind, name = spec.split(':')
+    return module.integrate(USER[name], log=kind == 'integrate_log')
+
+
 def tdep_kwargs(z, process_cls):
     """Keyword arguments of a tdep fixture: '@name' entries are the
     functions above, '@process' entries the process stored in the fixture's

@@ -1,0 +1,187 @@
+"""User SDEs through ``integrate`` (sdepy/integration.py:1843-1955): the SDE
+function traced into a program (sdepy_gb300/usersde.py) that the device
+interprets per state variable and step.
+
+* CPU: the program, evaluated op by op with numpy, equals the function on
+  arrays bit for bit (the tracer keeps Python's evaluation order and
+  numpy's fast forms of **); the numpy oracle replays the reference's
+  recorded increments to its paths exactly (tests/golden/user_*.npz, from
+  make_golden.py); unsupported functions are refused at decoration;
+* GPU: the device replays the same increments to 1e-12 (FP64); with device
+  noise it matches the C oracle (which evaluates the same program in C) to
+  1e-12, and FP32 matches it to FP32 accuracy.
+"""
+import glob
+import json
+import os
+
+import numpy as np
+import pytest
+
+import sdepy_gb300 as sg
+from sdepy_gb300 import _lib
+from conftest import GOLDEN
+from helpers import USER, oracle_paths, tdep_kwargs, user_class
+from oracle import euler
+
+CASES = sorted(glob.glob(os.path.join(GOLDEN, 'user_*.npz')))
+
+
+def _run_program(u, x, t, params):
+    """The program's value with numpy, op by op (registers r0 = x, r1 = t,
+    r2.. = parameters)."""
+    ops = {_lib.UOP_ADD: np.add, _lib.UOP_SUB: np.subtract, _lib.UOP_MUL: np.multiply,
+           _lib.UOP_DIV: np.true_divide, _lib.UOP_MAX: np.maximum, _lib.UOP_MIN: np.minimum,
+           _lib.UOP_POW: np.power}
+    un = {_lib.UOP_NEG: np.negative, _lib.UOP_ABS: np.absolute, _lib.UOP_EXP: np.exp, _lib.UOP_LOG: np.log,
+          _lib.UOP_SQRT: np.sqrt, _lib.UOP_SIN: np.sin, _lib.UOP_COS: np.cos, _lib.UOP_TAN: np.tan,
+          _lib.UOP_TANH: np.tanh, _lib.UOP_EXPM1: np.expm1, _lib.UOP_LOG1P: np.log1p,
+          _lib.UOP_ARCTAN: np.arctan, _lib.UOP_COPY: np.copy}
+    r = {0: x, 1: t}
+    for i, p in enumerate(params):
+        r[2 + i] = p
+    for op in u.ops[:u.n_ops]:
+        code, d, a, b = op & 0xff, (op >> 8) & 0xff, (op >> 16) & 0xff, op >> 24
+        if code == _lib.UOP_CONST:
+            r[d] = np.float64(u.consts[a])
+        elif code in ops:
+            r[d] = ops[code](r[a], r[b])
+        else:
+            r[d] = un[code](r[a])
+    return [r[u.term_register[i]] for i in range(u.n_terms)], [u.term_source[i] for i in range(u.n_terms)]
+
+
+@pytest.mark.parametrize('name', sorted(USER))
+def test_program_equals_function(name):
+    f = USER[name]
+    cls = sg.integrate(f)
+    g = np.random.default_rng(1)
+    x = np.abs(g.normal(size=1000)) + .01
+    t = .37
+    params = [np.float64(v) for v in cls._params.values()][1:]   # defaults, x0 excluded
+    got, srcs = _run_program(cls._program, x, np.float64(t), params)
+    with np.errstate(all='ignore'):
+        A = f(t, x, **dict(zip(cls._pnames, params)))
+    assert [{'dt': 0, 'dw': 1}[k] for k in A] == srcs
+    for v, (k, ref) in zip(got, A.items()):
+        np.testing.assert_array_equal(np.broadcast_to(v, x.shape), np.broadcast_to(ref, x.shape), err_msg=k)
+
+
+def test_tracer_forms_and_refusals():
+    @sg.integrate
+    def sq(t, x, a=2.):
+        return {'dt': x**2 + x**0.5 + x**-1 + x**1 + a**3, 'dw': np.square(x)}
+    codes = [op & 0xff for op in sq._program.ops[:sq._program.n_ops]]
+    assert _lib.UOP_POW in codes and _lib.UOP_SQRT in codes
+    with pytest.raises(NotImplementedError):       # branching on the state
+        @sg.integrate
+        def b1(t, x, a=1.):
+            return {'dt': a if x > 0 else -a, 'dw': 1.}
+    with pytest.raises(NotImplementedError):       # Python's max compares
+        @sg.integrate
+        def b2(t, x):
+            return {'dt': max(x, 0.), 'dw': 1.}
+    with pytest.raises(NotImplementedError):       # jumps
+        @sg.integrate
+        def b3(t, x, a=1.):
+            return {'dt': a, 'dw': 1., 'dj': 1.}
+    with pytest.raises(NotImplementedError):       # a system of SDEs
+        @sg.integrate(q=2, sources={'dt', 'dw'})
+        def b4(t, x, y, a=1.):
+            return ({'dt': a, 'dw': 1.}, {'dt': a, 'dw': 1.})
+    with pytest.raises(NotImplementedError):       # seven parameters
+        @sg.integrate
+        def b5(t, x, a=1., b=1., c=1., d=1., e=1., f=1., g=1.):
+            return {'dt': a + b + c + d + e + f + g, 'dw': 1.}
+    with pytest.raises(NotImplementedError):       # an unsupported ufunc
+        @sg.integrate
+        def b6(t, x):
+            return {'dt': np.arcsinh(x), 'dw': 1.}
+    with pytest.raises(TypeError):                 # unexpected keyword, as sdepy
+        sq(foo=1.)
+
+
+def _fixture_args(z):
+    kw = tdep_kwargs(z, sg.process)
+    vshape = kw.pop('vshape', ())
+    vshape = (vshape,) if isinstance(vshape, int) else tuple(vshape)
+    paths = int(z['paths'])
+    return kw, vshape, paths
+
+
+@pytest.mark.parametrize('path', CASES, ids=os.path.basename)
+def test_numpy_oracle_reproduces_reference(path):
+    z = np.load(path)
+    kw, vshape, paths = _fixture_args(z)
+    kw.pop('corr', None)
+    kind, name = str(z['cls']).split(':')
+    dw = euler.Replay(z['rec_dw'], paths=paths, vshape=z['rec_dw'].shape[1:-1])
+    res, info = euler.integrate('user', kw, z['timeline'], paths=paths, vshape=vshape,
+                                steps=json.loads(str(z['steps'])), i0=int(z['i0']), dw=dw,
+                                sde=USER[name], log_flag=kind == 'integrate_log')
+    np.testing.assert_array_equal(res, z['xx0'])
+    assert info['computed_steps'] == int(z['computed_steps'])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('path', CASES, ids=os.path.basename)
+def test_gpu_replay_matches_reference(lib, path):
+    z = np.load(path)
+    kw, vshape, paths = _fixture_args(z)
+    cls = user_class(sg, str(z['cls']))
+    dw = euler.Replay(z['rec_dw'], paths=paths, vshape=z['rec_dw'].shape[1:-1])
+    P = cls(paths=paths, vshape=vshape, steps=json.loads(str(z['steps'])), i0=int(z['i0']), dw=dw, **kw)
+    x = P(z['timeline'])
+    ref = z['xx0']
+    err = np.max(np.abs(np.asarray(x) - ref)/np.maximum(np.abs(ref), 1.))
+    assert err <= 1e-12, err
+    assert P.info['computed_steps'] == int(z['computed_steps'])
+
+
+DEVICE_CASES = [
+    ('ou', 'integrate:user_ou', dict(x0=1., theta=.5, k=2., sigma=.3), np.linspace(0, 1, 5), 40, 0),
+    ('ou_corr4', 'integrate:user_ou', dict(vshape=4, x0=0., theta=[[.1], [.2], [.3], [.4]], k=1.5, sigma=.3,
+                                           corr=np.array([[1., .3, .1, 0.], [.3, 1., .2, .1], [.1, .2, 1., .3],
+                                                          [0., .1, .3, 1.]])), (0., .5, 1.), 30, 0),
+    ('cev_i0', 'integrate:user_cev', dict(x0=1., mu=.05, sigma=.6, gamma=.7), np.linspace(0, 1, 5), 40, 2),
+    ('gbm_log', 'integrate_log:user_gbm', dict(x0=2., mu=.1, sigma=.3), np.linspace(0, 1, 6), 20, 0),
+    ('mixed_vec3', 'integrate:user_mixed', dict(vshape=3, x0=[[.5], [0.], [-.5]], a=1.5, b=.7, s=.25),
+     np.linspace(0, 2, 3), 50, 0),
+    ('cir_tdep', 'integrate:user_cir', None, (0., .5, 1.), 50, 0),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('case', DEVICE_CASES, ids=[c[0] for c in DEVICE_CASES])
+def test_device_rng_matches_c_oracle(lib, clib, case):
+    from helpers import TDEP
+    name, spec, kw, tl, steps, i0 = case
+    if kw is None:
+        kw = dict(vshape=2, x0=.04, k=1.5, theta=TDEP['tdep_theta_h'], xi=TDEP['tdep_xi'])
+    cls = user_class(sg, spec)
+    paths, seed = 777, 0x5eed
+    P = cls(paths=paths, steps=steps, i0=i0, rng=sg.philox_rng(seed, 2), **kw)
+    out = np.asarray(P(tl))
+    got = out.reshape(len(tl), -1, paths)
+    ref, _ = oracle_paths(clib, P, tl, seed, 2)
+    ref = ref.reshape(got.shape)
+    err = np.max(np.abs(got - ref)/np.maximum(np.abs(ref), 1.))
+    assert err <= 1e-12, err
+    P32 = cls(paths=paths, steps=steps, i0=i0, dtype=np.float32, rng=sg.philox_rng(seed, 2), **kw)
+    g32 = np.asarray(P32(tl), dtype=float).reshape(got.shape)
+    assert np.max(np.abs(g32 - ref)/np.maximum(np.abs(ref), 1.)) < 2e-3
+    # and the fused summary of the last row
+    x, mc = P.montecarlo(tl, bins=20, paths_out=True)
+    last = np.asarray(x[-1]).reshape(-1, paths)
+    np.testing.assert_allclose(np.asarray(mc.mean()).reshape(-1), last.mean(axis=-1), rtol=1e-12, atol=1e-15)
+
+
+@pytest.mark.gpu
+def test_user_sde_refusals(lib):
+    cls = user_class(sg, 'integrate:user_ou')
+    with pytest.raises(NotImplementedError):
+        cls(paths=4, dw=sg.odd_wiener_source)(np.linspace(0, 1, 3))
+    from sdepy_gb300.autograd import expectation
+    import torch
+    with pytest.raises(NotImplementedError):
+        expectation(cls, (0., 1.), [], paths=100, steps=10, x0=torch.tensor(1., requires_grad=True))
