@@ -472,6 +472,9 @@ def extra_configs(lib):
         g.n_pts, g.step_offset = leg.tt.size, 0
         o = _lib.SdeOut()
         o.xx, o.n_rows, o.on_device = None, len(timeline), 0
+        ptab = P._params_table(leg) if P._tdep else None          # time-dependent parameters
+        ctab = P._corr_table(leg) if P._corr_tdep else None       # and correlations
+        g.params_t, g.corr_t = _lib.dptr(ptab), _lib.dptr(ctab)
         req, so, arrs = P._stats_request(dict(row=len(timeline) - 1, bins=0, range=None, strikes=strikes))
         spec = P._make_spec(seed, 0)
         _lib.check(lib.sde_run_stats(C.byref(spec), C.byref(g), None, C.byref(o), C.byref(req), C.byref(so)), 'fwd')
@@ -575,6 +578,30 @@ def extra_configs(lib):
         anti[name] = row
     out['antithetic_fp32'] = anti
     out['process_post'] = process_post_bench(lib)
+    # ---- beyond the presets: CIR, a user SDE (integrate, interpreted
+    # coefficients) against the preset it restates, and a time-dependent
+    # correlation against a constant one; 2^22 paths, 499 steps on (0, 2),
+    # fused summary
+    K = 2**22
+    nxt = {'paths': K, 'steps': 499}
+
+    def rate(P):
+        ms = _time_call(lambda: fused(P, (0., 2.), [], 8), lib)
+        return {'kernel_ms': ms, 'path_steps_per_s': K*499/(ms*1e-3)}
+    nxt['cir_fp32'] = rate(sg.cox_ingersoll_ross_process(paths=K, steps=500, dtype=np.float32, x0=.04,
+                                                          theta=.04, k=1.5, xi=.5))
+    user_ou = sg.integrate(lambda t, x, theta=.5, k=2., sigma=.3: {'dt': k*(theta - x), 'dw': sigma})
+    for name, dtype in (('fp32', np.float32), ('fp64', None)):
+        nxt['user_ou_' + name] = rate(user_ou(paths=K, steps=500, dtype=dtype, x0=1.))
+        nxt['preset_ou_' + name] = rate(sg.ornstein_uhlenbeck_process(paths=K, steps=500, dtype=dtype, x0=1.,
+                                                                      theta=.5, k=2., sigma=.3))
+    Cm = np.array([[1., .5], [.5, 1.]])
+    nxt['ou2_corr_const_fp32'] = rate(sg.ornstein_uhlenbeck_process(vshape=2, paths=K, steps=500,
+                                                                     dtype=np.float32, corr=Cm))
+    nxt['ou2_corr_t_fp32'] = rate(sg.ornstein_uhlenbeck_process(
+        vshape=2, paths=K, steps=500, dtype=np.float32,
+        corr=lambda t: np.array([[1., .5*np.cos(t)], [.5*np.cos(t), 1.]])))
+    out['beyond_presets'] = nxt
     # ---- lognormal: FP64, 1e5 paths, 502 steps, all 253 rows written (host output)
     import time
     Ln = sg.lognorm_process(x0=1., mu=.05, sigma=.2, paths=100000, steps=252, rng=sg.philox_rng(0))

@@ -119,7 +119,7 @@ typedef struct SdeUserProgram {
  * path K + q takes the draws of path q with opposite Wiener increments and
  * the same Poisson counts and jump sizes, as sdepy's odd_wiener_source with
  * even_cpoisson_source (sdepy/infrastructure.py:2047-2150); groups of up to
- * 8 states, constant or time-dependent coefficients except an OU theta. */
+ * 8 states, constant or time-dependent coefficients and correlations. */
 #define SDE_FLAG_ANTITHETIC 1
 
 typedef struct SdeSpec {

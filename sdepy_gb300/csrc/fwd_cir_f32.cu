@@ -1,6 +1,7 @@
 // Instantiations of sde_fwd_kernel for the CIR model (float): device noise and
 // injected increments for groups of 1..16 states, device noise with
-// time-dependent coefficients (TDEP), antithetic pairs for groups of up to 8.
+// time-dependent coefficients (TDEP), antithetic pairs for groups of up to 8
+// (with and without TDEP).
 #include "sde_kernels.cuh"
 
 namespace sdegpu {
@@ -26,6 +27,10 @@ FwdLauncher<float> find_fwd_f32_cir(int maxm, bool inject, bool tdep, bool anti,
     SDE_CIR(4, false, true, false)
     SDE_CIR(8, false, true, false)
     SDE_CIR(16, false, true, false)
+    SDE_CIR(1, false, true, true)
+    SDE_CIR(2, false, true, true)
+    SDE_CIR(4, false, true, true)
+    SDE_CIR(8, false, true, true)
     SDE_CIR(1, false, false, true)
     SDE_CIR(2, false, false, true)
     SDE_CIR(4, false, false, true)

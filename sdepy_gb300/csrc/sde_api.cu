@@ -368,7 +368,7 @@ template <> struct Finder<double> {
         return f ? f : find_fwd_f64_ou_heston(model, maxm, inj, jmp, bps);
     }
     static FwdLauncher<double> find_tdep(int, int, int *) { return nullptr; }
-    static FwdLauncher<double> find_anti(int model, int maxm, bool jmp, int *bps) {
+    static FwdLauncher<double> find_anti(int model, int maxm, bool jmp, bool, int *bps) {
         if (model == SDE_MODEL_CIR) return jmp ? nullptr : find_fwd_f64_cir(maxm, false, true, bps);
         return find_fwd_f64_anti(model, maxm, jmp, bps);
     }
@@ -386,9 +386,11 @@ template <> struct Finder<float> {
         if (model == SDE_MODEL_CIR) return find_fwd_f32_cir(maxm, false, true, false, bps);
         return find_fwd_f32_tdep(model, maxm, bps);
     }
-    static FwdLauncher<float> find_anti(int model, int maxm, bool jmp, int *bps) {
-        if (model == SDE_MODEL_CIR) return jmp ? nullptr : find_fwd_f32_cir(maxm, false, false, true, bps);
-        return find_fwd_f32_anti(model, maxm, jmp, bps);
+    // tdep: the instantiations with per-step coefficients and correlation
+    // factors (and OU rows with the theta term)
+    static FwdLauncher<float> find_anti(int model, int maxm, bool jmp, bool tdep, int *bps) {
+        if (model == SDE_MODEL_CIR) return jmp ? nullptr : find_fwd_f32_cir(maxm, false, tdep, true, bps);
+        return tdep ? find_fwd_f32_anti_tdep(model, maxm, jmp, bps) : find_fwd_f32_anti(model, maxm, jmp, bps);
     }
 };
 
@@ -484,7 +486,7 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     const bool corr_steps = gr->corr_t != nullptr && !inject && M > 1;
     if (corr_steps && sizeof(R) == 4 && jumps && !anti)
         return fail(SDE_ERR_UNSUPPORTED, "time-dependent correlations of FP32 jump models");
-    if (corr_steps && tab && s->model == SDE_MODEL_OU && !anti) ou_b = true;
+    if (corr_steps && tab && s->model == SDE_MODEL_OU) ou_b = true;
     const int nb = ou_b ? 3 : 2;   // coefficient vectors per row
     // FP32 LINEAR / OU: the grid as runs of steps with one coefficient row
     // each, and the compact table of those rows (see FwdArgs::coef / runs)
@@ -769,15 +771,14 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
 
     // ---- launch ----------------------------------------------------------------------
     int bps = 0;
-    if (anti && ou_b) return fail(SDE_ERR_UNSUPPORTED, "antithetic paths with a time-dependent OU theta");
     // the FP32 Heston and CIR kernels of device noise read per-step
     // coefficients only in their time-dependent instantiation
-    const bool tdep_k = ou_b || (sizeof(R) == 4 && !inject && !anti &&
+    const bool tdep_k = ou_b || (sizeof(R) == 4 && !inject &&
                                  ((nprmt && (s->model == SDE_MODEL_HESTON || s->model == SDE_MODEL_CIR)) ||
                                   corr_steps));
     // (user-SDE kernels reload per-step parameters and factors in every form)
     FwdLauncher<R> L = user     ? Finder<R>::find(s->model, maxm_of(M), inject, jumps, &bps)
-                       : anti   ? Finder<R>::find_anti(s->model, maxm_of(M), jumps, &bps)
+                       : anti   ? Finder<R>::find_anti(s->model, maxm_of(M), jumps, tdep_k, &bps)
                        : tdep_k ? Finder<R>::find_tdep(s->model, maxm_of(M), &bps)
                                 : Finder<R>::find(s->model, maxm_of(M), inject, jumps, &bps);
     if (!L) return fail(SDE_ERR_UNSUPPORTED, "no kernel for model %d group size %d", s->model, M);

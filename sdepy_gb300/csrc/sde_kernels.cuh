@@ -702,10 +702,10 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     // per-step coefficient reloads compiled in (the non-table kernels but
     // the common FP32 Heston and CIR ones)
     constexpr bool USER = MODEL == SDE_MODEL_USER;
-    constexpr bool RELOAD = !TAB && (sizeof(R) == 8 || INJECT || ANTI || TDEP || USER);
+    constexpr bool RELOAD = !TAB && (sizeof(R) == 8 || INJECT || TDEP || USER);
     // per-step correlation factors compiled in (the same kernels, TAB ones
     // included, with device noise)
-    constexpr bool STEPCORR = !INJECT && (sizeof(R) == 8 || ANTI || TDEP || USER);
+    constexpr bool STEPCORR = !INJECT && (sizeof(R) == 8 || TDEP || USER);
     // parameter slots of a time-dependent table row (all six for USER)
     constexpr int NPT = USER ? 6 : 3;
     __shared__ R red[BLOCK / 32];
@@ -721,7 +721,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     const bool do_stats = a.partials != nullptr;
     const PhiloxKey key = a.key;  // by value: uniform registers, not indexed parameter loads
     if (((TAB && (a.coef == nullptr || a.runs == nullptr || (SHIFT && a.tshift == nullptr))) ||
-         (!TAB && !RELOAD && a.prm_t != nullptr)) &&
+         (!TAB && !RELOAD && a.prm_t != nullptr) || (!STEPCORR && a.chol_t != nullptr)) &&
         n_steps > 0) {  // uniform: the grid returns
         if (threadIdx.x == 0 && blockIdx.x == 0 && blockIdx.y == 0) atomicOr(a.err, ERRF_ARGS);
         return;
@@ -860,10 +860,18 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
             auto draw = [&](int k, R sq, R (&dW)[MAXM], R (&dJ)[MAXM]) {
 #pragma unroll
                 for (int m = 0; m < MAXM; ++m) dJ[m] = R(0);
-                // the step's correlation factor (uniform choice)
-                const R *chol = a.chol;
-                if constexpr (STEPCORR)
-                    if (a.chol_t) chol = a.chol_t + (int64_t)k * NCHOL;
+                // f(the step's correlation factor): the per-step table's row
+                // (uniform test), else the constant factor of the parameter
+                // block -- two copies of f, so that the constant one keeps
+                // its constant-bank loads
+                auto with_chol = [&](auto &&f) {
+                    if constexpr (STEPCORR)
+                        if (a.chol_t) {
+                            f(a.chol_t + (int64_t)k * NCHOL);
+                            return;
+                        }
+                    f(a.chol);
+                };
                 if (INJECT) {
 #pragma unroll
                     for (int m = 0; m < MAXM; ++m) {
@@ -895,18 +903,20 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                 } else if constexpr (NZ == 2) {
                     R z[MAXM];
                     pair.get(key, pre, k, a.step_offset, z[0], z[1]);
-                    correlate<R, MAXM>(chol, a.has_corr, z, sq, dW);
+                    with_chol([&](const R *chol) { correlate<R, MAXM>(chol, a.has_corr, z, sq, dW); });
                     return;
                 }
                 if constexpr (!JUMPS) {
-                    step_increments<R, MAXM, TAB>(key, pre, c1w, NC, chol, a.has_corr, sq, dW);
+                    with_chol([&](const R *chol) {
+                        step_increments<R, MAXM, TAB>(key, pre, c1w, NC, chol, a.has_corr, sq, dW);
+                    });
                     return;
                 }
                 uint32_t u[4 * NCMAX];
                 step_words<MAXM, JUMPS>(key, pre, c1w, NC, u);
                 R z[MAXM];
                 words_to_normals<R, MAXM, 4 * NCMAX, TAB>(u, z);
-                correlate<R, MAXM>(chol, a.has_corr, z, sq, dW);
+                with_chol([&](const R *chol) { correlate<R, MAXM>(chol, a.has_corr, z, sq, dW); });
 #pragma unroll
                 for (int m = 0; m < MAXM; ++m)
                     if (m < M) add_jumps(m, pick_word(u, 2 * P + m), k, c1w, dJ);
@@ -1169,6 +1179,9 @@ FwdLauncher<float> find_fwd_f32_user(int maxm, bool inject, int *bps);
 FwdLauncher<double> find_fwd_f64_user(int maxm, bool inject, int *bps);
 // antithetic kernels (device noise, groups of up to 8 states)
 FwdLauncher<float> find_fwd_f32_anti(int model, int maxm, bool jumps, int *bps);
+// FP32 antithetic kernels with per-step coefficients and correlation factors
+// (fwd_anti_tdep_f32.cu)
+FwdLauncher<float> find_fwd_f32_anti_tdep(int model, int maxm, bool jumps, int *bps);
 FwdLauncher<double> find_fwd_f64_anti(int model, int maxm, bool jumps, int *bps);
 
 }  // namespace sdegpu

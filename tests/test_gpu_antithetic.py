@@ -39,6 +39,14 @@ CASES = [
     ('cir', sg.cox_ingersoll_ross_process, dict(vshape=2, x0=.04, theta=.04, k=1.5, xi=.5), (0., 1.), 40, 0),
     ('ou_corr_t', sg.ornstein_uhlenbeck_process,
      dict(vshape=2, x0=.1, k=1.5, theta=.3, sigma=.3, corr=TDEP['tdep_corr2']), np.linspace(0, 1, 3), 30, 0),
+    ('ou_theta_t', sg.ornstein_uhlenbeck_process,
+     dict(vshape=2, x0=[[.3], [-.1]], k=TDEP['tdep_k2'], theta=TDEP['tdep_theta2'], sigma=.3),
+     np.linspace(0, 2, 5), 40, 0),
+    ('heston_tdep', sg.heston_process,
+     dict(x0=100., mu=TDEP['tdep_mu'], y0=.04, k=1.5, theta=TDEP['tdep_theta_h'], xi=.5, rho=TDEP['tdep_rho']),
+     (0., 1.), 40, 0),
+    ('merton_lam_t', sg.merton_jumpdiff_process,
+     dict(x0=1., mu=.03, sigma=.15, lam=TDEP['tdep_lam'], a=-.1, b=.15), np.linspace(0, 1, 3), 60, 0),
 ]
 
 
