@@ -686,7 +686,8 @@ def run_case(args):
     'batch' (256 instances of the heterogeneous workload, paths <= 65536),
     'lognorm_fp64' (FP64, 1e5 paths, 502 steps, 253 rows written
     to device memory), 'process_post' (FP32 device-resident 11 x 8 x 2^20
-    values: moments, cdf at 41 values, chf at 4 values of u)."""
+    values: moments, cdf at 41 values, chf at 4 values of u), 'cir_user'
+    (CIR and an interpreted user SDE, FP32, 2^20 paths x 499 steps)."""
     import ctypes as C
     import torch
     import sdepy_gb300 as sg
@@ -743,6 +744,21 @@ def run_case(args):
             ms.append(last[0])
         print(json.dumps({'case': args.case, 'kernel_ms': float(np.median(ms[args.warmup:])),
                           'path_steps': 100000*leg.n_steps}))
+    elif args.case == 'cir_user':
+        # CIR and an interpreted user SDE (the OU coefficients), FP32, 2^20
+        # paths x 499 steps on (0, 2), fused summary of the last point
+        user_ou = sg.integrate(lambda t, x, theta=.5, k=2., sigma=.3: {'dt': k*(theta - x), 'dw': sigma})
+        res = {}
+        for name, P in (('cir', sg.cox_ingersoll_ross_process(paths=2**20, steps=500, dtype=np.float32, x0=.04,
+                                                              theta=.04, k=1.5, xi=.5)),
+                        ('user_ou', user_ou(paths=2**20, steps=500, dtype=np.float32, x0=1.))):
+            ms = []
+            for i in range(args.warmup + args.steps):
+                P.montecarlo((0., 2.), bins=10)
+                lib.sde_timing(-1, last)
+                ms.append(last[0])
+            res[name + '_kernel_ms'] = float(np.median(ms[args.warmup:]))
+        print(json.dumps({'case': args.case, **res}))
     elif args.case == 'process_post':
         print(json.dumps({'case': args.case, 'result': process_post_bench(
             lib, reps=args.steps, api=False, dtypes=(np.float32,))}))
@@ -758,7 +774,8 @@ def main():
                     help='paths per step (profiling captures use fewer)')
     ap.add_argument('--quick', action='store_true',
                     help='timed steps only: no FP64 / e2e / CPU / probe extras')
-    ap.add_argument('--case', default=None, choices=['heston_adjoint', 'batch', 'lognorm_fp64', 'process_post'],
+    ap.add_argument('--case', default=None,
+                    choices=['heston_adjoint', 'batch', 'lognorm_fp64', 'process_post', 'cir_user'],
                     help='run one small single-kernel case (profiling)')
     args = ap.parse_args()
     if args.case:

@@ -280,10 +280,10 @@ class montecarlo:
         """A montecarlo instance equivalent to ``montecarlo(sample, bins,
         range)`` built from a device summary of ``sample`` (used by the
         fused process reductions)."""
-        a = cls(bins=bins, range=range)
+        a = cls(bins=bins if counts is not None else None, range=range)
         M = int(summ.reshape(-1, 7)[0, 0])
         a._update_moments(True, summ, vshape, M, sdtype)
-        if bins is not None:
+        if a._bins is not None:   # no histogram without counts (bins=0 or None)
             a._update_histogram(True, None, -1, counts, edges, vshape, M, sdtype)
         a._paths[0] = M
         return a
