@@ -38,6 +38,7 @@ _MAP = {
                        'k': (1, 1), 'theta': (1, 2), 'xi': (1, 3), 'rho': (0, 7)},
     'merton_jumpdiff_process': {'x0': (0, 0), 'mu': (0, 1), 'sigma': (0, 2), 'a': (0, 4), 'b': (0, 5)},
     'kou_jumpdiff_process': {'x0': (0, 0), 'mu': (0, 1), 'sigma': (0, 2), 'a': (0, 4), 'b': (0, 5)},
+    'cox_ingersoll_ross_process': {'x0': (0, 0), 'k': (0, 1), 'theta': (0, 2), 'xi': (0, 3)},
 }
 
 

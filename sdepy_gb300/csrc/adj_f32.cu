@@ -52,6 +52,22 @@ AdjLauncher<float> find_adj_f32(int model, int maxm, bool jumps, int *bps) {
         if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_OU, 8, false>();
         return &launch_adj<float, SDE_MODEL_OU, 8, false>;
     }
+    if (model == SDE_MODEL_CIR && maxm == 1 && jumps == false) {
+        if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_CIR, 1, false>();
+        return &launch_adj<float, SDE_MODEL_CIR, 1, false>;
+    }
+    if (model == SDE_MODEL_CIR && maxm == 2 && jumps == false) {
+        if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_CIR, 2, false>();
+        return &launch_adj<float, SDE_MODEL_CIR, 2, false>;
+    }
+    if (model == SDE_MODEL_CIR && maxm == 4 && jumps == false) {
+        if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_CIR, 4, false>();
+        return &launch_adj<float, SDE_MODEL_CIR, 4, false>;
+    }
+    if (model == SDE_MODEL_CIR && maxm == 8 && jumps == false) {
+        if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_CIR, 8, false>();
+        return &launch_adj<float, SDE_MODEL_CIR, 8, false>;
+    }
     if (model == SDE_MODEL_HESTON && maxm == 2 && jumps == false) {
         if (bps) *bps = adj_max_blocks_per_sm<float, SDE_MODEL_HESTON, 2, false>();
         return &launch_adj<float, SDE_MODEL_HESTON, 2, false>;

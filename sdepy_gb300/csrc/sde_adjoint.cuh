@@ -13,8 +13,8 @@
 //   Nothing per step is ever written to global memory.
 //
 // Integer Poisson counts are not differentiated (their intensity gets no
-// gradient); the Heston full-truncation kink contributes its one-sided
-// derivative (zero where y <= 0).
+// gradient); the full-truncation kink of Heston's variance and of CIR
+// contributes its one-sided derivative (zero where the state is <= 0).
 #pragma once
 #include "sde_kernels.cuh"
 
@@ -124,8 +124,8 @@ __device__ __forceinline__ R terminal_adjoint(const AdjArgs<R> &a, const R (&st)
     return val;
 }
 
-// one forward Euler step of the OU / Heston models (same arithmetic as the
-// forward kernel); z: uncorrelated normals, dW: correlated increments
+// one forward Euler step of the OU / CIR / Heston models (same arithmetic as
+// the forward kernel); z: uncorrelated normals, dW: correlated increments
 template <typename R, int MODEL, int MAXM>
 __device__ __forceinline__ void fwd_step(const R (&c0)[MAXM], const R (&c1)[MAXM], const R (&c2)[MAXM],
                                          R dt, const R (&dW)[MAXM], R (&st)[MAXM]) {
@@ -135,6 +135,14 @@ __device__ __forceinline__ void fwd_step(const R (&c0)[MAXM], const R (&c1)[MAXM
         for (int m = 0; m < MAXM; ++m) {
             const R drift = A::mul(c0[m], A::sub(c1[m], st[m]));
             st[m] = A::add(st[m], A::add(A::mul(drift, dt), A::mul(c2[m], dW[m])));
+        }
+    } else if (MODEL == SDE_MODEL_CIR) {
+#pragma unroll
+        for (int m = 0; m < MAXM; ++m) {
+            const R xp = fmax(st[m], R(0));
+            const R drift = A::mul(c0[m], A::sub(c1[m], xp));
+            const R vol = A::mul(c2[m], A::sqrt_(xp));
+            st[m] = A::add(st[m], A::add(A::mul(drift, dt), A::mul(vol, dW[m])));
         }
     } else {
         constexpr int h = MAXM / 2;
@@ -318,6 +326,21 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                             gr[m][2] += xbn * c0[m] * dt;         // theta
                             gr[m][3] += xbn * bw[k - k0][m];      // sigma
                             xb[m] = xbn * (R(1) - c0[m] * dt);
+                        }
+                    } else if (MODEL == SDE_MODEL_CIR) {
+#pragma unroll
+                        for (int m = 0; m < MAXM; ++m) {
+                            const R x = bx[k - k0][m];
+                            const R xp = fmax(x, R(0));
+                            const R s = A::sqrt_(xp);
+                            const R xbn = xb[m], dw = bw[k - k0][m];
+                            gr[m][1] += xbn * (c1[m] - xp) * dt;   // k
+                            gr[m][2] += xbn * c0[m] * dt;          // theta
+                            gr[m][3] += xbn * s * dw;              // xi
+                            // dx'/dx = 1 + (-k dt + xi dW / (2 sqrt x)) where x > 0
+                            R d = R(1);
+                            if (x > R(0) && s > R(0)) d = R(1) - c0[m] * dt + c2[m] * dw * (R(0.5) / s);
+                            xb[m] = xbn * d;
                         }
                     } else {
                         constexpr int h = MAXM / 2;

@@ -173,3 +173,29 @@ def test_autograd_expectation(lib):
     assert abs(x0.grad.item() - g['x0']) < 1e-12*max(1, abs(g['x0']))
     assert abs(y0.grad.item() - g['y0']) < 1e-12*max(1, abs(g['y0']))
     assert abs(rho.grad.item() - g['rho']) < 1e-12*max(1, abs(g['rho']))
+
+
+def test_cir_adjoint_vs_fd(lib):
+    """CIR (Feller condition 2 k theta > xi^2 holds, so truncation is rare):
+    the adjoint of x0, k, theta, xi against central finite differences on
+    common random numbers, mean and call payoffs."""
+    kw = dict(x0=.3, k=2., theta=.25, xi=.3)
+    tl, steps, paths = (0., .5, 1.), 50, 2**16
+    for strikes, weights, wm in (([], [], 1.), ([.2, .3], [.6, .4], 0.)):
+        grad, val = adjoint(lib, sg.cox_ingersoll_ross_process, tl, steps, paths,
+                            strikes, weights, wm, 7, 1, **kw)
+        for j, name in ((0, 'x0'), (1, 'k'), (2, 'theta'), (3, 'xi')):
+            f = fd(sg.cox_ingersoll_ross_process, name, 1e-5, tl, steps, paths, strikes, 7, 1, **kw)
+            target = wm*f[0] + sum(w*x for w, x in zip(weights, f[1:]))
+            assert abs(grad[0, j] - target) <= 1e-4*max(1., abs(target)), (name, grad[0, j], target)
+    # through torch.autograd
+    import torch
+    from sdepy_gb300.autograd import expectation
+    x0 = torch.tensor(kw['x0'], dtype=torch.float64, requires_grad=True)
+    xi = torch.tensor(kw['xi'], dtype=torch.float64, requires_grad=True)
+    v = expectation(sg.cox_ingersoll_ross_process, tl, [], paths=paths, steps=steps, dtype=np.float64,
+                    seed=7, stream=1, x0=x0, k=kw['k'], theta=kw['theta'], xi=xi)
+    v[0].backward()
+    grad, _ = adjoint(lib, sg.cox_ingersoll_ross_process, tl, steps, paths, [], [], 1., 7, 1, **kw)
+    assert abs(x0.grad.item() - grad[0, 0]) <= 1e-12*max(1., abs(grad[0, 0]))
+    assert abs(xi.grad.item() - grad[0, 3]) <= 1e-12*max(1., abs(grad[0, 3]))
