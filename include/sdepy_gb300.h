@@ -69,17 +69,25 @@ extern "C" {
  */
 
 /* A user SDE (sdepy's integrate decorator, sdepy/integration.py:1843-1955):
- * the coefficients A_dt and A_dw of one equation, compiled from the SDE
- * function into a straight-line program evaluated per state variable and
- * step.  Registers: r0 = x (the state), r1 = t (the step's start), r2..r7 =
- * parameters p0..p5, the rest temporaries; SDE_USER_MAX_REGS in all.  An
- * instruction is code | dst << 8 | a << 16 | b << 24 (SDE_UOP_*: dst = f(ra,
- * rb); SDE_UOP_CONST: dst = consts[a]).  The step is x + (A_1 dZ_1 + A_2 dZ_2)
- * with the terms in the order of the SDE function's returned dict (sdepy's
- * euler_next, sdepy/integration.py:707-718), dZ = dt or dw. */
+ * the coefficients A_dt and A_dw of q equations (q = n_eq; 1 for a single
+ * SDE), compiled from the SDE function into a straight-line program.  The
+ * program runs per step and per component: on the component's state x of
+ * a single equation, or on the states of that component in every equation
+ * of a system (sdepy's SDEs: a group of the spec is one last-axis slice of
+ * the working shape, holding group_size / q components of each equation,
+ * equation e's component h at e * (group_size / q) + h).  Registers: r0 =
+ * the state of equation 0, r1 = t (the step's start), r2..r7 = parameters
+ * p0..p5, r8..r(6 + q) = the states of equations 1..q-1, the rest
+ * temporaries; SDE_USER_MAX_REGS in all.  An instruction is code | dst << 8
+ * | a << 16 | b << 24 (SDE_UOP_*: dst = f(ra, rb); SDE_UOP_CONST: dst =
+ * consts[a]).  Equation e steps x + (A_1 dZ_1 + A_2 dZ_2), its coefficients
+ * in registers term_register[e][0..n_terms-1], the sources term_source[]
+ * in the order of the SDE function's returned dict (sdepy's euler_next,
+ * sdepy/integration.py:707-718), dZ = dt or dw. */
 #define SDE_USER_MAX_OPS    64
 #define SDE_USER_MAX_CONSTS 16
 #define SDE_USER_MAX_REGS   48
+#define SDE_USER_MAX_EQ     8
 #define SDE_SRC_DT 0
 #define SDE_SRC_DW 1
 enum {
@@ -90,9 +98,10 @@ enum {
 };
 typedef struct SdeUserProgram {
     int32_t n_ops;
-    int32_t n_terms;                  /* terms of the Euler sum, 0..2            */
+    int32_t n_eq;                     /* equations q, 1..SDE_USER_MAX_EQ          */
+    int32_t n_terms;                  /* terms of each equation's sum, 0..2      */
     int32_t term_source[2];           /* SDE_SRC_DT | SDE_SRC_DW, in dict order   */
-    int32_t term_register[2];         /* register holding each term's coefficient */
+    int32_t term_register[SDE_USER_MAX_EQ][2];   /* each term's coefficient      */
     uint32_t ops[SDE_USER_MAX_OPS];
     double consts[SDE_USER_MAX_CONSTS];
 } SdeUserProgram;

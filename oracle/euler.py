@@ -172,10 +172,12 @@ def shapes(preset, vshape, factors=1):
 
 def integrate(preset, params=None, timeline=(0., 1.), *, paths=1, vshape=(),
               steps=None, i0=0, dtype=None, corr=None, dw=None, dj=None,
-              rng=None, getinfo=True, sde=None, log_flag=False):
+              rng=None, getinfo=True, sde=None, log_flag=False, sde_q=0, addaxis=False):
     """Integrate one preset, or (preset 'user') the SDE function ``sde(t,
     x, **params)`` of sdepy's integrate decorator, in log space when
-    ``log_flag`` (sdepy/integration.py:1154-1197, 1843-1955).  ``dw`` /
+    ``log_flag`` (sdepy/integration.py:1154-1197, 1843-1955); ``sde_q`` > 0
+    makes it a system of that many equations, packed as sdepy's SDEs does
+    (``addaxis``, sdepy/integration.py:1680-1840).  ``dw`` /
     ``dj`` are source-protocol objects (e.g. Replay of recorded
     increments); when None they are realised with numpy from ``rng`` as
     sdepy's default sources do.  Returns (result, info) where result is an
@@ -185,7 +187,8 @@ def integrate(preset, params=None, timeline=(0., 1.), *, paths=1, vshape=(),
     if user:
         import inspect
         p = {'x0': 1.}
-        p.update({k: v.default for k, v in list(inspect.signature(sde).parameters.items())[2:]})
+        nv = 1 + max(sde_q, 1)
+        p.update({k: v.default for k, v in list(inspect.signature(sde).parameters.items())[nv:]})
     else:
         p = dict(DEFAULTS[preset])
     p.update(params or {})
@@ -194,6 +197,11 @@ def integrate(preset, params=None, timeline=(0., 1.), *, paths=1, vshape=(),
     P = {k: (v if k == 'factors' or callable(v) else np.asarray(v)) for k, v in p.items()}
     vshape = (vshape,) if isinstance(vshape, int) else tuple(vshape)
     xshape, wshape, addaxis = shapes(preset, vshape, p.get('factors', 1))
+    system = user and sde_q > 0
+    if system:   # SDEs.shapes (integration.py:1785-1792)
+        addaxis = addaxis or vshape == ()
+        wshape = vshape + (sde_q,) if addaxis else vshape[:-1] + (vshape[-1]*sde_q,)
+        xshape = wshape
     dtype = float if dtype is None else dtype
     jumps = 'jumpdiff' in preset
     heston = 'heston' in preset
@@ -204,11 +212,13 @@ def integrate(preset, params=None, timeline=(0., 1.), *, paths=1, vshape=(),
     if jumps and dj is None:
         dj = NumpyCPoisson(rng, paths, wshape, P['lam'], law_rvs(preset, p), dtype=dtype)
 
+    nq = sde_q if system else 2
+
     def unpack(X):
         if addaxis:
-            return X[..., 0, :], X[..., 1, :]
+            return tuple(X[..., e, :] for e in range(nq))
         d = vshape[-1]
-        return X[..., :d, :], X[..., d:, :]
+        return tuple(X[..., e*d:(e + 1)*d, :] for e in range(nq))
 
     def pack(xs):
         target = vshape + (paths,)
@@ -219,6 +229,10 @@ def integrate(preset, params=None, timeline=(0., 1.), *, paths=1, vshape=(),
 
     def sde(s, x):
         P = {k: (np.asarray(v(s)) if callable(v) else v) for k, v in P0.items()}
+        if system:   # SDEs.A (integration.py:1726-1744): pack the equations' terms
+            As = user_sde(s, *unpack(x), **{k: v for k, v in P.items() if k != 'x0'})
+            ids = [k for k in ('dt', 'dw') if any(k in z for z in As)]
+            return {i: pack(tuple(z.get(i, 0) for z in As)) for i in ids}
         if user:   # the function's own coefficients, its dict order kept
             return user_sde(s, x, **{k: v for k, v in P.items() if k != 'x0'})
         if preset == 'wiener_process':
@@ -248,6 +262,14 @@ def integrate(preset, params=None, timeline=(0., 1.), *, paths=1, vshape=(),
 
     def init(out_x):
         P = P0
+        if system:   # SDEs.init (integration.py:1794-1802)
+            x0s = P['x0']
+            if np.shape(x0s) == ():
+                x0s = (x0s,)*sde_q
+            out_x[...] = pack(tuple(x0s))
+            if log:
+                np.log(out_x, out=out_x)
+            return
         if heston:
             ox, oy = unpack(out_x)
             ox[...] = np.log(P['x0'])
@@ -312,6 +334,8 @@ def integrate(preset, params=None, timeline=(0., 1.), *, paths=1, vshape=(),
             info['jump_rate'][-1] = info['jump_rate'][-2]
     if log:
         np.exp(xx, out=xx)
+    if system:
+        return unpack(xx), info
     if preset == 'full_heston_process':
         a, b = unpack(xx)
         np.exp(a, out=a)

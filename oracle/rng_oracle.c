@@ -99,11 +99,13 @@ int oracle_cholesky(const double *C, int M, double *L) {
 static double np_maxd(double a, double b) { return (a != a) ? a : (b != b) ? b : (a >= b ? a : b); }
 static double np_mind(double a, double b) { return (a != a) ? a : (b != b) ? b : (a <= b ? a : b); }
 
-static void user_coefs(const SdeUserProgram *u, double x, double t, const double *p, double out[2]) {
+static void user_coefs(const SdeUserProgram *u, const double *xs, double t, const double *p,
+                       double out[][2]) {
     double r[SDE_USER_MAX_REGS] = {0};
-    r[0] = x;
+    r[0] = xs[0];
     r[1] = t;
     for (int i = 0; i < 6; ++i) r[2 + i] = p[i];
+    for (int e = 1; e < u->n_eq; ++e) r[7 + e] = xs[e];
     for (int i = 0; i < u->n_ops; ++i) {
         const uint32_t op = u->ops[i];
         const int c = op & 0xff, d = (op >> 8) & 0xff, ia = (op >> 16) & 0xff, ib = op >> 24;
@@ -137,8 +139,10 @@ static void user_coefs(const SdeUserProgram *u, double x, double t, const double
         }
         r[d] = v;
     }
-    out[0] = u->n_terms > 0 ? r[u->term_register[0]] : 0.0;
-    out[1] = u->n_terms > 1 ? r[u->term_register[1]] : 0.0;
+    for (int e = 0; e < u->n_eq; ++e) {
+        out[e][0] = u->n_terms > 0 ? r[u->term_register[e][0]] : 0.0;
+        out[e][1] = u->n_terms > 1 ? r[u->term_register[e][1]] : 0.0;
+    }
 }
 
 static double jump_size(int law, const uint32_t r[4], double a, double b, double pa) {
@@ -308,19 +312,28 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
                             const double drift = pp[0 * W + w] * (pp[1 * W + w] - st[m]);
                             st[m] = st[m] + (drift * dt + pp[2 * W + w] * dW[m]);
                         }
-                    } else if (s->model == SDE_MODEL_USER) {   /* sdepy/integration.py:707-718 */
-                        for (int m = 0; m < M; ++m) {
-                            const int w = gi * M + m;
-                            double pv[6], A[2];
-                            for (int i = 0; i < 6; ++i) pv[i] = pp[i * W + w];
-                            user_coefs(s->program, st[m], g->tt[k], pv, A);
-                            double sum = 0.0;
-                            for (int i = 0; i < s->program->n_terms; ++i) {
-                                const double term = A[i] * (s->program->term_source[i] == SDE_SRC_DT ? dt : dW[m]);
-                                sum = i == 0 ? term : sum + term;
+                    } else if (s->model == SDE_MODEL_USER) {   /* sdepy/integration.py:707-718, 1711-1783 */
+                        /* per component h: the states of the q equations
+                         * (equation e's component h at e * nc + h) */
+                        const int q = s->program->n_eq, nc = M / q;
+                        double nx[SDE_MAX_GROUP];
+                        for (int h = 0; h < nc; ++h) {
+                            double pv[6], xs[SDE_USER_MAX_EQ], A[SDE_USER_MAX_EQ][2];
+                            for (int i = 0; i < 6; ++i) pv[i] = pp[i * W + gi * M + h];
+                            for (int e = 0; e < q; ++e) xs[e] = st[e * nc + h];
+                            user_coefs(s->program, xs, g->tt[k], pv, A);
+                            for (int e = 0; e < q; ++e) {
+                                const int m = e * nc + h;
+                                double sum = 0.0;
+                                for (int i = 0; i < s->program->n_terms; ++i) {
+                                    const double term =
+                                        A[e][i] * (s->program->term_source[i] == SDE_SRC_DT ? dt : dW[m]);
+                                    sum = i == 0 ? term : sum + term;
+                                }
+                                nx[m] = st[m] + sum;
                             }
-                            st[m] = st[m] + sum;
                         }
+                        for (int m = 0; m < M; ++m) st[m] = nx[m];
                     } else if (s->model == SDE_MODEL_CIR) {   /* sdepy/integration.py:2350-2354 */
                         for (int m = 0; m < M; ++m) {
                             const int w = gi * M + m;

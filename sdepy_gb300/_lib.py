@@ -23,7 +23,7 @@ OK, ERR_INVALID, ERR_UNSUPPORTED, ERR_CUDA, ERR_DEVICE, ERR_NO_DEVICE = \
 
 MODEL_LINEAR, MODEL_OU, MODEL_HESTON, MODEL_CIR, MODEL_USER = 0, 1, 2, 3, 4
 # user SDE programs (SdeUserProgram)
-USER_MAX_OPS, USER_MAX_CONSTS, USER_MAX_REGS = 64, 16, 48
+USER_MAX_OPS, USER_MAX_CONSTS, USER_MAX_REGS, USER_MAX_EQ = 64, 16, 48, 8
 SRC_DT, SRC_DW = 0, 1
 (UOP_CONST, UOP_ADD, UOP_SUB, UOP_MUL, UOP_DIV, UOP_NEG, UOP_ABS, UOP_EXP, UOP_LOG, UOP_SQRT,
  UOP_MAX, UOP_MIN, UOP_SIN, UOP_COS, UOP_TAN, UOP_TANH, UOP_POW, UOP_EXPM1, UOP_LOG1P,
@@ -39,8 +39,8 @@ _lp = C.POINTER(C.c_int64)
 
 
 class SdeUserProgram(C.Structure):
-    _fields_ = [('n_ops', C.c_int32), ('n_terms', C.c_int32),
-                ('term_source', C.c_int32*2), ('term_register', C.c_int32*2),
+    _fields_ = [('n_ops', C.c_int32), ('n_eq', C.c_int32), ('n_terms', C.c_int32),
+                ('term_source', C.c_int32*2), ('term_register', (C.c_int32*2)*8),
                 ('ops', C.c_uint32*64), ('consts', C.c_double*16)]
 
 

@@ -285,10 +285,16 @@ static int check_spec(const SdeSpec *s, int *opg) {
         if (!u) return fail(SDE_ERR_INVALID, "a user SDE needs its program");
         if (u->n_ops < 0 || u->n_ops > SDE_USER_MAX_OPS) return fail(SDE_ERR_INVALID, "user program: n_ops");
         if (u->n_terms < 0 || u->n_terms > 2) return fail(SDE_ERR_INVALID, "user program: n_terms");
-        for (int i = 0; i < u->n_terms; ++i)
-            if ((u->term_source[i] != SDE_SRC_DT && u->term_source[i] != SDE_SRC_DW) || u->term_register[i] < 0 ||
-                u->term_register[i] >= SDE_USER_MAX_REGS)
+        if (u->n_eq < 1 || u->n_eq > SDE_USER_MAX_EQ || s->group_size % u->n_eq)
+            return fail(SDE_ERR_INVALID, "user program: %d equations in groups of %d", u->n_eq, s->group_size);
+        if (u->n_eq > 1 && s->group_size < 2) return fail(SDE_ERR_INVALID, "user program: system groups");
+        for (int i = 0; i < u->n_terms; ++i) {
+            if (u->term_source[i] != SDE_SRC_DT && u->term_source[i] != SDE_SRC_DW)
                 return fail(SDE_ERR_INVALID, "user program: term %d", i);
+            for (int e = 0; e < u->n_eq; ++e)
+                if (u->term_register[e][i] < 0 || u->term_register[e][i] >= SDE_USER_MAX_REGS)
+                    return fail(SDE_ERR_INVALID, "user program: term %d of equation %d", i, e);
+        }
         for (int i = 0; i < u->n_ops; ++i) {
             const uint32_t op = u->ops[i];
             const uint32_t code = op & 0xff, d = (op >> 8) & 0xff, ra = (op >> 16) & 0xff, rb = op >> 24;
@@ -362,7 +368,8 @@ static int maxm_of(int M) {
 template <typename R> struct Finder;
 template <> struct Finder<double> {
     static FwdLauncher<double> find(int model, int maxm, bool inj, bool jmp, int *bps) {
-        if (model == SDE_MODEL_USER) return jmp ? nullptr : find_fwd_f64_user(maxm, inj, bps);
+        if (model == SDE_MODEL_USER || model == SDE_MODEL_USER_SYS)
+            return jmp ? nullptr : find_fwd_f64_user(maxm, inj, model == SDE_MODEL_USER_SYS, bps);
         if (model == SDE_MODEL_CIR) return jmp ? nullptr : find_fwd_f64_cir(maxm, inj, false, bps);
         FwdLauncher<double> f = find_fwd_f64_linear(model, maxm, inj, jmp, bps);
         return f ? f : find_fwd_f64_ou_heston(model, maxm, inj, jmp, bps);
@@ -375,7 +382,8 @@ template <> struct Finder<double> {
 };
 template <> struct Finder<float> {
     static FwdLauncher<float> find(int model, int maxm, bool inj, bool jmp, int *bps) {
-        if (model == SDE_MODEL_USER) return jmp ? nullptr : find_fwd_f32_user(maxm, inj, bps);
+        if (model == SDE_MODEL_USER || model == SDE_MODEL_USER_SYS)
+            return jmp ? nullptr : find_fwd_f32_user(maxm, inj, model == SDE_MODEL_USER_SYS, bps);
         if (model == SDE_MODEL_CIR) return jmp ? nullptr : find_fwd_f32_cir(maxm, inj, false, false, bps);
         FwdLauncher<float> f = find_fwd_f32_linear(model, maxm, inj, jmp, bps);
         return f ? f : find_fwd_f32_ou_heston(model, maxm, inj, jmp, bps);
@@ -777,7 +785,8 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
                                  ((nprmt && (s->model == SDE_MODEL_HESTON || s->model == SDE_MODEL_CIR)) ||
                                   corr_steps));
     // (user-SDE kernels reload per-step parameters and factors in every form)
-    FwdLauncher<R> L = user     ? Finder<R>::find(s->model, maxm_of(M), inject, jumps, &bps)
+    const int kmodel = user && s->program->n_eq > 1 ? SDE_MODEL_USER_SYS : s->model;
+    FwdLauncher<R> L = user     ? Finder<R>::find(kmodel, maxm_of(M), inject, jumps, &bps)
                        : anti   ? Finder<R>::find_anti(s->model, maxm_of(M), jumps, tdep_k, &bps)
                        : tdep_k ? Finder<R>::find_tdep(s->model, maxm_of(M), &bps)
                                 : Finder<R>::find(s->model, maxm_of(M), inject, jumps, &bps);

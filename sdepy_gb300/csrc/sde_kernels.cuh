@@ -620,15 +620,19 @@ __device__ __forceinline__ R np_max(R a, R b) { return (a != a) ? a : (b != b) ?
 template <typename R>
 __device__ __forceinline__ R np_min(R a, R b) { return (a != a) ? a : (b != b) ? b : (a <= b ? a : b); }
 
+// xs[0..q-1]: the states of one component in the q equations (q = 1 for a
+// single SDE); out[e][j]: the coefficient of term j of equation e
 template <typename R>
-__device__ __noinline__ void user_coefs(const SdeUserProgram &u, R x, R t, const R (&p)[6], R (&out)[2]) {
+__device__ __noinline__ void user_coefs(const SdeUserProgram &u, const R *xs, R t, const R (&p)[6],
+                                        R (*out)[2]) {
     typedef Ar<R> A;
     typedef UFn<R> F;
     R r[SDE_USER_MAX_REGS];
-    r[0] = x;
+    r[0] = xs[0];
     r[1] = t;
 #pragma unroll
     for (int i = 0; i < 6; ++i) r[2 + i] = p[i];
+    for (int e = 1; e < u.n_eq; ++e) r[7 + e] = xs[e];
     for (int i = 0; i < u.n_ops; ++i) {
         const uint32_t op = u.ops[i];
         const int d = (op >> 8) & 0xff, ia = (op >> 16) & 0xff, ib = op >> 24;
@@ -663,9 +667,15 @@ __device__ __noinline__ void user_coefs(const SdeUserProgram &u, R x, R t, const
         }
         r[d] = v;
     }
-    out[0] = u.n_terms > 0 ? r[u.term_register[0]] : R(0);
-    out[1] = u.n_terms > 1 ? r[u.term_register[1]] : R(0);
+    for (int e = 0; e < u.n_eq; ++e) {
+        out[e][0] = u.n_terms > 0 ? r[u.term_register[e][0]] : R(0);
+        out[e][1] = u.n_terms > 1 ? r[u.term_register[e][1]] : R(0);
+    }
 }
+
+// the internal kernel model of user SDE systems (q > 1: SdeSpec.model is
+// SDE_MODEL_USER, the program's n_eq selects these instantiations)
+constexpr int SDE_MODEL_USER_SYS = 16;
 
 // ---------------------------------------------------------------------------
 // the forward kernel
@@ -678,7 +688,7 @@ template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS, bool ANTI = 
 struct FwdOccupancy {
     static constexpr int CAP_M = (MODEL == SDE_MODEL_HESTON || MODEL == SDE_MODEL_CIR ? 4 : 8) / (ANTI ? 2 : 1);
     static constexpr int MIN_BLOCKS =
-        (sizeof(R) == 4 && MAXM <= CAP_M && !INJECT && !JUMPS && MODEL != SDE_MODEL_USER) ? 3 : 1;
+        (sizeof(R) == 4 && MAXM <= CAP_M && !INJECT && !JUMPS && MODEL != SDE_MODEL_USER && MODEL < 8) ? 3 : 1;
 };
 
 // TDEP: time-dependent-coefficient instantiations of the FP32 device-noise
@@ -701,7 +711,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     constexpr bool TDB = TDEP && SHIFT;   // OU rows with the time-dependent-theta term
     // per-step coefficient reloads compiled in (the non-table kernels but
     // the common FP32 Heston and CIR ones)
-    constexpr bool USER = MODEL == SDE_MODEL_USER;
+    constexpr bool USER = MODEL == SDE_MODEL_USER || MODEL == SDE_MODEL_USER_SYS;
     constexpr bool RELOAD = !TAB && (sizeof(R) == 8 || INJECT || TDEP || USER);
     // per-step correlation factors compiled in (the same kernels, TAB ones
     // included, with device noise)
@@ -1020,16 +1030,53 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
 #pragma unroll
                         for (int m = 0; m < MAXM; ++m) {
                             const R pv[6] = {c0[m], c1[m], c2[m], c3[m], c4[m], c5[m]};
-                            R A2[2];
-                            user_coefs<R>(a.uprog, st[m], tk, pv, A2);
+                            R A2[1][2];
+                            const R xm[1] = {st[m]};
+                            user_coefs<R>(a.uprog, xm, tk, pv, A2);
                             R s = R(0);
                             for (int i = 0; i < a.uprog.n_terms; ++i) {
                                 const R dz = a.uprog.term_source[i] == SDE_SRC_DT ? dt : dW[m];
-                                const R term = A::mul(A2[i], dz);
+                                const R term = A::mul(A2[0][i], dz);
                                 s = i == 0 ? term : A::add(s, term);
                             }
                             st[m] = A::add(st[m], s);
                         }
+                    } else if (MODEL == SDE_MODEL_USER_SYS) {
+                        // the group is one last-axis slice: equation e's component
+                        // h at e * nc + h; the program runs per component on the
+                        // states of every equation, then all states step at once
+                        const int q = a.uprog.n_eq, nc = M / q;
+                        R sv[MAXM], dv[MAXM], nx[MAXM];
+#pragma unroll
+                        for (int m = 0; m < MAXM; ++m) {
+                            sv[m] = st[m];
+                            dv[m] = dW[m];
+                            nx[m] = st[m];
+                        }
+                        for (int h = 0; h < nc; ++h) {
+                            R xs[SDE_USER_MAX_EQ], A2[SDE_USER_MAX_EQ][2];
+                            for (int e = 0; e < q; ++e) xs[e] = sv[e * nc + h];
+                            // parameters broadcast along the equations: component h's
+                            R pv[6];
+                            for (int m = 0; m < MAXM; ++m)
+                                if (m == h) {
+                                    pv[0] = c0[m], pv[1] = c1[m], pv[2] = c2[m];
+                                    pv[3] = c3[m], pv[4] = c4[m], pv[5] = c5[m];
+                                }
+                            user_coefs<R>(a.uprog, xs, tk, pv, A2);
+                            for (int e = 0; e < q; ++e) {
+                                const int m = e * nc + h;
+                                R s = R(0);
+                                for (int i = 0; i < a.uprog.n_terms; ++i) {
+                                    const R dz = a.uprog.term_source[i] == SDE_SRC_DT ? dt : dv[m];
+                                    const R term = A::mul(A2[e][i], dz);
+                                    s = i == 0 ? term : A::add(s, term);
+                                }
+                                nx[m] = A::add(sv[m], s);
+                            }
+                        }
+#pragma unroll
+                        for (int m = 0; m < MAXM; ++m) st[m] = nx[m];
                     } else if (MODEL == SDE_MODEL_CIR) {   // k*(theta - x+), xi*sqrt(x+)
 #pragma unroll
                         for (int m = 0; m < MAXM; ++m) {
@@ -1174,9 +1221,10 @@ FwdLauncher<float> find_fwd_f32_tdep(int model, int maxm, int *bps);
 // CIR kernels (fwd_cir.cu): plain, time-dependent (FP32), antithetic
 FwdLauncher<float> find_fwd_f32_cir(int maxm, bool inject, bool tdep, bool anti, int *bps);
 FwdLauncher<double> find_fwd_f64_cir(int maxm, bool inject, bool anti, int *bps);
-// user-SDE kernels (fwd_user.cu): device or injected noise
-FwdLauncher<float> find_fwd_f32_user(int maxm, bool inject, int *bps);
-FwdLauncher<double> find_fwd_f64_user(int maxm, bool inject, int *bps);
+// user-SDE kernels (fwd_user_*.cu): device or injected noise; sys: systems
+// of equations (SDE_MODEL_USER_SYS)
+FwdLauncher<float> find_fwd_f32_user(int maxm, bool inject, bool sys, int *bps);
+FwdLauncher<double> find_fwd_f64_user(int maxm, bool inject, bool sys, int *bps);
 // antithetic kernels (device noise, groups of up to 8 states)
 FwdLauncher<float> find_fwd_f32_anti(int model, int maxm, bool jumps, int *bps);
 // FP32 antithetic kernels with per-step coefficients and correlation factors

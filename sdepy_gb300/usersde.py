@@ -13,14 +13,15 @@ terms in the order of the returned dict, as sdepy's ``euler_next`` does
 of roundings.
 
 Supported (no CPU fallback -- anything else raises NotImplementedError at
-decoration): one equation driven by 'dt' and / or 'dw'; up to 6 parameters,
+decoration): one equation, or a system of up to 8 (``q``, sdepy's SDEs),
+driven by 'dt' and / or 'dw'; up to 6 parameters,
 constant or functions / processes of t, per state variable; +, -, *, /,
 unary -, abs, ** (numpy's fast forms for the exponents 2, 0.5, -1, 1, 0),
 and numpy's exp, log, sqrt, maximum, minimum, sin, cos, tan, tanh, power,
 expm1, log1p, arctan, square, absolute, negative; correlated Wiener
 increments through ``corr`` / ``rho``; the ``log`` flag.  Control flow on the
-state (``if x > 0``, Python's ``max``), systems of SDEs (q > 0) and other
-sources (jumps) are refused.
+state (``if x > 0``, Python's ``max``) and other sources (jumps) are
+refused.
 """
 import ctypes as C
 import inspect
@@ -29,6 +30,7 @@ import numbers
 import numpy as np
 
 from . import _lib
+from .infrastructure import process
 from .integration import _const, _gpu_process, _per_var
 
 _MAX_PARAMS = 6
@@ -181,35 +183,49 @@ class _Sym:
     __hash__ = object.__hash__
 
 
-def compile_sde(f, pnames):
-    """SdeUserProgram of ``f(t, x, **params)`` with parameters ``pnames``
-    (registers r2...), and the recorded program for inspection."""
+def compile_sde(f, pnames, q=0):
+    """SdeUserProgram of ``f(t, x, **params)`` (``q`` = 0), or of a system
+    ``f(t, x, y, ..., **params)`` of ``q`` equations returning one dict per
+    equation, with parameters ``pnames`` (registers r2..r7; the states of
+    equations 1.. in r8...), and the recorded program for inspection."""
     prog = _Program()
-    x, t = _Sym(prog, 0), _Sym(prog, 1)
+    neq = max(q, 1)
+    if neq > _lib.USER_MAX_EQ:
+        raise NotImplementedError('systems of more than {} equations'.format(_lib.USER_MAX_EQ))
+    prog.nreg = 7 + neq if neq > 1 else 8   # temporaries after the inputs
+    xs = [_Sym(prog, 0)] + [_Sym(prog, 7 + e) for e in range(1, neq)]
+    t = _Sym(prog, 1)
     params = {n: _Sym(prog, 2 + i) for i, n in enumerate(pnames)}
     try:
-        A = f(t, x, **params)
+        A = f(t, *xs, **params)
     except NotImplementedError:
         raise
     except Exception as e:
         raise NotImplementedError('the SDE function {!r} cannot be traced for the GPU: {}: {}'
                                   .format(getattr(f, '__name__', f), type(e).__name__, e))
-    if not isinstance(A, dict):
-        raise NotImplementedError('the SDE function must return a dict of coefficients')
+    As = (A,) if q == 0 else tuple(A) if isinstance(A, (tuple, list)) else None
+    if As is None or len(As) != neq or not all(isinstance(z, dict) for z in As):
+        raise NotImplementedError('the SDE function must return {}'.format(
+            'a dict of coefficients' if q == 0 else 'one dict of coefficients per equation'))
     srcs = {'dt': _lib.SRC_DT, 'dw': _lib.SRC_DW}
-    terms = []
-    for k, v in A.items():
-        if k not in srcs:
-            raise NotImplementedError('source {!r} is not supported by the GPU integrator of user '
-                                      'SDEs (dt and dw are)'.format(k))
-        reg = v.reg if isinstance(v, _Sym) else prog.const(v).reg
-        terms.append((srcs[k], reg))
+    for z in As:
+        for k in z:
+            if k not in srcs:
+                raise NotImplementedError('source {!r} is not supported by the GPU integrator of '
+                                          'user SDEs (dt and dw are)'.format(k))
+    if q == 0:
+        order = list(As[0])          # the dict's order: the Euler sum's
+    else:                            # sdepy packs the union of the equations' ids;
+        order = [k for k in ('dt', 'dw') if any(k in z for z in As)]   # 2 terms commute
     u = _lib.SdeUserProgram()
+    u.n_eq = neq
+    u.n_terms = len(order)
+    for i, k in enumerate(order):
+        u.term_source[i] = srcs[k]
+        for e, z in enumerate(As):
+            v = z.get(k, 0.)     # a missing term has coefficient 0 (a.get(id, 0))
+            u.term_register[e][i] = v.reg if isinstance(v, _Sym) else prog.const(v).reg
     u.n_ops = len(prog.ops)
-    u.n_terms = len(terms)
-    for i, (s, r) in enumerate(terms):
-        u.term_source[i] = s
-        u.term_register[i] = r
     for i, op in enumerate(prog.ops):
         u.ops[i] = op
     for i, c in enumerate(prog.consts):
@@ -217,14 +233,14 @@ def compile_sde(f, pnames):
     return u, prog
 
 
-def _sde_parameters(f):
-    """Parameters of ``f`` after (t, x), with their defaults (sdepy's
+def _sde_parameters(f, nvars=1):
+    """Parameters of ``f`` after (t, x, ...), with their defaults (sdepy's
     _inspect_args_defaults, sdepy/integration.py:986-1055)."""
     ps = list(inspect.signature(f).parameters.values())
-    if len(ps) < 2:
-        raise TypeError('the SDE function takes (t, x, **params)')
+    if len(ps) < 1 + nvars:
+        raise TypeError('the SDE function takes (t, x, ..., **params)')
     out = {}
-    for p in ps[2:]:
+    for p in ps[1 + nvars:]:
         if p.kind not in (p.POSITIONAL_OR_KEYWORD, p.KEYWORD_ONLY):
             raise NotImplementedError('variable arguments of the SDE function')
         out[p.name] = None if p.default is p.empty else p.default
@@ -252,6 +268,65 @@ class _user_process(_gpu_process):
         s = super()._make_spec(seed, stream)
         s.program = C.pointer(self._program)
         return s
+
+
+class _user_sys_process(_user_process):
+    """A process class made by ``integrate`` from a system of SDEs
+    (sdepy's SDEs, sdepy/integration.py:1548-1840): the q equations are
+    packed along the last axis of the working shape (``addaxis``: a new
+    axis of q; else stacked, equation e's components at e*N..(e+1)*N-1),
+    one group per last-axis slice; the result is a tuple of q processes."""
+    _q = 2
+
+    def shapes(self, vshape):
+        q = self._q
+        self.addaxis = self._addaxis_flag or vshape == ()
+        if self.addaxis:
+            ws = vshape + (q,)
+        else:
+            ws = vshape[:-1] + (vshape[-1]*q,)
+        return vshape, ws, ws
+
+    def _groups(self):
+        M = self.wshape[-1]
+        if M > _lib.MAX_GROUP:
+            raise NotImplementedError('systems whose last working axis exceeds {} are not supported '
+                                      'by the GPU integrator'.format(_lib.MAX_GROUP))
+        return self._W // M, M
+
+    def _pack(self, xs, name):
+        """Per-state values of the working shape from q per-component
+        values (sdepy's SDEs.pack), each constant along the paths."""
+        vs = [_per_var(_const(x, name), self.vshape, self.paths, name).reshape(self.vshape)
+              for x in xs]
+        if self.addaxis:
+            return np.stack(vs, axis=-1).reshape(-1)
+        return np.concatenate(vs, axis=-1).reshape(-1)
+
+    def _coefficients(self, t=1., tmid=1.):
+        q = self._q
+        x0 = np.asarray(self._args['x0'], dtype=float) if not callable(self._args['x0']) else None
+        if x0 is None:
+            raise NotImplementedError('time-dependent initial values are not supported')
+        x0s = (x0,)*q if x0.shape == () else tuple(x0)   # sdepy's SDEs.init
+        if len(x0s) != q:
+            raise ValueError('x0 should give {} initial conditions'.format(q))
+        x0v = self._pack(x0s, 'x0')
+        if self._log:
+            x0v = np.log(x0v)
+        prm = np.zeros((_lib.MAX_PARAMS, self._W))
+        for i, n in enumerate(self._pnames):
+            prm[i] = self._pack((self._p(n, t),)*q, n)
+        return np.ascontiguousarray(x0v), np.ascontiguousarray(prm)
+
+    def exit(self, tt, xx):
+        q = self._q
+        if self.addaxis:
+            xs = tuple(xx[..., e, :] for e in range(q))
+        else:
+            d = self.vshape[-1]
+            xs = tuple(xx[..., e*d:(e + 1)*d, :] for e in range(q))
+        return tuple(process(tt, x=np.ascontiguousarray(x)) for x in xs)
 
 
 def integrate(sde=None, *, q=None, sources=None, log=False, addaxis=False):
@@ -288,22 +363,23 @@ def integrate(sde=None, *, q=None, sources=None, log=False, addaxis=False):
         if (q is not None and neq != q) or (sources is not None and set(sources) != ids):
             raise TypeError("test evaluation of {} inconsistent with given 'q' or 'sources'"
                             .format(sde))
-    if neq != 0:
-        raise NotImplementedError('systems of SDEs (q = {}) are not supported by the GPU '
-                                  'integrator'.format(neq))
+    if neq > _lib.USER_MAX_EQ:
+        raise NotImplementedError('systems of more than {} equations are not supported by the GPU '
+                                  'integrator'.format(_lib.USER_MAX_EQ))
     if not ids <= {'dt', 'dw'}:
         raise NotImplementedError('sources {} are not supported by the GPU integrator of user '
                                   'SDEs (dt and dw are)'.format(sorted(ids - {'dt', 'dw'})))
-    defaults = _sde_parameters(sde)
+    defaults = _sde_parameters(sde, max(neq, 1))
     if len(defaults) > _MAX_PARAMS:
         raise NotImplementedError('user SDEs take at most {} parameters on the GPU, not {}'
                                   .format(_MAX_PARAMS, len(defaults)))
     pnames = tuple(defaults)
-    program, _ = compile_sde(sde, pnames)
+    program, _ = compile_sde(sde, pnames, neq)
     params = {'x0': 1.}
     params.update(defaults)
     attrs = dict(_params=params, _pnames=pnames, _tdep_names=pnames, _program=program,
                  _log=bool(log), _out=_lib.OUT_EXP if log else _lib.OUT_STATE,
-                 sde=staticmethod(sde), q=0, sources_ids=frozenset(ids), addaxis=bool(addaxis),
-                 __doc__=sde.__doc__)
-    return type(getattr(sde, '__name__', 'sde_integrator'), (_user_process,), attrs)
+                 sde=staticmethod(sde), q=neq, sources_ids=frozenset(ids), addaxis=bool(addaxis),
+                 _addaxis_flag=bool(addaxis), _q=max(neq, 1), __doc__=sde.__doc__)
+    base = _user_process if neq == 0 else _user_sys_process
+    return type(getattr(sde, '__name__', 'sde_integrator'), (base,), attrs)

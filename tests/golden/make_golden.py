@@ -329,6 +329,13 @@ def user_cases(sdepy):
          seed=65)
     case('cir_tdep', 'integrate:user_cir', dict(x0=.04, k=1.5, theta=H.tdep_theta_h, xi=H.tdep_xi), (0., .5, 1.),
          (), paths=40, steps=50, seed=66)
+    # systems (sdepy's SDEs): scalar components (an added axis of 2), and a
+    # vector of 2 components per equation stacked along the last axis
+    case('sys_sv', 'integrate_q2:user_sv', dict(x0=(100., .04), mu=.05, k=1.5, theta=.04, xi=.5, rho=-.7),
+         (0., .5, 1.), (2,), paths=40, steps=50, rho=-.7, seed=67)
+    case('sys_coupled_vec', 'integrate_q2:user_coupled', dict(vshape=2, x0=(.5, -.2), a=[[1.], [2.]], b=.5, c=.3,
+                                                               s=[[.2], [.1]]),
+         np.linspace(0, 2, 3), (4,), paths=32, steps=40, i0=1, seed=68)
 
 
 def main():

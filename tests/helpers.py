@@ -239,14 +239,29 @@ def user_cir(t, x, k=1., theta=1., xi=1.):
     return {'dt': k*(theta - xp), 'dw': xi*np.sqrt(xp)}
 
 
+def user_sv(t, x, y, mu=.05, k=1.5, theta=.04, xi=.5):
+    # a system of two equations: price and variance, full truncation
+    yp = np.maximum(y, 0.)
+    return ({'dt': mu*x, 'dw': np.sqrt(yp)*x}, {'dt': k*(theta - yp), 'dw': xi*np.sqrt(yp)})
+
+
+def user_coupled(t, x, y, a=1., b=.5, c=.3, s=.2):
+    # two coupled OU-like equations, the second without a Wiener term
+    return ({'dt': -a*x + b*y, 'dw': s}, {'dt': c*x - a*y})
+
+
 USER = {name: f for name, f in dict(globals()).items() if name.startswith('user_')}
 
 
 def user_class(module, spec):
-    """The process class of a fixture's ``cls`` entry 'integrate:<function>'
-    or 'integrate_log:<function>', made by ``module.integrate``."""
+    """The process class of a fixture's ``cls`` entry '<kind>:<function>',
+    made by ``module.integrate``: kind is 'integrate' with optional '_log'
+    (log=True), '_q<n>' (a system of n equations) and '_addaxis'."""
     kind, name = spec.split(':')
-    return module.integrate(USER[name], log=kind == 'integrate_log')
+    parts = kind.split('_')
+    q = next((int(x[1:]) for x in parts if x.startswith('q')), None)
+    return module.integrate(USER[name], q=q, sources={'dt', 'dw'} if q else None, log='log' in parts,
+                            addaxis='addaxis' in parts)
 
 
 def tdep_kwargs(z, process_cls):

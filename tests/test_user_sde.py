@@ -27,9 +27,10 @@ from oracle import euler
 CASES = sorted(glob.glob(os.path.join(GOLDEN, 'user_*.npz')))
 
 
-def _run_program(u, x, t, params):
+def _run_program(u, x, t, params, ys=()):
     """The program's value with numpy, op by op (registers r0 = x, r1 = t,
-    r2.. = parameters)."""
+    r2.. = parameters, r8.. = the states of equations 1.. of a system);
+    the terms of every equation."""
     ops = {_lib.UOP_ADD: np.add, _lib.UOP_SUB: np.subtract, _lib.UOP_MUL: np.multiply,
            _lib.UOP_DIV: np.true_divide, _lib.UOP_MAX: np.maximum, _lib.UOP_MIN: np.minimum,
            _lib.UOP_POW: np.power}
@@ -40,6 +41,8 @@ def _run_program(u, x, t, params):
     r = {0: x, 1: t}
     for i, p in enumerate(params):
         r[2 + i] = p
+    for e, y in enumerate(ys):
+        r[8 + e] = y
     for op in u.ops[:u.n_ops]:
         code, d, a, b = op & 0xff, (op >> 8) & 0xff, (op >> 16) & 0xff, op >> 24
         if code == _lib.UOP_CONST:
@@ -48,23 +51,32 @@ def _run_program(u, x, t, params):
             r[d] = ops[code](r[a], r[b])
         else:
             r[d] = un[code](r[a])
-    return [r[u.term_register[i]] for i in range(u.n_terms)], [u.term_source[i] for i in range(u.n_terms)]
+    return ([[r[u.term_register[e][i]] for i in range(u.n_terms)] for e in range(u.n_eq)],
+            [u.term_source[i] for i in range(u.n_terms)])
 
 
 @pytest.mark.parametrize('name', sorted(USER))
 def test_program_equals_function(name):
+    import inspect
     f = USER[name]
-    cls = sg.integrate(f)
+    nvars = sum(p.default is p.empty for p in inspect.signature(f).parameters.values()) - 1
+    q = nvars if nvars > 1 else None
+    cls = sg.integrate(f, q=q, sources={'dt', 'dw'} if q else None)
     g = np.random.default_rng(1)
-    x = np.abs(g.normal(size=1000)) + .01
+    xs = [np.abs(g.normal(size=1000)) + .01 for _ in range(nvars)]
     t = .37
     params = [np.float64(v) for v in cls._params.values()][1:]   # defaults, x0 excluded
-    got, srcs = _run_program(cls._program, x, np.float64(t), params)
+    got, srcs = _run_program(cls._program, xs[0], np.float64(t), params, xs[1:])
     with np.errstate(all='ignore'):
-        A = f(t, x, **dict(zip(cls._pnames, params)))
-    assert [{'dt': 0, 'dw': 1}[k] for k in A] == srcs
-    for v, (k, ref) in zip(got, A.items()):
-        np.testing.assert_array_equal(np.broadcast_to(v, x.shape), np.broadcast_to(ref, x.shape), err_msg=k)
+        As = f(t, *xs, **dict(zip(cls._pnames, params)))
+    As = As if q else (As,)
+    keys = [{0: 'dt', 1: 'dw'}[s] for s in srcs]
+    if not q:
+        assert keys == list(As[0])   # the dict's order
+    for vals, A in zip(got, As):
+        for v, k in zip(vals, keys):
+            np.testing.assert_array_equal(np.broadcast_to(v, xs[0].shape),
+                                          np.broadcast_to(A.get(k, 0.), xs[0].shape), err_msg=k)
 
 
 def test_tracer_forms_and_refusals():
@@ -85,10 +97,10 @@ def test_tracer_forms_and_refusals():
         @sg.integrate
         def b3(t, x, a=1.):
             return {'dt': a, 'dw': 1., 'dj': 1.}
-    with pytest.raises(NotImplementedError):       # a system of SDEs
-        @sg.integrate(q=2, sources={'dt', 'dw'})
-        def b4(t, x, y, a=1.):
-            return ({'dt': a, 'dw': 1.}, {'dt': a, 'dw': 1.})
+    with pytest.raises(NotImplementedError):       # a system of nine equations
+        @sg.integrate(q=9, sources={'dt', 'dw'})
+        def b4(t, x, *ys, a=1.):
+            return ({'dt': a, 'dw': 1.},)*9
     with pytest.raises(NotImplementedError):       # seven parameters
         @sg.integrate
         def b5(t, x, a=1., b=1., c=1., d=1., e=1., f=1., g=1.):
@@ -109,17 +121,30 @@ def _fixture_args(z):
     return kw, vshape, paths
 
 
+def _spec(z):
+    kind, name = str(z['cls']).split(':')
+    parts = kind.split('_')
+    q = next((int(x[1:]) for x in parts if x.startswith('q')), 0)
+    return name, q, 'log' in parts, 'addaxis' in parts
+
+
+def _outputs(out):
+    return out if isinstance(out, tuple) else (out,)
+
+
 @pytest.mark.parametrize('path', CASES, ids=os.path.basename)
 def test_numpy_oracle_reproduces_reference(path):
     z = np.load(path)
     kw, vshape, paths = _fixture_args(z)
     kw.pop('corr', None)
-    kind, name = str(z['cls']).split(':')
+    kw.pop('rho', None)   # in the recorded increments
+    name, q, log, addaxis = _spec(z)
     dw = euler.Replay(z['rec_dw'], paths=paths, vshape=z['rec_dw'].shape[1:-1])
     res, info = euler.integrate('user', kw, z['timeline'], paths=paths, vshape=vshape,
                                 steps=json.loads(str(z['steps'])), i0=int(z['i0']), dw=dw,
-                                sde=USER[name], log_flag=kind == 'integrate_log')
-    np.testing.assert_array_equal(res, z['xx0'])
+                                sde=USER[name], log_flag=log, sde_q=q, addaxis=addaxis)
+    for k, o in enumerate(_outputs(res)):
+        np.testing.assert_array_equal(o, z['xx%d' % k])
     assert info['computed_steps'] == int(z['computed_steps'])
 
 
@@ -131,10 +156,13 @@ def test_gpu_replay_matches_reference(lib, path):
     cls = user_class(sg, str(z['cls']))
     dw = euler.Replay(z['rec_dw'], paths=paths, vshape=z['rec_dw'].shape[1:-1])
     P = cls(paths=paths, vshape=vshape, steps=json.loads(str(z['steps'])), i0=int(z['i0']), dw=dw, **kw)
-    x = P(z['timeline'])
-    ref = z['xx0']
-    err = np.max(np.abs(np.asarray(x) - ref)/np.maximum(np.abs(ref), 1.))
-    assert err <= 1e-12, err
+    outs = _outputs(P(z['timeline']))
+    assert len(outs) == int(z['n_out'])
+    for k, x in enumerate(outs):
+        ref = z['xx%d' % k]
+        assert x.shape == ref.shape
+        err = np.max(np.abs(np.asarray(x) - ref)/np.maximum(np.abs(ref), 1.))
+        assert err <= 1e-12, err
     assert P.info['computed_steps'] == int(z['computed_steps'])
 
 
@@ -148,6 +176,12 @@ DEVICE_CASES = [
     ('mixed_vec3', 'integrate:user_mixed', dict(vshape=3, x0=[[.5], [0.], [-.5]], a=1.5, b=.7, s=.25),
      np.linspace(0, 2, 3), 50, 0),
     ('cir_tdep', 'integrate:user_cir', None, (0., .5, 1.), 50, 0),
+    ('sys_sv', 'integrate_q2:user_sv', dict(x0=(100., .04), mu=.05, k=1.5, theta=.04, xi=.5, rho=-.7),
+     (0., .5, 1.), 50, 0),
+    ('sys_coupled_vec', 'integrate_q2:user_coupled', dict(vshape=2, x0=(.5, -.2), a=[[1.], [2.]], s=[[.2], [.1]]),
+     np.linspace(0, 2, 3), 40, 1),
+    ('sys_coupled_addaxis', 'integrate_q2_addaxis:user_coupled', dict(vshape=3, x0=(.5, -.2), b=.4),
+     (0., 1.), 30, 0),
 ]
 
 
@@ -161,19 +195,20 @@ def test_device_rng_matches_c_oracle(lib, clib, case):
     cls = user_class(sg, spec)
     paths, seed = 777, 0x5eed
     P = cls(paths=paths, steps=steps, i0=i0, rng=sg.philox_rng(seed, 2), **kw)
-    out = np.asarray(P(tl))
-    got = out.reshape(len(tl), -1, paths)
+    outs = _outputs(P(tl))
     ref, _ = oracle_paths(clib, P, tl, seed, 2)
-    ref = ref.reshape(got.shape)
-    err = np.max(np.abs(got - ref)/np.maximum(np.abs(ref), 1.))
-    assert err <= 1e-12, err
+    refs = _outputs(P.exit(np.asarray(tl), ref))   # the oracle's working-shape rows, unpacked alike
+    for x, r in zip(outs, refs):
+        err = np.max(np.abs(np.asarray(x) - np.asarray(r))/np.maximum(np.abs(r), 1.))
+        assert err <= 1e-12, err
     P32 = cls(paths=paths, steps=steps, i0=i0, dtype=np.float32, rng=sg.philox_rng(seed, 2), **kw)
-    g32 = np.asarray(P32(tl), dtype=float).reshape(got.shape)
-    assert np.max(np.abs(g32 - ref)/np.maximum(np.abs(ref), 1.)) < 2e-3
-    # and the fused summary of the last row
-    x, mc = P.montecarlo(tl, bins=20, paths_out=True)
-    last = np.asarray(x[-1]).reshape(-1, paths)
-    np.testing.assert_allclose(np.asarray(mc.mean()).reshape(-1), last.mean(axis=-1), rtol=1e-12, atol=1e-15)
+    for x, r in zip(_outputs(P32(tl)), refs):
+        assert np.max(np.abs(np.asarray(x, dtype=float) - r)/np.maximum(np.abs(r), 1.)) < 2e-3
+    if len(outs) == 1:   # and the fused summary of the last row
+        x, mc = P.montecarlo(tl, bins=20, paths_out=True)
+        last = np.asarray(x[-1]).reshape(-1, paths)
+        np.testing.assert_allclose(np.asarray(mc.mean()).reshape(-1), last.mean(axis=-1), rtol=1e-12,
+                                   atol=1e-15)
 
 
 @pytest.mark.gpu
