@@ -718,6 +718,10 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     constexpr bool STEPCORR = !INJECT && (sizeof(R) == 8 || TDEP || USER);
     // parameter slots of a time-dependent table row (all six for USER)
     constexpr int NPT = USER ? 6 : 3;
+    // steps per iteration of the step loops: two, so that the next step's
+    // draws overlap this step's arithmetic (5-12% on the FP32 kernels), but
+    // one for the 8- and 16-wide time-dependent forms, which would spill
+    constexpr int UNROLL = (TDEP && MAXM >= 8) ? 1 : 2;
     __shared__ R red[BLOCK / 32];
     __shared__ double part[MAXM][NPART];
     __shared__ R svs[NA][MAXM][BLOCK];   // this round's value of each output at the stats row
@@ -942,7 +946,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                     // from L1 rather than held in registers across the run
                     constexpr int NB = TDB ? 3 : 2;   // coefficient vectors per row
                     const float *tb = a.coef + ((int64_t)run.w * a.groups + g) * NB * MAXM;
-#pragma unroll 1
+#pragma unroll UNROLL
                     for (int k = run.x; k < run.y; ++k) {
                         R dW[MAXM], dJ[MAXM];
                         // sqrt|dt| sqrt(2 ln 2) is folded into c
@@ -985,7 +989,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                     if (run.z >= 0) store(run.z, true);
                 }
             } else {
-#pragma unroll 1
+#pragma unroll UNROLL
                 for (int k = 0; k < n_steps; ++k) {
                     const R dt = a.dt[k];
                     const R sq = a.sqdt[k];
