@@ -37,7 +37,7 @@ extern "C" {
 #define SDE_API
 #endif
 
-#define SDE_ABI_VERSION 3
+#define SDE_ABI_VERSION 4
 
 #define SDE_MAX_GROUP   16   /* largest correlated group (state vars) */
 #define SDE_MAX_PARAMS  6    /* coefficient arrays per state variable */
@@ -57,7 +57,7 @@ extern "C" {
 #define SDE_MODEL_OU      1  /* dx = k*(theta - x)*dt + sigma*dw: OU, Hull-White factors */
 #define SDE_MODEL_HESTON  2  /* (log x, y) with full truncation y+ = max(y, 0)           */
 #define SDE_MODEL_CIR     3  /* dx = k*(theta - x+)*dt + xi*sqrt(x+)*dw, x+ = max(x, 0)  */
-#define SDE_MODEL_USER    4  /* dx = A_dt(t, x, p)*dt + A_dw(t, x, p)*dw, SdeUserProgram  */
+#define SDE_MODEL_USER    4  /* dx = sum of A_s(t, x, p)*ds, s in dt, dw, dn, dj; SdeUserProgram */
 
 /* params[p][w] meaning, per model (w = state variable index):
  *   LINEAR : p0 = c_dt, p1 = c_dw, p2 = lam, p3 = a, p4 = b, p5 = pa
@@ -80,16 +80,26 @@ extern "C" {
  * p0..p5, r8..r(6 + q) = the states of equations 1..q-1, the rest
  * temporaries; SDE_USER_MAX_REGS in all.  An instruction is code | dst << 8
  * | a << 16 | b << 24 (SDE_UOP_*: dst = f(ra, rb); SDE_UOP_CONST: dst =
- * consts[a]).  Equation e steps x + (A_1 dZ_1 + A_2 dZ_2), its coefficients
- * in registers term_register[e][0..n_terms-1], the sources term_source[]
- * in the order of the SDE function's returned dict (sdepy's euler_next,
- * sdepy/integration.py:707-718), dZ = dt or dw. */
+ * consts[a]).  Equation e steps x + (A_1 dZ_1 + ... + A_n dZ_n), summed
+ * left to right, its coefficients in registers term_register[e][0..n-1],
+ * the sources term_source[] in the order of the SDE function's returned
+ * dict (sdepy's euler_next, sdepy/integration.py:707-718).  dZ is dt, the
+ * Wiener increment dw, the Poisson increment dn (sdepy's source_dn,
+ * sdepy/integration.py:1346-1378) or the compound Poisson increment dj
+ * (source_dj, :1380-1423).  With dn or dj terms, jump_params holds per
+ * state the Poisson intensity lam (shared by dn and dj, as the reference
+ * shares its 'lam' argument) and the jump-size law's a, b, pa (law
+ * SdeSpec.jump_law, which is SDE_JUMP_NONE without a dj term); dn and dj
+ * of one program are independent Poisson processes. */
 #define SDE_USER_MAX_OPS    64
 #define SDE_USER_MAX_CONSTS 16
 #define SDE_USER_MAX_REGS   48
 #define SDE_USER_MAX_EQ     8
+#define SDE_USER_MAX_TERMS  4
 #define SDE_SRC_DT 0
 #define SDE_SRC_DW 1
+#define SDE_SRC_DN 2
+#define SDE_SRC_DJ 3
 enum {
     SDE_UOP_CONST = 0, SDE_UOP_ADD, SDE_UOP_SUB, SDE_UOP_MUL, SDE_UOP_DIV, SDE_UOP_NEG,
     SDE_UOP_ABS, SDE_UOP_EXP, SDE_UOP_LOG, SDE_UOP_SQRT, SDE_UOP_MAX, SDE_UOP_MIN,
@@ -99,14 +109,16 @@ enum {
 typedef struct SdeUserProgram {
     int32_t n_ops;
     int32_t n_eq;                     /* equations q, 1..SDE_USER_MAX_EQ          */
-    int32_t n_terms;                  /* terms of each equation's sum, 0..2      */
-    int32_t term_source[2];           /* SDE_SRC_DT | SDE_SRC_DW, in dict order   */
-    int32_t term_register[SDE_USER_MAX_EQ][2];   /* each term's coefficient      */
+    int32_t n_terms;                  /* terms of each equation's sum, 0..4      */
+    int32_t term_source[SDE_USER_MAX_TERMS];     /* SDE_SRC_*, each at most once */
+    int32_t term_register[SDE_USER_MAX_EQ][SDE_USER_MAX_TERMS];   /* coefficients */
     uint32_t ops[SDE_USER_MAX_OPS];
     double consts[SDE_USER_MAX_CONSTS];
+    const double *jump_params;        /* [4][groups*M] lam, a, b, pa; NULL without dn / dj */
 } SdeUserProgram;
 
-/* jump-size law of the compound Poisson source (LINEAR model only) */
+/* jump-size law of the compound Poisson source (LINEAR model, and user
+ * SDEs with a dj term) */
 #define SDE_JUMP_NONE        0
 #define SDE_JUMP_NORM        1   /* y = a + b*z                    */
 #define SDE_JUMP_DOUBLE_EXP  2   /* y = a*e w.p. pa, else -b*e     */
@@ -173,12 +185,19 @@ typedef struct SdeGrid {
      * matrix (sde_cholesky).  Ignored with injected increments; sde_adjoint
      * and sde_run_stats_static return SDE_ERR_UNSUPPORTED. */
     const double *corr_t;
+    /* User SDEs with dn / dj terms: time-dependent Poisson intensity, or
+     * NULL (SdeUserProgram.jump_params row 0 applies at every step):
+     * [n_pts - 1][groups*M], row k evaluated at step k's midpoint
+     * tt[k] + dt/2 (sdepy/infrastructure.py:1629). */
+    const double *lam_t;
 } SdeGrid;
 
 typedef struct SdeNoise {   /* host arrays of injected increments (f64) */
     const double *dw;       /* [n_steps][groups*M][paths], required        */
     const double *dj;       /* [n_steps][groups*M][paths] or NULL           */
-    const int64_t *dn;      /* [n_steps][groups*M][paths] or NULL (info)    */
+    const int64_t *dn;      /* [n_steps][groups*M][paths] or NULL: the Poisson
+                             * counts of dj (jump_count info), or, for a user
+                             * SDE with a dn term, that source's increments */
 } SdeNoise;
 
 typedef struct SdeOut {

@@ -172,7 +172,8 @@ def shapes(preset, vshape, factors=1):
 
 def integrate(preset, params=None, timeline=(0., 1.), *, paths=1, vshape=(),
               steps=None, i0=0, dtype=None, corr=None, dw=None, dj=None,
-              rng=None, getinfo=True, sde=None, log_flag=False, sde_q=0, addaxis=False):
+              rng=None, getinfo=True, sde=None, log_flag=False, sde_q=0, addaxis=False,
+              dn=None, sde_sources=None, term_order=None):
     """Integrate one preset, or (preset 'user') the SDE function ``sde(t,
     x, **params)`` of sdepy's integrate decorator, in log space when
     ``log_flag`` (sdepy/integration.py:1154-1197, 1843-1955); ``sde_q`` > 0
@@ -180,8 +181,13 @@ def integrate(preset, params=None, timeline=(0., 1.), *, paths=1, vshape=(),
     (``addaxis``, sdepy/integration.py:1680-1840).  ``dw`` /
     ``dj`` are source-protocol objects (e.g. Replay of recorded
     increments); when None they are realised with numpy from ``rng`` as
-    sdepy's default sources do.  Returns (result, info) where result is an
-    array or a tuple of arrays (full Heston)."""
+    sdepy's default sources do.  A user SDE draws the sources
+    ``sde_sources`` (default dw): ``dw``, ``dn`` (its Poisson source) and
+    ``dj``, given as source-protocol objects; a system sums its packed
+    terms in ``term_order`` (default: the equations' first-appearance order
+    of the ids; sdepy iterates a set, sdepy/integration.py:1726-1731).
+    Returns (result, info) where result is an array or a tuple of arrays
+    (full Heston)."""
     user = preset == 'user'
     assert user or preset in PRESETS, preset
     if user:
@@ -207,7 +213,8 @@ def integrate(preset, params=None, timeline=(0., 1.), *, paths=1, vshape=(),
     heston = 'heston' in preset
     log = preset in ('lognorm_process',) or jumps or (user and log_flag)
     P0 = P
-    if dw is None:
+    ids = set(sde_sources) if (user and sde_sources) else {'dt', 'dw'}
+    if dw is None and 'dw' in ids:
         dw = NumpyWiener(rng, paths, wshape, corr=corr, dtype=dtype)
     if jumps and dj is None:
         dj = NumpyCPoisson(rng, paths, wshape, P['lam'], law_rvs(preset, p), dtype=dtype)
@@ -231,8 +238,12 @@ def integrate(preset, params=None, timeline=(0., 1.), *, paths=1, vshape=(),
         P = {k: (np.asarray(v(s)) if callable(v) else v) for k, v in P0.items()}
         if system:   # SDEs.A (integration.py:1726-1744): pack the equations' terms
             As = user_sde(s, *unpack(x), **{k: v for k, v in P.items() if k != 'x0'})
-            ids = [k for k in ('dt', 'dw') if any(k in z for z in As)]
-            return {i: pack(tuple(z.get(i, 0) for z in As)) for i in ids}
+            order = term_order
+            if order is None:
+                order = []
+                for z in As:
+                    order += [k for k in z if k not in order]
+            return {i: pack(tuple(z.get(i, 0) for z in As)) for i in order}
         if user:   # the function's own coefficients, its dict order kept
             return user_sde(s, x, **{k: v for k, v in P.items() if k != 'x0'})
         if preset == 'wiener_process':
@@ -295,6 +306,8 @@ def integrate(preset, params=None, timeline=(0., 1.), *, paths=1, vshape=(),
     sources = {'dw': dw}
     if jumps:
         sources['dj'] = dj
+    if user:   # the SDE's own sources (sdepy/integration.py:1227-1234)
+        sources = {k: v for k, v in (('dw', dw), ('dn', dn), ('dj', dj)) if k in ids}
     order = sorted(sources)
     for steps_leg, tt_leg, rows, reverse in legs:
         x = np.full(wshape + (paths,), np.nan, dtype=dtype)

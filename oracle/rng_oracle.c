@@ -14,7 +14,9 @@
  *     sdepy/integration.py:2066-2747) and sdepy's output transforms.
  * The counter layout is (path, step + offset, group << 8 | call, stream) for
  * normals and Poisson uniforms and (path, step + offset,
- * 0x80000000 | var << 12 | jump, stream) for jump sizes.  Groups of one
+ * 0x80000000 | var << 12 | jump, stream) for jump sizes; a user SDE with
+ * both dj and dn terms draws dn's Poisson uniform from word x of (path,
+ * step + offset, 0x40000000 | var, stream).  Groups of one
  * variable draw one call per two steps: the call of even step k gives its
  * Box-Muller pair's z0 to step k and z1 to step k + 1, and its words z and
  * w are the Poisson uniforms of steps k and k + 1.  Groups of two
@@ -100,7 +102,7 @@ static double np_maxd(double a, double b) { return (a != a) ? a : (b != b) ? b :
 static double np_mind(double a, double b) { return (a != a) ? a : (b != b) ? b : (a <= b ? a : b); }
 
 static void user_coefs(const SdeUserProgram *u, const double *xs, double t, const double *p,
-                       double out[][2]) {
+                       double out[][SDE_USER_MAX_TERMS]) {
     double r[SDE_USER_MAX_REGS] = {0};
     r[0] = xs[0];
     r[1] = t;
@@ -139,10 +141,8 @@ static void user_coefs(const SdeUserProgram *u, const double *xs, double t, cons
         }
         r[d] = v;
     }
-    for (int e = 0; e < u->n_eq; ++e) {
-        out[e][0] = u->n_terms > 0 ? r[u->term_register[e][0]] : 0.0;
-        out[e][1] = u->n_terms > 1 ? r[u->term_register[e][1]] : 0.0;
-    }
+    for (int e = 0; e < u->n_eq; ++e)
+        for (int j = 0; j < SDE_USER_MAX_TERMS; ++j) out[e][j] = j < u->n_terms ? r[u->term_register[e][j]] : 0.0;
 }
 
 static double jump_size(int law, const uint32_t r[4], double a, double b, double pa) {
@@ -175,7 +175,15 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
     const int M = s->group_size, G = s->groups, W = G * M;
     const int64_t paths = s->paths;
     const int n_steps = g->n_pts - 1;
-    const int jumps = s->jump_law != SDE_JUMP_NONE;
+    /* a user program's jump terms: bit 0 dj, bit 1 dn */
+    int ujs = 0;
+    if (s->model == SDE_MODEL_USER)
+        for (int i = 0; i < s->program->n_terms; ++i) {
+            if (s->program->term_source[i] == SDE_SRC_DJ) ujs |= 1;
+            if (s->program->term_source[i] == SDE_SRC_DN) ujs |= 2;
+        }
+    const int user = s->model == SDE_MODEL_USER;
+    const int jumps = user ? ujs != 0 : s->jump_law != SDE_JUMP_NONE;
     int opg;
     switch (s->out_mode) {
     case SDE_OUT_SUM: opg = 1; break;
@@ -215,7 +223,7 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
         const int64_t pc = (anti && p >= paths / 2) ? p - paths / 2 : p;
         const double zsign = (anti && p >= paths / 2) ? -1.0 : 1.0;
         for (int gi = 0; gi < G && !rc; ++gi) {
-            double st[SDE_MAX_GROUP], z[SDE_MAX_GROUP + 1], dW[SDE_MAX_GROUP], dJ[SDE_MAX_GROUP];
+            double st[SDE_MAX_GROUP], z[SDE_MAX_GROUP + 1], dW[SDE_MAX_GROUP], dJ[SDE_MAX_GROUP], dN[SDE_MAX_GROUP];
             int negc[SDE_MAX_GROUP] = {0}, jc[SDE_MAX_GROUP] = {0};
             int64_t row_jc = 0;
             double pz0 = 0.0, pz1 = 0.0;   /* one-variable groups: the even step's pair */
@@ -274,8 +282,44 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
                             dW[m] = z[m] * sq;
                         }
                         dJ[m] = 0.0;
+                        dN[m] = 0.0;
                     }
-                    if (jumps) {
+                    if (jumps && user) {
+                        /* a user SDE: dj from the Poisson word and as many jump
+                         * sizes; dn from the same count, or with a dj term too,
+                         * from its own word */
+                        const double *jp = s->program->jump_params;
+                        for (int m = 0; m < M; ++m) {
+                            const int w = gi * M + m;
+                            const double lamr = g->lam_t ? g->lam_t[(size_t)k * W + w] : jp[w];
+                            const double lam = fabs(dt) * lamr;
+                            const double p0 = exp(-lam);
+                            uint32_t word = u[2 * P + m];
+                            int cnt = u01(word) > p0 ? oracle_poisson(word, p0, lam) : 0;
+                            if (cnt < 0) { rc = -1; break; }
+                            if (ujs & 1) {
+                                double S = 0.0;
+                                for (int j = 0; j < cnt; ++j) {
+                                    const uint32_t ctr[4] = {(uint32_t)pc, c1,
+                                                             0x80000000u | ((uint32_t)w << 12) | (uint32_t)j, s->stream};
+                                    uint32_t r[4];
+                                    oracle_philox(ctr, key, r);
+                                    const double y = jump_size(s->jump_law, r, jp[W + w], jp[2 * W + w], jp[3 * W + w]);
+                                    S = (j == 0) ? y : S + y;
+                                }
+                                if (cnt) dJ[m] = sgn * S;
+                                if (ujs & 2) {
+                                    const uint32_t ctr[4] = {(uint32_t)pc, c1, 0x40000000u | (uint32_t)w, s->stream};
+                                    uint32_t r[4];
+                                    oracle_philox(ctr, key, r);
+                                    word = r[0];
+                                    cnt = u01(word) > p0 ? oracle_poisson(word, p0, lam) : 0;
+                                    if (cnt < 0) { rc = -1; break; }
+                                }
+                            }
+                            if ((ujs & 2) && cnt) dN[m] = sgn * (double)cnt;
+                        }
+                    } else if (jumps) {
                         for (int m = 0; m < M; ++m) {
                             const int w = gi * M + m;
                             const double lam = fabs(dt) * pp[2 * W + w];
@@ -318,7 +362,7 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
                         const int q = s->program->n_eq, nc = M / q;
                         double nx[SDE_MAX_GROUP];
                         for (int h = 0; h < nc; ++h) {
-                            double pv[6], xs[SDE_USER_MAX_EQ], A[SDE_USER_MAX_EQ][2];
+                            double pv[6], xs[SDE_USER_MAX_EQ], A[SDE_USER_MAX_EQ][SDE_USER_MAX_TERMS];
                             for (int i = 0; i < 6; ++i) pv[i] = pp[i * W + gi * M + h];
                             for (int e = 0; e < q; ++e) xs[e] = st[e * nc + h];
                             user_coefs(s->program, xs, g->tt[k], pv, A);
@@ -326,8 +370,12 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
                                 const int m = e * nc + h;
                                 double sum = 0.0;
                                 for (int i = 0; i < s->program->n_terms; ++i) {
-                                    const double term =
-                                        A[e][i] * (s->program->term_source[i] == SDE_SRC_DT ? dt : dW[m]);
+                                    const int src = s->program->term_source[i];
+                                    const double dz = src == SDE_SRC_DT   ? dt
+                                                      : src == SDE_SRC_DW ? dW[m]
+                                                      : src == SDE_SRC_DJ ? dJ[m]
+                                                                          : dN[m];
+                                    const double term = A[e][i] * dz;
                                     sum = i == 0 ? term : sum + term;
                                 }
                                 nx[m] = st[m] + sum;

@@ -13,7 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, '_native', 'libsdepy_gb300.so')
 
-ABI_VERSION = 3
+ABI_VERSION = 4
 MAX_GROUP = 16
 MAX_PARAMS = 6
 MAX_STRIKES = 8
@@ -23,8 +23,8 @@ OK, ERR_INVALID, ERR_UNSUPPORTED, ERR_CUDA, ERR_DEVICE, ERR_NO_DEVICE = \
 
 MODEL_LINEAR, MODEL_OU, MODEL_HESTON, MODEL_CIR, MODEL_USER = 0, 1, 2, 3, 4
 # user SDE programs (SdeUserProgram)
-USER_MAX_OPS, USER_MAX_CONSTS, USER_MAX_REGS, USER_MAX_EQ = 64, 16, 48, 8
-SRC_DT, SRC_DW = 0, 1
+USER_MAX_OPS, USER_MAX_CONSTS, USER_MAX_REGS, USER_MAX_EQ, USER_MAX_TERMS = 64, 16, 48, 8, 4
+SRC_DT, SRC_DW, SRC_DN, SRC_DJ = 0, 1, 2, 3
 (UOP_CONST, UOP_ADD, UOP_SUB, UOP_MUL, UOP_DIV, UOP_NEG, UOP_ABS, UOP_EXP, UOP_LOG, UOP_SQRT,
  UOP_MAX, UOP_MIN, UOP_SIN, UOP_COS, UOP_TAN, UOP_TANH, UOP_POW, UOP_EXPM1, UOP_LOG1P,
  UOP_ARCTAN, UOP_COPY) = range(21)
@@ -40,8 +40,8 @@ _lp = C.POINTER(C.c_int64)
 
 class SdeUserProgram(C.Structure):
     _fields_ = [('n_ops', C.c_int32), ('n_eq', C.c_int32), ('n_terms', C.c_int32),
-                ('term_source', C.c_int32*2), ('term_register', (C.c_int32*2)*8),
-                ('ops', C.c_uint32*64), ('consts', C.c_double*16)]
+                ('term_source', C.c_int32*4), ('term_register', (C.c_int32*4)*8),
+                ('ops', C.c_uint32*64), ('consts', C.c_double*16), ('jump_params', C.POINTER(C.c_double))]
 
 
 class SdeSpec(C.Structure):
@@ -57,7 +57,7 @@ class SdeSpec(C.Structure):
 
 class SdeGrid(C.Structure):
     _fields_ = [('tt', _dp), ('out_row', _ip), ('n_pts', C.c_int32),
-                ('step_offset', C.c_uint32), ('params_t', _dp), ('corr_t', _dp)]
+                ('step_offset', C.c_uint32), ('params_t', _dp), ('corr_t', _dp), ('lam_t', _dp)]
 
 
 class SdeNoise(C.Structure):

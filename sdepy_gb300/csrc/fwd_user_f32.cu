@@ -5,7 +5,8 @@
 
 namespace sdegpu {
 
-FwdLauncher<float> find_fwd_f32_user(int maxm, bool inject, bool sys, int *bps) {
+FwdLauncher<float> find_fwd_f32_user(int maxm, bool inject, bool sys, bool jumps, int *bps) {
+    if (jumps) return find_fwd_f32_user_jump(maxm, inject, sys, bps);
 #define SDE_USER(MODEL, M, INJ)                                                            \
     if (maxm == M && inject == INJ && sys == (MODEL == SDE_MODEL_USER_SYS)) {              \
         if (bps) *bps = fwd_max_blocks_per_sm<float, MODEL, M, INJ, false>();               \

@@ -5,7 +5,8 @@
 
 namespace sdegpu {
 
-FwdLauncher<double> find_fwd_f64_user(int maxm, bool inject, bool sys, int *bps) {
+FwdLauncher<double> find_fwd_f64_user(int maxm, bool inject, bool sys, bool jumps, int *bps) {
+    if (jumps) return find_fwd_f64_user_jump(maxm, inject, sys, bps);
 #define SDE_USER(MODEL, M, INJ)                                                            \
     if (maxm == M && inject == INJ && sys == (MODEL == SDE_MODEL_USER_SYS)) {              \
         if (bps) *bps = fwd_max_blocks_per_sm<double, MODEL, M, INJ, false>();               \

@@ -284,13 +284,16 @@ static int check_spec(const SdeSpec *s, int *opg) {
         const SdeUserProgram *u = s->program;
         if (!u) return fail(SDE_ERR_INVALID, "a user SDE needs its program");
         if (u->n_ops < 0 || u->n_ops > SDE_USER_MAX_OPS) return fail(SDE_ERR_INVALID, "user program: n_ops");
-        if (u->n_terms < 0 || u->n_terms > 2) return fail(SDE_ERR_INVALID, "user program: n_terms");
+        if (u->n_terms < 0 || u->n_terms > SDE_USER_MAX_TERMS) return fail(SDE_ERR_INVALID, "user program: n_terms");
         if (u->n_eq < 1 || u->n_eq > SDE_USER_MAX_EQ || s->group_size % u->n_eq)
             return fail(SDE_ERR_INVALID, "user program: %d equations in groups of %d", u->n_eq, s->group_size);
         if (u->n_eq > 1 && s->group_size < 2) return fail(SDE_ERR_INVALID, "user program: system groups");
+        int seen = 0;   // each source at most once
         for (int i = 0; i < u->n_terms; ++i) {
-            if (u->term_source[i] != SDE_SRC_DT && u->term_source[i] != SDE_SRC_DW)
+            const int src = u->term_source[i];
+            if (src < SDE_SRC_DT || src > SDE_SRC_DJ || (seen & (1 << src)))
                 return fail(SDE_ERR_INVALID, "user program: term %d", i);
+            seen |= 1 << src;
             for (int e = 0; e < u->n_eq; ++e)
                 if (u->term_register[e][i] < 0 || u->term_register[e][i] >= SDE_USER_MAX_REGS)
                     return fail(SDE_ERR_INVALID, "user program: term %d of equation %d", i, e);
@@ -303,7 +306,11 @@ static int check_spec(const SdeSpec *s, int *opg) {
             if (code == SDE_UOP_CONST ? ra >= SDE_USER_MAX_CONSTS : (ra >= SDE_USER_MAX_REGS || rb >= SDE_USER_MAX_REGS))
                 return fail(SDE_ERR_INVALID, "user program: operand of instruction %d", i);
         }
-        if (s->jump_law != SDE_JUMP_NONE) return fail(SDE_ERR_UNSUPPORTED, "user SDEs with jumps");
+        const bool has_dj = (seen >> SDE_SRC_DJ) & 1, has_dn = (seen >> SDE_SRC_DN) & 1;
+        if (has_dj != (s->jump_law != SDE_JUMP_NONE))
+            return fail(SDE_ERR_INVALID, "user program: a jump-size law goes with a dj term, and only with one");
+        if ((has_dj || has_dn) && !u->jump_params)
+            return fail(SDE_ERR_INVALID, "user program: dn / dj terms need jump_params");
         if (s->out_mode != SDE_OUT_STATE && s->out_mode != SDE_OUT_EXP)
             return fail(SDE_ERR_INVALID, "user SDEs store the state or its exp");
         if (s->flags & SDE_FLAG_ANTITHETIC) return fail(SDE_ERR_UNSUPPORTED, "antithetic paths of user SDEs");
@@ -320,8 +327,8 @@ static int check_spec(const SdeSpec *s, int *opg) {
         return fail(SDE_ERR_UNSUPPORTED, "too many state variables per path");
     if (s->jump_law < SDE_JUMP_NONE || s->jump_law > SDE_JUMP_EXP)
         return fail(SDE_ERR_UNSUPPORTED, "unknown jump law %d", s->jump_law);
-    if (s->jump_law != SDE_JUMP_NONE && s->model != SDE_MODEL_LINEAR)
-        return fail(SDE_ERR_UNSUPPORTED, "jumps are supported for the LINEAR model only");
+    if (s->jump_law != SDE_JUMP_NONE && s->model != SDE_MODEL_LINEAR && s->model != SDE_MODEL_USER)
+        return fail(SDE_ERR_UNSUPPORTED, "jumps are supported for the LINEAR model and user SDEs only");
     if (s->model == SDE_MODEL_HESTON) {
         const int M = s->group_size;
         if (M != 2 && M != 4 && M != 8 && M != 16)
@@ -369,7 +376,7 @@ template <typename R> struct Finder;
 template <> struct Finder<double> {
     static FwdLauncher<double> find(int model, int maxm, bool inj, bool jmp, int *bps) {
         if (model == SDE_MODEL_USER || model == SDE_MODEL_USER_SYS)
-            return jmp ? nullptr : find_fwd_f64_user(maxm, inj, model == SDE_MODEL_USER_SYS, bps);
+            return find_fwd_f64_user(maxm, inj, model == SDE_MODEL_USER_SYS, jmp, bps);
         if (model == SDE_MODEL_CIR) return jmp ? nullptr : find_fwd_f64_cir(maxm, inj, false, bps);
         FwdLauncher<double> f = find_fwd_f64_linear(model, maxm, inj, jmp, bps);
         return f ? f : find_fwd_f64_ou_heston(model, maxm, inj, jmp, bps);
@@ -383,7 +390,7 @@ template <> struct Finder<double> {
 template <> struct Finder<float> {
     static FwdLauncher<float> find(int model, int maxm, bool inj, bool jmp, int *bps) {
         if (model == SDE_MODEL_USER || model == SDE_MODEL_USER_SYS)
-            return jmp ? nullptr : find_fwd_f32_user(maxm, inj, model == SDE_MODEL_USER_SYS, bps);
+            return find_fwd_f32_user(maxm, inj, model == SDE_MODEL_USER_SYS, jmp, bps);
         if (model == SDE_MODEL_CIR) return jmp ? nullptr : find_fwd_f32_cir(maxm, inj, false, false, bps);
         FwdLauncher<float> f = find_fwd_f32_linear(model, maxm, inj, jmp, bps);
         return f ? f : find_fwd_f32_ou_heston(model, maxm, inj, jmp, bps);
@@ -425,7 +432,16 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     if (!out) return fail(SDE_ERR_INVALID, "out is NULL");
     if (out->n_rows < 1) return fail(SDE_ERR_INVALID, "out->n_rows must be >= 1");
     if ((rc = check_grid(gr, out->n_rows))) return rc;
-    const bool jumps = s->jump_law != SDE_JUMP_NONE;
+    // a user program's jump terms: bit 0 dj, bit 1 dn
+    int ujs = 0;
+    if (s->model == SDE_MODEL_USER)
+        for (int i = 0; i < s->program->n_terms; ++i) {
+            if (s->program->term_source[i] == SDE_SRC_DJ) ujs |= 1;
+            if (s->program->term_source[i] == SDE_SRC_DN) ujs |= 2;
+        }
+    const bool jumps = s->model == SDE_MODEL_USER ? ujs != 0 : s->jump_law != SDE_JUMP_NONE;
+    if (gr->lam_t && !(s->model == SDE_MODEL_USER && jumps))
+        return fail(SDE_ERR_INVALID, "grid lam_t applies to user SDEs with dn / dj terms");
     const bool inject = noise != nullptr;
     const bool anti = (s->flags & SDE_FLAG_ANTITHETIC) != 0;
     if (s->flags & ~SDE_FLAG_ANTITHETIC) return fail(SDE_ERR_INVALID, "unknown spec flags %d", s->flags);
@@ -437,8 +453,18 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
         if (s->group_size > 8) return fail(SDE_ERR_UNSUPPORTED, "antithetic paths take groups of up to 8 states");
     }
     if (inject) {
-        if (!noise->dw) return fail(SDE_ERR_INVALID, "injected noise needs dw");
-        if (jumps && !noise->dj) return fail(SDE_ERR_INVALID, "injected noise of a jump model needs dj");
+        // (a user SDE without a dw term has no Wiener source)
+        bool user_dw = false;
+        if (s->model == SDE_MODEL_USER)
+            for (int i = 0; i < s->program->n_terms; ++i) user_dw |= s->program->term_source[i] == SDE_SRC_DW;
+        if (!noise->dw && (s->model != SDE_MODEL_USER || user_dw))
+            return fail(SDE_ERR_INVALID, "injected noise needs dw");
+        if (s->model == SDE_MODEL_USER) {
+            if ((ujs & 1) && !noise->dj) return fail(SDE_ERR_INVALID, "injected noise of a dj term needs dj");
+            if ((ujs & 2) && !noise->dn) return fail(SDE_ERR_INVALID, "injected noise of a dn term needs dn");
+        } else if (jumps && !noise->dj) {
+            return fail(SDE_ERR_INVALID, "injected noise of a jump model needs dj");
+        }
     }
     const bool stats = req != nullptr;
     if (stats) {
@@ -573,7 +599,9 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     const size_t o_cholt = o_prmt + al(sizeof(R) * (nprmt + 1));
     const size_t ntk = user ? (size_t)n_steps : 0;   // step starts, for user SDEs
     const size_t o_tk = o_cholt + al(sizeof(R) * (nchol + 1));
-    const size_t o_end = o_tk + al(sizeof(R) * (ntk + 1));
+    const size_t njp = (user && jumps) ? (size_t)3 * W : 0;   // a user dj term's law: a, b, pa
+    const size_t o_jp = o_tk + al(sizeof(R) * (ntk + 1));
+    const size_t o_end = o_jp + al(sizeof(R) * (njp + 1));
     D->host_tables.resize(o_end);
     char *H = D->host_tables.data();
     R *h_dt = (R *)(H + o_dt), *h_sq = (R *)(H + o_sq), *h_x0 = (R *)(H + o_x0), *h_prm = (R *)(H + o_prm);
@@ -596,7 +624,10 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
         for (int k = 0; k < n_steps; ++k) {
             const double adt = fabs(gr->tt[k + 1] - gr->tt[k]);
             for (int w = 0; w < W; ++w) {
-                const double lam = params_of(k)[2 * W + w];
+                // a user SDE's intensity: its table at the step's midpoint, or its constant
+                const double lam = !user          ? params_of(k)[2 * W + w]
+                                   : gr->lam_t ? gr->lam_t[(size_t)k * W + w]
+                                               : s->program->jump_params[w];
                 if (!(lam >= 0.0) || !std::isfinite(lam))
                     return fail(SDE_ERR_INVALID, "Poisson intensity must be finite and >= 0");
                 const double L = adt * lam;
@@ -608,12 +639,19 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
                 poisson_thresholds(p0, L, h_thr[i], h_thr1[i]);
             }
         }
+        // the jump-size law's a, b, pa: parameter slots 3..5, or a user
+        // program's jump_params rows 1..3
+        const double *law = user ? s->program->jump_params + W : s->params + 3 * W;
         if (s->jump_law == SDE_JUMP_DOUBLE_EXP)
             for (int w = 0; w < W; ++w) {
-                const double a = s->params[3 * W + w], b = s->params[4 * W + w], pa = s->params[5 * W + w];
+                const double a = law[w], b = law[W + w], pa = law[2 * W + w];
                 if (!(a > 0) || !(b > 0) || !(pa >= 0 && pa <= 1))
                     return fail(SDE_ERR_INVALID, "domain error in arguments");
             }
+    }
+    if (njp) {
+        R *h_jp = (R *)(H + o_jp);
+        for (size_t i = 0; i < njp; ++i) h_jp[i] = (R)s->program->jump_params[W + i];
     }
 
     if (!runs.empty()) memcpy(H + o_runs, runs.data(), sizeof(int4) * runs.size());
@@ -694,6 +732,8 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     if (nchol) a.has_corr = 1;
     a.tk = ntk ? (const R *)(T + o_tk) : nullptr;
     if (user) a.uprog = *s->program;
+    a.jprm = njp ? (const R *)(T + o_jp) : nullptr;
+    a.user_jsrc = ujs;
     a.key = philox_schedule(s->seed);
     a.n_out_vars = n_out;
 
@@ -701,13 +741,18 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     const size_t nz = (size_t)n_steps * W * paths;
     if (inject && n_steps > 0) {
         void *p;
-        if ((rc = scratch(D, S_NOISE_DW, nz * sizeof(double), &p))) return rc;
-        CU(cudaMemcpyAsync(p, noise->dw, nz * sizeof(double), cudaMemcpyHostToDevice, st));
-        a.dw = (const double *)p;
-        if (jumps) {
+        if (noise->dw) {
+            if ((rc = scratch(D, S_NOISE_DW, nz * sizeof(double), &p))) return rc;
+            CU(cudaMemcpyAsync(p, noise->dw, nz * sizeof(double), cudaMemcpyHostToDevice, st));
+            a.dw = (const double *)p;
+        }
+        // (a user SDE's dj and dn are its two sources, each when its term is there)
+        if (jumps && (!user || (ujs & 1))) {
             if ((rc = scratch(D, S_NOISE_DJ, nz * sizeof(double), &p))) return rc;
             CU(cudaMemcpyAsync(p, noise->dj, nz * sizeof(double), cudaMemcpyHostToDevice, st));
             a.dj = (const double *)p;
+        }
+        if (jumps && (!user || (ujs & 2))) {
             if (noise->dn) {
                 if ((rc = scratch(D, S_NOISE_DN, nz * sizeof(int64_t), &p))) return rc;
                 CU(cudaMemcpyAsync(p, noise->dn, nz * sizeof(int64_t), cudaMemcpyHostToDevice, st));
@@ -755,7 +800,7 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
             a.neg_count = (int32_t *)p;
         }
     }
-    if (jumps && out->jump_count) {
+    if (jumps && !user && out->jump_count) {
         if (dev) a.jump_count = out->jump_count;
         else {
             void *p;
@@ -763,7 +808,7 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
             a.jump_count = (int32_t *)p;
         }
     }
-    if (jumps && out->row_jumps) {
+    if (jumps && !user && out->row_jumps) {
         if (dev) a.row_jumps = (unsigned long long *)out->row_jumps;
         else {
             void *p;

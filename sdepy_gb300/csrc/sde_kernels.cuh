@@ -70,9 +70,13 @@ struct FwdArgs {
     // each step's correlation matrix (rows as chol below), or NULL; read
     // only by the kernels that reload per-step coefficients (STEPCORR)
     const R *chol_t;
-    // SDE_MODEL_USER: the coefficient program, and each step's start time
+    // SDE_MODEL_USER: the coefficient program, and each step's start time;
+    // with dn / dj terms (user_jsrc bit 0: a dj term, bit 1: a dn term) the
+    // jump-size law's a, b, pa per state, [3][W]
     SdeUserProgram uprog;
     const R *tk;
+    const R *jprm;
+    int32_t user_jsrc;
     // and the grid as runs of steps sharing one coefficient row:
     // (first step, end step, output row stored after the run or -1, coef row)
     const int4 *runs;
@@ -624,7 +628,7 @@ __device__ __forceinline__ R np_min(R a, R b) { return (a != a) ? a : (b != b) ?
 // single SDE); out[e][j]: the coefficient of term j of equation e
 template <typename R>
 __device__ __noinline__ void user_coefs(const SdeUserProgram &u, const R *xs, R t, const R (&p)[6],
-                                        R (*out)[2]) {
+                                        R (*out)[SDE_USER_MAX_TERMS]) {
     typedef Ar<R> A;
     typedef UFn<R> F;
     R r[SDE_USER_MAX_REGS];
@@ -667,10 +671,9 @@ __device__ __noinline__ void user_coefs(const SdeUserProgram &u, const R *xs, R 
         }
         r[d] = v;
     }
-    for (int e = 0; e < u.n_eq; ++e) {
-        out[e][0] = u.n_terms > 0 ? r[u.term_register[e][0]] : R(0);
-        out[e][1] = u.n_terms > 1 ? r[u.term_register[e][1]] : R(0);
-    }
+    for (int e = 0; e < u.n_eq; ++e)
+#pragma unroll
+        for (int j = 0; j < SDE_USER_MAX_TERMS; ++j) out[e][j] = j < u.n_terms ? r[u.term_register[e][j]] : R(0);
 }
 
 // the internal kernel model of user SDE systems (q > 1: SdeSpec.model is
@@ -790,6 +793,15 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                 for (int m = 0; m < MAXM; ++m) negc1[m] = 0;
             }
             unsigned int row_jc = 0;
+            // a user SDE's Poisson increments dn of the step (dJ holds dj)
+            R dN[(USER && JUMPS) ? MAXM : 1] = {};
+            // the increment of a user SDE's term: dt, dw, dn or dj of state m
+            auto user_dz = [&](int src, R dt, R dw, R dj, int m) -> R {
+                if (src == SDE_SRC_DT) return dt;
+                if (src == SDE_SRC_DW) return dw;
+                if constexpr (USER && JUMPS) return src == SDE_SRC_DJ ? dj : dN[m];
+                return R(0);
+            };
 
             // store helper (lambda keeps the loop body readable): state s of
             // path pth, stats values in slot i; sh: the state is the
@@ -853,6 +865,37 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
             auto add_jumps = [&](int m, uint32_t word, int k, uint32_t c1w, R (&dJ)[MAXM]) {
                 const int w = g * M + m;
                 const int64_t tix = (int64_t)k * W + w;
+                if constexpr (USER) {
+                    // dj: the count of `word` and as many jump sizes; dn: that
+                    // count, or with a dj term too, the count of an
+                    // independent word (counter (p, step, 2^30 | w, stream))
+                    auto count = [&](uint32_t u) -> int {
+                        if ((long long)u <= a.thr[tix]) return 0;
+                        return (long long)u <= a.thr1[tix] ? 1 : poisson_tail(u, a.p0[tix], a.lamdt[tix], a.err);
+                    };
+                    int cnt = count(word);
+                    if (a.user_jsrc & 1) {
+                        if (cnt) {
+                            const R ja = a.jprm[w], jb = a.jprm[W + w], jpa = a.jprm[2 * W + w];
+                            R S = R(0);
+                            for (int j = 0; j < cnt; ++j) {
+                                const uint4 r = philox4x32_10(
+                                    make_uint4((uint32_t)p, c1w, 0x80000000u | ((uint32_t)w << 12) | (uint32_t)j,
+                                               a.stream),
+                                    key);
+                                const R y = jump_size<R>(a.jump_law, r, ja, jb, jpa);
+                                S = (j == 0) ? y : A::add(S, y);
+                            }
+                            dJ[m] = A::mul(a.sgn, S);
+                        }
+                        if (a.user_jsrc & 2)
+                            cnt = count(philox4x32_10(make_uint4((uint32_t)p, c1w, 0x40000000u | (uint32_t)w, a.stream),
+                                                      key).x);
+                    }
+                    if constexpr (JUMPS)
+                        if ((a.user_jsrc & 2) && cnt) dN[m] = A::mul(a.sgn, (R)cnt);
+                    return;
+                }
                 if ((long long)word > a.thr[tix]) {
                     const int cnt = (long long)word <= a.thr1[tix] ? 1 : poisson_tail(word, a.p0[tix], a.lamdt[tix], a.err);
                     R S = R(0);
@@ -874,6 +917,10 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
             auto draw = [&](int k, R sq, R (&dW)[MAXM], R (&dJ)[MAXM]) {
 #pragma unroll
                 for (int m = 0; m < MAXM; ++m) dJ[m] = R(0);
+                if constexpr (USER && JUMPS) {
+#pragma unroll
+                    for (int m = 0; m < MAXM; ++m) dN[m] = R(0);
+                }
                 // f(the step's correlation factor): the per-step table's row
                 // (uniform test), else the constant factor of the parameter
                 // block -- two copies of f, so that the constant one keeps
@@ -891,8 +938,12 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                     for (int m = 0; m < MAXM; ++m) {
                         if (m < M) {
                             const int64_t idx = ((int64_t)k * W + g * M + m) * a.paths + p;
-                            dW[m] = (R)a.dw[idx];
-                            if (JUMPS) {
+                            if constexpr (USER) dW[m] = a.dw ? (R)a.dw[idx] : R(0);   // a program without dw
+                            else dW[m] = (R)a.dw[idx];
+                            if constexpr (USER && JUMPS) {   // the program's own dj / dn sources
+                                if (a.dj) dJ[m] = (R)a.dj[idx];
+                                if (a.dn) dN[m] = (R)a.dn[idx];
+                            } else if (JUMPS) {
                                 dJ[m] = (R)a.dj[idx];
                                 if (a.dn) {
                                     const int c = (int)a.dn[idx];
@@ -1029,17 +1080,17 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                             st[m] = A::add(st[m], A::add(A::mul(drift, dt), A::mul(c2[m], dW[m])));
                         }
                     } else if (MODEL == SDE_MODEL_USER) {
-                        // x + (A_1 dZ_1 + A_2 dZ_2), the terms in the order of the
-                        // SDE function's dict (sdepy sums from 0: 0 + v == v)
+                        // x + (A_1 dZ_1 + ... + A_n dZ_n), the terms in the order of
+                        // the SDE function's dict (sdepy sums from 0: 0 + v == v)
 #pragma unroll
                         for (int m = 0; m < MAXM; ++m) {
                             const R pv[6] = {c0[m], c1[m], c2[m], c3[m], c4[m], c5[m]};
-                            R A2[1][2];
+                            R A2[1][SDE_USER_MAX_TERMS];
                             const R xm[1] = {st[m]};
                             user_coefs<R>(a.uprog, xm, tk, pv, A2);
                             R s = R(0);
                             for (int i = 0; i < a.uprog.n_terms; ++i) {
-                                const R dz = a.uprog.term_source[i] == SDE_SRC_DT ? dt : dW[m];
+                                const R dz = user_dz(a.uprog.term_source[i], dt, dW[m], dJ[m], m);
                                 const R term = A::mul(A2[0][i], dz);
                                 s = i == 0 ? term : A::add(s, term);
                             }
@@ -1058,7 +1109,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                             nx[m] = st[m];
                         }
                         for (int h = 0; h < nc; ++h) {
-                            R xs[SDE_USER_MAX_EQ], A2[SDE_USER_MAX_EQ][2];
+                            R xs[SDE_USER_MAX_EQ], A2[SDE_USER_MAX_EQ][SDE_USER_MAX_TERMS];
                             for (int e = 0; e < q; ++e) xs[e] = sv[e * nc + h];
                             // parameters broadcast along the equations: component h's
                             R pv[6];
@@ -1072,7 +1123,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                                 const int m = e * nc + h;
                                 R s = R(0);
                                 for (int i = 0; i < a.uprog.n_terms; ++i) {
-                                    const R dz = a.uprog.term_source[i] == SDE_SRC_DT ? dt : dv[m];
+                                    const R dz = user_dz(a.uprog.term_source[i], dt, dv[m], dJ[m], m);
                                     const R term = A::mul(A2[e][i], dz);
                                     s = i == 0 ? term : A::add(s, term);
                                 }
@@ -1227,8 +1278,14 @@ FwdLauncher<float> find_fwd_f32_cir(int maxm, bool inject, bool tdep, bool anti,
 FwdLauncher<double> find_fwd_f64_cir(int maxm, bool inject, bool anti, int *bps);
 // user-SDE kernels (fwd_user_*.cu): device or injected noise; sys: systems
 // of equations (SDE_MODEL_USER_SYS)
-FwdLauncher<float> find_fwd_f32_user(int maxm, bool inject, bool sys, int *bps);
-FwdLauncher<double> find_fwd_f64_user(int maxm, bool inject, bool sys, int *bps);
+FwdLauncher<float> find_fwd_f32_user(int maxm, bool inject, bool sys, bool jumps, int *bps);
+FwdLauncher<double> find_fwd_f64_user(int maxm, bool inject, bool sys, bool jumps, int *bps);
+// the same with dn / dj terms (fwd_user_jump_*.cu: single equations;
+// fwd_user_jump_sys_*.cu: systems)
+FwdLauncher<float> find_fwd_f32_user_jump(int maxm, bool inject, bool sys, int *bps);
+FwdLauncher<double> find_fwd_f64_user_jump(int maxm, bool inject, bool sys, int *bps);
+FwdLauncher<float> find_fwd_f32_user_jump_sys(int maxm, bool inject, int *bps);
+FwdLauncher<double> find_fwd_f64_user_jump_sys(int maxm, bool inject, int *bps);
 // antithetic kernels (device noise, groups of up to 8 states)
 FwdLauncher<float> find_fwd_f32_anti(int model, int maxm, bool jumps, int *bps);
 // FP32 antithetic kernels with per-step coefficients and correlation factors

@@ -150,19 +150,23 @@ class _gpu_process:
         y = self._args.get('y')
         return uniform_rv(0, 1) if y is None else y
 
-    def _setup_sources(self):
-        A = self._args
-        self.corr = get_corr_matrix(A['corr'], A['rho'])
+    def _setup_corr(self, corr, rho):
+        """The Wiener source's correlation (sdepy/infrastructure.py:1388-1460)."""
+        self.corr = get_corr_matrix(corr, rho)
         if self.corr is not None:
             if self.wshape == ():
                 raise ValueError(
                     'if vshape is (), no correlations apply, but '
-                    'corr={}, rho={} were given'.format(A['corr'], A['rho']))
+                    'corr={}, rho={} were given'.format(corr, rho))
             if self.corr.shape is not None and self.corr.shape[:2] != 2*self.wshape[-1:]:
                 raise ValueError(
                     'cannot instantiate a Wiener source with '
                     'values shape {} and correlation matrix shape {}'
                     .format(self.wshape, self.corr.shape))
+
+    def _setup_sources(self):
+        A = self._args
+        self._setup_corr(A['corr'], A['rho'])
         jumps = 'dj' in self._sources
         # antithetic paths drawn on the device: dw=odd_wiener_source and, for
         # jump models, dj=even_cpoisson_source (sdepy's antithetic sources,
@@ -373,6 +377,11 @@ class _gpu_process:
             tab[k] = self._coefficients(t=t0, tmid=t0 + (t1 - t0)/2)[1]
         return np.ascontiguousarray(tab)
 
+    def _lam_table(self, leg):
+        """Per-step Poisson intensities of the grid (SdeGrid.lam_t), or
+        None: the preset models carry theirs in the parameter table."""
+        return None
+
     def _corr_table(self, leg):
         """[n_steps][M][M] correlation matrices of the steps of ``leg``,
         each at its midpoint t + dt/2 (sdepy/infrastructure.py:1540)."""
@@ -418,6 +427,8 @@ class _gpu_process:
             g.params_t = _lib.dptr(ptab)
             ctab = self._corr_table(leg) if (self._corr_tdep and not self._inject) else None
             g.corr_t = _lib.dptr(ctab)
+            ltab = None if self._inject else self._lam_table(leg)
+            g.lam_t = _lib.dptr(ltab)
             out = _lib.SdeOut()
             out.xx = None if xx is None else xx.ctypes.data
             out.n_rows = rows
@@ -439,6 +450,7 @@ class _gpu_process:
                 noise.dw = _lib.dptr(dw)
                 if dj is not None:
                     noise.dj = _lib.dptr(np.ascontiguousarray(dj))
+                if dn is not None:
                     noise.dn = _lib.lptr(dn)
             if stats is not None and stats['row'] in leg.out_row:
                 req, so, arrs = self._stats_request(stats)

@@ -2,7 +2,7 @@
 (sdepy/integration.py:1843-1955).
 
 ``@integrate`` turns a function ``sde(t, x, **params)`` returning the
-coefficients ``{'dt': A_dt, 'dw': A_dw}`` of one Ito SDE into a process
+coefficients ``{'dt': A_dt, 'dw': A_dw, ...}`` of one Ito SDE into a process
 class, as sdepy does.  Here the function is traced once, at decoration, with
 symbolic values for t, x and the parameters: every arithmetic operation and
 numpy ufunc it applies is recorded, in Python's evaluation order, into a
@@ -14,14 +14,19 @@ of roundings.
 
 Supported (no CPU fallback -- anything else raises NotImplementedError at
 decoration): one equation, or a system of up to 8 (``q``, sdepy's SDEs),
-driven by 'dt' and / or 'dw'; up to 6 parameters,
+driven by any of 'dt', 'dw', 'dn' (Poisson increments, sdepy's source_dn,
+sdepy/integration.py:1346-1378) and 'dj' (compound Poisson increments,
+source_dj, :1380-1423; jump sizes ``y`` of the norm / uniform / exp /
+double_exp laws, intensity ``lam`` constant or a function of t); up to 6
+parameters,
 constant or functions / processes of t, per state variable; +, -, *, /,
 unary -, abs, ** (numpy's fast forms for the exponents 2, 0.5, -1, 1, 0),
 and numpy's exp, log, sqrt, maximum, minimum, sin, cos, tan, tanh, power,
 expm1, log1p, arctan, square, absolute, negative; correlated Wiener
-increments through ``corr`` / ``rho``; the ``log`` flag.  Control flow on the
-state (``if x > 0``, Python's ``max``) and other sources (jumps) are
-refused.
+increments through ``corr`` / ``rho``; the ``log`` flag; sources given as
+arguments (``dw=``, ``dn=``, ``dj=``), realised on the host and replayed.
+Control flow on the state (``if x > 0``, Python's ``max``), antithetic
+sources and other source ids are refused.
 """
 import ctypes as C
 import inspect
@@ -30,8 +35,12 @@ import numbers
 import numpy as np
 
 from . import _lib
-from .infrastructure import process
-from .integration import _const, _gpu_process, _per_var
+from .infrastructure import (
+    process, law_of, uniform_rv, wiener_source, poisson_source, cpoisson_source,
+    odd_wiener_source, even_poisson_source, even_cpoisson_source)
+from .integration import _const, _gpu_process, _per_var, _check_source
+
+_SOURCE_IDS = {'dt': _lib.SRC_DT, 'dw': _lib.SRC_DW, 'dn': _lib.SRC_DN, 'dj': _lib.SRC_DJ}
 
 _MAX_PARAMS = 6
 
@@ -207,16 +216,23 @@ def compile_sde(f, pnames, q=0):
     if As is None or len(As) != neq or not all(isinstance(z, dict) for z in As):
         raise NotImplementedError('the SDE function must return {}'.format(
             'a dict of coefficients' if q == 0 else 'one dict of coefficients per equation'))
-    srcs = {'dt': _lib.SRC_DT, 'dw': _lib.SRC_DW}
+    srcs = _SOURCE_IDS
     for z in As:
         for k in z:
             if k not in srcs:
                 raise NotImplementedError('source {!r} is not supported by the GPU integrator of '
-                                          'user SDEs (dt and dw are)'.format(k))
+                                          'user SDEs (dt, dw, dn and dj are)'.format(k))
     if q == 0:
         order = list(As[0])          # the dict's order: the Euler sum's
-    else:                            # sdepy packs the union of the equations' ids;
-        order = [k for k in ('dt', 'dw') if any(k in z for z in As)]   # 2 terms commute
+    else:
+        # sdepy packs the union of the equations' ids and sums in the
+        # iteration order of that set (sdepy/integration.py:1726-1731),
+        # which follows string hashing; the equations' first-appearance
+        # order is used here (two terms commute; with more the sums agree
+        # to rounding)
+        order = []
+        for z in As:
+            order += [k for k in z if k not in order]
     u = _lib.SdeUserProgram()
     u.n_eq = neq
     u.n_terms = len(order)
@@ -264,9 +280,123 @@ class _user_process(_gpu_process):
             prm[i] = _per_var(self._p(n, t), ws, P, n)
         return np.ascontiguousarray(x0), np.ascontiguousarray(prm)
 
+    # --- sources (sdepy's SDE.source_dw / source_dn / source_dj,
+    # sdepy/integration.py:1311-1423) --------------------------------------
+    def _source_defaults(self):
+        ids = self.sources_ids
+        d = {}
+        if 'dw' in ids:
+            d.update(dw=None, corr=None, rho=None)
+        if 'dn' in ids or 'dj' in ids:
+            d.update(dn=None, ptype=int, lam=1.)
+        if 'dj' in ids:
+            d.update(dj=None, y=None)
+        return d
+
+    def _setup_sources(self):
+        A, ids = self._args, self.sources_ids
+        self._setup_corr(A.get('corr'), A.get('rho'))
+        if A.get('dw') is odd_wiener_source or A.get('dn') is even_poisson_source or \
+           A.get('dj') is even_cpoisson_source:
+            raise NotImplementedError('antithetic sources of user SDEs are not supported by the GPU '
+                                      'integrator')
+        self._anti = False
+        self._inject = any(A.get(k) is not None for k in ('dw', 'dn', 'dj'))
+        self._law_kind, self._law = None, None
+        if 'dj' in ids:
+            self._law_kind, self._law = law_of(uniform_rv(0, 1) if A['y'] is None else A['y'])
+            if self._law_kind is None and not self._inject:
+                raise NotImplementedError('jump-size law {!r} is not supported by the GPU '
+                                          'integrator'.format(A['y']))
+        if not self._inject:
+            self.sources = {}
+            return
+        # sources given as arguments: every source of the SDE is realised on
+        # the host, sdepy's way, and replayed
+        missing = [k for k in ('dw', 'dn', 'dj') if k in ids and A[k] is None]
+        if missing and not isinstance(self._rng, (np.random.Generator, np.random.RandomState)):
+            raise NotImplementedError('sources realised on the host need a numpy rng')
+        rng, ws, P = self._rng, self.wshape, self.paths
+        y = uniform_rv(0, 1) if A.get('y') is None else A['y']
+
+        def setup(z, cls, **kw):
+            if z is None:
+                return cls(paths=P, vshape=ws, rng=rng, **kw)
+            if isinstance(z, type):
+                return z(paths=P, vshape=ws, rng=rng, **kw)
+            _check_source(z, P, ws)
+            return z
+        srcs = {}
+        if 'dw' in ids:
+            srcs['dw'] = setup(A['dw'], wiener_source, dtype=self.dtype, corr=A['corr'], rho=A['rho'])
+        if 'dn' in ids:
+            srcs['dn'] = setup(A['dn'], poisson_source, dtype=A['ptype'], lam=A['lam'])
+        if 'dj' in ids:
+            srcs['dj'] = setup(A['dj'], cpoisson_source, dtype=self.dtype, dn=A['dn'], ptype=A['ptype'],
+                               lam=A['lam'], y=y)
+        self.sources = srcs
+
+    def _realise(self, leg):
+        """Host realisation of the SDE's sources along one leg, in sdepy's
+        order (ascending ids: dj, dn, dw, sdepy/integration.py:1227-1234)."""
+        n, W, paths = leg.n_steps, self._W, self.paths
+        ids = self.sources_ids
+        arrs = {'dw': np.empty((n, W, paths)) if 'dw' in ids else None,
+                'dj': np.empty((n, W, paths)) if 'dj' in ids else None,
+                'dn': np.empty((n, W, paths), dtype=np.int64) if 'dn' in ids else None}
+        for k in range(n):
+            t, dt = leg.tt[k], leg.tt[k + 1] - leg.tt[k]
+            for sid in sorted(self.sources):
+                v = self.sources[sid](t, dt)
+                arrs[sid][k] = np.broadcast_to(v, self.wshape + (paths,)).reshape(W, paths)
+        return arrs['dw'], arrs['dj'], arrs['dn']
+
+    def _jumps(self):
+        return 'dn' in self.sources_ids or 'dj' in self.sources_ids
+
+    def _lam_table(self, leg):
+        """[n_steps][W] Poisson intensity at each step's midpoint, when
+        ``lam`` depends on time."""
+        if not self._jumps() or not callable(self._args['lam']):
+            return None
+        tt = leg.tt
+        tab = np.empty((leg.n_steps, self._W))
+        for k in range(leg.n_steps):
+            t0, t1 = float(tt[k]), float(tt[k + 1])
+            tab[k] = _per_var(self._p('lam', t0 + (t1 - t0)/2), self.wshape, self.paths, 'lam')
+        return np.ascontiguousarray(tab)
+
+    def _setup_spec(self):
+        super()._setup_spec()
+        ids = self.sources_ids
+        self._jump_law_id = _lib.JUMP_NONE
+        if 'dj' in ids:
+            self._jump_law_id = {
+                'norm': _lib.JUMP_NORM, 'double_exp': _lib.JUMP_DOUBLE_EXP,
+                'uniform': _lib.JUMP_UNIFORM, 'exp': _lib.JUMP_EXP,
+                None: _lib.JUMP_NORM}[self._law_kind]
+        # per state: lam (when constant), the jump-size law's a, b, pa
+        self._jp = None
+        if self._jumps():
+            ws, P = self.wshape, self.paths
+            jp = np.zeros((4, self._W))
+            lam = self._args['lam']
+            if not self._inject and not callable(lam):
+                jp[0] = _per_var(_const(lam, 'lam'), ws, P, 'lam')
+            law = self._law
+            if law is not None and not self._inject:
+                names = {'norm': ('a', 'b'), 'uniform': ('a', 'b'), 'exp': ('a',),
+                         'double_exp': ('a', 'b', 'pa')}[self._law_kind]
+                for i, n in enumerate(names):
+                    jp[1 + i] = _per_var(getattr(law, n), ws, P, n)
+            self._jp = np.ascontiguousarray(jp)
+
     def _make_spec(self, seed=0, stream=0):
         s = super()._make_spec(seed, stream)
-        s.program = C.pointer(self._program)
+        # the program with this instance's jump parameters
+        self._uprog = _lib.SdeUserProgram.from_buffer_copy(self._program)
+        self._uprog.jump_params = _lib.dptr(self._jp)
+        s.program = C.pointer(self._uprog)
         return s
 
 
@@ -366,9 +496,9 @@ def integrate(sde=None, *, q=None, sources=None, log=False, addaxis=False):
     if neq > _lib.USER_MAX_EQ:
         raise NotImplementedError('systems of more than {} equations are not supported by the GPU '
                                   'integrator'.format(_lib.USER_MAX_EQ))
-    if not ids <= {'dt', 'dw'}:
+    if not ids <= set(_SOURCE_IDS):
         raise NotImplementedError('sources {} are not supported by the GPU integrator of user '
-                                  'SDEs (dt and dw are)'.format(sorted(ids - {'dt', 'dw'})))
+                                  'SDEs (dt, dw, dn and dj are)'.format(sorted(ids - set(_SOURCE_IDS))))
     defaults = _sde_parameters(sde, max(neq, 1))
     if len(defaults) > _MAX_PARAMS:
         raise NotImplementedError('user SDEs take at most {} parameters on the GPU, not {}'

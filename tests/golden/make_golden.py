@@ -4,7 +4,7 @@ Run in a container where the reference is importable:
 
     python tests/golden/make_golden.py [REFERENCE_DIR [GROUP ...]]
 
-(groups path, mc, tdep, cir, corr_t, user; all by default)
+(groups path, mc, tdep, cir, corr_t, user, user_jump; all by default)
 
 REFERENCE_DIR defaults to /root/reference (the read-only sdepy checkout).
 Nothing under tests/ imports this script; the tests only read the .npz files
@@ -338,15 +338,109 @@ def user_cases(sdepy):
          np.linspace(0, 2, 3), (4,), paths=32, steps=40, i0=1, seed=68)
 
 
+def run_user_jump_case(sdepy, name, spec, kw, timeline, wshape, *, paths, steps, lam, law, seed, i0=0,
+                       rho=None):
+    """A user SDE with Poisson (dn) and / or compound Poisson (dj) terms:
+    each of its sources (sdepy's wiener_source, poisson_source and
+    cpoisson_source with intensity ``lam`` and jump sizes ``law``) wrapped
+    in a recorder and passed as dw= / dn= / dj=.  Saved: every source's
+    increments (rec_dw, rec_dnsrc, rec_dj with its counts rec_dn), the ids,
+    and for a system the order in which the reference sums its packed terms
+    (the iteration order of the set of ids built as sdepy's SDEs.A builds
+    it, sdepy/integration.py:1726-1731, in this process)."""
+    import helpers as H
+    inf = sdepy.infrastructure
+    cls = H.user_class(sdepy, spec)
+    f = H.USER[spec.split(':')[1]]
+    kind = spec.split(':')[0].split('_')
+    q = next((int(x[1:]) for x in kind if x.startswith('q')), 0)
+    one = np.array(1.)
+    As = f(one, *(one,)*max(q, 1))
+    As = As if q else (As,)
+    A_ids = set()
+    for z in As:
+        A_ids.update(z.keys())
+    order = list(A_ids) if q else list(As[0])
+    rng = np.random.default_rng(seed)
+    lam_v = H.TDEP[lam[1:]] if isinstance(lam, str) else lam
+    y = None
+    if law is not None:
+        k = law['kind']
+        y = {'norm': lambda: sdepy.norm_rv(a=law['a'], b=law['b']),
+             'uniform': lambda: sdepy.uniform_rv(a=law['a'], b=law['b']),
+             'exp': lambda: sdepy.exp_rv(a=law['a']),
+             'double_exp': lambda: sdepy.double_exp_rv(a=law['a'], b=law['b'], pa=law['pa'])}[k]()
+    recs = {}
+    if 'dw' in A_ids:
+        recs['dw'] = Recorder(inf.wiener_source(paths=paths, vshape=wshape, rng=rng, rho=rho))
+    if 'dn' in A_ids:
+        recs['dn'] = Recorder(inf.poisson_source(paths=paths, vshape=wshape, rng=rng, lam=lam_v))
+    if 'dj' in A_ids:
+        recs['dj'] = Recorder(inf.cpoisson_source(paths=paths, vshape=wshape, rng=rng, lam=lam_v, y=y))
+    args = dict(kw)
+    args.update(paths=paths, steps=steps, i0=i0, **recs)
+    P = cls(**args)
+    out = P(timeline)
+    outs = out if isinstance(out, tuple) else (out,)
+    arrays = {}
+    rec = {
+        'name': name, 'cls': spec, 'paths': paths, 'timeline': np.asarray(timeline),
+        'steps': json.dumps(steps), 'i0': i0, 'kw': encode_kw(sdepy, kw, arrays),
+        'ids': json.dumps(sorted(A_ids)), 'term_order': json.dumps(order),
+        'lam': json.dumps(lam), 'law': json.dumps(law), 'rho': json.dumps(rho),
+        'n_out': len(outs), 'computed_steps': P.info['computed_steps'],
+        'stored_steps': P.info['stored_steps'],
+    }
+    for sid, key in (('dw', 'rec_dw'), ('dn', 'rec_dnsrc'), ('dj', 'rec_dj')):
+        if sid in recs:
+            rec[key] = np.stack([np.broadcast_to(c[2], wshape + (paths,)) for c in recs[sid].calls])
+    if 'dj' in recs:
+        rec['rec_dn'] = np.stack([np.broadcast_to(c[3], wshape + (paths,))
+                                  for c in recs['dj'].calls]).astype(np.int64)
+    for k, o in enumerate(outs):
+        rec['xx%d' % k] = np.asarray(o)
+        rec['t%d' % k] = np.asarray(o.t)
+    rec.update(arrays)
+    np.savez_compressed(os.path.join(HERE, 'userj_%s.npz' % name), **rec)
+    print('wrote userj_%s.npz' % name, order)
+
+
+def user_jump_cases(sdepy):
+    """User SDEs with dn / dj terms: single equations (a log-space Merton
+    form, the reference's test_jumps form integrated as is, all four
+    sources) and the reference's test_integrator systems with Poisson and
+    compound Poisson jumps (sdepy/tests/test_integrator.py:295-365), with
+    time-dependent k and lam."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    import helpers as H
+    lin = np.linspace
+    run_user_jump_case(sdepy, 'jd_log', 'integrate_log:user_jd_log', dict(x0=1., mu=.03, sigma=.15),
+                       lin(0, 1, 5), (), paths=40, steps=40, lam=3., law=dict(kind='norm', a=-.1, b=.15), seed=71)
+    run_user_jump_case(sdepy, 'jd_asis', 'integrate:user_jd_asis', dict(x0=1., mu=-.1, sigma=.05, vshape=2),
+                       (1., 1.5, 2.), (2,), paths=32, steps=50, lam=5., law=dict(kind='uniform', a=.05, b=.1),
+                       seed=72)
+    run_user_jump_case(sdepy, 'jumps4', 'integrate:user_jumps4', dict(x0=.5, a=.3, b=.5, s=.2),
+                       lin(0, 2, 3), (), paths=40, steps=60, i0=1, lam='@tdep_lam',
+                       law=dict(kind='exp', a=-.2), seed=73)
+    run_user_jump_case(sdepy, 'sys_dn', 'integrate_q2:user_sys_dn', dict(x0=(0., 0.), k=H.tdep_kj),
+                       lin(0, 1, 4), (2,), paths=36, steps=30, lam='@tdep_lam', law=None, seed=74)
+    run_user_jump_case(sdepy, 'sys_dn_dw', 'integrate_q2:user_sys_dn_dw', dict(x0=(0., 0.), k=H.tdep_kj),
+                       lin(0, 1, 4), (2,), paths=36, steps=30, lam=2., law=None, rho=-.5, seed=75)
+    run_user_jump_case(sdepy, 'sys_dj_dw', 'integrate_q2:user_sys_dj_dw', dict(x0=(0., 0.), k=.7),
+                       lin(0, 1, 4), (2,), paths=36, steps=30, lam=3.,
+                       law=dict(kind='double_exp', a=1., b=2., pa=.1), rho=-.5, seed=76)
+
+
 def main():
-    # python make_golden.py [REFERENCE_DIR [GROUP ...]], groups path, mc, tdep, cir, corr_t, user
+    # python make_golden.py [REFERENCE_DIR [GROUP ...]], groups path, mc, tdep, cir, corr_t, user, user_jump
     ref = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
-    groups = sys.argv[2:] or ['path', 'mc', 'tdep', 'cir', 'corr_t', 'user']
+    groups = sys.argv[2:] or ['path', 'mc', 'tdep', 'cir', 'corr_t', 'user', 'user_jump']
     sys.path.insert(0, ref)
     import sdepy
     print('sdepy', sdepy.__version__, 'numpy', np.__version__)
     for name, f in (('path', path_cases), ('mc', mc_cases), ('tdep', tdep_cases), ('cir', cir_cases),
-                    ('corr_t', tdep_corr_cases), ('user', user_cases)):
+                    ('corr_t', tdep_corr_cases), ('user', user_cases), ('user_jump', user_jump_cases)):
         if name in groups:
             f(sdepy)
 

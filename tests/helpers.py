@@ -28,6 +28,8 @@ def oracle_paths(clib, proc, timeline, seed, stream=0):
         g.params_t = _lib.dptr(ptab)
         ctab = proc._corr_table(leg) if proc._corr_tdep else None   # time-dependent correlation
         g.corr_t = _lib.dptr(ctab)
+        ltab = proc._lam_table(leg)   # a user SDE's time-dependent Poisson intensity
+        g.lam_t = _lib.dptr(ltab)
         neg = np.zeros((proc._G*proc._M//2, proc.paths), dtype=np.int32)
         jc = np.zeros((proc._W, proc.paths), dtype=np.int32)
         rj = np.zeros(rows, dtype=np.int64)
@@ -211,6 +213,10 @@ def tdep_corr4(t):
     return C/np.outer(d, d)
 
 
+def tdep_kj(t):
+    return .5 + .3*t
+
+
 TDEP = {name: f for name, f in dict(globals()).items() if name.startswith('tdep_')}
 
 
@@ -250,7 +256,48 @@ def user_coupled(t, x, y, a=1., b=.5, c=.3, s=.2):
     return ({'dt': -a*x + b*y, 'dw': s}, {'dt': c*x - a*y})
 
 
+def user_jd_log(t, x, mu=.03, sigma=.15):
+    # Merton's jump diffusion in log space (integrate(log=True)): jumps of
+    # the compound Poisson source's law added to log x
+    return {'dt': mu - sigma*sigma/2, 'dw': sigma, 'dj': 1}
+
+
+def user_jd_asis(t, x, mu=0., sigma=1.):
+    # a jump diffusion integrated as is, the form of the reference's
+    # test_jumps (sdepy/tests/test_processes.py:614-619)
+    return {'dt': mu*x, 'dw': sigma*x, 'dj': x}
+
+
+def user_jumps4(t, x, a=.3, b=.5, s=.2):
+    # every source, the Euler sum of four terms in the dict's order
+    return {'dn': a, 'dt': -b*x, 'dj': x, 'dw': s}
+
+
+def user_sys_dn(t, x, y, k=1.):
+    # systems with Poisson jumps, the forms of the reference's
+    # test_integrator (sdepy/tests/test_integrator.py:295-365)
+    return ({'dt': x, 'dn': k}, {'dt': 1, 'dn': k*y})
+
+
+def user_sys_dn_dw(t, x, y, k=1.):
+    return ({'dt': x, 'dn': k, 'dw': y}, {'dt': 1, 'dn': k*y, 'dw': x - y})
+
+
+def user_sys_dj_dw(t, x, y, k=1.):
+    return ({'dt': x, 'dj': k, 'dw': y}, {'dt': 1, 'dj': k*y, 'dw': x - y})
+
+
 USER = {name: f for name, f in dict(globals()).items() if name.startswith('user_')}
+
+
+def user_sources(f, q):
+    """The source ids of a system's SDE function (its equations' keys at
+    unit arguments)."""
+    one = np.array(1.)
+    ids = set()
+    for z in f(one, *(one,)*q):
+        ids.update(z.keys())
+    return ids
 
 
 def user_class(module, spec):
@@ -260,7 +307,8 @@ def user_class(module, spec):
     kind, name = spec.split(':')
     parts = kind.split('_')
     q = next((int(x[1:]) for x in parts if x.startswith('q')), None)
-    return module.integrate(USER[name], q=q, sources={'dt', 'dw'} if q else None, log='log' in parts,
+    f = USER[name]
+    return module.integrate(f, q=q, sources=user_sources(f, q) if q else None, log='log' in parts,
                             addaxis='addaxis' in parts)
 
 

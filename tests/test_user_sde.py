@@ -10,6 +10,12 @@ interprets per state variable and step.
 * GPU: the device replays the same increments to 1e-12 (FP64); with device
   noise it matches the C oracle (which evaluates the same program in C) to
   1e-12, and FP32 matches it to FP32 accuracy.
+* Jump sources (dn, dj): the reference's recorded Wiener, Poisson and
+  compound Poisson increments (tests/golden/userj_*.npz) replay to its
+  paths exactly through the numpy oracle and to 1e-12 on the device; with
+  device noise a log-space Merton SDE written by the user gives the
+  merton_jumpdiff_process preset's paths bit for bit (C oracle on the CPU,
+  FP64 kernels on the GPU).
 """
 import glob
 import json
@@ -21,10 +27,12 @@ import pytest
 import sdepy_gb300 as sg
 from sdepy_gb300 import _lib
 from conftest import GOLDEN
-from helpers import USER, oracle_paths, tdep_kwargs, user_class
+from helpers import USER, oracle_paths, tdep_kwargs, user_class, user_sources
 from oracle import euler
 
 CASES = sorted(glob.glob(os.path.join(GOLDEN, 'user_*.npz')))
+JCASES = sorted(glob.glob(os.path.join(GOLDEN, 'userj_*.npz')))
+KEYS = {_lib.SRC_DT: 'dt', _lib.SRC_DW: 'dw', _lib.SRC_DN: 'dn', _lib.SRC_DJ: 'dj'}
 
 
 def _run_program(u, x, t, params, ys=()):
@@ -61,7 +69,7 @@ def test_program_equals_function(name):
     f = USER[name]
     nvars = sum(p.default is p.empty for p in inspect.signature(f).parameters.values()) - 1
     q = nvars if nvars > 1 else None
-    cls = sg.integrate(f, q=q, sources={'dt', 'dw'} if q else None)
+    cls = sg.integrate(f, q=q, sources=user_sources(f, q) if q else None)
     g = np.random.default_rng(1)
     xs = [np.abs(g.normal(size=1000)) + .01 for _ in range(nvars)]
     t = .37
@@ -70,7 +78,7 @@ def test_program_equals_function(name):
     with np.errstate(all='ignore'):
         As = f(t, *xs, **dict(zip(cls._pnames, params)))
     As = As if q else (As,)
-    keys = [{0: 'dt', 1: 'dw'}[s] for s in srcs]
+    keys = [KEYS[s] for s in srcs]
     if not q:
         assert keys == list(As[0])   # the dict's order
     for vals, A in zip(got, As):
@@ -93,10 +101,10 @@ def test_tracer_forms_and_refusals():
         @sg.integrate
         def b2(t, x):
             return {'dt': max(x, 0.), 'dw': 1.}
-    with pytest.raises(NotImplementedError):       # jumps
+    with pytest.raises(NotImplementedError):       # a source id sdepy does not define
         @sg.integrate
         def b3(t, x, a=1.):
-            return {'dt': a, 'dw': 1., 'dj': 1.}
+            return {'dt': a, 'dw': 1., 'dq': 1.}
     with pytest.raises(NotImplementedError):       # a system of nine equations
         @sg.integrate(q=9, sources={'dt', 'dw'})
         def b4(t, x, *ys, a=1.):
@@ -220,3 +228,161 @@ def test_user_sde_refusals(lib):
     import torch
     with pytest.raises(NotImplementedError):
         expectation(cls, (0., 1.), [], paths=100, steps=10, x0=torch.tensor(1., requires_grad=True))
+
+
+# ---------------------------------------------------------------------------
+# jump sources
+# ---------------------------------------------------------------------------
+def _jump_replays(z, paths):
+    """Replays of a userj fixture's recorded sources, by id."""
+    out = {}
+    for sid, key in (('dw', 'rec_dw'), ('dn', 'rec_dnsrc'), ('dj', 'rec_dj')):
+        if key in z:
+            out[sid] = euler.Replay(z[key], dn=z['rec_dn'] if sid == 'dj' else None, paths=paths,
+                                    vshape=z[key].shape[1:-1])
+    return out
+
+
+@pytest.mark.parametrize('path', JCASES, ids=os.path.basename)
+def test_numpy_oracle_reproduces_reference_jumps(path):
+    z = np.load(path)
+    kw, vshape, paths = _fixture_args(z)
+    name, q, log, addaxis = _spec(z)
+    srcs = _jump_replays(z, paths)
+    res, info = euler.integrate('user', kw, z['timeline'], paths=paths, vshape=vshape,
+                                steps=json.loads(str(z['steps'])), i0=int(z['i0']), sde=USER[name],
+                                log_flag=log, sde_q=q, addaxis=addaxis, sde_sources=json.loads(str(z['ids'])),
+                                term_order=json.loads(str(z['term_order'])) if q else None, **srcs)
+    for k, o in enumerate(_outputs(res)):
+        np.testing.assert_array_equal(o, z['xx%d' % k])
+    assert info['computed_steps'] == int(z['computed_steps'])
+
+
+def test_user_jump_sources_and_arguments():
+    """The drop-in's keyword surface follows sdepy's source_dn / source_dj
+    (sdepy/integration.py:1346-1423): lam / ptype with a dn or dj term, y
+    with dj, corr / rho only with dw; jump programs carry their sources."""
+    jd = user_class(sg, 'integrate_log:user_jd_log')
+    P = jd(paths=8, lam=2., y=sg.norm_rv(-.1, .2))
+    assert {'lam', 'y', 'dn', 'dj', 'ptype', 'dw', 'corr', 'rho'} <= set(P.args)
+    srcs = [jd._program.term_source[i] for i in range(jd._program.n_terms)]
+    assert srcs == [_lib.SRC_DT, _lib.SRC_DW, _lib.SRC_DJ]
+    sysdn = user_class(sg, 'integrate_q2:user_sys_dn')
+    with pytest.raises(TypeError):   # no Wiener source: corr is unexpected, as in sdepy
+        sysdn(paths=4, x0=(0., 0.), corr=np.eye(2))
+    with pytest.raises(TypeError):   # no compound Poisson source: no y
+        sysdn(paths=4, x0=(0., 0.), y=sg.norm_rv(0., 1.))
+    with pytest.raises(NotImplementedError):   # antithetic sources
+        jd(paths=4, dj=sg.even_cpoisson_source)
+    with pytest.raises(NotImplementedError):   # a time-dependent jump-size law on the device
+        jd(paths=4, y=object())
+
+
+def _spec_run(clib, P, tl, seed, stream):
+    ref, _ = oracle_paths(clib, P, tl, seed, stream)
+    return ref
+
+
+def test_c_oracle_user_merton_equals_preset(clib):
+    """The C oracle's user-program path with a dj term draws the preset's
+    Poisson words and jump sizes: a log-space Merton SDE gives the
+    merton_jumpdiff_process paths exactly (FP64), also for groups of 4."""
+    jd = user_class(sg, 'integrate_log:user_jd_log')
+    tl = np.linspace(0, 1, 5)
+    for vshape in ((), (4,)):
+        kw = dict(paths=257, vshape=vshape, steps=50, x0=1., mu=.03, sigma=.15, lam=3.)
+        U = jd(rng=sg.philox_rng(9, 1), y=sg.norm_rv(-.1, .15), **kw)
+        M = sg.merton_jumpdiff_process(rng=sg.philox_rng(9, 1), a=-.1, b=.15, **kw)
+        assert U._M == M._M and U._G == M._G
+        xu = _spec_run(clib, U, tl, 9, 1)
+        xm = _spec_run(clib, M, tl, 9, 1)
+        np.testing.assert_array_equal(xu, xm)
+
+
+JDEVICE_CASES = [
+    ('jd_log', 'integrate_log:user_jd_log', dict(x0=1., mu=.03, sigma=.15, lam=3., y=('norm', -.1, .15)),
+     np.linspace(0, 1, 5), 40, 0),
+    ('jd_asis_vec2', 'integrate:user_jd_asis', dict(vshape=2, x0=1., mu=-.1, sigma=.05, lam=5.,
+                                                     y=('uniform', .05, .1)), (1., 1.5, 2.), 50, 0),
+    ('jumps4_i0', 'integrate:user_jumps4', dict(x0=.5, lam='tdep_lam', y=('exp', -.2)),
+     np.linspace(0, 2, 3), 60, 1),
+    ('jumps4_vec3', 'integrate:user_jumps4', dict(vshape=3, x0=.5, lam=2., y=('double_exp', .3, .2, .4)),
+     (0., 1.), 40, 0),
+    ('sys_dn', 'integrate_q2:user_sys_dn', dict(x0=(0., 0.), k='tdep_kj', lam='tdep_lam'),
+     np.linspace(0, 1, 4), 30, 0),
+    ('sys_dn_dw', 'integrate_q2:user_sys_dn_dw', dict(x0=(0., 0.), k='tdep_kj', lam=2., rho=-.5),
+     np.linspace(0, 1, 4), 30, 0),
+    ('sys_dj_dw_vec2', 'integrate_q2:user_sys_dj_dw', dict(vshape=2, x0=(0., 0.), k=.7, lam=3.,
+                                                            y=('double_exp', 1., 2., .1)),
+     np.linspace(0, 1, 4), 30, 0),
+]
+
+
+def _jkw(kw):
+    from helpers import TDEP
+    out = {}
+    for k, v in kw.items():
+        if isinstance(v, str):
+            out[k] = TDEP[v]
+        elif k == 'y':
+            out[k] = {'norm': sg.norm_rv, 'uniform': sg.uniform_rv, 'exp': sg.exp_rv,
+                      'double_exp': sg.double_exp_rv}[v[0]](*v[1:])
+        else:
+            out[k] = v
+    return out
+
+
+def test_c_oracle_user_jumps_runs(clib):
+    """Every device case runs through the C oracle with jumps drawn (no
+    GPU): the dn / dj terms move the paths."""
+    for name, spec, kw, tl, steps, i0 in JDEVICE_CASES:
+        P = user_class(sg, spec)(paths=64, steps=steps, i0=i0, rng=sg.philox_rng(3, 4), **_jkw(kw))
+        ref = _spec_run(clib, P, tl, 3, 4)
+        assert np.isfinite(ref).all(), name
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('path', JCASES, ids=os.path.basename)
+def test_gpu_replay_matches_reference_jumps(lib, path):
+    z = np.load(path)
+    kw, vshape, paths = _fixture_args(z)
+    cls = user_class(sg, str(z['cls']))
+    P = cls(paths=paths, vshape=vshape, steps=json.loads(str(z['steps'])), i0=int(z['i0']),
+            **_jump_replays(z, paths), **kw)
+    outs = _outputs(P(z['timeline']))
+    assert len(outs) == int(z['n_out'])
+    for k, x in enumerate(outs):
+        ref = z['xx%d' % k]
+        assert x.shape == ref.shape
+        err = np.max(np.abs(np.asarray(x) - ref)/np.maximum(np.abs(ref), 1.))
+        assert err <= 1e-12, err
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('case', JDEVICE_CASES, ids=[c[0] for c in JDEVICE_CASES])
+def test_device_rng_jumps_match_c_oracle(lib, clib, case):
+    name, spec, kw, tl, steps, i0 = case
+    cls = user_class(sg, spec)
+    paths, seed = 513, 0x7a11
+    P = cls(paths=paths, steps=steps, i0=i0, rng=sg.philox_rng(seed, 5), **_jkw(kw))
+    outs = _outputs(P(tl))
+    refs = _outputs(P.exit(np.asarray(tl), _spec_run(clib, P, tl, seed, 5)))
+    for x, r in zip(outs, refs):
+        err = np.max(np.abs(np.asarray(x) - np.asarray(r))/np.maximum(np.abs(r), 1.))
+        assert err <= 1e-12, err
+    P32 = cls(paths=paths, steps=steps, i0=i0, dtype=np.float32, rng=sg.philox_rng(seed, 5), **_jkw(kw))
+    for x, r in zip(_outputs(P32(tl)), refs):
+        assert np.max(np.abs(np.asarray(x, dtype=float) - r)/np.maximum(np.abs(r), 1.)) < 2e-3
+
+
+@pytest.mark.gpu
+def test_gpu_user_merton_equals_preset(lib):
+    """FP64 device kernels: the user-written log-space Merton SDE and the
+    merton_jumpdiff_process preset give the same paths bit for bit."""
+    jd = user_class(sg, 'integrate_log:user_jd_log')
+    tl = np.linspace(0, 1, 5)
+    for vshape in ((), (4,)):
+        kw = dict(paths=4099, vshape=vshape, steps=100, x0=1., mu=.03, sigma=.15, lam=3.)
+        xu = jd(rng=sg.philox_rng(11, 2), y=sg.norm_rv(-.1, .15), **kw)(tl)
+        xm = sg.merton_jumpdiff_process(rng=sg.philox_rng(11, 2), a=-.1, b=.15, **kw)(tl)
+        np.testing.assert_array_equal(np.asarray(xu), np.asarray(xm))
