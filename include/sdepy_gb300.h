@@ -316,6 +316,8 @@ SDE_API int32_t sde_run_stats(const SdeSpec *spec, const SdeGrid *grid,
  * [groups*M][8]: per state variable d L / d of x0 (integration variable),
  * params p0..p5, and in slot 7 of a group's first variable d L / d rho
  * (2-variable Heston group with corr = [[1, rho], [rho, 1]]).  value = L.
+ * For a user SDE (single equation, dt / dw terms) slot 1 + j is d L / d
+ * of the program's parameter p_j, from a tangent-mode run of its program.
  * The adjoint of the Euler recursion is propagated backwards through
  * checkpointed segments recomputed from Philox counters (constant for the
  * LINEAR model); no path is stored.  No counterpart in the reference

@@ -15,6 +15,10 @@ Differentiable parameters per preset:
   heston_process            x0, mu, sigma, y0, k, theta, xi, rho
   merton_jumpdiff_process   x0, mu, sigma, a, b
   kou_jumpdiff_process      x0, mu, sigma, a, b
+  cox_ingersoll_ross_process x0, k, theta, xi
+  user SDEs (``integrate``)  x0 and every parameter of the SDE function, for
+                             single equations driven by dt / dw (the
+                             device runs the traced program in tangent mode)
 Poisson intensities and the Kou probability pa select integer / discrete
 outcomes and are not differentiated.
 """
@@ -42,12 +46,31 @@ _MAP = {
 }
 
 
-def _param_grads(name, g, vals):
+def _user_map(cls):
+    """Gradient slots of a user SDE class: x0 in slot 0, parameter j of
+    the SDE function in slot 1 + j; None if the class is not a user SDE."""
+    from .usersde import _user_process, _user_sys_process
+    if not (isinstance(cls, type) and issubclass(cls, _user_process)):
+        return None
+    if issubclass(cls, _user_sys_process):
+        raise NotImplementedError('gradients of systems of user SDEs are not supported')
+    if not set(cls.sources_ids) <= {'dt', 'dw'}:
+        raise NotImplementedError('gradients of user SDEs with dn / dj terms are not supported')
+    m = {'x0': (0, 0)}
+    m.update({n: (0, 1 + i) for i, n in enumerate(cls._pnames)})
+    return m
+
+
+def _param_grads(name, g, vals, mp=None, log=False):
     """d/d(user parameter) from the per-state gradient slots g[w][8]."""
-    m = _MAP[name]
+    m = _MAP[name] if mp is None else mp
     out = {}
     for p, (w, j) in m.items():
         out[p] = g[w, j]
+    if mp is not None:   # a user SDE: its state is log x with the log flag
+        if log:
+            out['x0'] = g[0, 0]/vals['x0']
+        return out
     log_models = name in ('lognorm_process', 'merton_jumpdiff_process',
                           'kou_jumpdiff_process', 'heston_process')
     if log_models:
@@ -61,10 +84,11 @@ def _param_grads(name, g, vals):
 class _Expectation(torch.autograd.Function):
 
     @staticmethod
-    def forward(ctx, spec_fn, names, *tensors):
+    def forward(ctx, spec_fn, names, mp, *tensors):
         proc, grid, strikes, seed, stream, value = spec_fn()
         ctx.spec_fn = spec_fn
         ctx.names = names
+        ctx.mp = mp
         ctx.shapes = [t.shape for t in tensors]
         ctx.dtypes = [t.dtype for t in tensors]
         return torch.as_tensor(value, dtype=torch.float64)
@@ -93,13 +117,13 @@ class _Expectation(torch.autograd.Function):
         st = lib.sde_adjoint(C.byref(spec), C.byref(g), C.byref(req),
                              _lib.dptr(grad), C.byref(val))
         _lib.check(st, 'sde_adjoint')
-        vals = {k: float(np.asarray(v)) for k, v in proc.args.items()
-                if k in _MAP[type(proc).__name__]}
-        pg = _param_grads(type(proc).__name__, grad, vals)
+        mp = ctx.mp if ctx.mp is not None else _MAP[type(proc).__name__]
+        vals = {k: float(np.asarray(v)) for k, v in proc.args.items() if k in mp}
+        pg = _param_grads(type(proc).__name__, grad, vals, ctx.mp, getattr(proc, '_log', False))
         outs = []
         for n, shp, dt in zip(ctx.names, ctx.shapes, ctx.dtypes):
             outs.append(torch.full(shp, pg[n], dtype=dt))
-        return (None, None) + tuple(outs)
+        return (None, None, None) + tuple(outs)
 
 
 def expectation(cls, timeline, strikes=(), *, paths, steps=None,
@@ -109,8 +133,10 @@ def expectation(cls, timeline, strikes=(), *, paths, steps=None,
     ``timeline``; torch-tensor parameters with requires_grad get gradients
     from the adjoint kernel (same Philox paths as the forward)."""
     name = cls.__name__
-    if name not in _MAP:
+    mp = _user_map(cls)
+    if mp is None and name not in _MAP:
         raise NotImplementedError('no adjoint for {}'.format(name))
+    pmap = _MAP[name] if mp is None else mp
     strikes = [float(k) for k in strikes]
     if len(strikes) > _lib.MAX_STRIKES:
         raise ValueError('at most {} strikes'.format(_lib.MAX_STRIKES))
@@ -118,7 +144,7 @@ def expectation(cls, timeline, strikes=(), *, paths, steps=None,
     plain = {}
     for k, v in params.items():
         if isinstance(v, torch.Tensor):
-            if k not in _MAP[name]:
+            if k not in pmap:
                 raise NotImplementedError('parameter {!r} is not differentiable'.format(k))
             if v.numel() != 1:
                 raise NotImplementedError('differentiable parameters must be scalars')
@@ -127,7 +153,7 @@ def expectation(cls, timeline, strikes=(), *, paths, steps=None,
             plain[k] = float(v.detach().cpu())
         else:
             plain[k] = v
-    if 'rho' in plain and name != 'heston_process':
+    if 'rho' in plain and mp is None and name != 'heston_process':
         raise NotImplementedError('rho is differentiable for heston_process only')
     if any(k in plain for k in ('dw', 'dj', 'dn')):
         raise NotImplementedError('gradients are taken on the default device sources '
@@ -147,4 +173,4 @@ def expectation(cls, timeline, strikes=(), *, paths, steps=None,
                                     np.asarray(mc.payoff).reshape(-1)))
         return P, grid, strikes, seed, stream, value
 
-    return _Expectation.apply(spec_fn, tuple(names), *tensors)
+    return _Expectation.apply(spec_fn, tuple(names), mp, *tensors)

@@ -6,7 +6,7 @@
 // * LINEAR models (wiener, lognorm, jump-diffusions): dx'/dx = 1, so the
 //   adjoint is constant along the path and one forward sweep accumulating
 //   sum dt, sum dW and the jump-size derivatives gives the exact gradient.
-// * OU and Heston: the path is swept forward once storing the state every
+// * OU, CIR, Heston and user SDEs: the path is swept forward once storing the state every
 //   `seg` steps (checkpoints, seg ~ sqrt(N)); then, segment by segment from
 //   the last, the segment's states and increments are recomputed from their
 //   Philox counters and the adjoint is propagated backwards through it.
@@ -15,6 +15,9 @@
 // Integer Poisson counts are not differentiated (their intensity gets no
 // gradient); the full-truncation kink of Heston's variance and of CIR
 // contributes its one-sided derivative (zero where the state is <= 0).
+// User SDEs (single equations driven by dt / dw): the program is run in
+// tangent mode for dA/dx and dA/dp (user_coefs_tan); slot 1 + j of a state
+// is the gradient of its parameter p_j.
 #pragma once
 #include "sde_kernels.cuh"
 
@@ -43,7 +46,118 @@ struct AdjArgs {
     R wmean;
     double *partials;  // [groups][gridDim.x][MAXM*NGV + 2]
     int32_t *err;
+    // SDE_MODEL_USER: the coefficient program and each step's start time
+    SdeUserProgram uprog;
+    const R *tk;
 };
+
+// Tangent-mode run of a user program (single equation): the terms' values
+// A[i] and their derivatives dA[i][0] = dA_i/dx, dA[i][1 + j] = dA_i/dp_j.
+// Derivative rules per instruction (d = the operands' tangents): sums and
+// products by the chain rule; abs, maximum and minimum take the selected
+// branch (maximum(x, 0) has derivative 0 where x < 0); sqrt has derivative 0
+// at 0 (the one-sided value of the truncated models); a ** b adds the b
+// term v log a only where a > 0.
+constexpr int UTAN = 7;
+template <typename R>
+__device__ __noinline__ void user_coefs_tan(const SdeUserProgram &u, R x, R t, const R (&p)[6],
+                                            R (&A)[SDE_USER_MAX_TERMS], R (&dA)[SDE_USER_MAX_TERMS][UTAN]) {
+    typedef Ar<R> Ao;
+    typedef UFn<R> F;
+    R r[SDE_USER_MAX_REGS];
+    R d[SDE_USER_MAX_REGS][UTAN];
+    r[0] = x;
+    r[1] = t;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) r[2 + i] = p[i];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < UTAN; ++j) d[i][j] = R(0);
+    d[0][0] = R(1);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) d[2 + i][1 + i] = R(1);
+    for (int i = 0; i < u.n_ops; ++i) {
+        const uint32_t op = u.ops[i];
+        const int dst = (op >> 8) & 0xff, ia = (op >> 16) & 0xff, ib = op >> 24;
+        const int code = op & 0xff;
+        if (code == SDE_UOP_CONST) {
+            r[dst] = (R)u.consts[ia];
+#pragma unroll
+            for (int j = 0; j < UTAN; ++j) d[dst][j] = R(0);
+            continue;
+        }
+        const R va = r[ia], vb = r[ib];
+        R v, da = R(0), db = R(0);   // the result and its partials in a and b
+        switch (code) {
+        case SDE_UOP_ADD: v = Ao::add(va, vb); da = R(1); db = R(1); break;
+        case SDE_UOP_SUB: v = Ao::sub(va, vb); da = R(1); db = R(-1); break;
+        case SDE_UOP_MUL: v = Ao::mul(va, vb); da = vb; db = va; break;
+        case SDE_UOP_DIV: v = va / vb; da = R(1) / vb; db = -v / vb; break;
+        case SDE_UOP_NEG: v = -va; da = R(-1); break;
+        case SDE_UOP_ABS: v = fabs(va); da = va < R(0) ? R(-1) : R(1); break;
+        case SDE_UOP_EXP: v = F::exp_(va); da = v; break;
+        case SDE_UOP_LOG: v = F::log_(va); da = R(1) / va; break;
+        case SDE_UOP_SQRT: v = Ao::sqrt_(va); da = v > R(0) ? R(0.5) / v : R(0); break;
+        case SDE_UOP_MAX: v = np_max(va, vb); if (va >= vb) da = R(1); else db = R(1); break;
+        case SDE_UOP_MIN: v = np_min(va, vb); if (va <= vb) da = R(1); else db = R(1); break;
+        case SDE_UOP_SIN: v = F::sin_(va); da = F::cos_(va); break;
+        case SDE_UOP_COS: v = F::cos_(va); da = -F::sin_(va); break;
+        case SDE_UOP_TAN: v = F::tan_(va); da = R(1) + v * v; break;
+        case SDE_UOP_TANH: v = F::tanh_(va); da = R(1) - v * v; break;
+        case SDE_UOP_POW:
+            v = F::pow_(va, vb);
+            da = vb * F::pow_(va, vb - R(1));
+            db = va > R(0) ? v * F::log_(va) : R(0);
+            break;
+        case SDE_UOP_EXPM1: v = F::expm1_(va); da = v + R(1); break;
+        case SDE_UOP_LOG1P: v = F::log1p_(va); da = R(1) / (R(1) + va); break;
+        case SDE_UOP_ARCTAN: v = F::atan_(va); da = R(1) / (R(1) + va * va); break;
+        default: v = va; da = R(1); break;   // SDE_UOP_COPY
+        }
+        R nd[UTAN];
+#pragma unroll
+        for (int j = 0; j < UTAN; ++j) {
+            // a zero tangent contributes nothing (no 0 * inf)
+            const R ta = d[ia][j], tb = d[ib][j];
+            R s = ta != R(0) ? da * ta : R(0);
+            if (tb != R(0) && db != R(0)) s = s + db * tb;
+            nd[j] = s;
+        }
+        r[dst] = v;
+#pragma unroll
+        for (int j = 0; j < UTAN; ++j) d[dst][j] = nd[j];
+    }
+#pragma unroll
+    for (int i = 0; i < SDE_USER_MAX_TERMS; ++i) {
+        const int reg = i < u.n_terms ? u.term_register[0][i] : 0;
+        A[i] = i < u.n_terms ? r[reg] : R(0);
+#pragma unroll
+        for (int j = 0; j < UTAN; ++j) dA[i][j] = i < u.n_terms ? d[reg][j] : R(0);
+    }
+}
+
+// one forward Euler step of a user SDE (the forward kernel's arithmetic):
+// x + (A_1 dZ_1 + A_2 dZ_2), dZ = dt or dW
+template <typename R, int MAXM>
+__device__ __forceinline__ void user_step(const SdeUserProgram &u, const R (&c0)[MAXM], const R (&c1)[MAXM],
+                                          const R (&c2)[MAXM], const R (&c3)[MAXM], const R (&c4)[MAXM],
+                                          const R (&c5)[MAXM], R t, R dt, const R (&dW)[MAXM], R (&st)[MAXM]) {
+    typedef Ar<R> A;
+#pragma unroll
+    for (int m = 0; m < MAXM; ++m) {
+        const R pv[6] = {c0[m], c1[m], c2[m], c3[m], c4[m], c5[m]};
+        R A2[1][SDE_USER_MAX_TERMS];
+        const R xm[1] = {st[m]};
+        user_coefs<R>(u, xm, t, pv, A2);
+        R s = R(0);
+        for (int i = 0; i < u.n_terms; ++i) {
+            const R term = A::mul(A2[0][i], u.term_source[i] == SDE_SRC_DT ? dt : dW[m]);
+            s = i == 0 ? term : A::add(s, term);
+        }
+        st[m] = A::add(st[m], s);
+    }
+}
 
 template <typename R>
 __device__ __forceinline__ R f_value(const AdjArgs<R> &a, R X) {
@@ -291,7 +405,8 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                 uint32_t u[4 * NCMAX];
                 R z[MAXM], dW[MAXM];
                 noise(k, sq, u, z, dW);
-                fwd_step<R, MODEL, MAXM>(c0, c1, c2, a.dt[k], dW, st);
+                if constexpr (MODEL == SDE_MODEL_USER) user_step<R, MAXM>(a.uprog, c0, c1, c2, c3, c4, c5, a.tk[k], a.dt[k], dW, st);
+                else fwd_step<R, MODEL, MAXM>(c0, c1, c2, a.dt[k], dW, st);
             }
             R xb[MAXM];
             val = terminal_adjoint<R, MAXM>(a, st, xb);
@@ -313,11 +428,32 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                     }
                     bz[k - k0][0] = z[0];
                     bz[k - k0][1] = MAXM > 1 ? z[MAXM > 1 ? 1 : 0] : R(0);
-                    fwd_step<R, MODEL, MAXM>(c0, c1, c2, a.dt[k], dW, st);
+                    if constexpr (MODEL == SDE_MODEL_USER) user_step<R, MAXM>(a.uprog, c0, c1, c2, c3, c4, c5, a.tk[k], a.dt[k], dW, st);
+                    else fwd_step<R, MODEL, MAXM>(c0, c1, c2, a.dt[k], dW, st);
                 }
                 for (int k = k1 - 1; k >= k0; --k) {
                     const R dt = a.dt[k], sq = a.sqdt[k];
-                    if (MODEL == SDE_MODEL_OU) {
+                    if constexpr (MODEL == SDE_MODEL_USER) {
+                        // x' = x + sum_i A_i(t, x, p) dZ_i: dx'/dx = 1 + sum_i dA_i/dx dZ_i,
+                        // dx'/dp_j = sum_i dA_i/dp_j dZ_i
+#pragma unroll
+                        for (int m = 0; m < MAXM; ++m) {
+                            const R pv[6] = {c0[m], c1[m], c2[m], c3[m], c4[m], c5[m]};
+                            R Av[SDE_USER_MAX_TERMS], dA[SDE_USER_MAX_TERMS][UTAN];
+                            user_coefs_tan<R>(a.uprog, bx[k - k0][m], a.tk[k], pv, Av, dA);
+                            R gx = R(0), gp[6] = {R(0), R(0), R(0), R(0), R(0), R(0)};
+                            for (int i = 0; i < a.uprog.n_terms; ++i) {
+                                const R dz = a.uprog.term_source[i] == SDE_SRC_DT ? dt : bw[k - k0][m];
+                                gx += dA[i][0] * dz;
+#pragma unroll
+                                for (int j = 0; j < 6; ++j) gp[j] += dA[i][1 + j] * dz;
+                            }
+                            const R xbn = xb[m];
+#pragma unroll
+                            for (int j = 0; j < 6; ++j) gr[m][1 + j] += xbn * gp[j];
+                            xb[m] = xbn * (R(1) + gx);
+                        }
+                    } else if (MODEL == SDE_MODEL_OU) {
 #pragma unroll
                         for (int m = 0; m < MAXM; ++m) {
                             const R x = bx[k - k0][m];
@@ -412,5 +548,8 @@ int adj_max_blocks_per_sm() {
 
 AdjLauncher<float> find_adj_f32(int model, int maxm, bool jumps, int *bps);
 AdjLauncher<double> find_adj_f64(int model, int maxm, bool jumps, int *bps);
+// user SDEs (adj_user.cu)
+AdjLauncher<float> find_adj_user_f32(int maxm, int *bps);
+AdjLauncher<double> find_adj_user_f64(int maxm, int *bps);
 
 }  // namespace sdegpu

@@ -1104,10 +1104,16 @@ __global__ void __launch_bounds__(BLOCK) reduce_partials_kernel(const double *pa
 
 template <typename R> struct AdjFinder;
 template <> struct AdjFinder<float> {
-    static AdjLauncher<float> find(int model, int maxm, bool jumps, int *bps) { return find_adj_f32(model, maxm, jumps, bps); }
+    static AdjLauncher<float> find(int model, int maxm, bool jumps, int *bps) {
+        if (model == SDE_MODEL_USER) return jumps ? nullptr : find_adj_user_f32(maxm, bps);
+        return find_adj_f32(model, maxm, jumps, bps);
+    }
 };
 template <> struct AdjFinder<double> {
-    static AdjLauncher<double> find(int model, int maxm, bool jumps, int *bps) { return find_adj_f64(model, maxm, jumps, bps); }
+    static AdjLauncher<double> find(int model, int maxm, bool jumps, int *bps) {
+        if (model == SDE_MODEL_USER) return jumps ? nullptr : find_adj_user_f64(maxm, bps);
+        return find_adj_f64(model, maxm, jumps, bps);
+    }
 };
 
 template <typename R>
@@ -1121,6 +1127,15 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
         if (!(gr->tt[k + 1] > gr->tt[k])) return fail(SDE_ERR_UNSUPPORTED, "the adjoint integrates forward grids only");
     if (req->n_strikes < 0 || req->n_strikes > SDE_MAX_STRIKES) return fail(SDE_ERR_INVALID, "bad n_strikes");
     const int M = s->group_size, W = s->groups * M;
+    const bool user = s->model == SDE_MODEL_USER;
+    if (user) {
+        // single equations driven by dt / dw
+        const SdeUserProgram *u = s->program;
+        if (u->n_eq != 1) return fail(SDE_ERR_UNSUPPORTED, "the adjoint of user SDEs takes single equations");
+        for (int i = 0; i < u->n_terms; ++i)
+            if (u->term_source[i] != SDE_SRC_DT && u->term_source[i] != SDE_SRC_DW)
+                return fail(SDE_ERR_UNSUPPORTED, "the adjoint of user SDEs takes dt and dw terms only");
+    }
     const bool jumps = s->jump_law != SDE_JUMP_NONE;
     int maxm = maxm_of(M);
     if (maxm > 8) return fail(SDE_ERR_UNSUPPORTED, "the adjoint supports groups of up to 8 state variables");
@@ -1144,10 +1159,13 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     const size_t o_prm = o_x0 + al(sizeof(R) * W), o_lam = o_prm + al(sizeof(R) * SDE_MAX_PARAMS * W);
     const size_t o_p0 = o_lam + al(sizeof(double) * njt), o_thr = o_p0 + al(sizeof(double) * njt);
     const size_t o_thr1 = o_thr + al(sizeof(long long) * njt);
-    const size_t o_end = o_thr1 + al(sizeof(long long) * njt);
+    const size_t o_tk = o_thr1 + al(sizeof(long long) * njt);   // step starts, for user SDEs
+    const size_t o_end = o_tk + al(sizeof(R) * (user ? n_steps : 1));
     D->host_tables.resize(o_end);
     char *H = D->host_tables.data();
     R *h_dt = (R *)(H + o_dt), *h_sq = (R *)(H + o_sq), *h_x0 = (R *)(H + o_x0), *h_prm = (R *)(H + o_prm);
+    if (user)
+        for (int k = 0; k < n_steps; ++k) ((R *)(H + o_tk))[k] = (R)gr->tt[k];
     double *h_lam = (double *)(H + o_lam), *h_p0 = (double *)(H + o_p0);
     long long *h_thr = (long long *)(H + o_thr), *h_thr1 = (long long *)(H + o_thr1);
     for (int k = 0; k < n_steps; ++k) {
@@ -1206,6 +1224,10 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     a.p0 = (const double *)(T + o_p0);
     a.thr = (const long long *)(T + o_thr);
     a.thr1 = (const long long *)(T + o_thr1);
+    if (user) {
+        a.uprog = *s->program;
+        a.tk = (const R *)(T + o_tk);
+    }
     a.n_strikes = req->n_strikes;
     for (int i = 0; i < req->n_strikes; ++i) {
         a.strikes[i] = (R)req->strikes[i];

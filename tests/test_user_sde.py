@@ -219,15 +219,70 @@ def test_device_rng_matches_c_oracle(lib, clib, case):
                                    atol=1e-15)
 
 
-@pytest.mark.gpu
-def test_user_sde_refusals(lib):
+def test_user_sde_refusals():
     cls = user_class(sg, 'integrate:user_ou')
     with pytest.raises(NotImplementedError):
         cls(paths=4, dw=sg.odd_wiener_source)(np.linspace(0, 1, 3))
     from sdepy_gb300.autograd import expectation
     import torch
-    with pytest.raises(NotImplementedError):
-        expectation(cls, (0., 1.), [], paths=100, steps=10, x0=torch.tensor(1., requires_grad=True))
+    x0 = torch.tensor(1., requires_grad=True)
+    for spec in ('integrate_q2:user_sv', 'integrate_log:user_jd_log'):   # systems, jump terms
+        with pytest.raises(NotImplementedError):
+            expectation(user_class(sg, spec), (0., 1.), [], paths=100, steps=10, x0=x0)
+    with pytest.raises(NotImplementedError):   # a time-dependent parameter
+        expectation(cls, (0., 1.), [], paths=100, steps=10, x0=x0, theta=lambda t: t)
+
+
+def _grads(cls, strikes, dtype=np.float64, **kw):
+    """(value, {name: gradient}) of expectation() for torch-scalar kw."""
+    import torch
+    from sdepy_gb300.autograd import expectation
+    ts = {k: torch.tensor(float(v), dtype=torch.float64, requires_grad=True) for k, v in kw.items()}
+    y = expectation(cls, (0., 1.), strikes, paths=200003, steps=64, dtype=dtype, seed=21, stream=3, **ts)
+    y.sum().backward()
+    return y.detach().numpy(), {k: float(t.grad) for k, t in ts.items()}
+
+
+@pytest.mark.gpu
+def test_gpu_user_adjoint_equals_presets(lib):
+    """The tangent-mode adjoint of a user SDE gives the preset adjoints'
+    gradients (FP64): an OU written by the user against
+    ornstein_uhlenbeck_process, a log-space GBM (dw term first) against
+    lognorm_process, with a mean and two call payoffs."""
+    K = [.2, .5]
+    vu, gu = _grads(user_class(sg, 'integrate:user_ou'), K, x0=.1, theta=.6, k=2., sigma=.3)
+    vp, gp = _grads(sg.ornstein_uhlenbeck_process, K, x0=.1, theta=.6, k=2., sigma=.3)
+    np.testing.assert_allclose(vu, vp, rtol=1e-12)
+    for n in gp:
+        assert abs(gu[n] - gp[n]) <= 1e-9*max(1., abs(gp[n])), (n, gu[n], gp[n])
+    K = [1., 1.2]
+    vu, gu = _grads(user_class(sg, 'integrate_log:user_gbm'), K, x0=1.1, mu=.05, sigma=.25)
+    vp, gp = _grads(sg.lognorm_process, K, x0=1.1, mu=.05, sigma=.25)
+    np.testing.assert_allclose(vu, vp, rtol=1e-12)
+    for n in gp:
+        assert abs(gu[n] - gp[n]) <= 1e-9*max(1., abs(gp[n])), (n, gu[n], gp[n])
+
+
+@pytest.mark.gpu
+def test_gpu_user_adjoint_matches_finite_differences(lib):
+    """A CEV SDE (maximum, ** with a parameter exponent; paths stay away
+    from the kink at 0) and a mixed one
+    (sin(t), exp(-t), sqrt, tanh): the adjoint gradient of the mean equals
+    the central difference of the forward mean on common random numbers
+    (h = 1e-4 relative, FP64); FP32 adjoints agree to FP32 accuracy."""
+    for spec, kw in (('integrate:user_cev', dict(x0=1., mu=.05, sigma=.2, gamma=.7)),
+                     ('integrate:user_mixed', dict(x0=.5, a=1.5, b=.7, s=.25))):
+        cls = user_class(sg, spec)
+        v, g = _grads(cls, [], **kw)
+        for n, base in kw.items():
+            h = 1e-4*max(abs(base), 1e-2)
+            up = _grads(cls, [], **dict(kw, **{n: base + h}))[0][0]
+            dn = _grads(cls, [], **dict(kw, **{n: base - h}))[0][0]
+            fd = (up - dn)/(2*h)
+            assert abs(g[n] - fd) <= 1e-6*max(1., abs(fd)), (spec, n, g[n], fd)
+        v32, g32 = _grads(cls, [], dtype=np.float32, **kw)
+        for n in g:
+            assert abs(g32[n] - g[n]) <= 2e-3*max(1., abs(g[n])), (spec, n, g32[n], g[n])
 
 
 # ---------------------------------------------------------------------------
