@@ -474,7 +474,8 @@ def extra_configs(lib):
         o.xx, o.n_rows, o.on_device = None, len(timeline), 0
         ptab = P._params_table(leg) if P._tdep else None          # time-dependent parameters
         ctab = P._corr_table(leg) if P._corr_tdep else None       # and correlations
-        g.params_t, g.corr_t = _lib.dptr(ptab), _lib.dptr(ctab)
+        ltab = P._lam_table(leg)                                  # a user SDE's intensity
+        g.params_t, g.corr_t, g.lam_t = _lib.dptr(ptab), _lib.dptr(ctab), _lib.dptr(ltab)
         req, so, arrs = P._stats_request(dict(row=len(timeline) - 1, bins=0, range=None, strikes=strikes))
         spec = P._make_spec(seed, 0)
         _lib.check(lib.sde_run_stats(C.byref(spec), C.byref(g), None, C.byref(o), C.byref(req), C.byref(so)), 'fwd')
@@ -595,6 +596,43 @@ def extra_configs(lib):
         nxt['user_ou_' + name] = rate(user_ou(paths=K, steps=500, dtype=dtype, x0=1.))
         nxt['preset_ou_' + name] = rate(sg.ornstein_uhlenbeck_process(paths=K, steps=500, dtype=dtype, x0=1.,
                                                                       theta=.5, k=2., sigma=.3))
+    # a user-written Merton SDE (log space, dj term) against the preset,
+    # 364 steps on (0, 1) as the jump-diffusion workload above
+    jd = sg.integrate(lambda t, x, mu=.03, sigma=.15: {'dt': mu - sigma*sigma/2, 'dw': sigma, 'dj': 1},
+                      log=True)
+    for name, P in (('user_merton_fp32', jd(paths=K, steps=365, dtype=np.float32, x0=1., lam=1.,
+                                             y=sg.norm_rv(-.1, .15))),
+                    ('preset_merton_fp32', sg.merton_jumpdiff_process(paths=K, steps=365, dtype=np.float32, x0=1.,
+                                                                      mu=.03, sigma=.15, lam=1., a=-.1, b=.15))):
+        ms = _time_call(lambda: fused(P, (0., 1.), [], 8), lib)
+        nxt[name] = {'kernel_ms': ms, 'path_steps_per_s': K*364/(ms*1e-3), 'steps': 364}
+
+    # adjoint against forward cost for user SDEs (tangent-mode program) and
+    # the OU preset, mean and one call payoff, 499 steps on (0, 2)
+    def adj_ms(P, strike):
+        leg = Grid((0., 2.), P.steps).legs[-1]
+        g = _lib.SdeGrid()
+        g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
+        g.n_pts, g.step_offset = leg.tt.size, 0
+        req = _lib.SdeAdjReq()
+        req.n_strikes, req.checkpoint, req.mean_weight = 1, 0, 1.
+        req.strikes[0], req.weights[0] = strike, 1.
+        grad = np.zeros((P._W, 8))
+        v = C.c_double()
+
+        def call():
+            spec = P._make_spec(8, 0)
+            _lib.check(lib.sde_adjoint(C.byref(spec), C.byref(g), C.byref(req), _lib.dptr(grad), C.byref(v)),
+                       'adj')
+        return _time_call(call, lib)
+    cev = sg.integrate(lambda t, x, mu=.05, sigma=.2, gamma=.7: {'dt': mu*x, 'dw': sigma*np.maximum(x, 0.)**gamma})
+    for name, P, strike in (('user_ou', user_ou(paths=K, steps=500, dtype=np.float32, x0=1.), .5),
+                            ('preset_ou', sg.ornstein_uhlenbeck_process(paths=K, steps=500, dtype=np.float32,
+                                                                        x0=1., theta=.5, k=2., sigma=.3), .5),
+                            ('user_cev', cev(paths=K, steps=500, dtype=np.float32, x0=1.), 1.)):
+        f_ms = _time_call(lambda: fused(P, (0., 2.), [strike], 8), lib)
+        a_ms = adj_ms(P, strike)
+        nxt[name + '_adjoint_fp32'] = {'forward_ms': f_ms, 'adjoint_ms': a_ms, 'grad_over_forward': a_ms/f_ms}
     Cm = np.array([[1., .5], [.5, 1.]])
     nxt['ou2_corr_const_fp32'] = rate(sg.ornstein_uhlenbeck_process(vshape=2, paths=K, steps=500,
                                                                      dtype=np.float32, corr=Cm))
