@@ -591,17 +591,27 @@ def extra_configs(lib):
         return {'kernel_ms': ms, 'path_steps_per_s': K*499/(ms*1e-3)}
     nxt['cir_fp32'] = rate(sg.cox_ingersoll_ross_process(paths=K, steps=500, dtype=np.float32, x0=.04,
                                                           theta=.04, k=1.5, xi=.5))
-    user_ou = sg.integrate(lambda t, x, theta=.5, k=2., sigma=.3: {'dt': k*(theta - x), 'dw': sigma})
+    ou_f = lambda t, x, theta=.5, k=2., sigma=.3: {'dt': k*(theta - x), 'dw': sigma}   # noqa: E731
+    user_ou = sg.integrate(ou_f, jit=False)
+    user_ou_jit = sg.integrate(ou_f, jit=True)     # the program compiled at run time (NVRTC)
     for name, dtype in (('fp32', np.float32), ('fp64', None)):
         nxt['user_ou_' + name] = rate(user_ou(paths=K, steps=500, dtype=dtype, x0=1.))
+        Pj = user_ou_jit(paths=K, steps=500, dtype=dtype, x0=1.)
+        t0 = time.perf_counter()
+        fused(Pj, (0., 2.), [], 8)                 # first call: compiles
+        compile_s = time.perf_counter() - t0
+        nxt['user_ou_jit_' + name] = dict(rate(Pj), first_call_s=compile_s)
         nxt['preset_ou_' + name] = rate(sg.ornstein_uhlenbeck_process(paths=K, steps=500, dtype=dtype, x0=1.,
                                                                       theta=.5, k=2., sigma=.3))
     # a user-written Merton SDE (log space, dj term) against the preset,
     # 364 steps on (0, 1) as the jump-diffusion workload above
-    jd = sg.integrate(lambda t, x, mu=.03, sigma=.15: {'dt': mu - sigma*sigma/2, 'dw': sigma, 'dj': 1},
-                      log=True)
+    jd_f = lambda t, x, mu=.03, sigma=.15: {'dt': mu - sigma*sigma/2, 'dw': sigma, 'dj': 1}   # noqa: E731
+    jd = sg.integrate(jd_f, log=True, jit=False)
+    jdj = sg.integrate(jd_f, log=True, jit=True)
     for name, P in (('user_merton_fp32', jd(paths=K, steps=365, dtype=np.float32, x0=1., lam=1.,
                                              y=sg.norm_rv(-.1, .15))),
+                    ('user_merton_jit_fp32', jdj(paths=K, steps=365, dtype=np.float32, x0=1., lam=1.,
+                                                 y=sg.norm_rv(-.1, .15))),
                     ('preset_merton_fp32', sg.merton_jumpdiff_process(paths=K, steps=365, dtype=np.float32, x0=1.,
                                                                       mu=.03, sigma=.15, lam=1., a=-.1, b=.15))):
         ms = _time_call(lambda: fused(P, (0., 1.), [], 8), lib)
@@ -625,7 +635,8 @@ def extra_configs(lib):
             _lib.check(lib.sde_adjoint(C.byref(spec), C.byref(g), C.byref(req), _lib.dptr(grad), C.byref(v)),
                        'adj')
         return _time_call(call, lib)
-    cev = sg.integrate(lambda t, x, mu=.05, sigma=.2, gamma=.7: {'dt': mu*x, 'dw': sigma*np.maximum(x, 0.)**gamma})
+    cev = sg.integrate(lambda t, x, mu=.05, sigma=.2, gamma=.7: {'dt': mu*x, 'dw': sigma*np.maximum(x, 0.)**gamma},
+                       jit=False)
     for name, P, strike in (('user_ou', user_ou(paths=K, steps=500, dtype=np.float32, x0=1.), .5),
                             ('preset_ou', sg.ornstein_uhlenbeck_process(paths=K, steps=500, dtype=np.float32,
                                                                         x0=1., theta=.5, k=2., sigma=.3), .5),

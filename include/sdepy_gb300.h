@@ -25,7 +25,9 @@
 #ifndef SDEPY_GB300_H
 #define SDEPY_GB300_H
 
+#ifndef __CUDACC_RTC__   /* runtime compilation (NVRTC) defines the integer types itself */
 #include <stdint.h>
+#endif
 
 #ifdef __cplusplus
 extern "C" {
@@ -115,6 +117,10 @@ typedef struct SdeUserProgram {
     uint32_t ops[SDE_USER_MAX_OPS];
     double consts[SDE_USER_MAX_CONSTS];
     const double *jump_params;        /* [4][groups*M] lam, a, b, pa; NULL without dn / dj */
+    int32_t jit;                      /* 1: compile the program to native code for the
+                                       * forward kernel (NVRTC, cached per process;
+                                       * sde_jit_available()), 0: interpret it */
+    int32_t reserved;
 } SdeUserProgram;
 
 /* jump-size law of the compound Poisson source (LINEAR model, and user
@@ -239,6 +245,16 @@ SDE_API int32_t sde_last_error(char *buf, int32_t len);
 
 /* number of visible CUDA devices (0 if none); never fails */
 SDE_API int32_t sde_device_count(void);
+
+/* 1 if user SDE programs can be compiled at run time (NVRTC found), else 0. */
+SDE_API int32_t sde_jit_available(void);
+
+/* Compile, without loading, the forward kernel of a user program for a
+ * precision (SDE_FP64 / SDE_FP32), group size, noise mode (injected 0/1)
+ * and jump terms (0/1): a check of the code generation that needs no
+ * device.  Returns SDE_OK or an error with NVRTC's log in log[len]. */
+SDE_API int32_t sde_jit_compile(const SdeUserProgram *program, int32_t precision, int32_t group_size,
+                                int32_t injected, int32_t jumps, char *log, int32_t len);
 
 /* free the device scratch cached by the library on the current device */
 SDE_API int32_t sde_release(void);

@@ -70,7 +70,7 @@ def build(force=False, verbose=False):
     with cf.ThreadPoolExecutor(workers) as ex:
         objs = list(ex.map(run, jobs))
     tmp = LIB + '.tmp'
-    cmd = [cc] + ARCH + ['-shared', '-o', tmp] + objs + ['-lcudart']
+    cmd = [cc] + ARCH + ['-shared', '-o', tmp] + objs + ['-lcudart', '-ldl']
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError('link failed:\n{}\n{}'.format(r.stdout, r.stderr))

@@ -41,7 +41,8 @@ _lp = C.POINTER(C.c_int64)
 class SdeUserProgram(C.Structure):
     _fields_ = [('n_ops', C.c_int32), ('n_eq', C.c_int32), ('n_terms', C.c_int32),
                 ('term_source', C.c_int32*4), ('term_register', (C.c_int32*4)*8),
-                ('ops', C.c_uint32*64), ('consts', C.c_double*16), ('jump_params', C.POINTER(C.c_double))]
+                ('ops', C.c_uint32*64), ('consts', C.c_double*16), ('jump_params', C.POINTER(C.c_double)),
+                ('jit', C.c_int32), ('reserved', C.c_int32)]
 
 
 class SdeSpec(C.Structure):
@@ -110,6 +111,9 @@ SIGNATURES = {
     'sde_abi_version': (C.c_int32, []),
     'sde_last_error': (C.c_int32, [C.c_char_p, C.c_int32]),
     'sde_device_count': (C.c_int32, []),
+    'sde_jit_available': (C.c_int32, []),
+    'sde_jit_compile': (C.c_int32, [C.POINTER(SdeUserProgram), C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                    C.c_char_p, C.c_int32]),
     'sde_release': (C.c_int32, []),
     'sde_set_stream': (C.c_int32, [C.c_void_p]),
     'sde_normal_pairs': (C.c_int32, [C.POINTER(C.c_uint32), C.c_int64, C.c_int32, _dp]),

@@ -22,7 +22,9 @@
 // sine / cosine (ln_u01_f64, sincospi_f64 below); FP32 evaluates it with the
 // SFU approximations, so both precisions consume identical draws.
 #pragma once
+#ifndef __CUDACC_RTC__
 #include <cstdint>
+#endif
 
 #include "fp64_tables.h"
 

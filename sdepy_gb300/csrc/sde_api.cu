@@ -12,6 +12,7 @@
 #include "sde_stats.cuh"
 #include "sde_adjoint.cuh"
 #include "sde_runtime.h"
+#include "sde_jit.h"
 
 using namespace sdegpu;
 
@@ -831,11 +832,20 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
                                   corr_steps));
     // (user-SDE kernels reload per-step parameters and factors in every form)
     const int kmodel = user && s->program->n_eq > 1 ? SDE_MODEL_USER_SYS : s->model;
-    FwdLauncher<R> L = user     ? Finder<R>::find(kmodel, maxm_of(M), inject, jumps, &bps)
-                       : anti   ? Finder<R>::find_anti(s->model, maxm_of(M), jumps, tdep_k, &bps)
-                       : tdep_k ? Finder<R>::find_tdep(s->model, maxm_of(M), &bps)
-                                : Finder<R>::find(s->model, maxm_of(M), inject, jumps, &bps);
-    if (!L) return fail(SDE_ERR_UNSUPPORTED, "no kernel for model %d group size %d", s->model, M);
+    // a user program compiled at run time, or an instantiated kernel
+    cudaKernel_t jk = nullptr;
+    FwdLauncher<R> L = nullptr;
+    if (user && s->program->jit) {
+        std::string err;
+        if ((rc = jit_fwd_kernel(*s->program, sizeof(R) == 8, maxm_of(M), inject, jumps, &jk, &bps, &err)))
+            return fail(rc, "%s", err.c_str());
+    } else {
+        L = user     ? Finder<R>::find(kmodel, maxm_of(M), inject, jumps, &bps)
+            : anti   ? Finder<R>::find_anti(s->model, maxm_of(M), jumps, tdep_k, &bps)
+            : tdep_k ? Finder<R>::find_tdep(s->model, maxm_of(M), &bps)
+                     : Finder<R>::find(s->model, maxm_of(M), inject, jumps, &bps);
+        if (!L) return fail(SDE_ERR_UNSUPPORTED, "no kernel for model %d group size %d", s->model, M);
+    }
     // antithetic kernels integrate two paths per thread
     const int nbx = path_blocks(D, anti ? paths / 2 : paths, s->groups, bps);
     a.stats_row = -1;
@@ -855,7 +865,12 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
         }
     }
     if (D->timing) CU(cudaEventRecord(D->ev[0], st));
-    L(a, dim3(nbx, s->groups), st);
+    if (jk) {
+        void *args[] = {(void *)&a};
+        CU(cudaLaunchKernel((const void *)jk, dim3(nbx, s->groups), dim3(BLOCK), args, 0, st));
+    } else {
+        L(a, dim3(nbx, s->groups), st);
+    }
     CU(cudaGetLastError());
     if (D->timing) CU(cudaEventRecord(D->ev[1], st));
 

@@ -1,0 +1,266 @@
+// Runtime compilation of user SDE programs (sdepy's integrate decorator,
+// sdepy/integration.py:1843-1955).
+//
+// The straight-line program of an SdeUserProgram is written out as CUDA C++
+// (UserJitFn<R>::coefs: one statement per instruction, the interpreter's own
+// arithmetic -- Ar<R> / UFn<R> / np_max -- so FP64 results are bit-identical
+// to user_coefs), compiled with NVRTC for sm_103a together with the forward
+// kernel header, and the resulting cubin is loaded through the runtime's
+// library API.  The forward kernel instantiated with SDE_MODEL_USER_JIT /
+// SDE_MODEL_USER_SYS_JIT then evaluates the coefficients inline, with no
+// register file in local memory and no dispatch.  Kernels are cached per
+// (source, precision, group width, noise mode) for the life of the process.
+//
+// NVRTC is loaded with dlopen: a library without it still runs the
+// interpreted kernels (SdeUserProgram.jit = 0).
+#include <dlfcn.h>
+#include <nvrtc.h>
+
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "sde_jit.h"
+#include "sde_kernels.cuh"
+
+namespace sdegpu {
+
+namespace {
+
+struct Nvrtc {
+    decltype(&nvrtcCreateProgram) create = nullptr;
+    decltype(&nvrtcAddNameExpression) add_name = nullptr;
+    decltype(&nvrtcCompileProgram) compile = nullptr;
+    decltype(&nvrtcGetProgramLogSize) log_size = nullptr;
+    decltype(&nvrtcGetProgramLog) log = nullptr;
+    decltype(&nvrtcGetLoweredName) lowered = nullptr;
+    decltype(&nvrtcGetCUBINSize) cubin_size = nullptr;
+    decltype(&nvrtcGetCUBIN) cubin = nullptr;
+    decltype(&nvrtcDestroyProgram) destroy = nullptr;
+    bool ok = false;
+    std::string include_dir;   // csrc/, beside the library's _native/
+};
+
+Nvrtc &nvrtc() {
+    static Nvrtc N;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        const char *names[] = {"libnvrtc.so.13", "libnvrtc.so", "/usr/local/cuda/lib64/libnvrtc.so.13",
+                               "/usr/local/cuda/lib64/libnvrtc.so"};
+        void *h = nullptr;
+        for (const char *n : names)
+            if ((h = dlopen(n, RTLD_NOW | RTLD_LOCAL))) break;
+        if (!h) return;
+#define SDE_NVRTC(field, sym) N.field = (decltype(N.field))dlsym(h, #sym)
+        SDE_NVRTC(create, nvrtcCreateProgram);
+        SDE_NVRTC(add_name, nvrtcAddNameExpression);
+        SDE_NVRTC(compile, nvrtcCompileProgram);
+        SDE_NVRTC(log_size, nvrtcGetProgramLogSize);
+        SDE_NVRTC(log, nvrtcGetProgramLog);
+        SDE_NVRTC(lowered, nvrtcGetLoweredName);
+        SDE_NVRTC(cubin_size, nvrtcGetCUBINSize);
+        SDE_NVRTC(cubin, nvrtcGetCUBIN);
+        SDE_NVRTC(destroy, nvrtcDestroyProgram);
+#undef SDE_NVRTC
+        Dl_info info;
+        if (!dladdr((void *)&sde_jit_available, &info) || !info.dli_fname) return;
+        std::string so = info.dli_fname;   // .../sdepy_gb300/_native/libsdepy_gb300.so
+        size_t a = so.rfind('/');
+        if (a == std::string::npos) return;
+        size_t b = so.rfind('/', a - 1);
+        if (b == std::string::npos) return;
+        N.include_dir = so.substr(0, b) + "/csrc";
+        N.ok = N.create && N.add_name && N.compile && N.log_size && N.log && N.lowered && N.cubin_size &&
+               N.cubin && N.destroy;
+    });
+    return N;
+}
+
+// one instruction of the program as a statement on r[]
+std::string op_statement(const SdeUserProgram &u, uint32_t op) {
+    const int code = op & 0xff, d = (op >> 8) & 0xff, ia = (op >> 16) & 0xff, ib = op >> 24;
+    char buf[160];
+    const char *un = nullptr, *bin = nullptr;
+    switch (code) {
+    case SDE_UOP_CONST: {
+        uint64_t bits;
+        memcpy(&bits, &u.consts[ia], sizeof bits);
+        snprintf(buf, sizeof buf, "r[%d] = (R)__longlong_as_double((long long)0x%016llxULL);", d,
+                 (unsigned long long)bits);
+        return buf;
+    }
+    case SDE_UOP_ADD: bin = "A::add"; break;
+    case SDE_UOP_SUB: bin = "A::sub"; break;
+    case SDE_UOP_MUL: bin = "A::mul"; break;
+    case SDE_UOP_MAX: bin = "np_max"; break;
+    case SDE_UOP_MIN: bin = "np_min"; break;
+    case SDE_UOP_POW: bin = "F::pow_"; break;
+    case SDE_UOP_DIV:
+        snprintf(buf, sizeof buf, "r[%d] = r[%d] / r[%d];", d, ia, ib);
+        return buf;
+    case SDE_UOP_NEG: snprintf(buf, sizeof buf, "r[%d] = -r[%d];", d, ia); return buf;
+    case SDE_UOP_ABS: un = "fabs"; break;
+    case SDE_UOP_EXP: un = "F::exp_"; break;
+    case SDE_UOP_LOG: un = "F::log_"; break;
+    case SDE_UOP_SQRT: un = "A::sqrt_"; break;
+    case SDE_UOP_SIN: un = "F::sin_"; break;
+    case SDE_UOP_COS: un = "F::cos_"; break;
+    case SDE_UOP_TAN: un = "F::tan_"; break;
+    case SDE_UOP_TANH: un = "F::tanh_"; break;
+    case SDE_UOP_EXPM1: un = "F::expm1_"; break;
+    case SDE_UOP_LOG1P: un = "F::log1p_"; break;
+    case SDE_UOP_ARCTAN: un = "F::atan_"; break;
+    default: snprintf(buf, sizeof buf, "r[%d] = r[%d];", d, ia); return buf;   // SDE_UOP_COPY
+    }
+    if (bin) snprintf(buf, sizeof buf, "r[%d] = %s(r[%d], r[%d]);", d, bin, ia, ib);
+    else snprintf(buf, sizeof buf, "r[%d] = %s(r[%d]);", d, un, ia);
+    return buf;
+}
+
+std::string kernel_name(const char *rt, int model, int maxm, bool inject, bool jumps) {
+    char buf[160];
+    snprintf(buf, sizeof buf, "sdegpu::sde_fwd_kernel<%s, %d, %d, %s, %s, false, false>", rt, model, maxm,
+             inject ? "true" : "false", jumps ? "true" : "false");
+    return buf;
+}
+
+std::string jit_source(const SdeUserProgram &u, const char *rt, int model, int maxm, bool inject, bool jumps) {
+    std::string s = "#include \"sde_kernels.cuh\"\nnamespace sdegpu {\ntemplate <> struct UserJitFn<";
+    s += rt;
+    s += "> {\n  typedef ";
+    s += rt;
+    s += " R;\n  static __device__ __forceinline__ void coefs(const R *xs, R t, const R (&p)[6],"
+         " R (*out)[SDE_USER_MAX_TERMS]) {\n"
+         "    typedef Ar<R> A;\n    typedef UFn<R> F;\n    R r[SDE_USER_MAX_REGS];\n"
+         "    r[0] = xs[0];\n    r[1] = t;\n";
+    for (int i = 0; i < 6; ++i) s += "    r[" + std::to_string(2 + i) + "] = p[" + std::to_string(i) + "];\n";
+    for (int e = 1; e < u.n_eq; ++e) s += "    r[" + std::to_string(7 + e) + "] = xs[" + std::to_string(e) + "];\n";
+    for (int i = 0; i < u.n_ops; ++i) s += "    " + op_statement(u, u.ops[i]) + "\n";
+    for (int e = 0; e < u.n_eq; ++e)
+        for (int j = 0; j < SDE_USER_MAX_TERMS; ++j)
+            s += "    out[" + std::to_string(e) + "][" + std::to_string(j) + "] = " +
+                 (j < u.n_terms ? "r[" + std::to_string(u.term_register[e][j]) + "]" : std::string("R(0)")) + ";\n";
+    s += "  }\n};\ntemplate __global__ void " + kernel_name(rt, model, maxm, inject, jumps) +
+         "(const __grid_constant__ FwdArgs<" + rt + ">);\n}  // namespace sdegpu\n";
+    return s;
+}
+
+struct Entry {
+    cudaLibrary_t lib;
+    cudaKernel_t kernel;
+    int bps;
+};
+
+std::mutex g_cache_mu;
+std::map<std::string, Entry> g_cache;
+
+// compile src to a cubin; the kernel's lowered name in *low
+int compile_cubin(const std::string &src, const std::string &name, std::vector<char> *cubin, std::string *low,
+                  std::string *err) {
+    Nvrtc &N = nvrtc();
+    if (!N.ok) {
+        *err = "NVRTC is not available for compiling user SDE programs";
+        return SDE_ERR_UNSUPPORTED;
+    }
+    nvrtcProgram prog;
+    if (N.create(&prog, src.c_str(), "sde_user_jit.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS) {
+        *err = "nvrtcCreateProgram failed";
+        return SDE_ERR_CUDA;
+    }
+    N.add_name(prog, name.c_str());
+    const std::string inc = "-I" + N.include_dir;
+    // the library build's target and language (sm_103a, C++17; no fast math)
+    const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-default-device", inc.c_str()};
+    const nvrtcResult rc = N.compile(prog, 4, opts);
+    if (rc != NVRTC_SUCCESS) {
+        size_t n = 0;
+        N.log_size(prog, &n);
+        std::vector<char> log(n + 1, 0);
+        N.log(prog, log.data());
+        *err = "compiling the user SDE program: " + std::string(log.data()).substr(0, 600);
+        N.destroy(&prog);
+        return SDE_ERR_UNSUPPORTED;
+    }
+    const char *lowered = nullptr;
+    size_t nb = 0;
+    N.lowered(prog, name.c_str(), &lowered);
+    N.cubin_size(prog, &nb);
+    cubin->assign(nb, 0);
+    N.cubin(prog, cubin->data());
+    *low = lowered ? lowered : "";
+    N.destroy(&prog);
+    return SDE_OK;
+}
+
+}  // namespace
+
+bool jit_available() { return nvrtc().ok; }
+
+int jit_compile_check(const SdeUserProgram &u, bool fp64, int maxm, bool inject, bool jumps, std::string *err) {
+    const char *rt = fp64 ? "double" : "float";
+    const int model = u.n_eq > 1 ? SDE_MODEL_USER_SYS_JIT : SDE_MODEL_USER_JIT;
+    std::vector<char> cubin;
+    std::string low;
+    return compile_cubin(jit_source(u, rt, model, maxm, inject, jumps), kernel_name(rt, model, maxm, inject, jumps),
+                         &cubin, &low, err);
+}
+
+int jit_fwd_kernel(const SdeUserProgram &u, bool fp64, int maxm, bool inject, bool jumps, cudaKernel_t *kernel,
+                   int *bps, std::string *err) {
+    const char *rt = fp64 ? "double" : "float";
+    const int model = u.n_eq > 1 ? SDE_MODEL_USER_SYS_JIT : SDE_MODEL_USER_JIT;
+    const std::string src = jit_source(u, rt, model, maxm, inject, jumps);
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    auto it = g_cache.find(src);
+    if (it != g_cache.end()) {
+        *kernel = it->second.kernel;
+        *bps = it->second.bps;
+        return SDE_OK;
+    }
+    std::vector<char> cubin;
+    std::string low;
+    int rc;
+    if ((rc = compile_cubin(src, kernel_name(rt, model, maxm, inject, jumps), &cubin, &low, err))) return rc;
+    Entry e;
+    if (cudaLibraryLoadData(&e.lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0) != cudaSuccess ||
+        cudaLibraryGetKernel(&e.kernel, e.lib, low.c_str()) != cudaSuccess) {
+        *err = std::string("loading the compiled user SDE program: ") + cudaGetErrorString(cudaGetLastError());
+        return SDE_ERR_CUDA;
+    }
+    e.bps = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e.bps, (const void *)e.kernel, BLOCK, 0) != cudaSuccess ||
+        e.bps < 1) {
+        cudaGetLastError();
+        e.bps = 1;
+    }
+    g_cache.emplace(src, e);
+    *kernel = e.kernel;
+    *bps = e.bps;
+    return SDE_OK;
+}
+
+}  // namespace sdegpu
+
+extern "C" int32_t sde_jit_available(void) { return sdegpu::jit_available() ? 1 : 0; }
+
+extern "C" int32_t sde_jit_compile(const SdeUserProgram *program, int32_t precision, int32_t group_size,
+                                   int32_t injected, int32_t jumps, char *log, int32_t len) {
+    std::string err;
+    int rc = SDE_ERR_INVALID;
+    if (!program || group_size < 1 || group_size > SDE_MAX_GROUP || program->n_eq < 1 ||
+        program->n_eq > SDE_USER_MAX_EQ || program->n_ops < 0 || program->n_ops > SDE_USER_MAX_OPS ||
+        program->n_terms < 0 || program->n_terms > SDE_USER_MAX_TERMS) {
+        err = "invalid program or group size";
+    } else {
+        const int maxm = group_size <= 1 ? 1 : group_size <= 2 ? 2 : group_size <= 4 ? 4 : group_size <= 8 ? 8 : 16;
+        rc = sdegpu::jit_compile_check(*program, precision == SDE_FP64, maxm, injected != 0, jumps != 0, &err);
+    }
+    if (log && len > 0) {
+        strncpy(log, err.c_str(), (size_t)len - 1);
+        log[len - 1] = 0;
+    }
+    return rc;
+}

@@ -13,8 +13,18 @@
 // with the coefficients of SDE.sde for each preset, using _rn intrinsics so
 // that no multiply-add is contracted.  FP32 lets the compiler fuse.
 #pragma once
+#ifdef __CUDACC_RTC__
+// runtime compilation of user SDE programs (sde_jit.cu): no host headers
+typedef signed char int8_t;
+typedef int int32_t;
+typedef unsigned int uint32_t;
+typedef long long int64_t;
+typedef unsigned long long uint64_t;
+#define INFINITY __int_as_float(0x7f800000)
+#else
 #include <cstdint>
 #include <cuda_runtime.h>
+#endif
 
 #include "../../include/sdepy_gb300.h"
 #include "rng.cuh"
@@ -290,6 +300,7 @@ __device__ __forceinline__ int group_outputs(const R (&st)[MAXM], int M, int out
 // poisson_tail (the temporaries keep the host compiler from fusing them).
 // F * 2^32 is exact and so is subtracting 0.5 (F < 1), so each comparison
 // is exactly the FP64 one; a step with one event needs no FP64 arithmetic.
+#ifndef __CUDACC_RTC__
 static inline void poisson_thresholds(double p0, double lam, long long &thr0, long long &thr1) {
     thr0 = (long long)floor(p0 * 4294967296.0 - 0.5);
     volatile double pk = p0 * lam;
@@ -297,6 +308,7 @@ static inline void poisson_thresholds(double p0, double lam, long long &thr0, lo
     volatile double F1 = p0 + pk1;
     thr1 = (long long)floor(F1 * 4294967296.0 - 0.5);
 }
+#endif
 
 __device__ __forceinline__ int poisson_tail(uint32_t word, double p0, double lam, int32_t *err) {
     const double u = u01_f64(word);
@@ -679,6 +691,23 @@ __device__ __noinline__ void user_coefs(const SdeUserProgram &u, const R *xs, R 
 // the internal kernel model of user SDE systems (q > 1: SdeSpec.model is
 // SDE_MODEL_USER, the program's n_eq selects these instantiations)
 constexpr int SDE_MODEL_USER_SYS = 16;
+// user SDEs compiled at run time (sde_jit.cu): the program becomes the
+// straight-line function UserJitFn<R>::coefs of a runtime-compiled unit,
+// which instantiates the forward kernel with these models
+constexpr int SDE_MODEL_USER_JIT = 32;
+constexpr int SDE_MODEL_USER_SYS_JIT = 48;
+template <typename R>
+struct UserJitFn;   // defined only in runtime-compiled units
+
+// a user program's coefficients: compiled, or interpreted
+template <typename R, int MODEL>
+__device__ __forceinline__ void user_eval(const SdeUserProgram &u, const R *xs, R t, const R (&p)[6],
+                                          R (*out)[SDE_USER_MAX_TERMS]) {
+    if constexpr (MODEL == SDE_MODEL_USER_JIT || MODEL == SDE_MODEL_USER_SYS_JIT)
+        UserJitFn<R>::coefs(xs, t, p, out);
+    else
+        user_coefs<R>(u, xs, t, p, out);
+}
 
 // ---------------------------------------------------------------------------
 // the forward kernel
@@ -714,7 +743,8 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     constexpr bool TDB = TDEP && SHIFT;   // OU rows with the time-dependent-theta term
     // per-step coefficient reloads compiled in (the non-table kernels but
     // the common FP32 Heston and CIR ones)
-    constexpr bool USER = MODEL == SDE_MODEL_USER || MODEL == SDE_MODEL_USER_SYS;
+    constexpr bool USER = MODEL == SDE_MODEL_USER || MODEL == SDE_MODEL_USER_SYS ||
+                          MODEL == SDE_MODEL_USER_JIT || MODEL == SDE_MODEL_USER_SYS_JIT;
     constexpr bool RELOAD = !TAB && (sizeof(R) == 8 || INJECT || TDEP || USER);
     // per-step correlation factors compiled in (the same kernels, TAB ones
     // included, with device noise)
@@ -1079,7 +1109,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                             const R drift = A::mul(c0[m], A::sub(c1[m], st[m]));
                             st[m] = A::add(st[m], A::add(A::mul(drift, dt), A::mul(c2[m], dW[m])));
                         }
-                    } else if (MODEL == SDE_MODEL_USER) {
+                    } else if (MODEL == SDE_MODEL_USER || MODEL == SDE_MODEL_USER_JIT) {
                         // x + (A_1 dZ_1 + ... + A_n dZ_n), the terms in the order of
                         // the SDE function's dict (sdepy sums from 0: 0 + v == v)
 #pragma unroll
@@ -1087,7 +1117,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                             const R pv[6] = {c0[m], c1[m], c2[m], c3[m], c4[m], c5[m]};
                             R A2[1][SDE_USER_MAX_TERMS];
                             const R xm[1] = {st[m]};
-                            user_coefs<R>(a.uprog, xm, tk, pv, A2);
+                            user_eval<R, MODEL>(a.uprog, xm, tk, pv, A2);
                             R s = R(0);
                             for (int i = 0; i < a.uprog.n_terms; ++i) {
                                 const R dz = user_dz(a.uprog.term_source[i], dt, dW[m], dJ[m], m);
@@ -1096,7 +1126,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                             }
                             st[m] = A::add(st[m], s);
                         }
-                    } else if (MODEL == SDE_MODEL_USER_SYS) {
+                    } else if (MODEL == SDE_MODEL_USER_SYS || MODEL == SDE_MODEL_USER_SYS_JIT) {
                         // the group is one last-axis slice: equation e's component
                         // h at e * nc + h; the program runs per component on the
                         // states of every equation, then all states step at once
@@ -1118,7 +1148,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                                     pv[0] = c0[m], pv[1] = c1[m], pv[2] = c2[m];
                                     pv[3] = c3[m], pv[4] = c4[m], pv[5] = c5[m];
                                 }
-                            user_coefs<R>(a.uprog, xs, tk, pv, A2);
+                            user_eval<R, MODEL>(a.uprog, xs, tk, pv, A2);
                             for (int e = 0; e < q; ++e) {
                                 const int m = e * nc + h;
                                 R s = R(0);
@@ -1248,6 +1278,7 @@ coef_table_kernel(const double *tt, int n_steps, const double *x0, const double 
     t[maxm + m] = (float)__dmul_rn(__dmul_rn(prm[ip * W + w], sq), SDE_SQRT_2LN2);
 }
 
+#ifndef __CUDACC_RTC__
 // launcher signature shared by the instantiation units
 template <typename R>
 using FwdLauncher = void (*)(const FwdArgs<R> &, dim3, cudaStream_t);
@@ -1292,5 +1323,6 @@ FwdLauncher<float> find_fwd_f32_anti(int model, int maxm, bool jumps, int *bps);
 // (fwd_anti_tdep_f32.cu)
 FwdLauncher<float> find_fwd_f32_anti_tdep(int model, int maxm, bool jumps, int *bps);
 FwdLauncher<double> find_fwd_f64_anti(int model, int maxm, bool jumps, int *bps);
+#endif  // !__CUDACC_RTC__
 
 }  // namespace sdegpu

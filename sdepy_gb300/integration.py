@@ -415,6 +415,7 @@ class _gpu_process:
             legs = [leg for leg in legs if stats['row'] in leg.out_row][-1:]
         neg = jc = rj = None
         stats_res = None
+        self._work = self.paths*sum(leg.n_steps for leg in legs)   # path-steps of this call
         for leg in legs:
             spec = self._make_spec(0, 0) if self._inject else \
                 self._make_spec(seed, stream)

@@ -41,6 +41,8 @@ from .infrastructure import (
 from .integration import _const, _gpu_process, _per_var, _check_source
 
 _SOURCE_IDS = {'dt': _lib.SRC_DT, 'dw': _lib.SRC_DW, 'dn': _lib.SRC_DN, 'dj': _lib.SRC_DJ}
+# path-steps of a call from which integrate(jit=None) compiles the program
+JIT_WORK = 2**30
 
 _MAX_PARAMS = 6
 
@@ -268,6 +270,7 @@ class _user_process(_gpu_process):
     _model = _lib.MODEL_USER
     _pnames = ()
     _program = None
+    _jit = None
 
     def _coefficients(self, t=1., tmid=1.):
         A = self._args
@@ -393,9 +396,16 @@ class _user_process(_gpu_process):
 
     def _make_spec(self, seed=0, stream=0):
         s = super()._make_spec(seed, stream)
-        # the program with this instance's jump parameters
+        # the program with this instance's jump parameters, compiled at run
+        # time (NVRTC, a few seconds once per process and program) when the
+        # class was made with jit=True, or by default for runs of at least
+        # JIT_WORK path-steps when the library can compile
         self._uprog = _lib.SdeUserProgram.from_buffer_copy(self._program)
         self._uprog.jump_params = _lib.dptr(self._jp)
+        jit = self._jit
+        if jit is None:
+            jit = getattr(self, '_work', 0) >= JIT_WORK and bool(_lib.load().sde_jit_available())
+        self._uprog.jit = 1 if jit else 0
         s.program = C.pointer(self._uprog)
         return s
 
@@ -459,15 +469,21 @@ class _user_sys_process(_user_process):
         return tuple(process(tt, x=np.ascontiguousarray(x)) for x in xs)
 
 
-def integrate(sde=None, *, q=None, sources=None, log=False, addaxis=False):
+def integrate(sde=None, *, q=None, sources=None, log=False, addaxis=False, jit=None):
     """Decorator making a GPU process class of an SDE function
     ``sde(t, x, **params)`` (sdepy's ``integrate``,
     sdepy/integration.py:1890-1955): ``@integrate def my_process(t, x,
     theta=1., k=1., sigma=1.): return {'dt': k*(theta - x), 'dw': sigma}``,
-    then ``my_process(x0=1, sigma=.5, paths=..., steps=...)(timeline)``."""
+    then ``my_process(x0=1, sigma=.5, paths=..., steps=...)(timeline)``.
+
+    ``jit`` (an addition to sdepy's signature): True compiles the traced
+    program into the forward kernel at run time (NVRTC, once per process
+    and program), False interprets it on the device, None (default)
+    compiles for calls of at least JIT_WORK path-steps when the library
+    can."""
     if sde is None:
         def decorator(f):
-            return integrate(f, q=q, sources=sources, log=log, addaxis=addaxis)
+            return integrate(f, q=q, sources=sources, log=log, addaxis=addaxis, jit=jit)
         return decorator
     # the reference's test evaluation (sdepy/integration.py:1843-1886)
     if q is not None and sources is not None:
@@ -509,7 +525,7 @@ def integrate(sde=None, *, q=None, sources=None, log=False, addaxis=False):
     params.update(defaults)
     attrs = dict(_params=params, _pnames=pnames, _tdep_names=pnames, _program=program,
                  _log=bool(log), _out=_lib.OUT_EXP if log else _lib.OUT_STATE,
-                 sde=staticmethod(sde), q=neq, sources_ids=frozenset(ids), addaxis=bool(addaxis),
+                 sde=staticmethod(sde), q=neq, sources_ids=frozenset(ids), addaxis=bool(addaxis), _jit=jit,
                  _addaxis_flag=bool(addaxis), _q=max(neq, 1), __doc__=sde.__doc__)
     base = _user_process if neq == 0 else _user_sys_process
     return type(getattr(sde, '__name__', 'sde_integrator'), (base,), attrs)

@@ -300,16 +300,17 @@ def user_sources(f, q):
     return ids
 
 
-def user_class(module, spec):
+def user_class(module, spec, **kw):
     """The process class of a fixture's ``cls`` entry '<kind>:<function>',
     made by ``module.integrate``: kind is 'integrate' with optional '_log'
-    (log=True), '_q<n>' (a system of n equations) and '_addaxis'."""
+    (log=True), '_q<n>' (a system of n equations) and '_addaxis'; ``kw``
+    more keywords of the drop-in's integrate (jit)."""
     kind, name = spec.split(':')
     parts = kind.split('_')
     q = next((int(x[1:]) for x in parts if x.startswith('q')), None)
     f = USER[name]
     return module.integrate(f, q=q, sources=user_sources(f, q) if q else None, log='log' in parts,
-                            addaxis='addaxis' in parts)
+                            addaxis='addaxis' in parts, **kw)
 
 
 def tdep_kwargs(z, process_cls):

@@ -441,3 +441,80 @@ def test_gpu_user_merton_equals_preset(lib):
         xu = jd(rng=sg.philox_rng(11, 2), y=sg.norm_rv(-.1, .15), **kw)(tl)
         xm = sg.merton_jumpdiff_process(rng=sg.philox_rng(11, 2), a=-.1, b=.15, **kw)(tl)
         np.testing.assert_array_equal(np.asarray(xu), np.asarray(xm))
+
+
+# ---------------------------------------------------------------------------
+# runtime compilation of the programs (NVRTC)
+# ---------------------------------------------------------------------------
+def test_jit_compiles_every_program():
+    """Every test function's program compiles into the forward kernel
+    through the library's code generator and NVRTC (no device needed), in
+    both precisions, for single groups and the widths the tests use, with
+    device and injected noise."""
+    import ctypes as C
+    from sdepy_gb300 import _build
+    _build.build()
+    lib = _lib.load()
+    if not lib.sde_jit_available():
+        pytest.skip('NVRTC not available')
+    buf = C.create_string_buffer(1024)
+    for name, f in sorted(USER.items()):
+        import inspect
+        nvars = sum(p.default is p.empty for p in inspect.signature(f).parameters.values()) - 1
+        q = nvars if nvars > 1 else None
+        cls = sg.integrate(f, q=q, sources=user_sources(f, q) if q else None)
+        jumps = int(bool({'dn', 'dj'} & set(cls.sources_ids)))
+        # one combination per program, rotating precision, width and noise mode
+        i = sorted(USER).index(name)
+        prec = (_lib.FP64, _lib.FP32)[i % 2]
+        M = ((2, 4) if q else (1, 4))[(i // 2) % 2]
+        inj = (i // 4) % 2
+        rc = lib.sde_jit_compile(C.byref(cls._program), prec, M, inj, jumps, buf, 1024)
+        assert rc == 0, (name, prec, M, inj, buf.value.decode())
+
+
+JIT_CASES = [
+    ('ou', 'integrate:user_ou', dict(x0=1., theta=.5, k=2., sigma=.3), np.linspace(0, 1, 5), 40, 0),
+    ('cev_vec4', 'integrate:user_cev', dict(vshape=4, x0=1., mu=.05, sigma=.6, gamma=.7), (0., 1.), 40, 0),
+    ('mixed_i0', 'integrate:user_mixed', dict(x0=.5, a=1.5, b=.7, s=.25), np.linspace(0, 2, 3), 50, 1),
+    ('sys_sv', 'integrate_q2:user_sv', dict(x0=(100., .04), mu=.05, k=1.5, theta=.04, xi=.5, rho=-.7),
+     (0., .5, 1.), 50, 0),
+    ('jumps4', 'integrate:user_jumps4', dict(x0=.5, lam='tdep_lam', y=('exp', -.2)), np.linspace(0, 2, 3), 60, 0),
+    ('sys_dj_dw', 'integrate_q2:user_sys_dj_dw', dict(x0=(0., 0.), k=.7, lam=3., y=('double_exp', 1., 2., .1)),
+     np.linspace(0, 1, 4), 30, 0),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('case', JIT_CASES, ids=[c[0] for c in JIT_CASES])
+def test_gpu_jit_equals_interpreter(lib, case):
+    """The runtime-compiled program gives the interpreter's paths: bit for
+    bit in FP64 (the same rounded operations), to FP32 accuracy in FP32
+    (the compiler may fuse a product into a sum)."""
+    name, spec, kw, tl, steps, i0 = case
+    assert lib.sde_jit_available()
+    for dtype in (None, np.float32):
+        outs = []
+        for jit in (False, True):
+            P = user_class(sg, spec, jit=jit)(paths=2049, steps=steps, i0=i0, dtype=dtype,
+                                               rng=sg.philox_rng(77, 1), **_jkw(kw))
+            outs.append([np.asarray(x, dtype=float) for x in _outputs(P(tl))])
+        for a, b in zip(*outs):
+            if dtype is None:
+                np.testing.assert_array_equal(a, b)
+            else:
+                assert np.max(np.abs(a - b)/np.maximum(np.abs(b), 1.)) < 1e-4
+
+
+@pytest.mark.gpu
+def test_gpu_jit_replays_reference(lib):
+    """The compiled program replays the reference's recorded increments of
+    a system with compound Poisson and Wiener terms to 1e-12."""
+    z = np.load(os.path.join(GOLDEN, 'userj_sys_dj_dw.npz'))
+    kw, vshape, paths = _fixture_args(z)
+    cls = user_class(sg, str(z['cls']), jit=True)
+    P = cls(paths=paths, vshape=vshape, steps=json.loads(str(z['steps'])), i0=int(z['i0']),
+            **_jump_replays(z, paths), **kw)
+    for k, x in enumerate(_outputs(P(z['timeline']))):
+        ref = z['xx%d' % k]
+        assert np.max(np.abs(np.asarray(x) - ref)/np.maximum(np.abs(ref), 1.)) <= 1e-12
