@@ -638,6 +638,7 @@ def extra_configs(lib):
     cev = sg.integrate(lambda t, x, mu=.05, sigma=.2, gamma=.7: {'dt': mu*x, 'dw': sigma*np.maximum(x, 0.)**gamma},
                        jit=False)
     for name, P, strike in (('user_ou', user_ou(paths=K, steps=500, dtype=np.float32, x0=1.), .5),
+                            ('user_ou_jit', user_ou_jit(paths=K, steps=500, dtype=np.float32, x0=1.), .5),
                             ('preset_ou', sg.ornstein_uhlenbeck_process(paths=K, steps=500, dtype=np.float32,
                                                                         x0=1., theta=.5, k=2., sigma=.3), .5),
                             ('user_cev', cev(paths=K, steps=500, dtype=np.float32, x0=1.), 1.)):

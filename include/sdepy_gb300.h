@@ -256,6 +256,11 @@ SDE_API int32_t sde_jit_available(void);
 SDE_API int32_t sde_jit_compile(const SdeUserProgram *program, int32_t precision, int32_t group_size,
                                 int32_t injected, int32_t jumps, char *log, int32_t len);
 
+/* The same for the adjoint kernel of a single-equation program (group
+ * size 1..8): the coefficients and their tangents compiled in. */
+SDE_API int32_t sde_jit_compile_adjoint(const SdeUserProgram *program, int32_t precision, int32_t group_size,
+                                        char *log, int32_t len);
+
 /* free the device scratch cached by the library on the current device */
 SDE_API int32_t sde_release(void);
 
@@ -333,7 +338,8 @@ SDE_API int32_t sde_run_stats(const SdeSpec *spec, const SdeGrid *grid,
  * params p0..p5, and in slot 7 of a group's first variable d L / d rho
  * (2-variable Heston group with corr = [[1, rho], [rho, 1]]).  value = L.
  * For a user SDE (single equation, dt / dw terms) slot 1 + j is d L / d
- * of the program's parameter p_j, from a tangent-mode run of its program.
+ * of the program's parameter p_j, from a tangent-mode run of its program
+ * (interpreted, or compiled at run time with SdeUserProgram.jit = 1).
  * The adjoint of the Euler recursion is propagated backwards through
  * checkpointed segments recomputed from Philox counters (constant for the
  * LINEAR model); no path is stored.  No counterpart in the reference

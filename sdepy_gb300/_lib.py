@@ -114,6 +114,8 @@ SIGNATURES = {
     'sde_jit_available': (C.c_int32, []),
     'sde_jit_compile': (C.c_int32, [C.POINTER(SdeUserProgram), C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                     C.c_char_p, C.c_int32]),
+    'sde_jit_compile_adjoint': (C.c_int32, [C.POINTER(SdeUserProgram), C.c_int32, C.c_int32, C.c_char_p,
+                                            C.c_int32]),
     'sde_release': (C.c_int32, []),
     'sde_set_stream': (C.c_int32, [C.c_void_p]),
     'sde_normal_pairs': (C.c_int32, [C.POINTER(C.c_uint32), C.c_int64, C.c_int32, _dp]),

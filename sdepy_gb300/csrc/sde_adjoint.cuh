@@ -59,13 +59,12 @@ struct AdjArgs {
 // at 0 (the one-sided value of the truncated models); a ** b adds the b
 // term v log a only where a > 0.
 constexpr int UTAN = 7;
+
+// the seeds of a tangent-mode run: r0 = x (d/dx = 1), r1 = t, r2..r7 = p
+// (d/dp_j = 1)
 template <typename R>
-__device__ __noinline__ void user_coefs_tan(const SdeUserProgram &u, R x, R t, const R (&p)[6],
-                                            R (&A)[SDE_USER_MAX_TERMS], R (&dA)[SDE_USER_MAX_TERMS][UTAN]) {
-    typedef Ar<R> Ao;
-    typedef UFn<R> F;
-    R r[SDE_USER_MAX_REGS];
-    R d[SDE_USER_MAX_REGS][UTAN];
+__device__ __forceinline__ void tan_inputs(R x, R t, const R (&p)[6], R (&r)[SDE_USER_MAX_REGS],
+                                           R (&d)[SDE_USER_MAX_REGS][UTAN]) {
     r[0] = x;
     r[1] = t;
 #pragma unroll
@@ -77,57 +76,70 @@ __device__ __noinline__ void user_coefs_tan(const SdeUserProgram &u, R x, R t, c
     d[0][0] = R(1);
 #pragma unroll
     for (int i = 0; i < 6; ++i) d[2 + i][1 + i] = R(1);
-    for (int i = 0; i < u.n_ops; ++i) {
-        const uint32_t op = u.ops[i];
-        const int dst = (op >> 8) & 0xff, ia = (op >> 16) & 0xff, ib = op >> 24;
-        const int code = op & 0xff;
-        if (code == SDE_UOP_CONST) {
-            r[dst] = (R)u.consts[ia];
-#pragma unroll
-            for (int j = 0; j < UTAN; ++j) d[dst][j] = R(0);
-            continue;
-        }
-        const R va = r[ia], vb = r[ib];
-        R v, da = R(0), db = R(0);   // the result and its partials in a and b
-        switch (code) {
-        case SDE_UOP_ADD: v = Ao::add(va, vb); da = R(1); db = R(1); break;
-        case SDE_UOP_SUB: v = Ao::sub(va, vb); da = R(1); db = R(-1); break;
-        case SDE_UOP_MUL: v = Ao::mul(va, vb); da = vb; db = va; break;
-        case SDE_UOP_DIV: v = va / vb; da = R(1) / vb; db = -v / vb; break;
-        case SDE_UOP_NEG: v = -va; da = R(-1); break;
-        case SDE_UOP_ABS: v = fabs(va); da = va < R(0) ? R(-1) : R(1); break;
-        case SDE_UOP_EXP: v = F::exp_(va); da = v; break;
-        case SDE_UOP_LOG: v = F::log_(va); da = R(1) / va; break;
-        case SDE_UOP_SQRT: v = Ao::sqrt_(va); da = v > R(0) ? R(0.5) / v : R(0); break;
-        case SDE_UOP_MAX: v = np_max(va, vb); if (va >= vb) da = R(1); else db = R(1); break;
-        case SDE_UOP_MIN: v = np_min(va, vb); if (va <= vb) da = R(1); else db = R(1); break;
-        case SDE_UOP_SIN: v = F::sin_(va); da = F::cos_(va); break;
-        case SDE_UOP_COS: v = F::cos_(va); da = -F::sin_(va); break;
-        case SDE_UOP_TAN: v = F::tan_(va); da = R(1) + v * v; break;
-        case SDE_UOP_TANH: v = F::tanh_(va); da = R(1) - v * v; break;
-        case SDE_UOP_POW:
-            v = F::pow_(va, vb);
-            da = vb * F::pow_(va, vb - R(1));
-            db = va > R(0) ? v * F::log_(va) : R(0);
-            break;
-        case SDE_UOP_EXPM1: v = F::expm1_(va); da = v + R(1); break;
-        case SDE_UOP_LOG1P: v = F::log1p_(va); da = R(1) / (R(1) + va); break;
-        case SDE_UOP_ARCTAN: v = F::atan_(va); da = R(1) / (R(1) + va * va); break;
-        default: v = va; da = R(1); break;   // SDE_UOP_COPY
-        }
-        R nd[UTAN];
-#pragma unroll
-        for (int j = 0; j < UTAN; ++j) {
-            // a zero tangent contributes nothing (no 0 * inf)
-            const R ta = d[ia][j], tb = d[ib][j];
-            R s = ta != R(0) ? da * ta : R(0);
-            if (tb != R(0) && db != R(0)) s = s + db * tb;
-            nd[j] = s;
-        }
-        r[dst] = v;
-#pragma unroll
-        for (int j = 0; j < UTAN; ++j) d[dst][j] = nd[j];
+}
+
+// one instruction (not SDE_UOP_CONST) in tangent mode: value and tangents
+template <typename R>
+__device__ __forceinline__ void tan_op(uint32_t op, R (&r)[SDE_USER_MAX_REGS], R (&d)[SDE_USER_MAX_REGS][UTAN]) {
+    typedef Ar<R> Ao;
+    typedef UFn<R> F;
+    const int dst = (op >> 8) & 0xff, ia = (op >> 16) & 0xff, ib = op >> 24;
+    const int code = op & 0xff;
+    const R va = r[ia], vb = r[ib];
+    R v, da = R(0), db = R(0);   // the result and its partials in a and b
+    switch (code) {
+    case SDE_UOP_ADD: v = Ao::add(va, vb); da = R(1); db = R(1); break;
+    case SDE_UOP_SUB: v = Ao::sub(va, vb); da = R(1); db = R(-1); break;
+    case SDE_UOP_MUL: v = Ao::mul(va, vb); da = vb; db = va; break;
+    case SDE_UOP_DIV: v = va / vb; da = R(1) / vb; db = -v / vb; break;
+    case SDE_UOP_NEG: v = -va; da = R(-1); break;
+    case SDE_UOP_ABS: v = fabs(va); da = va < R(0) ? R(-1) : R(1); break;
+    case SDE_UOP_EXP: v = F::exp_(va); da = v; break;
+    case SDE_UOP_LOG: v = F::log_(va); da = R(1) / va; break;
+    case SDE_UOP_SQRT: v = Ao::sqrt_(va); da = v > R(0) ? R(0.5) / v : R(0); break;
+    case SDE_UOP_MAX: v = np_max(va, vb); if (va >= vb) da = R(1); else db = R(1); break;
+    case SDE_UOP_MIN: v = np_min(va, vb); if (va <= vb) da = R(1); else db = R(1); break;
+    case SDE_UOP_SIN: v = F::sin_(va); da = F::cos_(va); break;
+    case SDE_UOP_COS: v = F::cos_(va); da = -F::sin_(va); break;
+    case SDE_UOP_TAN: v = F::tan_(va); da = R(1) + v * v; break;
+    case SDE_UOP_TANH: v = F::tanh_(va); da = R(1) - v * v; break;
+    case SDE_UOP_POW:
+        v = F::pow_(va, vb);
+        da = vb * F::pow_(va, vb - R(1));
+        db = va > R(0) ? v * F::log_(va) : R(0);
+        break;
+    case SDE_UOP_EXPM1: v = F::expm1_(va); da = v + R(1); break;
+    case SDE_UOP_LOG1P: v = F::log1p_(va); da = R(1) / (R(1) + va); break;
+    case SDE_UOP_ARCTAN: v = F::atan_(va); da = R(1) / (R(1) + va * va); break;
+    default: v = va; da = R(1); break;   // SDE_UOP_COPY
     }
+    R nd[UTAN];
+#pragma unroll
+    for (int j = 0; j < UTAN; ++j) {
+        // a zero tangent contributes nothing (no 0 * inf)
+        const R ta = d[ia][j], tb = d[ib][j];
+        R s = ta != R(0) ? da * ta : R(0);
+        if (tb != R(0) && db != R(0)) s = s + db * tb;
+        nd[j] = s;
+    }
+    r[dst] = v;
+#pragma unroll
+    for (int j = 0; j < UTAN; ++j) d[dst][j] = nd[j];
+}
+
+// a constant in tangent mode
+template <typename R>
+__device__ __forceinline__ void tan_const(int dst, R c, R (&r)[SDE_USER_MAX_REGS], R (&d)[SDE_USER_MAX_REGS][UTAN]) {
+    r[dst] = c;
+#pragma unroll
+    for (int j = 0; j < UTAN; ++j) d[dst][j] = R(0);
+}
+
+// the terms' values and tangents from the registers
+template <typename R>
+__device__ __forceinline__ void tan_outputs(const SdeUserProgram &u, const R (&r)[SDE_USER_MAX_REGS],
+                                            const R (&d)[SDE_USER_MAX_REGS][UTAN], R (&A)[SDE_USER_MAX_TERMS],
+                                            R (&dA)[SDE_USER_MAX_TERMS][UTAN]) {
 #pragma unroll
     for (int i = 0; i < SDE_USER_MAX_TERMS; ++i) {
         const int reg = i < u.n_terms ? u.term_register[0][i] : 0;
@@ -137,9 +149,36 @@ __device__ __noinline__ void user_coefs_tan(const SdeUserProgram &u, R x, R t, c
     }
 }
 
+template <typename R>
+__device__ __noinline__ void user_coefs_tan(const SdeUserProgram &u, R x, R t, const R (&p)[6],
+                                            R (&A)[SDE_USER_MAX_TERMS], R (&dA)[SDE_USER_MAX_TERMS][UTAN]) {
+    R r[SDE_USER_MAX_REGS];
+    R d[SDE_USER_MAX_REGS][UTAN];
+    tan_inputs<R>(x, t, p, r, d);
+    for (int i = 0; i < u.n_ops; ++i) {
+        const uint32_t op = u.ops[i];
+        if ((op & 0xff) == SDE_UOP_CONST) tan_const<R>((op >> 8) & 0xff, (R)u.consts[(op >> 16) & 0xff], r, d);
+        else tan_op<R>(op, r, d);
+    }
+    tan_outputs<R>(u, r, d, A, dA);
+}
+
+// runtime-compiled tangent run (sde_jit.cu: UserJitTan<R>::tan, the same
+// steps with the instructions as constants), else the interpreter
+template <typename R>
+struct UserJitTan;
+template <typename R, int MODEL>
+__device__ __forceinline__ void user_tan_eval(const SdeUserProgram &u, R x, R t, const R (&p)[6],
+                                              R (&A)[SDE_USER_MAX_TERMS], R (&dA)[SDE_USER_MAX_TERMS][UTAN]) {
+    if constexpr (MODEL == SDE_MODEL_USER_JIT)
+        UserJitTan<R>::tan(u, x, t, p, A, dA);
+    else
+        user_coefs_tan<R>(u, x, t, p, A, dA);
+}
+
 // one forward Euler step of a user SDE (the forward kernel's arithmetic):
 // x + (A_1 dZ_1 + A_2 dZ_2), dZ = dt or dW
-template <typename R, int MAXM>
+template <typename R, int MAXM, int MODEL = SDE_MODEL_USER>
 __device__ __forceinline__ void user_step(const SdeUserProgram &u, const R (&c0)[MAXM], const R (&c1)[MAXM],
                                           const R (&c2)[MAXM], const R (&c3)[MAXM], const R (&c4)[MAXM],
                                           const R (&c5)[MAXM], R t, R dt, const R (&dW)[MAXM], R (&st)[MAXM]) {
@@ -149,7 +188,7 @@ __device__ __forceinline__ void user_step(const SdeUserProgram &u, const R (&c0)
         const R pv[6] = {c0[m], c1[m], c2[m], c3[m], c4[m], c5[m]};
         R A2[1][SDE_USER_MAX_TERMS];
         const R xm[1] = {st[m]};
-        user_coefs<R>(u, xm, t, pv, A2);
+        user_eval<R, MODEL>(u, xm, t, pv, A2);
         R s = R(0);
         for (int i = 0; i < u.n_terms; ++i) {
             const R term = A::mul(A2[0][i], u.term_source[i] == SDE_SRC_DT ? dt : dW[m]);
@@ -281,6 +320,8 @@ __device__ __forceinline__ void fwd_step(const R (&c0)[MAXM], const R (&c1)[MAXM
 template <typename R, int MODEL, int MAXM, bool JUMPS>
 __global__ void __launch_bounds__(BLOCK, (sizeof(R) == 4 && MAXM <= 2) ? 3 : 1)
 sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
+    // a user SDE: interpreted, or compiled at run time
+    constexpr bool UJ = MODEL == SDE_MODEL_USER || MODEL == SDE_MODEL_USER_JIT;
     typedef Ar<R> A;
     constexpr int NCMAX = NoiseShape<MAXM, JUMPS>::NCMAX;
     constexpr int NPA = MAXM * NGV + 2;
@@ -405,7 +446,7 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                 uint32_t u[4 * NCMAX];
                 R z[MAXM], dW[MAXM];
                 noise(k, sq, u, z, dW);
-                if constexpr (MODEL == SDE_MODEL_USER) user_step<R, MAXM>(a.uprog, c0, c1, c2, c3, c4, c5, a.tk[k], a.dt[k], dW, st);
+                if constexpr (UJ) user_step<R, MAXM, MODEL>(a.uprog, c0, c1, c2, c3, c4, c5, a.tk[k], a.dt[k], dW, st);
                 else fwd_step<R, MODEL, MAXM>(c0, c1, c2, a.dt[k], dW, st);
             }
             R xb[MAXM];
@@ -428,19 +469,19 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                     }
                     bz[k - k0][0] = z[0];
                     bz[k - k0][1] = MAXM > 1 ? z[MAXM > 1 ? 1 : 0] : R(0);
-                    if constexpr (MODEL == SDE_MODEL_USER) user_step<R, MAXM>(a.uprog, c0, c1, c2, c3, c4, c5, a.tk[k], a.dt[k], dW, st);
+                    if constexpr (UJ) user_step<R, MAXM, MODEL>(a.uprog, c0, c1, c2, c3, c4, c5, a.tk[k], a.dt[k], dW, st);
                     else fwd_step<R, MODEL, MAXM>(c0, c1, c2, a.dt[k], dW, st);
                 }
                 for (int k = k1 - 1; k >= k0; --k) {
                     const R dt = a.dt[k], sq = a.sqdt[k];
-                    if constexpr (MODEL == SDE_MODEL_USER) {
+                    if constexpr (UJ) {
                         // x' = x + sum_i A_i(t, x, p) dZ_i: dx'/dx = 1 + sum_i dA_i/dx dZ_i,
                         // dx'/dp_j = sum_i dA_i/dp_j dZ_i
 #pragma unroll
                         for (int m = 0; m < MAXM; ++m) {
                             const R pv[6] = {c0[m], c1[m], c2[m], c3[m], c4[m], c5[m]};
                             R Av[SDE_USER_MAX_TERMS], dA[SDE_USER_MAX_TERMS][UTAN];
-                            user_coefs_tan<R>(a.uprog, bx[k - k0][m], a.tk[k], pv, Av, dA);
+                            user_tan_eval<R, MODEL>(a.uprog, bx[k - k0][m], a.tk[k], pv, Av, dA);
                             R gx = R(0), gp[6] = {R(0), R(0), R(0), R(0), R(0), R(0)};
                             for (int i = 0; i < a.uprog.n_terms; ++i) {
                                 const R dz = a.uprog.term_source[i] == SDE_SRC_DT ? dt : bw[k - k0][m];
@@ -531,6 +572,7 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
     if (threadIdx.x == 0) a.partials[(((int64_t)g * gridDim.x + blockIdx.x) * NPA) + NPA - 1] = 0.0;
 }
 
+#ifndef __CUDACC_RTC__
 template <typename R>
 using AdjLauncher = void (*)(const AdjArgs<R> &, dim3, cudaStream_t);
 
@@ -551,5 +593,6 @@ AdjLauncher<double> find_adj_f64(int model, int maxm, bool jumps, int *bps);
 // user SDEs (adj_user.cu)
 AdjLauncher<float> find_adj_user_f32(int maxm, int *bps);
 AdjLauncher<double> find_adj_user_f64(int maxm, int *bps);
+#endif  // !__CUDACC_RTC__
 
 }  // namespace sdegpu

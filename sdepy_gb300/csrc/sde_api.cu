@@ -1255,8 +1255,16 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     a.err = (int32_t *)d_err;
 
     int bps = 0;
-    AdjLauncher<R> L = AdjFinder<R>::find(s->model, maxm, jumps, &bps);
-    if (!L) return fail(SDE_ERR_UNSUPPORTED, "no adjoint kernel for model %d group size %d", s->model, M);
+    // a user program compiled at run time, or an instantiated kernel
+    cudaKernel_t jk = nullptr;
+    AdjLauncher<R> L = nullptr;
+    if (user && s->program->jit) {
+        std::string err;
+        if ((rc = jit_adj_kernel(*s->program, sizeof(R) == 8, maxm, &jk, &bps, &err))) return fail(rc, "%s", err.c_str());
+    } else {
+        L = AdjFinder<R>::find(s->model, maxm, jumps, &bps);
+        if (!L) return fail(SDE_ERR_UNSUPPORTED, "no adjoint kernel for model %d group size %d", s->model, M);
+    }
     const int nbx = path_blocks(D, s->paths, s->groups, bps);
     const int npa = maxm * NGV + 2;
     void *part, *res;
@@ -1264,7 +1272,12 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     if ((rc = scratch(D, S_RES, sizeof(double) * (size_t)s->groups * npa, &res))) return rc;
     a.partials = (double *)part;
     if (D->timing) CU(cudaEventRecord(D->ev[0], st));
-    L(a, dim3(nbx, s->groups), st);
+    if (jk) {
+        void *args[] = {(void *)&a};
+        CU(cudaLaunchKernel((const void *)jk, dim3(nbx, s->groups), dim3(BLOCK), args, 0, st));
+    } else {
+        L(a, dim3(nbx, s->groups), st);
+    }
     CU(cudaGetLastError());
     if (D->timing) CU(cudaEventRecord(D->ev[1], st));
     for (int g = 0; g < s->groups; ++g) {

@@ -127,8 +127,9 @@ std::string kernel_name(const char *rt, int model, int maxm, bool inject, bool j
     return buf;
 }
 
-std::string jit_source(const SdeUserProgram &u, const char *rt, int model, int maxm, bool inject, bool jumps) {
-    std::string s = "#include \"sde_kernels.cuh\"\nnamespace sdegpu {\ntemplate <> struct UserJitFn<";
+// UserJitFn<R>: the program as straight-line coefficient code
+std::string coefs_struct(const SdeUserProgram &u, const char *rt) {
+    std::string s = "template <> struct UserJitFn<";
     s += rt;
     s += "> {\n  typedef ";
     s += rt;
@@ -143,8 +144,55 @@ std::string jit_source(const SdeUserProgram &u, const char *rt, int model, int m
         for (int j = 0; j < SDE_USER_MAX_TERMS; ++j)
             s += "    out[" + std::to_string(e) + "][" + std::to_string(j) + "] = " +
                  (j < u.n_terms ? "r[" + std::to_string(u.term_register[e][j]) + "]" : std::string("R(0)")) + ";\n";
-    s += "  }\n};\ntemplate __global__ void " + kernel_name(rt, model, maxm, inject, jumps) +
-         "(const __grid_constant__ FwdArgs<" + rt + ">);\n}  // namespace sdegpu\n";
+    s += "  }\n};\n";
+    return s;
+}
+
+std::string jit_source(const SdeUserProgram &u, const char *rt, int model, int maxm, bool inject, bool jumps) {
+    return "#include \"sde_kernels.cuh\"\nnamespace sdegpu {\n" + coefs_struct(u, rt) + "template __global__ void " +
+           kernel_name(rt, model, maxm, inject, jumps) + "(const __grid_constant__ FwdArgs<" + rt +
+           ">);\n}  // namespace sdegpu\n";
+}
+
+std::string adj_kernel_name(const char *rt, int maxm) {
+    char buf[160];
+    snprintf(buf, sizeof buf, "sdegpu::sde_adj_kernel<%s, %d, %d, false>", rt, SDE_MODEL_USER_JIT, maxm);
+    return buf;
+}
+
+// the adjoint kernel of a single-equation program: the coefficients, and
+// UserJitTan<R>::tan, the interpreter's tangent steps (tan_op) with the
+// instructions as constants and the terms read from fixed registers
+std::string jit_adj_source(const SdeUserProgram &u, const char *rt, int maxm) {
+    std::string s = "#include \"sde_adjoint.cuh\"\nnamespace sdegpu {\n" + coefs_struct(u, rt);
+    s += "template <> struct UserJitTan<";
+    s += rt;
+    s += "> {\n  typedef ";
+    s += rt;
+    s += " R;\n  static __device__ __forceinline__ void tan(const SdeUserProgram &, R x, R t, const R (&p)[6],"
+         " R (&A)[SDE_USER_MAX_TERMS], R (&dA)[SDE_USER_MAX_TERMS][UTAN]) {\n"
+         "    R r[SDE_USER_MAX_REGS];\n    R d[SDE_USER_MAX_REGS][UTAN];\n    tan_inputs<R>(x, t, p, r, d);\n";
+    char buf[160];
+    for (int i = 0; i < u.n_ops; ++i) {
+        const uint32_t op = u.ops[i];
+        if ((op & 0xff) == SDE_UOP_CONST) {
+            uint64_t bits;
+            memcpy(&bits, &u.consts[(op >> 16) & 0xff], sizeof bits);
+            snprintf(buf, sizeof buf, "    tan_const<R>(%d, (R)__longlong_as_double((long long)0x%016llxULL), r, d);\n",
+                     (int)((op >> 8) & 0xff), (unsigned long long)bits);
+        } else {
+            snprintf(buf, sizeof buf, "    tan_op<R>(0x%08xu, r, d);\n", op);
+        }
+        s += buf;
+    }
+    for (int j = 0; j < SDE_USER_MAX_TERMS; ++j) {
+        const std::string reg = std::to_string(j < u.n_terms ? u.term_register[0][j] : 0);
+        s += "    A[" + std::to_string(j) + "] = " + (j < u.n_terms ? "r[" + reg + "]" : std::string("R(0)")) + ";\n";
+        s += "#pragma unroll\n    for (int j = 0; j < UTAN; ++j) dA[" + std::to_string(j) + "][j] = " +
+             (j < u.n_terms ? "d[" + reg + "][j]" : std::string("R(0)")) + ";\n";
+    }
+    s += "  }\n};\ntemplate __global__ void " + adj_kernel_name(rt, maxm) + "(const __grid_constant__ AdjArgs<" + rt +
+         ">);\n}  // namespace sdegpu\n";
     return s;
 }
 
@@ -208,11 +256,9 @@ int jit_compile_check(const SdeUserProgram &u, bool fp64, int maxm, bool inject,
                          &cubin, &low, err);
 }
 
-int jit_fwd_kernel(const SdeUserProgram &u, bool fp64, int maxm, bool inject, bool jumps, cudaKernel_t *kernel,
-                   int *bps, std::string *err) {
-    const char *rt = fp64 ? "double" : "float";
-    const int model = u.n_eq > 1 ? SDE_MODEL_USER_SYS_JIT : SDE_MODEL_USER_JIT;
-    const std::string src = jit_source(u, rt, model, maxm, inject, jumps);
+// the kernel `name` of `src`, compiled and loaded once per process
+static int cached_kernel(const std::string &src, const std::string &name, cudaKernel_t *kernel, int *bps,
+                         std::string *err) {
     std::lock_guard<std::mutex> lk(g_cache_mu);
     auto it = g_cache.find(src);
     if (it != g_cache.end()) {
@@ -223,7 +269,7 @@ int jit_fwd_kernel(const SdeUserProgram &u, bool fp64, int maxm, bool inject, bo
     std::vector<char> cubin;
     std::string low;
     int rc;
-    if ((rc = compile_cubin(src, kernel_name(rt, model, maxm, inject, jumps), &cubin, &low, err))) return rc;
+    if ((rc = compile_cubin(src, name, &cubin, &low, err))) return rc;
     Entry e;
     if (cudaLibraryLoadData(&e.lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0) != cudaSuccess ||
         cudaLibraryGetKernel(&e.kernel, e.lib, low.c_str()) != cudaSuccess) {
@@ -242,9 +288,47 @@ int jit_fwd_kernel(const SdeUserProgram &u, bool fp64, int maxm, bool inject, bo
     return SDE_OK;
 }
 
+int jit_compile_check_adjoint(const SdeUserProgram &u, bool fp64, int maxm, std::string *err) {
+    const char *rt = fp64 ? "double" : "float";
+    std::vector<char> cubin;
+    std::string low;
+    return compile_cubin(jit_adj_source(u, rt, maxm), adj_kernel_name(rt, maxm), &cubin, &low, err);
+}
+
+int jit_fwd_kernel(const SdeUserProgram &u, bool fp64, int maxm, bool inject, bool jumps, cudaKernel_t *kernel,
+                   int *bps, std::string *err) {
+    const char *rt = fp64 ? "double" : "float";
+    const int model = u.n_eq > 1 ? SDE_MODEL_USER_SYS_JIT : SDE_MODEL_USER_JIT;
+    return cached_kernel(jit_source(u, rt, model, maxm, inject, jumps), kernel_name(rt, model, maxm, inject, jumps),
+                         kernel, bps, err);
+}
+
+int jit_adj_kernel(const SdeUserProgram &u, bool fp64, int maxm, cudaKernel_t *kernel, int *bps, std::string *err) {
+    const char *rt = fp64 ? "double" : "float";
+    return cached_kernel(jit_adj_source(u, rt, maxm), adj_kernel_name(rt, maxm), kernel, bps, err);
+}
+
 }  // namespace sdegpu
 
 extern "C" int32_t sde_jit_available(void) { return sdegpu::jit_available() ? 1 : 0; }
+
+extern "C" int32_t sde_jit_compile_adjoint(const SdeUserProgram *program, int32_t precision, int32_t group_size,
+                                           char *log, int32_t len) {
+    std::string err;
+    int rc = SDE_ERR_INVALID;
+    if (!program || group_size < 1 || group_size > 8 || program->n_eq != 1 || program->n_ops < 0 ||
+        program->n_ops > SDE_USER_MAX_OPS || program->n_terms < 0 || program->n_terms > SDE_USER_MAX_TERMS) {
+        err = "invalid program (single equations) or group size (1..8)";
+    } else {
+        const int maxm = group_size <= 1 ? 1 : group_size <= 2 ? 2 : group_size <= 4 ? 4 : 8;
+        rc = sdegpu::jit_compile_check_adjoint(*program, precision == SDE_FP64, maxm, &err);
+    }
+    if (log && len > 0) {
+        strncpy(log, err.c_str(), (size_t)len - 1);
+        log[len - 1] = 0;
+    }
+    return rc;
+}
 
 extern "C" int32_t sde_jit_compile(const SdeUserProgram *program, int32_t precision, int32_t group_size,
                                    int32_t injected, int32_t jumps, char *log, int32_t len) {

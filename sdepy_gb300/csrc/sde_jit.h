@@ -14,6 +14,7 @@ bool jit_available();
 // compile (no load) the forward kernel of a program: the code generator and
 // NVRTC without a device
 int jit_compile_check(const SdeUserProgram &u, bool fp64, int maxm, bool inject, bool jumps, std::string *err);
+int jit_compile_check_adjoint(const SdeUserProgram &u, bool fp64, int maxm, std::string *err);
 
 // the forward kernel with the program's coefficients compiled in
 // (SDE_MODEL_USER_JIT, or SDE_MODEL_USER_SYS_JIT for systems), compiled on
@@ -21,5 +22,9 @@ int jit_compile_check(const SdeUserProgram &u, bool fp64, int maxm, bool inject,
 // an SDE_ERR_* status with a message in *err.
 int jit_fwd_kernel(const SdeUserProgram &u, bool fp64, int maxm, bool inject, bool jumps, cudaKernel_t *kernel,
                    int *bps, std::string *err);
+
+// the adjoint kernel of a single-equation program (dt / dw terms) with its
+// coefficients and their tangents compiled in (SDE_MODEL_USER_JIT)
+int jit_adj_kernel(const SdeUserProgram &u, bool fp64, int maxm, cudaKernel_t *kernel, int *bps, std::string *err);
 
 }  // namespace sdegpu

@@ -471,6 +471,9 @@ def test_jit_compiles_every_program():
         inj = (i // 4) % 2
         rc = lib.sde_jit_compile(C.byref(cls._program), prec, M, inj, jumps, buf, 1024)
         assert rc == 0, (name, prec, M, inj, buf.value.decode())
+        if not q and not jumps and i % 3 == 0:   # adjoint kernels of single equations
+            rc = lib.sde_jit_compile_adjoint(C.byref(cls._program), prec, M, buf, 1024)
+            assert rc == 0, (name, 'adjoint', prec, M, buf.value.decode())
 
 
 JIT_CASES = [
@@ -518,3 +521,16 @@ def test_gpu_jit_replays_reference(lib):
     for k, x in enumerate(_outputs(P(z['timeline']))):
         ref = z['xx%d' % k]
         assert np.max(np.abs(np.asarray(x) - ref)/np.maximum(np.abs(ref), 1.)) <= 1e-12
+
+
+@pytest.mark.gpu
+def test_gpu_jit_adjoint_equals_interpreter(lib):
+    """The compiled tangent-mode program gives the interpreted adjoint's
+    gradients (FP64, the same rounded operations) for a CEV and a mixed
+    SDE, with a mean and a call payoff."""
+    for spec, kw in (('integrate:user_cev', dict(x0=1., mu=.05, sigma=.3, gamma=.7)),
+                     ('integrate:user_mixed', dict(x0=.5, a=1.5, b=.7, s=.25))):
+        res = [_grads(user_class(sg, spec, jit=jit), [1.], **kw) for jit in (False, True)]
+        np.testing.assert_allclose(res[0][0], res[1][0], rtol=1e-13)
+        for n in kw:
+            assert abs(res[0][1][n] - res[1][1][n]) <= 1e-12*max(1., abs(res[0][1][n])), (spec, n)
