@@ -7,7 +7,9 @@ class, as sdepy does.  Here the function is traced once, at decoration, with
 symbolic values for t, x and the parameters: every arithmetic operation and
 numpy ufunc it applies is recorded, in Python's evaluation order, into a
 straight-line program (``SdeUserProgram`` of include/sdepy_gb300.h) that the
-device evaluates per state variable and step.  The Euler step then adds the
+device evaluates per state variable and step: interpreted, or compiled at
+run time into the forward and adjoint kernels (``jit``; NVRTC, once per
+process and program; FP64 results identical).  The Euler step then adds the
 terms in the order of the returned dict, as sdepy's ``euler_next`` does
 (sdepy/integration.py:707-718), so the FP64 result follows numpy's sequence
 of roundings.
@@ -26,7 +28,9 @@ expm1, log1p, arctan, square, absolute, negative; correlated Wiener
 increments through ``corr`` / ``rho``; the ``log`` flag; sources given as
 arguments (``dw=``, ``dn=``, ``dj=``), realised on the host and replayed.
 Control flow on the state (``if x > 0``, Python's ``max``), antithetic
-sources and other source ids are refused.
+sources and other source ids are refused.  Pathwise gradients
+(sdepy_gb300.autograd.expectation) are taken for single equations driven
+by 'dt' / 'dw'.
 """
 import ctypes as C
 import inspect
