@@ -534,3 +534,55 @@ def test_gpu_jit_adjoint_equals_interpreter(lib):
         np.testing.assert_allclose(res[0][0], res[1][0], rtol=1e-13)
         for n in kw:
             assert abs(res[0][1][n] - res[1][1][n]) <= 1e-12*max(1., abs(res[0][1][n])), (spec, n)
+
+
+# ---------------------------------------------------------------------------
+# distribution of the device jump draws (C oracle, which the kernels match
+# to 1e-12), and the host realisation order of given sources
+# ---------------------------------------------------------------------------
+def test_c_oracle_user_jump_distributions(clib):
+    """Over t in [0, 1] with lam = 3: a dn term counts Poisson(3) events; a
+    dj term sums norm(.5, .2) jumps (mean 1.5, variance 3 * .29); with both
+    terms the two processes are independent (variance 3 + .87, against
+    6.87 for one shared count); a time-dependent lam(t) = 2 + sin 3t is
+    taken at each step's midpoint (mean 2 + (1 - cos 3) / 3).  Means within
+    4 standard errors, variances within 5 %."""
+    paths, tl = 40000, (0., 1.)
+
+    def last(f, **kw):
+        cls = sg.integrate(f)
+        P = cls(paths=paths, steps=50, rng=sg.philox_rng(5, 9), x0=0., **kw)
+        return _spec_run(clib, P, tl, 5, 9)[-1].reshape(-1)
+
+    def check(x, mean, var):
+        assert abs(x.mean() - mean) <= 4*np.sqrt(var/paths), (x.mean(), mean)
+        assert abs(x.var()/var - 1) <= .05, (x.var(), var)
+
+    check(last(lambda t, x: {'dn': 1.}, lam=3.), 3., 3.)
+    check(last(lambda t, x: {'dj': 1.}, lam=3., y=sg.norm_rv(.5, .2)), 1.5, 3*.29)
+    check(last(lambda t, x: {'dn': 1., 'dj': 1.}, lam=3., y=sg.norm_rv(.5, .2)), 1.5 + 3., 3. + 3*.29)
+    from helpers import TDEP
+    m = 2 + (1 - np.cos(3.))/3
+    check(last(lambda t, x: {'dn': 1.}, lam=TDEP['tdep_lam']), m, m)
+
+
+def test_user_sources_realised_in_sdepy_order():
+    """Given sources are realised per step in ascending id order (dj, dn,
+    dw; sdepy/integration.py:1227-1234) and land in the injected arrays by
+    id."""
+    from sdepy_gb300.grid import Grid
+    calls = []
+
+    class Src:
+        def __init__(self, sid, paths, vshape, value):
+            self.sid, self.paths, self.vshape, self.value = sid, paths, vshape, value
+
+        def __call__(self, t, dt):
+            calls.append(self.sid)
+            return np.full(self.vshape + (self.paths,), self.value)
+    cls = user_class(sg, 'integrate:user_jumps4')
+    P = cls(paths=3, steps=4, dw=Src('dw', 3, (), .5), dn=Src('dn', 3, (), 2), dj=Src('dj', 3, (), -1.))
+    leg = Grid((0., 1.), 4).legs[0]
+    dw, dj, dn = P._realise(leg)
+    assert calls == ['dj', 'dn', 'dw']*leg.n_steps
+    assert (dw == .5).all() and (dj == -1.).all() and (dn == 2).all() and dn.dtype == np.int64
