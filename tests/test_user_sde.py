@@ -586,3 +586,28 @@ def test_user_sources_realised_in_sdepy_order():
     dw, dj, dn = P._realise(leg)
     assert calls == ['dj', 'dn', 'dw']*leg.n_steps
     assert (dw == .5).all() and (dj == -1.).all() and (dn == 2).all() and dn.dtype == np.int64
+
+
+def test_user_jump_host_tables():
+    """Per-state jump parameters (lam, a, b, pa broadcast over the working
+    shape), the intensity table at each step's midpoint for a callable lam,
+    the law id, and a system's term order (first appearance over the
+    equations)."""
+    from sdepy_gb300.grid import Grid
+    from helpers import TDEP
+    cls = user_class(sg, 'integrate:user_jumps4')
+    P = cls(paths=4, vshape=3, steps=8, lam=[[1.], [2.], [3.]], y=sg.double_exp_rv(a=[[.1], [.2], [.3]], b=.4, pa=.6))
+    assert P._jump_law_id == _lib.JUMP_DOUBLE_EXP
+    np.testing.assert_array_equal(P._jp, [[1., 2., 3.], [.1, .2, .3], [.4, .4, .4], [.6, .6, .6]])
+    assert P._lam_table(Grid((0., 1.), 8).legs[0]) is None
+    Pt = cls(paths=4, steps=8, lam=TDEP['tdep_lam'], y=sg.exp_rv(-.2))
+    leg = Grid((0., 1.), 8).legs[0]
+    tab = Pt._lam_table(leg)
+    mid = (leg.tt[:-1] + leg.tt[1:])/2
+    np.testing.assert_allclose(tab[:, 0], TDEP['tdep_lam'](mid), rtol=1e-15)
+    assert Pt._jp[0, 0] == 0. and Pt._jp[1, 0] == -.2   # lam from the table
+    sysc = user_class(sg, 'integrate_q2:user_sys_dn_dw')
+    assert [sysc._program.term_source[i] for i in range(sysc._program.n_terms)] == \
+        [_lib.SRC_DT, _lib.SRC_DN, _lib.SRC_DW]
+    with pytest.raises(TypeError):   # sdepy's keyword surface: no y without a dj term
+        user_class(sg, 'integrate_q2:user_sys_dn')(paths=4, x0=(0., 0.), y=sg.exp_rv(1.))
