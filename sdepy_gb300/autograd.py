@@ -30,7 +30,6 @@ import torch
 from . import _lib
 from .grid import Grid
 from .infrastructure import philox_rng
-from . import integration as I
 
 # (state index, gradient slot) per differentiable parameter; slot j + 1 is
 # parameter array p_j, slot 0 the initial state, slot 7 rho

@@ -12,7 +12,6 @@ FP32 states; the summary is the mean and standard deviation of X(T) of its
 first state variable and the pathwise derivatives of that mean.
 """
 import ctypes as C
-import time
 
 import numpy as np
 

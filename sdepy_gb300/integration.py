@@ -31,8 +31,8 @@ import numpy as np
 from . import _lib, _pinned
 from .grid import Grid
 from .infrastructure import (
-    process, philox_rng, draw_key, check_rng, get_corr_matrix, corr_of_t, law_of,
-    wiener_source, cpoisson_source, poisson_source, norm_rv, double_exp_rv,
+    process, draw_key, check_rng, get_corr_matrix, corr_of_t, law_of,
+    wiener_source, cpoisson_source, norm_rv, double_exp_rv,
     uniform_rv, _shape_setup, odd_wiener_source, even_cpoisson_source)
 from . import infrastructure as _inf
 

@@ -10,7 +10,6 @@ reference's, and its recorded ones at their printed precision, with the
 reference's own pass rule (at most 1.01 times the recorded error).
 """
 import glob
-import json
 import os
 
 import numpy as np
