@@ -60,6 +60,51 @@ def test_numpy_oracle_reproduces_quant_errors(path):
             np.testing.assert_allclose((m, M), z['file_err_' + name], rtol=1e-4)
 
 
+PDIST = sorted(__import__('glob').glob(os.path.join(GOLDEN, 'pdist2_*.npz')))
+
+
+@pytest.mark.parametrize('path', PDIST, ids=os.path.basename)
+def test_numpy_oracle_reproduces_params_distribution(path):
+    # sdepy/tests/test_quant.py params_case (:527-590): the cdf at the mean
+    # initial value and the characteristic function at u = 1 (of log x for
+    # the log forms) at t1 across each parameter sweep, including the
+    # Merton / Kou sweeps of sigma and lam.  The oracle's restated sources
+    # integrate to the reference's paths, and its cdf / chf restatements
+    # (oracle/process_post.py) give the reference's estimates and errors,
+    # and the errors recorded in sdepy/tests/cfr/params2_err_expected.txt
+    from oracle import process_post
+    z = np.load(path)
+    params = quant_params(z)
+    vshape = params.pop('vshape', ())
+    vshape = (vshape,) if isinstance(vshape, int) else tuple(vshape)
+    paths = int(z['paths'])
+    dw, dj = quant_sources(str(z['cls']), params, tuple(z['wshape']), paths, np.random.RandomState(1234))
+    dw = Recording(dw)
+    dj = None if dj is None else Recording(dj)
+    res, _ = euler.integrate(str(z['cls']), params, z['timeline'], paths=paths, vshape=vshape,
+                             steps=int(z['steps']), dw=dw, dj=dj)
+    calls = {'dw': dw.calls} if dj is None else {'dw': dw.calls, 'dj': dj.calls}
+    assert noise_digest(calls, tuple(z['wshape']), paths) == str(z['noise_sha256'])
+    x = res[0] if isinstance(res, tuple) else res
+    np.testing.assert_array_equal(x, z['xx'])
+    if x.ndim == 4:   # Heston's extra axis
+        x = x[:, :, 0, :]
+    t = z['timeline']
+    est = {}
+    if 'ref_cdf' in z.files:
+        est['cdf'] = process_post.cdf(t, x, t[-1], z['y'])
+    if 'ref_chf_re' in z.files:
+        c = process_post.chf(t, np.log(x) if int(z['log_chf']) else x, t[-1], z['u'])
+        est['chf_re'], est['chf_im'] = np.real(c), np.imag(c)
+    assert est
+    for name, v in est.items():
+        np.testing.assert_allclose(v, z['ref_' + name], rtol=1e-13, atol=1e-15)
+        d = np.abs(z['closed_' + name] - v)
+        np.testing.assert_allclose((d.mean(), d.max()), z['ref_err_' + name], rtol=1e-10)
+        if int(z['file_matches']):
+            np.testing.assert_allclose((d.mean(), d.max()), z['file_err_' + name], rtol=1e-4)
+
+
 def test_numpy_oracle_reproduces_blackscholes():
     # sdepy/tests/test_quant.py:593-640: call and put on 100_000 lognormal
     # paths from RandomState(1234), within 3 standard errors of bscall/bsput
