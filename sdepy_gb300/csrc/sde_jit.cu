@@ -8,8 +8,11 @@
 // kernel header, and the resulting cubin is loaded through the runtime's
 // library API.  The forward kernel instantiated with SDE_MODEL_USER_JIT /
 // SDE_MODEL_USER_SYS_JIT then evaluates the coefficients inline, with no
-// register file in local memory and no dispatch.  Kernels are cached per
-// (source, precision, group width, noise mode) for the life of the process.
+// register file in local memory and no dispatch; the adjoint kernel
+// (sde_adjoint.cuh, SDE_MODEL_USER_JIT) also gets the tangent-mode run
+// (UserJitTan<R>::tan).  Kernels are cached per generated source (program,
+// precision, group width, noise mode, forward or adjoint) for the life of
+// the process.
 //
 // NVRTC is loaded with dlopen: a library without it still runs the
 // interpreted kernels (SdeUserProgram.jit = 0).
