@@ -202,3 +202,36 @@ def test_synthetic_batch_workload():
     ou = [s for s in insts if s.model == OU]
     assert {s.nvars for s in ou} == {1, 2, 3, 4}
     assert all(s.nvars == 2 and -.9 <= s.rho <= -.5 for s in insts if s.model == HESTON)
+
+
+def test_host_sources_specific():
+    """The reference's test_source_specific (sdepy/tests/test_source.py:
+    234-270) on the host sources that feed injection: shapes, the
+    correlation / shape check, antithetic halves (opposite for dw, equal
+    for dn and dj) and odd path counts refused, a Poisson intensity that
+    does not broadcast refused, and compound Poisson sums of a constant law
+    equal to count x value."""
+    from numpy.testing import assert_allclose, assert_array_equal
+    from sdepy_gb300 import infrastructure as inf
+    rng = np.random.default_rng(3)
+    src = inf.wiener_source(vshape=3, paths=5, rng=rng)
+    assert src(0., 1.).shape == (3, 5)
+    with pytest.raises(ValueError):
+        inf.wiener_source(vshape=3, paths=10, corr=((1., .5), (.5, 1.)), rng=rng)(0., 1.)
+    for cls, sign in ((inf.odd_wiener_source, -1), (inf.even_poisson_source, 1),
+                      (inf.even_cpoisson_source, 1)):
+        s = cls(vshape=(2, 3), paths=10, rng=rng)(0., 1.)
+        assert_array_equal(s[..., :5], sign*s[..., 5:])
+        with pytest.raises(ValueError):
+            cls(paths=3, rng=rng)
+    with pytest.raises(ValueError):
+        inf.poisson_source(vshape=(3, 2), lam=(1., 2., 3.), rng=rng)
+    val = 2.
+
+    class const_rv:
+        def rvs(self, size, random_state=None):
+            return np.full(size, fill_value=val)
+    src = inf.cpoisson_source(lam=1., paths=100, ptype=np.int16, y=const_rv(), rng=rng)
+    for dt in (1., 100.):
+        s = src(0., dt)
+        assert_allclose(src.dn_value*val, s, rtol=np.finfo(float).eps)
