@@ -33,5 +33,9 @@ def load_c():
                                    C.c_int32, C.POINTER(C.c_int32),
                                    C.POINTER(C.c_int32), C.POINTER(C.c_int64)]
         lib.oracle_run.restype = C.c_int
+        lib.oracle_adjoint_user.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_int,
+                                            C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                            C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        lib.oracle_adjoint_user.restype = C.c_int
         _clib = lib
     return _clib

@@ -452,3 +452,195 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
     free(Lt);
     return rc;
 }
+
+/*
+ * Adjoint of a user SDE (single equation, dt / dw terms; sde_adjoint of
+ * include/sdepy_gb300.h): the gradient of
+ *   L = mean_paths sum_states f(X(T)),  f(X) = w0 X + sum_s w_s max(X - K_s, 0),
+ * X the stored output (the state, or its exp for SDE_OUT_EXP), with respect
+ * to x0 (slot 0 of each state) and the program's parameters p_j (slot
+ * 1 + j); grad is [groups*M][8], value = L.  Each path's states and Wiener
+ * increments are recomputed from the same counters as oracle_run, then
+ * x_bar is carried backwards: x_bar <- x_bar (1 + sum_i dA_i/dx dZ_i),
+ * g_j += x_bar sum_i dA_i/dp_j dZ_i.  The tangents of the program follow
+ * the chain rule per instruction: maximum / minimum / abs take the selected
+ * branch, sqrt has derivative 0 at 0, a ** b adds v log a only where a > 0.
+ * Returns 0, or -1 for another model or a bad argument.
+ */
+#define UTAN 7
+static void user_tan(const SdeUserProgram *u, double x, double t, const double *p, double A[SDE_USER_MAX_TERMS],
+                     double dA[SDE_USER_MAX_TERMS][UTAN]) {
+    double r[SDE_USER_MAX_REGS] = {0}, d[SDE_USER_MAX_REGS][UTAN];
+    memset(d, 0, sizeof d);
+    r[0] = x;
+    r[1] = t;
+    d[0][0] = 1.0;
+    for (int i = 0; i < 6; ++i) {
+        r[2 + i] = p[i];
+        d[2 + i][1 + i] = 1.0;
+    }
+    for (int i = 0; i < u->n_ops; ++i) {
+        const uint32_t op = u->ops[i];
+        const int c = op & 0xff, dst = (op >> 8) & 0xff, ia = (op >> 16) & 0xff, ib = op >> 24;
+        if (c == SDE_UOP_CONST) {
+            r[dst] = u->consts[ia];
+            for (int j = 0; j < UTAN; ++j) d[dst][j] = 0.0;
+            continue;
+        }
+        const double va = r[ia], vb = r[ib];
+        double v, da = 0.0, db = 0.0;
+        switch (c) {
+        case SDE_UOP_ADD: v = va + vb; da = 1.0; db = 1.0; break;
+        case SDE_UOP_SUB: v = va - vb; da = 1.0; db = -1.0; break;
+        case SDE_UOP_MUL: v = va * vb; da = vb; db = va; break;
+        case SDE_UOP_DIV: v = va / vb; da = 1.0 / vb; db = -v / vb; break;
+        case SDE_UOP_NEG: v = -va; da = -1.0; break;
+        case SDE_UOP_ABS: v = fabs(va); da = va < 0.0 ? -1.0 : 1.0; break;
+        case SDE_UOP_EXP: v = exp(va); da = v; break;
+        case SDE_UOP_LOG: v = log(va); da = 1.0 / va; break;
+        case SDE_UOP_SQRT: v = sqrt(va); da = v > 0.0 ? 0.5 / v : 0.0; break;
+        case SDE_UOP_MAX: v = np_maxd(va, vb); if (va >= vb) da = 1.0; else db = 1.0; break;
+        case SDE_UOP_MIN: v = np_mind(va, vb); if (va <= vb) da = 1.0; else db = 1.0; break;
+        case SDE_UOP_SIN: v = sin(va); da = cos(va); break;
+        case SDE_UOP_COS: v = cos(va); da = -sin(va); break;
+        case SDE_UOP_TAN: v = tan(va); da = 1.0 + v * v; break;
+        case SDE_UOP_TANH: v = tanh(va); da = 1.0 - v * v; break;
+        case SDE_UOP_POW:
+            v = pow(va, vb);
+            da = vb * pow(va, vb - 1.0);
+            db = va > 0.0 ? v * log(va) : 0.0;
+            break;
+        case SDE_UOP_EXPM1: v = expm1(va); da = v + 1.0; break;
+        case SDE_UOP_LOG1P: v = log1p(va); da = 1.0 / (1.0 + va); break;
+        case SDE_UOP_ARCTAN: v = atan(va); da = 1.0 / (1.0 + va * va); break;
+        default: v = va; da = 1.0;
+        }
+        double nd[UTAN];
+        for (int j = 0; j < UTAN; ++j) {
+            const double ta = d[ia][j], tb = d[ib][j];
+            double sj = ta != 0.0 ? da * ta : 0.0;
+            if (tb != 0.0 && db != 0.0) sj = sj + db * tb;
+            nd[j] = sj;
+        }
+        r[dst] = v;
+        for (int j = 0; j < UTAN; ++j) d[dst][j] = nd[j];
+    }
+    for (int i = 0; i < SDE_USER_MAX_TERMS; ++i) {
+        const int reg = i < u->n_terms ? u->term_register[0][i] : 0;
+        A[i] = i < u->n_terms ? r[reg] : 0.0;
+        for (int j = 0; j < UTAN; ++j) dA[i][j] = i < u->n_terms ? d[reg][j] : 0.0;
+    }
+}
+
+int oracle_adjoint_user(const SdeSpec *s, const SdeGrid *g, double mean_weight, int n_strikes,
+                        const double *strikes, const double *weights, double *grad, double *value) {
+    if (!s || !g || s->model != SDE_MODEL_USER || !s->program || s->program->n_eq != 1 || g->n_pts < 2 ||
+        n_strikes < 0 || n_strikes > SDE_MAX_STRIKES)
+        return -1;
+    const SdeUserProgram *u = s->program;
+    for (int i = 0; i < u->n_terms; ++i)
+        if (u->term_source[i] != SDE_SRC_DT && u->term_source[i] != SDE_SRC_DW) return -1;
+    const int M = s->group_size, G = s->groups, W = G * M;
+    const int64_t paths = s->paths;
+    const int n_steps = g->n_pts - 1;
+    double L[SDE_MAX_GROUP * SDE_MAX_GROUP];
+    if (s->corr && oracle_cholesky(s->corr, M, L)) return -1;
+    const uint32_t key[2] = {(uint32_t)s->seed, (uint32_t)(s->seed >> 32)};
+    double *xk = malloc(sizeof(double) * (size_t)(n_steps + 1) * M);
+    double *wk = malloc(sizeof(double) * (size_t)n_steps * M);
+    memset(grad, 0, sizeof(double) * (size_t)W * 8);
+    double val = 0.0;
+    const int P = (M + 1) / 2, NC = (2 * P + 3) / 4;
+    for (int64_t p = 0; p < paths; ++p) {
+        for (int gi = 0; gi < G; ++gi) {
+            double st[SDE_MAX_GROUP], z[SDE_MAX_GROUP + 1], pz0 = 0.0, pz1 = 0.0, pz[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int m = 0; m < M; ++m) st[m] = s->x0[gi * M + m];
+            /* forward: the states at each step's start and the increments,
+             * drawn as oracle_run draws them */
+            for (int k = 0; k < n_steps; ++k) {
+                const double dt = g->tt[k + 1] - g->tt[k], sq = sqrt(fabs(dt));
+                const uint32_t c1 = (uint32_t)k + g->step_offset;
+                uint32_t uw[4 * ((2 * SDE_MAX_GROUP + 3) / 4) + 4];
+                if (M == 1) {
+                    if ((k & 1) == 0) {
+                        const uint32_t ctr[4] = {(uint32_t)p, c1, (uint32_t)gi << 8, s->stream};
+                        uint32_t r[4];
+                        oracle_philox(ctr, key, r);
+                        oracle_normal2(r[0], r[1], &pz0, &pz1);
+                    }
+                    z[0] = (k & 1) ? pz1 : pz0;
+                } else if (M == 2) {
+                    if ((k & 1) == 0) {
+                        const uint32_t ctr[4] = {(uint32_t)p, c1, (uint32_t)gi << 8, s->stream};
+                        uint32_t r[4];
+                        oracle_philox(ctr, key, r);
+                        oracle_normal2(r[0], r[1], &pz[0], &pz[1]);
+                        oracle_normal2(r[2], r[3], &pz[2], &pz[3]);
+                    }
+                    z[0] = (k & 1) ? pz[2] : pz[0];
+                    z[1] = (k & 1) ? pz[3] : pz[1];
+                } else {
+                    for (int c = 0; c < NC; ++c) {
+                        const uint32_t ctr[4] = {(uint32_t)p, c1, ((uint32_t)gi << 8) | (uint32_t)c, s->stream};
+                        oracle_philox(ctr, key, &uw[4 * c]);
+                    }
+                    for (int q = 0; q < P; ++q) oracle_normal2(uw[2 * q], uw[2 * q + 1], &z[2 * q], &z[2 * q + 1]);
+                }
+                for (int m = 0; m < M; ++m) {
+                    double dWm;
+                    if (s->corr) {
+                        double acc = L[m * M + 0] * z[0];
+                        for (int j = 1; j <= m; ++j) acc = acc + L[m * M + j] * z[j];
+                        dWm = acc * sq;
+                    } else {
+                        dWm = z[m] * sq;
+                    }
+                    const int w = gi * M + m;
+                    double pv[6], A[SDE_USER_MAX_TERMS][SDE_USER_MAX_TERMS];
+                    for (int i = 0; i < 6; ++i) pv[i] = s->params[i * W + w];
+                    xk[(size_t)k * M + m] = st[m];
+                    wk[(size_t)k * M + m] = dWm;
+                    user_coefs(u, &st[m], g->tt[k], pv, A);
+                    double sum = 0.0;
+                    for (int i = 0; i < u->n_terms; ++i) {
+                        const double term = A[0][i] * (u->term_source[i] == SDE_SRC_DT ? dt : dWm);
+                        sum = i == 0 ? term : sum + term;
+                    }
+                    st[m] = st[m] + sum;
+                }
+            }
+            /* the functional and its derivative in the final states */
+            for (int m = 0; m < M; ++m) {
+                const int w = gi * M + m;
+                const double X = s->out_mode == SDE_OUT_EXP ? exp(st[m]) : st[m];
+                double f = mean_weight * X, fp = mean_weight;
+                for (int i = 0; i < n_strikes; ++i) {
+                    f += weights[i] * (X > strikes[i] ? X - strikes[i] : 0.0);
+                    if (X > strikes[i]) fp += weights[i];
+                }
+                val += f;
+                double xb = fp * (s->out_mode == SDE_OUT_EXP ? X : 1.0);
+                double pv[6];
+                for (int i = 0; i < 6; ++i) pv[i] = s->params[i * W + w];
+                for (int k = n_steps - 1; k >= 0; --k) {
+                    const double dt = g->tt[k + 1] - g->tt[k];
+                    double A[SDE_USER_MAX_TERMS], dA[SDE_USER_MAX_TERMS][UTAN], gx = 0.0, gp[6] = {0};
+                    user_tan(u, xk[(size_t)k * M + m], g->tt[k], pv, A, dA);
+                    for (int i = 0; i < u->n_terms; ++i) {
+                        const double dz = u->term_source[i] == SDE_SRC_DT ? dt : wk[(size_t)k * M + m];
+                        gx += dA[i][0] * dz;
+                        for (int j = 0; j < 6; ++j) gp[j] += dA[i][1 + j] * dz;
+                    }
+                    for (int j = 0; j < 6; ++j) grad[(size_t)w * 8 + 1 + j] += xb * gp[j];
+                    xb = xb * (1.0 + gx);
+                }
+                grad[(size_t)w * 8] += xb;
+            }
+        }
+    }
+    for (int i = 0; i < W * 8; ++i) grad[i] /= (double)paths;
+    if (value) *value = val / (double)paths;
+    free(xk);
+    free(wk);
+    return 0;
+}

@@ -611,3 +611,58 @@ def test_user_jump_host_tables():
         [_lib.SRC_DT, _lib.SRC_DN, _lib.SRC_DW]
     with pytest.raises(TypeError):   # sdepy's keyword surface: no y without a dj term
         user_class(sg, 'integrate_q2:user_sys_dn')(paths=4, x0=(0., 0.), y=sg.exp_rv(1.))
+
+
+def _c_adjoint(clib, P, tl, seed, stream, strikes=(), mean_weight=1.):
+    """The C oracle's user-SDE adjoint: (value, grad[W][8])."""
+    import ctypes as C
+    from sdepy_gb300.grid import Grid
+    leg = Grid(tl, P.steps).legs[-1]
+    g = _lib.SdeGrid()
+    g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
+    g.n_pts, g.step_offset = leg.tt.size, leg.step_offset
+    spec = P._make_spec(seed, stream)
+    K = np.array(list(strikes) + [0.], dtype=float)
+    w = np.ones(len(strikes) + 1)
+    grad = np.zeros((P._W, 8))
+    v = C.c_double()
+    rc = clib.oracle_adjoint_user(C.addressof(spec), C.addressof(g), mean_weight, len(strikes),
+                                  K.ctypes.data_as(C.POINTER(C.c_double)), w.ctypes.data_as(C.POINTER(C.c_double)),
+                                  grad.ctypes.data_as(C.POINTER(C.c_double)), C.byref(v))
+    assert rc == 0
+    return v.value, grad
+
+
+def test_c_oracle_user_adjoint_matches_finite_differences(clib):
+    """The C restatement of the user-SDE adjoint (oracle_adjoint_user: the
+    tangent rules of the device's user_coefs_tan) on its own paths: its
+    value is the mean of oracle_run's final states, and its gradients equal
+    central differences of that mean on common random numbers (h = 1e-5
+    relative) for a CEV SDE (maximum, ** with a parameter exponent), a
+    mixed SDE (sin(t), exp(-t), sqrt, tanh) and a log-space GBM (x0 through
+    exp), over groups of 1 and 4 states."""
+    tl = (0., 1.)
+    for spec, kw in (('integrate:user_cev', dict(x0=1., mu=.05, sigma=.2, gamma=.7)),
+                     ('integrate:user_mixed', dict(x0=.5, a=1.5, b=.7, s=.25)),
+                     ('integrate_log:user_gbm', dict(x0=1.1, mu=.05, sigma=.25))):
+        cls = user_class(sg, spec, jit=False)
+        for vshape in ((), (4,)):
+            def mean(**over):
+                P = cls(paths=3001, vshape=vshape, steps=40, rng=sg.philox_rng(12, 3), **dict(kw, **over))
+                x = np.asarray(P.exit(np.asarray(tl), _spec_run(clib, P, tl, 12, 3)))
+                return x[-1].mean(axis=-1).sum()
+            P = cls(paths=3001, vshape=vshape, steps=40, rng=sg.philox_rng(12, 3), **kw)
+            val, grad = _c_adjoint(clib, P, tl, 12, 3)
+            m0 = mean()
+            assert abs(val - m0) <= 1e-12*max(1., abs(m0)), (spec, vshape)
+            names = list(cls._pnames)
+            for n, base in kw.items():
+                h = 1e-5*max(abs(base), 1e-2)
+                fd = (mean(**{n: base + h}) - mean(**{n: base - h}))/(2*h)
+                if n == 'x0':
+                    g = grad[:, 0].sum()
+                    if 'log' in spec:
+                        g = g/base
+                else:
+                    g = grad[:, 1 + names.index(n)].sum()
+                assert abs(g - fd) <= 1e-6*max(1., abs(fd)), (spec, vshape, n, g, fd)
