@@ -25,6 +25,8 @@ def load_c():
         lib.oracle_normal2.argtypes = [C.c_uint32, C.c_uint32,
                                        C.POINTER(C.c_double), C.POINTER(C.c_double)]
         lib.oracle_normal2.restype = None
+        lib.oracle_normal2_libm.argtypes = lib.oracle_normal2.argtypes
+        lib.oracle_normal2_libm.restype = None
         lib.oracle_poisson.argtypes = [C.c_uint32, C.c_double, C.c_double]
         lib.oracle_poisson.restype = C.c_int
         lib.oracle_cholesky.argtypes = [C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_double)]

@@ -9,11 +9,12 @@ OUT = os.path.join(HERE, '_build')
 LIB = os.path.join(OUT, 'liboracle.so')
 SRC = os.path.join(HERE, 'rng_oracle.c')
 HDR = os.path.join(HERE, '..', 'include', 'sdepy_gb300.h')
+TAB = os.path.join(HERE, 'oracle_tables.h')
 
 
 def build(force=False):
     if not force and os.path.exists(LIB) and \
-       os.path.getmtime(LIB) >= max(os.path.getmtime(SRC), os.path.getmtime(HDR)):
+       os.path.getmtime(LIB) >= max(os.path.getmtime(p) for p in (SRC, HDR, TAB)):
         return LIB
     os.makedirs(OUT, exist_ok=True)
     cmd = ['gcc', '-O2', '-std=c11', '-D_DEFAULT_SOURCE', '-fPIC', '-shared',

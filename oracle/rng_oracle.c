@@ -6,7 +6,10 @@
  *   - Philox-4x32-10 (Salmon et al., SC'11: multipliers 0xD2511F53,
  *     0xCD9E8D57; Weyl increments 0x9E3779B9, 0xBB67AE85; 10 rounds);
  *   - uniforms u = (x + 0.5) 2^-32, Box-Muller normals
- *     r = sqrt(-2 log u(a)), v = (b >> 9) 2^-22 - 1, (r cos pi v, r sin pi v);
+ *     r = sqrt(-2 log u(a)), v = (b >> 9) 2^-22 - 1, (r cos pi v, r sin pi v),
+ *     with the logarithm and sin / cos of pi v evaluated by the table-driven
+ *     methods named at ln_u01 and sincospi_v (so the FP64 device transform,
+ *     which uses the same methods, matches bit for bit);
  *   - Poisson counts by CDF inversion of one uniform word;
  *   - jump sizes of the norm / double_exp / uniform / exp laws;
  *   - the Euler step in sdepy's operation order
@@ -35,6 +38,7 @@
 #include <string.h>
 
 #include "../include/sdepy_gb300.h"
+#include "oracle_tables.h"
 
 void oracle_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
     uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
@@ -57,13 +61,83 @@ void oracle_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]
 static double u01(uint32_t x) { return ((double)x + 0.5) * 0x1p-32; }
 static double vpm1(uint32_t b) { return (double)(b >> 9) * 0x1p-22 - 1.0; }
 
+/*
+ * ln u(a), u(a) = (a + 0.5) 2^-32 = (2a + 1) 2^-33, by Tang's table-driven
+ * method (ACM TOMS 15(2), 1989): 2a + 1 = 2^e m with m in [0.75, 1.5) taken
+ * from the integer's bits, m = c_j (1 + r) with c_j = 0.75 + j/128 the
+ * nearest table point, ln u = (e - 33) ln 2 + ln c_j + log1p(r), log1p by
+ * its Taylor series to r^7 evaluated with fused multiply-adds.  The tables
+ * (oracle_tables.h) are 50-digit mpmath values rounded once.
+ */
+static double ln_u01(uint32_t a) {
+    const uint64_t v = 2ull * a + 1ull;
+    const int lz = __builtin_clzll(v);
+    const int e = 63 - lz;
+    const uint64_t frac = ((v << lz) << 1) >> 12;   /* the 52 bits below the leading one */
+    const uint32_t fhi = (uint32_t)(frac >> 32);
+    const int upper = fhi >= 0x80000u;              /* 1.f >= 1.5: m = 1.f / 2 */
+    const int j = upper ? (int)((fhi + 0x2000u) >> 14) - 32 : (int)((fhi + 0x1000u) >> 13) + 32;
+    const int k = e - 33 + upper;
+    const uint64_t mbits = ((upper ? 1022ull : 1023ull) << 52) | frac;
+    double m;
+    memcpy(&m, &mbits, sizeof m);
+    const double d = m - ORC_LOG_C[j];
+    const double r = d * ORC_LOG_INVC[j];
+    const double r2 = r * r;
+    double q = 1.0 / 7.0;
+    q = fma(q, r, -1.0 / 6.0);
+    q = fma(q, r, 1.0 / 5.0);
+    q = fma(q, r, -0.25);
+    q = fma(q, r, 1.0 / 3.0);
+    q = fma(q, r, -0.5);
+    const double p = fma(q, r2, r);
+    return (ORC_KLN2_HI[k + 35] + ORC_LOG_LNC[j]) + (ORC_KLN2_LO[k + 35] + p);
+}
+
+/*
+ * sin(pi v), cos(pi v) for v = (b >> 9) 2^-22 - 1: v = n/64 + f, |f| <= 1/128,
+ * x = pi f, Taylor series of sin x to x^7 and cos x to x^6, and the angle
+ * addition formulas over the tabulated sin(pi n/64), cos(pi n/64).
+ */
+static void sincospi_v(uint32_t b, double *s, double *c) {
+    const int q = (int)(b >> 9);
+    const int nn = (q + 0x8000) >> 16;              /* n + 64 */
+    const int qd = q - (nn << 16);                  /* f = qd 2^-22 */
+    const double x = (double)qd * (0x1p-22 * ORC_PI_HI);
+    const double x2 = x * x;
+    double ps = -1.0 / 5040.0;
+    ps = fma(ps, x2, 1.0 / 120.0);
+    ps = fma(ps, x2, -1.0 / 6.0);
+    const double sx = fma(x * x2, ps, x);
+    double pc = -1.0 / 720.0;
+    pc = fma(pc, x2, 1.0 / 24.0);
+    pc = fma(pc, x2, -0.5);
+    const double cx = fma(x2, pc, 1.0);
+    const double S = ORC_SINPI_N[nn], C = ORC_COSPI_N[nn];
+    *s = fma(S, cx, C * sx);
+    *c = fma(C, cx, -(S * sx));
+}
+
+/* Box-Muller pair: r = sqrt(-2 ln u(a)), (r cos pi v, r sin pi v) */
 void oracle_normal2(uint32_t a, uint32_t b, double *z0, double *z1) {
+    const double r = sqrt(-2.0 * ln_u01(a));
+    double s, c;
+    sincospi_v(b, &s, &c);
+    *z0 = r * c;
+    *z1 = r * s;
+}
+
+/* the same pair by libm (log, cos, sin of the rounded angle pi v), kept to
+ * check the table-driven pair against */
+void oracle_normal2_libm(uint32_t a, uint32_t b, double *z0, double *z1) {
     const double r = sqrt(-2.0 * log(u01(a)));
-    const double v = vpm1(b);
-    const double th = M_PI * v;
+    const double th = M_PI * vpm1(b);
     *z0 = r * cos(th);
     *z1 = r * sin(th);
 }
+
+/* the unit exponential -ln u(a) */
+double oracle_expo(uint32_t a) { return -ln_u01(a); }
 
 /* smallest k with u(word) <= F(k), F the Poisson(lam) CDF, p0 = exp(-lam) */
 int oracle_poisson(uint32_t word, double p0, double lam) {
@@ -152,14 +226,14 @@ static double jump_size(int law, const uint32_t r[4], double a, double b, double
         oracle_normal2(r[0], r[1], &z0, &z1);
         return a + b * z0;
     case SDE_JUMP_DOUBLE_EXP: {
-        const double e = -log(u01(r[0]));
+        const double e = oracle_expo(r[0]);
         const double us = u01(r[2]);
         return (us <= pa) ? a * e : -(b * e);
     }
     case SDE_JUMP_UNIFORM:
         return a + (b - a) * u01(r[2]);
     case SDE_JUMP_EXP:
-        return a * (-log(u01(r[0])));
+        return a * oracle_expo(r[0]);
     }
     return 0.0;
 }

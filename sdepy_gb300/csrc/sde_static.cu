@@ -19,7 +19,10 @@
 //     in the 16 MiB array; larger requests fail with SDE_ERR_INVALID;
 //   * the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (with that device current) -- make that first
-//     call before any stream capture;
+//     call before any stream capture.  The address is kept for the life of
+//     the process: do not call this entry again on a device after
+//     cudaDeviceReset (the reset unloads the module, and a reloaded array
+//     may sit elsewhere);
 //   * calls share the array, which keeps the last call's contents: the
 //     counters are cleared at the start of every call, and calls that
 //     overlap on the GPU would race (calls from different host threads are
@@ -130,6 +133,9 @@ int run_static(const SdeSpec *s, const SdeGrid *gr, const SdeStatsReq *req, SdeS
     if ((s->out_mode == SDE_OUT_HESTON_X || s->out_mode == SDE_OUT_HESTON_XY) && s->model != SDE_MODEL_HESTON)
         return fail_static(SDE_ERR_INVALID, "Heston outputs need the Heston model");
     if (!gr->tt || !gr->out_row || gr->n_pts < 1) return fail_static(SDE_ERR_INVALID, "grid arrays are required");
+    // a negative row would match the grid's unstored points (out_row -1)
+    // and summarise nothing
+    if (req->row < 0) return fail_static(SDE_ERR_INVALID, "stats row must be >= 0");
     bool row_seen = false;
     for (int k = 0; k < gr->n_pts; ++k) {
         if (!std::isfinite(gr->tt[k])) return fail_static(SDE_ERR_INVALID, "grid point %d is not finite", k);
@@ -152,6 +158,14 @@ int run_static(const SdeSpec *s, const SdeGrid *gr, const SdeStatsReq *req, SdeS
     if (req->n_strikes > 0 && !so->payoff) return fail_static(SDE_ERR_INVALID, "payoff array is required");
     if (req->has_range && !(std::isfinite(req->range_lo) && std::isfinite(req->range_hi) && req->range_lo <= req->range_hi))
         return fail_static(SDE_ERR_INVALID, "histogram range must be finite with min <= max");
+    // the correlation factor, before anything is queued on the stream: a
+    // failure below the first enqueue would leave work writing the shared
+    // array after this call (and its lock) had returned
+    double Lc[SDE_MAX_GROUP * SDE_MAX_GROUP];
+    if (s->corr) {
+        const int rc = sde_cholesky(s->corr, M, Lc);
+        if (rc) return rc;
+    }
 
     // ---- device and the array's address ------------------------------------------------
     int dev = 0;
@@ -235,9 +249,6 @@ int run_static(const SdeSpec *s, const SdeGrid *gr, const SdeStatsReq *req, SdeS
     FwdArgs<R> a;
     memset(&a, 0, sizeof a);
     if (s->corr) {
-        double Lc[SDE_MAX_GROUP * SDE_MAX_GROUP];
-        const int rc = sde_cholesky(s->corr, M, Lc);
-        if (rc) return rc;
         for (int i = 0; i < M; ++i)
             for (int j = 0; j <= i; ++j) a.chol[i * (i + 1) / 2 + j] = (R)Lc[i * M + j];
         a.has_corr = 1;

@@ -530,28 +530,36 @@ class wiener_source(source):
                     .format(self.vshape, corr.shape))
 
     def __call__(self, t, dt):
-        paths, vshape, dtype = self.paths, self.vshape, self.dtype
+        # numpy draws in the order sdepy's source makes them, so that an
+        # identically seeded generator yields identical increments
         t, dt = np.broadcast_arrays(t, dt)
-        tshape = dt.shape
+        steps = dt.shape
+        inner = self.vshape + (self.paths,)
         if self.corr is None:
-            dz = self.rng.normal(0., 1., size=tshape + vshape + (paths,)
-                                 ).astype(dtype, copy=False)
-        elif not callable(self.corr):
-            M = vshape[-1]
-            dz = self.rng.multivariate_normal(
-                mean=np.zeros(M), cov=self.corr,
-                size=tshape + vshape[:-1] + (paths,)).astype(dtype, copy=False)
-            dz = dz.swapaxes(-1, -2)
-        else:   # corr(t + dt/2), one draw per time point
-            M = vshape[-1]
-            dz = np.empty(tshape + vshape[:-1] + (paths, M), dtype=dtype)
-            for i in np.ndindex(tshape):
-                dz[i] = self.rng.multivariate_normal(
-                    mean=np.zeros(M), cov=self.corr(t[i] + dt[i]/2), size=vshape[:-1] + (paths,))
-            dz = dz.swapaxes(-1, -2)
-        dt = dt.reshape(tshape + (1,)*len(vshape) + (1,))
-        dz *= np.sqrt(np.abs(dt))
-        return dz
+            draws = self.rng.normal(0., 1., size=steps + inner)
+        else:
+            draws = self._correlated(t, dt, steps)
+        draws = draws.astype(self.dtype, copy=False)
+        draws *= np.sqrt(np.abs(dt)).reshape(steps + (1,)*len(inner))
+        return draws
+
+    def _correlated(self, t, dt, steps):
+        """Draws correlated along the last vshape axis: one
+        multivariate_normal call for a constant matrix, one per step for
+        corr(t + dt/2).  numpy puts the correlated axis last; it is moved
+        in front of the paths axis."""
+        width = self.vshape[-1]
+        batch = self.vshape[:-1] + (self.paths,)
+        zero = np.zeros(width)
+        if callable(self.corr):
+            per_step = [self.rng.multivariate_normal(
+                mean=zero, cov=self.corr(t[i] + dt[i]/2), size=batch)
+                for i in np.ndindex(steps)]
+            out = np.asarray(per_step).reshape(steps + batch + (width,))
+        else:
+            out = self.rng.multivariate_normal(mean=zero, cov=self.corr,
+                                               size=steps + batch)
+        return np.moveaxis(out, -1, -2)
 
 
 def _test_shape(f):
@@ -584,14 +592,16 @@ class poisson_source(source):
                 .format(self.lam.shape, self.vshape + (paths,)))
 
     def __call__(self, t, dt):
+        # one poisson call per step at the step's mid-point intensity, in
+        # sdepy's order; a backward step counts negative events
         t, dt = np.broadcast_arrays(t, dt)
-        abs_dt, sign_dt = np.abs(dt), np.sign(dt).astype(int)
-        tshape = dt.shape
-        dn = np.empty(tshape + self.vshape + (self.paths,), dtype=self.dtype)
-        for i in np.ndindex(tshape):
-            L = self.lam(t[i] + dt[i]/2) if callable(self.lam) else self.lam
-            dn[i] = sign_dt[i]*self.rng.poisson(abs_dt[i]*L, self.vshape + (self.paths,))
-        return dn
+        inner = self.vshape + (self.paths,)
+        counts = np.empty(dt.shape + inner, dtype=self.dtype)
+        for i in np.ndindex(dt.shape):
+            lam = self.lam(t[i] + dt[i]/2) if callable(self.lam) else self.lam
+            n = self.rng.poisson(np.abs(dt[i])*lam, inner)
+            counts[i] = n if dt[i] >= 0 else -n
+        return counts
 
 
 class cpoisson_source(source):
@@ -614,26 +624,26 @@ class cpoisson_source(source):
         self.y = uniform_rv(a=0, b=1) if y is None else y
 
     def __call__(self, t, dt):
+        # for each step, the paths with exactly n events (n = 1, 2, ...)
+        # get the sum of n draws of y, made by one rvs call of shape
+        # (such paths, n): sdepy's draw order, so that replays match
         t, dt = np.broadcast_arrays(t, dt)
-        sign_dt = np.sign(dt).astype(int)
-        shape = self.vshape + (self.paths,)
-        dn = self.dn(t, dt)
-        dz = np.zeros(dt.shape + shape, dtype=self.dtype)
-        y_value = []
+        counts = self.dn(t, dt)
+        sums = np.zeros(dt.shape + self.vshape + (self.paths,), dtype=self.dtype)
+        draws = []
         for i in np.ndindex(dt.shape):
-            dn_positive_i = sign_dt[i]*dn[i]
-            nmax = dn_positive_i.max()
-            rv = self.y(t[i] + dt[i]/2) if callable(self.y) else self.y
-            for j in range(1, nmax + 1):
-                index = (dn_positive_i == j)
-                if index.any():
-                    y_sample = rv.rvs(size=(index.sum(), j),
-                                      random_state=self.rng)
-                    dz[i][index] = sign_dt[i]*y_sample.sum(axis=-1)
-                    y_value.append(y_sample)
-        self.dn_value = dn
-        self.y_value = y_value
-        return dz
+            sgn = int(np.sign(dt[i]))
+            events = sgn*counts[i]
+            law = self.y(t[i] + dt[i]/2) if callable(self.y) else self.y
+            for n in range(1, events.max() + 1):
+                hit = events == n
+                if not hit.any():
+                    continue
+                y = law.rvs(size=(int(hit.sum()), n), random_state=self.rng)
+                sums[i][hit] = sgn*y.sum(axis=-1)
+                draws.append(y)
+        self.dn_value, self.y_value = counts, draws
+        return sums
 
 
 # ---------------------------------------------------------------------------

@@ -2,11 +2,12 @@
 
 Run in a container where the reference is importable:
 
-    python tests/golden/make_golden.py [REFERENCE_DIR [GROUP ...]]
+    python tests/golden/make_golden.py REFERENCE_DIR [GROUP ...]
 
 (groups path, mc, tdep, cir, corr_t, user, user_jump; all by default)
 
-REFERENCE_DIR defaults to /root/reference (the read-only sdepy checkout).
+REFERENCE_DIR (or $SDEPY_REFERENCE) is the sdepy checkout to run; it is
+required.
 Nothing under tests/ imports this script; the tests only read the .npz files
 it writes, so the fixtures travel to machines without the reference.
 
@@ -26,6 +27,7 @@ import os
 import sys
 
 import numpy as np
+from refdir import reference_dir
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -433,8 +435,8 @@ def user_jump_cases(sdepy):
 
 
 def main():
-    # python make_golden.py [REFERENCE_DIR [GROUP ...]], groups path, mc, tdep, cir, corr_t, user, user_jump
-    ref = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+    # python make_golden.py REFERENCE_DIR [GROUP ...], groups path, mc, tdep, cir, corr_t, user, user_jump
+    ref = reference_dir()
     groups = sys.argv[2:] or ['path', 'mc', 'tdep', 'cir', 'corr_t', 'user', 'user_jump']
     sys.path.insert(0, ref)
     import sdepy

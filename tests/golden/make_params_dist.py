@@ -14,7 +14,7 @@ to the same paths (make_quant.check_restated), and stores the paths, y, u,
 the reference's estimates, the closed forms, the errors realised here and
 the recorded ones.
 
-    python tests/golden/make_params_dist.py [REFERENCE_DIR]
+    python tests/golden/make_params_dist.py REFERENCE_DIR
 """
 import json
 import os
@@ -25,6 +25,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 import make_quant as MQ   # noqa: E402  (sets up the paths of tests/ and the oracle)
+from refdir import reference_dir
 
 K = 20
 # id -> (cdf form, chf form) of params_case (sdepy/tests/test_quant.py:431-450)
@@ -124,4 +125,4 @@ def main(ref_dir):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+    main(reference_dir())

@@ -16,12 +16,13 @@ stored with the fixture.
 
 Run where the reference is importable:
 
-    python tests/golden/make_process_post.py [REFERENCE_DIR]
+    python tests/golden/make_process_post.py REFERENCE_DIR
 """
 import os
 import sys
 
 import numpy as np
+from refdir import reference_dir
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -104,7 +105,7 @@ def run(sdepy, name, c):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+    ref = reference_dir()
     sys.path.insert(0, ref)
     import sdepy
     for name, c in cases().items():

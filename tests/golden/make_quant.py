@@ -12,7 +12,7 @@ reference's quantitative tests (sdepy/tests/test_quant.py):
 
 Run where the reference is importable:
 
-    python tests/golden/make_quant.py [REFERENCE_DIR [CASE_ID ...]]
+    python tests/golden/make_quant.py REFERENCE_DIR [CASE_ID ...]
 
 The reference's tests seed numpy's legacy generator (RandomState(1234),
 sdepy/tests/shared.py:169,199-219) before each case and fail when a realised
@@ -47,6 +47,7 @@ sys.path.insert(0, HERE)
 sys.path.insert(0, os.path.dirname(HERE))                     # tests/helpers.py
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))    # the oracle
 from make_golden import Recorder  # noqa: E402
+from refdir import reference_dir
 
 LEGACY_SEED = 1234
 STORE_PATHS_MAX = 1000   # larger cases keep per-point statistics, not paths
@@ -289,5 +290,5 @@ def main(ref_dir, ids=()):
 
 
 if __name__ == '__main__':
-    # python make_quant.py [REFERENCE_DIR [CASE_ID ...]]
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference', tuple(sys.argv[2:]))
+    # python make_quant.py REFERENCE_DIR [CASE_ID ...]
+    main(reference_dir(), tuple(sys.argv[2:]))

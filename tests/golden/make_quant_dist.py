@@ -17,7 +17,7 @@ oracle's restated sources reproduce every batch's draws (SHA-256, as
 make_quant.py), and stores the reference's estimates, the closed forms,
 the errors realised here and the recorded ones.
 
-    python tests/golden/make_quant_dist.py [REFERENCE_DIR]
+    python tests/golden/make_quant_dist.py REFERENCE_DIR
 """
 import json
 import os
@@ -28,6 +28,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 import make_quant as MQ   # noqa: E402  (sets up the paths of tests/ and the oracle)
+from refdir import reference_dir
 
 # id -> (closed-form pdf, cdf, chf names; pdf / chf of log x)
 FORMS = {
@@ -133,4 +134,4 @@ def main(ref_dir):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+    main(reference_dir())

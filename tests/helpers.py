@@ -43,6 +43,28 @@ def oracle_paths(clib, proc, timeline, seed, stream=0):
     return xx.reshape((rows,) + tuple(proc.xshape) + (proc.paths,)), info
 
 
+def relerr(got, ref, floor=1e-3):
+    """Largest error of ``got`` against ``ref`` relative to each value, with
+    each variable's scale floor at ``floor`` times that variable's largest
+    magnitude (so that values crossing zero are not divided by ~0).  Arrays
+    are process layouts (timeline,) + vshape + (paths,): a variable is one
+    index of the middle axes, its values span the timeline and the paths."""
+    got, ref = np.asarray(got, float), np.asarray(ref, float)
+    if not ref.size:
+        return 0.0
+    assert got.shape == ref.shape, (got.shape, ref.shape)
+    mag = np.abs(ref)
+    axes = (0, ref.ndim - 1) if ref.ndim >= 2 else (0,)
+    vmax = np.nanmax(mag, axis=axes, keepdims=True)
+    scale = np.maximum(mag, floor*vmax)
+    d = np.abs(got - ref)
+    # exact agreement (zero error, NaN in both) needs no scale
+    both_nan = np.isnan(got) & np.isnan(ref)
+    r = np.where(d == 0, 0.0, d/np.where(scale > 0, scale, 1.0))
+    r = np.where(both_nan, 0.0, r)
+    return float(np.max(r))
+
+
 # ---------------------------------------------------------------------------
 # the reference's quantitative tests (sdepy/tests/test_quant.py, contexts
 # 'quant2' and 'params2'; fixtures from tests/golden/make_quant.py)

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import sdepy_gb300 as sg
-from helpers import TDEP, oracle_paths
+from helpers import TDEP, oracle_paths, relerr
 
 pytestmark = pytest.mark.gpu
 
@@ -68,7 +68,7 @@ def test_antithetic_matches_c_oracle(lib, clib, case):
                           (out if isinstance(out, tuple) else (out,))], axis=1)
     ref, info = oracle_paths(clib, P, tl, seed, 5)
     ref = ref.reshape(got.shape)
-    err = np.max(np.abs(got - ref)/np.maximum(np.abs(ref), 1.))
+    err = relerr(got, ref)
     assert err <= 1e-12, err
     if 'jump_count' in P.info:
         jc = P.info['jump_count'].reshape(-1, paths)

@@ -2,7 +2,8 @@
 
 * Injected noise: the increments the reference consumed (recorded in
   tests/golden by running sdepy) are replayed through the drop-in classes;
-  FP64 paths must match the reference's to 1e-12 relative, with Poisson
+  FP64 paths must match the reference's to 1e-12 relative (each value's
+  scale floored at 1e-3 of its variable's largest magnitude), with Poisson
   counts, jump rates and negative-variance counts exact.
 * Device RNG: the FP64 kernel must match the C oracle (same Philox
   counters) to 1e-12 relative per path, integer counts bit-exact; the FP32
@@ -16,7 +17,7 @@ import pytest
 
 import sdepy_gb300 as sg
 from conftest import golden_cases
-from helpers import oracle_paths
+from helpers import oracle_paths, relerr
 from oracle.euler import Replay, shapes
 
 pytestmark = pytest.mark.gpu
@@ -33,6 +34,7 @@ def _kwargs(z):
 
 
 def _relerr(a, b):
+    """FP32-vs-FP64 error: relative to each value, absolute below 1."""
     a, b = np.asarray(a, float), np.asarray(b, float)
     scale = np.maximum(np.abs(b), 1.0)
     return float(np.max(np.abs(a - b)/scale)) if a.size else 0.0
@@ -62,7 +64,7 @@ def test_injected_noise_matches_reference(lib, path):
         ref = z['xx%d' % k]
         assert o.shape == ref.shape
         np.testing.assert_array_equal(o.t, z['t%d' % k])
-        assert _relerr(o, ref) <= RTOL64, _relerr(o, ref)
+        assert relerr(o, ref) <= RTOL64, relerr(o, ref)
     assert P.info['computed_steps'] == int(z['computed_steps'])
     assert P.info['stored_steps'] == int(z['stored_steps'])
     if 'jump_count' in z:
@@ -111,7 +113,7 @@ def test_device_rng_fp64_matches_c_oracle(lib, clib, case):
     ref, info = oracle_paths(clib, P, timeline, seed, 7)
     ref = ref.reshape(got.shape[0], -1, paths)
     assert np.isfinite(got).all()
-    err = _relerr(got, ref)
+    err = relerr(got, ref)
     assert err <= RTOL64, err
     if 'negative_y_count' in P.info:
         np.testing.assert_array_equal(P.info['negative_y_count'].reshape(-1, paths), info['neg'])

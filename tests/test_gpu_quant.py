@@ -23,7 +23,7 @@ import pytest
 
 import sdepy_gb300 as sg
 from conftest import GOLDEN, quant_cases
-from helpers import quant_kwargs, quant_sources, quant_stats_errors
+from helpers import quant_kwargs, quant_sources, quant_stats_errors, relerr
 
 pytestmark = pytest.mark.gpu
 
@@ -38,7 +38,7 @@ def test_quant_errors_reproduced(lib, path):
     if 'xx' in z:
         ref = z['xx']
         assert x.shape == ref.shape
-        assert np.max(np.abs(np.asarray(x) - ref)/np.maximum(np.abs(ref), 1.)) <= 1e-12
+        assert relerr(x, ref) <= 1e-12
     for name, (m, M, real) in quant_stats_errors(x, z).items():
         np.testing.assert_allclose(real, z['ref_stat_' + name], rtol=1e-11)
         np.testing.assert_allclose((m, M), z['ref_err_' + name], rtol=1e-9)

@@ -180,6 +180,53 @@ def test_c_oracle_normals(clib):
     assert abs(zs.var() - 1) < 4*np.sqrt(2/n)
 
 
+def _header_tables(path, prefix):
+    import re
+    text = open(path).read()
+    out = {}
+    for m in re.finditer(r'(%s[A-Z0-9_]+)\[\d+\] = \{(.*?)\};' % prefix, text, re.S):
+        out[m.group(1)[len(prefix):]] = [float(x) for x in m.group(2).split(',') if x.strip()]
+    for m in re.finditer(r'(%s[A-Z0-9_]+) = ([-0-9.e+]+);' % prefix, text):
+        out[m.group(1)[len(prefix):]] = float(m.group(2))
+    return out
+
+
+def test_fp64_transform_tables_agree():
+    """The oracle's tables (mpmath, oracle/make_tables.py) and the library's
+    (decimal series, csrc/make_fp64_tables.py) are computed independently;
+    entry for entry they are the same doubles, and the oracle's header is
+    what its generator writes."""
+    here = os.path.dirname(os.path.abspath(__file__))
+    orc = _header_tables(os.path.join(here, '..', 'oracle', 'oracle_tables.h'), 'ORC_')
+    lib = _header_tables(os.path.join(here, '..', 'sdepy_gb300', 'csrc', 'fp64_tables.h'), 'F64_')
+    assert set(orc) <= set(lib) and len(orc) == 8
+    for k, v in orc.items():
+        assert np.array_equal(np.asarray(v), np.asarray(lib[k])), k
+    pytest.importorskip('mpmath')
+    from oracle import make_tables
+    for k, v in make_tables.tables().items():
+        assert np.array_equal(np.asarray(v), np.asarray(orc[k[4:]])), k
+
+
+def test_c_oracle_table_normals_vs_libm(clib):
+    """The table-driven pair is within a few ulp of libm's log / cos / sin on
+    the extreme and boundary words and on random ones."""
+    rng = np.random.default_rng(8)
+    edge = np.array([0, 1, 2, 2**31 - 1, 2**31, 2**32 - 2, 2**32 - 1], dtype=np.uint64)
+    bedge = np.array([0, 511, 512, 2**31 - 512, 2**31, 2**31 + 511, 2**32 - 1,
+                      (2**23 + 2**15) << 9, (2**22 - 2**15) << 9], dtype=np.uint64)
+    a = np.concatenate([np.repeat(edge, bedge.size), rng.integers(0, 2**32, 20000, dtype=np.uint64)])
+    b = np.concatenate([np.tile(bedge, edge.size), rng.integers(0, 2**32, 20000, dtype=np.uint64)])
+    t0, t1, l0, l1 = (C.c_double() for _ in range(4))
+    worst = 0.
+    for x, y in zip(a, b):
+        clib.oracle_normal2(int(x), int(y), C.byref(t0), C.byref(t1))
+        clib.oracle_normal2_libm(int(x), int(y), C.byref(l0), C.byref(l1))
+        r = np.hypot(l0.value, l1.value)
+        worst = max(worst, abs(t0.value - l0.value)/r, abs(t1.value - l1.value)/r)
+    assert worst < 4e-15, worst
+
+
 def test_c_oracle_cholesky(clib):
     A = np.random.default_rng(7).normal(size=(8, 8))
     Cm = A @ A.T + .1*np.eye(8)

@@ -19,7 +19,7 @@ import pytest
 
 import sdepy_gb300 as sg
 from conftest import tdep_cases
-from helpers import TDEP, oracle_paths, tdep_kwargs
+from helpers import TDEP, oracle_paths, relerr, tdep_kwargs
 from oracle import euler
 
 
@@ -70,7 +70,7 @@ def test_gpu_replay_matches_reference_tdep(lib, path):
     outs = out if isinstance(out, tuple) else (out,)
     for k, o in enumerate(outs):
         ref = z['xx%d' % k]
-        err = np.max(np.abs(np.asarray(o) - ref)/np.maximum(np.abs(ref), 1.))
+        err = relerr(o, ref)
         assert err <= 1e-12, err
     assert P.info['computed_steps'] == int(z['computed_steps'])
 
@@ -121,7 +121,7 @@ def test_device_rng_tdep_matches_c_oracle(lib, clib, case):
                           (out if isinstance(out, tuple) else (out,))], axis=1)
     ref, info = oracle_paths(clib, P, tl, seed, 3)
     ref = ref.reshape(got.shape)
-    err = np.max(np.abs(got - ref)/np.maximum(np.abs(ref), 1.))
+    err = relerr(got, ref)
     assert err <= 1e-12, err
     if 'jump_count' in P.info:
         np.testing.assert_array_equal(P.info['jump_count'].reshape(-1, paths), info['jump_count'])

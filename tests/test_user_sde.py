@@ -27,7 +27,7 @@ import pytest
 import sdepy_gb300 as sg
 from sdepy_gb300 import _lib
 from conftest import GOLDEN
-from helpers import USER, oracle_paths, tdep_kwargs, user_class, user_sources
+from helpers import USER, oracle_paths, relerr, tdep_kwargs, user_class, user_sources
 from oracle import euler
 
 CASES = sorted(glob.glob(os.path.join(GOLDEN, 'user_*.npz')))
@@ -169,7 +169,7 @@ def test_gpu_replay_matches_reference(lib, path):
     for k, x in enumerate(outs):
         ref = z['xx%d' % k]
         assert x.shape == ref.shape
-        err = np.max(np.abs(np.asarray(x) - ref)/np.maximum(np.abs(ref), 1.))
+        err = relerr(x, ref)
         assert err <= 1e-12, err
     assert P.info['computed_steps'] == int(z['computed_steps'])
 
@@ -207,7 +207,7 @@ def test_device_rng_matches_c_oracle(lib, clib, case):
     ref, _ = oracle_paths(clib, P, tl, seed, 2)
     refs = _outputs(P.exit(np.asarray(tl), ref))   # the oracle's working-shape rows, unpacked alike
     for x, r in zip(outs, refs):
-        err = np.max(np.abs(np.asarray(x) - np.asarray(r))/np.maximum(np.abs(r), 1.))
+        err = relerr(x, r)
         assert err <= 1e-12, err
     P32 = cls(paths=paths, steps=steps, i0=i0, dtype=np.float32, rng=sg.philox_rng(seed, 2), **kw)
     for x, r in zip(_outputs(P32(tl)), refs):
@@ -409,7 +409,7 @@ def test_gpu_replay_matches_reference_jumps(lib, path):
     for k, x in enumerate(outs):
         ref = z['xx%d' % k]
         assert x.shape == ref.shape
-        err = np.max(np.abs(np.asarray(x) - ref)/np.maximum(np.abs(ref), 1.))
+        err = relerr(x, ref)
         assert err <= 1e-12, err
 
 
@@ -423,7 +423,7 @@ def test_device_rng_jumps_match_c_oracle(lib, clib, case):
     outs = _outputs(P(tl))
     refs = _outputs(P.exit(np.asarray(tl), _spec_run(clib, P, tl, seed, 5)))
     for x, r in zip(outs, refs):
-        err = np.max(np.abs(np.asarray(x) - np.asarray(r))/np.maximum(np.abs(r), 1.))
+        err = relerr(x, r)
         assert err <= 1e-12, err
     P32 = cls(paths=paths, steps=steps, i0=i0, dtype=np.float32, rng=sg.philox_rng(seed, 5), **_jkw(kw))
     for x, r in zip(_outputs(P32(tl)), refs):
@@ -520,7 +520,7 @@ def test_gpu_jit_replays_reference(lib):
             **_jump_replays(z, paths), **kw)
     for k, x in enumerate(_outputs(P(z['timeline']))):
         ref = z['xx%d' % k]
-        assert np.max(np.abs(np.asarray(x) - ref)/np.maximum(np.abs(ref), 1.)) <= 1e-12
+        assert relerr(x, ref) <= 1e-12
 
 
 @pytest.mark.gpu
