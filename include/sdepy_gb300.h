@@ -39,7 +39,7 @@ extern "C" {
 #define SDE_API
 #endif
 
-#define SDE_ABI_VERSION 4
+#define SDE_ABI_VERSION 5
 
 #define SDE_MAX_GROUP   16   /* largest correlated group (state vars) */
 #define SDE_MAX_PARAMS  6    /* coefficient arrays per state variable */
@@ -164,7 +164,11 @@ typedef struct SdeSpec {
     const double *corr;    /* [M*M] correlation matrix shared by all groups, or NULL */
     uint64_t seed;         /* Philox-4x32-10 key */
     uint32_t stream;       /* Philox counter word 3 (call / instance id) */
-    uint32_t reserved1;
+    /* Added to the local path index in Philox counter word 0: the call
+     * integrates paths [path_offset, path_offset + paths) of a larger sample
+     * (path_offset + paths <= 2^32), so that contiguous path ranges run on
+     * different devices or calls reproduce one run of all the paths. */
+    uint32_t path_offset;
     const SdeUserProgram *program;   /* SDE_MODEL_USER: the coefficients, else NULL */
 } SdeSpec;
 

@@ -294,7 +294,7 @@ int oracle_run(const SdeSpec *s, const SdeGrid *g, double *xx, int32_t n_rows,
     const int anti = (s->flags & SDE_FLAG_ANTITHETIC) != 0;
     for (int64_t p = 0; p < paths && !rc; ++p) {
         /* the counters' path word, and the sign of the normals */
-        const int64_t pc = (anti && p >= paths / 2) ? p - paths / 2 : p;
+        const int64_t pc = ((anti && p >= paths / 2) ? p - paths / 2 : p) + s->path_offset;
         const double zsign = (anti && p >= paths / 2) ? -1.0 : 1.0;
         for (int gi = 0; gi < G && !rc; ++gi) {
             double st[SDE_MAX_GROUP], z[SDE_MAX_GROUP + 1], dW[SDE_MAX_GROUP], dJ[SDE_MAX_GROUP], dN[SDE_MAX_GROUP];
@@ -637,7 +637,7 @@ int oracle_adjoint_user(const SdeSpec *s, const SdeGrid *g, double mean_weight, 
                 uint32_t uw[4 * ((2 * SDE_MAX_GROUP + 3) / 4) + 4];
                 if (M == 1) {
                     if ((k & 1) == 0) {
-                        const uint32_t ctr[4] = {(uint32_t)p, c1, (uint32_t)gi << 8, s->stream};
+                        const uint32_t ctr[4] = {(uint32_t)p + s->path_offset, c1, (uint32_t)gi << 8, s->stream};
                         uint32_t r[4];
                         oracle_philox(ctr, key, r);
                         oracle_normal2(r[0], r[1], &pz0, &pz1);
@@ -645,7 +645,7 @@ int oracle_adjoint_user(const SdeSpec *s, const SdeGrid *g, double mean_weight, 
                     z[0] = (k & 1) ? pz1 : pz0;
                 } else if (M == 2) {
                     if ((k & 1) == 0) {
-                        const uint32_t ctr[4] = {(uint32_t)p, c1, (uint32_t)gi << 8, s->stream};
+                        const uint32_t ctr[4] = {(uint32_t)p + s->path_offset, c1, (uint32_t)gi << 8, s->stream};
                         uint32_t r[4];
                         oracle_philox(ctr, key, r);
                         oracle_normal2(r[0], r[1], &pz[0], &pz[1]);
@@ -655,7 +655,7 @@ int oracle_adjoint_user(const SdeSpec *s, const SdeGrid *g, double mean_weight, 
                     z[1] = (k & 1) ? pz[3] : pz[1];
                 } else {
                     for (int c = 0; c < NC; ++c) {
-                        const uint32_t ctr[4] = {(uint32_t)p, c1, ((uint32_t)gi << 8) | (uint32_t)c, s->stream};
+                        const uint32_t ctr[4] = {(uint32_t)p + s->path_offset, c1, ((uint32_t)gi << 8) | (uint32_t)c, s->stream};
                         oracle_philox(ctr, key, &uw[4 * c]);
                     }
                     for (int q = 0; q < P; ++q) oracle_normal2(uw[2 * q], uw[2 * q + 1], &z[2 * q], &z[2 * q + 1]);

@@ -13,7 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, '_native', 'libsdepy_gb300.so')
 
-ABI_VERSION = 4
+ABI_VERSION = 5
 MAX_GROUP = 16
 MAX_PARAMS = 6
 MAX_STRIKES = 8
@@ -53,7 +53,7 @@ class SdeSpec(C.Structure):
                 ('flags', C.c_int32),
                 ('x0', _dp), ('params', _dp), ('corr', _dp),
                 ('seed', C.c_uint64), ('stream', C.c_uint32),
-                ('reserved1', C.c_uint32), ('program', C.POINTER(SdeUserProgram))]
+                ('path_offset', C.c_uint32), ('program', C.POINTER(SdeUserProgram))]
 
 
 class SdeGrid(C.Structure):

@@ -34,6 +34,7 @@ struct AdjArgs {
     int32_t out_mode, jump_law, has_corr, rho_grad;
     uint64_t seed;
     uint32_t stream;
+    uint32_t path_offset;   // added to the path index in counter word 0
     PhiloxKey key;
     const R *dt, *sqdt;
     const double *lamdt, *p0;
@@ -358,7 +359,8 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
         for (int m = 0; m < MAXM; ++m)
 #pragma unroll
             for (int j = 0; j < NGV; ++j) gr[m][j] = R(0);
-        const PathPre<NCMAX> pre(key, (uint32_t)p, (uint32_t)g, a.stream);
+        const uint32_t pc = (uint32_t)p + a.path_offset;   // counter word 0 of this path
+        const PathPre<NCMAX> pre(key, pc, (uint32_t)g, a.stream);
         constexpr int NZ = Paired<MAXM, JUMPS>::NZ;
         PairedSteps<R, NZ == 0 ? 1 : NZ> pair;   // groups of one or two variables
         // the words, normals and increments of step k, exactly as the
@@ -406,7 +408,7 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                             R S = R(0);
                             for (int j = 0; j < cnt; ++j) {
                                 const uint4 r = philox4x32_10(
-                                    make_uint4((uint32_t)p, c1w, 0x80000000u | ((uint32_t)w << 12) | (uint32_t)j,
+                                    make_uint4(pc, c1w, 0x80000000u | ((uint32_t)w << 12) | (uint32_t)j,
                                                a.stream), key);
                                 const R y = jump_size<R>(a.jump_law, r, c3[m], c4[m], c5[m]);
                                 R da, db;

@@ -320,6 +320,8 @@ static int check_spec(const SdeSpec *s, int *opg) {
         return fail(SDE_ERR_UNSUPPORTED, "unknown precision %d", s->precision);
     if (s->paths < 1 || s->paths > 0x7fffffffLL)
         return fail(SDE_ERR_INVALID, "paths must be in [1, 2^31-1], not %lld", (long long)s->paths);
+    if ((uint64_t)s->path_offset + (uint64_t)s->paths > 0x100000000ull)
+        return fail(SDE_ERR_INVALID, "path_offset + paths must be <= 2^32 (the counter's path word)");
     if (s->groups < 1) return fail(SDE_ERR_INVALID, "groups must be >= 1");
     if (s->groups > 65535) return fail(SDE_ERR_UNSUPPORTED, "more than 65535 groups per path");
     if (s->group_size < 1 || s->group_size > SDE_MAX_GROUP)
@@ -710,6 +712,7 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     a.opg = opg;
     a.seed = s->seed;
     a.stream = s->stream;
+    a.path_offset = s->path_offset;
     a.sgn = (R)sgn;
     a.dt = (const R *)(T + o_dt);
     a.sqdt = (const R *)(T + o_sq);
@@ -857,9 +860,11 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
         void *p;
         if ((rc = scratch(D, S_PART, sizeof(double) * NPART * (size_t)s->groups * nbx * opg, &p))) return rc;
         a.partials = (double *)p;
-        // the histogram pass reads device memory: a private copy of the row
-        // when the paths go only to host memory
-        if (bins > 0 && (!a.xx || xx_mapped)) {
+        // the histogram pass, and the summary of the kernels that reduce the
+        // stored row in a second launch, read device memory: a private copy
+        // of the row when the paths go only to host memory
+        const bool row_pass = fwd_summary_from_row(sizeof(R) == 4, s->model, inject, jumps, anti, tdep_k, user);
+        if ((bins > 0 || row_pass) && (!a.xx || xx_mapped)) {
             if ((rc = scratch(D, S_VALS, sizeof(R) * n_out * paths, &p))) return rc;
             a.stats_vals = (R *)p;
         }
@@ -1230,6 +1235,7 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     a.jump_law = s->jump_law;
     a.seed = s->seed;
     a.stream = s->stream;
+    a.path_offset = s->path_offset;
     a.key = philox_schedule(s->seed);
     a.dt = (const R *)(T + o_dt);
     a.sqdt = (const R *)(T + o_sq);

@@ -47,6 +47,7 @@ struct FwdArgs {
     int32_t jump_law, out_mode, opg, has_corr;
     uint64_t seed;
     uint32_t stream;
+    uint32_t path_offset;   // added to the path index in counter word 0
     PhiloxKey key;  // round keys of seed
     R sgn;  // sign of dt on this leg (+1 forward, -1 backward)
     // per-step tables
@@ -887,7 +888,8 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                     for (int m = 0; m < MAXM; ++m) st1[m] = st[m];
                 }
             }
-            const PathPre<NCMAX> pre(key, (uint32_t)p, (uint32_t)g, a.stream);
+            const uint32_t pc = (uint32_t)p + a.path_offset;   // counter word 0 of this path
+            const PathPre<NCMAX> pre(key, pc, (uint32_t)g, a.stream);
             constexpr int NZ = Paired<MAXM, JUMPS>::NZ;
             PairedSteps<R, NZ == 0 ? 1 : NZ, TAB> pair;   // groups of one or two variables
             // Poisson count of state m at step k from uniform word `word`, and
@@ -910,7 +912,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                             R S = R(0);
                             for (int j = 0; j < cnt; ++j) {
                                 const uint4 r = philox4x32_10(
-                                    make_uint4((uint32_t)p, c1w, 0x80000000u | ((uint32_t)w << 12) | (uint32_t)j,
+                                    make_uint4(pc, c1w, 0x80000000u | ((uint32_t)w << 12) | (uint32_t)j,
                                                a.stream),
                                     key);
                                 const R y = jump_size<R>(a.jump_law, r, ja, jb, jpa);
@@ -919,7 +921,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                             dJ[m] = A::mul(a.sgn, S);
                         }
                         if (a.user_jsrc & 2)
-                            cnt = count(philox4x32_10(make_uint4((uint32_t)p, c1w, 0x40000000u | (uint32_t)w, a.stream),
+                            cnt = count(philox4x32_10(make_uint4(pc, c1w, 0x40000000u | (uint32_t)w, a.stream),
                                                       key).x);
                     }
                     if constexpr (JUMPS)
@@ -931,7 +933,7 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                     R S = R(0);
                     for (int j = 0; j < cnt; ++j) {
                         const uint4 r = philox4x32_10(
-                            make_uint4((uint32_t)p, c1w, 0x80000000u | ((uint32_t)w << 12) | (uint32_t)j, a.stream),
+                            make_uint4(pc, c1w, 0x80000000u | ((uint32_t)w << 12) | (uint32_t)j, a.stream),
                             key);
                         const R y = jump_size<R>(a.jump_law, r, c3[m], c4[m], c5[m]);
                         S = (j == 0) ? y : A::add(S, y);
@@ -1294,6 +1296,15 @@ int fwd_max_blocks_per_sm() {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sde_fwd_kernel<R, MODEL, MAXM, INJECT, JUMPS, TDEP, ANTI>,
                                                   BLOCK, 0);
     return n;
+}
+
+// The FP32 LINEAR / OU kernels of device noise without jumps, antithetic
+// paths or time-dependent coefficients (sde_fwd_tab_kernel, sde_tab.cuh)
+// store the summarised row and reduce it in a second launch: a summary
+// needs FwdArgs::stats_vals, or xx in device memory
+inline bool fwd_summary_from_row(bool fp32, int model, bool inject, bool jumps, bool anti, bool tdep, bool user) {
+    return fp32 && !inject && !jumps && !anti && !tdep && !user &&
+           (model == SDE_MODEL_LINEAR || model == SDE_MODEL_OU);
 }
 
 // dispatch lookup implemented in the instantiation units (fwd_*.cu)

@@ -15,8 +15,9 @@
 //   * device-RNG paths, no jumps, no path output (the summary only), the
 //     summarised row given by req->row;
 //   * everything the call needs (grid, coefficients, tables, block partials,
-//     results, histogram and, when bins > 0, the summarised values) must fit
-//     in the 16 MiB array; larger requests fail with SDE_ERR_INVALID;
+//     results, histogram and, when bins > 0 or for the FP32 LINEAR / OU
+//     kernels, the summarised values) must fit in the 16 MiB array; larger
+//     requests fail with SDE_ERR_INVALID;
 //   * the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (with that device current) -- make that first
 //     call before any stream capture.  The address is kept for the life of
@@ -115,6 +116,8 @@ int run_static(const SdeSpec *s, const SdeGrid *gr, const SdeStatsReq *req, SdeS
     if (s->jump_law != SDE_JUMP_NONE)
         return fail_static(SDE_ERR_UNSUPPORTED, "sde_run_stats_static does not integrate jump models");
     if (s->paths < 1 || s->paths > 0x7fffffffLL) return fail_static(SDE_ERR_INVALID, "paths out of range");
+    if ((uint64_t)s->path_offset + (uint64_t)s->paths > 0x100000000ull)
+        return fail_static(SDE_ERR_INVALID, "path_offset + paths must be <= 2^32");
     if (s->groups < 1 || s->groups > 65535) return fail_static(SDE_ERR_INVALID, "groups out of range");
     const int M = s->group_size;
     if (M < 1 || M > SDE_MAX_GROUP) return fail_static(SDE_ERR_UNSUPPORTED, "group size %d outside 1..%d", M, SDE_MAX_GROUP);
@@ -223,7 +226,10 @@ int run_static(const SdeSpec *s, const SdeGrid *gr, const SdeStatsReq *req, SdeS
     lo.edges = o; o = al256(o + sizeof(R) * (size_t)(bins + 1) * n_out);
     lo.edges64 = o; o = al256(o + sizeof(double) * (size_t)(bins + 1) * n_out);
     lo.counts = o; o = al256(o + sizeof(int64_t) * (size_t)bins * n_out);
-    lo.vals = o; o = al256(o + (bins > 0 ? sizeof(R) * (size_t)n_out * paths : 0));
+    // the summarised values: for the histogram, and for the kernels that
+    // reduce the stored row in a second launch
+    const bool need_vals = bins > 0 || fwd_summary_from_row(sizeof(R) == 4, s->model, false, false, false, false, false);
+    lo.vals = o; o = al256(o + (need_vals ? sizeof(R) * (size_t)n_out * paths : 0));
     lo.mom = o; o = al256(o + sizeof(double) * 8 * n_out);
     lo.pay = o; o = al256(o + sizeof(double) * (size_t)req->n_strikes * n_out);
     lo.err = o; o = al256(o + 16);
@@ -264,6 +270,7 @@ int run_static(const SdeSpec *s, const SdeGrid *gr, const SdeStatsReq *req, SdeS
     a.opg = opg;
     a.seed = s->seed;
     a.stream = s->stream;
+    a.path_offset = s->path_offset;
     a.sgn = (R)(sgn < 0 ? -1.0 : 1.0);
     a.dt = (const R *)(base + lo.dt);
     a.sqdt = (const R *)(base + lo.sq);
@@ -292,7 +299,7 @@ int run_static(const SdeSpec *s, const SdeGrid *gr, const SdeStatsReq *req, SdeS
     a.n_strikes = req->n_strikes;
     for (int i = 0; i < req->n_strikes; ++i) a.strikes[i] = (R)req->strikes[i];
     a.partials = (double *)(base + lo.part);
-    a.stats_vals = bins > 0 ? (R *)(base + lo.vals) : nullptr;
+    a.stats_vals = need_vals ? (R *)(base + lo.vals) : nullptr;
     a.err = (int32_t *)(base + lo.err);
     L(a, dim3(nbx, s->groups), st);
     CUS(cudaGetLastError());

@@ -1,7 +1,14 @@
-"""Replica merging: paths are independent, so N GPUs (or N processes) run
-independent replicas -- distinct Philox streams -- and only their montecarlo
-summaries are exchanged and merged on the host.  There is no collective on
-the data path.
+"""Path-range sharding and summary merging: paths are independent, so N
+GPUs (or N processes) each integrate a contiguous range of the paths of one
+run -- the same Philox key, the range's start as the process's path_offset,
+so the ranks' paths are exactly the paths one device would integrate -- and
+only their montecarlo summaries are exchanged and merged on the host.  There
+is no collective on the data path.
+
+Histograms follow sdepy's montecarlo over batches
+(sdepy/infrastructure.py:2961-3021): the bins are fixed by the first sample
+(rank 0's range, numpy's rule for an integer number of bins), every later
+sample is counted in those edges; sharded_summary shares rank 0's edges.
 
 A summary is the sufficient statistic of a montecarlo sample: count, mean,
 central sums M2..M4 (per component) and, when bins were fixed, histogram
@@ -22,13 +29,29 @@ def summary(n, mean, M2, M3=None, M4=None, counts=None, edges=None):
             'edges': None if edges is None else np.asarray(edges, dtype=float)}
 
 
-def summary_of_sample(sample, axis=-1, edges=None):
-    """Summary of a host sample (numpy), counts in ``edges`` if given."""
-    s = np.moveaxis(np.asarray(sample, dtype=float), axis, -1)
+def path_range(paths, rank, world):
+    """Rank ``rank``'s contiguous share of ``paths`` paths split over
+    ``world`` ranks: (path_offset, count); the shares tile [0, paths)."""
+    if not 0 <= rank < world:
+        raise ValueError('rank {} outside 0..{}'.format(rank, world - 1))
+    base, extra = divmod(int(paths), int(world))
+    return rank*base + min(rank, extra), base + (1 if rank < extra else 0)
+
+
+def summary_of_sample(sample, axis=-1, edges=None, bins=None):
+    """Summary of a host sample (numpy): counts in ``edges`` if given, or,
+    with an integer ``bins``, the counts and edges of numpy's rule for a
+    first sample (the sample's range in its own dtype)."""
+    raw = np.moveaxis(np.asarray(sample), axis, -1)
+    s = raw.astype(float)
     mean = s.mean(axis=-1)
     d = s - mean[..., None]
     counts = None
-    if edges is not None:
+    if bins is not None and edges is None:
+        pairs = [np.histogram(raw[i], bins=bins) for i in np.ndindex(s.shape[:-1])]
+        counts = np.stack([c for c, _ in pairs]).reshape(s.shape[:-1] + (-1,))
+        edges = np.stack([e for _, e in pairs]).astype(float).reshape(s.shape[:-1] + (-1,))
+    elif edges is not None:
         e = np.asarray(edges, dtype=float)
         counts = np.stack([np.histogram(s[i], bins=e[i])[0]
                            for i in np.ndindex(s.shape[:-1])]).reshape(s.shape[:-1] + (-1,))
@@ -75,6 +98,22 @@ def allgather_merge(s, group=None):
     got = [None]*world
     dist.all_gather_object(got, s, group=group)
     return merge_all(got)
+
+
+def sharded_summary(sample, bins=None, group=None, axis=-1):
+    """The merged summary of every rank's sample, as sdepy's montecarlo
+    summarises the ranks' samples fed in rank order: rank 0's sample fixes
+    the bins (integer ``bins``), the others are counted in its edges.  Every
+    rank returns the same result."""
+    import torch.distributed as dist
+    if bins is None:
+        return allgather_merge(summary_of_sample(sample, axis), group)
+    mine = summary_of_sample(sample, axis, bins=bins) if dist.get_rank(group) == 0 else None
+    obj = [None if mine is None else mine['edges']]
+    dist.broadcast_object_list(obj, src=0, group=group)
+    if mine is None:
+        mine = summary_of_sample(sample, axis, edges=obj[0])
+    return allgather_merge(mine, group)
 
 
 def statistics(s):

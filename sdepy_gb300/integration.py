@@ -88,7 +88,7 @@ class _gpu_process:
 
     def __init__(self, *, paths=1, vshape=(), dtype=None, rng=None,
                  steps=None, i0=0, info=None, getinfo=True, method='euler',
-                 **args):
+                 path_offset=0, **args):
         if method != 'euler':
             raise ValueError(
                 'unrecognized integration method {}: '
@@ -103,6 +103,15 @@ class _gpu_process:
         all_args = {**expected, **args}
         self.vshape = _shape_setup(vshape)
         self.paths = paths
+        # GPU extension (no sdepy counterpart): these paths are paths
+        # [path_offset, path_offset + paths) of a larger sample drawn from
+        # the same device random stream, so that path ranges integrated
+        # apart (on other devices, or in later calls) reproduce one run
+        path_offset = int(path_offset)
+        if path_offset < 0 or path_offset + int(paths) > 2**32:
+            raise ValueError('path_offset must be >= 0 with path_offset + paths <= 2**32, '
+                             'not {} + {}'.format(path_offset, paths))
+        self.path_offset = path_offset
         self.dtype = dtype
         self.steps, self.i0 = steps, i0
         self.info = {} if info is None else info
@@ -289,6 +298,7 @@ class _gpu_process:
         s.corr = _lib.dptr(self._corr_c)
         s.seed = seed
         s.stream = stream
+        s.path_offset = self.path_offset
         return s
 
     @property

@@ -235,3 +235,13 @@ def test_host_sources_specific():
     for dt in (1., 100.):
         s = src(0., dt)
         assert_allclose(src.dn_value*val, s, rtol=np.finfo(float).eps)
+
+
+def test_path_offset_range_is_checked():
+    """path_offset + paths must fit the 32-bit path word of the counters."""
+    import sdepy_gb300 as sg
+    assert sg.lognorm_process(paths=10, path_offset=2**32 - 10)._make_spec().path_offset == 2**32 - 10
+    with pytest.raises(ValueError):
+        sg.lognorm_process(paths=10, path_offset=2**32 - 5)
+    with pytest.raises(ValueError):
+        sg.lognorm_process(paths=10, path_offset=-1)
