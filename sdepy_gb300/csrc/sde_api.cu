@@ -713,6 +713,7 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
     a.seed = s->seed;
     a.stream = s->stream;
     a.path_offset = s->path_offset;
+    a.tab_row0 = gr->out_row[0];
     a.sgn = (R)sgn;
     a.dt = (const R *)(T + o_dt);
     a.sqdt = (const R *)(T + o_sq);

@@ -101,6 +101,10 @@ struct FwdArgs {
     int64_t n_out_vars;
     int32_t *neg_count, *jump_count;
     unsigned long long *row_jumps;
+    // the output row of the grid's first point (out_row[0], read on the
+    // host), which the FP32 LINEAR / OU launcher fills with x0 by a separate
+    // launch; -1: none
+    int32_t tab_row0;
     // fused statistics
     int32_t stats_row, n_strikes;
     R strikes[SDE_MAX_STRIKES];

@@ -271,6 +271,7 @@ int run_static(const SdeSpec *s, const SdeGrid *gr, const SdeStatsReq *req, SdeS
     a.seed = s->seed;
     a.stream = s->stream;
     a.path_offset = s->path_offset;
+    a.tab_row0 = gr->out_row[0];
     a.sgn = (R)(sgn < 0 ? -1.0 : 1.0);
     a.dt = (const R *)(base + lo.dt);
     a.sqdt = (const R *)(base + lo.sq);
