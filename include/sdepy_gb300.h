@@ -184,8 +184,8 @@ typedef struct SdeGrid {
      * for jump models slot 2 is the Poisson intensity evaluated at the
      * step's midpoint tt[k] + dt/2 (sdepy/infrastructure.py:1629); slots
      * 3..5 (jump-size laws) are read from SdeSpec.params.  sde_run and
-     * sde_run_stats accept it; sde_adjoint and sde_run_stats_static return
-     * SDE_ERR_UNSUPPORTED. */
+     * sde_run_stats accept it, and sde_adjoint (per-step gradients,
+     * SdeAdjReq.grad_t); sde_run_stats_static returns SDE_ERR_UNSUPPORTED. */
     const double *params_t;
     /* Time-dependent correlation, or NULL (SdeSpec.corr applies at every
      * step): [n_pts - 1][M][M], row k the correlation matrix of the Wiener
@@ -351,10 +351,21 @@ SDE_API int32_t sde_run_stats(const SdeSpec *spec, const SdeGrid *grid,
  * sdepy/integration.py:707-718. */
 typedef struct SdeAdjReq {
     int32_t n_strikes;
-    int32_t checkpoint;      /* steps per segment, 0: ceil(sqrt(steps)) */
+    int32_t checkpoint;      /* steps per segment, 0: ceil(sqrt(steps)); runs
+                              * needing more than 64 segments use two levels
+                              * of checkpoints (up to 64^3 steps) */
     double strikes[SDE_MAX_STRIKES];
     double weights[SDE_MAX_STRIKES];
     double mean_weight;
+    /* With SdeGrid.params_t (the preset models without jumps): out,
+     * [n_steps][3][groups*M], d L / d of parameter slot j (0..2) of step k
+     * of each state variable -- the per-step coefficients the table gives
+     * (sdepy evaluates callable parameters per step, SDE.A at
+     * sdepy/integration.py:1216-1225); grad's slots 1..3 are then unused.
+     * NULL without params_t.  The per-step table is reduced in shared
+     * memory: steps x 3 x group width x 4 (FP32) or 8 (FP64) bytes must not
+     * exceed 160 KiB. */
+    double *grad_t;
 } SdeAdjReq;
 
 SDE_API int32_t sde_adjoint(const SdeSpec *spec, const SdeGrid *grid,

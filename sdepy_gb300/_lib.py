@@ -87,7 +87,8 @@ class SdeAdjReq(C.Structure):
     _fields_ = [('n_strikes', C.c_int32), ('checkpoint', C.c_int32),
                 ('strikes', C.c_double*MAX_STRIKES),
                 ('weights', C.c_double*MAX_STRIKES),
-                ('mean_weight', C.c_double)]
+                ('mean_weight', C.c_double),
+                ('grad_t', C.POINTER(C.c_double))]
 
 
 class SdeBatchInstance(C.Structure):

@@ -140,6 +140,23 @@ def run_single(s, precision=_lib.FP32):
     return mom[0, 1], np.sqrt(mom[0, 2]/mom[0, 0])
 
 
+def run_single_with_gradient(s, precision=_lib.FP32):
+    """run_single plus sde_adjoint of the mean of X(T) of the first state on
+    the same paths: the work one batch instance does (its summary and its
+    pathwise derivatives), done by the single-instance entry points.
+    Returns (mean, std, gradient slots [state][8])."""
+    lib = _lib.load()
+    mean, std = run_single(s, precision)
+    spec, g, keep = single_spec(s, precision)
+    req = _lib.SdeAdjReq()
+    req.n_strikes, req.checkpoint, req.mean_weight = 0, 0, 1.
+    grad = np.zeros((s.nvars if s.model != HESTON else 2, 8))
+    v = C.c_double()
+    _lib.check(lib.sde_adjoint(C.byref(spec), C.byref(g), C.byref(req), _lib.dptr(grad), C.byref(v)),
+               'sde_adjoint')
+    return mean, std, grad
+
+
 _TUNED = {}
 
 

@@ -25,11 +25,18 @@ namespace sdegpu {
 
 constexpr int NGV = 8;          // gradient slots per state variable
 constexpr int ADJ_MAXSEG = 64;  // checkpoints and steps per segment
+// the per-step gradient table of the kernels with time-dependent
+// parameters lives in shared memory: at most this many bytes per block
+// (steps x 3 x group width x sizeof(R)), and the SM's share for the table
+constexpr size_t ADJ_TD_SMEM = 160 * 1024;
+constexpr size_t ADJ_TD_SMEM_SM = 220 * 1024;
 
 template <typename R>
 struct AdjArgs {
     int64_t paths;
-    int32_t groups, M, W, n_steps, seg, nseg;
+    // checkpoints: level 1 every `seg` steps (nseg of them); within a
+    // level-1 segment, level 2 every `seg2` steps (seg2 == seg: one level)
+    int32_t groups, M, W, n_steps, seg, nseg, seg2;
     uint32_t step_offset;
     int32_t out_mode, jump_law, has_corr, rho_grad;
     uint64_t seed;
@@ -50,6 +57,12 @@ struct AdjArgs {
     // SDE_MODEL_USER: the coefficient program and each step's start time
     SdeUserProgram uprog;
     const R *tk;
+    // time-dependent parameters (kernels compiled with TD): slots 0..2 of
+    // each step, [n_steps][3][W]; the gradients of those slots, per step,
+    // go to tdpart [groups][gridDim.x][n_steps][3][MAXM] instead of the
+    // per-variable slots 1..3
+    const R *prm_t;
+    double *tdpart;
 };
 
 // Tangent-mode run of a user program (single equation): the terms' values
@@ -318,7 +331,13 @@ __device__ __forceinline__ void fwd_step(const R (&c0)[MAXM], const R (&c1)[MAXM
 
 // FP32 kernels of one or two states are held to 80 registers: 3 resident
 // blocks per SM (measured 2.4 % faster for Heston than 2 blocks at 90)
-template <typename R, int MODEL, int MAXM, bool JUMPS>
+// TD: time-dependent parameter slots 0..2 (AdjArgs::prm_t), reloaded at every
+// step of every sweep, with per-step gradients: each warp sums a step's
+// contributions over its paths and adds them to a block table in shared
+// memory (n_steps * 3 * MAXM values of R), written out at the block's end.
+// Every lane of a warp walks a path in every round (the last round's spare
+// lanes contribute zero), so the warp sums see whole warps.
+template <typename R, int MODEL, int MAXM, bool JUMPS, bool TD = false>
 __global__ void __launch_bounds__(BLOCK, (sizeof(R) == 4 && MAXM <= 2) ? 3 : 1)
 sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
     // a user SDE: interpreted, or compiled at run time
@@ -351,9 +370,41 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
     R acc[NPA], cmp[NPA];
 #pragma unroll
     for (int i = 0; i < NPA; ++i) acc[i] = cmp[i] = R(0);
+    extern __shared__ unsigned char td_raw[];
+    R *tdtab = reinterpret_cast<R *>(td_raw);
+    const int ntd = TD ? a.n_steps * 3 * MAXM : 0;
+    if constexpr (TD) {
+        for (int i = threadIdx.x; i < ntd; i += BLOCK) tdtab[i] = R(0);
+        __syncthreads();
+    }
+    // a step's coefficients (TD): slots 0..2 from the table
+    auto load_step = [&](int k) {
+        if constexpr (TD) {
+            const R *pk = a.prm_t + (int64_t)k * 3 * W;
+#pragma unroll
+            for (int m = 0; m < MAXM; ++m) {
+                const int w = g * M + (m < M ? m : 0);
+                c0[m] = pk[w];
+                c1[m] = pk[W + w];
+                c2[m] = pk[2 * W + w];
+            }
+        }
+    };
 
     const int64_t stride = (int64_t)gridDim.x * BLOCK;
-    for (int64_t p = (int64_t)blockIdx.x * BLOCK + threadIdx.x; p < a.paths; p += stride) {
+    const int64_t rounds = (a.paths + stride - 1) / stride;
+    for (int64_t rd = 0; rd < rounds; ++rd) {
+        const int64_t pr = rd * stride + (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+        const bool act = pr < a.paths;
+        if (!TD && !act) continue;   // TD: spare lanes walk path 0 and contribute zero
+        const int64_t p = act ? pr : 0;
+        // d L / d (slot j of state m at step k) += v
+        auto addp = [&](int k, int m, int j, R v) {
+            if constexpr (TD) {
+                v = warp_sum<R>(act ? v : R(0));
+                if ((threadIdx.x & 31) == 0) atomicAdd(&tdtab[(k * 3 + j) * MAXM + m], v);
+            }
+        };
         R gr[MAXM][NGV];
 #pragma unroll
         for (int m = 0; m < MAXM; ++m)
@@ -393,6 +444,7 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                 uint32_t u[4 * NCMAX];
                 R z[MAXM], dW[MAXM];
                 noise(k, sq, u, z, dW);
+                load_step(k);
                 sdt = sdt + dt;
 #pragma unroll
                 for (int m = 0; m < MAXM; ++m) {
@@ -433,6 +485,21 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                 gr[m][4] = xb[m] * sja[m];
                 gr[m][5] = xb[m] * sjb[m];
             }
+            if constexpr (TD) {
+                // the constant adjoint xb times each step's dt and dW: the
+                // increments are drawn again (the kernels with TD take no jumps)
+                for (int k = 0; k < a.n_steps; ++k) {
+                    const R dt = a.dt[k], sq = a.sqdt[k];
+                    uint32_t u[4 * NCMAX];
+                    R z[MAXM], dW[MAXM];
+                    noise(k, sq, u, z, dW);
+#pragma unroll
+                    for (int m = 0; m < MAXM; ++m) {
+                        addp(k, m, 0, xb[m] * dt);
+                        addp(k, m, 1, xb[m] * dW[m]);
+                    }
+                }
+            }
         } else {
             // ---- checkpointed reverse sweep (OU, Heston) ----------------------------
             R ck[ADJ_MAXSEG][MAXM];
@@ -448,17 +515,43 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                 uint32_t u[4 * NCMAX];
                 R z[MAXM], dW[MAXM];
                 noise(k, sq, u, z, dW);
+                load_step(k);
                 if constexpr (UJ) user_step<R, MAXM, MODEL>(a.uprog, c0, c1, c2, c3, c4, c5, a.tk[k], a.dt[k], dW, st);
                 else fwd_step<R, MODEL, MAXM>(c0, c1, c2, a.dt[k], dW, st);
             }
             R xb[MAXM];
             val = terminal_adjoint<R, MAXM>(a, st, xb);
             R bx[ADJ_MAXSEG][MAXM], bw[ADJ_MAXSEG][MAXM], bz[ADJ_MAXSEG][2];
-            for (int sidx = a.nseg - 1; sidx >= 0; --sidx) {
-                const int k0 = sidx * a.seg;
-                const int k1 = min(k0 + a.seg, a.n_steps);
+            // level-2 checkpoints of the current level-1 segment (two levels
+            // only: runs longer than ADJ_MAXSEG^2 steps)
+            R ck2[ADJ_MAXSEG][MAXM];
+            const bool two = a.seg2 < a.seg;
+            for (int s1 = a.nseg - 1; s1 >= 0; --s1) {
+              const int l0 = s1 * a.seg;
+              const int l1 = min(l0 + a.seg, a.n_steps);
+              if (two) {
 #pragma unroll
-                for (int m = 0; m < MAXM; ++m) st[m] = ck[sidx][m];
+                  for (int m = 0; m < MAXM; ++m) st[m] = ck[s1][m];
+                  for (int k = l0; k < l1; ++k) {
+                      if ((k - l0) % a.seg2 == 0) {
+#pragma unroll
+                          for (int m = 0; m < MAXM; ++m) ck2[(k - l0) / a.seg2][m] = st[m];
+                      }
+                      const R sq = a.sqdt[k];
+                      uint32_t u[4 * NCMAX];
+                      R z[MAXM], dW[MAXM];
+                      noise(k, sq, u, z, dW);
+                      load_step(k);
+                      if constexpr (UJ) user_step<R, MAXM, MODEL>(a.uprog, c0, c1, c2, c3, c4, c5, a.tk[k], a.dt[k], dW, st);
+                      else fwd_step<R, MODEL, MAXM>(c0, c1, c2, a.dt[k], dW, st);
+                  }
+              }
+              const int nseg2 = two ? (l1 - l0 + a.seg2 - 1) / a.seg2 : 1;
+              for (int sidx = nseg2 - 1; sidx >= 0; --sidx) {
+                const int k0 = two ? l0 + sidx * a.seg2 : l0;
+                const int k1 = two ? min(k0 + a.seg2, l1) : l1;
+#pragma unroll
+                for (int m = 0; m < MAXM; ++m) st[m] = two ? ck2[sidx][m] : ck[s1][m];
                 for (int k = k0; k < k1; ++k) {
                     const R sq = a.sqdt[k];
                     uint32_t u[4 * NCMAX];
@@ -471,11 +564,13 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                     }
                     bz[k - k0][0] = z[0];
                     bz[k - k0][1] = MAXM > 1 ? z[MAXM > 1 ? 1 : 0] : R(0);
+                    load_step(k);
                     if constexpr (UJ) user_step<R, MAXM, MODEL>(a.uprog, c0, c1, c2, c3, c4, c5, a.tk[k], a.dt[k], dW, st);
                     else fwd_step<R, MODEL, MAXM>(c0, c1, c2, a.dt[k], dW, st);
                 }
                 for (int k = k1 - 1; k >= k0; --k) {
                     const R dt = a.dt[k], sq = a.sqdt[k];
+                    load_step(k);
                     if constexpr (UJ) {
                         // x' = x + sum_i A_i(t, x, p) dZ_i: dx'/dx = 1 + sum_i dA_i/dx dZ_i,
                         // dx'/dp_j = sum_i dA_i/dp_j dZ_i
@@ -501,9 +596,15 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                         for (int m = 0; m < MAXM; ++m) {
                             const R x = bx[k - k0][m];
                             const R xbn = xb[m];
-                            gr[m][1] += xbn * (c1[m] - x) * dt;   // k
-                            gr[m][2] += xbn * c0[m] * dt;         // theta
-                            gr[m][3] += xbn * bw[k - k0][m];      // sigma
+                            if constexpr (TD) {
+                                addp(k, m, 0, xbn * (c1[m] - x) * dt);
+                                addp(k, m, 1, xbn * c0[m] * dt);
+                                addp(k, m, 2, xbn * bw[k - k0][m]);
+                            } else {
+                                gr[m][1] += xbn * (c1[m] - x) * dt;   // k
+                                gr[m][2] += xbn * c0[m] * dt;         // theta
+                                gr[m][3] += xbn * bw[k - k0][m];      // sigma
+                            }
                             xb[m] = xbn * (R(1) - c0[m] * dt);
                         }
                     } else if (MODEL == SDE_MODEL_CIR) {
@@ -513,9 +614,15 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                             const R xp = fmax(x, R(0));
                             const R s = A::sqrt_(xp);
                             const R xbn = xb[m], dw = bw[k - k0][m];
-                            gr[m][1] += xbn * (c1[m] - xp) * dt;   // k
-                            gr[m][2] += xbn * c0[m] * dt;          // theta
-                            gr[m][3] += xbn * s * dw;              // xi
+                            if constexpr (TD) {
+                                addp(k, m, 0, xbn * (c1[m] - xp) * dt);
+                                addp(k, m, 1, xbn * c0[m] * dt);
+                                addp(k, m, 2, xbn * s * dw);
+                            } else {
+                                gr[m][1] += xbn * (c1[m] - xp) * dt;   // k
+                                gr[m][2] += xbn * c0[m] * dt;          // theta
+                                gr[m][3] += xbn * s * dw;              // xi
+                            }
                             // dx'/dx = 1 + (-k dt + xi dW / (2 sqrt x)) where x > 0
                             R d = R(1);
                             if (x > R(0) && s > R(0)) d = R(1) - c0[m] * dt + c2[m] * dw * (R(0.5) / s);
@@ -532,11 +639,19 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                             const R mu = c0[i], sg = c1[i];
                             const R kk = c0[h + i], th = c1[h + i], xi = c2[h + i];
                             const R dWx = bw[k - k0][i], dWy = bw[k - k0][h + i];
-                            gr[i][1] += ab * dt;                              // mu
-                            gr[i][2] += ab * (s * dWx - sg * yp * dt);         // sigma
-                            gr[h + i][1] += ybn * (th - yp) * dt;              // k
-                            gr[h + i][2] += ybn * kk * dt;                     // theta
-                            gr[h + i][3] += ybn * s * dWy;                     // xi
+                            if constexpr (TD) {
+                                addp(k, i, 0, ab * dt);
+                                addp(k, i, 1, ab * (s * dWx - sg * yp * dt));
+                                addp(k, h + i, 0, ybn * (th - yp) * dt);
+                                addp(k, h + i, 1, ybn * kk * dt);
+                                addp(k, h + i, 2, ybn * s * dWy);
+                            } else {
+                                gr[i][1] += ab * dt;                              // mu
+                                gr[i][2] += ab * (s * dWx - sg * yp * dt);         // sigma
+                                gr[h + i][1] += ybn * (th - yp) * dt;              // k
+                                gr[h + i][2] += ybn * kk * dt;                     // theta
+                                gr[h + i][3] += ybn * s * dWy;                     // xi
+                            }
                             if (MAXM == 2 && a.rho_grad) {
                                 // dW_y = (rho z0 + sqrt(1 - rho^2) z1) sq
                                 const R ddw = (bz[k - k0][0] + a.rho_k * bz[k - k0][1]) * sq;
@@ -553,16 +668,19 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                         }
                     }
                 }
+              }
             }
 #pragma unroll
             for (int m = 0; m < MAXM; ++m) gr[m][0] = xb[m];
         }
         // accumulate this path
+        if (act) {
 #pragma unroll
-        for (int m = 0; m < MAXM; ++m)
+            for (int m = 0; m < MAXM; ++m)
 #pragma unroll
-            for (int j = 0; j < NGV; ++j) kahan_add(acc[m * NGV + j], cmp[m * NGV + j], gr[m][j]);
-        kahan_add(acc[MAXM * NGV], cmp[MAXM * NGV], val);
+                for (int j = 0; j < NGV; ++j) kahan_add(acc[m * NGV + j], cmp[m * NGV + j], gr[m][j]);
+            kahan_add(acc[MAXM * NGV], cmp[MAXM * NGV], val);
+        }
     }
     // block reduction, FP64 partial per block
 #pragma unroll
@@ -572,26 +690,43 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
             a.partials[(((int64_t)g * gridDim.x + blockIdx.x) * NPA) + i] = (double)s;
     }
     if (threadIdx.x == 0) a.partials[(((int64_t)g * gridDim.x + blockIdx.x) * NPA) + NPA - 1] = 0.0;
+    if constexpr (TD) {
+        __syncthreads();
+        double *dst = a.tdpart + ((int64_t)g * gridDim.x + blockIdx.x) * ntd;
+        for (int i = threadIdx.x; i < ntd; i += BLOCK) dst[i] = (double)tdtab[i];
+    }
 }
 
 #ifndef __CUDACC_RTC__
 template <typename R>
 using AdjLauncher = void (*)(const AdjArgs<R> &, dim3, cudaStream_t);
 
-template <typename R, int MODEL, int MAXM, bool JUMPS>
+template <typename R, int MODEL, int MAXM, bool JUMPS, bool TD = false>
 void launch_adj(const AdjArgs<R> &a, dim3 grid, cudaStream_t s) {
-    sde_adj_kernel<R, MODEL, MAXM, JUMPS><<<grid, BLOCK, 0, s>>>(a);
+    if constexpr (TD) {
+        // the block's per-step table; the bytes were checked by the caller
+        const size_t smem = sizeof(R) * (size_t)a.n_steps * 3 * MAXM;
+        cudaFuncSetAttribute(sde_adj_kernel<R, MODEL, MAXM, JUMPS, TD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        sde_adj_kernel<R, MODEL, MAXM, JUMPS, TD><<<grid, BLOCK, smem, s>>>(a);
+    } else {
+        sde_adj_kernel<R, MODEL, MAXM, JUMPS><<<grid, BLOCK, 0, s>>>(a);
+    }
 }
 
-template <typename R, int MODEL, int MAXM, bool JUMPS>
+template <typename R, int MODEL, int MAXM, bool JUMPS, bool TD = false>
 int adj_max_blocks_per_sm() {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sde_adj_kernel<R, MODEL, MAXM, JUMPS>, BLOCK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sde_adj_kernel<R, MODEL, MAXM, JUMPS, TD>, BLOCK, 0);
     return n;
 }
 
 AdjLauncher<float> find_adj_f32(int model, int maxm, bool jumps, int *bps);
 AdjLauncher<double> find_adj_f64(int model, int maxm, bool jumps, int *bps);
+// time-dependent parameter slots, no jumps (adj_td.cu); the occupancy
+// returned is for the kernel without its per-step table
+AdjLauncher<float> find_adj_td_f32(int model, int maxm, int *bps);
+AdjLauncher<double> find_adj_td_f64(int model, int maxm, int *bps);
 // user SDEs (adj_user.cu)
 AdjLauncher<float> find_adj_user_f32(int maxm, int *bps);
 AdjLauncher<double> find_adj_user_f64(int maxm, int *bps);

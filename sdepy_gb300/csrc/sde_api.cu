@@ -1129,12 +1129,14 @@ template <> struct AdjFinder<float> {
         if (model == SDE_MODEL_USER) return jumps ? nullptr : find_adj_user_f32(maxm, bps);
         return find_adj_f32(model, maxm, jumps, bps);
     }
+    static AdjLauncher<float> find_td(int model, int maxm, int *bps) { return find_adj_td_f32(model, maxm, bps); }
 };
 template <> struct AdjFinder<double> {
     static AdjLauncher<double> find(int model, int maxm, bool jumps, int *bps) {
         if (model == SDE_MODEL_USER) return jumps ? nullptr : find_adj_user_f64(maxm, bps);
         return find_adj_f64(model, maxm, jumps, bps);
     }
+    static AdjLauncher<double> find_td(int model, int maxm, int *bps) { return find_adj_td_f64(model, maxm, bps); }
 };
 
 template <typename R>
@@ -1160,11 +1162,34 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     const bool jumps = s->jump_law != SDE_JUMP_NONE;
     int maxm = maxm_of(M);
     if (maxm > 8) return fail(SDE_ERR_UNSUPPORTED, "the adjoint supports groups of up to 8 state variables");
+    // time-dependent parameter slots: per-step gradients into req->grad_t
+    const bool td = gr->params_t != nullptr;
+    const size_t td_smem = td ? sizeof(R) * (size_t)n_steps * 3 * maxm : 0;
+    if (td) {
+        if (user || jumps)
+            return fail(SDE_ERR_UNSUPPORTED, "gradients with time-dependent parameters take the preset models "
+                                             "without jumps");
+        if (!req->grad_t) return fail(SDE_ERR_INVALID, "time-dependent parameters need the request's grad_t");
+        if (td_smem > ADJ_TD_SMEM)
+            return fail(SDE_ERR_UNSUPPORTED, "gradients with time-dependent parameters: at most %d steps for "
+                                             "groups of %d", (int)(ADJ_TD_SMEM / (sizeof(R) * 3 * maxm)), M);
+    }
+    // checkpoints: one level of ceil(sqrt(steps)) steps up to ADJ_MAXSEG^2
+    // steps; beyond, two levels (level 1 every ceil(steps / ADJ_MAXSEG)
+    // steps, level 2 inside it), one more forward sweep of the paths
     int seg = req->checkpoint > 0 ? req->checkpoint : (int)ceil(sqrt((double)n_steps));
     if (seg > ADJ_MAXSEG) seg = ADJ_MAXSEG;
+    if (seg < 1) seg = 1;
+    int seg2 = seg;
+    if (s->model != SDE_MODEL_LINEAR && (n_steps + seg - 1) / seg > ADJ_MAXSEG) {
+        seg = (n_steps + ADJ_MAXSEG - 1) / ADJ_MAXSEG;
+        seg2 = (int)ceil(sqrt((double)seg));
+        if ((seg + seg2 - 1) / seg2 > ADJ_MAXSEG) seg2 = (seg + ADJ_MAXSEG - 1) / ADJ_MAXSEG;
+        if (seg2 > ADJ_MAXSEG)
+            return fail(SDE_ERR_UNSUPPORTED, "the adjoint supports up to %d steps",
+                        ADJ_MAXSEG * ADJ_MAXSEG * ADJ_MAXSEG);
+    }
     const int nseg = (n_steps + seg - 1) / seg;
-    if (s->model != SDE_MODEL_LINEAR && nseg > ADJ_MAXSEG)
-        return fail(SDE_ERR_UNSUPPORTED, "the adjoint supports up to %d steps", ADJ_MAXSEG * ADJ_MAXSEG);
 
     std::lock_guard<std::mutex> lk(g_mu);
     Device *D;
@@ -1181,7 +1206,8 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     const size_t o_p0 = o_lam + al(sizeof(double) * njt), o_thr = o_p0 + al(sizeof(double) * njt);
     const size_t o_thr1 = o_thr + al(sizeof(long long) * njt);
     const size_t o_tk = o_thr1 + al(sizeof(long long) * njt);   // step starts, for user SDEs
-    const size_t o_end = o_tk + al(sizeof(R) * (user ? n_steps : 1));
+    const size_t o_pt = o_tk + al(sizeof(R) * (user ? n_steps : 1));   // slots 0..2 per step
+    const size_t o_end = o_pt + al(sizeof(R) * (td ? (size_t)n_steps * 3 * W : 1));
     D->host_tables.resize(o_end);
     char *H = D->host_tables.data();
     R *h_dt = (R *)(H + o_dt), *h_sq = (R *)(H + o_sq), *h_x0 = (R *)(H + o_x0), *h_prm = (R *)(H + o_prm);
@@ -1196,6 +1222,13 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     }
     for (int w = 0; w < W; ++w) h_x0[w] = (R)s->x0[w];
     for (int i = 0; i < SDE_MAX_PARAMS * W; ++i) h_prm[i] = (R)s->params[i];
+    if (td) {   // slots 0..2 of each step of the grid's [steps][SDE_MAX_PARAMS][W] table
+        R *h_pt = (R *)(H + o_pt);
+        for (int k = 0; k < n_steps; ++k)
+            for (int j = 0; j < 3; ++j)
+                for (int w = 0; w < W; ++w)
+                    h_pt[((size_t)k * 3 + j) * W + w] = (R)gr->params_t[((size_t)k * SDE_MAX_PARAMS + j) * W + w];
+    }
     if (jumps)
         for (int k = 0; k < n_steps; ++k)
             for (int w = 0; w < W; ++w) {
@@ -1231,6 +1264,7 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     a.n_steps = n_steps;
     a.seg = seg;
     a.nseg = nseg;
+    a.seg2 = seg2;
     a.step_offset = gr->step_offset;
     a.out_mode = s->out_mode;
     a.jump_law = s->jump_law;
@@ -1250,6 +1284,7 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
         a.uprog = *s->program;
         a.tk = (const R *)(T + o_tk);
     }
+    if (td) a.prm_t = (const R *)(T + o_pt);
     a.n_strikes = req->n_strikes;
     for (int i = 0; i < req->n_strikes; ++i) {
         a.strikes[i] = (R)req->strikes[i];
@@ -1269,8 +1304,13 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
         std::string err;
         if ((rc = jit_adj_kernel(*s->program, sizeof(R) == 8, maxm, &jk, &bps, &err))) return fail(rc, "%s", err.c_str());
     } else {
-        L = AdjFinder<R>::find(s->model, maxm, jumps, &bps);
-        if (!L) return fail(SDE_ERR_UNSUPPORTED, "no adjoint kernel for model %d group size %d", s->model, M);
+        L = td ? AdjFinder<R>::find_td(s->model, maxm, &bps) : AdjFinder<R>::find(s->model, maxm, jumps, &bps);
+        if (!L) return fail(SDE_ERR_UNSUPPORTED, "no adjoint kernel for model %d group size %d%s", s->model, M,
+                            td ? " with time-dependent parameters" : "");
+    }
+    if (td) {   // the per-step table lowers the resident blocks
+        const int by_smem = (int)(ADJ_TD_SMEM_SM / (td_smem + 1024));
+        if (by_smem < bps) bps = by_smem < 1 ? 1 : by_smem;
     }
     const int nbx = path_blocks(D, s->paths, s->groups, bps);
     const int npa = maxm * NGV + 2;
@@ -1278,6 +1318,13 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     if ((rc = scratch(D, S_PART, sizeof(double) * (size_t)s->groups * nbx * npa, &part))) return rc;
     if ((rc = scratch(D, S_RES, sizeof(double) * (size_t)s->groups * npa, &res))) return rc;
     a.partials = (double *)part;
+    const int ntd = td ? n_steps * 3 * maxm : 0;
+    void *tdpart = nullptr, *tdres = nullptr;
+    if (td) {
+        if ((rc = scratch(D, S_VALS, sizeof(double) * (size_t)s->groups * nbx * ntd, &tdpart))) return rc;
+        if ((rc = scratch(D, S_EDGES64, sizeof(double) * (size_t)s->groups * ntd, &tdres))) return rc;
+        a.tdpart = (double *)tdpart;
+    }
     if (D->timing) CU(cudaEventRecord(D->ev[0], st));
     if (jk) {
         void *args[] = {(void *)&a};
@@ -1290,11 +1337,15 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     for (int g = 0; g < s->groups; ++g) {
         reduce_partials_kernel<<<npa, BLOCK, 0, st>>>((const double *)part + (size_t)g * nbx * npa, nbx, npa,
                                                      (double *)res + (size_t)g * npa);
+        if (td)
+            reduce_partials_kernel<<<ntd, BLOCK, 0, st>>>((const double *)tdpart + (size_t)g * nbx * ntd, nbx, ntd,
+                                                         (double *)tdres + (size_t)g * ntd);
     }
     CU(cudaGetLastError());
-    std::vector<double> h((size_t)s->groups * npa);
+    std::vector<double> h((size_t)s->groups * npa), htd((size_t)s->groups * ntd);
     int32_t herr = 0;
     CU(cudaMemcpyAsync(h.data(), res, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st));
+    if (td) CU(cudaMemcpyAsync(htd.data(), tdres, sizeof(double) * htd.size(), cudaMemcpyDeviceToHost, st));
     CU(cudaMemcpyAsync(&herr, d_err, sizeof herr, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
     if (D->timing) {
@@ -1314,14 +1365,19 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
         v += h[(size_t)g * npa + maxm * NGV];
     }
     if (value) *value = v * inv;
+    if (td)   // grad_t[k][j][w], w = g * M + m
+        for (int g = 0; g < s->groups; ++g)
+            for (int k = 0; k < n_steps; ++k)
+                for (int j = 0; j < 3; ++j)
+                    for (int m = 0; m < M; ++m)
+                        req->grad_t[((size_t)k * 3 + j) * W + (size_t)g * M + m] =
+                            htd[(size_t)g * ntd + ((size_t)k * 3 + j) * maxm + m] * inv;
     return SDE_OK;
 }
 
 extern "C" int32_t sde_adjoint(const SdeSpec *spec, const SdeGrid *grid, const SdeAdjReq *req, double *grad,
                                double *value) {
     if (!spec) return fail(SDE_ERR_INVALID, "spec is NULL");
-    if (grid && grid->params_t)
-        return fail(SDE_ERR_UNSUPPORTED, "the adjoint takes constant parameters (grid params_t must be NULL)");
     if (grid && grid->corr_t)
         return fail(SDE_ERR_UNSUPPORTED, "the adjoint takes a constant correlation (grid corr_t must be NULL)");
     if (spec->flags) return fail(SDE_ERR_UNSUPPORTED, "the adjoint takes no spec flags (antithetic paths)");

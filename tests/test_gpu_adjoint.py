@@ -199,3 +199,136 @@ def test_cir_adjoint_vs_fd(lib):
     grad, _ = adjoint(lib, sg.cox_ingersoll_ross_process, tl, steps, paths, [], [], 1., 7, 1, **kw)
     assert abs(x0.grad.item() - grad[0, 0]) <= 1e-12*max(1., abs(grad[0, 0]))
     assert abs(xi.grad.item() - grad[0, 3]) <= 1e-12*max(1., abs(grad[0, 3]))
+
+
+HES = dict(x0=100., mu=.02, y0=.04, k=1.5, theta=.04, xi=.5, rho=-.7)
+
+
+@pytest.mark.parametrize('dtype', [np.float64, np.float32], ids=['fp64', 'fp32'])
+def test_two_level_checkpoints_reproduce_one_level(lib, dtype):
+    """Recomputed states are the original ones bit for bit, so the gradient
+    does not depend on where the checkpoints fall: a checkpoint length that
+    needs more than 64 level-1 segments switches to two levels (level 1
+    every ceil(steps / 64) steps, level 2 inside), with the same result."""
+    tl, steps, paths = (0., 1.), 1000, 4099
+    one, v1 = adjoint(lib, sg.heston_process, tl, steps, paths, [95., 105.], [.5, .5], .1, 5, 2,
+                      dtype=dtype, **HES)
+    two, v2 = adjoint(lib, sg.heston_process, tl, steps, paths, [95., 105.], [.5, .5], .1, 5, 2,
+                      dtype=dtype, checkpoint=10, **HES)
+    np.testing.assert_array_equal(one, two)
+    assert v1 == v2
+
+
+def test_adjoint_beyond_4096_steps(lib):
+    """An OU run of 5000 steps (two checkpoint levels): the gradient of
+    E[X_T] w.r.t. x0 and theta is the Euler recursion's own, path by path:
+    prod(1 - k dt) and 1 - prod(1 - k dt)."""
+    k, theta, sigma, steps = 1.3, .4, .3, 5000
+    tl = (0., 2.)
+    grad, val = adjoint(lib, sg.ornstein_uhlenbeck_process, tl, steps, 2048, [], [], 1., 9, 1,
+                        x0=.1, k=k, theta=theta, sigma=sigma)
+    dt = np.diff(Grid(tl, steps).legs[-1].tt)
+    decay = np.prod(1 - k*dt)
+    np.testing.assert_allclose(grad[0, 0], decay, rtol=1e-12)
+    np.testing.assert_allclose(grad[0, 2], 1 - decay, rtol=1e-10)
+    est = estimate(sg.ornstein_uhlenbeck_process, tl, steps, 2048, [], 9, 1, x0=.1, k=k, theta=theta, sigma=sigma)
+    assert abs(val - est[0]) < 1e-12*max(1., abs(est[0]))
+
+
+def adjoint_t(lib, P, timeline, strikes, weights, wmean, seed, stream):
+    """sde_adjoint with the process's time-dependent parameter table: the
+    per-variable slots and the per-step gradients [steps][3][W]."""
+    leg = Grid(timeline, P.steps).legs[-1]
+    g = _lib.SdeGrid()
+    g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
+    g.n_pts, g.step_offset = leg.tt.size, 0
+    ptab = P._params_table(leg) if P._tdep else \
+        np.ascontiguousarray(np.broadcast_to(P._prm, (leg.tt.size - 1,) + P._prm.shape))
+    g.params_t = _lib.dptr(ptab)
+    req = _lib.SdeAdjReq()
+    req.n_strikes, req.checkpoint, req.mean_weight = len(strikes), 0, wmean
+    for i, (K, w) in enumerate(zip(strikes, weights)):
+        req.strikes[i], req.weights[i] = K, w
+    grad_t = np.zeros((leg.tt.size - 1, 3, P._W))
+    req.grad_t = _lib.dptr(grad_t)
+    spec = P._make_spec(seed, stream)
+    grad = np.zeros((P._W, 8))
+    val = C.c_double()
+    _lib.check(lib.sde_adjoint(C.byref(spec), C.byref(g), C.byref(req), _lib.dptr(grad), C.byref(val)),
+               'sde_adjoint')
+    return grad, grad_t, val.value, leg
+
+
+@pytest.mark.parametrize('case', ['ou', 'cir', 'heston', 'lognorm'])
+def test_per_step_gradients_sum_to_constant_gradients(lib, case):
+    """A constant parameter given as a per-step table: the per-step
+    gradients of each slot sum to the constant-parameter gradient of that
+    slot (the kernels without the table), in FP64."""
+    cls, kw, strikes = {
+        'ou': (sg.ornstein_uhlenbeck_process, dict(vshape=2, x0=.1, k=[[1.2], [.7]], theta=[[.3], [-.2]], sigma=.4), []),
+        'cir': (sg.cox_ingersoll_ross_process, dict(x0=.04, k=1.5, theta=.05, xi=.3), [.04]),
+        'heston': (sg.heston_process, HES, [100.]),
+        'lognorm': (sg.lognorm_process, LN, [1.05]),
+    }[case]
+    tl, steps, paths, seed = (0., 1.), 60, 2053, 17
+    P = cls(paths=paths, steps=steps, rng=sg.philox_rng(seed, 1), **kw)
+    grad, gt, val, leg = adjoint_t(lib, P, tl, strikes, [1.]*len(strikes), .5, seed, 1)
+    ref, vref = adjoint(lib, cls, tl, steps, paths, strikes, [1.]*len(strikes), .5, seed, 1, **kw)
+    assert abs(val - vref) <= 1e-12*max(1., abs(vref))
+    np.testing.assert_allclose(grad[:, 0], ref[:, 0], rtol=1e-10, atol=1e-14)   # x0
+    np.testing.assert_allclose(gt.sum(axis=0).T, ref[:, 1:4], rtol=1e-9, atol=1e-12)
+
+
+def test_per_step_gradients_of_a_time_dependent_theta(lib):
+    """OU with theta(t) = a + b t: d E[X_T] / d(a, b) from the per-step
+    gradients by the chain rule, against the Euler recursion's own
+    derivative (E[X_T] is linear in theta) and central differences on the
+    same paths."""
+    a0, b0, k, steps, paths, seed = .3, .5, 1.4, 80, 4096, 23
+    tl = (0., 2.)
+
+    def proc(a, b):
+        return sg.ornstein_uhlenbeck_process(paths=paths, steps=steps, x0=.2, k=k, sigma=.3,
+                                             theta=lambda t: a + b*t, rng=sg.philox_rng(seed, 2))
+    P = proc(a0, b0)
+    grad, gt, val, leg = adjoint_t(lib, P, tl, [], [], 1., seed, 2)
+    tk = leg.tt[:-1]
+    da, db = gt[:, 1, 0].sum(), (gt[:, 1, 0]*tk).sum()
+    # the recursion: x_N = ... + sum_k k dt_k theta_k prod_{j > k} (1 - k dt_j)
+    dt = np.diff(leg.tt)
+    w = k*dt*np.array([np.prod(1 - k*dt[i + 1:]) for i in range(dt.size)])
+    np.testing.assert_allclose(gt[:, 1, 0], w, rtol=1e-10)
+    np.testing.assert_allclose((da, db), (w.sum(), (w*tk).sum()), rtol=1e-10)
+
+    def mean(a, b):
+        return float(np.asarray(proc(a, b).montecarlo(tl, bins=None).mean()).reshape(-1)[0])
+    h = 1e-4
+    fa = (mean(a0 + h, b0) - mean(a0 - h, b0))/(2*h)
+    fb = (mean(a0, b0 + h) - mean(a0, b0 - h))/(2*h)
+    np.testing.assert_allclose((da, db), (fa, fb), rtol=1e-6)
+
+
+def test_per_step_gradients_heston_xi_vs_differences(lib):
+    """Heston with xi(t) = xi0 (1 + t/2): the chain rule over the per-step
+    gradients of xi against central differences in xi0 on the same paths.
+    The parameters keep the variance away from 0 (2 k theta > xi(t)^2):
+    where it reaches 0 the pathwise derivatives of sqrt(y+) are unbounded
+    and their mean need not be the derivative of the expectation."""
+    tl, steps, paths, seed = (0., 1.), 50, 2**15, 31
+    xi0 = .2
+    kw = dict(x0=100., mu=.02, y0=.06, k=3., theta=.06, rho=-.7)
+
+    def proc(x):
+        return sg.heston_process(paths=paths, steps=steps, xi=lambda t: x*(1 + t/2), rng=sg.philox_rng(seed, 4), **kw)
+    P = proc(xi0)
+    grad, gt, val, leg = adjoint_t(lib, P, tl, [100.], [1.], .3, seed, 4)
+    tk = leg.tt[:-1]
+    dxi0 = (gt[:, 2, 1]*(1 + tk/2)).sum()   # the variance state's slot 2 is xi
+
+    def value(x):
+        mc = proc(x).montecarlo(tl, bins=None, strikes=[100.])
+        return .3*float(np.asarray(mc.mean()).reshape(-1)[0]) + float(np.asarray(mc.payoff).reshape(-1)[0])
+    h = 1e-4*xi0
+    fd_ = (value(xi0 + h) - value(xi0 - h))/(2*h)
+    assert abs(val - value(xi0)) <= 1e-11*abs(val)
+    np.testing.assert_allclose(dxi0, fd_, rtol=2e-3)
