@@ -21,6 +21,15 @@ Differentiable parameters per preset:
                              device runs the traced program in tangent mode)
 Poisson intensities and the Kou probability pa select integer / discrete
 outcomes and are not differentiated.
+
+Time-dependent parameters (the presets without jumps): a parameter may be a
+function of time, evaluated at each Euler step's start as sdepy evaluates
+callable parameters.  When the function returns a torch tensor for a torch
+tensor of times -- ``theta=lambda t: a + b*t`` with ``a``, ``b`` requiring
+grad -- the backward pass gets the gradient of every step's parameter value
+from the adjoint kernel (SdeAdjReq.grad_t) and torch carries it to ``a`` and
+``b`` through the function.  Constant parameters then receive the sum of
+their per-step gradients.
 """
 import ctypes as C
 
@@ -113,15 +122,34 @@ class _Expectation(torch.autograd.Function):
         spec = proc._make_spec(seed, stream)
         grad = np.zeros((proc._W, 8))
         val = C.c_double()
+        name = type(proc).__name__
+        td = bool(proc._tdep)
+        if td:   # per-step slot gradients of the time-dependent table
+            ptab = proc._params_table(leg)
+            g.params_t = _lib.dptr(ptab)
+            gt = np.zeros((leg.tt.size - 1, 3, proc._W))
+            req.grad_t = _lib.dptr(gt)
         st = lib.sde_adjoint(C.byref(spec), C.byref(g), C.byref(req),
                              _lib.dptr(grad), C.byref(val))
         _lib.check(st, 'sde_adjoint')
-        mp = ctx.mp if ctx.mp is not None else _MAP[type(proc).__name__]
-        vals = {k: float(np.asarray(v)) for k, v in proc.args.items() if k in mp}
-        pg = _param_grads(type(proc).__name__, grad, vals, ctx.mp, getattr(proc, '_log', False))
+        mp = ctx.mp if ctx.mp is not None else _MAP[name]
+        vals = {k: float(np.asarray(v)) for k, v in proc.args.items() if k in mp and not callable(v)}
+        if td:
+            # initial states (slot 0) and rho from the per-variable slots;
+            # every slot parameter from its per-step gradients (summed for a
+            # constant one)
+            pg = {p: grad[w, j] for p, (w, j) in mp.items() if j in (0, 7)}
+            if name in ('lognorm_process', 'heston_process'):
+                pg['x0'] = grad[0, 0]/float(np.asarray(proc.args['x0']))   # state log x0
+            for k, v in _step_grads(name, gt, proc, leg).items():
+                pg[k] = v if callable(proc.args.get(k)) else float(v.sum())
+        else:
+            pg = _param_grads(name, grad, vals, ctx.mp, getattr(proc, '_log', False))
         outs = []
         for n, shp, dt in zip(ctx.names, ctx.shapes, ctx.dtypes):
-            outs.append(torch.full(shp, pg[n], dtype=dt))
+            v = pg[n]
+            outs.append(torch.tensor(np.broadcast_to(v, shp), dtype=dt) if np.ndim(v) else
+                        torch.full(shp, v, dtype=dt))
         return (None, None, None) + tuple(outs)
 
 
@@ -157,9 +185,29 @@ def expectation(cls, timeline, strikes=(), *, paths, steps=None,
     if any(k in plain for k in ('dw', 'dj', 'dn')):
         raise NotImplementedError('gradients are taken on the default device sources '
                                   '(no explicit, injected or antithetic sources)')
-    if any(callable(v) for v in plain.values()):
-        raise NotImplementedError('gradients need constant parameters (the adjoint '
-                                  'kernel takes no time-dependent parameters)')
+    # time-dependent parameters: a torch-valued function of time is evaluated
+    # at the steps' starts as a torch tensor (the input whose gradient the
+    # backward pass returns) and handed to the process as a numpy function
+    tdep = [k for k, v in plain.items() if callable(v)]
+    if tdep:
+        if mp is not None or name in ('merton_jumpdiff_process', 'kou_jumpdiff_process') or \
+                name not in _TD_SLOTS:
+            raise NotImplementedError('gradients with time-dependent parameters take the preset '
+                                      'models without jumps')
+        bad = [k for k in tdep if k not in _TD_SLOTS[name]]
+        if bad:
+            raise NotImplementedError('{} cannot depend on time here'.format(bad))
+        tk = Grid(timeline, steps, 0).legs[-1].tt[:-1]
+        t_torch = torch.as_tensor(tk, dtype=torch.float64)
+        for k in tdep:
+            f = plain[k]
+            v = f(t_torch)
+            if isinstance(v, torch.Tensor):
+                vals = torch.broadcast_to(v.to(torch.float64), t_torch.shape)
+                if vals.requires_grad:
+                    names.append(k)
+                    tensors.append(vals)
+                plain[k] = _numpy_of(f)
 
     def spec_fn(run=True):
         P = cls(paths=paths, steps=steps, dtype=dtype,
@@ -173,3 +221,36 @@ def expectation(cls, timeline, strikes=(), *, paths, steps=None,
         return P, grid, strikes, seed, stream, value
 
     return _Expectation.apply(spec_fn, tuple(names), mp, *tensors)
+
+
+def _numpy_of(f):
+    """A torch function of time as the numpy function a process evaluates."""
+    def g(t):
+        v = f(torch.as_tensor(np.asarray(t, dtype=float), dtype=torch.float64))
+        return v.detach().cpu().numpy() if isinstance(v, torch.Tensor) else v
+    return g
+
+
+# per-step slots of the time-dependent adjoint: parameter -> (state, slot)
+_TD_SLOTS = {
+    'wiener_process': {'mu': (0, 0), 'sigma': (0, 1)},
+    'lognorm_process': {'mu': (0, 0), 'sigma': (0, 1)},
+    'ornstein_uhlenbeck_process': {'k': (0, 0), 'theta': (0, 1), 'sigma': (0, 2)},
+    'cox_ingersoll_ross_process': {'k': (0, 0), 'theta': (0, 1), 'xi': (0, 2)},
+    'heston_process': {'mu': (0, 0), 'sigma': (0, 1), 'k': (1, 0), 'theta': (1, 1), 'xi': (1, 2)},
+}
+
+
+def _step_grads(name, gt, proc, leg):
+    """Per-step gradients of each user parameter (numpy [steps]) from the
+    slot gradients gt[steps][3][W]; lognormal slots are mu - sigma^2/2 and
+    sigma."""
+    out = {}
+    for p, (w, j) in _TD_SLOTS[name].items():
+        out[p] = gt[:, j, w].copy()
+    if name == 'lognorm_process':
+        ptab = proc._params_table(leg) if proc._tdep else \
+            np.broadcast_to(proc._prm, (leg.tt.size - 1,) + proc._prm.shape)
+        sig = ptab[:, 1, 0]
+        out['sigma'] = -sig*gt[:, 0, 0] + gt[:, 1, 0]
+    return out

@@ -150,9 +150,51 @@ def test_host_wiener_source_reproduces_reference_correlated_draws(name):
 
 
 @pytest.mark.gpu
-def test_adjoint_refuses_time_dependent_parameters(lib):
+def test_adjoint_refuses_time_dependent_parameters_with_jumps(lib):
     from sdepy_gb300.autograd import expectation
     import torch
     with pytest.raises(NotImplementedError):
-        expectation(sg.lognorm_process, (0., 1.), [], paths=100, steps=10,
-                    x0=torch.tensor(1., requires_grad=True), mu=TDEP['tdep_mu'], sigma=.2)
+        expectation(sg.merton_jumpdiff_process, (0., 1.), [], paths=100, steps=10,
+                    x0=torch.tensor(1., requires_grad=True), mu=TDEP['tdep_mu'], sigma=.2,
+                    lam=1., a=-.1, b=.1)
+
+
+@pytest.mark.gpu
+def test_autograd_through_time_dependent_parameters(lib):
+    """expectation() with torch functions of time: theta(t) = a + b t for
+    OU, mu(t) = m0 + m1 t for the lognormal; the gradients of a, b, m0, m1
+    and of the constant tensors against central differences on the same
+    paths (FP64)."""
+    from sdepy_gb300.autograd import expectation
+    import torch
+    tl, steps, paths = (0., 2.), 60, 2**14
+
+    def ou(a, b, k, strikes=(.3,)):
+        return expectation(sg.ornstein_uhlenbeck_process, tl, list(strikes), paths=paths, steps=steps,
+                           dtype=np.float64, seed=5, x0=.1, k=k, sigma=.3, theta=lambda t: a + b*t)
+    a, b, k = (torch.tensor(v, dtype=torch.float64, requires_grad=True) for v in (.2, .3, 1.2))
+    out = ou(a, b, k)
+    (out[0] + out[1]).backward()
+    h = 1e-5
+    for t, name in ((a, 'a'), (b, 'b'), (k, 'k')):
+        vals = {'a': .2, 'b': .3, 'k': 1.2}
+        up, dn = dict(vals), dict(vals)
+        up[name] += h
+        dn[name] -= h
+        fu = ou(up['a'], up['b'], up['k'])
+        fd_ = (float(fu[0] + fu[1]) - float(sum(ou(dn['a'], dn['b'], dn['k']))))/(2*h)
+        np.testing.assert_allclose(float(t.grad), fd_, rtol=2e-4, err_msg=name)
+
+    def ln(m0, m1, s):
+        return expectation(sg.lognorm_process, (0., 1.), [1.05], paths=paths, steps=50, dtype=np.float64,
+                           seed=6, x0=1., sigma=s, mu=lambda t: m0 + m1*t)
+    m0, m1, s = (torch.tensor(v, dtype=torch.float64, requires_grad=True) for v in (.03, .04, .2))
+    out = ln(m0, m1, s)
+    out.sum().backward()
+    for t, name in ((m0, 'm0'), (m1, 'm1'), (s, 's')):
+        vals = {'m0': .03, 'm1': .04, 's': .2}
+        up, dn = dict(vals), dict(vals)
+        up[name] += h
+        dn[name] -= h
+        fd_ = (float(ln(up['m0'], up['m1'], up['s']).sum()) - float(ln(dn['m0'], dn['m1'], dn['s']).sum()))/(2*h)
+        np.testing.assert_allclose(float(t.grad), fd_, rtol=2e-4, err_msg=name)
