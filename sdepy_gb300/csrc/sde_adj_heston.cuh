@@ -1,0 +1,194 @@
+// The FP32 adjoint of the 2-variable Heston model (constant parameters, no
+// jumps, one checkpoint level): the gradient of configs like E[max(S_T - K,
+// 0)] w.r.t. x0, mu, sigma, y0, k, theta, xi and rho.
+//
+// It computes what sde_adj_kernel<float, HESTON, 2> computes -- the same
+// checkpoints every `seg` steps, the same recomputed segments and the same
+// backward recursion -- with the segment's values in shared memory instead of
+// per-thread local arrays, and the step loop written like the forward table
+// kernel (sde_tab.cuh): parameters and Philox keys in registers or
+// constant-bank operands, no reference to the parameter block handed to a
+// helper.  Per step the recomputation stores the variance before the step
+// and the two normals (3 floats, [seg][3][BLOCK] so that a warp's stores
+// are contiguous); the backward pass rebuilds the correlated increments from
+// the normals with the forward's arithmetic, so they are the forward's bit
+// for bit.  Only the eight slots the model has are accumulated (Kahan, per
+// thread), then reduced per block into sde_adj_kernel's partial layout.
+#pragma once
+
+#include "sde_adjoint.cuh"
+
+namespace sdegpu {
+
+static __global__ void __launch_bounds__(BLOCK, 3) sde_adj_heston_kernel(const __grid_constant__ AdjArgs<float> a) {
+    typedef Ar<float> A;
+    constexpr int NPA = 2 * NGV + 2;
+    extern __shared__ float hbuf[];   // [seg][3][BLOCK]: y, z0, z1
+    __shared__ float red[BLOCK / 32];
+    __shared__ float ks[SDE_MAX_STRIKES], kw[SDE_MAX_STRIKES];
+    const int g = blockIdx.y;
+    const int W = a.W;
+    const PhiloxKey key = a.key;
+    const uint32_t step_offset = a.step_offset;
+    const int seg = a.seg, nseg = a.nseg, n_steps = a.n_steps;
+    // the group's parameters: x (mu, sigma), y (k, theta, xi)
+    const float x0a = a.x0[g * 2], x0b = a.x0[g * 2 + 1];
+    const float mu = a.prm[g * 2], sg = a.prm[W + g * 2];
+    const float kk = a.prm[g * 2 + 1], th = a.prm[W + g * 2 + 1], xi = a.prm[2 * W + g * 2 + 1];
+    const float L00 = a.has_corr ? a.chol[0] : 1.f, L10 = a.has_corr ? a.chol[1] : 0.f,
+                L11 = a.has_corr ? a.chol[2] : 1.f;
+    const bool corr = a.has_corr != 0, rho_grad = a.rho_grad != 0, out_xy = a.out_mode == SDE_OUT_HESTON_XY;
+    const float rho_k = a.rho_k, wmean = a.wmean;
+    const int n_strikes = a.n_strikes;
+#pragma unroll
+    for (int i = 0; i < SDE_MAX_STRIKES; ++i)   // constant indices: no parameter address
+        if (threadIdx.x == i) {
+            ks[i] = a.strikes[i];
+            kw[i] = a.weights[i];
+        }
+    __syncthreads();
+    auto fval = [&](float X) {
+        float v = wmean * X;
+        for (int s = 0; s < n_strikes; ++s) v += kw[s] * fmaxf(X - ks[s], 0.f);
+        return v;
+    };
+    auto fder = [&](float X) {
+        float d = wmean;
+        for (int s = 0; s < n_strikes; ++s)
+            if (X > ks[s]) d += kw[s];
+        return d;
+    };
+    // the correlated increments of a step from its normals (correlate())
+    auto incr = [&](float z0, float z1, float sq, float &dWx, float &dWy) {
+        if (corr) {
+            dWx = (L00 * z0) * sq;
+            dWy = fmaf(L11, z1, L10 * z0) * sq;
+        } else {
+            dWx = z0 * sq;
+            dWy = z1 * sq;
+        }
+    };
+    // one Euler step (fwd_step<float, HESTON, 2>)
+    auto step = [&](float dt, float dWx, float dWy, float &x, float &y) {
+        const float yp = fmaxf(y, 0.f);
+        const float sqy = A::sqrt_(yp);
+        const float adt = A::sub(mu, A::mul(A::mul(A::mul(sg, sg), yp), 0.5f));
+        const float nx = A::add(x, A::add(A::mul(adt, dt), A::mul(A::mul(sg, sqy), dWx)));
+        const float bdt = A::mul(kk, A::sub(th, yp));
+        const float ny = A::add(y, A::add(A::mul(bdt, dt), A::mul(A::mul(xi, sqy), dWy)));
+        x = nx;
+        y = ny;
+    };
+
+    // Kahan sums of the slots: x0, mu, sigma, rho | y0, k, theta, xi, and the value
+    float acc[9], cmp[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) acc[i] = cmp[i] = 0.f;
+    const int64_t stride = (int64_t)gridDim.x * BLOCK;
+    for (int64_t p = (int64_t)blockIdx.x * BLOCK + threadIdx.x; p < a.paths; p += stride) {
+        const PathPre<1> pre(key, (uint32_t)p + a.path_offset, (uint32_t)g, a.stream);
+        PairedSteps<float, 2> pair;
+        float ck[ADJ_MAXSEG][2];
+        float x = x0a, y = x0b;
+        for (int k = 0, kc = 0, ci = 0; k < n_steps; ++k) {
+            if (kc == 0) {   // a checkpoint every seg steps
+                ck[ci][0] = x;
+                ck[ci][1] = y;
+                ++ci;
+            }
+            kc = kc + 1 == seg ? 0 : kc + 1;
+            float z0, z1, dWx, dWy;
+            pair.get(key, pre, k, step_offset, z0, z1);
+            incr(z0, z1, __ldg(a.sqdt + k), dWx, dWy);
+            step(__ldg(a.dt + k), dWx, dWy, x, y);
+        }
+        // terminal adjoint (HESTON_X: f(exp(x)); HESTON_XY adds f(y))
+        const float X = A::exp_(x);
+        float val = fval(X);
+        float xbx = fder(X) * X, xby = 0.f;
+        if (out_xy) {
+            val += fval(y);
+            xby = fder(y);
+        }
+        float gmu = 0.f, gsg = 0.f, grho = 0.f, gk = 0.f, gth = 0.f, gxi = 0.f;
+        for (int s = nseg - 1; s >= 0; --s) {
+            const int k0 = s * seg, k1 = min(k0 + seg, n_steps);
+            float sx = ck[s][0], sy = ck[s][1];
+            for (int k = k0; k < k1; ++k) {
+                float z0, z1, dWx, dWy;
+                pair.get(key, pre, k, step_offset, z0, z1);
+                float *b = hbuf + (k - k0) * 3 * BLOCK + threadIdx.x;
+                b[0] = sy;
+                b[BLOCK] = z0;
+                b[2 * BLOCK] = z1;
+                incr(z0, z1, __ldg(a.sqdt + k), dWx, dWy);
+                step(__ldg(a.dt + k), dWx, dWy, sx, sy);
+            }
+            for (int k = k1 - 1; k >= k0; --k) {
+                const float *b = hbuf + (k - k0) * 3 * BLOCK + threadIdx.x;
+                const float yv = b[0], z0 = b[BLOCK], z1 = b[2 * BLOCK];
+                const float dt = __ldg(a.dt + k), sq = __ldg(a.sqdt + k);
+                float dWx, dWy;
+                incr(z0, z1, sq, dWx, dWy);
+                const float yp = fmaxf(yv, 0.f);
+                const float sr = A::sqrt_(yp);
+                const float ab = xbx, ybn = xby;
+                gmu += ab * dt;
+                gsg += ab * (sr * dWx - sg * yp * dt);
+                gk += ybn * (th - yp) * dt;
+                gth += ybn * kk * dt;
+                gxi += ybn * sr * dWy;
+                if (rho_grad) grho += ybn * xi * sr * ((z0 + rho_k * z1) * sq);
+                float ny = ybn;
+                if (yv > 0.f && sr > 0.f) {
+                    const float inv = 0.5f / sr;
+                    const float dadyp = -sg * sg * dt * 0.5f + sg * dWx * inv;
+                    const float dydyp = -kk * dt + xi * dWy * inv;
+                    ny = ybn + ab * dadyp + ybn * dydyp;
+                }
+                xby = ny;
+            }
+        }
+        kahan_add(acc[0], cmp[0], xbx);
+        kahan_add(acc[1], cmp[1], gmu);
+        kahan_add(acc[2], cmp[2], gsg);
+        kahan_add(acc[3], cmp[3], grho);
+        kahan_add(acc[4], cmp[4], xby);
+        kahan_add(acc[5], cmp[5], gk);
+        kahan_add(acc[6], cmp[6], gth);
+        kahan_add(acc[7], cmp[7], gxi);
+        kahan_add(acc[8], cmp[8], val);
+    }
+    // block reduction into sde_adj_kernel's partial layout: slot j of state
+    // m at m * NGV + j, the value at 2 * NGV, then a zero
+    const int slot[9] = {0, 1, 2, 7, NGV + 0, NGV + 1, NGV + 2, NGV + 3, 2 * NGV};
+    double *dst = a.partials + ((int64_t)g * gridDim.x + blockIdx.x) * NPA;
+    if (threadIdx.x < NPA) dst[threadIdx.x] = 0.0;
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const float v = block_sum<float>(acc[i] - cmp[i], red);
+        if (threadIdx.x == 0) dst[slot[i]] = (double)v;
+    }
+}
+
+#ifndef __CUDACC_RTC__
+// the segment buffer's bytes: 3 floats per step and thread
+static inline size_t adj_heston_smem(int seg) { return sizeof(float) * 3 * (size_t)seg * BLOCK; }
+
+static inline void launch_adj_heston(const AdjArgs<float> &a, dim3 grid, cudaStream_t s) {
+    const size_t smem = adj_heston_smem(a.seg);
+    cudaFuncSetAttribute(sde_adj_heston_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    sde_adj_heston_kernel<<<grid, BLOCK, smem, s>>>(a);
+}
+
+static inline int adj_heston_max_blocks_per_sm(int seg) {
+    int n = 0;
+    cudaFuncSetAttribute(sde_adj_heston_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)adj_heston_smem(seg));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sde_adj_heston_kernel, BLOCK, adj_heston_smem(seg));
+    return n;
+}
+#endif
+
+}  // namespace sdegpu

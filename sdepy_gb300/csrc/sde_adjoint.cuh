@@ -30,6 +30,9 @@ constexpr int ADJ_MAXSEG = 64;  // checkpoints and steps per segment
 // (steps x 3 x group width x sizeof(R)), and the SM's share for the table
 constexpr size_t ADJ_TD_SMEM = 160 * 1024;
 constexpr size_t ADJ_TD_SMEM_SM = 220 * 1024;
+// steps per segment of the FP32 Heston adjoint that keep three 256-thread
+// blocks per SM (3 floats per step and thread in shared memory)
+constexpr int ADJ_HESTON_SEG = 24;
 
 template <typename R>
 struct AdjArgs {
@@ -723,6 +726,10 @@ int adj_max_blocks_per_sm() {
 
 AdjLauncher<float> find_adj_f32(int model, int maxm, bool jumps, int *bps);
 AdjLauncher<double> find_adj_f64(int model, int maxm, bool jumps, int *bps);
+// the FP32 2-variable Heston adjoint with its segment in shared memory
+// (sde_adj_heston.cuh, in adj_f32.cu): constant parameters, no jumps, one
+// checkpoint level of at most ADJ_HESTON_SEG steps per segment
+AdjLauncher<float> find_adj_heston_f32(int seg, int *bps);
 // time-dependent parameter slots, no jumps (adj_td.cu); the occupancy
 // returned is for the kernel without its per-step table
 AdjLauncher<float> find_adj_td_f32(int model, int maxm, int *bps);

@@ -1130,6 +1130,7 @@ template <> struct AdjFinder<float> {
         return find_adj_f32(model, maxm, jumps, bps);
     }
     static AdjLauncher<float> find_td(int model, int maxm, int *bps) { return find_adj_td_f32(model, maxm, bps); }
+    static AdjLauncher<float> find_heston(int seg, int *bps) { return find_adj_heston_f32(seg, bps); }
 };
 template <> struct AdjFinder<double> {
     static AdjLauncher<double> find(int model, int maxm, bool jumps, int *bps) {
@@ -1137,6 +1138,7 @@ template <> struct AdjFinder<double> {
         return find_adj_f64(model, maxm, jumps, bps);
     }
     static AdjLauncher<double> find_td(int model, int maxm, int *bps) { return find_adj_td_f64(model, maxm, bps); }
+    static AdjLauncher<double> find_heston(int, int *) { return nullptr; }
 };
 
 template <typename R>
@@ -1189,6 +1191,11 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
             return fail(SDE_ERR_UNSUPPORTED, "the adjoint supports up to %d steps",
                         ADJ_MAXSEG * ADJ_MAXSEG * ADJ_MAXSEG);
     }
+    // the FP32 2-variable Heston adjoint keeps its segment in shared memory:
+    // segments of at most ADJ_HESTON_SEG steps (one checkpoint level)
+    const bool heston_fast = sizeof(R) == 4 && s->model == SDE_MODEL_HESTON && M == 2 && !jumps && !td &&
+                             seg2 == seg && (n_steps + ADJ_HESTON_SEG - 1) / ADJ_HESTON_SEG <= ADJ_MAXSEG;
+    if (heston_fast && seg > ADJ_HESTON_SEG) seg = seg2 = ADJ_HESTON_SEG;
     const int nseg = (n_steps + seg - 1) / seg;
 
     std::lock_guard<std::mutex> lk(g_mu);
@@ -1303,6 +1310,8 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     if (user && s->program->jit) {
         std::string err;
         if ((rc = jit_adj_kernel(*s->program, sizeof(R) == 8, maxm, &jk, &bps, &err))) return fail(rc, "%s", err.c_str());
+    } else if (heston_fast) {
+        L = AdjFinder<R>::find_heston(seg, &bps);
     } else {
         L = td ? AdjFinder<R>::find_td(s->model, maxm, &bps) : AdjFinder<R>::find(s->model, maxm, jumps, &bps);
         if (!L) return fail(SDE_ERR_UNSUPPORTED, "no adjoint kernel for model %d group size %d%s", s->model, M,
