@@ -499,6 +499,91 @@ def heston_gradient_check(lib, batches=16, paths=2**18, steps=500):
     return out
 
 
+def _fused(lib, P, timeline, strikes, seed):
+    """One forward run of process P with the fused summary (moments and
+    call payoffs) of the last timeline point; no path written."""
+    import ctypes as C
+    from sdepy_gb300 import _lib
+    from sdepy_gb300.grid import Grid
+    leg = Grid(timeline, P.steps).legs[-1]
+    g = _lib.SdeGrid()
+    g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
+    g.n_pts, g.step_offset = leg.tt.size, 0
+    o = _lib.SdeOut()
+    o.xx, o.n_rows, o.on_device = None, len(timeline), 0
+    ptab = P._params_table(leg) if P._tdep else None          # time-dependent parameters
+    ctab = P._corr_table(leg) if P._corr_tdep else None       # and correlations
+    ltab = P._lam_table(leg)                                  # a user SDE's intensity
+    g.params_t, g.corr_t, g.lam_t = _lib.dptr(ptab), _lib.dptr(ctab), _lib.dptr(ltab)
+    req, so, arrs = P._stats_request(dict(row=len(timeline) - 1, bins=0, range=None, strikes=strikes))
+    spec = P._make_spec(seed, 0)
+    _lib.check(lib.sde_run_stats(C.byref(spec), C.byref(g), None, C.byref(o), C.byref(req), C.byref(so)), 'fwd')
+    return arrs, leg
+
+
+def _adjoint_ms(lib, P, timeline, strike):
+    """Device time of one adjoint call (mean and one call payoff of the last
+    timeline point) of process P."""
+    import ctypes as C
+    from sdepy_gb300 import _lib
+    from sdepy_gb300.grid import Grid
+    leg = Grid(timeline, P.steps).legs[-1]
+    g = _lib.SdeGrid()
+    g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
+    g.n_pts, g.step_offset = leg.tt.size, 0
+    ltab = P._lam_table(leg)
+    g.lam_t = _lib.dptr(ltab)
+    req = _lib.SdeAdjReq()
+    req.n_strikes, req.checkpoint, req.mean_weight = 1, 0, 1.
+    req.strikes[0], req.weights[0] = strike, 1.
+    grad = np.zeros((P._W, 8))
+    v = C.c_double()
+
+    def call():
+        spec = P._make_spec(8, 0)
+        _lib.check(lib.sde_adjoint(C.byref(spec), C.byref(g), C.byref(req), _lib.dptr(grad), C.byref(v)), 'adj')
+    call()   # (a compiled program's first call compiles it)
+    return _time_call(call, lib)
+
+
+def user_adjoint_bench(lib, K=2**22):
+    """Adjoint against forward cost (mean and one call payoff, FP32, K
+    paths): user SDEs -- interpreted (tangent mode) and compiled
+    (reverse-mode kernel) OU, a compiled CEV, a compiled stochastic-
+    volatility system and a compiled Merton jump diffusion (dj term) --
+    beside the OU and Merton presets; 499 steps on (0, 2), 364 on (0, 1)
+    for the jump diffusions."""
+    import sdepy_gb300 as sg
+    ou_f = lambda t, x, theta=.5, k=2., sigma=.3: {'dt': k*(theta - x), 'dw': sigma}   # noqa: E731
+    cev_f = lambda t, x, mu=.05, sigma=.2, gamma=.7: {'dt': mu*x, 'dw': sigma*np.maximum(x, 0.)**gamma}  # noqa: E731
+
+    def sv_f(t, x, y, mu=.05, k=2., theta=.04, xi=.3):
+        yp = np.maximum(y, 0.)
+        return ({'dt': mu*x, 'dw': np.sqrt(yp)*x}, {'dt': k*(theta - yp), 'dw': xi*np.sqrt(yp)})
+    jd_f = lambda t, x, mu=.03, sigma=.15: {'dt': mu - sigma*sigma/2, 'dw': sigma, 'dj': 1}   # noqa: E731
+    f32 = dict(dtype=np.float32)
+    cases = (
+        ('user_ou', sg.integrate(ou_f, jit=False)(paths=K, steps=500, x0=1., **f32), (0., 2.), .5),
+        ('user_ou_jit', sg.integrate(ou_f, jit=True)(paths=K, steps=500, x0=1., **f32), (0., 2.), .5),
+        ('preset_ou', sg.ornstein_uhlenbeck_process(paths=K, steps=500, x0=1., theta=.5, k=2., sigma=.3, **f32),
+         (0., 2.), .5),
+        ('user_cev_jit', sg.integrate(cev_f, jit=True)(paths=K, steps=500, x0=1., **f32), (0., 2.), 1.),
+        ('user_sv_system_jit', sg.integrate(sv_f, q=2, sources=('dt', 'dw'), jit=True)(
+            paths=K, steps=500, x0=(100., .04), rho=-.6, **f32), (0., 2.), 100.),
+        ('user_merton_jit', sg.integrate(jd_f, log=True, jit=True)(paths=K, steps=365, x0=1., lam=1.,
+                                                                   y=sg.norm_rv(-.1, .15), **f32), (0., 1.), 1.),
+        ('preset_merton', sg.merton_jumpdiff_process(paths=K, steps=365, x0=1., mu=.03, sigma=.15, lam=1., a=-.1,
+                                                     b=.15, **f32), (0., 1.), 1.),
+    )
+    out = {}
+    for name, P, tl, strike in cases:
+        _fused(lib, P, tl, [strike], 8)   # (compiles a compiled program's forward)
+        f_ms = _time_call(lambda: _fused(lib, P, tl, [strike], 8), lib)
+        a_ms = _adjoint_ms(lib, P, tl, strike)
+        out[name + '_adjoint_fp32'] = {'forward_ms': f_ms, 'adjoint_ms': a_ms, 'grad_over_forward': a_ms/f_ms}
+    return out
+
+
 def extra_configs(lib):
     """Heston 2^22 paths x 499 steps (FP32 forward with fused call payoffs
     vs the adjoint gradient of the 6 parameters; FP64 forward), Merton / Kou
@@ -512,20 +597,7 @@ def extra_configs(lib):
     lib.sde_timing(1, None)
 
     def fused(P, timeline, strikes, seed):
-        leg = Grid(timeline, P.steps).legs[-1]
-        g = _lib.SdeGrid()
-        g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
-        g.n_pts, g.step_offset = leg.tt.size, 0
-        o = _lib.SdeOut()
-        o.xx, o.n_rows, o.on_device = None, len(timeline), 0
-        ptab = P._params_table(leg) if P._tdep else None          # time-dependent parameters
-        ctab = P._corr_table(leg) if P._corr_tdep else None       # and correlations
-        ltab = P._lam_table(leg)                                  # a user SDE's intensity
-        g.params_t, g.corr_t, g.lam_t = _lib.dptr(ptab), _lib.dptr(ctab), _lib.dptr(ltab)
-        req, so, arrs = P._stats_request(dict(row=len(timeline) - 1, bins=0, range=None, strikes=strikes))
-        spec = P._make_spec(seed, 0)
-        _lib.check(lib.sde_run_stats(C.byref(spec), C.byref(g), None, C.byref(o), C.byref(req), C.byref(so)), 'fwd')
-        return arrs, leg
+        return _fused(lib, P, timeline, strikes, seed)
 
     import time
     # ---- Heston, 2^22 paths, 499 steps on (0, 2)
@@ -726,34 +798,8 @@ def extra_configs(lib):
         ms = _time_call(lambda: fused(P, (0., 1.), [], 8), lib)
         nxt[name] = {'kernel_ms': ms, 'path_steps_per_s': K*364/(ms*1e-3), 'steps': 364}
 
-    # adjoint against forward cost for user SDEs (tangent-mode program) and
-    # the OU preset, mean and one call payoff, 499 steps on (0, 2)
-    def adj_ms(P, strike):
-        leg = Grid((0., 2.), P.steps).legs[-1]
-        g = _lib.SdeGrid()
-        g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
-        g.n_pts, g.step_offset = leg.tt.size, 0
-        req = _lib.SdeAdjReq()
-        req.n_strikes, req.checkpoint, req.mean_weight = 1, 0, 1.
-        req.strikes[0], req.weights[0] = strike, 1.
-        grad = np.zeros((P._W, 8))
-        v = C.c_double()
-
-        def call():
-            spec = P._make_spec(8, 0)
-            _lib.check(lib.sde_adjoint(C.byref(spec), C.byref(g), C.byref(req), _lib.dptr(grad), C.byref(v)),
-                       'adj')
-        return _time_call(call, lib)
-    cev = sg.integrate(lambda t, x, mu=.05, sigma=.2, gamma=.7: {'dt': mu*x, 'dw': sigma*np.maximum(x, 0.)**gamma},
-                       jit=False)
-    for name, P, strike in (('user_ou', user_ou(paths=K, steps=500, dtype=np.float32, x0=1.), .5),
-                            ('user_ou_jit', user_ou_jit(paths=K, steps=500, dtype=np.float32, x0=1.), .5),
-                            ('preset_ou', sg.ornstein_uhlenbeck_process(paths=K, steps=500, dtype=np.float32,
-                                                                        x0=1., theta=.5, k=2., sigma=.3), .5),
-                            ('user_cev', cev(paths=K, steps=500, dtype=np.float32, x0=1.), 1.)):
-        f_ms = _time_call(lambda: fused(P, (0., 2.), [strike], 8), lib)
-        a_ms = adj_ms(P, strike)
-        nxt[name + '_adjoint_fp32'] = {'forward_ms': f_ms, 'adjoint_ms': a_ms, 'grad_over_forward': a_ms/f_ms}
+    # adjoint against forward cost for user SDEs and the presets they restate
+    nxt.update(user_adjoint_bench(lib, K))
     Cm = np.array([[1., .5], [.5, 1.]])
     nxt['ou2_corr_const_fp32'] = rate(sg.ornstein_uhlenbeck_process(vshape=2, paths=K, steps=500,
                                                                      dtype=np.float32, corr=Cm))
@@ -916,7 +962,9 @@ def run_case(args):
     'lognorm_fp64' (FP64, 1e5 paths, 502 steps, 253 rows written
     to device memory), 'process_post' (FP32 device-resident 11 x 8 x 2^20
     values: moments, cdf at 41 values, chf at 4 values of u), 'cir_user'
-    (CIR and an interpreted user SDE, FP32, 2^20 paths x 499 steps)."""
+    (CIR and an interpreted user SDE, FP32, 2^20 paths x 499 steps),
+    'user_adjoint' (the user-SDE adjoints against their forwards, 2^20
+    paths)."""
     import ctypes as C
     import torch
     import sdepy_gb300 as sg
@@ -988,6 +1036,8 @@ def run_case(args):
                 ms.append(last[0])
             res[name + '_kernel_ms'] = float(np.median(ms[args.warmup:]))
         print(json.dumps({'case': args.case, **res}))
+    elif args.case == 'user_adjoint':
+        print(json.dumps({'case': args.case, **user_adjoint_bench(lib, 2**20)}))
     elif args.case == 'process_post':
         print(json.dumps({'case': args.case, 'result': process_post_bench(
             lib, reps=args.steps, api=False, dtypes=(np.float32,))}))
@@ -1004,7 +1054,8 @@ def main():
     ap.add_argument('--quick', action='store_true',
                     help='timed steps only: no FP64 / e2e / CPU / probe extras')
     ap.add_argument('--case', default=None,
-                    choices=['heston_adjoint', 'batch', 'lognorm_fp64', 'process_post', 'cir_user'],
+                    choices=['heston_adjoint', 'batch', 'lognorm_fp64', 'process_post', 'cir_user',
+                             'user_adjoint'],
                     help='run one small single-kernel case (profiling)')
     args = ap.parse_args()
     if args.case:

@@ -260,8 +260,10 @@ SDE_API int32_t sde_jit_available(void);
 SDE_API int32_t sde_jit_compile(const SdeUserProgram *program, int32_t precision, int32_t group_size,
                                 int32_t injected, int32_t jumps, char *log, int32_t len);
 
-/* The same for the adjoint kernel of a single-equation program (group
- * size 1..8): the coefficients and their tangents compiled in. */
+/* The same for the adjoint kernel of a program (single equations and
+ * systems, any terms) for groups of group_size states (1..8, whole
+ * components of a system): the coefficients and the generated
+ * reverse-mode step compiled in. */
 SDE_API int32_t sde_jit_compile_adjoint(const SdeUserProgram *program, int32_t precision, int32_t group_size,
                                         char *log, int32_t len);
 
@@ -341,9 +343,15 @@ SDE_API int32_t sde_run_stats(const SdeSpec *spec, const SdeGrid *grid,
  * [groups*M][8]: per state variable d L / d of x0 (integration variable),
  * params p0..p5, and in slot 7 of a group's first variable d L / d rho
  * (2-variable Heston group with corr = [[1, rho], [rho, 1]]).  value = L.
- * For a user SDE (single equation, dt / dw terms) slot 1 + j is d L / d
- * of the program's parameter p_j, from a tangent-mode run of its program
- * (interpreted, or compiled at run time with SdeUserProgram.jit = 1).
+ * For a user SDE slot 1 + j is d L / d of the program's parameter p_j:
+ * single equations driven by dt / dw with SdeUserProgram.jit = 0 run the
+ * interpreted program in tangent mode; with jit = 1, and always for systems
+ * and programs with dn / dj terms, the program is compiled at run time
+ * with its generated reverse-mode step (NVRTC; SDE_ERR_UNSUPPORTED
+ * without it).  For a system, f reads the first equation's states of each
+ * group and slot 1 + j of state h holds the gradient of component h's
+ * parameter; jump counts, intensities (SdeGrid.lam_t accepted) and
+ * jump-size laws are not differentiated.
  * The adjoint of the Euler recursion is propagated backwards through
  * checkpointed segments recomputed from Philox counters (constant for the
  * LINEAR model); no path is stored.  No counterpart in the reference

@@ -16,11 +16,18 @@ Differentiable parameters per preset:
   merton_jumpdiff_process   x0, mu, sigma, a, b
   kou_jumpdiff_process      x0, mu, sigma, a, b
   cox_ingersoll_ross_process x0, k, theta, xi
-  user SDEs (``integrate``)  x0 and every parameter of the SDE function, for
-                             single equations driven by dt / dw (the
-                             device runs the traced program in tangent mode)
-Poisson intensities and the Kou probability pa select integer / discrete
-outcomes and are not differentiated.
+  user SDEs (``integrate``)  x0 and every parameter of the SDE function:
+                             single equations and systems (the expectation
+                             of the first equation's process; x0 a scalar
+                             or one value per equation), with dt, dw, dn
+                             and dj terms.  A compiled program runs its
+                             generated reverse-mode step, an interpreted one
+                             (single equations, dt / dw) the traced program
+                             in tangent mode; systems and jump terms are
+                             compiled.
+Poisson intensities (constant or functions of time), the Kou probability pa
+and the jump-size laws of user SDEs select integer / discrete outcomes or
+are drawn through them and are not differentiated.
 
 Time-dependent parameters (the presets without jumps): a parameter may be a
 function of time, evaluated at each Euler step's start as sdepy evaluates
@@ -55,30 +62,42 @@ _MAP = {
 
 
 def _user_map(cls):
-    """Gradient slots of a user SDE class: x0 in slot 0, parameter j of
-    the SDE function in slot 1 + j; None if the class is not a user SDE."""
-    from .usersde import _user_process, _user_sys_process
+    """Gradient slots of a user SDE class: x0 in slot 0 (of each equation's
+    state for a system), parameter j of the SDE function in slot 1 + j of
+    state 0; None if the class is not a user SDE."""
+    from .usersde import _user_process
     if not (isinstance(cls, type) and issubclass(cls, _user_process)):
         return None
-    if issubclass(cls, _user_sys_process):
-        raise NotImplementedError('gradients of systems of user SDEs are not supported')
-    if not set(cls.sources_ids) <= {'dt', 'dw'}:
-        raise NotImplementedError('gradients of user SDEs with dn / dj terms are not supported')
     m = {'x0': (0, 0)}
     m.update({n: (0, 1 + i) for i, n in enumerate(cls._pnames)})
     return m
 
 
-def _param_grads(name, g, vals, mp=None, log=False):
-    """d/d(user parameter) from the per-state gradient slots g[w][8]."""
-    m = _MAP[name] if mp is None else mp
+def _user_grads(proc, g):
+    """d/d(parameter) of a user SDE from the per-state gradient slots g[w][8]
+    of a scalar process: for a system (states = equations) the x0 gradient
+    has one value per equation; with the log flag the states start at log
+    x0."""
+    from .usersde import _user_sys_process
+    out = {n: g[0, 1 + i] for i, n in enumerate(proc._pnames)}
+    if isinstance(proc, _user_sys_process):
+        q = proc._q
+        x0 = np.broadcast_to(np.asarray(proc.args['x0'], dtype=float), (q,))
+        gx = g[:q, 0].copy()
+    else:
+        x0 = np.asarray(proc.args['x0'], dtype=float)
+        gx = g[0, 0]
+    if getattr(proc, '_log', False):
+        gx = gx/x0
+    out['x0'] = gx
+    return out
+
+
+def _param_grads(name, g, vals):
+    """d/d(preset parameter) from the per-state gradient slots g[w][8]."""
     out = {}
-    for p, (w, j) in m.items():
+    for p, (w, j) in _MAP[name].items():
         out[p] = g[w, j]
-    if mp is not None:   # a user SDE: its state is log x with the log flag
-        if log:
-            out['x0'] = g[0, 0]/vals['x0']
-        return out
     log_models = name in ('lognorm_process', 'merton_jumpdiff_process',
                           'kou_jumpdiff_process', 'heston_process')
     if log_models:
@@ -123,7 +142,10 @@ class _Expectation(torch.autograd.Function):
         grad = np.zeros((proc._W, 8))
         val = C.c_double()
         name = type(proc).__name__
-        td = bool(proc._tdep)
+        td = bool(proc._tdep) and ctx.mp is None
+        lam_t = proc._lam_table(leg) if ctx.mp is not None else None
+        if lam_t is not None:   # a user jump term's intensity, a function of time
+            g.lam_t = _lib.dptr(lam_t)
         if td:   # per-step slot gradients of the time-dependent table
             ptab = proc._params_table(leg)
             g.params_t = _lib.dptr(ptab)
@@ -133,7 +155,6 @@ class _Expectation(torch.autograd.Function):
                              _lib.dptr(grad), C.byref(val))
         _lib.check(st, 'sde_adjoint')
         mp = ctx.mp if ctx.mp is not None else _MAP[name]
-        vals = {k: float(np.asarray(v)) for k, v in proc.args.items() if k in mp and not callable(v)}
         if td:
             # initial states (slot 0) and rho from the per-variable slots;
             # every slot parameter from its per-step gradients (summed for a
@@ -143,11 +164,16 @@ class _Expectation(torch.autograd.Function):
                 pg['x0'] = grad[0, 0]/float(np.asarray(proc.args['x0']))   # state log x0
             for k, v in _step_grads(name, gt, proc, leg).items():
                 pg[k] = v if callable(proc.args.get(k)) else float(v.sum())
+        elif ctx.mp is not None:
+            pg = _user_grads(proc, grad)
         else:
-            pg = _param_grads(name, grad, vals, ctx.mp, getattr(proc, '_log', False))
+            vals = {k: float(np.asarray(v)) for k, v in proc.args.items() if k in mp and not callable(v)}
+            pg = _param_grads(name, grad, vals)
         outs = []
         for n, shp, dt in zip(ctx.names, ctx.shapes, ctx.dtypes):
             v = pg[n]
+            if np.ndim(v) and int(np.prod(shp)) == 1:   # one x0 for every equation
+                v = float(np.sum(v))
             outs.append(torch.tensor(np.broadcast_to(v, shp), dtype=dt) if np.ndim(v) else
                         torch.full(shp, v, dtype=dt))
         return (None, None, None) + tuple(outs)
@@ -156,7 +182,8 @@ class _Expectation(torch.autograd.Function):
 def expectation(cls, timeline, strikes=(), *, paths, steps=None,
                 dtype=np.float32, seed=0, stream=0, **params):
     """Differentiable Monte Carlo estimate of [E[X_T], E[max(X_T - K, 0)]
-    for K in strikes] for a scalar preset process ``cls`` integrated along
+    for K in strikes] for a scalar preset process ``cls``, or a user SDE
+    class (of a system: its first equation's process), integrated along
     ``timeline``; torch-tensor parameters with requires_grad get gradients
     from the adjoint kernel (same Philox paths as the forward)."""
     name = cls.__name__
@@ -167,17 +194,22 @@ def expectation(cls, timeline, strikes=(), *, paths, steps=None,
     strikes = [float(k) for k in strikes]
     if len(strikes) > _lib.MAX_STRIKES:
         raise ValueError('at most {} strikes'.format(_lib.MAX_STRIKES))
+    if tuple(np.atleast_1d(params.get('vshape', ()) or ())) != ():
+        raise NotImplementedError('expectation() takes scalar processes (vshape=())')
+    q = getattr(cls, '_q', 1) if mp is not None and getattr(cls, 'q', 0) else 1
     names, tensors = [], []
     plain = {}
     for k, v in params.items():
         if isinstance(v, torch.Tensor):
             if k not in pmap:
                 raise NotImplementedError('parameter {!r} is not differentiable'.format(k))
-            if v.numel() != 1:
-                raise NotImplementedError('differentiable parameters must be scalars')
+            if v.numel() != 1 and not (k == 'x0' and q > 1 and v.numel() == q):
+                raise NotImplementedError('differentiable parameters must be scalars (x0 of a system: '
+                                          'one value per equation)')
             names.append(k)
             tensors.append(v)
-            plain[k] = float(v.detach().cpu())
+            vv = v.detach().cpu().numpy().astype(float)
+            plain[k] = float(vv.reshape(-1)[0]) if v.numel() == 1 else tuple(vv.reshape(-1))
         else:
             plain[k] = v
     if 'rho' in plain and mp is None and name != 'heston_process':
@@ -188,7 +220,9 @@ def expectation(cls, timeline, strikes=(), *, paths, steps=None,
     # time-dependent parameters: a torch-valued function of time is evaluated
     # at the steps' starts as a torch tensor (the input whose gradient the
     # backward pass returns) and handed to the process as a numpy function
-    tdep = [k for k, v in plain.items() if callable(v)]
+    # (a user SDE's intensity may depend on time, and its jump-size law is
+    # an object: neither is differentiated)
+    tdep = [k for k, v in plain.items() if callable(v) and not (mp is not None and k in ('lam', 'y'))]
     if tdep:
         if mp is not None or name in ('merton_jumpdiff_process', 'kou_jumpdiff_process') or \
                 name not in _TD_SLOTS:
@@ -216,8 +250,9 @@ def expectation(cls, timeline, strikes=(), *, paths, steps=None,
         value = None
         if run:
             mc = P.montecarlo(timeline, bins=None, strikes=strikes)
+            # the first state: a scalar process, or a system's first equation
             value = np.concatenate(([float(np.asarray(mc.mean()).reshape(-1)[0])],
-                                    np.asarray(mc.payoff).reshape(-1)))
+                                    np.asarray(mc.payoff).reshape(-1)[:len(strikes)]))
         return P, grid, strikes, seed, stream, value
 
     return _Expectation.apply(spec_fn, tuple(names), mp, *tensors)

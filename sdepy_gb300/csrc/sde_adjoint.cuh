@@ -15,9 +15,10 @@
 // Integer Poisson counts are not differentiated (their intensity gets no
 // gradient); the full-truncation kink of Heston's variance and of CIR
 // contributes its one-sided derivative (zero where the state is <= 0).
-// User SDEs (single equations driven by dt / dw): the program is run in
-// tangent mode for dA/dx and dA/dp (user_coefs_tan); slot 1 + j of a state
-// is the gradient of its parameter p_j.
+// User SDEs interpreted on the device (single equations driven by dt /
+// dw): the program is run in tangent mode for dA/dx and dA/dp
+// (user_coefs_tan); slot 1 + j of a state is the gradient of its parameter
+// p_j.  Compiled user programs have their own kernel (sde_adj_user.cuh).
 #pragma once
 #include "sde_kernels.cuh"
 
@@ -33,6 +34,9 @@ constexpr size_t ADJ_TD_SMEM_SM = 220 * 1024;
 // steps per segment of the FP32 Heston adjoint that keep three 256-thread
 // blocks per SM (3 floats per step and thread in shared memory)
 constexpr int ADJ_HESTON_SEG = 24;
+// shared-memory bytes per block for the segment buffer of the compiled
+// user-SDE adjoint (sde_adj_user.cuh)
+constexpr size_t UADJ_SMEM = 96 * 1024;
 
 template <typename R>
 struct AdjArgs {
@@ -66,6 +70,10 @@ struct AdjArgs {
     // per-variable slots 1..3
     const R *prm_t;
     double *tdpart;
+    // a user SDE's jump terms (sde_adj_user_kernel): the jump-size law's a,
+    // b, pa per state ([3][W]), and the terms present (bit 0 dj, bit 1 dn)
+    const R *jprm;
+    int32_t user_jsrc;
 };
 
 // Tangent-mode run of a user program (single equation): the terms' values
@@ -178,19 +186,6 @@ __device__ __noinline__ void user_coefs_tan(const SdeUserProgram &u, R x, R t, c
         else tan_op<R>(op, r, d);
     }
     tan_outputs<R>(u, r, d, A, dA);
-}
-
-// runtime-compiled tangent run (sde_jit.cu: UserJitTan<R>::tan, the same
-// steps with the instructions as constants), else the interpreter
-template <typename R>
-struct UserJitTan;
-template <typename R, int MODEL>
-__device__ __forceinline__ void user_tan_eval(const SdeUserProgram &u, R x, R t, const R (&p)[6],
-                                              R (&A)[SDE_USER_MAX_TERMS], R (&dA)[SDE_USER_MAX_TERMS][UTAN]) {
-    if constexpr (MODEL == SDE_MODEL_USER_JIT)
-        UserJitTan<R>::tan(u, x, t, p, A, dA);
-    else
-        user_coefs_tan<R>(u, x, t, p, A, dA);
 }
 
 // one forward Euler step of a user SDE (the forward kernel's arithmetic):
@@ -343,8 +338,8 @@ __device__ __forceinline__ void fwd_step(const R (&c0)[MAXM], const R (&c1)[MAXM
 template <typename R, int MODEL, int MAXM, bool JUMPS, bool TD = false>
 __global__ void __launch_bounds__(BLOCK, (sizeof(R) == 4 && MAXM <= 2) ? 3 : 1)
 sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
-    // a user SDE: interpreted, or compiled at run time
-    constexpr bool UJ = MODEL == SDE_MODEL_USER || MODEL == SDE_MODEL_USER_JIT;
+    // a user SDE interpreted on the device
+    constexpr bool UJ = MODEL == SDE_MODEL_USER;
     typedef Ar<R> A;
     constexpr int NCMAX = NoiseShape<MAXM, JUMPS>::NCMAX;
     constexpr int NPA = MAXM * NGV + 2;
@@ -581,7 +576,7 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                         for (int m = 0; m < MAXM; ++m) {
                             const R pv[6] = {c0[m], c1[m], c2[m], c3[m], c4[m], c5[m]};
                             R Av[SDE_USER_MAX_TERMS], dA[SDE_USER_MAX_TERMS][UTAN];
-                            user_tan_eval<R, MODEL>(a.uprog, bx[k - k0][m], a.tk[k], pv, Av, dA);
+                            user_coefs_tan<R>(a.uprog, bx[k - k0][m], a.tk[k], pv, Av, dA);
                             R gx = R(0), gp[6] = {R(0), R(0), R(0), R(0), R(0), R(0)};
                             for (int i = 0; i < a.uprog.n_terms; ++i) {
                                 const R dz = a.uprog.term_source[i] == SDE_SRC_DT ? dt : bw[k - k0][m];

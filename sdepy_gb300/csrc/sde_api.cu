@@ -1153,15 +1153,28 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     if (req->n_strikes < 0 || req->n_strikes > SDE_MAX_STRIKES) return fail(SDE_ERR_INVALID, "bad n_strikes");
     const int M = s->group_size, W = s->groups * M;
     const bool user = s->model == SDE_MODEL_USER;
-    if (user) {
-        // single equations driven by dt / dw
-        const SdeUserProgram *u = s->program;
-        if (u->n_eq != 1) return fail(SDE_ERR_UNSUPPORTED, "the adjoint of user SDEs takes single equations");
-        for (int i = 0; i < u->n_terms; ++i)
-            if (u->term_source[i] != SDE_SRC_DT && u->term_source[i] != SDE_SRC_DW)
-                return fail(SDE_ERR_UNSUPPORTED, "the adjoint of user SDEs takes dt and dw terms only");
-    }
-    const bool jumps = s->jump_law != SDE_JUMP_NONE;
+    // a user program's terms: ujs bit 0 dj, bit 1 dn; nv the values per
+    // state and step the compiled adjoint keeps (the state, dw, dn, dj)
+    int ujs = 0, nv = 1;
+    if (user)
+        for (int i = 0; i < s->program->n_terms; ++i) {
+            const int src = s->program->term_source[i];
+            if (src == SDE_SRC_DJ) ujs |= 1;
+            if (src == SDE_SRC_DN) ujs |= 2;
+            if (src != SDE_SRC_DT) ++nv;
+        }
+    // compiled programs, systems and jump terms take the reverse-mode kernel
+    // (sde_adj_user.cuh); the interpreter takes single equations driven by
+    // dt / dw (tangent mode)
+    const bool ujit = user && (s->program->jit || s->program->n_eq > 1 || ujs);
+    if (ujit && !jit_available())
+        return fail(SDE_ERR_UNSUPPORTED, "the adjoint of user systems and jump terms compiles the program at run "
+                                         "time: NVRTC is not available");
+    const bool jumps = user ? ujs != 0 : s->jump_law != SDE_JUMP_NONE;
+    if (gr->lam_t && !(user && jumps))
+        return fail(SDE_ERR_INVALID, "grid lam_t applies to user SDEs with dn / dj terms");
+    if (user && jumps && !s->program->jump_params)
+        return fail(SDE_ERR_INVALID, "a user program with dn / dj terms needs jump_params");
     int maxm = maxm_of(M);
     if (maxm > 8) return fail(SDE_ERR_UNSUPPORTED, "the adjoint supports groups of up to 8 state variables");
     // time-dependent parameter slots: per-step gradients into req->grad_t
@@ -1191,6 +1204,30 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
             return fail(SDE_ERR_UNSUPPORTED, "the adjoint supports up to %d steps",
                         ADJ_MAXSEG * ADJ_MAXSEG * ADJ_MAXSEG);
     }
+    // the compiled user adjoint keeps each level-2 segment's states and
+    // increments in shared memory: at most `cap` steps of nv * M values per
+    // thread in UADJ_SMEM bytes
+    size_t ubytes = 0;
+    if (ujit) {
+        const size_t per_step = sizeof(R) * (size_t)nv * M * BLOCK;
+        int cap = (int)(UADJ_SMEM / per_step);
+        if (cap > ADJ_MAXSEG) cap = ADJ_MAXSEG;
+        if (cap < 1) return fail(SDE_ERR_UNSUPPORTED, "the adjoint's segment buffer does not fit groups of %d", M);
+        seg = req->checkpoint > 0 ? req->checkpoint : (int)ceil(sqrt((double)n_steps));
+        if (seg > cap) seg = cap;
+        if (seg < 1) seg = 1;
+        seg2 = seg;
+        if ((n_steps + seg - 1) / seg > ADJ_MAXSEG) {   // two levels
+            seg = (n_steps + ADJ_MAXSEG - 1) / ADJ_MAXSEG;
+            seg2 = (int)ceil(sqrt((double)seg));
+            if (seg2 > cap) seg2 = cap;
+            if ((seg + seg2 - 1) / seg2 > ADJ_MAXSEG) seg2 = (seg + ADJ_MAXSEG - 1) / ADJ_MAXSEG;
+            if (seg2 > cap)
+                return fail(SDE_ERR_UNSUPPORTED, "the adjoint supports up to %d steps for groups of %d",
+                            ADJ_MAXSEG * ADJ_MAXSEG * cap, M);
+        }
+        ubytes = per_step * seg2;
+    }
     // the FP32 2-variable Heston adjoint keeps its segment in shared memory:
     // segments of at most ADJ_HESTON_SEG steps (one checkpoint level)
     const bool heston_fast = sizeof(R) == 4 && s->model == SDE_MODEL_HESTON && M == 2 && !jumps && !td &&
@@ -1214,7 +1251,8 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     const size_t o_thr1 = o_thr + al(sizeof(long long) * njt);
     const size_t o_tk = o_thr1 + al(sizeof(long long) * njt);   // step starts, for user SDEs
     const size_t o_pt = o_tk + al(sizeof(R) * (user ? n_steps : 1));   // slots 0..2 per step
-    const size_t o_end = o_pt + al(sizeof(R) * (td ? (size_t)n_steps * 3 * W : 1));
+    const size_t o_jp = o_pt + al(sizeof(R) * (td ? (size_t)n_steps * 3 * W : 1));   // a user dj law's a, b, pa
+    const size_t o_end = o_jp + al(sizeof(R) * (user && jumps ? (size_t)3 * W : 1));
     D->host_tables.resize(o_end);
     char *H = D->host_tables.data();
     R *h_dt = (R *)(H + o_dt), *h_sq = (R *)(H + o_sq), *h_x0 = (R *)(H + o_x0), *h_prm = (R *)(H + o_prm);
@@ -1236,10 +1274,15 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
                 for (int w = 0; w < W; ++w)
                     h_pt[((size_t)k * 3 + j) * W + w] = (R)gr->params_t[((size_t)k * SDE_MAX_PARAMS + j) * W + w];
     }
+    if (user && jumps)
+        for (int i = 0; i < 3 * W; ++i) ((R *)(H + o_jp))[i] = (R)s->program->jump_params[W + i];
     if (jumps)
         for (int k = 0; k < n_steps; ++k)
             for (int w = 0; w < W; ++w) {
-                const double L = (gr->tt[k + 1] - gr->tt[k]) * s->params[2 * W + w];
+                // a user SDE's intensity: its table at the step's midpoint, or its constant
+                const double lam = !user ? s->params[2 * W + w]
+                                   : gr->lam_t ? gr->lam_t[(size_t)k * W + w] : s->program->jump_params[w];
+                const double L = (gr->tt[k + 1] - gr->tt[k]) * lam;
                 if (!(L >= 0.0) || L > 700.0) return fail(SDE_ERR_INVALID, "bad Poisson intensity");
                 const double p0 = exp(-L);
                 h_lam[(size_t)k * W + w] = L;
@@ -1290,6 +1333,8 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     if (user) {
         a.uprog = *s->program;
         a.tk = (const R *)(T + o_tk);
+        a.user_jsrc = ujs;
+        if (jumps) a.jprm = (const R *)(T + o_jp);
     }
     if (td) a.prm_t = (const R *)(T + o_pt);
     a.n_strikes = req->n_strikes;
@@ -1307,9 +1352,12 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     // a user program compiled at run time, or an instantiated kernel
     cudaKernel_t jk = nullptr;
     AdjLauncher<R> L = nullptr;
-    if (user && s->program->jit) {
+    if (ujit) {
         std::string err;
-        if ((rc = jit_adj_kernel(*s->program, sizeof(R) == 8, maxm, &jk, &bps, &err))) return fail(rc, "%s", err.c_str());
+        if ((rc = jit_adj_kernel(*s->program, sizeof(R) == 8, M, &jk, &err))) return fail(rc, "%s", err.c_str());
+        CU(cudaFuncSetAttribute((const void *)jk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ubytes));
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void *)jk, BLOCK, ubytes));
+        if (bps < 1) bps = 1;
     } else if (heston_fast) {
         L = AdjFinder<R>::find_heston(seg, &bps);
     } else {
@@ -1337,7 +1385,7 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     if (D->timing) CU(cudaEventRecord(D->ev[0], st));
     if (jk) {
         void *args[] = {(void *)&a};
-        CU(cudaLaunchKernel((const void *)jk, dim3(nbx, s->groups), dim3(BLOCK), args, 0, st));
+        CU(cudaLaunchKernel((const void *)jk, dim3(nbx, s->groups), dim3(BLOCK), args, ubytes, st));
     } else {
         L(a, dim3(nbx, s->groups), st);
     }

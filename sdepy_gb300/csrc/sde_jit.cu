@@ -9,10 +9,12 @@
 // library API.  The forward kernel instantiated with SDE_MODEL_USER_JIT /
 // SDE_MODEL_USER_SYS_JIT then evaluates the coefficients inline, with no
 // register file in local memory and no dispatch; the adjoint kernel
-// (sde_adjoint.cuh, SDE_MODEL_USER_JIT) also gets the tangent-mode run
-// (UserJitTan<R>::tan).  Kernels are cached per generated source (program,
-// precision, group width, noise mode, forward or adjoint) for the life of
-// the process.
+// (sde_adj_user.cuh) also gets the program's reverse-mode step
+// (UserJitAdj<R>::back), generated here instruction by instruction.
+// Kernels are cached per generated source (program, precision, group
+// width, noise mode, forward or adjoint) for the life of the process; with
+// SDEPY_GB300_JIT_DUMP set to a directory, each generated source is also
+// written there (sde_jit_<hash>.cu) for inspection.
 //
 // NVRTC is loaded with dlopen: a library without it still runs the
 // interpreted kernels (SdeUserProgram.jit = 0).
@@ -20,7 +22,9 @@
 #include <nvrtc.h>
 
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <string>
@@ -130,13 +134,25 @@ std::string kernel_name(const char *rt, int model, int maxm, bool inject, bool j
     return buf;
 }
 
-// UserJitFn<R>: the program as straight-line coefficient code
+// the sources of a program's terms as a constexpr function of the term index
+std::string src_function(const SdeUserProgram &u) {
+    std::string s = "  static __device__ __forceinline__ constexpr int src(int i) { return ";
+    for (int i = 0; i < u.n_terms; ++i)
+        s += "i == " + std::to_string(i) + " ? " + std::to_string(u.term_source[i]) + " : ";
+    return s + "-1; }\n";
+}
+
+// UserJitFn<R>: the program's shape as constants (NEQ equations, NT terms,
+// src(i) the source of term i) and the program as straight-line
+// coefficient code
 std::string coefs_struct(const SdeUserProgram &u, const char *rt) {
     std::string s = "template <> struct UserJitFn<";
     s += rt;
     s += "> {\n  typedef ";
     s += rt;
-    s += " R;\n  static __device__ __forceinline__ void coefs(const R *xs, R t, const R (&p)[6],"
+    s += " R;\n  static constexpr int NEQ = " + std::to_string(u.n_eq) + ", NT = " + std::to_string(u.n_terms) +
+         ";\n" + src_function(u);
+    s += "  static __device__ __forceinline__ void coefs(const R *xs, R t, const R (&p)[6],"
          " R (*out)[SDE_USER_MAX_TERMS]) {\n"
          "    typedef Ar<R> A;\n    typedef UFn<R> F;\n    R r[SDE_USER_MAX_REGS];\n"
          "    r[0] = xs[0];\n    r[1] = t;\n";
@@ -157,46 +173,125 @@ std::string jit_source(const SdeUserProgram &u, const char *rt, int model, int m
            ">);\n}  // namespace sdegpu\n";
 }
 
-std::string adj_kernel_name(const char *rt, int maxm) {
-    char buf[160];
-    snprintf(buf, sizeof buf, "sdegpu::sde_adj_kernel<%s, %d, %d, false>", rt, SDE_MODEL_USER_JIT, maxm);
-    return buf;
+// the parameters a program reads: 1 + the highest j of a register 2 + j
+// read by an instruction or a term
+int params_read(const SdeUserProgram &u) {
+    int np = 0;
+    auto see = [&](int r) {
+        if (r >= 2 && r <= 7 && r - 1 > np) np = r - 1;
+    };
+    for (int i = 0; i < u.n_ops; ++i) {
+        const uint32_t op = u.ops[i];
+        const int code = op & 0xff;
+        if (code == SDE_UOP_CONST) continue;
+        see((op >> 16) & 0xff);
+        if (code == SDE_UOP_ADD || code == SDE_UOP_SUB || code == SDE_UOP_MUL || code == SDE_UOP_DIV ||
+            code == SDE_UOP_MAX || code == SDE_UOP_MIN || code == SDE_UOP_POW)
+            see(op >> 24);
+    }
+    for (int e = 0; e < u.n_eq; ++e)
+        for (int i = 0; i < u.n_terms; ++i) see(u.term_register[e][i]);
+    return np;
 }
 
-// the adjoint kernel of a single-equation program: the coefficients, and
-// UserJitTan<R>::tan, the interpreter's tangent steps (tan_op) with the
-// instructions as constants and the terms read from fixed registers
-std::string jit_adj_source(const SdeUserProgram &u, const char *rt, int maxm) {
-    std::string s = "#include \"sde_adjoint.cuh\"\nnamespace sdegpu {\n" + coefs_struct(u, rt);
-    s += "template <> struct UserJitTan<";
+// one instruction's reverse-mode statements: b[] holds the adjoints of the
+// registers; the partials are the tangent rules of the interpreted adjoint
+// (sde_adjoint.cuh, tan_op), and a zero adjoint propagates nothing where a
+// partial may be infinite (no 0 * inf)
+std::string op_reverse(uint32_t op) {
+    const int code = op & 0xff, d = (op >> 8) & 0xff, ia = (op >> 16) & 0xff, ib = op >> 24;
+    if (code == SDE_UOP_CONST) return "";
+    const std::string D = "b[" + std::to_string(d) + "]", BA = "b[" + std::to_string(ia) + "]",
+                      BB = "b[" + std::to_string(ib) + "]", RA = "r[" + std::to_string(ia) + "]",
+                      RB = "r[" + std::to_string(ib) + "]", RD = "r[" + std::to_string(d) + "]";
+    auto guarded = [&](const std::string &body) { return "if (" + D + " != R(0)) { " + body + " }"; };
+    switch (code) {
+    case SDE_UOP_ADD: return BA + " += " + D + "; " + BB + " += " + D + ";";
+    case SDE_UOP_SUB: return BA + " += " + D + "; " + BB + " -= " + D + ";";
+    case SDE_UOP_MUL: return guarded(BA + " += " + D + " * " + RB + "; " + BB + " += " + D + " * " + RA + ";");
+    case SDE_UOP_DIV:
+        return guarded("const R q_ = " + D + " / " + RB + "; " + BA + " += q_; " + BB + " -= q_ * " + RD + ";");
+    case SDE_UOP_NEG: return BA + " -= " + D + ";";
+    case SDE_UOP_ABS: return BA + " += " + RA + " < R(0) ? -" + D + " : " + D + ";";
+    case SDE_UOP_EXP: return guarded(BA + " += " + D + " * " + RD + ";");
+    case SDE_UOP_LOG: return guarded(BA + " += " + D + " / " + RA + ";");
+    case SDE_UOP_SQRT: return "if (" + RD + " > R(0)) " + BA + " += " + D + " * (R(0.5) / " + RD + ");";
+    case SDE_UOP_MAX: return "if (" + RA + " >= " + RB + ") " + BA + " += " + D + "; else " + BB + " += " + D + ";";
+    case SDE_UOP_MIN: return "if (" + RA + " <= " + RB + ") " + BA + " += " + D + "; else " + BB + " += " + D + ";";
+    case SDE_UOP_SIN: return BA + " += " + D + " * F::cos_(" + RA + ");";
+    case SDE_UOP_COS: return BA + " -= " + D + " * F::sin_(" + RA + ");";
+    case SDE_UOP_TAN: return guarded(BA + " += " + D + " * (R(1) + " + RD + " * " + RD + ");");
+    case SDE_UOP_TANH: return BA + " += " + D + " * (R(1) - " + RD + " * " + RD + ");";
+    case SDE_UOP_POW:
+        return guarded(BA + " += " + D + " * (" + RB + " * F::pow_(" + RA + ", " + RB + " - R(1))); if (" + RA +
+                       " > R(0)) " + BB + " += " + D + " * (" + RD + " * F::log_(" + RA + "));");
+    case SDE_UOP_EXPM1: return guarded(BA + " += " + D + " * (" + RD + " + R(1));");
+    case SDE_UOP_LOG1P: return guarded(BA + " += " + D + " / (R(1) + " + RA + ");");
+    case SDE_UOP_ARCTAN: return BA + " += " + D + " / (R(1) + " + RA + " * " + RA + ");";
+    default: return BA + " += " + D + ";";   // SDE_UOP_COPY
+    }
+}
+
+// UserJitAdj<R>: the parameters read and the sources present as
+// constants (UserJitFn<R> holds the terms' sources), and back(): at the
+// states xs before a step, with the step's increments dz[e][i] of each
+// term, adds to the adjoints xb of the states d(x' . xb)/dx - xb, and to pb
+// d(x' . xb)/dp, where x'_e = x_e + sum_i A_ei(t, x, p) dz[e][i]: one value
+// pass of the program, the terms' adjoints xb_e dz[e][i], then the
+// instructions in reverse order
+std::string adj_struct(const SdeUserProgram &u, const char *rt) {
+    bool has[4] = {false, false, false, false};
+    for (int i = 0; i < u.n_terms; ++i) has[u.term_source[i]] = true;
+    std::string s = "template <> struct UserJitAdj<";
     s += rt;
     s += "> {\n  typedef ";
     s += rt;
-    s += " R;\n  static __device__ __forceinline__ void tan(const SdeUserProgram &, R x, R t, const R (&p)[6],"
-         " R (&A)[SDE_USER_MAX_TERMS], R (&dA)[SDE_USER_MAX_TERMS][UTAN]) {\n"
-         "    R r[SDE_USER_MAX_REGS];\n    R d[SDE_USER_MAX_REGS][UTAN];\n    tan_inputs<R>(x, t, p, r, d);\n";
-    char buf[160];
-    for (int i = 0; i < u.n_ops; ++i) {
-        const uint32_t op = u.ops[i];
-        if ((op & 0xff) == SDE_UOP_CONST) {
-            uint64_t bits;
-            memcpy(&bits, &u.consts[(op >> 16) & 0xff], sizeof bits);
-            snprintf(buf, sizeof buf, "    tan_const<R>(%d, (R)__longlong_as_double((long long)0x%016llxULL), r, d);\n",
-                     (int)((op >> 8) & 0xff), (unsigned long long)bits);
-        } else {
-            snprintf(buf, sizeof buf, "    tan_op<R>(0x%08xu, r, d);\n", op);
-        }
-        s += buf;
+    s += " R;\n  static constexpr int NEQ = " + std::to_string(u.n_eq) + ", NT = " + std::to_string(u.n_terms) +
+         ", NP = " + std::to_string(params_read(u)) + ";\n";
+    s += std::string("  static constexpr bool HAS_DW = ") + (has[SDE_SRC_DW] ? "true" : "false") +
+         ", HAS_DN = " + (has[SDE_SRC_DN] ? "true" : "false") + ", HAS_DJ = " + (has[SDE_SRC_DJ] ? "true" : "false") +
+         ";\n";
+    s += "  static __device__ __forceinline__ void back(const R (&xs)[NEQ], R t, const R (&p)[6],"
+         " const R (&dz)[NEQ][SDE_USER_MAX_TERMS], R (&xb)[NEQ], R (&pb)[6]) {\n"
+         "    typedef Ar<R> A;\n    typedef UFn<R> F;\n    R r[SDE_USER_MAX_REGS], b[SDE_USER_MAX_REGS];\n"
+         "#pragma unroll\n    for (int i = 0; i < SDE_USER_MAX_REGS; ++i) b[i] = R(0);\n"
+         "    r[0] = xs[0];\n    r[1] = t;\n";
+    for (int i = 0; i < 6; ++i) s += "    r[" + std::to_string(2 + i) + "] = p[" + std::to_string(i) + "];\n";
+    for (int e = 1; e < u.n_eq; ++e) s += "    r[" + std::to_string(7 + e) + "] = xs[" + std::to_string(e) + "];\n";
+    for (int i = 0; i < u.n_ops; ++i) s += "    " + op_statement(u, u.ops[i]) + "\n";
+    for (int e = 0; e < u.n_eq; ++e)
+        for (int i = 0; i < u.n_terms; ++i)
+            s += "    b[" + std::to_string(u.term_register[e][i]) + "] += xb[" + std::to_string(e) + "] * dz[" +
+                 std::to_string(e) + "][" + std::to_string(i) + "];\n";
+    for (int i = u.n_ops - 1; i >= 0; --i) {
+        const std::string st = op_reverse(u.ops[i]);
+        if (!st.empty()) s += "    " + st + "\n";
     }
-    for (int j = 0; j < SDE_USER_MAX_TERMS; ++j) {
-        const std::string reg = std::to_string(j < u.n_terms ? u.term_register[0][j] : 0);
-        s += "    A[" + std::to_string(j) + "] = " + (j < u.n_terms ? "r[" + reg + "]" : std::string("R(0)")) + ";\n";
-        s += "#pragma unroll\n    for (int j = 0; j < UTAN; ++j) dA[" + std::to_string(j) + "][j] = " +
-             (j < u.n_terms ? "d[" + reg + "][j]" : std::string("R(0)")) + ";\n";
-    }
-    s += "  }\n};\ntemplate __global__ void " + adj_kernel_name(rt, maxm) + "(const __grid_constant__ AdjArgs<" + rt +
-         ">);\n}  // namespace sdegpu\n";
+    for (int e = 0; e < u.n_eq; ++e)
+        s += "    xb[" + std::to_string(e) + "] += b[" + std::to_string(e == 0 ? 0 : 7 + e) + "];\n";
+    for (int j = 0; j < 6; ++j) s += "    pb[" + std::to_string(j) + "] += b[" + std::to_string(2 + j) + "];\n";
+    s += "  }\n};\n";
     return s;
+}
+
+// resident blocks the adjoint kernel is compiled for: FP32 groups of up to
+// two states at three 256-thread blocks per SM
+int adj_user_min_blocks(bool fp64, int mg) {
+    if (mg <= 2) return fp64 ? 2 : 3;
+    return mg <= 4 ? 2 : 1;
+}
+
+std::string adj_kernel_name(const char *rt, int maxm, int mg, int minb) {
+    char buf[160];
+    snprintf(buf, sizeof buf, "sdegpu::sde_adj_user_kernel<%s, %d, %d, %d>", rt, maxm, mg, minb);
+    return buf;
+}
+
+// the adjoint kernel of a program for groups of mg states (sde_adj_user.cuh)
+std::string jit_adj_source(const SdeUserProgram &u, const char *rt, int maxm, int mg, int minb) {
+    return "#include \"sde_adj_user.cuh\"\nnamespace sdegpu {\n" + coefs_struct(u, rt) + adj_struct(u, rt) +
+           "template __global__ void " + adj_kernel_name(rt, maxm, mg, minb) + "(const __grid_constant__ AdjArgs<" +
+           rt + ">);\n}  // namespace sdegpu\n";
 }
 
 struct Entry {
@@ -215,6 +310,14 @@ int compile_cubin(const std::string &src, const std::string &name, std::vector<c
     if (!N.ok) {
         *err = "NVRTC is not available for compiling user SDE programs";
         return SDE_ERR_UNSUPPORTED;
+    }
+    if (const char *dir = getenv("SDEPY_GB300_JIT_DUMP")) {
+        char path[4096];
+        snprintf(path, sizeof path, "%s/sde_jit_%016zx.cu", dir, std::hash<std::string>()(src));
+        if (FILE *f = fopen(path, "w")) {
+            fprintf(f, "// %s\n%s", name.c_str(), src.c_str());
+            fclose(f);
+        }
     }
     nvrtcProgram prog;
     if (N.create(&prog, src.c_str(), "sde_user_jit.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS) {
@@ -291,11 +394,15 @@ static int cached_kernel(const std::string &src, const std::string &name, cudaKe
     return SDE_OK;
 }
 
-int jit_compile_check_adjoint(const SdeUserProgram &u, bool fp64, int maxm, std::string *err) {
+static int maxm_of_group(int mg) { return mg <= 1 ? 1 : mg <= 2 ? 2 : mg <= 4 ? 4 : 8; }
+
+int jit_compile_check_adjoint(const SdeUserProgram &u, bool fp64, int mg, std::string *err) {
     const char *rt = fp64 ? "double" : "float";
+    const int maxm = maxm_of_group(mg), minb = adj_user_min_blocks(fp64, mg);
     std::vector<char> cubin;
     std::string low;
-    return compile_cubin(jit_adj_source(u, rt, maxm), adj_kernel_name(rt, maxm), &cubin, &low, err);
+    return compile_cubin(jit_adj_source(u, rt, maxm, mg, minb), adj_kernel_name(rt, maxm, mg, minb), &cubin, &low,
+                         err);
 }
 
 int jit_fwd_kernel(const SdeUserProgram &u, bool fp64, int maxm, bool inject, bool jumps, cudaKernel_t *kernel,
@@ -306,9 +413,12 @@ int jit_fwd_kernel(const SdeUserProgram &u, bool fp64, int maxm, bool inject, bo
                          kernel, bps, err);
 }
 
-int jit_adj_kernel(const SdeUserProgram &u, bool fp64, int maxm, cudaKernel_t *kernel, int *bps, std::string *err) {
+int jit_adj_kernel(const SdeUserProgram &u, bool fp64, int mg, cudaKernel_t *kernel, std::string *err) {
     const char *rt = fp64 ? "double" : "float";
-    return cached_kernel(jit_adj_source(u, rt, maxm), adj_kernel_name(rt, maxm), kernel, bps, err);
+    const int maxm = maxm_of_group(mg), minb = adj_user_min_blocks(fp64, mg);
+    int bps;
+    return cached_kernel(jit_adj_source(u, rt, maxm, mg, minb), adj_kernel_name(rt, maxm, mg, minb), kernel, &bps,
+                         err);
 }
 
 }  // namespace sdegpu
@@ -319,12 +429,12 @@ extern "C" int32_t sde_jit_compile_adjoint(const SdeUserProgram *program, int32_
                                            char *log, int32_t len) {
     std::string err;
     int rc = SDE_ERR_INVALID;
-    if (!program || group_size < 1 || group_size > 8 || program->n_eq != 1 || program->n_ops < 0 ||
-        program->n_ops > SDE_USER_MAX_OPS || program->n_terms < 0 || program->n_terms > SDE_USER_MAX_TERMS) {
-        err = "invalid program (single equations) or group size (1..8)";
+    if (!program || group_size < 1 || group_size > 8 || program->n_eq < 1 || program->n_eq > SDE_USER_MAX_EQ ||
+        group_size % program->n_eq || program->n_ops < 0 || program->n_ops > SDE_USER_MAX_OPS ||
+        program->n_terms < 0 || program->n_terms > SDE_USER_MAX_TERMS) {
+        err = "invalid program or group size (1..8, whole components of a system)";
     } else {
-        const int maxm = group_size <= 1 ? 1 : group_size <= 2 ? 2 : group_size <= 4 ? 4 : 8;
-        rc = sdegpu::jit_compile_check_adjoint(*program, precision == SDE_FP64, maxm, &err);
+        rc = sdegpu::jit_compile_check_adjoint(*program, precision == SDE_FP64, group_size, &err);
     }
     if (log && len > 0) {
         strncpy(log, err.c_str(), (size_t)len - 1);

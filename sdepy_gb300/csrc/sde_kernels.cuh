@@ -714,6 +714,25 @@ __device__ __forceinline__ void user_eval(const SdeUserProgram &u, const R *xs, 
         user_coefs<R>(u, xs, t, p, out);
 }
 
+// a user program's shape: the equations, the terms and each term's source
+// (SDE_SRC_*), compile-time constants of a compiled program (UserJitFn's
+// NEQ, NT, src), else read from the program
+template <typename R, int MODEL>
+__device__ __forceinline__ int user_neq(const SdeUserProgram &u) {
+    if constexpr (MODEL == SDE_MODEL_USER_JIT || MODEL == SDE_MODEL_USER_SYS_JIT) return UserJitFn<R>::NEQ;
+    else return u.n_eq;
+}
+template <typename R, int MODEL>
+__device__ __forceinline__ int user_nt(const SdeUserProgram &u) {
+    if constexpr (MODEL == SDE_MODEL_USER_JIT || MODEL == SDE_MODEL_USER_SYS_JIT) return UserJitFn<R>::NT;
+    else return u.n_terms;
+}
+template <typename R, int MODEL>
+__device__ __forceinline__ int user_src(const SdeUserProgram &u, int i) {
+    if constexpr (MODEL == SDE_MODEL_USER_JIT || MODEL == SDE_MODEL_USER_SYS_JIT) return UserJitFn<R>::src(i);
+    else return u.term_source[i];
+}
+
 // ---------------------------------------------------------------------------
 // the forward kernel
 // ---------------------------------------------------------------------------
@@ -1125,45 +1144,65 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                             const R xm[1] = {st[m]};
                             user_eval<R, MODEL>(a.uprog, xm, tk, pv, A2);
                             R s = R(0);
-                            for (int i = 0; i < a.uprog.n_terms; ++i) {
-                                const R dz = user_dz(a.uprog.term_source[i], dt, dW[m], dJ[m], m);
-                                const R term = A::mul(A2[0][i], dz);
-                                s = i == 0 ? term : A::add(s, term);
-                            }
+#pragma unroll
+                            for (int i = 0; i < SDE_USER_MAX_TERMS; ++i)
+                                if (i < user_nt<R, MODEL>(a.uprog)) {
+                                    const R dz = user_dz(user_src<R, MODEL>(a.uprog, i), dt, dW[m], dJ[m], m);
+                                    const R term = A::mul(A2[0][i], dz);
+                                    s = i == 0 ? term : A::add(s, term);
+                                }
                             st[m] = A::add(st[m], s);
                         }
                     } else if (MODEL == SDE_MODEL_USER_SYS || MODEL == SDE_MODEL_USER_SYS_JIT) {
                         // the group is one last-axis slice: equation e's component
                         // h at e * nc + h; the program runs per component on the
-                        // states of every equation, then all states step at once
-                        const int q = a.uprog.n_eq, nc = M / q;
-                        R sv[MAXM], dv[MAXM], nx[MAXM];
+                        // states of every equation, then all states step at once.
+                        // States are gathered and scattered by unrolled selects
+                        // (compile-time indices: registers, not local memory).
+                        const int q = user_neq<R, MODEL>(a.uprog), nc = M / q;
+                        R nx[MAXM];
 #pragma unroll
-                        for (int m = 0; m < MAXM; ++m) {
-                            sv[m] = st[m];
-                            dv[m] = dW[m];
-                            nx[m] = st[m];
-                        }
-                        for (int h = 0; h < nc; ++h) {
+                        for (int m = 0; m < MAXM; ++m) nx[m] = st[m];
+#pragma unroll
+                        for (int h = 0; h < MAXM; ++h) {
+                            if (h >= nc) break;
                             R xs[SDE_USER_MAX_EQ], A2[SDE_USER_MAX_EQ][SDE_USER_MAX_TERMS];
-                            for (int e = 0; e < q; ++e) xs[e] = sv[e * nc + h];
+#pragma unroll
+                            for (int e = 0; e < SDE_USER_MAX_EQ; ++e) {
+                                xs[e] = R(0);
+#pragma unroll
+                                for (int m = 0; m < MAXM; ++m)
+                                    if (e < q && m == e * nc + h) xs[e] = st[m];
+                            }
                             // parameters broadcast along the equations: component h's
-                            R pv[6];
-                            for (int m = 0; m < MAXM; ++m)
-                                if (m == h) {
-                                    pv[0] = c0[m], pv[1] = c1[m], pv[2] = c2[m];
-                                    pv[3] = c3[m], pv[4] = c4[m], pv[5] = c5[m];
-                                }
+                            const R pv[6] = {c0[h], c1[h], c2[h], c3[h], c4[h], c5[h]};
                             user_eval<R, MODEL>(a.uprog, xs, tk, pv, A2);
-                            for (int e = 0; e < q; ++e) {
-                                const int m = e * nc + h;
+#pragma unroll
+                            for (int e = 0; e < SDE_USER_MAX_EQ; ++e) {
+                                if (e >= q) break;
+                                const int mm = e * nc + h;
+                                R dwv = R(0), djv = R(0), dnv = R(0);
+#pragma unroll
+                                for (int m = 0; m < MAXM; ++m)
+                                    if (m == mm) {
+                                        dwv = dW[m];
+                                        djv = dJ[m];
+                                        if constexpr (USER && JUMPS) dnv = dN[m];
+                                    }
                                 R s = R(0);
-                                for (int i = 0; i < a.uprog.n_terms; ++i) {
-                                    const R dz = user_dz(a.uprog.term_source[i], dt, dv[m], dJ[m], m);
-                                    const R term = A::mul(A2[e][i], dz);
-                                    s = i == 0 ? term : A::add(s, term);
-                                }
-                                nx[m] = A::add(sv[m], s);
+#pragma unroll
+                                for (int i = 0; i < SDE_USER_MAX_TERMS; ++i)
+                                    if (i < user_nt<R, MODEL>(a.uprog)) {
+                                        const int src = user_src<R, MODEL>(a.uprog, i);
+                                        const R dz = src == SDE_SRC_DT ? dt : src == SDE_SRC_DW ? dwv
+                                                     : src == SDE_SRC_DJ ? djv : src == SDE_SRC_DN ? dnv : R(0);
+                                        const R term = A::mul(A2[e][i], dz);
+                                        s = i == 0 ? term : A::add(s, term);
+                                    }
+                                const R v = A::add(xs[e], s);
+#pragma unroll
+                                for (int m = 0; m < MAXM; ++m)
+                                    if (m == mm) nx[m] = v;
                             }
                         }
 #pragma unroll

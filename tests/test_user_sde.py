@@ -226,19 +226,21 @@ def test_user_sde_refusals():
     from sdepy_gb300.autograd import expectation
     import torch
     x0 = torch.tensor(1., requires_grad=True)
-    for spec in ('integrate_q2:user_sv', 'integrate_log:user_jd_log'):   # systems, jump terms
-        with pytest.raises(NotImplementedError):
-            expectation(user_class(sg, spec), (0., 1.), [], paths=100, steps=10, x0=x0)
+    with pytest.raises(NotImplementedError):   # expectations of scalar processes
+        expectation(cls, (0., 1.), [], paths=100, steps=10, x0=x0, vshape=3)
+    with pytest.raises(NotImplementedError):   # x0 of a system: a scalar or one per equation
+        expectation(user_class(sg, 'integrate_q2:user_sv'), (0., 1.), [], paths=100, steps=10,
+                    x0=torch.tensor([1., .1, 2.], requires_grad=True))
     with pytest.raises(NotImplementedError):   # a time-dependent parameter
         expectation(cls, (0., 1.), [], paths=100, steps=10, x0=x0, theta=lambda t: t)
 
 
-def _grads(cls, strikes, dtype=np.float64, **kw):
+def _grads(cls, strikes, dtype=np.float64, steps=64, **kw):
     """(value, {name: gradient}) of expectation() for torch-scalar kw."""
     import torch
     from sdepy_gb300.autograd import expectation
     ts = {k: torch.tensor(float(v), dtype=torch.float64, requires_grad=True) for k, v in kw.items()}
-    y = expectation(cls, (0., 1.), strikes, paths=200003, steps=64, dtype=dtype, seed=21, stream=3, **ts)
+    y = expectation(cls, (0., 1.), strikes, paths=200003, steps=steps, dtype=dtype, seed=21, stream=3, **ts)
     y.sum().backward()
     return y.detach().numpy(), {k: float(t.grad) for k, t in ts.items()}
 
@@ -447,10 +449,10 @@ def test_gpu_user_merton_equals_preset(lib):
 # runtime compilation of the programs (NVRTC)
 # ---------------------------------------------------------------------------
 def test_jit_compiles_every_program():
-    """Every test function's program compiles into the forward kernel
-    through the library's code generator and NVRTC (no device needed), in
-    both precisions, for single groups and the widths the tests use, with
-    device and injected noise."""
+    """Every test function's program compiles into the forward kernel and
+    into the reverse-mode adjoint kernel through the library's code
+    generator and NVRTC (no device needed), in both precisions, for single
+    groups and the widths the tests use, with device and injected noise."""
     import ctypes as C
     from sdepy_gb300 import _build
     _build.build()
@@ -471,9 +473,10 @@ def test_jit_compiles_every_program():
         inj = (i // 4) % 2
         rc = lib.sde_jit_compile(C.byref(cls._program), prec, M, inj, jumps, buf, 1024)
         assert rc == 0, (name, prec, M, inj, buf.value.decode())
-        if not q and not jumps and i % 3 == 0:   # adjoint kernels of single equations
-            rc = lib.sde_jit_compile_adjoint(C.byref(cls._program), prec, M, buf, 1024)
-            assert rc == 0, (name, 'adjoint', prec, M, buf.value.decode())
+        # the reverse-mode adjoint kernel of every program (systems and jump
+        # terms included), in the other precision
+        rc = lib.sde_jit_compile_adjoint(C.byref(cls._program), _lib.FP32 + _lib.FP64 - prec, M, buf, 1024)
+        assert rc == 0, (name, 'adjoint', prec, M, buf.value.decode())
 
 
 JIT_CASES = [
@@ -525,15 +528,109 @@ def test_gpu_jit_replays_reference(lib):
 
 @pytest.mark.gpu
 def test_gpu_jit_adjoint_equals_interpreter(lib):
-    """The compiled tangent-mode program gives the interpreted adjoint's
-    gradients (FP64, the same rounded operations) for a CEV and a mixed
-    SDE, with a mean and a call payoff."""
-    for spec, kw in (('integrate:user_cev', dict(x0=1., mu=.05, sigma=.3, gamma=.7)),
-                     ('integrate:user_mixed', dict(x0=.5, a=1.5, b=.7, s=.25))):
-        res = [_grads(user_class(sg, spec, jit=jit), [1.], **kw) for jit in (False, True)]
+    """The compiled reverse-mode adjoint (the program's generated backward
+    step) gives the interpreted tangent-mode adjoint's gradients (FP64: the
+    same paths, the chain rule summed in another order) for a CEV and a
+    mixed SDE, with a mean and a call payoff; and over 2000 steps, where the
+    compiled kernel's shared-memory segments take two checkpoint levels."""
+    for spec, kw, steps in (('integrate:user_cev', dict(x0=1., mu=.05, sigma=.3, gamma=.7), 64),
+                            ('integrate:user_mixed', dict(x0=.5, a=1.5, b=.7, s=.25), 64),
+                            ('integrate:user_ou', dict(x0=.1, theta=.6, k=2., sigma=.3), 2000)):
+        res = [_grads(user_class(sg, spec, jit=jit), [1.], steps=steps, **kw) for jit in (False, True)]
         np.testing.assert_allclose(res[0][0], res[1][0], rtol=1e-13)
         for n in kw:
             assert abs(res[0][1][n] - res[1][1][n]) <= 1e-12*max(1., abs(res[0][1][n])), (spec, n)
+
+
+def _sys_grads(cls, strikes, tensors, dtype=np.float64, paths=100003, steps=50, tl=(0., 1.), **plain):
+    """(value, {name: gradient}) of expectation() with torch-tensor entries
+    ``tensors`` (a tuple value: one per equation) and plain keywords."""
+    import torch
+    from sdepy_gb300.autograd import expectation
+    ts = {k: torch.tensor(v, dtype=torch.float64, requires_grad=True) for k, v in tensors.items()}
+    y = expectation(cls, tl, strikes, paths=paths, steps=steps, dtype=dtype, seed=31, stream=2, **ts, **plain)
+    y.sum().backward()
+    return y.detach().numpy(), {k: t.grad.numpy().copy() for k, t in ts.items()}
+
+
+def _check_fd(cls, strikes, tensors, plain, rel=1e-6, **run):
+    """The adjoint gradient of every tensor entry against the central
+    difference of the forward value on common random numbers (FP64, h =
+    1e-4 relative)."""
+    v, g = _sys_grads(cls, strikes, tensors, **run, **plain)
+    for n, base in tensors.items():
+        b = np.atleast_1d(np.asarray(base, dtype=float))
+        for i in range(b.size):
+            h = 1e-4*max(abs(b[i]), 1e-2)
+            up, dn = b.copy(), b.copy()
+            up[i] += h
+            dn[i] -= h
+            as_arg = (lambda x: tuple(x)) if np.ndim(base) else (lambda x: float(x[0]))
+            fu = _sys_grads(cls, strikes, dict(tensors, **{n: as_arg(up)}), **run, **plain)[0].sum()
+            fdn = _sys_grads(cls, strikes, dict(tensors, **{n: as_arg(dn)}), **run, **plain)[0].sum()
+            fd = (fu - fdn)/(2*h)
+            gi = np.atleast_1d(g[n])[i]
+            assert abs(gi - fd) <= rel*max(1., abs(fd)), (n, i, gi, fd)
+    return v, g
+
+
+@pytest.mark.gpu
+def test_gpu_user_system_adjoint_matches_finite_differences(lib):
+    """Systems (compiled reverse-mode adjoint): the expectation of the first
+    equation's process; the gradients of x0 (one value per equation) and of
+    every parameter equal central differences on common random numbers
+    (of the mean: a payoff's kink makes differences of paths that cross the
+    strike) -- a stochastic-volatility system with correlated
+    Wiener terms (a variance that stays many standard deviations away from
+    0, where sqrt's derivative makes the pathwise estimator heavy-tailed
+    and no longer the differences' limit at h = 1e-4) and two coupled
+    OU-like equations, the second without a Wiener term; FP32 agrees with
+    FP64 to FP32 accuracy, with a call payoff."""
+    sv = user_class(sg, 'integrate_q2:user_sv')
+    t_sv = dict(x0=(100., .09), mu=.05, k=3., theta=.09, xi=.1)
+    _check_fd(sv, [], t_sv, dict(rho=-.6))
+    co = user_class(sg, 'integrate_q2:user_coupled')
+    t_co = dict(x0=(.5, -.2), a=1.2, b=.5, c=.3, s=.2)
+    _check_fd(co, [], t_co, {})
+    v64, g64 = _sys_grads(co, [.3], t_co)
+    v32, g32 = _sys_grads(co, [.3], t_co, dtype=np.float32)
+    for n in g64:
+        assert np.max(np.abs(g32[n] - g64[n])) <= 2e-3*max(1., np.max(np.abs(g64[n]))), (n, g32[n], g64[n])
+
+
+@pytest.mark.gpu
+def test_gpu_user_jump_adjoint_matches_finite_differences(lib):
+    """dn / dj terms (compiled reverse-mode adjoint; Poisson counts and jump
+    sizes are common random numbers, not differentiated): every source in
+    one SDE (dn, dt, dj, dw), a time-dependent intensity, and a system with
+    compound Poisson and Wiener terms -- gradients against central
+    differences; FP32 against FP64."""
+    j4 = user_class(sg, 'integrate:user_jumps4')
+    t4 = dict(x0=.5, a=.3, b=.5, s=.2)
+    _check_fd(j4, [], t4, dict(lam=2., y=sg.exp_rv(.2)))
+    _check_fd(j4, [], t4, dict(lam=lambda t: 1. + t, y=sg.double_exp_rv(.1, .2, .4)))
+    sj = user_class(sg, 'integrate_q2:user_sys_dj_dw')
+    tsj = dict(x0=(.1, .2), k=.7)
+    _check_fd(sj, [], tsj, dict(lam=3., y=sg.norm_rv(.1, .2)))
+    v64, g64 = _sys_grads(sj, [.5], tsj, lam=3., y=sg.norm_rv(.1, .2))
+    v32, g32 = _sys_grads(sj, [.5], tsj, dtype=np.float32, lam=3., y=sg.norm_rv(.1, .2))
+    for n in g64:
+        assert np.max(np.abs(g32[n] - g64[n])) <= 2e-3*max(1., np.max(np.abs(g64[n]))), (n, g32[n], g64[n])
+
+
+@pytest.mark.gpu
+def test_gpu_user_merton_adjoint_equals_preset(lib):
+    """Merton's jump diffusion written as a user SDE in log space (a dj
+    term) gives the preset's adjoint gradients for x0, mu and sigma: the same
+    paths (the forwards are bit-identical), the preset's constant-adjoint
+    sweep against the program's reverse-mode steps."""
+    kw = dict(x0=1.1, mu=.03, sigma=.15)
+    vu, gu = _sys_grads(user_class(sg, 'integrate_log:user_jd_log'), [1., 1.2], kw, lam=1.5,
+                        y=sg.norm_rv(-.1, .15))
+    vp, gp = _sys_grads(sg.merton_jumpdiff_process, [1., 1.2], kw, lam=1.5, a=-.1, b=.15)
+    np.testing.assert_allclose(vu, vp, rtol=1e-12)
+    for n in kw:
+        assert abs(gu[n] - gp[n]) <= 1e-9*max(1., abs(gp[n])), (n, gu[n], gp[n])
 
 
 # ---------------------------------------------------------------------------
