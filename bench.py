@@ -499,9 +499,10 @@ def heston_gradient_check(lib, batches=16, paths=2**18, steps=500):
     return out
 
 
-def _fused(lib, P, timeline, strikes, seed):
+def _fused(lib, P, timeline, strikes, seed, ckpt=None):
     """One forward run of process P with the fused summary (moments and
-    call payoffs) of the last timeline point; no path written."""
+    call payoffs) of the last timeline point; no path written (ckpt: the
+    adjoint's checkpoints, (device pointer, segment), written too)."""
     import ctypes as C
     from sdepy_gb300 import _lib
     from sdepy_gb300.grid import Grid
@@ -511,6 +512,8 @@ def _fused(lib, P, timeline, strikes, seed):
     g.n_pts, g.step_offset = leg.tt.size, 0
     o = _lib.SdeOut()
     o.xx, o.n_rows, o.on_device = None, len(timeline), 0
+    if ckpt is not None:
+        o.ckpt, o.ckpt_seg = ckpt
     ptab = P._params_table(leg) if P._tdep else None          # time-dependent parameters
     ctab = P._corr_table(leg) if P._corr_tdep else None       # and correlations
     ltab = P._lam_table(leg)                                  # a user SDE's intensity
@@ -599,6 +602,9 @@ def extra_configs(lib):
     def fused(P, timeline, strikes, seed):
         return _fused(lib, P, timeline, strikes, seed)
 
+    def fused_ck(P, timeline, strikes, seed, ckpt):
+        return _fused(lib, P, timeline, strikes, seed, ckpt)
+
     import time
     # ---- Heston, 2^22 paths, 499 steps on (0, 2)
     tl = (0., 2.)
@@ -607,7 +613,7 @@ def extra_configs(lib):
     fwd_ms = _time_call(lambda: fused(H, tl, STRIKES, 3), lib)
     arrs, _ = fused(H, tl, STRIKES, 3)
 
-    def adj():
+    def adj(ckpt=None):
         g = _lib.SdeGrid()
         g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
         g.n_pts, g.step_offset = leg.tt.size, 0
@@ -615,6 +621,8 @@ def extra_configs(lib):
         req.n_strikes, req.checkpoint, req.mean_weight = 5, 0, 0.
         for i, K in enumerate(STRIKES):
             req.strikes[i], req.weights[i] = K, .2
+        if ckpt is not None:
+            req.ckpt, req.checkpoint = ckpt
         grad = np.zeros((2, 8))
         v = C.c_double()
         spec = H._make_spec(3, 0)
@@ -622,6 +630,23 @@ def extra_configs(lib):
         return grad
     adj_ms = _time_call(adj, lib)
     grad = adj()
+    # the forward writing the adjoint's checkpoints to device memory, and
+    # the adjoint reading them instead of its own checkpoint sweep (the
+    # sequence autograd.expectation runs)
+    import torch
+    g = _lib.SdeGrid()
+    g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
+    g.n_pts, g.step_offset = leg.tt.size, 0
+    seg, nb = C.c_int32(), C.c_int64()
+    _lib.check(lib.sde_adjoint_checkpoints(C.byref(H._make_spec(3, 0)), C.byref(g), C.byref(seg), C.byref(nb)),
+               'ckpts')
+    ckbuf = torch.empty(nb.value, dtype=torch.uint8, device='cuda')
+    ck = (ckbuf.data_ptr(), seg.value)
+    fwd_ck_ms = _time_call(lambda: fused_ck(H, tl, STRIKES, 3, ck), lib)
+    fused_ck(H, tl, STRIKES, 3, ck)
+    adj_ck_ms = _time_call(lambda: adj(ck), lib)
+    grad_ck = adj(ck)
+    del ckbuf
     check = heston_gradient_check(lib)
     # FP64 on identical noise: the same paths, the same call
     H64 = sg.heston_process(paths=2**22, steps=500, **HESTON)
@@ -650,6 +675,12 @@ def extra_configs(lib):
         'paths': 2**22, 'computed_steps': n,
         'fp32_forward_ms': fwd_ms, 'fp32_adjoint_ms': adj_ms,
         'grad_over_forward': adj_ms/fwd_ms,
+        'from_forward_checkpoints': {
+            'checkpoint_bytes': nb.value, 'segment': seg.value,
+            'fp32_forward_writing_them_ms': fwd_ck_ms, 'fp32_adjoint_ms': adj_ck_ms,
+            'grad_over_forward': adj_ck_ms/fwd_ms,
+            'forward_plus_gradient_over_forward': (fwd_ck_ms + adj_ck_ms)/fwd_ms,
+            'gradient_identical': bool(np.array_equal(grad, grad_ck))},
         'fp32_path_steps_per_s': 2**22*n/(fwd_ms*1e-3),
         'fp64_path_steps_per_s': 2**22*n/(fwd64_ms*1e-3),
         'call_prices': [float(x) for x in arrs[1][0]],
@@ -991,7 +1022,25 @@ def run_case(args):
             _lib.check(lib.sde_adjoint(C.byref(spec), C.byref(g), C.byref(req), _lib.dptr(grad), C.byref(v)), 'adj')
             lib.sde_timing(-1, last)
             ms.append(last[0])
+        # the same after forward runs that wrote the checkpoints
+        seg, nb = C.c_int32(), C.c_int64()
+        _lib.check(lib.sde_adjoint_checkpoints(C.byref(H._make_spec(3, 0)), C.byref(g), C.byref(seg),
+                                               C.byref(nb)), 'ckpts')
+        ckbuf = torch.empty(nb.value, dtype=torch.uint8, device='cuda')
+        fms, cms = [], []
+        for i in range(args.warmup + args.steps):
+            _fused(lib, H, (0., 2.), STRIKES, 3, (ckbuf.data_ptr(), seg.value))
+            lib.sde_timing(-1, last)
+            fms.append(last[0] + last[1])
+            req.ckpt, req.checkpoint = ckbuf.data_ptr(), seg.value
+            spec = H._make_spec(3, 0)
+            _lib.check(lib.sde_adjoint(C.byref(spec), C.byref(g), C.byref(req), _lib.dptr(grad), C.byref(v)), 'adj')
+            lib.sde_timing(-1, last)
+            cms.append(last[0])
+            req.ckpt, req.checkpoint = None, 0
         print(json.dumps({'case': args.case, 'adjoint_ms': float(np.median(ms[args.warmup:])),
+                          'forward_writing_checkpoints_ms': float(np.median(fms[args.warmup:])),
+                          'adjoint_from_checkpoints_ms': float(np.median(cms[args.warmup:])),
                           'value': float(v.value)}))
     elif args.case == 'batch':
         from sdepy_gb300.batch import batch, synthetic_instances

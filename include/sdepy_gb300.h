@@ -39,7 +39,7 @@ extern "C" {
 #define SDE_API
 #endif
 
-#define SDE_ABI_VERSION 5
+#define SDE_ABI_VERSION 6
 
 #define SDE_MAX_GROUP   16   /* largest correlated group (state vars) */
 #define SDE_MAX_PARAMS  6    /* coefficient arrays per state variable */
@@ -217,6 +217,16 @@ typedef struct SdeOut {
     int32_t *neg_count;     /* HESTON: [groups*M/2][paths] steps with y < 0, or NULL */
     int32_t *jump_count;    /* jumps:  [groups*M][paths] Poisson events, or NULL     */
     int64_t *row_jumps;     /* jumps:  [n_rows] events per output interval, or NULL  */
+    /* Adjoint checkpoints, or NULL: device memory the run fills with the
+     * state before every ckpt_seg-th step (steps 0, ckpt_seg, 2 ckpt_seg,
+     * ...), [ceil(n_steps / ckpt_seg)][groups*M][paths] in the spec's
+     * precision, so that an sde_adjoint of the same spec and grid reads them
+     * (SdeAdjReq.ckpt) instead of its own forward sweep;
+     * sde_adjoint_checkpoints gives the segment and the bytes.  Device RNG
+     * only, no antithetic paths; the FP32 LINEAR / OU run-table kernels
+     * write none (SDE_ERR_UNSUPPORTED; the adjoint recomputes them). */
+    void *ckpt;
+    int32_t ckpt_seg;
 } SdeOut;
 
 typedef struct SdeStatsReq {
@@ -374,10 +384,26 @@ typedef struct SdeAdjReq {
      * memory: steps x 3 x group width x 4 (FP32) or 8 (FP64) bytes must not
      * exceed 160 KiB. */
     double *grad_t;
+    /* Checkpoints written by the forward run of the same spec and grid
+     * (SdeOut.ckpt with ckpt_seg == checkpoint), or NULL: the adjoint then
+     * skips its checkpoint sweep and recomputes each segment from them, and
+     * takes the terminal states from the last segment's recomputation.  The
+     * gradient is the same: bit for bit in FP64 (the forward's and the
+     * adjoint's paths are the same rounded operations), to FP32 rounding in
+     * FP32 (the compiler may fuse a product into a sum differently in the
+     * two kernels). */
+    const void *ckpt;
 } SdeAdjReq;
 
 SDE_API int32_t sde_adjoint(const SdeSpec *spec, const SdeGrid *grid,
                             const SdeAdjReq *req, double *grad, double *value);
+
+/* The checkpoints sde_adjoint can read for (spec, grid): *seg the steps per
+ * segment to pass as SdeOut.ckpt_seg and SdeAdjReq.checkpoint, *bytes the
+ * size of the SdeOut.ckpt array.  *seg = 0 (and *bytes = 0) where the
+ * adjoint takes none: the LINEAR model (one sweep), the FP32 LINEAR / OU
+ * run-table forward, time-dependent parameters. */
+SDE_API int32_t sde_adjoint_checkpoints(const SdeSpec *spec, const SdeGrid *grid, int32_t *seg, int64_t *bytes);
 
 /* sde_run_stats for callers that cannot allocate device memory: a serving
  * or real-time loop where cudaMalloc's implicit synchronisation is not

@@ -13,7 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, '_native', 'libsdepy_gb300.so')
 
-ABI_VERSION = 5
+ABI_VERSION = 6
 MAX_GROUP = 16
 MAX_PARAMS = 6
 MAX_STRIKES = 8
@@ -68,7 +68,8 @@ class SdeNoise(C.Structure):
 class SdeOut(C.Structure):
     _fields_ = [('xx', C.c_void_p), ('n_rows', C.c_int32),
                 ('on_device', C.c_int32), ('neg_count', _ip),
-                ('jump_count', _ip), ('row_jumps', _lp)]
+                ('jump_count', _ip), ('row_jumps', _lp),
+                ('ckpt', C.c_void_p), ('ckpt_seg', C.c_int32)]
 
 
 class SdeStatsReq(C.Structure):
@@ -88,7 +89,8 @@ class SdeAdjReq(C.Structure):
                 ('strikes', C.c_double*MAX_STRIKES),
                 ('weights', C.c_double*MAX_STRIKES),
                 ('mean_weight', C.c_double),
-                ('grad_t', C.POINTER(C.c_double))]
+                ('grad_t', C.POINTER(C.c_double)),
+                ('ckpt', C.c_void_p)]
 
 
 class SdeBatchInstance(C.Structure):
@@ -133,6 +135,8 @@ SIGNATURES = {
                                   C.POINTER(SdeStatsOut)]),
     'sde_adjoint': (C.c_int32, [C.POINTER(SdeSpec), C.POINTER(SdeGrid),
                                 C.POINTER(SdeAdjReq), _dp, _dp]),
+    'sde_adjoint_checkpoints': (C.c_int32, [C.POINTER(SdeSpec), C.POINTER(SdeGrid),
+                                            C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
     'sde_run_stats_static': (C.c_int32, [C.POINTER(SdeSpec), C.POINTER(SdeGrid),
                                          C.POINTER(SdeStatsReq),
                                          C.POINTER(SdeStatsOut), C.c_void_p]),

@@ -5,8 +5,11 @@ x0=torch.tensor(100., requires_grad=True), ...)`` returns the torch tensor
 ``[E[X_T], E[max(X_T - K_1, 0)], ...]`` of the terminal values of a scalar
 preset process; its backward pass runs the adjoint kernel of the Euler
 recursion (sde_adjoint) on the same Philox paths, recomputing states from
-checkpoints instead of storing them.  Any parameter passed as a torch tensor
-with requires_grad receives d(output)/d(parameter).
+checkpoints instead of storing them.  The forward run writes those
+checkpoints (the state every ~sqrt(steps) steps, in device memory, up to
+CHECKPOINT_SHARE of the free memory) where its kernel can, so that the
+backward pass skips the adjoint's own checkpoint sweep.  Any parameter passed
+as a torch tensor with requires_grad receives d(output)/d(parameter).
 
 Differentiable parameters per preset:
   wiener_process            x0, mu, sigma
@@ -112,7 +115,8 @@ class _Expectation(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, spec_fn, names, mp, *tensors):
-        proc, grid, strikes, seed, stream, value = spec_fn()
+        proc, grid, strikes, seed, stream, value, ckpt = spec_fn()
+        ctx.ckpt = ckpt
         ctx.spec_fn = spec_fn
         ctx.names = names
         ctx.mp = mp
@@ -122,7 +126,7 @@ class _Expectation(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, grad_out):
-        proc, grid, strikes, seed, stream, _ = ctx.spec_fn(run=False)
+        proc, grid, strikes, seed, stream, _, _ = ctx.spec_fn(run=False)
         lib = _lib.load()
         w = grad_out.detach().to('cpu', torch.float64).numpy()
         req = _lib.SdeAdjReq()
@@ -151,8 +155,12 @@ class _Expectation(torch.autograd.Function):
             g.params_t = _lib.dptr(ptab)
             gt = np.zeros((leg.tt.size - 1, 3, proc._W))
             req.grad_t = _lib.dptr(gt)
+        if ctx.ckpt is not None:   # the forward's checkpoints: no checkpoint sweep
+            buf, seg = ctx.ckpt
+            req.ckpt, req.checkpoint = buf.data_ptr(), seg
         st = lib.sde_adjoint(C.byref(spec), C.byref(g), C.byref(req),
                              _lib.dptr(grad), C.byref(val))
+        ctx.ckpt = None
         _lib.check(st, 'sde_adjoint')
         mp = ctx.mp if ctx.mp is not None else _MAP[name]
         if td:
@@ -247,15 +255,45 @@ def expectation(cls, timeline, strikes=(), *, paths, steps=None,
         P = cls(paths=paths, steps=steps, dtype=dtype,
                 rng=philox_rng(seed, stream), **plain)
         grid = Grid(timeline, steps, 0)
-        value = None
+        value = ckpt = None
         if run:
+            ckpt = _checkpoints(P, grid, seed, stream)
+            if ckpt is not None:
+                P._ckpt_out = (ckpt[0].data_ptr(), ckpt[1])
             mc = P.montecarlo(timeline, bins=None, strikes=strikes)
+            P._ckpt_out = None
             # the first state: a scalar process, or a system's first equation
             value = np.concatenate(([float(np.asarray(mc.mean()).reshape(-1)[0])],
                                     np.asarray(mc.payoff).reshape(-1)[:len(strikes)]))
-        return P, grid, strikes, seed, stream, value
+        return P, grid, strikes, seed, stream, value, ckpt
 
     return _Expectation.apply(spec_fn, tuple(names), mp, *tensors)
+
+
+# the largest share of free device memory the forward's checkpoints may take
+CHECKPOINT_SHARE = .25
+
+
+def _checkpoints(P, grid, seed, stream):
+    """(device buffer, segment) for the forward run to write the adjoint's
+    checkpoints into (sde_adjoint_checkpoints), or None: the models and
+    kernels that take none, device memory too short, no CUDA device."""
+    if not torch.cuda.is_available():
+        return None
+    lib = _lib.load()
+    leg = grid.legs[-1]
+    g = _lib.SdeGrid()
+    g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
+    g.n_pts, g.step_offset = leg.tt.size, leg.step_offset
+    ptab = P._params_table(leg) if P._tdep else None
+    g.params_t = _lib.dptr(ptab)
+    spec = P._make_spec(seed, stream)
+    seg, nbytes = C.c_int32(), C.c_int64()
+    _lib.check(lib.sde_adjoint_checkpoints(C.byref(spec), C.byref(g), C.byref(seg), C.byref(nbytes)),
+               'sde_adjoint_checkpoints')
+    if seg.value < 1 or nbytes.value > CHECKPOINT_SHARE*torch.cuda.mem_get_info()[0]:
+        return None
+    return torch.empty(nbytes.value, dtype=torch.uint8, device='cuda'), seg.value
 
 
 def _numpy_of(f):

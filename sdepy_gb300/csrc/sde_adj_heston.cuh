@@ -58,11 +58,12 @@ static __global__ void __launch_bounds__(BLOCK, 3) sde_adj_heston_kernel(const _
             if (X > ks[s]) d += kw[s];
         return d;
     };
-    // the correlated increments of a step from its normals (correlate())
+    // the correlated increments of a step from its normals (correlate()'s
+    // operations)
     auto incr = [&](float z0, float z1, float sq, float &dWx, float &dWy) {
         if (corr) {
-            dWx = (L00 * z0) * sq;
-            dWy = fmaf(L11, z1, L10 * z0) * sq;
+            dWx = A::mul(A::mul(L00, z0), sq);
+            dWy = A::mul(A::add(A::mul(L10, z0), A::mul(L11, z1)), sq);
         } else {
             dWx = z0 * sq;
             dWy = z1 * sq;
@@ -89,31 +90,49 @@ static __global__ void __launch_bounds__(BLOCK, 3) sde_adj_heston_kernel(const _
         const PathPre<1> pre(key, (uint32_t)p + a.path_offset, (uint32_t)g, a.stream);
         PairedSteps<float, 2> pair;
         float ck[ADJ_MAXSEG][2];
-        float x = x0a, y = x0b;
-        for (int k = 0, kc = 0, ci = 0; k < n_steps; ++k) {
-            if (kc == 0) {   // a checkpoint every seg steps
-                ck[ci][0] = x;
-                ck[ci][1] = y;
-                ++ci;
-            }
-            kc = kc + 1 == seg ? 0 : kc + 1;
-            float z0, z1, dWx, dWy;
-            pair.get(key, pre, k, step_offset, z0, z1);
-            incr(z0, z1, __ldg(a.sqdt + k), dWx, dWy);
-            step(__ldg(a.dt + k), dWx, dWy, x, y);
-        }
+        float val = 0.f, xbx = 0.f, xby = 0.f;
         // terminal adjoint (HESTON_X: f(exp(x)); HESTON_XY adds f(y))
-        const float X = A::exp_(x);
-        float val = fval(X);
-        float xbx = fder(X) * X, xby = 0.f;
-        if (out_xy) {
-            val += fval(y);
-            xby = fder(y);
+        auto terminal = [&](float x, float y) {
+            const float X = A::exp_(x);
+            val = fval(X);
+            xbx = fder(X) * X;
+            xby = 0.f;
+            if (out_xy) {
+                val += fval(y);
+                xby = fder(y);
+            }
+        };
+        // checkpoints every seg steps: this sweep, or the forward's (device
+        // memory; the terminal adjoint then follows the last segment's
+        // recomputation)
+        const bool fromck = a.ckpt != nullptr;
+        if (!fromck) {
+            float x = x0a, y = x0b;
+            for (int k = 0, kc = 0, ci = 0; k < n_steps; ++k) {
+                if (kc == 0) {
+                    ck[ci][0] = x;
+                    ck[ci][1] = y;
+                    ++ci;
+                }
+                kc = kc + 1 == seg ? 0 : kc + 1;
+                float z0, z1, dWx, dWy;
+                pair.get(key, pre, k, step_offset, z0, z1);
+                incr(z0, z1, __ldg(a.sqdt + k), dWx, dWy);
+                step(__ldg(a.dt + k), dWx, dWy, x, y);
+            }
+            terminal(x, y);
         }
         float gmu = 0.f, gsg = 0.f, grho = 0.f, gk = 0.f, gth = 0.f, gxi = 0.f;
         for (int s = nseg - 1; s >= 0; --s) {
             const int k0 = s * seg, k1 = min(k0 + seg, n_steps);
-            float sx = ck[s][0], sy = ck[s][1];
+            float sx, sy;
+            if (fromck) {
+                sx = a.ckpt[((int64_t)s * W + g * 2) * a.paths + p];
+                sy = a.ckpt[((int64_t)s * W + g * 2 + 1) * a.paths + p];
+            } else {
+                sx = ck[s][0];
+                sy = ck[s][1];
+            }
             for (int k = k0; k < k1; ++k) {
                 float z0, z1, dWx, dWy;
                 pair.get(key, pre, k, step_offset, z0, z1);
@@ -124,6 +143,7 @@ static __global__ void __launch_bounds__(BLOCK, 3) sde_adj_heston_kernel(const _
                 incr(z0, z1, __ldg(a.sqdt + k), dWx, dWy);
                 step(__ldg(a.dt + k), dWx, dWy, sx, sy);
             }
+            if (fromck && s == nseg - 1) terminal(sx, sy);
             for (int k = k1 - 1; k >= k0; --k) {
                 const float *b = hbuf + (k - k0) * 3 * BLOCK + threadIdx.x;
                 const float yv = b[0], z0 = b[BLOCK], z1 = b[2 * BLOCK];

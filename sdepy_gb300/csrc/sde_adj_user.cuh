@@ -184,33 +184,47 @@ __global__ void __launch_bounds__(BLOCK, MINB) sde_adj_user_kernel(const __grid_
             }
         };
 
-        // ---- forward sweep: level-1 checkpoints every seg steps ----------------
-        R ck[ADJ_MAXSEG][MG];
-        R st[MG];
-#pragma unroll
-        for (int m = 0; m < MG; ++m) st[m] = x0[m];
-        for (int k = 0, kc = 0, ci = 0; k < n_steps; ++k) {
-            if (kc == 0) {
-#pragma unroll
-                for (int m = 0; m < MG; ++m) ck[ci][m] = st[m];
-                ++ci;
-            }
-            kc = kc + 1 == seg ? 0 : kc + 1;
-            R dW[MAXM], dN[MAXM], dJ[MAXM];
-            noise(k, dW, dN, dJ);
-            step(k, st, dW, dN, dJ);
-        }
-        // ---- terminal adjoint --------------------------------------------------
+        // ---- terminal adjoint of the final states st ---------------------------
         R xb[MG], val = R(0);
-        const bool ex = a.out_mode == SDE_OUT_EXP;
+        R st[MG];
+        auto terminal = [&]() {
+            const bool ex = a.out_mode == SDE_OUT_EXP;
+            val = R(0);
 #pragma unroll
-        for (int m = 0; m < MG; ++m) {
-            xb[m] = R(0);
-            if (m < NF) {
-                const R X = ex ? A::exp_(st[m]) : st[m];
-                val += f_value(a, X);
-                xb[m] = ex ? f_prime(a, X) * X : f_prime(a, X);
+            for (int m = 0; m < MG; ++m) {
+                xb[m] = R(0);
+                if (m < NF) {
+                    const R X = ex ? A::exp_(st[m]) : st[m];
+                    val += f_value(a, X);
+                    xb[m] = ex ? f_prime(a, X) * X : f_prime(a, X);
+                }
             }
+        };
+        // ---- level-1 checkpoints every seg steps: this forward sweep, or the
+        // forward run's (device memory; the terminal adjoint then follows the
+        // recomputation of the last steps) ------------------------------------
+        R ck[ADJ_MAXSEG][MG];
+        const bool fromck = a.ckpt != nullptr;
+        auto ck_load = [&](int s1) {
+#pragma unroll
+            for (int m = 0; m < MG; ++m)
+                st[m] = fromck ? a.ckpt[((int64_t)s1 * W + g * MG + m) * a.paths + p] : ck[s1][m];
+        };
+        if (!fromck) {
+#pragma unroll
+            for (int m = 0; m < MG; ++m) st[m] = x0[m];
+            for (int k = 0, kc = 0, ci = 0; k < n_steps; ++k) {
+                if (kc == 0) {
+#pragma unroll
+                    for (int m = 0; m < MG; ++m) ck[ci][m] = st[m];
+                    ++ci;
+                }
+                kc = kc + 1 == seg ? 0 : kc + 1;
+                R dW[MAXM], dN[MAXM], dJ[MAXM];
+                noise(k, dW, dN, dJ);
+                step(k, st, dW, dN, dJ);
+            }
+            terminal();
         }
         R gp[NCP][NP > 0 ? NP : 1];
 #pragma unroll
@@ -222,16 +236,20 @@ __global__ void __launch_bounds__(BLOCK, MINB) sde_adj_user_kernel(const __grid_
         for (int s1 = nseg - 1; s1 >= 0; --s1) {
             const int l0 = s1 * seg, l1 = min(l0 + seg, n_steps);
             if (two) {
-#pragma unroll
-                for (int m = 0; m < MG; ++m) st[m] = ck[s1][m];
+                ck_load(s1);
                 sweep(l0, l1, st, ck2);
+                if (fromck && s1 == nseg - 1) terminal();
             }
             const int nseg2 = two ? (l1 - l0 + seg2 - 1) / seg2 : 1;
             for (int s2 = nseg2 - 1; s2 >= 0; --s2) {
                 const int k0 = two ? l0 + s2 * seg2 : l0;
                 const int k1 = two ? min(k0 + seg2, l1) : l1;
+                if (two) {
 #pragma unroll
-                for (int m = 0; m < MG; ++m) st[m] = two ? ck2[s2][m] : ck[s1][m];
+                    for (int m = 0; m < MG; ++m) st[m] = ck2[s2][m];
+                } else {
+                    ck_load(s1);
+                }
                 for (int k = k0; k < k1; ++k) {
                     R dW[MAXM], dN[MAXM], dJ[MAXM];
                     noise(k, dW, dN, dJ);
@@ -245,6 +263,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) sde_adj_user_kernel(const __grid_
                     }
                     step(k, st, dW, dN, dJ);
                 }
+                if (fromck && !two && s1 == nseg - 1) terminal();
                 for (int k = k1 - 1; k >= k0; --k) {
                     const R *b = ub + (size_t)(k - k0) * NV * MG * BLOCK + threadIdx.x;
                     R xv[MG], dW[MAXM], dN[MAXM], dJ[MAXM];

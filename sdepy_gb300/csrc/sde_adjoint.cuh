@@ -74,6 +74,9 @@ struct AdjArgs {
     // b, pa per state ([3][W]), and the terms present (bit 0 dj, bit 1 dn)
     const R *jprm;
     int32_t user_jsrc;
+    // level-1 checkpoints written by the forward run, [nseg][W][paths], or
+    // NULL (the kernel's own checkpoint sweep)
+    const R *ckpt;
 };
 
 // Tangent-mode run of a user program (single equation): the terms' values
@@ -429,7 +432,7 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
             }
             correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
         };
-        R val;
+        R val = R(0);
         if (MODEL == SDE_MODEL_LINEAR) {
             // ---- constant adjoint: one forward sweep ------------------------------
             R st[MAXM], sdw[MAXM], sja[MAXM], sjb[MAXM];
@@ -502,23 +505,34 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
             // ---- checkpointed reverse sweep (OU, Heston) ----------------------------
             R ck[ADJ_MAXSEG][MAXM];
             R st[MAXM];
-#pragma unroll
-            for (int m = 0; m < MAXM; ++m) st[m] = x0[m];
-            for (int k = 0; k < a.n_steps; ++k) {
-                if (k % a.seg == 0) {
-#pragma unroll
-                    for (int m = 0; m < MAXM; ++m) ck[k / a.seg][m] = st[m];
-                }
-                const R sq = a.sqdt[k];
-                uint32_t u[4 * NCMAX];
-                R z[MAXM], dW[MAXM];
-                noise(k, sq, u, z, dW);
-                load_step(k);
-                if constexpr (UJ) user_step<R, MAXM, MODEL>(a.uprog, c0, c1, c2, c3, c4, c5, a.tk[k], a.dt[k], dW, st);
-                else fwd_step<R, MODEL, MAXM>(c0, c1, c2, a.dt[k], dW, st);
-            }
             R xb[MAXM];
-            val = terminal_adjoint<R, MAXM>(a, st, xb);
+            // level-1 checkpoints: this sweep, or the forward's (device
+            // memory; the terminal adjoint then follows the recomputation
+            // of the last steps)
+            const bool fromck = a.ckpt != nullptr;
+            auto ck_load = [&](int s1) {
+#pragma unroll
+                for (int m = 0; m < MAXM; ++m)
+                    st[m] = fromck ? a.ckpt[((int64_t)s1 * W + g * M + (m < M ? m : 0)) * a.paths + p] : ck[s1][m];
+            };
+            if (!fromck) {
+#pragma unroll
+                for (int m = 0; m < MAXM; ++m) st[m] = x0[m];
+                for (int k = 0; k < a.n_steps; ++k) {
+                    if (k % a.seg == 0) {
+#pragma unroll
+                        for (int m = 0; m < MAXM; ++m) ck[k / a.seg][m] = st[m];
+                    }
+                    const R sq = a.sqdt[k];
+                    uint32_t u[4 * NCMAX];
+                    R z[MAXM], dW[MAXM];
+                    noise(k, sq, u, z, dW);
+                    load_step(k);
+                    if constexpr (UJ) user_step<R, MAXM, MODEL>(a.uprog, c0, c1, c2, c3, c4, c5, a.tk[k], a.dt[k], dW, st);
+                    else fwd_step<R, MODEL, MAXM>(c0, c1, c2, a.dt[k], dW, st);
+                }
+                val = terminal_adjoint<R, MAXM>(a, st, xb);
+            }
             R bx[ADJ_MAXSEG][MAXM], bw[ADJ_MAXSEG][MAXM], bz[ADJ_MAXSEG][2];
             // level-2 checkpoints of the current level-1 segment (two levels
             // only: runs longer than ADJ_MAXSEG^2 steps)
@@ -528,8 +542,7 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
               const int l0 = s1 * a.seg;
               const int l1 = min(l0 + a.seg, a.n_steps);
               if (two) {
-#pragma unroll
-                  for (int m = 0; m < MAXM; ++m) st[m] = ck[s1][m];
+                  ck_load(s1);
                   for (int k = l0; k < l1; ++k) {
                       if ((k - l0) % a.seg2 == 0) {
 #pragma unroll
@@ -543,13 +556,18 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                       if constexpr (UJ) user_step<R, MAXM, MODEL>(a.uprog, c0, c1, c2, c3, c4, c5, a.tk[k], a.dt[k], dW, st);
                       else fwd_step<R, MODEL, MAXM>(c0, c1, c2, a.dt[k], dW, st);
                   }
+                  if (fromck && s1 == a.nseg - 1) val = terminal_adjoint<R, MAXM>(a, st, xb);
               }
               const int nseg2 = two ? (l1 - l0 + a.seg2 - 1) / a.seg2 : 1;
               for (int sidx = nseg2 - 1; sidx >= 0; --sidx) {
                 const int k0 = two ? l0 + sidx * a.seg2 : l0;
                 const int k1 = two ? min(k0 + a.seg2, l1) : l1;
+                if (two) {
 #pragma unroll
-                for (int m = 0; m < MAXM; ++m) st[m] = two ? ck2[sidx][m] : ck[s1][m];
+                    for (int m = 0; m < MAXM; ++m) st[m] = ck2[sidx][m];
+                } else {
+                    ck_load(s1);
+                }
                 for (int k = k0; k < k1; ++k) {
                     const R sq = a.sqdt[k];
                     uint32_t u[4 * NCMAX];
@@ -566,6 +584,7 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                     if constexpr (UJ) user_step<R, MAXM, MODEL>(a.uprog, c0, c1, c2, c3, c4, c5, a.tk[k], a.dt[k], dW, st);
                     else fwd_step<R, MODEL, MAXM>(c0, c1, c2, a.dt[k], dW, st);
                 }
+                if (fromck && !two && s1 == a.nseg - 1) val = terminal_adjoint<R, MAXM>(a, st, xb);
                 for (int k = k1 - 1; k >= k0; --k) {
                     const R dt = a.dt[k], sq = a.sqdt[k];
                     load_step(k);

@@ -822,6 +822,15 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
         }
         CU(cudaMemsetAsync(a.row_jumps, 0, sizeof(int64_t) * out->n_rows, st));
     }
+    // adjoint checkpoints (device memory of the caller)
+    if (out->ckpt && n_steps > 0) {
+        if (out->ckpt_seg < 1) return fail(SDE_ERR_INVALID, "ckpt_seg must be >= 1");
+        if (inject || anti)
+            return fail(SDE_ERR_UNSUPPORTED, "checkpoints are written for device-RNG paths without antithetics");
+        if (tab) return fail(SDE_ERR_UNSUPPORTED, "the FP32 LINEAR / OU run-table kernels write no checkpoints");
+        a.ckpt = (R *)out->ckpt;
+        a.ckpt_seg = out->ckpt_seg;
+    }
     void *d_err;
     if ((rc = scratch(D, S_ERR, 16, &d_err))) return rc;
     CU(cudaMemsetAsync(d_err, 0, 16, st));
@@ -1141,6 +1150,101 @@ template <> struct AdjFinder<double> {
     static AdjLauncher<double> find_heston(int, int *) { return nullptr; }
 };
 
+// what the adjoint of a spec runs: a user program's terms (ujs bit 0 dj,
+// bit 1 dn; nv the values per state and step the compiled kernel keeps:
+// the state, dw, dn, dj); compiled programs, systems and jump terms take
+// the reverse-mode kernel (sde_adj_user.cuh), the interpreter single
+// equations driven by dt / dw (tangent mode)
+struct AdjKind {
+    bool user, ujit, jumps;
+    int ujs, nv;
+};
+
+static AdjKind adjoint_kind(const SdeSpec *s) {
+    AdjKind K;
+    K.user = s->model == SDE_MODEL_USER;
+    K.ujs = 0;
+    K.nv = 1;
+    if (K.user)
+        for (int i = 0; i < s->program->n_terms; ++i) {
+            const int src = s->program->term_source[i];
+            if (src == SDE_SRC_DJ) K.ujs |= 1;
+            if (src == SDE_SRC_DN) K.ujs |= 2;
+            if (src != SDE_SRC_DT) ++K.nv;
+        }
+    K.ujit = K.user && (s->program->jit || s->program->n_eq > 1 || K.ujs);
+    K.jumps = K.user ? K.ujs != 0 : s->jump_law != SDE_JUMP_NONE;
+    return K;
+}
+
+// The adjoint's segments: level-1 checkpoints every `seg` steps (nseg of
+// them), level 2 every `seg2` steps inside a level-1 segment (seg2 == seg:
+// one level); the kernel's per-segment buffer holds at most `cap` steps.
+// Without checkpoints from the forward, level 1 is ceil(sqrt(steps)) steps
+// (capped), and runs needing more than ADJ_MAXSEG level-1 segments (the
+// kernels' local checkpoint arrays) take level 1 every ceil(steps /
+// ADJ_MAXSEG) steps and a second level inside, one more forward sweep.
+// With checkpoints from the forward (read from device memory: any number),
+// level 1 is their segment, split in two levels when longer than cap.
+struct AdjPlan {
+    bool heston_fast;   // the FP32 2-variable Heston kernel (sde_adj_heston.cuh)
+    int cap, seg, seg2, nseg;
+    size_t ubytes;      // the compiled user-SDE kernel's shared-memory buffer
+};
+
+template <typename R>
+static int adjoint_plan(const SdeSpec *s, int n_steps, bool jumps, bool td, bool ujit, int nv, int req_seg,
+                        bool fromck, AdjPlan *P) {
+    const int M = s->group_size;
+    const bool linear = s->model == SDE_MODEL_LINEAR;
+    // the FP32 2-variable Heston adjoint keeps its segment in shared memory:
+    // at most ADJ_HESTON_SEG steps, one checkpoint level
+    P->heston_fast = sizeof(R) == 4 && s->model == SDE_MODEL_HESTON && M == 2 && !jumps && !td &&
+                     (fromck ? req_seg <= ADJ_HESTON_SEG
+                             : (n_steps + ADJ_HESTON_SEG - 1) / ADJ_HESTON_SEG <= ADJ_MAXSEG);
+    int cap = P->heston_fast ? ADJ_HESTON_SEG : ADJ_MAXSEG;
+    size_t per_step = 0;
+    if (ujit) {   // nv * M values per thread and step in UADJ_SMEM bytes
+        per_step = sizeof(R) * (size_t)nv * M * BLOCK;
+        cap = (int)(UADJ_SMEM / per_step);
+        if (cap > ADJ_MAXSEG) cap = ADJ_MAXSEG;
+        if (cap < 1) return fail(SDE_ERR_UNSUPPORTED, "the adjoint's segment buffer does not fit groups of %d", M);
+    }
+    int seg, seg2;
+    auto level2 = [&]() {   // level-2 length inside level-1 segments of seg steps
+        int s2 = (int)ceil(sqrt((double)seg));
+        if (s2 > cap) s2 = cap;
+        if ((seg + s2 - 1) / s2 > ADJ_MAXSEG) s2 = (seg + ADJ_MAXSEG - 1) / ADJ_MAXSEG;
+        return s2;
+    };
+    if (fromck) {
+        seg = seg2 = req_seg;
+        if (!linear && seg > cap) {
+            seg2 = level2();
+            if (seg2 > cap)
+                return fail(SDE_ERR_UNSUPPORTED, "checkpoint segments of at most %d steps", ADJ_MAXSEG * cap);
+        }
+    } else {
+        seg = req_seg > 0 ? req_seg : (int)ceil(sqrt((double)n_steps));
+        if (seg > cap) seg = cap;
+        if (seg < 1) seg = 1;
+        seg2 = seg;
+        if (!linear && (n_steps + seg - 1) / seg > ADJ_MAXSEG) {
+            seg = (n_steps + ADJ_MAXSEG - 1) / ADJ_MAXSEG;
+            seg2 = level2();
+            if (seg2 > cap)
+                return fail(SDE_ERR_UNSUPPORTED, "the adjoint supports up to %d steps for groups of %d",
+                            ADJ_MAXSEG * ADJ_MAXSEG * cap, M);
+        }
+    }
+    P->cap = cap;
+    P->seg = seg;
+    P->seg2 = seg2;
+    P->nseg = (n_steps + seg - 1) / seg;
+    P->ubytes = per_step * seg2;
+    return SDE_OK;
+}
+
 template <typename R>
 static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *req, double *grad, double *value) {
     int opg = 0, rc;
@@ -1152,25 +1256,13 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
         if (!(gr->tt[k + 1] > gr->tt[k])) return fail(SDE_ERR_UNSUPPORTED, "the adjoint integrates forward grids only");
     if (req->n_strikes < 0 || req->n_strikes > SDE_MAX_STRIKES) return fail(SDE_ERR_INVALID, "bad n_strikes");
     const int M = s->group_size, W = s->groups * M;
-    const bool user = s->model == SDE_MODEL_USER;
-    // a user program's terms: ujs bit 0 dj, bit 1 dn; nv the values per
-    // state and step the compiled adjoint keeps (the state, dw, dn, dj)
-    int ujs = 0, nv = 1;
-    if (user)
-        for (int i = 0; i < s->program->n_terms; ++i) {
-            const int src = s->program->term_source[i];
-            if (src == SDE_SRC_DJ) ujs |= 1;
-            if (src == SDE_SRC_DN) ujs |= 2;
-            if (src != SDE_SRC_DT) ++nv;
-        }
-    // compiled programs, systems and jump terms take the reverse-mode kernel
-    // (sde_adj_user.cuh); the interpreter takes single equations driven by
-    // dt / dw (tangent mode)
-    const bool ujit = user && (s->program->jit || s->program->n_eq > 1 || ujs);
+    const AdjKind K = adjoint_kind(s);
+    const bool user = K.user, ujit = K.ujit;
+    const int ujs = K.ujs, nv = K.nv;
     if (ujit && !jit_available())
         return fail(SDE_ERR_UNSUPPORTED, "the adjoint of user systems and jump terms compiles the program at run "
                                          "time: NVRTC is not available");
-    const bool jumps = user ? ujs != 0 : s->jump_law != SDE_JUMP_NONE;
+    const bool jumps = K.jumps;
     if (gr->lam_t && !(user && jumps))
         return fail(SDE_ERR_INVALID, "grid lam_t applies to user SDEs with dn / dj terms");
     if (user && jumps && !s->program->jump_params)
@@ -1189,51 +1281,15 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
             return fail(SDE_ERR_UNSUPPORTED, "gradients with time-dependent parameters: at most %d steps for "
                                              "groups of %d", (int)(ADJ_TD_SMEM / (sizeof(R) * 3 * maxm)), M);
     }
-    // checkpoints: one level of ceil(sqrt(steps)) steps up to ADJ_MAXSEG^2
-    // steps; beyond, two levels (level 1 every ceil(steps / ADJ_MAXSEG)
-    // steps, level 2 inside it), one more forward sweep of the paths
-    int seg = req->checkpoint > 0 ? req->checkpoint : (int)ceil(sqrt((double)n_steps));
-    if (seg > ADJ_MAXSEG) seg = ADJ_MAXSEG;
-    if (seg < 1) seg = 1;
-    int seg2 = seg;
-    if (s->model != SDE_MODEL_LINEAR && (n_steps + seg - 1) / seg > ADJ_MAXSEG) {
-        seg = (n_steps + ADJ_MAXSEG - 1) / ADJ_MAXSEG;
-        seg2 = (int)ceil(sqrt((double)seg));
-        if ((seg + seg2 - 1) / seg2 > ADJ_MAXSEG) seg2 = (seg + ADJ_MAXSEG - 1) / ADJ_MAXSEG;
-        if (seg2 > ADJ_MAXSEG)
-            return fail(SDE_ERR_UNSUPPORTED, "the adjoint supports up to %d steps",
-                        ADJ_MAXSEG * ADJ_MAXSEG * ADJ_MAXSEG);
-    }
-    // the compiled user adjoint keeps each level-2 segment's states and
-    // increments in shared memory: at most `cap` steps of nv * M values per
-    // thread in UADJ_SMEM bytes
-    size_t ubytes = 0;
-    if (ujit) {
-        const size_t per_step = sizeof(R) * (size_t)nv * M * BLOCK;
-        int cap = (int)(UADJ_SMEM / per_step);
-        if (cap > ADJ_MAXSEG) cap = ADJ_MAXSEG;
-        if (cap < 1) return fail(SDE_ERR_UNSUPPORTED, "the adjoint's segment buffer does not fit groups of %d", M);
-        seg = req->checkpoint > 0 ? req->checkpoint : (int)ceil(sqrt((double)n_steps));
-        if (seg > cap) seg = cap;
-        if (seg < 1) seg = 1;
-        seg2 = seg;
-        if ((n_steps + seg - 1) / seg > ADJ_MAXSEG) {   // two levels
-            seg = (n_steps + ADJ_MAXSEG - 1) / ADJ_MAXSEG;
-            seg2 = (int)ceil(sqrt((double)seg));
-            if (seg2 > cap) seg2 = cap;
-            if ((seg + seg2 - 1) / seg2 > ADJ_MAXSEG) seg2 = (seg + ADJ_MAXSEG - 1) / ADJ_MAXSEG;
-            if (seg2 > cap)
-                return fail(SDE_ERR_UNSUPPORTED, "the adjoint supports up to %d steps for groups of %d",
-                            ADJ_MAXSEG * ADJ_MAXSEG * cap, M);
-        }
-        ubytes = per_step * seg2;
-    }
-    // the FP32 2-variable Heston adjoint keeps its segment in shared memory:
-    // segments of at most ADJ_HESTON_SEG steps (one checkpoint level)
-    const bool heston_fast = sizeof(R) == 4 && s->model == SDE_MODEL_HESTON && M == 2 && !jumps && !td &&
-                             seg2 == seg && (n_steps + ADJ_HESTON_SEG - 1) / ADJ_HESTON_SEG <= ADJ_MAXSEG;
-    if (heston_fast && seg > ADJ_HESTON_SEG) seg = seg2 = ADJ_HESTON_SEG;
-    const int nseg = (n_steps + seg - 1) / seg;
+    // checkpoints written by the forward run (the LINEAR adjoint takes none)
+    const bool fromck = req->ckpt != nullptr && s->model != SDE_MODEL_LINEAR;
+    if (fromck && req->checkpoint < 1)
+        return fail(SDE_ERR_INVALID, "checkpoints from the forward need req->checkpoint, their segment length");
+    AdjPlan plan;
+    if ((rc = adjoint_plan<R>(s, n_steps, jumps, td, ujit, nv, req->checkpoint, fromck, &plan))) return rc;
+    const bool heston_fast = plan.heston_fast;
+    const int seg = plan.seg, seg2 = plan.seg2, nseg = plan.nseg;
+    const size_t ubytes = plan.ubytes;
 
     std::lock_guard<std::mutex> lk(g_mu);
     Device *D;
@@ -1315,6 +1371,7 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     a.seg = seg;
     a.nseg = nseg;
     a.seg2 = seg2;
+    a.ckpt = fromck ? (const R *)req->ckpt : nullptr;
     a.step_offset = gr->step_offset;
     a.out_mode = s->out_mode;
     a.jump_law = s->jump_law;
@@ -1430,6 +1487,30 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
                         req->grad_t[((size_t)k * 3 + j) * W + (size_t)g * M + m] =
                             htd[(size_t)g * ntd + ((size_t)k * 3 + j) * maxm + m] * inv;
     return SDE_OK;
+}
+
+template <typename R>
+static int adjoint_checkpoints_impl(const SdeSpec *s, const SdeGrid *gr, int32_t *seg, int64_t *bytes) {
+    int opg = 0, rc;
+    if ((rc = check_spec(s, &opg))) return rc;
+    if (!gr || gr->n_pts < 2) return fail(SDE_ERR_INVALID, "the adjoint needs a grid of >= 2 points");
+    *seg = 0;
+    *bytes = 0;
+    const int n_steps = gr->n_pts - 1;
+    const bool table = sizeof(R) == 4 && (s->model == SDE_MODEL_LINEAR || s->model == SDE_MODEL_OU);
+    if (s->model == SDE_MODEL_LINEAR || table || s->flags) return SDE_OK;   // none written or read
+    const AdjKind K = adjoint_kind(s);
+    AdjPlan P;
+    if ((rc = adjoint_plan<R>(s, n_steps, K.jumps, gr->params_t != nullptr, K.ujit, K.nv, 0, false, &P))) return rc;
+    *seg = P.seg;
+    *bytes = (int64_t)P.nseg * s->groups * s->group_size * s->paths * (int64_t)sizeof(R);
+    return SDE_OK;
+}
+
+extern "C" int32_t sde_adjoint_checkpoints(const SdeSpec *spec, const SdeGrid *grid, int32_t *seg, int64_t *bytes) {
+    if (!spec || !seg || !bytes) return fail(SDE_ERR_INVALID, "spec, seg and bytes are required");
+    if (spec->precision == SDE_FP32) return adjoint_checkpoints_impl<float>(spec, grid, seg, bytes);
+    return adjoint_checkpoints_impl<double>(spec, grid, seg, bytes);
 }
 
 extern "C" int32_t sde_adjoint(const SdeSpec *spec, const SdeGrid *grid, const SdeAdjReq *req, double *grad,

@@ -96,6 +96,10 @@ struct FwdArgs {
     // injected increments (FP64, device)
     const double *dw, *dj;
     const long long *dn;
+    // adjoint checkpoints (the general kernels): the state before every
+    // ckpt_seg-th step, [ceil(n_steps / ckpt_seg)][W][paths], or NULL
+    R *ckpt;
+    int32_t ckpt_seg;
     // outputs
     R *xx;
     int64_t n_out_vars;
@@ -1095,8 +1099,21 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                     if (run.z >= 0) store(run.z, true);
                 }
             } else {
+                // adjoint checkpoints: the state before steps 0, ckpt_seg, ...
+                // (kc counts down to the next one; uniform branch)
+                int kc = 0, ci = 0;
 #pragma unroll UNROLL
                 for (int k = 0; k < n_steps; ++k) {
+                    if (a.ckpt) {
+                        if (kc == 0) {
+#pragma unroll
+                            for (int m = 0; m < MAXM; ++m)
+                                if (m < M) a.ckpt[((int64_t)ci * W + g * M + m) * a.paths + p] = st[m];
+                            ++ci;
+                            kc = a.ckpt_seg;
+                        }
+                        --kc;
+                    }
                     const R dt = a.dt[k];
                     const R sq = a.sqdt[k];
                     // time-dependent coefficients of step k (uniform test; not

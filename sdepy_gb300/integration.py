@@ -444,6 +444,9 @@ class _gpu_process:
             out.xx = None if xx is None else xx.ctypes.data
             out.n_rows = rows
             out.on_device = 0
+            ck = getattr(self, '_ckpt_out', None)   # adjoint checkpoints (autograd.expectation)
+            if ck is not None and leg is legs[-1]:
+                out.ckpt, out.ckpt_seg = ck
             if self.getinfo and heston:
                 neg = np.zeros((self._G*self._M//2, self.paths), dtype=np.int32)
                 out.neg_count = _lib.iptr(neg)

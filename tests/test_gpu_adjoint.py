@@ -344,3 +344,110 @@ def test_per_step_gradients_heston_xi_vs_differences(lib):
     fd_ = (value(xi0 + h) - value(xi0 - h))/(2*h)
     assert abs(val - value(xi0)) <= 1e-11*abs(val)
     np.testing.assert_allclose(dxi0, fd_, rtol=2e-3)
+
+
+def adjoint_ck(lib, P, tl, strikes, weights, wmean, seed, stream, from_forward):
+    """sde_adjoint of process P with its own checkpoint sweep, or after a
+    forward run (sde_run_stats) that wrote the checkpoints
+    sde_adjoint_checkpoints asks for (SdeOut.ckpt, read back through
+    SdeAdjReq.ckpt)."""
+    import torch
+    leg = Grid(tl, P.steps).legs[-1]
+    g = _lib.SdeGrid()
+    g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
+    g.n_pts, g.step_offset = leg.tt.size, 0
+    ltab = P._lam_table(leg)
+    g.lam_t = _lib.dptr(ltab)
+    spec = P._make_spec(seed, stream)
+    req = _lib.SdeAdjReq()
+    req.n_strikes, req.mean_weight = len(strikes), wmean
+    for i, (K, w) in enumerate(zip(strikes, weights)):
+        req.strikes[i], req.weights[i] = K, w
+    buf = None
+    if from_forward:
+        seg, nb = C.c_int32(), C.c_int64()
+        _lib.check(lib.sde_adjoint_checkpoints(C.byref(spec), C.byref(g), C.byref(seg), C.byref(nb)), 'ckpts')
+        assert seg.value > 0 and nb.value == -(-leg.n_steps//seg.value)*P._W*P.paths*(4 if P._precision == _lib.FP32 else 8)
+        buf = torch.empty(nb.value, dtype=torch.uint8, device='cuda')
+        o = _lib.SdeOut()
+        o.xx, o.n_rows, o.on_device = None, len(tl), 0
+        o.ckpt, o.ckpt_seg = buf.data_ptr(), seg.value
+        sreq, so, _ = P._stats_request(dict(row=len(tl) - 1, bins=0, range=None, strikes=[]))
+        _lib.check(lib.sde_run_stats(C.byref(spec), C.byref(g), None, C.byref(o), C.byref(sreq), C.byref(so)),
+                   'sde_run_stats')
+        req.ckpt, req.checkpoint = buf.data_ptr(), seg.value
+    grad = np.zeros((P._W, 8))
+    val = C.c_double()
+    _lib.check(lib.sde_adjoint(C.byref(spec), C.byref(g), C.byref(req), _lib.dptr(grad), C.byref(val)),
+               'sde_adjoint')
+    del buf
+    return grad, val.value
+
+
+def _user(f, **kw):
+    return sg.integrate(f, **kw)
+
+
+CK_CASES = [
+    ('heston_fp32', lambda: sg.heston_process(paths=20011, steps=499, dtype=np.float32, **HES), (0., 2.),
+     [90., 100.]),
+    ('heston_fp64', lambda: sg.heston_process(paths=20011, steps=100, **HES), (0., 1.), [100.]),
+    ('ou_fp64', lambda: sg.ornstein_uhlenbeck_process(paths=20011, steps=300, x0=.1, k=1.3, theta=.4, sigma=.3),
+     (0., 1.), [.3]),
+    ('ou_fp64_5000_steps', lambda: sg.ornstein_uhlenbeck_process(paths=2048, steps=5000, x0=.1, k=1.3, theta=.4,
+                                                                  sigma=.3), (0., 2.), [.3]),
+    ('cir_fp32', lambda: sg.cox_ingersoll_ross_process(paths=20011, steps=200, dtype=np.float32, x0=.04, k=2.,
+                                                       theta=.04, xi=.2), (0., 1.), [.04]),
+    ('user_ou_interpreted', lambda: _user(lambda t, x, theta=.5, k=2., sigma=.3: {'dt': k*(theta - x), 'dw': sigma},
+                                          jit=False)(paths=20011, steps=200, x0=1.), (0., 1.), [.6]),
+    ('user_ou_compiled_fp32', lambda: _user(lambda t, x, theta=.5, k=2., sigma=.3: {'dt': k*(theta - x),
+                                                                                      'dw': sigma}, jit=True)(
+        paths=20011, steps=200, dtype=np.float32, x0=1.), (0., 1.), [.6]),
+    ('user_jumps_compiled', lambda: _user(lambda t, x, a=.3, b=.5, s=.2: {'dn': a, 'dt': -b*x, 'dj': x, 'dw': s})(
+        paths=20011, steps=100, x0=.5, lam=2., y=sg.exp_rv(.2)), (0., 1.), [.5]),
+]
+
+
+@pytest.mark.parametrize('case', CK_CASES, ids=[c[0] for c in CK_CASES])
+def test_adjoint_from_forward_checkpoints(lib, case):
+    """The checkpoints a forward run writes (SdeOut.ckpt) replace the
+    adjoint's own checkpoint sweep: the same segments recomputed from the
+    forward's states.  FP64: the forward kernel's paths are the adjoint's
+    bit for bit (the same rounded operations), so the gradient and the value
+    are identical; FP32: equal to FP32 rounding (the compiler fuses products
+    into sums per kernel) -- Heston (the FP32 shared-memory kernel and
+    FP64), OU (one and two levels), CIR, user SDEs interpreted and compiled,
+    a program with dn / dj terms."""
+    name, make, tl, strikes = case
+    P = make()
+    w = [.5]*len(strikes)
+    own = adjoint_ck(lib, P, tl, strikes, w, .1, 7, 3, False)
+    fwd = adjoint_ck(lib, P, tl, strikes, w, .1, 7, 3, True)
+    if P._precision == _lib.FP64:
+        np.testing.assert_array_equal(own[0], fwd[0])
+        assert own[1] == fwd[1]
+    else:
+        np.testing.assert_allclose(fwd[0], own[0], rtol=1e-5, atol=1e-6*np.max(np.abs(own[0])))
+        assert abs(fwd[1] - own[1]) <= 1e-6*abs(own[1])
+
+
+def test_checkpoints_where_the_forward_writes_none(lib):
+    """sde_adjoint_checkpoints answers 0 for the models whose adjoint takes
+    no checkpoints (LINEAR) and for the FP32 OU run-table forward, which
+    refuses a checkpoint array."""
+    for P in (sg.lognorm_process(paths=100, steps=10, x0=1., mu=.1, sigma=.2),
+              sg.ornstein_uhlenbeck_process(paths=100, steps=10, dtype=np.float32)):
+        leg = Grid((0., 1.), 10).legs[-1]
+        g = _lib.SdeGrid()
+        g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
+        g.n_pts = leg.tt.size
+        spec = P._make_spec(1, 1)
+        seg, nb = C.c_int32(7), C.c_int64(7)
+        _lib.check(lib.sde_adjoint_checkpoints(C.byref(spec), C.byref(g), C.byref(seg), C.byref(nb)), 'ckpts')
+        assert seg.value == 0 and nb.value == 0
+    import torch
+    P = sg.ornstein_uhlenbeck_process(paths=100, steps=10, dtype=np.float32)
+    buf = torch.empty(4*100*10, dtype=torch.uint8, device='cuda')
+    o = _lib.SdeOut()
+    o.n_rows, o.ckpt, o.ckpt_seg = 2, buf.data_ptr(), 4
+    assert lib.sde_run(C.byref(P._make_spec(1, 1)), C.byref(g), None, C.byref(o)) == _lib.ERR_UNSUPPORTED
