@@ -32,6 +32,10 @@ Poisson intensities (constant or functions of time), the Kou probability pa
 and the jump-size laws of user SDEs select integer / discrete outcomes or
 are drawn through them and are not differentiated.
 
+A correlation (``corr``, or Heston's ``rho``) may be a function of time, as
+sdepy's wiener_source takes it (evaluated at each step's midpoint); it is not
+differentiated (no ``rho`` gradient then).
+
 Time-dependent parameters (the presets without jumps): a parameter may be a
 function of time, evaluated at each Euler step's start as sdepy evaluates
 callable parameters.  When the function returns a torch tensor for a torch
@@ -150,6 +154,9 @@ class _Expectation(torch.autograd.Function):
         lam_t = proc._lam_table(leg) if ctx.mp is not None else None
         if lam_t is not None:   # a user jump term's intensity, a function of time
             g.lam_t = _lib.dptr(lam_t)
+        corr_t = proc._corr_table(leg) if proc._corr_tdep else None
+        if corr_t is not None:   # a correlation that depends on time (not differentiated)
+            g.corr_t = _lib.dptr(corr_t)
         if td:   # per-step slot gradients of the time-dependent table
             ptab = proc._params_table(leg)
             g.params_t = _lib.dptr(ptab)
@@ -229,8 +236,9 @@ def expectation(cls, timeline, strikes=(), *, paths, steps=None,
     # at the steps' starts as a torch tensor (the input whose gradient the
     # backward pass returns) and handed to the process as a numpy function
     # (a user SDE's intensity may depend on time, and its jump-size law is
-    # an object: neither is differentiated)
-    tdep = [k for k, v in plain.items() if callable(v) and not (mp is not None and k in ('lam', 'y'))]
+    # an object; a correlation may depend on time: none is differentiated)
+    tdep = [k for k, v in plain.items() if callable(v) and k not in ('corr', 'rho') and
+            not (mp is not None and k in ('lam', 'y'))]
     if tdep:
         if mp is not None or name in ('merton_jumpdiff_process', 'kou_jumpdiff_process') or \
                 name not in _TD_SLOTS:
@@ -287,6 +295,8 @@ def _checkpoints(P, grid, seed, stream):
     g.n_pts, g.step_offset = leg.tt.size, leg.step_offset
     ptab = P._params_table(leg) if P._tdep else None
     g.params_t = _lib.dptr(ptab)
+    ctab = P._corr_table(leg) if P._corr_tdep else None
+    g.corr_t = _lib.dptr(ctab)
     spec = P._make_spec(seed, stream)
     seg, nbytes = C.c_int32(), C.c_int64()
     _lib.check(lib.sde_adjoint_checkpoints(C.byref(spec), C.byref(g), C.byref(seg), C.byref(nbytes)),

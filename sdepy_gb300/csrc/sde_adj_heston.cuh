@@ -20,6 +20,9 @@
 
 namespace sdegpu {
 
+// CK: checkpoints from the forward run (AdjArgs::ckpt), compiled apart so
+// that the kernel with its own checkpoint sweep carries no test of it
+template <bool CK>
 static __global__ void __launch_bounds__(BLOCK, 3) sde_adj_heston_kernel(const __grid_constant__ AdjArgs<float> a) {
     typedef Ar<float> A;
     constexpr int NPA = 2 * NGV + 2;
@@ -105,8 +108,8 @@ static __global__ void __launch_bounds__(BLOCK, 3) sde_adj_heston_kernel(const _
         // checkpoints every seg steps: this sweep, or the forward's (device
         // memory; the terminal adjoint then follows the last segment's
         // recomputation)
-        const bool fromck = a.ckpt != nullptr;
-        if (!fromck) {
+        constexpr bool fromck = CK;
+        if constexpr (!fromck) {
             float x = x0a, y = x0b;
             for (int k = 0, kc = 0, ci = 0; k < n_steps; ++k) {
                 if (kc == 0) {
@@ -126,7 +129,7 @@ static __global__ void __launch_bounds__(BLOCK, 3) sde_adj_heston_kernel(const _
         for (int s = nseg - 1; s >= 0; --s) {
             const int k0 = s * seg, k1 = min(k0 + seg, n_steps);
             float sx, sy;
-            if (fromck) {
+            if constexpr (fromck) {
                 sx = a.ckpt[((int64_t)s * W + g * 2) * a.paths + p];
                 sy = a.ckpt[((int64_t)s * W + g * 2 + 1) * a.paths + p];
             } else {
@@ -143,7 +146,8 @@ static __global__ void __launch_bounds__(BLOCK, 3) sde_adj_heston_kernel(const _
                 incr(z0, z1, __ldg(a.sqdt + k), dWx, dWy);
                 step(__ldg(a.dt + k), dWx, dWy, sx, sy);
             }
-            if (fromck && s == nseg - 1) terminal(sx, sy);
+            if constexpr (fromck)
+                if (s == nseg - 1) terminal(sx, sy);
             for (int k = k1 - 1; k >= k0; --k) {
                 const float *b = hbuf + (k - k0) * 3 * BLOCK + threadIdx.x;
                 const float yv = b[0], z0 = b[BLOCK], z1 = b[2 * BLOCK];
@@ -198,16 +202,23 @@ static inline size_t adj_heston_smem(int seg) { return sizeof(float) * 3 * (size
 
 static inline void launch_adj_heston(const AdjArgs<float> &a, dim3 grid, cudaStream_t s) {
     const size_t smem = adj_heston_smem(a.seg);
-    cudaFuncSetAttribute(sde_adj_heston_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    sde_adj_heston_kernel<<<grid, BLOCK, smem, s>>>(a);
+    if (a.ckpt) {
+        cudaFuncSetAttribute(sde_adj_heston_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        sde_adj_heston_kernel<true><<<grid, BLOCK, smem, s>>>(a);
+    } else {
+        cudaFuncSetAttribute(sde_adj_heston_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        sde_adj_heston_kernel<false><<<grid, BLOCK, smem, s>>>(a);
+    }
 }
 
 static inline int adj_heston_max_blocks_per_sm(int seg) {
-    int n = 0;
-    cudaFuncSetAttribute(sde_adj_heston_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)adj_heston_smem(seg));
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sde_adj_heston_kernel, BLOCK, adj_heston_smem(seg));
-    return n;
+    int n = 0, n1 = 0;
+    const size_t smem = adj_heston_smem(seg);
+    cudaFuncSetAttribute(sde_adj_heston_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(sde_adj_heston_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sde_adj_heston_kernel<false>, BLOCK, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, sde_adj_heston_kernel<true>, BLOCK, smem);
+    return n < n1 ? n : n1;
 }
 #endif
 

@@ -155,15 +155,17 @@ __global__ void __launch_bounds__(BLOCK, MINB) sde_adj_user_kernel(const __grid_
             } else if constexpr (NZ == 2) {
                 R z[MAXM];
                 pair.get(key, pre, k, a.step_offset, z[0], z[1]);
-                correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
+                with_step_chol(a, k, [&](const R *chol) { correlate<R, MAXM>(chol, a.has_corr, z, sq, dW); });
             } else if constexpr (!JUMPS) {
-                step_increments<R, MAXM, false>(key, pre, c1w, NCALL, a.chol, a.has_corr, sq, dW);
+                with_step_chol(a, k, [&](const R *chol) {
+                    step_increments<R, MAXM, false>(key, pre, c1w, NCALL, chol, a.has_corr, sq, dW);
+                });
             } else {
                 uint32_t u[4 * NCMAX];
                 step_words<MAXM, JUMPS>(key, pre, c1w, NCALL, u);
                 R z[MAXM];
                 words_to_normals<R, MAXM, 4 * NCMAX, false>(u, z);
-                correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
+                with_step_chol(a, k, [&](const R *chol) { correlate<R, MAXM>(chol, a.has_corr, z, sq, dW); });
 #pragma unroll
                 for (int m = 0; m < MG; ++m) jumps(m, pick_word(u, 2 * PP + m), k, c1w, dN, dJ);
             }

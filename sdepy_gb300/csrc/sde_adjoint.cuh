@@ -77,7 +77,19 @@ struct AdjArgs {
     // level-1 checkpoints written by the forward run, [nseg][W][paths], or
     // NULL (the kernel's own checkpoint sweep)
     const R *ckpt;
+    // time-dependent correlation: [steps][NCHOL] packed Cholesky factors of
+    // each step's correlation matrix, or NULL (chol applies throughout)
+    const R *chol_t;
 };
+
+// f(the Cholesky factor of step k): the per-step table's row (uniform
+// test), else the constant factor of the parameter block -- two copies of
+// f, so that the constant one keeps its constant-bank loads
+template <typename R, typename F>
+__device__ __forceinline__ void with_step_chol(const AdjArgs<R> &a, int k, F &&f) {
+    if (a.chol_t) f(a.chol_t + (int64_t)k * NCHOL);
+    else f(a.chol);
+}
 
 // Tangent-mode run of a user program (single equation): the terms' values
 // A[i] and their derivatives dA[i][0] = dA_i/dx, dA[i][1 + j] = dA_i/dp_j.
@@ -430,7 +442,7 @@ sde_adj_kernel(const __grid_constant__ AdjArgs<R> a) {
                 step_words<MAXM, JUMPS>(key, pre, (uint32_t)k + a.step_offset, NC, u);
                 words_to_normals<R, MAXM>(u, z);
             }
-            correlate<R, MAXM>(a.chol, a.has_corr, z, sq, dW);
+            with_step_chol(a, k, [&](const R *chol) { correlate<R, MAXM>(chol, a.has_corr, z, sq, dW); });
         };
         R val = R(0);
         if (MODEL == SDE_MODEL_LINEAR) {

@@ -1193,13 +1193,14 @@ struct AdjPlan {
 };
 
 template <typename R>
-static int adjoint_plan(const SdeSpec *s, int n_steps, bool jumps, bool td, bool ujit, int nv, int req_seg,
-                        bool fromck, AdjPlan *P) {
+static int adjoint_plan(const SdeSpec *s, int n_steps, bool jumps, bool td, bool corr_t, bool ujit, int nv,
+                        int req_seg, bool fromck, AdjPlan *P) {
     const int M = s->group_size;
     const bool linear = s->model == SDE_MODEL_LINEAR;
     // the FP32 2-variable Heston adjoint keeps its segment in shared memory:
-    // at most ADJ_HESTON_SEG steps, one checkpoint level
-    P->heston_fast = sizeof(R) == 4 && s->model == SDE_MODEL_HESTON && M == 2 && !jumps && !td &&
+    // at most ADJ_HESTON_SEG steps, one checkpoint level; constant parameters
+    // and correlation
+    P->heston_fast = sizeof(R) == 4 && s->model == SDE_MODEL_HESTON && M == 2 && !jumps && !td && !corr_t &&
                      (fromck ? req_seg <= ADJ_HESTON_SEG
                              : (n_steps + ADJ_HESTON_SEG - 1) / ADJ_HESTON_SEG <= ADJ_MAXSEG);
     int cap = P->heston_fast ? ADJ_HESTON_SEG : ADJ_MAXSEG;
@@ -1286,7 +1287,8 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     if (fromck && req->checkpoint < 1)
         return fail(SDE_ERR_INVALID, "checkpoints from the forward need req->checkpoint, their segment length");
     AdjPlan plan;
-    if ((rc = adjoint_plan<R>(s, n_steps, jumps, td, ujit, nv, req->checkpoint, fromck, &plan))) return rc;
+    const bool corr_t = gr->corr_t != nullptr;
+    if ((rc = adjoint_plan<R>(s, n_steps, jumps, td, corr_t, ujit, nv, req->checkpoint, fromck, &plan))) return rc;
     const bool heston_fast = plan.heston_fast;
     const int seg = plan.seg, seg2 = plan.seg2, nseg = plan.nseg;
     const size_t ubytes = plan.ubytes;
@@ -1308,7 +1310,8 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     const size_t o_tk = o_thr1 + al(sizeof(long long) * njt);   // step starts, for user SDEs
     const size_t o_pt = o_tk + al(sizeof(R) * (user ? n_steps : 1));   // slots 0..2 per step
     const size_t o_jp = o_pt + al(sizeof(R) * (td ? (size_t)n_steps * 3 * W : 1));   // a user dj law's a, b, pa
-    const size_t o_end = o_jp + al(sizeof(R) * (user && jumps ? (size_t)3 * W : 1));
+    const size_t o_ct = o_jp + al(sizeof(R) * (user && jumps ? (size_t)3 * W : 1));   // per-step Cholesky rows
+    const size_t o_end = o_ct + al(sizeof(R) * (corr_t ? (size_t)n_steps * NCHOL : 1));
     D->host_tables.resize(o_end);
     char *H = D->host_tables.data();
     R *h_dt = (R *)(H + o_dt), *h_sq = (R *)(H + o_sq), *h_x0 = (R *)(H + o_x0), *h_prm = (R *)(H + o_prm);
@@ -1345,7 +1348,22 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
                 h_p0[(size_t)k * W + w] = p0;
                 poisson_thresholds(p0, L, h_thr[(size_t)k * W + w], h_thr1[(size_t)k * W + w]);
             }
-    if (s->corr) {
+    if (corr_t) {   // each step's factor, as the forward run factors them
+        R *h_ct = (R *)(H + o_ct);
+        std::vector<double> L(M * M);
+        for (int k = 0; k < n_steps; ++k) {
+            if ((rc = sde_cholesky(gr->corr_t + (size_t)k * M * M, M, L.data()))) {
+                char m[256];
+                snprintf(m, sizeof m, "correlation of step %d: %s", k, g_err.c_str());
+                return fail(rc, "%s", m);
+            }
+            R *row = h_ct + (size_t)k * NCHOL;
+            for (int i = 0; i < NCHOL; ++i) row[i] = R(0);
+            for (int i = 0; i < M; ++i)
+                for (int j = 0; j <= i; ++j) row[i * (i + 1) / 2 + j] = (R)L[i * M + j];
+        }
+        a.has_corr = 1;   // (no gradient of a time-dependent correlation)
+    } else if (s->corr) {
         std::vector<double> L(M * M);
         if ((rc = sde_cholesky(s->corr, M, L.data()))) return rc;
         for (int i = 0; i < M; ++i)
@@ -1372,6 +1390,7 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     a.nseg = nseg;
     a.seg2 = seg2;
     a.ckpt = fromck ? (const R *)req->ckpt : nullptr;
+    a.chol_t = corr_t ? (const R *)(T + o_ct) : nullptr;
     a.step_offset = gr->step_offset;
     a.out_mode = s->out_mode;
     a.jump_law = s->jump_law;
@@ -1501,7 +1520,9 @@ static int adjoint_checkpoints_impl(const SdeSpec *s, const SdeGrid *gr, int32_t
     if (s->model == SDE_MODEL_LINEAR || table || s->flags) return SDE_OK;   // none written or read
     const AdjKind K = adjoint_kind(s);
     AdjPlan P;
-    if ((rc = adjoint_plan<R>(s, n_steps, K.jumps, gr->params_t != nullptr, K.ujit, K.nv, 0, false, &P))) return rc;
+    if ((rc = adjoint_plan<R>(s, n_steps, K.jumps, gr->params_t != nullptr, gr->corr_t != nullptr, K.ujit, K.nv, 0,
+                              false, &P)))
+        return rc;
     *seg = P.seg;
     *bytes = (int64_t)P.nseg * s->groups * s->group_size * s->paths * (int64_t)sizeof(R);
     return SDE_OK;
@@ -1516,8 +1537,6 @@ extern "C" int32_t sde_adjoint_checkpoints(const SdeSpec *spec, const SdeGrid *g
 extern "C" int32_t sde_adjoint(const SdeSpec *spec, const SdeGrid *grid, const SdeAdjReq *req, double *grad,
                                double *value) {
     if (!spec) return fail(SDE_ERR_INVALID, "spec is NULL");
-    if (grid && grid->corr_t)
-        return fail(SDE_ERR_UNSUPPORTED, "the adjoint takes a constant correlation (grid corr_t must be NULL)");
     if (spec->flags) return fail(SDE_ERR_UNSUPPORTED, "the adjoint takes no spec flags (antithetic paths)");
     if (spec->precision == SDE_FP32) return adjoint_impl<float>(spec, grid, req, grad, value);
     return adjoint_impl<double>(spec, grid, req, grad, value);

@@ -451,3 +451,57 @@ def test_checkpoints_where_the_forward_writes_none(lib):
     o = _lib.SdeOut()
     o.n_rows, o.ckpt, o.ckpt_seg = 2, buf.data_ptr(), 4
     assert lib.sde_run(C.byref(P._make_spec(1, 1)), C.byref(g), None, C.byref(o)) == _lib.ERR_UNSUPPORTED
+
+
+def test_adjoint_with_time_dependent_correlation(lib):
+    """A correlation that depends on time (SdeGrid.corr_t: each step's
+    Cholesky factor, as the forward run draws) -- an OU pair with
+    corr(t) = [[1, .6 cos t], [.6 cos t, 1]] through the C-ABI, and Heston
+    with rho(t) = -.5 - .3 t through autograd.expectation: the gradients of
+    the other parameters against central differences on common random
+    numbers (FP64); the correlation itself is not differentiated."""
+    from sdepy_gb300.autograd import expectation
+    import torch
+    corr = lambda t: np.array([[1., .6*np.cos(t)], [.6*np.cos(t), 1.]])   # noqa: E731
+    tl, steps, paths = (0., 1.), 120, 20011
+    kw = dict(x0=.2, k=1.5, theta=.4, sigma=.3)
+
+    def mean(**over):   # the two components' terminal means
+        P = sg.ornstein_uhlenbeck_process(paths=paths, steps=steps, vshape=2, corr=corr,
+                                          rng=sg.philox_rng(4, 2), **dict(kw, **over))
+        return np.asarray(P.montecarlo(tl, bins=None).mean()).reshape(-1)
+    P = sg.ornstein_uhlenbeck_process(paths=paths, steps=steps, vshape=2, corr=corr,
+                                      rng=sg.philox_rng(4, 2), **kw)
+    leg = Grid(tl, steps).legs[-1]
+    g = _lib.SdeGrid()
+    g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
+    g.n_pts, g.step_offset = leg.tt.size, 0
+    ctab = P._corr_table(leg)
+    g.corr_t = _lib.dptr(ctab)
+    req = _lib.SdeAdjReq()
+    req.mean_weight = 1.
+    grad = np.zeros((2, 8))
+    val = C.c_double()
+    _lib.check(lib.sde_adjoint(C.byref(P._make_spec(4, 2)), C.byref(g), C.byref(req), _lib.dptr(grad),
+                               C.byref(val)), 'sde_adjoint')
+    m0 = mean()
+    assert abs(val.value - m0.sum()) <= 1e-12*max(1., abs(m0.sum()))
+    for name, slot in (('x0', 0), ('k', 1), ('theta', 2), ('sigma', 3)):
+        h = 1e-5*max(abs(kw[name]), 1e-2)
+        fd_ = (mean(**{name: kw[name] + h}).sum() - mean(**{name: kw[name] - h}).sum())/(2*h)
+        assert abs(grad[:, slot].sum() - fd_) <= 1e-7*max(1., abs(fd_)), (name, grad[:, slot].sum(), fd_)
+
+    hk = dict(x0=100., mu=.03, sigma=1., y0=.09, k=3., theta=.09, xi=.1)
+    rho = lambda t: -.5 - .3*t   # noqa: E731
+
+    def hes(**over):
+        ts = {n: torch.tensor(v, dtype=torch.float64, requires_grad=True) for n, v in dict(hk, **over).items()}
+        y = expectation(sg.heston_process, (0., 1.), [], paths=paths, steps=100, dtype=np.float64, seed=6,
+                        rho=rho, **ts)
+        y.sum().backward()
+        return float(y.sum().detach()), {n: float(t.grad) for n, t in ts.items()}
+    v, gr = hes()
+    for name in hk:
+        h = 1e-5*max(abs(hk[name]), 1e-2)
+        fd_ = (hes(**{name: hk[name] + h})[0] - hes(**{name: hk[name] - h})[0])/(2*h)
+        assert abs(gr[name] - fd_) <= 1e-6*max(1., abs(fd_)), (name, gr[name], fd_)
