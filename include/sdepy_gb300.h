@@ -192,8 +192,10 @@ typedef struct SdeGrid {
      * increments of step k, evaluated at its midpoint tt[k] + dt/2 as
      * sdepy's wiener_source evaluates a callable corr
      * (sdepy/infrastructure.py:1540).  The library factors every step's
-     * matrix (sde_cholesky).  Ignored with injected increments; sde_adjoint
-     * and sde_run_stats_static return SDE_ERR_UNSUPPORTED. */
+     * matrix (sde_cholesky).  Ignored with injected increments;
+     * sde_adjoint draws with the same factors (the correlation is not
+     * differentiated: no rho gradient); sde_run_stats_static returns
+     * SDE_ERR_UNSUPPORTED. */
     const double *corr_t;
     /* User SDEs with dn / dj terms: time-dependent Poisson intensity, or
      * NULL (SdeUserProgram.jump_params row 0 applies at every step):
