@@ -524,9 +524,10 @@ def _fused(lib, P, timeline, strikes, seed, ckpt=None):
     return arrs, leg
 
 
-def _adjoint_ms(lib, P, timeline, strike):
+def _adjoint_ms(lib, P, timeline, strike, ckpt=None):
     """Device time of one adjoint call (mean and one call payoff of the last
-    timeline point) of process P."""
+    timeline point) of process P (ckpt: (device pointer, segment) of
+    checkpoints a forward run wrote)."""
     import ctypes as C
     from sdepy_gb300 import _lib
     from sdepy_gb300.grid import Grid
@@ -539,6 +540,8 @@ def _adjoint_ms(lib, P, timeline, strike):
     req = _lib.SdeAdjReq()
     req.n_strikes, req.checkpoint, req.mean_weight = 1, 0, 1.
     req.strikes[0], req.weights[0] = strike, 1.
+    if ckpt is not None:
+        req.ckpt, req.checkpoint = ckpt
     grad = np.zeros((P._W, 8))
     v = C.c_double()
 
@@ -578,12 +581,33 @@ def user_adjoint_bench(lib, K=2**22):
         ('preset_merton', sg.merton_jumpdiff_process(paths=K, steps=365, x0=1., mu=.03, sigma=.15, lam=1., a=-.1,
                                                      b=.15, **f32), (0., 1.), 1.),
     )
+    import ctypes as C
+    import torch
+    from sdepy_gb300 import _lib
+    from sdepy_gb300.grid import Grid
     out = {}
     for name, P, tl, strike in cases:
         _fused(lib, P, tl, [strike], 8)   # (compiles a compiled program's forward)
         f_ms = _time_call(lambda: _fused(lib, P, tl, [strike], 8), lib)
         a_ms = _adjoint_ms(lib, P, tl, strike)
-        out[name + '_adjoint_fp32'] = {'forward_ms': f_ms, 'adjoint_ms': a_ms, 'grad_over_forward': a_ms/f_ms}
+        row = {'forward_ms': f_ms, 'adjoint_ms': a_ms, 'grad_over_forward': a_ms/f_ms}
+        # the forward writing the adjoint's checkpoints, the adjoint reading them
+        leg = Grid(tl, P.steps).legs[-1]
+        g = _lib.SdeGrid()
+        g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
+        g.n_pts = leg.tt.size
+        seg, nb = C.c_int32(), C.c_int64()
+        _lib.check(lib.sde_adjoint_checkpoints(C.byref(P._make_spec(8, 0)), C.byref(g), C.byref(seg),
+                                               C.byref(nb)), 'ckpts')
+        if seg.value > 0:
+            buf = torch.empty(nb.value, dtype=torch.uint8, device='cuda')
+            ck = (buf.data_ptr(), seg.value)
+            fc_ms = _time_call(lambda: _fused(lib, P, tl, [strike], 8, ck), lib)
+            ac_ms = _adjoint_ms(lib, P, tl, strike, ck)
+            row.update(forward_writing_checkpoints_ms=fc_ms, adjoint_from_checkpoints_ms=ac_ms,
+                       grad_over_forward_from_checkpoints=ac_ms/f_ms)
+            del buf
+        out[name + '_adjoint_fp32'] = row
     return out
 
 

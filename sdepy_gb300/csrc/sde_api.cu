@@ -827,7 +827,13 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
         if (out->ckpt_seg < 1) return fail(SDE_ERR_INVALID, "ckpt_seg must be >= 1");
         if (inject || anti)
             return fail(SDE_ERR_UNSUPPORTED, "checkpoints are written for device-RNG paths without antithetics");
-        if (tab) return fail(SDE_ERR_UNSUPPORTED, "the FP32 LINEAR / OU run-table kernels write no checkpoints");
+        // (the FP32 OU run-table kernel writes them for the state output with
+        // constant parameters and correlation)
+        const bool tab_ck = s->model == SDE_MODEL_OU && s->out_mode == SDE_OUT_STATE && !gr->params_t &&
+                            !gr->corr_t && M <= 8;
+        if (tab && !tab_ck)
+            return fail(SDE_ERR_UNSUPPORTED, "the FP32 LINEAR run-table kernels, and the OU one with a time-dependent "
+                                             "coefficient or correlation or another output, write no checkpoints");
         a.ckpt = (R *)out->ckpt;
         a.ckpt_seg = out->ckpt_seg;
     }
@@ -1516,8 +1522,12 @@ static int adjoint_checkpoints_impl(const SdeSpec *s, const SdeGrid *gr, int32_t
     *seg = 0;
     *bytes = 0;
     const int n_steps = gr->n_pts - 1;
-    const bool table = sizeof(R) == 4 && (s->model == SDE_MODEL_LINEAR || s->model == SDE_MODEL_OU);
-    if (s->model == SDE_MODEL_LINEAR || table || s->flags) return SDE_OK;   // none written or read
+    // none read (LINEAR), or none written: antithetic runs, and the FP32 OU
+    // run-table forward but for the state output with constant parameters
+    // and correlation
+    const bool table_none = sizeof(R) == 4 && s->model == SDE_MODEL_OU &&
+                            (s->out_mode != SDE_OUT_STATE || gr->params_t || gr->corr_t);
+    if (s->model == SDE_MODEL_LINEAR || table_none || s->flags) return SDE_OK;
     const AdjKind K = adjoint_kind(s);
     AdjPlan P;
     if ((rc = adjoint_plan<R>(s, n_steps, K.jumps, gr->params_t != nullptr, gr->corr_t != nullptr, K.ujit, K.nv, 0,

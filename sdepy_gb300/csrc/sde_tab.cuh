@@ -100,8 +100,10 @@ __device__ __forceinline__ void tab_store_state(float *xx, float *stats_vals, co
 }
 
 // ALT: an output transform other than OUT_STATE (exp of the states, their
-// sum); the initial row is written by tab_row0_kernel
-template <int MODEL, int MAXM, bool CORR, bool ALT>
+// sum); the initial row is written by tab_row0_kernel.  CK: the OU state
+// (theta0 added back) is also stored before every ckpt_seg-th step, the
+// adjoint's checkpoints (FwdArgs::ckpt)
+template <int MODEL, int MAXM, bool CORR, bool ALT, bool CK = false>
 __global__ void __launch_bounds__(BLOCK, TabOccupancy<MAXM>::MIN_BLOCKS)
 sde_fwd_tab_kernel(const __grid_constant__ FwdArgs<float> a) {
     constexpr bool SHIFT = MODEL == SDE_MODEL_OU;
@@ -130,6 +132,7 @@ sde_fwd_tab_kernel(const __grid_constant__ FwdArgs<float> a) {
         // first Philox rounds of this path's calls (independent of the step)
         const PathPre<NZ ? 1 : NCN> pre(key, (uint32_t)p + a.path_offset, (uint32_t)g, a.stream);
         PairedSteps<float, NZ ? NZ : 1, true> pair;
+        int next_ck = 0, ci = 0;   // CK: the next checkpoint's step and index
 
 #pragma unroll 1
         for (int ri = 0; ri < a.n_runs; ++ri) {
@@ -137,6 +140,17 @@ sde_fwd_tab_kernel(const __grid_constant__ FwdArgs<float> a) {
             const float *tb = a.coef + ((int64_t)run.w * a.groups + g) * 2 * MAXM;
 #pragma unroll UNROLL
             for (int k = run.x; k < run.y; ++k) {
+                if constexpr (CK) {
+                    if (k == next_ck) {
+#pragma unroll
+                        for (int m = 0; m < MAXM; ++m)
+                            if (m < a.M)
+                                a.ckpt[((int64_t)ci * a.W + g * a.M + m) * a.paths + p] =
+                                    SHIFT ? st[m] + __ldg(a.tshift + g * 2 * MAXM + m) : st[m];
+                        ++ci;
+                        next_ck += a.ckpt_seg;
+                    }
+                }
                 float dW[MAXM];
                 if constexpr (NZ == 1) {
                     uint32_t w_unused;
@@ -328,10 +342,22 @@ void launch_fwd_tab(const FwdArgs<float> &a, dim3 grid, cudaStream_t s) {
         tab_row0_kernel<MAXM><<<grid, BLOCK, 0, s>>>(a.x0, a.xx, a.stats_vals, a.paths, a.n_out_vars, a.M, a.out_mode,
                                                      a.opg, a.tab_row0, a.stats_row);
     const bool corr = a.has_corr && MAXM > 1, alt = a.out_mode != SDE_OUT_STATE;
-    if (corr && alt) sde_fwd_tab_kernel<MODEL, MAXM, true, true><<<grid, BLOCK, 0, s>>>(a);
-    else if (corr) sde_fwd_tab_kernel<MODEL, MAXM, true, false><<<grid, BLOCK, 0, s>>>(a);
-    else if (alt) sde_fwd_tab_kernel<MODEL, MAXM, false, true><<<grid, BLOCK, 0, s>>>(a);
-    else sde_fwd_tab_kernel<MODEL, MAXM, false, false><<<grid, BLOCK, 0, s>>>(a);
+    bool ck = false;
+    if constexpr (MODEL == SDE_MODEL_OU && MAXM <= 8) {   // the OU state with the adjoint's checkpoints
+        ck = a.ckpt && !alt;
+        if (ck && corr) sde_fwd_tab_kernel<MODEL, MAXM, true, false, true><<<grid, BLOCK, 0, s>>>(a);
+        else if (ck) sde_fwd_tab_kernel<MODEL, MAXM, false, false, true><<<grid, BLOCK, 0, s>>>(a);
+    }
+    if (ck) {
+    } else if (corr && alt) {
+        sde_fwd_tab_kernel<MODEL, MAXM, true, true><<<grid, BLOCK, 0, s>>>(a);
+    } else if (corr) {
+        sde_fwd_tab_kernel<MODEL, MAXM, true, false><<<grid, BLOCK, 0, s>>>(a);
+    } else if (alt) {
+        sde_fwd_tab_kernel<MODEL, MAXM, false, true><<<grid, BLOCK, 0, s>>>(a);
+    } else {
+        sde_fwd_tab_kernel<MODEL, MAXM, false, false><<<grid, BLOCK, 0, s>>>(a);
+    }
     if (a.partials && a.stats_row >= 0) {
         const float *vals = a.stats_vals ? a.stats_vals : a.xx ? a.xx + (int64_t)a.stats_row * a.n_out_vars * a.paths
                                                                 : nullptr;

@@ -396,6 +396,9 @@ CK_CASES = [
      (0., 1.), [.3]),
     ('ou_fp64_5000_steps', lambda: sg.ornstein_uhlenbeck_process(paths=2048, steps=5000, x0=.1, k=1.3, theta=.4,
                                                                   sigma=.3), (0., 2.), [.3]),
+    ('ou_fp32_run_table', lambda: sg.ornstein_uhlenbeck_process(paths=20011, steps=300, dtype=np.float32,
+                                                                 vshape=2, corr=[[1., .5], [.5, 1.]], x0=.1, k=1.3,
+                                                                 theta=.4, sigma=.3), (0., 1.), [.3]),
     ('cir_fp32', lambda: sg.cox_ingersoll_ross_process(paths=20011, steps=200, dtype=np.float32, x0=.04, k=2.,
                                                        theta=.04, xi=.2), (0., 1.), [.04]),
     ('user_ou_interpreted', lambda: _user(lambda t, x, theta=.5, k=2., sigma=.3: {'dt': k*(theta - x), 'dw': sigma},
@@ -433,20 +436,21 @@ def test_adjoint_from_forward_checkpoints(lib, case):
 
 def test_checkpoints_where_the_forward_writes_none(lib):
     """sde_adjoint_checkpoints answers 0 for the models whose adjoint takes
-    no checkpoints (LINEAR) and for the FP32 OU run-table forward, which
-    refuses a checkpoint array."""
+    no checkpoints (LINEAR) and for the FP32 OU run-table forward with a
+    time-dependent theta, which refuses a checkpoint array."""
+    leg = Grid((0., 1.), 10).legs[-1]
     for P in (sg.lognorm_process(paths=100, steps=10, x0=1., mu=.1, sigma=.2),
-              sg.ornstein_uhlenbeck_process(paths=100, steps=10, dtype=np.float32)):
-        leg = Grid((0., 1.), 10).legs[-1]
+              sg.ornstein_uhlenbeck_process(paths=100, steps=10, dtype=np.float32, theta=lambda t: 1. + t)):
         g = _lib.SdeGrid()
         g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
         g.n_pts = leg.tt.size
+        ptab = P._params_table(leg) if P._tdep else None
+        g.params_t = _lib.dptr(ptab)
         spec = P._make_spec(1, 1)
         seg, nb = C.c_int32(7), C.c_int64(7)
         _lib.check(lib.sde_adjoint_checkpoints(C.byref(spec), C.byref(g), C.byref(seg), C.byref(nb)), 'ckpts')
         assert seg.value == 0 and nb.value == 0
     import torch
-    P = sg.ornstein_uhlenbeck_process(paths=100, steps=10, dtype=np.float32)
     buf = torch.empty(4*100*10, dtype=torch.uint8, device='cuda')
     o = _lib.SdeOut()
     o.n_rows, o.ckpt, o.ckpt_seg = 2, buf.data_ptr(), 4
