@@ -17,10 +17,13 @@ def build(force=False):
        os.path.getmtime(LIB) >= max(os.path.getmtime(p) for p in (SRC, HDR, TAB)):
         return LIB
     os.makedirs(OUT, exist_ok=True)
+    # (a file of this process's own, renamed into place: processes that
+    # build at the same time never load a partly written library)
+    tmp = '{}.{}.tmp'.format(LIB, os.getpid())
     cmd = ['gcc', '-O2', '-std=c11', '-D_DEFAULT_SOURCE', '-fPIC', '-shared',
-           '-ffp-contract=off', '-fno-fast-math', SRC, '-o', LIB + '.tmp', '-lm']
+           '-ffp-contract=off', '-fno-fast-math', SRC, '-o', tmp, '-lm']
     subprocess.run(cmd, check=True)
-    os.replace(LIB + '.tmp', LIB)
+    os.replace(tmp, LIB)
     return LIB
 
 

@@ -69,7 +69,7 @@ def build(force=False, verbose=False):
     workers = max(1, min(len(jobs), os.cpu_count() or 1))
     with cf.ThreadPoolExecutor(workers) as ex:
         objs = list(ex.map(run, jobs))
-    tmp = LIB + '.tmp'
+    tmp = '{}.{}.tmp'.format(LIB, os.getpid())   # renamed into place when linked
     cmd = [cc] + ARCH + ['-shared', '-o', tmp] + objs + ['-lcudart', '-ldl']
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

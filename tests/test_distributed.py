@@ -115,6 +115,7 @@ def test_gloo_two_ranks_shard_one_run():
     import multiprocessing as mp
     from helpers import oracle_paths
     from oracle import load_c
+    load_c()   # built here, before the ranks load it
     ctx = mp.get_context('spawn')
     q = ctx.Queue()
     port = _free_port()
