@@ -1019,7 +1019,8 @@ def run_case(args):
     values: moments, cdf at 41 values, chf at 4 values of u), 'cir_user'
     (CIR and an interpreted user SDE, FP32, 2^20 paths x 499 steps),
     'user_adjoint' (the user-SDE adjoints against their forwards, 2^20
-    paths)."""
+    paths), 'user_ou_adjoint' (the compiled user OU adjoint, 2^20 paths, with
+    and without forward checkpoints)."""
     import ctypes as C
     import torch
     import sdepy_gb300 as sg
@@ -1111,6 +1112,27 @@ def run_case(args):
         print(json.dumps({'case': args.case, **res}))
     elif args.case == 'user_adjoint':
         print(json.dumps({'case': args.case, **user_adjoint_bench(lib, 2**20)}))
+    elif args.case == 'user_ou_adjoint':
+        # the compiled user OU adjoint alone: 2^20 paths x 499 steps, FP32;
+        # own checkpoint sweep, then after forward runs writing checkpoints
+        ou_f = lambda t, x, theta=.5, k=2., sigma=.3: {'dt': k*(theta - x), 'dw': sigma}   # noqa: E731
+        P = sg.integrate(ou_f, jit=True)(paths=2**20, steps=500, x0=1., dtype=np.float32)
+        tl = (0., 2.)
+        _fused(lib, P, tl, [.5], 8)
+        own = [_adjoint_ms(lib, P, tl, .5) for _ in range(args.warmup + args.steps)]
+        leg = Grid(tl, P.steps).legs[-1]
+        g = _lib.SdeGrid()
+        g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
+        g.n_pts = leg.tt.size
+        seg, nb = C.c_int32(), C.c_int64()
+        _lib.check(lib.sde_adjoint_checkpoints(C.byref(P._make_spec(8, 0)), C.byref(g), C.byref(seg),
+                                               C.byref(nb)), 'ckpts')
+        buf = torch.empty(nb.value, dtype=torch.uint8, device='cuda')
+        ck = (buf.data_ptr(), seg.value)
+        _fused(lib, P, tl, [.5], 8, ck)
+        fromck = [_adjoint_ms(lib, P, tl, .5, ck) for _ in range(args.warmup + args.steps)]
+        print(json.dumps({'case': args.case, 'adjoint_ms': own[-1], 'adjoint_from_checkpoints_ms': fromck[-1],
+                          'segment': seg.value, 'checkpoint_bytes': nb.value}))
     elif args.case == 'process_post':
         print(json.dumps({'case': args.case, 'result': process_post_bench(
             lib, reps=args.steps, api=False, dtypes=(np.float32,))}))
@@ -1128,7 +1150,7 @@ def main():
                     help='timed steps only: no FP64 / e2e / CPU / probe extras')
     ap.add_argument('--case', default=None,
                     choices=['heston_adjoint', 'batch', 'lognorm_fp64', 'process_post', 'cir_user',
-                             'user_adjoint'],
+                             'user_adjoint', 'user_ou_adjoint'],
                     help='run one small single-kernel case (profiling)')
     args = ap.parse_args()
     if args.case:
