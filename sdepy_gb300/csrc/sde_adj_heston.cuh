@@ -9,11 +9,10 @@
 // kernel (sde_tab.cuh): parameters and Philox keys in registers or
 // constant-bank operands, no reference to the parameter block handed to a
 // helper.  Per step the recomputation stores the variance before the step
-// and the two normals (3 floats, [seg][3][BLOCK] so that a warp's stores
-// are contiguous); the backward pass rebuilds the correlated increments from
-// the normals with the forward's arithmetic, so they are the forward's bit
-// for bit.  Only the eight slots the model has are accumulated (Kahan, per
-// thread), then reduced per block into sde_adj_kernel's partial layout.
+// and the two correlated increments (3 floats, [seg][3][BLOCK] so that a
+// warp's stores are contiguous), which the backward pass reads back.  Only
+// the eight slots the model has are accumulated (Kahan, per thread), then
+// reduced per block into sde_adj_kernel's partial layout.
 #pragma once
 
 #include "sde_adjoint.cuh"
@@ -42,6 +41,11 @@ static __global__ void __launch_bounds__(BLOCK, 3) sde_adj_heston_kernel(const _
                 L11 = a.has_corr ? a.chol[2] : 1.f;
     const bool corr = a.has_corr != 0, rho_grad = a.rho_grad != 0, out_xy = a.out_mode == SDE_OUT_HESTON_XY;
     const float rho_k = a.rho_k, wmean = a.wmean;
+    // (z0 + rho_k z1) sqrt(dt) = rw1 dWx + rw2 dWy for dWx = L00 z0 sqrt(dt),
+    // dWy = (L10 z0 + L11 z1) sqrt(dt): the rho derivative's increment
+    const float rw2 = rho_grad ? rho_k / L11 : 0.f;
+    const float rw1 = rho_grad ? (1.f - rw2 * L10) / L00 : 0.f;
+    const float hsg2 = -0.5f * sg * sg, nkk = -kk;   // loop constants of the backward step
     const int n_strikes = a.n_strikes;
 #pragma unroll
     for (int i = 0; i < SDE_MAX_STRIKES; ++i)   // constant indices: no parameter address
@@ -139,40 +143,41 @@ static __global__ void __launch_bounds__(BLOCK, 3) sde_adj_heston_kernel(const _
             for (int k = k0; k < k1; ++k) {
                 float z0, z1, dWx, dWy;
                 pair.get(key, pre, k, step_offset, z0, z1);
+                incr(z0, z1, __ldg(a.sqdt + k), dWx, dWy);
                 float *b = hbuf + (k - k0) * 3 * BLOCK + threadIdx.x;
                 b[0] = sy;
-                b[BLOCK] = z0;
-                b[2 * BLOCK] = z1;
-                incr(z0, z1, __ldg(a.sqdt + k), dWx, dWy);
+                b[BLOCK] = dWx;
+                b[2 * BLOCK] = dWy;
                 step(__ldg(a.dt + k), dWx, dWy, sx, sy);
             }
             if constexpr (fromck)
                 if (s == nseg - 1) terminal(sx, sy);
             for (int k = k1 - 1; k >= k0; --k) {
                 const float *b = hbuf + (k - k0) * 3 * BLOCK + threadIdx.x;
-                const float yv = b[0], z0 = b[BLOCK], z1 = b[2 * BLOCK];
-                const float dt = __ldg(a.dt + k), sq = __ldg(a.sqdt + k);
-                float dWx, dWy;
-                incr(z0, z1, sq, dWx, dWy);
+                const float yv = b[0], dWx = b[BLOCK], dWy = b[2 * BLOCK];
+                const float dt = __ldg(a.dt + k);
                 const float yp = fmaxf(yv, 0.f);
                 const float sr = A::sqrt_(yp);
                 const float ab = xbx, ybn = xby;
+                const float ys = ybn * sr;
                 gmu += ab * dt;
                 gsg += ab * (sr * dWx - sg * yp * dt);
                 gk += ybn * (th - yp) * dt;
-                gth += ybn * kk * dt;
-                gxi += ybn * sr * dWy;
-                if (rho_grad) grho += ybn * xi * sr * ((z0 + rho_k * z1) * sq);
+                gth += ybn * dt;   // (times k at the path's end)
+                gxi += ys * dWy;
+                // (z0 + rho_k z1) sqrt(dt) from the increments
+                if (rho_grad) grho += (ys * xi) * fmaf(rw1, dWx, rw2 * dWy);
                 float ny = ybn;
                 if (yv > 0.f && sr > 0.f) {
-                    const float inv = 0.5f / sr;
-                    const float dadyp = -sg * sg * dt * 0.5f + sg * dWx * inv;
-                    const float dydyp = -kk * dt + xi * dWy * inv;
-                    ny = ybn + ab * dadyp + ybn * dydyp;
+                    const float inv = __fdividef(0.5f, sr);   // (approximate: a gradient term)
+                    const float dadyp = fmaf(sg * dWx, inv, hsg2 * dt);
+                    const float dydyp = fmaf(xi * dWy, inv, nkk * dt);
+                    ny = fmaf(ab, dadyp, fmaf(ybn, dydyp, ybn));
                 }
                 xby = ny;
             }
         }
+        gth *= kk;
         kahan_add(acc[0], cmp[0], xbx);
         kahan_add(acc[1], cmp[1], gmu);
         kahan_add(acc[2], cmp[2], gsg);
