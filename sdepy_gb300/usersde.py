@@ -29,8 +29,10 @@ increments through ``corr`` / ``rho``; the ``log`` flag; sources given as
 arguments (``dw=``, ``dn=``, ``dj=``), realised on the host and replayed.
 Control flow on the state (``if x > 0``, Python's ``max``), antithetic
 sources and other source ids are refused.  Pathwise gradients
-(sdepy_gb300.autograd.expectation) are taken for single equations driven
-by 'dt' / 'dw'.
+(sdepy_gb300.autograd.expectation) are taken for every supported program:
+single equations and systems, any of the four terms (interpreted in
+tangent mode for single equations driven by 'dt' / 'dw' with jit=False;
+otherwise compiled with a generated reverse-mode step).
 """
 import ctypes as C
 import inspect
