@@ -388,6 +388,11 @@ def _user(f, **kw):
     return sg.integrate(f, **kw)
 
 
+def _sv(t, x, y, mu=.05, k=3., theta=.09, xi=.1):
+    yp = np.maximum(y, 0.)
+    return ({'dt': mu*x, 'dw': np.sqrt(yp)*x}, {'dt': k*(theta - yp), 'dw': xi*np.sqrt(yp)})
+
+
 CK_CASES = [
     ('heston_fp32', lambda: sg.heston_process(paths=20011, steps=499, dtype=np.float32, **HES), (0., 2.),
      [90., 100.]),
@@ -408,6 +413,14 @@ CK_CASES = [
         paths=20011, steps=200, dtype=np.float32, x0=1.), (0., 1.), [.6]),
     ('user_jumps_compiled', lambda: _user(lambda t, x, a=.3, b=.5, s=.2: {'dn': a, 'dt': -b*x, 'dj': x, 'dw': s})(
         paths=20011, steps=100, x0=.5, lam=2., y=sg.exp_rv(.2)), (0., 1.), [.5]),
+    # a system (two correlated equations) and a compiled program over 2000
+    # steps, whose checkpoint segments exceed the shared-memory buffer (two
+    # levels inside each)
+    ('user_system_compiled', lambda: _user(_sv, q=2, sources=('dt', 'dw'))(
+        paths=20011, steps=150, x0=(100., .09), rho=-.6), (0., 1.), [100.]),
+    ('user_ou_compiled_2000_steps', lambda: _user(lambda t, x, theta=.5, k=2., sigma=.3: {'dt': k*(theta - x),
+                                                                                        'dw': sigma}, jit=True)(
+        paths=4099, steps=2000, x0=1.), (0., 1.), [.6]),
 ]
 
 
