@@ -197,6 +197,9 @@ __device__ __forceinline__ float path_heston(const DevInst &I, const PhiloxKey &
     const int n_steps = I.n_steps;
     const PathPre<1> pre(key, p, 0u, I.stream);
     PairedSteps<float, 2> pair;   // one Philox call per two steps
+    // the tangent recursion's constants (dt is the instance's)
+    const float hsdt = -0.5f * sg * sg * dt, kdt1 = 1.f - kk * dt, kdt = kk * dt, sgdt = sg * dt;
+    const float xrsq = xi * sq, xrksq = xi * rho_k * sq;
 #pragma unroll 1
     for (int k = 0; k < n_steps; ++k) {
         float z0, z1;
@@ -207,13 +210,12 @@ __device__ __forceinline__ float path_heston(const DevInst &I, const PhiloxKey &
         const float s = approx_sqrt(yp);
         float Ay = 0.f, By = 1.f;
         if (y > 0.f && s > 0.f) {
-            const float inv = 0.5f / s;
-            Ay = -sg * sg * dt * 0.5f + sg * dW1 * inv;
-            By = 1.f - kk * dt + xi * dW2 * inv;
+            const float inv = __fdividef(0.5f, s);   // (approximate: a derivative term)
+            Ay = fmaf(sg * dW1, inv, hsdt);
+            By = fmaf(xi * dW2, inv, kdt1);
         }
-        ta1 = ta1 + dt;
-        ta2 = ta2 + (s * dW1 - sg * yp * dt);
-        const float ey[NT] = {0.f, (th - yp) * dt, kk * dt, s * dW2, xi * s * (z0 + rho_k * z1) * sq};
+        ta2 = fmaf(s, dW1, fmaf(-sgdt, yp, ta2));
+        const float ey[NT] = {0.f, (th - yp) * dt, kdt, s * dW2, s * fmaf(xrksq, z1, xrsq * z0)};
 #pragma unroll
         for (int j = 0; j < NT; ++j) {
             const float nta = ta[j] + Ay * ty[j];
@@ -224,6 +226,7 @@ __device__ __forceinline__ float path_heston(const DevInst &I, const PhiloxKey &
         y = y + kk * (th - yp) * dt + xi * s * dW2;
         a = na;
     }
+    ta1 = (float)n_steps * dt;   // the sum of the steps
     const float X = __expf(a);
     g[0] = X;
     g[1] = X * ta1;
