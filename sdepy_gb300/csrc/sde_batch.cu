@@ -129,9 +129,8 @@ __device__ __forceinline__ float path_ou(const DevInst &I, const PhiloxKey &key,
 #pragma unroll
     for (int m = 0; m < 4; ++m) x[m] = I.x0[m];
     // tangents of x[0] w.r.t. x0, k, theta, sigma
-    float tx = 1.f, tk = 0.f, tth = 0.f, tsg = 0.f;
+    float tx, tth, tk = 0.f, tsg = 0.f;
     const float rho0 = 1.f - I.d[0];
-    const float kdt = I.d[0];
     const int W = I.nvars;
     const PathPre<1> pre(key, p, 0u, I.stream);
     // one or two variables: one Philox call per two steps
@@ -165,13 +164,16 @@ __device__ __forceinline__ float path_ou(const DevInst &I, const PhiloxKey &key,
         }
         const float dth = th0 - x[0];
         tk = fmaf(rho0, tk, dth * dt);
-        tth = fmaf(rho0, tth, kdt);
         tsg = fmaf(rho0, tsg, sq * z[0]);
-        tx = rho0 * tx;
 #pragma unroll
         for (int m = 0; m < 4; ++m)
             if (m < W) x[m] = x[m] + fmaf(-cd[m], x[m], cb[m]) + cc[m] * z[m];
     }
+    // the path-independent tangents: d x / d x0 = (1 - k dt)^n and
+    // d x / d theta = 1 - (1 - k dt)^n (the recursions t' = (1 - k dt) t
+    // and t' = (1 - k dt) t + k dt in closed form)
+    tx = powf(rho0, (float)n_steps);
+    tth = 1.f - tx;
     g[0] = tx;
     g[1] = tk;
     g[2] = tth;
