@@ -124,6 +124,8 @@ __device__ __forceinline__ float path_lin(const DevInst &I, const PhiloxKey &key
     return X;
 }
 
+// WM: the states the step loop carries (the instance's W <= WM; 1, 2 or 4)
+template <int WM>
 __device__ __forceinline__ float path_ou(const DevInst &I, const PhiloxKey &key, uint32_t p, float (&g)[NB_GRAD]) {
     float x[4];
 #pragma unroll
@@ -149,11 +151,11 @@ __device__ __forceinline__ float path_ou(const DevInst &I, const PhiloxKey &key,
 #pragma unroll 1
     for (int k = 0; k < n_steps; ++k) {
         float z[4];
-        if (W == 1) {
+        if (WM == 1) {
             uint32_t pw;
             pair1.get(key, pre, k, 0u, z[0], pw);
             z[1] = z[2] = z[3] = 0.f;
-        } else if (W == 2) {
+        } else if (WM == 2) {
             pair2.get(key, pre, k, 0u, z[0], z[1]);
             z[2] = z[3] = 0.f;
         } else {
@@ -166,7 +168,7 @@ __device__ __forceinline__ float path_ou(const DevInst &I, const PhiloxKey &key,
         tk = fmaf(rho0, tk, dth * dt);
         tsg = fmaf(rho0, tsg, sq * z[0]);
 #pragma unroll
-        for (int m = 0; m < 4; ++m)
+        for (int m = 0; m < WM; ++m)
             if (m < W) x[m] = x[m] + fmaf(-cd[m], x[m], cb[m]) + cc[m] * z[m];
     }
     // the path-independent tangents: d x / d x0 = (1 - k dt)^n and
@@ -274,7 +276,9 @@ batch_kernel(const DevInst *insts, const Item *items, int n_items, unsigned int 
             float X;
             if (CLS == 1) X = path_heston(I, key, p, g);
             else if (I.model == SDE_MODEL_LINEAR) X = path_lin(I, key, p, g, err);
-            else X = path_ou(I, key, p, g);
+            else if (I.nvars == 1) X = path_ou<1>(I, key, p, g);
+            else if (I.nvars == 2) X = path_ou<2>(I, key, p, g);
+            else X = path_ou<4>(I, key, p, g);
             n += 1.f;
             const float dd = X - mean;
             mean += dd / n;
