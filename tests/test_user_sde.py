@@ -763,3 +763,57 @@ def test_c_oracle_user_adjoint_matches_finite_differences(clib):
                 else:
                     g = grad[:, 1 + names.index(n)].sum()
                 assert abs(g - fd) <= 1e-6*max(1., abs(fd)), (spec, vshape, n, g, fd)
+
+
+def _abi_adjoint(lib, P, tl, strikes=(), seed=13, stream=4):
+    """sde_adjoint of process P through the C-ABI: gradient slots [W][8]
+    and the value."""
+    import ctypes as C
+    from sdepy_gb300.grid import Grid
+    leg = Grid(tl, P.steps).legs[-1]
+    g = _lib.SdeGrid()
+    g.tt, g.out_row = _lib.dptr(leg.tt), _lib.iptr(leg.out_row)
+    g.n_pts, g.step_offset = leg.tt.size, 0
+    ltab = P._lam_table(leg)
+    g.lam_t = _lib.dptr(ltab)
+    req = _lib.SdeAdjReq()
+    req.mean_weight = 1.
+    req.n_strikes = len(strikes)
+    for i, K in enumerate(strikes):
+        req.strikes[i], req.weights[i] = K, .5
+    grad = np.zeros((P._W, 8))
+    v = C.c_double()
+    _lib.check(lib.sde_adjoint(C.byref(P._make_spec(seed, stream)), C.byref(g), C.byref(req), _lib.dptr(grad),
+                               C.byref(v)), 'sde_adjoint')
+    return grad, v.value
+
+
+@pytest.mark.gpu
+def test_gpu_compiled_adjoint_of_wide_groups(lib):
+    """The compiled reverse-mode adjoint on groups of several states (a
+    correlated group of 4: four normals per Philox call, the general
+    increments path) equals the interpreted tangent-mode adjoint, every
+    state's slots (FP64); and a program with dn / dj terms over a group of 2
+    (the Poisson words beside the normals) against central differences of
+    the forward mean, per state."""
+    A = np.array([[1., .3, .2, .1], [.3, 1., .25, .2], [.2, .25, 1., .3], [.1, .2, .3, 1.]])
+    kw = dict(paths=20011, steps=60, vshape=4, x0=1., mu=.05, sigma=.3, gamma=.7, corr=A,
+              rng=sg.philox_rng(13, 4))
+    tl = (0., 1.)
+    gi, vi = _abi_adjoint(lib, user_class(sg, 'integrate:user_cev', jit=False)(**kw), tl, [1.])
+    gc, vc = _abi_adjoint(lib, user_class(sg, 'integrate:user_cev', jit=True)(**kw), tl, [1.])
+    assert abs(vc - vi) <= 1e-13*abs(vi)
+    np.testing.assert_allclose(gc, gi, rtol=1e-11, atol=1e-13)
+    j4 = user_class(sg, 'integrate:user_jumps4')
+    base = dict(paths=20011, steps=60, vshape=2, x0=.5, lam=2., y=sg.exp_rv(.2), a=.3, b=.5, s=.2,
+                rng=sg.philox_rng(13, 4))
+    grad, val = _abi_adjoint(lib, j4(**base), tl)
+
+    def mean(**over):
+        P = j4(**dict(base, **over, rng=sg.philox_rng(13, 4)))
+        return np.asarray(P.montecarlo(tl, bins=None).mean()).reshape(-1).sum()
+    assert abs(val - mean()) <= 1e-12*max(1., abs(val))
+    for name, slot in (('x0', 0), ('a', 1), ('b', 2), ('s', 3)):
+        h = 1e-5*max(abs(base[name]), 1e-2)
+        fd = (mean(**{name: base[name] + h}) - mean(**{name: base[name] - h}))/(2*h)
+        assert abs(grad[:, slot].sum() - fd) <= 1e-6*max(1., abs(fd)), (name, grad[:, slot].sum(), fd)
