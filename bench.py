@@ -1020,7 +1020,8 @@ def run_case(args):
     (CIR and an interpreted user SDE, FP32, 2^20 paths x 499 steps),
     'user_adjoint' (the user-SDE adjoints against their forwards, 2^20
     paths), 'user_ou_adjoint' (the compiled user OU adjoint, 2^20 paths, with
-    and without forward checkpoints)."""
+    and without forward checkpoints), 'fwd_general' (the general forward
+    kernel: FP32 Heston and a compiled user OU, 2^20 paths x 499 steps)."""
     import ctypes as C
     import torch
     import sdepy_gb300 as sg
@@ -1112,6 +1113,22 @@ def run_case(args):
         print(json.dumps({'case': args.case, **res}))
     elif args.case == 'user_adjoint':
         print(json.dumps({'case': args.case, **user_adjoint_bench(lib, 2**20)}))
+    elif args.case == 'fwd_general':
+        # the general forward kernel: FP32 Heston and a compiled user OU,
+        # 2^20 paths x 499 steps on (0, 2), fused summary with one payoff
+        ou_f = lambda t, x, theta=.5, k=2., sigma=.3: {'dt': k*(theta - x), 'dw': sigma}   # noqa: E731
+        res = {}
+        for name, P in (('heston', sg.heston_process(paths=2**20, steps=500, dtype=np.float32, **HESTON)),
+                        ('user_ou_jit', sg.integrate(ou_f, jit=True)(paths=2**20, steps=500, x0=1.,
+                                                                     dtype=np.float32))):
+            _fused(lib, P, (0., 2.), [1.], 8)
+            ms = []
+            for _ in range(args.warmup + args.steps):
+                _fused(lib, P, (0., 2.), [1.], 8)
+                lib.sde_timing(-1, last)
+                ms.append(last[0] + last[1])
+            res[name + '_ms'] = float(np.median(ms[args.warmup:]))
+        print(json.dumps({'case': args.case, **res}))
     elif args.case == 'user_ou_adjoint':
         # the compiled user OU adjoint alone: 2^20 paths x 499 steps, FP32;
         # own checkpoint sweep, then after forward runs writing checkpoints
@@ -1150,7 +1167,7 @@ def main():
                     help='timed steps only: no FP64 / e2e / CPU / probe extras')
     ap.add_argument('--case', default=None,
                     choices=['heston_adjoint', 'batch', 'lognorm_fp64', 'process_post', 'cir_user',
-                             'user_adjoint', 'user_ou_adjoint'],
+                             'user_adjoint', 'user_ou_adjoint', 'fwd_general'],
                     help='run one small single-kernel case (profiling)')
     args = ap.parse_args()
     if args.case:

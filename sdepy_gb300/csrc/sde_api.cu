@@ -588,6 +588,31 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
             }
             runs.push_back(make_int4(k0, k, row, ci));
         }
+    } else if (sizeof(R) == 4 && n_steps > 0) {
+        // the other FP32 kernels: runs of steps with one dt (and sqrt|dt|),
+        // ending where a row is stored, split where an adjoint checkpoint
+        // falls (bit 0 of w: a checkpoint before the run's first step)
+        const int cseg = (out->ckpt && out->ckpt_seg > 0) ? out->ckpt_seg : 0;
+        auto dts = [&](int k, R *d, R *q) {
+            const double dt = gr->tt[k + 1] - gr->tt[k];
+            *d = (R)dt;
+            *q = (R)sqrt(fabs(dt));
+        };
+        int k = 0;
+        while (k < n_steps) {
+            const int k0 = k;
+            R d0, q0, d1, q1;
+            dts(k, &d0, &q0);
+            int row = -1;
+            for (;;) {
+                ++k;
+                if (gr->out_row[k] >= 0) { row = gr->out_row[k]; break; }
+                if (k == n_steps || (cseg && k % cseg == 0)) break;
+                dts(k, &d1, &q1);
+                if (memcmp(&d1, &d0, sizeof(R)) != 0 || memcmp(&q1, &q0, sizeof(R)) != 0) break;
+            }
+            runs.push_back(make_int4(k0, k, row, (cseg && k0 % cseg == 0) ? 1 : 0));
+        }
     }
     const size_t o_thr1 = o_thr + al(sizeof(long long) * njt);
     const size_t o_runs = o_thr1 + al(sizeof(long long) * njt);
@@ -731,6 +756,9 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
         a.runs = (const int4 *)(T + o_runs);
         a.n_runs = (int32_t)runs.size();
         a.tshift = tshift.empty() ? nullptr : (const float *)(T + o_tsh);
+    } else if (!runs.empty()) {   // the other FP32 kernels' runs of one dt
+        a.runs = (const int4 *)(T + o_runs);
+        a.n_runs = (int32_t)runs.size();
     }
     a.prm_t = nprmt ? (const R *)(T + o_prmt) : nullptr;
     a.chol_t = nchol ? (const R *)(T + o_cholt) : nullptr;

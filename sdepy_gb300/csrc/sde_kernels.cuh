@@ -89,7 +89,9 @@ struct FwdArgs {
     const R *jprm;
     int32_t user_jsrc;
     // and the grid as runs of steps sharing one coefficient row:
-    // (first step, end step, output row stored after the run or -1, coef row)
+    // (first step, end step, output row stored after the run or -1, coef row);
+    // for the other FP32 kernels, runs of steps with one dt, w = 1 where an
+    // adjoint checkpoint falls before the run's first step, or NULL
     const int4 *runs;
     int32_t n_runs;
     R chol[NCHOL];      // packed lower triangle, row m at m*(m+1)/2
@@ -783,6 +785,9 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     // draws overlap this step's arithmetic (5-12% on the FP32 kernels), but
     // one for the 8- and 16-wide time-dependent forms, which would spill
     constexpr int UNROLL = (TDEP && MAXM >= 8) ? 1 : 2;
+    // the FP32 kernels other than the run-table ones step through runs of
+    // one dt (FwdArgs::runs, when the host gives them)
+    constexpr bool RUNS = sizeof(R) == 4 && !TAB;
     __shared__ R red[BLOCK / 32];
     __shared__ double part[MAXM][NPART];
     __shared__ R svs[NA][MAXM][BLOCK];   // this round's value of each output at the stats row
@@ -1100,22 +1105,15 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                 }
             } else {
                 // adjoint checkpoints: the state before steps 0, ckpt_seg, ...
-                // (kc counts down to the next one; uniform branch)
-                int kc = 0, ci = 0;
-#pragma unroll UNROLL
-                for (int k = 0; k < n_steps; ++k) {
-                    if (a.ckpt) {
-                        if (kc == 0) {
+                int ci = 0;
+                auto ck_store = [&]() {
 #pragma unroll
-                            for (int m = 0; m < MAXM; ++m)
-                                if (m < M) a.ckpt[((int64_t)ci * W + g * M + m) * a.paths + p] = st[m];
-                            ++ci;
-                            kc = a.ckpt_seg;
-                        }
-                        --kc;
-                    }
-                    const R dt = a.dt[k];
-                    const R sq = a.sqdt[k];
+                    for (int m = 0; m < MAXM; ++m)
+                        if (m < M) a.ckpt[((int64_t)ci * W + g * M + m) * a.paths + p] = st[m];
+                    ++ci;
+                };
+                // one Euler step, k from tt[k] (dt, sq = sqrt|dt|)
+                auto step_k = [&](int k, const R dt, const R sq) {
                     // time-dependent coefficients of step k (uniform test; not
                     // compiled into the FP32 Heston kernels' common form)
                     if (RELOAD && a.prm_t) {
@@ -1264,8 +1262,35 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
                         for (int m = 0; m < MAXM; ++m) dWn[m] = -dW[m];
                         euler(st1, dWn, negc1);
                     }
-                    const int r = a.out_row[k + 1];
-                    if (r >= 0) store(r, false);
+                };
+                if (RUNS && a.runs) {
+                    // runs of steps with one dt, ending where a row is stored
+                    // and split where a checkpoint falls (bit 0 of run.w): no
+                    // per-step row test or dt load
+#pragma unroll 1
+                    for (int ri = 0; ri < a.n_runs; ++ri) {
+                        const int4 run = __ldg(a.runs + ri);
+                        if (a.ckpt && (run.w & 1)) ck_store();
+                        const R dt = a.dt[run.x], sq = a.sqdt[run.x];
+#pragma unroll UNROLL
+                        for (int k = run.x; k < run.y; ++k) step_k(k, dt, sq);
+                        if (run.z >= 0) store(run.z, false);
+                    }
+                } else {
+                    int kc = 0;   // steps to the next checkpoint
+#pragma unroll UNROLL
+                    for (int k = 0; k < n_steps; ++k) {
+                        if (a.ckpt) {
+                            if (kc == 0) {
+                                ck_store();
+                                kc = a.ckpt_seg;
+                            }
+                            --kc;
+                        }
+                        step_k(k, a.dt[k], a.sqdt[k]);
+                        const int r = a.out_row[k + 1];
+                        if (r >= 0) store(r, false);
+                    }
                 }
             }
             if (MODEL == SDE_MODEL_HESTON && a.neg_count) {
