@@ -588,8 +588,8 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
             }
             runs.push_back(make_int4(k0, k, row, ci));
         }
-    } else if (sizeof(R) == 4 && n_steps > 0) {
-        // the other FP32 kernels: runs of steps with one dt (and sqrt|dt|),
+    } else if (n_steps > 0) {
+        // the other kernels: runs of steps with one dt (and sqrt|dt|),
         // ending where a row is stored, split where an adjoint checkpoint
         // falls (bit 0 of w: a checkpoint before the run's first step)
         const int cseg = (out->ckpt && out->ckpt_seg > 0) ? out->ckpt_seg : 0;
@@ -756,7 +756,7 @@ static int run_impl(const SdeSpec *s, const SdeGrid *gr, const SdeNoise *noise, 
         a.runs = (const int4 *)(T + o_runs);
         a.n_runs = (int32_t)runs.size();
         a.tshift = tshift.empty() ? nullptr : (const float *)(T + o_tsh);
-    } else if (!runs.empty()) {   // the other FP32 kernels' runs of one dt
+    } else if (!runs.empty()) {   // the other kernels' runs of one dt
         a.runs = (const int4 *)(T + o_runs);
         a.n_runs = (int32_t)runs.size();
     }

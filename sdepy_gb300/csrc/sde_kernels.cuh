@@ -90,7 +90,7 @@ struct FwdArgs {
     int32_t user_jsrc;
     // and the grid as runs of steps sharing one coefficient row:
     // (first step, end step, output row stored after the run or -1, coef row);
-    // for the other FP32 kernels, runs of steps with one dt, w = 1 where an
+    // for the other kernels, runs of steps with one dt, w = 1 where an
     // adjoint checkpoint falls before the run's first step, or NULL
     const int4 *runs;
     int32_t n_runs;
@@ -749,8 +749,12 @@ __device__ __forceinline__ int user_src(const SdeUserProgram &u, int i) {
 template <typename R, int MODEL, int MAXM, bool INJECT, bool JUMPS, bool ANTI = false>
 struct FwdOccupancy {
     static constexpr int CAP_M = (MODEL == SDE_MODEL_HESTON || MODEL == SDE_MODEL_CIR ? 4 : 8) / (ANTI ? 2 : 1);
+    // the other FP32 kernels of up to 4 states: at least two blocks per SM
+    // (128 registers; one more register halves the resident warps; wider
+    // groups would spill)
     static constexpr int MIN_BLOCKS =
-        (sizeof(R) == 4 && MAXM <= CAP_M && !INJECT && !JUMPS && MODEL != SDE_MODEL_USER && MODEL < 8) ? 3 : 1;
+        (sizeof(R) == 4 && MAXM <= CAP_M && !INJECT && !JUMPS && MODEL != SDE_MODEL_USER && MODEL < 8) ? 3
+        : (sizeof(R) == 4 && MAXM <= 4) ? 2 : 1;
 };
 
 // TDEP: time-dependent-coefficient instantiations of the FP32 device-noise
@@ -785,9 +789,9 @@ sde_fwd_kernel(const __grid_constant__ FwdArgs<R> a) {
     // draws overlap this step's arithmetic (5-12% on the FP32 kernels), but
     // one for the 8- and 16-wide time-dependent forms, which would spill
     constexpr int UNROLL = (TDEP && MAXM >= 8) ? 1 : 2;
-    // the FP32 kernels other than the run-table ones step through runs of
+    // the kernels other than the FP32 run-table ones step through runs of
     // one dt (FwdArgs::runs, when the host gives them)
-    constexpr bool RUNS = sizeof(R) == 4 && !TAB;
+    constexpr bool RUNS = !TAB;
     __shared__ R red[BLOCK / 32];
     __shared__ double part[MAXM][NPART];
     __shared__ R svs[NA][MAXM][BLOCK];   // this round's value of each output at the stats row
