@@ -15,6 +15,8 @@
 // reduced per block into sde_adj_kernel's partial layout.
 #pragma once
 
+#include <type_traits>
+
 #include "sde_adjoint.cuh"
 
 namespace sdegpu {
@@ -113,19 +115,36 @@ static __global__ void __launch_bounds__(BLOCK, 3) sde_adj_heston_kernel(const _
         // memory; the terminal adjoint then follows the last segment's
         // recomputation)
         constexpr bool fromck = CK;
-        if constexpr (!fromck) {
-            float x = x0a, y = x0b;
-            for (int k = 0, kc = 0, ci = 0; k < n_steps; ++k) {
-                if (kc == 0) {
-                    ck[ci][0] = x;
-                    ck[ci][1] = y;
-                    ++ci;
-                }
-                kc = kc + 1 == seg ? 0 : kc + 1;
+        // steps [k0, k1) from (x, y), dt and sqrt(dt) from DT(k), SQ(k); BUF:
+        // each step's variance and increments to the segment buffer
+        auto sweep = [&](int k0, int k1, float &x, float &y, auto BUF, auto DT, auto SQ) {
+            for (int k = k0; k < k1; ++k) {
                 float z0, z1, dWx, dWy;
                 pair.get(key, pre, k, step_offset, z0, z1);
-                incr(z0, z1, __ldg(a.sqdt + k), dWx, dWy);
-                step(__ldg(a.dt + k), dWx, dWy, x, y);
+                incr(z0, z1, SQ(k), dWx, dWy);
+                if constexpr (decltype(BUF)::value) {
+                    float *b = hbuf + (k - k0) * 3 * BLOCK + threadIdx.x;
+                    b[0] = y;
+                    b[BLOCK] = dWx;
+                    b[2 * BLOCK] = dWy;
+                }
+                step(DT(k), dWx, dWy, x, y);
+            }
+        };
+        // f(DT, SQ) for segment s: its one dt as constants (the usual case),
+        // else the per-step tables
+        auto with_dt = [&](int s, auto &&f) {
+            const float2 ds = __ldg(reinterpret_cast<const float2 *>(a.segdt) + s);
+            if (ds.x == ds.x) f([=](int) { return ds.x; }, [=](int) { return ds.y; });
+            else f([&](int k) { return __ldg(a.dt + k); }, [&](int k) { return __ldg(a.sqdt + k); });
+        };
+        if constexpr (!fromck) {
+            float x = x0a, y = x0b;
+            for (int s = 0; s < nseg; ++s) {
+                ck[s][0] = x;
+                ck[s][1] = y;
+                const int k0 = s * seg, k1 = min(k0 + seg, n_steps);
+                with_dt(s, [&](auto DT, auto SQ) { sweep(k0, k1, x, y, std::false_type(), DT, SQ); });
             }
             terminal(x, y);
         }
@@ -140,22 +159,14 @@ static __global__ void __launch_bounds__(BLOCK, 3) sde_adj_heston_kernel(const _
                 sx = ck[s][0];
                 sy = ck[s][1];
             }
-            for (int k = k0; k < k1; ++k) {
-                float z0, z1, dWx, dWy;
-                pair.get(key, pre, k, step_offset, z0, z1);
-                incr(z0, z1, __ldg(a.sqdt + k), dWx, dWy);
-                float *b = hbuf + (k - k0) * 3 * BLOCK + threadIdx.x;
-                b[0] = sy;
-                b[BLOCK] = dWx;
-                b[2 * BLOCK] = dWy;
-                step(__ldg(a.dt + k), dWx, dWy, sx, sy);
-            }
+            with_dt(s, [&](auto DT, auto SQ) { sweep(k0, k1, sx, sy, std::true_type(), DT, SQ); });
             if constexpr (fromck)
                 if (s == nseg - 1) terminal(sx, sy);
+            with_dt(s, [&](auto DT, auto) {
             for (int k = k1 - 1; k >= k0; --k) {
                 const float *b = hbuf + (k - k0) * 3 * BLOCK + threadIdx.x;
                 const float yv = b[0], dWx = b[BLOCK], dWy = b[2 * BLOCK];
-                const float dt = __ldg(a.dt + k);
+                const float dt = DT(k);
                 const float yp = fmaxf(yv, 0.f);
                 const float sr = A::sqrt_(yp);
                 const float ab = xbx, ybn = xby;
@@ -176,6 +187,7 @@ static __global__ void __launch_bounds__(BLOCK, 3) sde_adj_heston_kernel(const _
                 }
                 xby = ny;
             }
+            });
         }
         gth *= kk;
         kahan_add(acc[0], cmp[0], xbx);

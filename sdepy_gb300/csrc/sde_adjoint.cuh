@@ -80,6 +80,9 @@ struct AdjArgs {
     // time-dependent correlation: [steps][NCHOL] packed Cholesky factors of
     // each step's correlation matrix, or NULL (chol applies throughout)
     const R *chol_t;
+    // [nseg][2]: a level-1 segment's dt and sqrt(dt) when all its steps
+    // share them, else NaN (read by the FP32 Heston kernel)
+    const R *segdt;
 };
 
 // f(the Cholesky factor of step k): the per-step table's row (uniform

@@ -1345,7 +1345,8 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     const size_t o_pt = o_tk + al(sizeof(R) * (user ? n_steps : 1));   // slots 0..2 per step
     const size_t o_jp = o_pt + al(sizeof(R) * (td ? (size_t)n_steps * 3 * W : 1));   // a user dj law's a, b, pa
     const size_t o_ct = o_jp + al(sizeof(R) * (user && jumps ? (size_t)3 * W : 1));   // per-step Cholesky rows
-    const size_t o_end = o_ct + al(sizeof(R) * (corr_t ? (size_t)n_steps * NCHOL : 1));
+    const size_t o_sd = o_ct + al(sizeof(R) * (corr_t ? (size_t)n_steps * NCHOL : 1));   // per-segment dt
+    const size_t o_end = o_sd + al(sizeof(R) * 2 * (size_t)nseg);
     D->host_tables.resize(o_end);
     char *H = D->host_tables.data();
     R *h_dt = (R *)(H + o_dt), *h_sq = (R *)(H + o_sq), *h_x0 = (R *)(H + o_x0), *h_prm = (R *)(H + o_prm);
@@ -1360,6 +1361,17 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     }
     for (int w = 0; w < W; ++w) h_x0[w] = (R)s->x0[w];
     for (int i = 0; i < SDE_MAX_PARAMS * W; ++i) h_prm[i] = (R)s->params[i];
+    {   // each level-1 segment's dt and sqrt(dt), when its steps share them
+        R *h_sd = (R *)(H + o_sd);
+        for (int sg = 0; sg < nseg; ++sg) {
+            const int k0 = sg * seg, k1 = k0 + seg < n_steps ? k0 + seg : n_steps;
+            bool one = true;
+            for (int k = k0 + 1; k < k1 && one; ++k)
+                one = memcmp(&h_dt[k], &h_dt[k0], sizeof(R)) == 0 && memcmp(&h_sq[k], &h_sq[k0], sizeof(R)) == 0;
+            h_sd[2 * sg] = one ? h_dt[k0] : (R)NAN;
+            h_sd[2 * sg + 1] = one ? h_sq[k0] : (R)NAN;
+        }
+    }
     if (td) {   // slots 0..2 of each step of the grid's [steps][SDE_MAX_PARAMS][W] table
         R *h_pt = (R *)(H + o_pt);
         for (int k = 0; k < n_steps; ++k)
@@ -1425,6 +1437,7 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
     a.seg2 = seg2;
     a.ckpt = fromck ? (const R *)req->ckpt : nullptr;
     a.chol_t = corr_t ? (const R *)(T + o_ct) : nullptr;
+    a.segdt = (const R *)(T + o_sd);
     a.step_offset = gr->step_offset;
     a.out_mode = s->out_mode;
     a.jump_law = s->jump_law;
