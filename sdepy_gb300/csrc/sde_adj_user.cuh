@@ -85,8 +85,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) sde_adj_user_kernel(const __grid_
     };
     // one Euler step of the group, in the forward kernel's order:
     // x + (A_1 dZ_1 + ... + A_n dZ_n) per state
-    auto step = [&](int k, R (&st)[MG], const R (&dW)[MAXM], const R (&dN)[MAXM], const R (&dJ)[MAXM]) {
-        const R t = a.tk[k], dt = a.dt[k];
+    auto step = [&](int k, const R dt, R (&st)[MG], const R (&dW)[MAXM], const R (&dN)[MAXM], const R (&dJ)[MAXM]) {
+        const R t = a.tk[k];
 #pragma unroll
         for (int h = 0; h < NCP; ++h) {
             R xs[Q];
@@ -141,8 +141,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) sde_adj_user_kernel(const __grid_
                 if (cnt) dN[m] = (R)cnt;
         };
         // the increments of step k, drawn as the forward kernel draws them
-        auto noise = [&](int k, R (&dW)[MAXM], R (&dN)[MAXM], R (&dJ)[MAXM]) {
-            const R sq = a.sqdt[k];
+        auto noise = [&](int k, const R sq, R (&dW)[MAXM], R (&dN)[MAXM], R (&dJ)[MAXM]) {
             const uint32_t c1w = (uint32_t)k + a.step_offset;
 #pragma unroll
             for (int m = 0; m < MAXM; ++m) dN[m] = dJ[m] = R(0);
@@ -172,7 +171,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) sde_adj_user_kernel(const __grid_
         };
         // steps [k0, k1) from state st, with level-2 checkpoints every seg2
         // steps when ck2 is given
-        auto sweep = [&](int k0, int k1, R (&st)[MG], R (*ck2)[MG]) {
+        auto sweep = [&](int k0, int k1, R (&st)[MG], R (*ck2)[MG], auto DT, auto SQ) {
             for (int k = k0, kc = 0, ci = 0; k < k1; ++k) {
                 if (ck2 && kc == 0) {
 #pragma unroll
@@ -181,9 +180,16 @@ __global__ void __launch_bounds__(BLOCK, MINB) sde_adj_user_kernel(const __grid_
                 }
                 kc = kc + 1 == seg2 ? 0 : kc + 1;
                 R dW[MAXM], dN[MAXM], dJ[MAXM];
-                noise(k, dW, dN, dJ);
-                step(k, st, dW, dN, dJ);
+                noise(k, SQ(k), dW, dN, dJ);
+                step(k, DT(k), st, dW, dN, dJ);
             }
+        };
+        // f(DT, SQ) for level-1 segment s1: its one dt as constants (the
+        // usual case), else the per-step tables
+        auto with_dt = [&](int s1, auto &&f) {
+            const R d = a.segdt[2 * s1], q = a.segdt[2 * s1 + 1];
+            if (d == d) f([=](int) { return d; }, [=](int) { return q; });
+            else f([&](int k) { return a.dt[k]; }, [&](int k) { return a.sqdt[k]; });
         };
 
         // ---- terminal adjoint of the final states st ---------------------------
@@ -215,16 +221,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) sde_adj_user_kernel(const __grid_
         if (!fromck) {
 #pragma unroll
             for (int m = 0; m < MG; ++m) st[m] = x0[m];
-            for (int k = 0, kc = 0, ci = 0; k < n_steps; ++k) {
-                if (kc == 0) {
+            for (int s1 = 0; s1 < nseg; ++s1) {
 #pragma unroll
-                    for (int m = 0; m < MG; ++m) ck[ci][m] = st[m];
-                    ++ci;
-                }
-                kc = kc + 1 == seg ? 0 : kc + 1;
-                R dW[MAXM], dN[MAXM], dJ[MAXM];
-                noise(k, dW, dN, dJ);
-                step(k, st, dW, dN, dJ);
+                for (int m = 0; m < MG; ++m) ck[s1][m] = st[m];
+                const int l0 = s1 * seg, l1 = min(l0 + seg, n_steps);
+                with_dt(s1, [&](auto DT, auto SQ) { sweep(l0, l1, st, (R(*)[MG]) nullptr, DT, SQ); });
             }
             terminal();
         }
@@ -239,7 +240,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) sde_adj_user_kernel(const __grid_
             const int l0 = s1 * seg, l1 = min(l0 + seg, n_steps);
             if (two) {
                 ck_load(s1);
-                sweep(l0, l1, st, ck2);
+                with_dt(s1, [&](auto DT, auto SQ) { sweep(l0, l1, st, ck2, DT, SQ); });
                 if (fromck && s1 == nseg - 1) terminal();
             }
             const int nseg2 = two ? (l1 - l0 + seg2 - 1) / seg2 : 1;
@@ -252,9 +253,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) sde_adj_user_kernel(const __grid_
                 } else {
                     ck_load(s1);
                 }
+                with_dt(s1, [&](auto DT, auto SQ) {
                 for (int k = k0; k < k1; ++k) {
                     R dW[MAXM], dN[MAXM], dJ[MAXM];
-                    noise(k, dW, dN, dJ);
+                    noise(k, SQ(k), dW, dN, dJ);
                     R *b = ub + (size_t)(k - k0) * NV * MG * BLOCK + threadIdx.x;
 #pragma unroll
                     for (int m = 0; m < MG; ++m) {
@@ -263,7 +265,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) sde_adj_user_kernel(const __grid_
                         if constexpr (DN) b[(IN * MG + m) * BLOCK] = dN[m];
                         if constexpr (DJ) b[(IJ * MG + m) * BLOCK] = dJ[m];
                     }
-                    step(k, st, dW, dN, dJ);
+                    step(k, DT(k), st, dW, dN, dJ);
                 }
                 if (fromck && !two && s1 == nseg - 1) terminal();
                 for (int k = k1 - 1; k >= k0; --k) {
@@ -278,7 +280,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) sde_adj_user_kernel(const __grid_
                         if constexpr (DN) dN[m] = b[(IN * MG + m) * BLOCK];
                         if constexpr (DJ) dJ[m] = b[(IJ * MG + m) * BLOCK];
                     }
-                    const R t = a.tk[k], dt = a.dt[k];
+                    const R t = a.tk[k], dt = DT(k);
 #pragma unroll
                     for (int h = 0; h < NCP; ++h) {
                         R xs[Q], xbv[Q], dz[Q][SDE_USER_MAX_TERMS];
@@ -299,6 +301,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) sde_adj_user_kernel(const __grid_
                         for (int j = 0; j < NP; ++j) gp[h][j] += pb[j];
                     }
                 }
+                });
             }
         }
         // ---- this path's contributions -------------------------------------------
