@@ -960,12 +960,14 @@ class CpuPool:
                 .format(self.cores, self.per_worker, spread[0], spread[1]))
 
 
-def cpu_baseline(args, per_worker=CPU_SAMPLE_PATHS, samples=2):
-    """The port on all host cores (median of `samples` bounded samples) and
-    in one process, with the CPU model."""
+def cpu_baseline(args, per_worker=CPU_SAMPLE_PATHS, samples=3):
+    """The port on all host cores (median of `samples` bounded samples after
+    one warm-up sample, as the reference arm takes them) and in one process,
+    with the CPU model."""
     pool = CpuPool(per_worker)
     try:
         rates, spread = [], None
+        pool.sample()   # warm-up: the workers' first integration
         for _ in range(samples):
             r, spread = pool.sample()
             rates.append(r)
@@ -993,7 +995,7 @@ def run_reference(args):
     finally:
         pool.close()
     wall = time.perf_counter() - t0
-    v = float(np.mean(vals))
+    v = float(np.median(vals))
     res = {'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': UNIT,
            'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
            'ms_per_step': wall/(args.warmup + args.steps)*1e3, 'higher_is_better': True,
