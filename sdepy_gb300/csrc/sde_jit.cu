@@ -222,9 +222,10 @@ std::string op_reverse(uint32_t op) {
     case SDE_UOP_COS: return BA + " -= " + D + " * F::sin_(" + RA + ");";
     case SDE_UOP_TAN: return guarded(BA + " += " + D + " * (R(1) + " + RD + " * " + RD + ");");
     case SDE_UOP_TANH: return BA + " += " + D + " * (R(1) - " + RD + " * " + RD + ");";
-    case SDE_UOP_POW:
-        return guarded(BA + " += " + D + " * (" + RB + " * F::pow_(" + RA + ", " + RB + " - R(1))); if (" + RA +
-                       " > R(0)) " + BB + " += " + D + " * (" + RD + " * F::log_(" + RA + "));");
+    case SDE_UOP_POW:   // d(a^b)/da = b a^(b-1), a^b / a where a > 0 (no second power)
+        return guarded("const R pa_ = " + RA + " > R(0) ? " + RD + " / " + RA + " : F::pow_(" + RA + ", " + RB +
+                       " - R(1)); " + BA + " += " + D + " * (" + RB + " * pa_); if (" + RA + " > R(0)) " + BB +
+                       " += " + D + " * (" + RD + " * F::log_(" + RA + "));");
     case SDE_UOP_EXPM1: return guarded(BA + " += " + D + " * (" + RD + " + R(1));");
     case SDE_UOP_LOG1P: return guarded(BA + " += " + D + " / (R(1) + " + RA + ");");
     case SDE_UOP_ARCTAN: return BA + " += " + D + " / (R(1) + " + RA + " * " + RA + ");";
