@@ -1,6 +1,7 @@
 // Instantiations of sde_adj_kernel (float)
 #include "sde_adjoint.cuh"
 #include "sde_adj_heston.cuh"
+#include "sde_adj_ou.cuh"
 
 namespace sdegpu {
 
@@ -82,6 +83,12 @@ AdjLauncher<float> find_adj_f32(int model, int maxm, bool jumps, int *bps) {
         return &launch_adj<float, SDE_MODEL_HESTON, 8, false>;
     }
     return nullptr;
+}
+
+AdjLauncher<float> find_adj_ou_f32(int seg, int *bps) {
+    if (seg < 1 || seg > ADJ_OU_SEG) return nullptr;
+    if (bps) *bps = adj_ou_max_blocks_per_sm(seg);
+    return &launch_adj_ou;
 }
 
 AdjLauncher<float> find_adj_heston_f32(int seg, int *bps) {

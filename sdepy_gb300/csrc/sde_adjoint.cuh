@@ -34,6 +34,8 @@ constexpr size_t ADJ_TD_SMEM_SM = 220 * 1024;
 // steps per segment of the FP32 Heston adjoint that keep three 256-thread
 // blocks per SM (3 floats per step and thread in shared memory)
 constexpr int ADJ_HESTON_SEG = 24;
+// the same for the scalar FP32 OU adjoint (2 floats per step and thread)
+constexpr int ADJ_OU_SEG = 32;
 // shared-memory bytes per block for the segment buffer of the compiled
 // user-SDE adjoint (sde_adj_user.cuh)
 constexpr size_t UADJ_SMEM = 96 * 1024;
@@ -759,6 +761,10 @@ AdjLauncher<double> find_adj_f64(int model, int maxm, bool jumps, int *bps);
 // (sde_adj_heston.cuh, in adj_f32.cu): constant parameters, no jumps, one
 // checkpoint level of at most ADJ_HESTON_SEG steps per segment
 AdjLauncher<float> find_adj_heston_f32(int seg, int *bps);
+// the scalar FP32 OU adjoint with its segment in shared memory
+// (sde_adj_ou.cuh, in adj_f32.cu): constant parameters, the state output,
+// one checkpoint level of at most ADJ_OU_SEG steps per segment
+AdjLauncher<float> find_adj_ou_f32(int seg, int *bps);
 // time-dependent parameter slots, no jumps (adj_td.cu); the occupancy
 // returned is for the kernel without its per-step table
 AdjLauncher<float> find_adj_td_f32(int model, int maxm, int *bps);

@@ -1174,6 +1174,7 @@ template <> struct AdjFinder<float> {
     }
     static AdjLauncher<float> find_td(int model, int maxm, int *bps) { return find_adj_td_f32(model, maxm, bps); }
     static AdjLauncher<float> find_heston(int seg, int *bps) { return find_adj_heston_f32(seg, bps); }
+    static AdjLauncher<float> find_ou(int seg, int *bps) { return find_adj_ou_f32(seg, bps); }
 };
 template <> struct AdjFinder<double> {
     static AdjLauncher<double> find(int model, int maxm, bool jumps, int *bps) {
@@ -1182,6 +1183,7 @@ template <> struct AdjFinder<double> {
     }
     static AdjLauncher<double> find_td(int model, int maxm, int *bps) { return find_adj_td_f64(model, maxm, bps); }
     static AdjLauncher<double> find_heston(int, int *) { return nullptr; }
+    static AdjLauncher<double> find_ou(int, int *) { return nullptr; }
 };
 
 // what the adjoint of a spec runs: a user program's terms (ujs bit 0 dj,
@@ -1222,6 +1224,7 @@ static AdjKind adjoint_kind(const SdeSpec *s) {
 // level 1 is their segment, split in two levels when longer than cap.
 struct AdjPlan {
     bool heston_fast;   // the FP32 2-variable Heston kernel (sde_adj_heston.cuh)
+    bool ou_fast;       // the scalar FP32 OU kernel (sde_adj_ou.cuh)
     int cap, seg, seg2, nseg;
     size_t ubytes;      // the compiled user-SDE kernel's shared-memory buffer
 };
@@ -1237,7 +1240,11 @@ static int adjoint_plan(const SdeSpec *s, int n_steps, bool jumps, bool td, bool
     P->heston_fast = sizeof(R) == 4 && s->model == SDE_MODEL_HESTON && M == 2 && !jumps && !td && !corr_t &&
                      (fromck ? req_seg <= ADJ_HESTON_SEG
                              : (n_steps + ADJ_HESTON_SEG - 1) / ADJ_HESTON_SEG <= ADJ_MAXSEG);
-    int cap = P->heston_fast ? ADJ_HESTON_SEG : ADJ_MAXSEG;
+    // and the scalar FP32 OU one: at most ADJ_OU_SEG steps, the state output
+    P->ou_fast = sizeof(R) == 4 && s->model == SDE_MODEL_OU && M == 1 && !jumps && !td && !corr_t && !ujit &&
+                 s->out_mode == SDE_OUT_STATE &&
+                 (fromck ? req_seg <= ADJ_OU_SEG : (n_steps + ADJ_OU_SEG - 1) / ADJ_OU_SEG <= ADJ_MAXSEG);
+    int cap = P->heston_fast ? ADJ_HESTON_SEG : P->ou_fast ? ADJ_OU_SEG : ADJ_MAXSEG;
     size_t per_step = 0;
     if (ujit) {   // nv * M values per thread and step in UADJ_SMEM bytes
         per_step = sizeof(R) * (size_t)nv * M * BLOCK;
@@ -1483,6 +1490,8 @@ static int adjoint_impl(const SdeSpec *s, const SdeGrid *gr, const SdeAdjReq *re
         if (bps < 1) bps = 1;
     } else if (heston_fast) {
         L = AdjFinder<R>::find_heston(seg, &bps);
+    } else if (plan.ou_fast) {
+        L = AdjFinder<R>::find_ou(seg, &bps);
     } else {
         L = td ? AdjFinder<R>::find_td(s->model, maxm, &bps) : AdjFinder<R>::find(s->model, maxm, jumps, &bps);
         if (!L) return fail(SDE_ERR_UNSUPPORTED, "no adjoint kernel for model %d group size %d%s", s->model, M,

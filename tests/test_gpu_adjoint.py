@@ -401,6 +401,8 @@ CK_CASES = [
      (0., 1.), [.3]),
     ('ou_fp64_5000_steps', lambda: sg.ornstein_uhlenbeck_process(paths=2048, steps=5000, x0=.1, k=1.3, theta=.4,
                                                                   sigma=.3), (0., 2.), [.3]),
+    ('ou_fp32_scalar', lambda: sg.ornstein_uhlenbeck_process(paths=20011, steps=300, dtype=np.float32, x0=.1, k=1.3,
+                                                             theta=.4, sigma=.3), (0., 1.), [.3]),
     ('ou_fp32_run_table', lambda: sg.ornstein_uhlenbeck_process(paths=20011, steps=300, dtype=np.float32,
                                                                  vshape=2, corr=[[1., .5], [.5, 1.]], x0=.1, k=1.3,
                                                                  theta=.4, sigma=.3), (0., 1.), [.3]),
@@ -522,3 +524,19 @@ def test_adjoint_with_time_dependent_correlation(lib):
         h = 1e-5*max(abs(hk[name]), 1e-2)
         fd_ = (hes(**{name: hk[name] + h})[0] - hes(**{name: hk[name] - h})[0])/(2*h)
         assert abs(gr[name] - fd_) <= 1e-6*max(1., abs(fd_)), (name, gr[name], fd_)
+
+
+def test_fp32_scalar_ou_adjoint_matches_fp64(lib):
+    """The scalar FP32 OU adjoint (its own kernel: the segment in shared
+    memory, the segment's dt in registers) against the FP64 general kernel
+    on the same paths: value and the x0, k, theta, sigma gradients to FP32
+    accuracy, with a mean and two call payoffs; 300 steps and 1500 (the
+    longest run it takes in one level of 32-step segments)."""
+    for steps in (300, 1500):
+        kw = dict(x0=.1, k=1.3, theta=.4, sigma=.3)
+        g32, v32 = adjoint(lib, sg.ornstein_uhlenbeck_process, (0., 1.), steps, 40009, [.3, .5], [.5, .5], 1., 3, 1,
+                           dtype=np.float32, **kw)
+        g64, v64 = adjoint(lib, sg.ornstein_uhlenbeck_process, (0., 1.), steps, 40009, [.3, .5], [.5, .5], 1., 3, 1,
+                           **kw)
+        assert abs(v32 - v64) <= 1e-5*abs(v64)
+        np.testing.assert_allclose(g32[0, :4], g64[0, :4], rtol=2e-4, atol=1e-6)
