@@ -24,10 +24,11 @@ Differentiable parameters per preset:
                              of the first equation's process; x0 a scalar
                              or one value per equation), with dt, dw, dn
                              and dj terms.  A compiled program runs its
-                             generated reverse-mode step, an interpreted one
-                             (single equations, dt / dw) the traced program
-                             in tangent mode; systems and jump terms are
-                             compiled.
+                             generated reverse-mode step (jit=True, and by
+                             default when NVRTC is there), an interpreted one
+                             (jit=False; single equations, dt / dw) the
+                             traced program in tangent mode; systems and
+                             jump terms are compiled.
 Poisson intensities (constant or functions of time), the Kou probability pa
 and the jump-size laws of user SDEs select integer / discrete outcomes or
 are drawn through them and are not differentiated.
@@ -147,6 +148,11 @@ class _Expectation(torch.autograd.Function):
         g.n_pts = leg.tt.size
         g.step_offset = leg.step_offset
         spec = proc._make_spec(seed, stream)
+        if ctx.mp is not None and proc._jit is None and lib.sde_jit_available():
+            # a user SDE left to choose (jit=None): the gradient takes the
+            # compiled reverse-mode kernel, several times the interpreted
+            # tangent-mode one's speed (compiled once per process and program)
+            proc._uprog.jit = 1
         grad = np.zeros((proc._W, 8))
         val = C.c_double()
         name = type(proc).__name__
